@@ -1,0 +1,342 @@
+"""CPU oracle for the CAPOW periodic power-spectrum path (TEST INFRASTRUCTURE ONLY).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--impl
+reference`` legs of ``bench.py`` import this package, always as the checker or the
+timed CPU baseline, never as part of the product. The product (``capow_gb300``)
+never imports it.
+
+Two oracles live here:
+
+* ``liborc`` -- ``capow_oracle.c``, a plain-C restatement of the reference's periodic
+  path (src/read_data.c:32-179, 514-745; src/main.c:106-148, 211-225, 266-271,
+  302-468, 1019-1056). It builds on any host, including the GPU machine.
+* ``oracle/_ref/capow_ref`` -- the UNMODIFIED reference sources compiled against the
+  single-rank MPI / FFTW / GSL stand-ins in ``shims/`` (``Makefile.ref``). It can only
+  be built where the reference sources are mounted; it pins the restatement and
+  generates the committed golden fixtures.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+import subprocess
+import sys
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liborc.so")
+REF_BIN = os.path.join(HERE, "_ref", "capow_ref")
+REF_SRC = "/root/reference"
+
+_CFLAGS = ["-O2", "-std=gnu99", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", "-Wno-unused-function"]
+
+
+def build(force: bool = False) -> str:
+    """Compile liborc.so (and, where the reference sources exist, oracle/_ref/capow_ref)."""
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = [os.path.join(HERE, f) for f in ("capow_oracle.c", "orc_fft.c")]
+    hdrs = [os.path.join(HERE, f) for f in ("capow_oracle.h", "orc_fft.h")]
+    newest = max(os.path.getmtime(f) for f in srcs + hdrs)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
+        subprocess.check_call(["gcc", *_CFLAGS, "-o", LIB, *srcs, "-lm"])
+    if os.path.isdir(os.path.join(REF_SRC, "src")):
+        subprocess.check_call(
+            ["make", "-s", "-f", os.path.join("oracle", "Makefile.ref"), f"REF={REF_SRC}"],
+            cwd=os.path.dirname(HERE),
+        )
+    return LIB
+
+
+class OrcParams(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+        ("xmin", ctypes.c_double), ("xmax", ctypes.c_double),
+        ("ymin", ctypes.c_double), ("ymax", ctypes.c_double),
+        ("zmin", ctypes.c_double), ("zmax", ctypes.c_double),
+        ("interp_order", ctypes.c_int), ("do_interlacing", ctypes.c_int), ("los", ctypes.c_int),
+        ("omega_m", ctypes.c_double), ("redshift", ctypes.c_double),
+        ("nk", ctypes.c_int), ("nmu", ctypes.c_int), ("output_2d", ctypes.c_int),
+        ("output_log", ctypes.c_int), ("odd_multipoles", ctypes.c_int),
+        ("mink", ctypes.c_double), ("maxk", ctypes.c_double),
+    ]
+
+
+class OrcStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("nread", "nout", "ngrid", "npv", "nsq", "vr_ave", "vr2_ave", "vr3_ave", "vr4_ave")] + [
+        ("fatal", ctypes.c_int)]
+
+
+@dataclasses.dataclass
+class Params:
+    """The periodic-path subset of the reference's run_parameters.dat tags (src/read_params.c:65-227)."""
+    NX: int = 32
+    NY: int = 32
+    NZ: int = 32
+    XMIN: float = 0.0
+    XMAX: float = 1000.0
+    YMIN: float = 0.0
+    YMAX: float = 1000.0
+    ZMIN: float = 0.0
+    ZMAX: float = 1000.0
+    InterpOrder: int = 2
+    DoInterlacing: int = 1
+    NK: int = 20
+    NMU: int = 4
+    Mink: float = 0.0
+    Maxk: float = 0.2
+    Output2D: int = 0
+    OutputLog: int = 0
+    Omega_m: float = 0.3089
+    Redshift: float = 0.1
+    LOS: int = 0
+    Momentum: int = 0
+    Odd_Multipoles: int = 0
+
+    def to_c(self) -> OrcParams:
+        return OrcParams(self.NX, self.NY, self.NZ, self.XMIN, self.XMAX, self.YMIN, self.YMAX, self.ZMIN,
+                         self.ZMAX, self.InterpOrder, self.DoInterlacing, self.LOS, self.Omega_m, self.Redshift,
+                         self.NK, self.NMU, self.Output2D, self.OutputLog, self.Odd_Multipoles, self.Mink, self.Maxk)
+
+    def write_file(self, path: str) -> None:
+        """Write a complete run_parameters.dat (all 41 tags the reference parser requires)."""
+        tags = dict(
+            NumFilesInParallel=1, NX=self.NX, NY=self.NY, NZ=self.NZ,
+            XMIN=repr(float(self.XMIN)), XMAX=repr(float(self.XMAX)), YMIN=repr(float(self.YMIN)),
+            YMAX=repr(float(self.YMAX)), ZMIN=repr(float(self.ZMIN)), ZMAX=repr(float(self.ZMAX)),
+            DoInterlacing=self.DoInterlacing, InterpOrder=self.InterpOrder, NK=self.NK, NMU=self.NMU,
+            Output2D=self.Output2D, OutputLog=self.OutputLog, Mink=repr(float(self.Mink)),
+            Maxk=repr(float(self.Maxk)), Omega_m=repr(float(self.Omega_m)), Redshift=repr(float(self.Redshift)),
+            Periodic=1, LOS=self.LOS, Survey=0, Momentum=self.Momentum, X_Origin=0, Y_Origin=0, Z_Origin=0,
+            REDMININ=0, REDMAXIN=1, NOBJ_Max=1, Coord_Type=0, x_Column=1, y_Column=2, z_Column=3,
+            NBAR_Column=-1, SkyArea=1, FKP_Column=-1, FKP_Pk=0, FKP_Pk_mom=0, FKP_Pk_cross=0,
+            Odd_Multipoles=self.Odd_Multipoles,
+        )
+        with open(path, "w") as f:
+            f.write("% CAPOW run parameters\n")
+            for k, v in tags.items():
+                f.write(f"{k:<20s} {v}\n")
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = ctypes.CDLL(LIB)
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        P = ctypes.POINTER(OrcParams)
+        L.orc_grid_doubles.restype = ctypes.c_int64
+        L.orc_grid_doubles.argtypes = [P]
+        L.orc_slice_doubles.restype = ctypes.c_int64
+        L.orc_slice_doubles.argtypes = [P]
+        L.orc_paint.restype = ctypes.c_int
+        L.orc_paint.argtypes = [P, ctypes.c_int, ctypes.c_int64] + [dp] * 11 + [ctypes.POINTER(OrcStats)]
+        L.orc_shot_norm.argtypes = [P, ctypes.c_int, ctypes.POINTER(OrcStats), dp, dp, dp]
+        L.orc_subtract_mean.argtypes = [P, ctypes.c_int, ctypes.c_double, dp, dp]
+        L.orc_fft_grids.argtypes = [P, ctypes.c_int, dp, dp, dp, dp]
+        L.orc_compute_power.argtypes = [P, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp, dp, ip, dp, ip]
+        L.orc_normalise.restype = ctypes.c_int
+        L.orc_normalise.argtypes = [P, ctypes.c_double, ctypes.c_double, dp, dp, dp, dp, dp, ip, dp, ip]
+        L.orc_kbin.restype = ctypes.c_int
+        L.orc_kbin.argtypes = [P, ctypes.c_double]
+        L.orc_fft_r2c_3d_inplace.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
+        L.orc_fft_c2c_1d.argtypes = [ctypes.c_int, dp, dp]
+        L.orc_fft_c2r_3d_inplace.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
+        _lib = L
+    return _lib
+
+
+def _dp(a: Optional[np.ndarray]):
+    if a is None:
+        return ctypes.cast(None, ctypes.POINTER(ctypes.c_double))
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a: Optional[np.ndarray]):
+    if a is None:
+        return ctypes.cast(None, ctypes.POINTER(ctypes.c_int))
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def has_mom_grid(momentum: int) -> bool:
+    return momentum not in (0, 2, 5)
+
+
+def paint(p: Params, x, y, z, vx, vy, vz, w=None, momentum: Optional[int] = None):
+    """Paint particles as the reference's periodic reader does. Returns (grids dict, stats dict).
+
+    Grids are the padded [NX+InterpOrder][NY][2(NZ/2+1)] float64 arrays after the halo fold.
+    """
+    L = lib()
+    m = p.Momentum if momentum is None else momentum
+    pc = p.to_c()
+    nd = L.orc_grid_doubles(ctypes.byref(pc))
+    g = {"ddg": np.zeros(nd)}
+    if p.DoInterlacing:
+        g["ddg_interlace"] = np.zeros(nd)
+    if has_mom_grid(m):
+        g["ddg_mom"] = np.zeros(nd)
+        if p.DoInterlacing:
+            g["ddg_mom_interlace"] = np.zeros(nd)
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z, vx, vy, vz)]
+    wa = None if w is None else np.ascontiguousarray(w, dtype=np.float64)
+    st = OrcStats()
+    rc = L.orc_paint(ctypes.byref(pc), m, len(arrs[0]), *[_dp(a) for a in arrs], _dp(wa), _dp(g.get("ddg")),
+                     _dp(g.get("ddg_interlace")), _dp(g.get("ddg_mom")), _dp(g.get("ddg_mom_interlace")),
+                     ctypes.byref(st))
+    stats = {f: getattr(st, f) for f, _ in OrcStats._fields_}
+    if rc != 0:
+        raise ValueError("particle out of grid bounds with LOS == 0 (the reference aborts here)")
+    return g, stats
+
+
+def shot_norm(p: Params, stats: dict, momentum: Optional[int] = None):
+    m = p.Momentum if momentum is None else momentum
+    st = OrcStats(**{k: v for k, v in stats.items()})
+    a, s, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    lib().orc_shot_norm(ctypes.byref(p.to_c()), m, ctypes.byref(st), ctypes.byref(a), ctypes.byref(s),
+                        ctypes.byref(n))
+    return a.value, s.value, n.value
+
+
+def compute_power(p: Params, g: dict, momentum: Optional[int] = None):
+    """Raw bin sums of src/main.c:302-468 from FFT'd grids."""
+    m = p.Momentum if momentum is None else momentum
+    NK, NMU = p.NK, p.NMU
+    pk = [np.zeros(NK) for _ in range(5)]
+    nm = np.zeros(NK, np.int32)
+    pk2d = np.zeros(NK * NMU) if p.Output2D else None
+    nm2d = np.zeros(NK * NMU, np.int32) if p.Output2D else None
+    lib().orc_compute_power(ctypes.byref(p.to_c()), m, _dp(g.get("ddg")), _dp(g.get("ddg_interlace")),
+                            _dp(g.get("ddg_mom")), _dp(g.get("ddg_mom_interlace")), *[_dp(a) for a in pk],
+                            _ip(nm), _dp(pk2d), _ip(nm2d))
+    out = {"Pk0": pk[0], "Pk1": pk[1], "Pk2": pk[2], "Pk3": pk[3], "Pk4": pk[4], "Nmodes": nm}
+    if p.Output2D:
+        out["Pk_2D"] = pk2d
+        out["Nmodes_2D"] = nm2d
+    return out
+
+
+def normalise(p: Params, raw: dict, shot: float, norm: float):
+    """src/main.c:1019-1056 on copies of the raw sums; returns (dict, last_zeroed_bin)."""
+    o = {k: np.array(v, copy=True) for k, v in raw.items()}
+    pk2d = o.get("Pk_2D")
+    nm2d = o.get("Nmodes_2D")
+    last = lib().orc_normalise(ctypes.byref(p.to_c()), shot, norm, _dp(o["Pk0"]), _dp(o["Pk1"]), _dp(o["Pk2"]),
+                               _dp(o["Pk3"]), _dp(o["Pk4"]), _ip(o["Nmodes"]), _dp(pk2d), _ip(nm2d))
+    return o, last
+
+
+def run(p: Params, x, y, z, vx, vy, vz, w=None, momentum: Optional[int] = None, fft=None):
+    """The whole periodic branch of main() (src/main.c:75-288) for one Momentum value.
+
+    ``fft`` (optional) replaces the oracle FFT: a callable taking (grid, p) and transforming
+    the padded grid in place (e.g. a scipy-backed one for CPU baseline timing)."""
+    m = p.Momentum if momentum is None else momentum
+    g, st = paint(p, x, y, z, vx, vy, vz, w, momentum=m)
+    alpha, shot, norm = shot_norm(p, st, m)
+    L = lib()
+    pc = p.to_c()
+    L.orc_subtract_mean(ctypes.byref(pc), m, alpha, _dp(g["ddg"]), _dp(g.get("ddg_interlace")))
+    if fft is None:
+        L.orc_fft_grids(ctypes.byref(pc), m, _dp(g.get("ddg")), _dp(g.get("ddg_interlace")), _dp(g.get("ddg_mom")),
+                        _dp(g.get("ddg_mom_interlace")))
+    else:
+        for k in g:
+            fft(g[k], p)
+    raw = compute_power(p, g, m)
+    normed, last = normalise(p, raw, shot, norm)
+    return {"raw": raw, "norm": normed, "last": last, "stats": st, "alpha": alpha, "shot": shot, "normf": norm,
+            "grids": g}
+
+
+def fft_r2c_inplace(grid: np.ndarray, nx: int, ny: int, nz: int) -> None:
+    lib().orc_fft_r2c_3d_inplace(nx, ny, nz, _dp(grid))
+
+
+def real_view(p: Params, grid: np.ndarray) -> np.ndarray:
+    """[NX][NY][NZ] view of the FFT region of a padded grid (halo and padding excluded)."""
+    row = 2 * (p.NZ // 2 + 1)
+    return grid[: p.NX * p.NY * row].reshape(p.NX, p.NY, row)[:, :, : p.NZ]
+
+
+def complex_view(p: Params, grid: np.ndarray) -> np.ndarray:
+    nzc = p.NZ // 2 + 1
+    return grid[: p.NX * p.NY * 2 * nzc].view(np.complex128).reshape(p.NX, p.NY, nzc)
+
+
+# --------------------------------------------------------------------------- reference binary
+def ref_available() -> bool:
+    return os.path.exists(REF_BIN)
+
+
+def write_catalogue(path: str, x, y, z, vx, vy, vz) -> None:
+    """ASCII catalogue in the reference's `x y z vx vy vz` format with exact round-trip precision."""
+    data = np.stack([np.asarray(a, dtype=np.float64) for a in (x, y, z, vx, vy, vz)], axis=1)
+    np.savetxt(path, data, fmt="%.17g")
+
+
+def parse_dump(path: str) -> dict:
+    out = {}
+    with open(path) as f:
+        for line in f:
+            parts = line.split()
+            if not parts:
+                continue
+            k, vals = parts[0], parts[1:]
+            if k in ("NK", "NMU"):
+                out[k] = int(vals[0])
+            elif k in ("Nmodes", "Nmodes_2D"):
+                out[k] = np.array([int(v) for v in vals], dtype=np.int64)
+            else:
+                out[k] = np.array([float(v) for v in vals])
+    return out
+
+
+def run_ref_binary(p: Params, workdir: str, x, y, z, vx, vy, vz, grids: bool = False):
+    """Run the unmodified reference (oracle/_ref/capow_ref) on one catalogue.
+
+    Returns dict with stdout, output-file text, the raw-sum dump and (optionally) the painted grids."""
+    os.makedirs(workdir, exist_ok=True)
+    pf, df, of, dump = (os.path.join(workdir, n) for n in ("params.dat", "data.txt", "out.txt", "dump.txt"))
+    p.write_file(pf)
+    write_catalogue(df, x, y, z, vx, vy, vz)
+    for name in ("ddg", "ddg_interlace", "ddg_mom", "ddg_mom_interlace"):
+        stale = os.path.join(workdir, f"g.{name}.bin")
+        if os.path.exists(stale):
+            os.remove(stale)
+    for stale in (of, dump, of + "_2D"):
+        if os.path.exists(stale):
+            os.remove(stale)
+    env = dict(os.environ, CAPOW_REF_DUMP=dump)
+    if grids:
+        env["CAPOW_REF_GRIDS"] = os.path.join(workdir, "g")
+    r = subprocess.run([REF_BIN, pf, df, "none", of], capture_output=True, text=True, env=env)
+    res = {"returncode": r.returncode, "stdout": r.stdout}
+    if os.path.exists(of):
+        with open(of) as f:
+            res["output"] = f.read()
+    if os.path.exists(dump):
+        res["dump"] = parse_dump(dump)
+    if grids:
+        for name in ("ddg", "ddg_interlace", "ddg_mom", "ddg_mom_interlace"):
+            fp = os.path.join(workdir, f"g.{name}.bin")
+            if os.path.exists(fp):
+                res.setdefault("grids", {})[name] = np.fromfile(fp, dtype=np.float64)
+    return res
+
+
+if __name__ == "__main__":  # pragma: no cover
+    build(force="--force" in sys.argv)
+    print(LIB)
