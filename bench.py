@@ -1,0 +1,380 @@
+"""Benchmark: ms per P0/P2/P4(k) evaluation of the periodic power-spectrum path.
+
+Workload (the headline configuration): 256^3 = 16,777,216 Zel'dovich-displaced lattice particles
+(float32, seeded synthetic; no dataset), box L = 1000 Mpc/h, TSC on a 512^3 grid with interlacing,
+density-density, density-momentum and momentum-momentum spectra from one paint, LOS = z (RSD shift),
+NK = 161 linear bins to k = 1.61 h/Mpc.
+
+One step = one full evaluation: paint (4 grids) -> 4 in-place cuFFT R2C -> fused bin kernel ->
+device-to-host copy of the bins. ``value`` times steps with the particles already resident in HBM
+(CUDA events on the context stream, barrier + synchronize on both sides, max over ranks);
+``e2e`` times the same evaluation through the public C-ABI call with pinned HOST particle buffers,
+host-to-device copies inside the timed region. Grids (2.15 GB) and particles (268 MB) exceed L2,
+so no separate flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With N > 1 (torchrun) every rank runs an independent replica (the path does not shard without an
+exchange step); value = max-over-ranks time / (N * K).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms per P0/2/4(k) at 512³ grid, 16.7M particles: FP32-mixed vs FP64 GPU vs CPU"
+UNIT = "ms"
+WORKLOAD = ("256^3 Zel'dovich particles (16,777,216, f32), L=1000 Mpc/h, TSC 512^3, interlaced, "
+            "dd+dp+pp P0/P2/P4, LOS=z (RSD), NK=161 to k=1.61")
+
+PARAMS = dict(NX=512, NY=512, NZ=512, XMIN=0.0, XMAX=1000.0, YMIN=0.0, YMAX=1000.0, ZMIN=0.0, ZMAX=1000.0,
+              InterpOrder=3, DoInterlacing=1, NK=161, NMU=1, Output2D=0, OutputLog=0, Mink=0.0, Maxk=1.61,
+              Omega_m=0.3089, Redshift=0.1, LOS=3, Momentum=0, Odd_Multipoles=0)
+N_SIDE = 256
+SEED = 2
+
+
+def algorithmic_bytes(n_particles: int, ng: int, nc: int, grids: int, b_p: int, b_r: int, b_c: int) -> int:
+    """B = N_p b_p + G N_g b_r + G (N_g b_r + N_c b_c) + G N_c b_c (paint write, FFT read+write, bin read)."""
+    return n_particles * b_p + grids * ng * b_r + grids * (ng * b_r + nc * b_c) + grids * nc * b_c
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.rows.append([c.strip() for c in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    except Exception:
+        return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def make_particles(torch, device):
+    from capow_gb300 import synth
+
+    return synth.zeldovich(N_SIDE, L=1000.0, mesh=512, rms_cells=1.5, seed=SEED, torch_device=device)
+
+
+def dist_init():
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(world, v: float, device) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------------------------------ CPU
+def cpu_reference(steps: int, warmup: int, parts, log=print) -> dict:
+    """The reference algorithm on the host cores (CPU oracle restatement; 1 core, as the reference's
+    periodic path is single threaded without MPI). Each step is a bounded sample of the workload scaled
+    to one full evaluation: paint of a 1/16 particle subsample (x16), one 512^3 double r2c FFT (x8: the
+    three reference runs Momentum 0, 1, 2 need 2 + 4 + 2 transforms) and the full binning loop of one
+    grid pair (x3 runs)."""
+    import oracle as orc
+
+    try:
+        import scipy.fft as sfft
+
+        def fft(g, p):
+            row = 2 * (p.NZ // 2 + 1)
+            a = g[: p.NX * p.NY * row].reshape(p.NX, p.NY, row)
+            c = sfft.rfftn(a[:, :, : p.NZ], workers=1)
+            a[:] = c.view(np.float64).reshape(p.NX, p.NY, row)
+        fft_name = "scipy.fft (pocketfft, 1 thread; the reference links FFTW)"
+    except Exception:  # pragma: no cover
+        def fft(g, p):
+            orc.fft_r2c_inplace(g, p.NX, p.NY, p.NZ)
+        fft_name = "oracle C FFT"
+    orc.build()
+    p = orc.Params(**{k: v for k, v in PARAMS.items() if k in orc.Params.__dataclass_fields__})
+    x, y, z, vx, vy, vz = [np.asarray(a, dtype=np.float64) for a in parts]
+    n = len(x)
+    sub = slice(0, n // 16)
+    samples = []
+    for it in range(warmup + steps):
+        t0 = time.perf_counter()
+        g, st = orc.paint(p, x[sub], y[sub], z[sub], vx[sub], vy[sub], vz[sub], momentum=1)  # 4 grids
+        t1 = time.perf_counter()
+        fft(g["ddg"], p)
+        t2 = time.perf_counter()
+        g["ddg_interlace"][:] = g["ddg"]
+        g["ddg_mom"][:] = g["ddg"]
+        g["ddg_mom_interlace"][:] = g["ddg"]
+        t3 = time.perf_counter()
+        orc.compute_power(p, g, momentum=1)
+        t4 = time.perf_counter()
+        # Momentum 0 and 2 runs paint 2 grids each, Momentum 1 paints 4: 8 grid-paints = 2x the 4-grid paint
+        paint_ms = (t1 - t0) * 16 * 2 * 1e3
+        fft_ms = (t2 - t1) * 8 * 1e3
+        bin_ms = (t4 - t3) * 3 * 1e3
+        total = paint_ms + fft_ms + bin_ms
+        if it >= warmup:
+            samples.append((total, paint_ms, fft_ms, bin_ms))
+        log(f"cpu step {it}: est {total:.0f} ms (paint {paint_ms:.0f}, fft {fft_ms:.0f}, bin {bin_ms:.0f})")
+    tot = statistics.median(s[0] for s in samples)
+    return {"value": tot, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": ("per step: paint of 1/16 of the particles (x16, x2 for the three Momentum runs' 8 grids), "
+                       f"one 512^3 float64 r2c FFT x8 [{fft_name}], one full binning pass x3"),
+            "stages_ms": {"paint": statistics.median(s[1] for s in samples),
+                          "fft": statistics.median(s[2] for s in samples),
+                          "bin": statistics.median(s[3] for s in samples)}}
+
+
+# ------------------------------------------------------------------------------------------ GPU
+def gpu_bench(args, world, rank, local):
+    import torch
+
+    import capow_gb300 as cg
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    parts = make_particles(torch, dev)
+    x, y, z, vx, vy, vz = parts
+    n = len(x)
+    params = cg.Params(**PARAMS)
+    d = [torch.from_numpy(a).to(dev) for a in (x, y, z, vz)]
+    host = [torch.from_numpy(a).pin_memory() for a in (x, y, z, vz)]
+    ps = cg.PowerSpectrum(params, precision="fp32", spectra=["dd", "dp", "pp"], device=local)
+
+    def step_device():
+        ps.paint(*d)
+        return ps.power()
+
+    def step_host():
+        ps.paint(*[h.numpy() for h in host])
+        return ps.power()
+
+    for _ in range(args.warmup):
+        res = step_device()
+    stage = ps.stage_ms()
+    # ---- value: device-resident inputs
+    barrier(world)
+    torch.cuda.synchronize()
+    launches0 = ps.kernel_launches()
+    with ClockSampler(local) as clk:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        ev0.record()
+        stage_acc = np.zeros(3)
+        for _ in range(args.steps):
+            res = step_device()
+            stage_acc += np.array(ps.stage_ms())
+        ev1.record()
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - t0) * 1e3
+    launches = ps.kernel_launches() - launches0
+    dev_ms = ev0.elapsed_time(ev1)
+    total_ms = max(dev_ms, 0.0)
+    total_ms = max_over_ranks(world, total_ms, dev)
+    barrier(world)
+    ms_per = total_ms / (args.steps * world)
+    stage_ms = stage_acc / args.steps
+    # ---- e2e: host buffers through the public API
+    for _ in range(2):
+        step_host()
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res_h = step_host()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1e3
+    e2e_ms = max_over_ranks(world, e2e_ms, dev) / (args.steps * world)
+    h2d = sum(int(h.numel() * h.element_size()) for h in host)
+    d2h = 3 * 5 * PARAMS["NK"] * 8
+    # ---- FP64 GPU path on the same workload (fewer steps: it is the slow baseline)
+    ps.close()
+    fp64_ms = None
+    acc = None
+    try:
+        p64 = cg.PowerSpectrum(params, precision="fp64", spectra=["dd", "dp", "pp"], device=local)
+        p64.paint(*d)
+        r64 = p64.power()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        k64 = max(1, min(3, args.steps))
+        e0.record()
+        for _ in range(k64):
+            p64.paint(*d)
+            r64 = p64.power()
+        e1.record()
+        torch.cuda.synchronize()
+        fp64_ms = e0.elapsed_time(e1) / k64
+        p64.close()
+        # accuracy of the FP32-mixed bins against the FP64 GPU path (itself checked against the oracle)
+        acc = {}
+        m = np.asarray(r64[0]["Nmodes"]) > 0
+        for q, name in enumerate(("dd", "dp", "pp")):
+            n0 = np.abs(r64[q]["Pk0"]) if name != "dp" else np.sqrt(np.abs(r64[0]["Pk0"] * r64[2]["Pk0"]))
+            acc[name] = {f"l{l}": float(np.max((2 * l + 1) * np.abs(res[q][f"Pk{l}"][m] - r64[q][f"Pk{l}"][m])
+                                               / n0[m])) for l in (0, 2, 4)}
+            acc[name]["nmodes_equal"] = bool(np.array_equal(res[q]["Nmodes"], r64[q]["Nmodes"]))
+    except cg.CapowError as e:  # pragma: no cover
+        fp64_ms = None
+        acc = {"error": str(e)}
+    ng = 512 ** 3
+    nc = 512 * 512 * 257
+    B32 = algorithmic_bytes(n, ng, nc, 4, 16, 4, 8)
+    B64 = algorithmic_bytes(n, ng, nc, 4, 32, 8, 16)
+    pk = peaks()
+    return {
+        "ms_per": ms_per, "wall_ms": wall, "stage_ms": stage_ms, "launches": launches, "e2e_ms": e2e_ms, "h2d": h2d,
+        "d2h": d2h, "fp64_ms": fp64_ms, "acc": acc, "B32": B32, "B64": B64, "peaks": pk, "clocks": clk.summary(),
+        "n": n, "parts": parts,
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_init()
+    log = (lambda *a: print(*a, file=sys.stderr, flush=True))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from capow_gb300 import synth
+
+        parts = synth.zeldovich(N_SIDE, L=1000.0, mesh=512, rms_cells=1.5, seed=SEED)
+        cpu = cpu_reference(args.steps, 1, parts, log)
+        line = {"metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": 1, "ms_per_step": cpu["value"], "higher_is_better": False, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Zel'dovich lattice)",
+                "config": {"workload": WORKLOAD, "grid": 512, "particles": N_SIDE ** 3}, "impl": "reference",
+                "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "stages_ms": cpu["stages_ms"]}
+        print(json.dumps(line), flush=True)
+        return
+
+    r = gpu_bench(args, world, rank, local)
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_reference(args.cpu_steps, 0, r["parts"], log)
+    pk = r["peaks"]
+    eval_gbs = r["B32"] / (r["ms_per"] * world * 1e-3) / 1e9
+    paint_ms, fft_ms, bin_ms = [float(v) for v in r["stage_ms"]]
+    line = {
+        "metric": METRIC, "value": round(r["ms_per"], 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(r["ms_per"] * world, 4), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Zel'dovich lattice, float32 positions/velocities)",
+        "config": {"workload": WORKLOAD, "grid": 512, "particles": r["n"], "interp": "TSC", "interlacing": True,
+                   "spectra": ["dd", "dp", "pp"], "precision": "fp32-mixed (FP64 bin sums, exact k-bins)",
+                   "l2": "inputs larger than L2 (grids 2.15 GB, particles 268 MB)", "parallelism": "replicas"},
+        "e2e": {"value": round(r["e2e_ms"], 4), "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
+                "d2h_bytes_per_step": r["d2h"]},
+        "gpu_launches": int(r["launches"]),
+        "stages_ms": {"paint": round(paint_ms, 4), "fft": round(fft_ms, 4), "bin": round(bin_ms, 4)},
+        "roofline": None,
+        "roofline_eval": {"bound": "hbm", "achieved": round(eval_gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                          "frac": round(eval_gbs / pk["hbm_gbs"], 4), "algorithmic_bytes": r["B32"],
+                          "peak_source": pk["source"]},
+        "fp64_gpu": {"ms": round(r["fp64_ms"], 3) if r["fp64_ms"] else None, "algorithmic_bytes": r["B64"]},
+        "accuracy_fp32_vs_fp64_gpu": r["acc"],
+        "clocks": r["clocks"],
+        "cpu_baseline": ({k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")} if cpu else None),
+    }
+    # dominant own kernel: paint stage (tile kernel dominates it) or bin kernel
+    pb = {"paint": (r["n"] * 16 + 4 * 512 ** 3 * 4, paint_ms), "bin": (4 * 512 * 512 * 257 * 8, bin_ms)}
+    dom = max(pb, key=lambda k: pb[k][1])
+    ach = pb[dom][0] / (pb[dom][1] * 1e-3) / 1e9
+    line["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": pk["hbm_gbs"],
+                        "unit": "GB/s", "frac": round(ach / pk["hbm_gbs"], 4), "traffic": None,
+                        "peak_source": pk["source"]}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,361 @@
+"""capow_gb300: GB300 (sm_103a) implementation of CAPOW's periodic-box power-spectrum path.
+
+The product is the C-ABI library ``libcapow_gpu.so`` (declared in ``include/capow.h``) and
+the ``capow`` command-line driver. This module is a thin ctypes mirror of that C ABI for
+Python callers and tests. Inputs may be NumPy arrays (host: copied to the GPU inside the
+call) or any object exposing ``data_ptr()`` on a CUDA device (e.g. torch tensors: passed
+through as device pointers, resident in HBM).
+
+There is no CPU fallback: if the compiled library is missing, importing the bindings raises.
+Build it with ``python -m capow_gb300.build`` (or ``__graft_entry__.build()``).
+
+Reference mapping (paths in the CAPOW source tree):
+  Params / read_params     src/read_params.c:30-428   read_parameterfile, check_inputs
+  PowerSpectrum()          src/main.c:1123-1251       create_grids
+  PowerSpectrum.paint      src/read_data.c:32-179, 514-745
+  PowerSpectrum.power      src/main.c:106-148, 211-225, 266-271, 302-468
+  normalise                src/main.c:1019-1056       output_power arithmetic
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+from typing import List, Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libcapow_gpu.so")
+DRIVER_PATH = os.path.join(HERE, "bin", "capow")
+
+# status codes (capow.h)
+OK, EINVAL, ENOMEM, ECUDA, EBOUNDS, ETIMEOUT, ESTATE, ECUFFT, ENOTSUP = range(9)
+FP64, FP32_MIXED, FP32_DETERMINISTIC = 0, 1, 2
+SPEC_REFERENCE, SPEC_DD, SPEC_DP, SPEC_PP = 0, 1, 2, 4
+F32, F64 = 0, 1
+PRECISIONS = {"fp64": FP64, "fp32": FP32_MIXED, "det": FP32_DETERMINISTIC}
+
+
+class CapowError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(msg)
+        self.status = status
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [
+        ("NX", ctypes.c_int), ("NY", ctypes.c_int), ("NZ", ctypes.c_int),
+        ("XMIN", ctypes.c_double), ("XMAX", ctypes.c_double), ("YMIN", ctypes.c_double),
+        ("YMAX", ctypes.c_double), ("ZMIN", ctypes.c_double), ("ZMAX", ctypes.c_double),
+        ("InterpOrder", ctypes.c_int), ("DoInterlacing", ctypes.c_int),
+        ("NK", ctypes.c_int), ("NMU", ctypes.c_int), ("Output2D", ctypes.c_int), ("OutputLog", ctypes.c_int),
+        ("Mink", ctypes.c_double), ("Maxk", ctypes.c_double),
+        ("Omega_m", ctypes.c_double), ("Redshift", ctypes.c_double),
+        ("LOS", ctypes.c_int), ("Momentum", ctypes.c_int), ("Odd_Multipoles", ctypes.c_int),
+    ]
+
+
+class _Options(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("spectra", ctypes.c_int), ("device", ctypes.c_int),
+                ("stream", ctypes.c_void_p), ("reserved", ctypes.c_int * 8)]
+
+
+class _Particles(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_size_t), ("dtype", ctypes.c_int), ("on_device", ctypes.c_int),
+                ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("z", ctypes.c_void_p),
+                ("vlos", ctypes.c_void_p), ("w", ctypes.c_void_p)]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [("nread", ctypes.c_double), ("nout", ctypes.c_double), ("ngrid", ctypes.c_double),
+                ("nsq", ctypes.c_double), ("vr", ctypes.c_double * 4), ("first_out_of_box", ctypes.c_int64)]
+
+
+class _Spectrum(ctypes.Structure):
+    _fields_ = [("pk", ctypes.POINTER(ctypes.c_double) * 5), ("nmodes", ctypes.POINTER(ctypes.c_int64)),
+                ("pk2d", ctypes.POINTER(ctypes.c_double)), ("nmodes2d", ctypes.POINTER(ctypes.c_int64)),
+                ("shot", ctypes.c_double), ("norm", ctypes.c_double), ("alpha", ctypes.c_double),
+                ("last_bin", ctypes.c_int), ("kind", ctypes.c_int)]
+
+
+# every entry point include/capow.h declares
+EXPORTS = [
+    "capow_create", "capow_paint", "capow_get_stats", "capow_power", "capow_normalise", "capow_num_spectra",
+    "capow_copy_grid", "capow_stage_ms", "capow_kernel_launches", "capow_destroy", "capow_read_params",
+    "capow_read_catalogue", "capow_free", "capow_write_output", "capow_bin_centre", "capow_strerror",
+    "capow_last_error",
+]
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load libcapow_gpu.so. Raises if it has not been built: there is no fallback."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing; build it with `python -m capow_gb300.build` "
+                          "(the CUDA library is required: there is no CPU path)")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, ip = ctypes.c_void_p, ctypes.c_int
+    P, O = ctypes.POINTER(_Params), ctypes.POINTER(_Options)
+    L.capow_create.argtypes = [P, O, ctypes.POINTER(vp)]
+    L.capow_paint.argtypes = [vp, ctypes.POINTER(_Particles)]
+    L.capow_get_stats.argtypes = [vp, ctypes.POINTER(_Stats)]
+    L.capow_power.argtypes = [vp, ctypes.POINTER(_Spectrum), ip]
+    L.capow_normalise.argtypes = [P, ctypes.POINTER(_Spectrum)]
+    L.capow_num_spectra.argtypes = [vp]
+    L.capow_copy_grid.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_double)]
+    L.capow_stage_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                 ctypes.POINTER(ctypes.c_float)]
+    L.capow_kernel_launches.argtypes = [vp]
+    L.capow_kernel_launches.restype = ctypes.c_int64
+    L.capow_destroy.argtypes = [vp]
+    L.capow_destroy.restype = None
+    L.capow_read_params.argtypes = [ctypes.c_char_p, P, ctypes.c_char_p, ctypes.c_size_t]
+    dpp = ctypes.POINTER(ctypes.POINTER(ctypes.c_double))
+    L.capow_read_catalogue.argtypes = [ctypes.c_char_p, ip, ctypes.POINTER(ctypes.c_size_t), dpp, dpp, dpp, dpp,
+                                       ctypes.c_char_p, ctypes.c_size_t]
+    L.capow_free.argtypes = [vp]
+    L.capow_free.restype = None
+    L.capow_write_output.argtypes = [ctypes.c_char_p, P, ctypes.POINTER(_Spectrum)]
+    L.capow_bin_centre.argtypes = [P, ip]
+    L.capow_bin_centre.restype = ctypes.c_double
+    L.capow_strerror.argtypes = [ip]
+    L.capow_strerror.restype = ctypes.c_char_p
+    L.capow_last_error.argtypes = [vp]
+    L.capow_last_error.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+@dataclasses.dataclass
+class Params:
+    """capow_params: the run_parameters.dat tags of the periodic path (src/read_params.c:65-227)."""
+    NX: int = 32
+    NY: int = 32
+    NZ: int = 32
+    XMIN: float = 0.0
+    XMAX: float = 1000.0
+    YMIN: float = 0.0
+    YMAX: float = 1000.0
+    ZMIN: float = 0.0
+    ZMAX: float = 1000.0
+    InterpOrder: int = 2
+    DoInterlacing: int = 1
+    NK: int = 20
+    NMU: int = 4
+    Output2D: int = 0
+    OutputLog: int = 0
+    Mink: float = 0.0
+    Maxk: float = 0.2
+    Omega_m: float = 0.3089
+    Redshift: float = 0.1
+    LOS: int = 0
+    Momentum: int = 0
+    Odd_Multipoles: int = 0
+
+    def to_c(self) -> _Params:
+        return _Params(**{f.name: getattr(self, f.name) for f in dataclasses.fields(self)})
+
+    @classmethod
+    def from_c(cls, c: _Params) -> "Params":
+        return cls(**{f.name: getattr(c, f.name) for f in dataclasses.fields(cls)})
+
+
+def read_params(path: str) -> Params:
+    """capow_read_params: the reference's parameter-file reader and checks."""
+    c = _Params()
+    msg = ctypes.create_string_buffer(8192)
+    rc = lib().capow_read_params(path.encode(), ctypes.byref(c), msg, len(msg))
+    if rc != OK:
+        raise CapowError(rc, msg.value.decode())
+    return Params.from_c(c)
+
+
+def read_catalogue(path: str, los: int):
+    """capow_read_catalogue: returns (x, y, z, vlos) float64 arrays."""
+    L = lib()
+    n = ctypes.c_size_t()
+    ptrs = [ctypes.POINTER(ctypes.c_double)() for _ in range(4)]
+    msg = ctypes.create_string_buffer(4096)
+    rc = L.capow_read_catalogue(path.encode(), los, ctypes.byref(n), *[ctypes.byref(p) for p in ptrs], msg, len(msg))
+    if rc != OK:
+        raise CapowError(rc, msg.value.decode())
+    out = []
+    for p in ptrs:
+        a = np.ctypeslib.as_array(p, shape=(n.value,)).copy() if n.value else np.zeros(0)
+        L.capow_free(ctypes.cast(p, ctypes.c_void_p))
+        out.append(a)
+    return tuple(out)
+
+
+def _ptr_of(a):
+    """(address, dtype code, on_device, keepalive) for a numpy array or a CUDA tensor-like."""
+    if a is None:
+        return None, None, None, None
+    if hasattr(a, "data_ptr") and hasattr(a, "is_cuda"):
+        if not a.is_cuda:
+            a = a.numpy()
+        else:
+            if not a.is_contiguous():
+                raise ValueError("device arrays must be contiguous")
+            name = str(a.dtype)
+            code = F64 if "float64" in name else (F32 if "float32" in name else None)
+            if code is None:
+                raise ValueError("device arrays must be float32 or float64")
+            return a.data_ptr(), code, 1, a
+    arr = np.ascontiguousarray(a)
+    if arr.dtype not in (np.float32, np.float64):
+        arr = arr.astype(np.float64)
+    return arr.ctypes.data, (F64 if arr.dtype == np.float64 else F32), 0, arr
+
+
+class PowerSpectrum:
+    """One capow context: paint a catalogue, then P_l(k) for the requested spectra.
+
+    precision: "fp32" (FP32-mixed, default), "fp64" (plain double path), "det" (int64 fixed-point grids).
+    spectra:   None -> one spectrum chosen by params.Momentum (one reference run); or any of
+               ("dd", "dp", "pp") computed from one paint and one set of FFTs.
+    """
+
+    def __init__(self, params: Params, precision: str = "fp32", spectra=None, device: int = 0, stream=None):
+        self.params = params
+        self._pc = params.to_c()
+        mask = 0
+        for s in (spectra or []):
+            mask |= {"dd": SPEC_DD, "dp": SPEC_DP, "pp": SPEC_PP}[s]
+        self.spectra_mask = mask
+        opt = _Options(PRECISIONS[precision], mask, device, ctypes.c_void_p(stream or 0))
+        self._ctx = ctypes.c_void_p()
+        rc = lib().capow_create(ctypes.byref(self._pc), ctypes.byref(opt), ctypes.byref(self._ctx))
+        if rc != OK:
+            err = self._err()
+            self.close()
+            raise CapowError(rc, f"capow_create: {lib().capow_strerror(rc).decode()}: {err}")
+        self.nspec = lib().capow_num_spectra(self._ctx)
+        self._keep = []
+
+    def _err(self) -> str:
+        if not self._ctx:
+            return ""
+        return lib().capow_last_error(self._ctx).decode()
+
+    def _check(self, rc: int, what: str):
+        if rc != OK:
+            raise CapowError(rc, f"{what}: {lib().capow_strerror(rc).decode()}: {self._err()}")
+
+    def paint(self, x, y, z, vlos=None, w=None) -> None:
+        parts = []
+        for a in (x, y, z, vlos, w):
+            parts.append(_ptr_of(a))
+        codes = {p[1] for p in parts if p[0] is not None}
+        devs = {p[2] for p in parts if p[0] is not None}
+        if len(codes) != 1 or len(devs) != 1:
+            raise ValueError("all particle arrays must share one dtype and one location")
+        n = len(parts[0][3])
+        for p in parts:
+            if p[0] is not None and len(p[3]) != n:
+                raise ValueError("particle arrays differ in length")
+        self._keep = [p[3] for p in parts]
+        pc = _Particles(n, codes.pop(), devs.pop(), *[p[0] for p in parts])
+        self._check(lib().capow_paint(self._ctx, ctypes.byref(pc)), "capow_paint")
+
+    def stats(self) -> dict:
+        s = _Stats()
+        self._check(lib().capow_get_stats(self._ctx, ctypes.byref(s)), "capow_get_stats")
+        return {"nread": s.nread, "nout": s.nout, "ngrid": s.ngrid, "nsq": s.nsq, "vr": list(s.vr),
+                "first_out_of_box": s.first_out_of_box}
+
+    def grid(self, which: int) -> np.ndarray:
+        """Painted grid (0 A, 1 A interlaced, 2 B, 3 B interlaced) in the padded reference layout."""
+        p = self.params
+        n = p.NX * p.NY * 2 * (p.NZ // 2 + 1)
+        out = np.zeros(n)
+        self._check(lib().capow_copy_grid(self._ctx, which, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+                    "capow_copy_grid")
+        return out
+
+    def power(self) -> List[dict]:
+        """Raw bin sums + shot/norm/alpha for each spectrum (capow_power)."""
+        p = self.params
+        n2d = p.NK * p.NMU if p.Output2D else 0
+        specs = (_Spectrum * self.nspec)()
+        bufs = []
+        for q in range(self.nspec):
+            pk = [np.zeros(p.NK) for _ in range(5)]
+            nm = np.zeros(p.NK, np.int64)
+            p2 = np.zeros(max(n2d, 1))
+            n2 = np.zeros(max(n2d, 1), np.int64)
+            bufs.append((pk, nm, p2, n2))
+            for l in range(5):
+                specs[q].pk[l] = pk[l].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+            specs[q].nmodes = nm.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+            if n2d:
+                specs[q].pk2d = p2.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+                specs[q].nmodes2d = n2.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        self._check(lib().capow_power(self._ctx, specs, self.nspec), "capow_power")
+        out = []
+        for q in range(self.nspec):
+            pk, nm, p2, n2 = bufs[q]
+            d = {"Pk0": pk[0], "Pk1": pk[1], "Pk2": pk[2], "Pk3": pk[3], "Pk4": pk[4], "Nmodes": nm,
+                 "shot": specs[q].shot, "norm": specs[q].norm, "alpha": specs[q].alpha,
+                 "kind": {0: "ref", SPEC_DD: "dd", SPEC_DP: "dp", SPEC_PP: "pp"}[specs[q].kind]}
+            if n2d:
+                d["Pk_2D"] = p2[:n2d]
+                d["Nmodes_2D"] = n2[:n2d]
+            out.append(d)
+        return out
+
+    def normalise(self, raw: dict) -> dict:
+        """capow_normalise (output_power arithmetic) on a copy of one raw spectrum."""
+        p = self.params
+        d = {k: (np.array(v, copy=True) if isinstance(v, np.ndarray) else v) for k, v in raw.items()}
+        s = _Spectrum()
+        for l in range(5):
+            s.pk[l] = d[f"Pk{l}"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        s.nmodes = d["Nmodes"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        if p.Output2D:
+            s.pk2d = d["Pk_2D"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+            s.nmodes2d = d["Nmodes_2D"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        s.shot, s.norm = d["shot"], d["norm"]
+        rc = lib().capow_normalise(ctypes.byref(self._pc), ctypes.byref(s))
+        if rc != OK:
+            raise CapowError(rc, "capow_normalise")
+        d["last_bin"] = s.last_bin
+        return d
+
+    def stage_ms(self):
+        a, b, c = ctypes.c_float(), ctypes.c_float(), ctypes.c_float()
+        self._check(lib().capow_stage_ms(self._ctx, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+                    "capow_stage_ms")
+        return a.value, b.value, c.value
+
+    def kernel_launches(self) -> int:
+        return int(lib().capow_kernel_launches(self._ctx))
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            lib().capow_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def run(params: Params, x, y, z, vlos=None, w=None, precision: str = "fp32", spectra=None, device: int = 0):
+    """Paint + power in one call; returns the list of raw spectra dicts."""
+    with PowerSpectrum(params, precision=precision, spectra=spectra, device=device) as ps:
+        ps.paint(x, y, z, vlos, w)
+        return ps.power()

@@ -1,0 +1,57 @@
+// Binning-stage interfaces (bin.cu) and the host-side threshold construction.
+#pragma once
+#include <vector>
+
+#include "common.cuh"
+
+#define CAPOW_MAX_SPEC 3
+
+// One spectrum: power = Re or Im of conj(X) * Y for X, Y in {field A = 0, field B = 1}
+// (src/main.c:432-441: |F|^2, Im(F* P) as dkr*dki_mom - dki*dkr_mom, Re(F* P)).
+struct SpecDef {
+  int x, y;   // field index
+  int imag;   // 1: imaginary part
+};
+
+// Device tables for one grid geometry. All "f" quantities follow src/main.c:335-352, 382-389.
+struct BinTables {
+  // exact squared frequencies, fl(f*f), for the reference's s = (fx*fx + fy*fy) + fz*fz
+  double *fx2d, *fy2d, *fz2d;
+  float *fx2f, *fy2f, *fz2f;
+  double *fxd, *fyd, *fzd;  // signed frequencies (mu numerator, 2-D bins)
+  float *fxf, *fyf, *fzf;
+  // deconvolution factors sinc^(-2p) per axis and interlacing phases e^{i pi f d} per axis
+  double *cxd, *cyd, *czd;
+  float *cxf, *cyf, *czf;
+  double2 *exd, *eyd, *ezd;
+  float2 *exf, *eyf, *ezf;
+  // merged k-bin edges E[0..NK] in s (bin b iff E[b] <= s < E[b+1]) and FP32 safe edges
+  double *E;
+  float *Elo, *Ehi;  // E[b]*(1+eps), E[b]*(1-eps) rounded outward/inward: safe FP32 tests
+};
+
+struct BinParams {
+  int nx, ny, nz, nzc, xhalf;
+  int nk, nmu, los, interlace, odd, out2d;
+  int nspec, nfields;
+  SpecDef spec[CAPOW_MAX_SPEC];
+  int mean_sub_a;           // field A had the mean subtracted (DC correction)
+  double two_pi;
+};
+
+// Host: exact k-bin of one |k|^2 value s, following src/main.c:355, 369-375.
+// Returns -1 (below), 0..NK-1, or NK (above or beyond Nyquist).
+int host_kbin_of_s(double s, double mink, double binwidth, int nk, int output_log, double min_nyquist);
+
+// Host: build and upload tables. Returns 0 on success.
+int build_bin_tables(const capow_params &p, const Geom &g, int precision, BinTables &t, std::vector<void *> &allocs,
+                     cudaStream_t s);
+
+// launchers
+void launch_mode_counts(cudaStream_t s, const BinParams &bp, const BinTables &t, unsigned long long *nmodes,
+                        unsigned long long *nmodes2d, long long *launches);
+void launch_bin(cudaStream_t s, int precision, const BinParams &bp, const BinTables &t, void *const slots[4],
+                const double *dcv, double *bins, double *bins2d, long long *launches);
+// DC corrections: dcv[slot] = painted sum (minus NGRID for mean-subtracted field A slots)
+void launch_dc_prepare(cudaStream_t s, const void *st, int deterministic, int nslot, int nfields, int mean_sub_a,
+                       const double *fixed_scale, double *dcv, long long *launches);

@@ -1,0 +1,631 @@
+// C ABI of libcapow_gpu (include/capow.h): context, orchestration of paint -> cuFFT -> bin,
+// host-side reference arithmetic for alpha / shot / norm (src/main.c:106-148) and the
+// output normalisation (src/main.c:1019-1056).
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "bin.cuh"
+#include "paint.cuh"
+
+struct capow_ctx {
+  capow_params p;
+  capow_options o;
+  int prec;
+  Geom g;
+  FieldSpec fs;
+  TileGeo tg;
+  BinParams bp;
+  BinTables bt;
+  int nslot;
+  int spec_kind[CAPOW_MAX_SPEC];
+  int shot_moment[CAPOW_MAX_SPEC];  // 0: N, n: <v^n> N
+  int moments;
+  cudaStream_t stream;
+  bool own_stream;
+  // device buffers
+  void *grid_base;      // nslot padded grids, contiguous
+  size_t grid_elems;    // reals per padded grid
+  DevStats *st;
+  PaintBufs pb;
+  double *fixed_scale;
+  double *dcv;
+  double *bins, *bins2d;
+  unsigned long long *nmodes_d, *nmodes2d_d;
+  std::vector<unsigned long long> nmodes, nmodes2d;
+  cufftHandle plan;
+  bool plan_ok;
+  // staging for host particle input
+  void *stage[5];
+  size_t stage_bytes[5];
+  capow_particles last;   // device view of the last painted catalogue
+  bool painted, powered;
+  // host pinned readback
+  double *h_bins;
+  DevStats *h_st;
+  std::vector<void *> allocs;
+  cudaEvent_t ev[4];
+  long long launches;
+  char err[512];
+};
+
+#define FAIL(ctx, code, ...)                                        \
+  do {                                                              \
+    if (ctx) snprintf((ctx)->err, sizeof((ctx)->err), __VA_ARGS__); \
+    return (code);                                                  \
+  } while (0)
+
+#define CK(ctx, call)                                                                                       \
+  do {                                                                                                      \
+    cudaError_t e_ = (call);                                                                                \
+    if (e_ != cudaSuccess) FAIL(ctx, CAPOW_ECUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                                __LINE__);                                                                  \
+  } while (0)
+
+#define CKFFT(ctx, call)                                                         \
+  do {                                                                           \
+    cufftResult r_ = (call);                                                     \
+    if (r_ != CUFFT_SUCCESS) FAIL(ctx, CAPOW_ECUFFT, "%s failed: cufft status %d", #call, (int)r_); \
+  } while (0)
+
+extern "C" const char *capow_strerror(int s) {
+  switch (s) {
+    case CAPOW_OK: return "ok";
+    case CAPOW_EINVAL: return "invalid argument or parameter";
+    case CAPOW_ENOMEM: return "out of memory";
+    case CAPOW_ECUDA: return "CUDA runtime error";
+    case CAPOW_EBOUNDS: return "particle out of grid bounds (LOS == 0)";
+    case CAPOW_ETIMEOUT: return "device wait timed out";
+    case CAPOW_ESTATE: return "call out of order";
+    case CAPOW_ECUFFT: return "cuFFT error";
+    case CAPOW_ENOTSUP: return "not supported";
+  }
+  return "unknown status";
+}
+
+extern "C" const char *capow_last_error(const capow_ctx *ctx) { return ctx ? ctx->err : "no context"; }
+
+// check_inputs semantics (src/read_params.c:294-428) plus what the GPU layout requires.
+static int validate(const capow_params *p, const capow_options *o, char *err, size_t n) {
+#define BAD(...)                   \
+  do {                             \
+    snprintf(err, n, __VA_ARGS__); \
+    return CAPOW_EINVAL;           \
+  } while (0)
+  if (p->LOS < 0 || p->LOS > 3) BAD("LOS is neither 0 (real-space), 1, 2 nor 3");
+  if (p->InterpOrder < 1 || p->InterpOrder > 3) BAD("InterpOrder is neither 1, 2 nor 3");
+  if (p->DoInterlacing != 0 && p->DoInterlacing != 1) BAD("DoInterlacing is neither 0 nor 1");
+  if (p->Output2D != 0 && p->Output2D != 1) BAD("Output2D is neither 0 nor 1");
+  if (p->Output2D && p->NMU <= 0) BAD("NMU is less than 1");
+  if (p->OutputLog != 0 && p->OutputLog != 1) BAD("OutputLog is neither 0 nor 1");
+  if (p->NX <= 0 || p->NY <= 0 || p->NZ <= 0) BAD("NX, NY and NZ must be > 0");
+  if (p->NK <= 0) BAD("NK is less than 1");
+  if (!(p->XMAX > p->XMIN) || !(p->YMAX > p->YMIN) || !(p->ZMAX > p->ZMIN)) BAD("box MAX must exceed MIN");
+  if (p->Maxk < p->Mink) BAD("Maxk is less than Mink");
+  if (p->Momentum < 0 || p->Momentum > 8) BAD("Momentum must be 0..8");
+  if (o->precision < 0 || o->precision > 2) BAD("unknown precision");
+  if (o->spectra < 0 || o->spectra > 7) BAD("unknown spectra mask");
+  if (o->precision != CAPOW_FP64 && (p->NX < 4 || p->NY < 4 || p->NZ < 4))
+    BAD("the FP32 paths need NX, NY, NZ >= 4");
+  long long nzc = p->NZ / 2 + 1;
+  if ((long long)p->NX * p->NY * 2 * nzc >= (1LL << 40)) BAD("grid too large");
+  return CAPOW_OK;
+#undef BAD
+}
+
+static Geom make_geom(const capow_params &p) {
+  Geom g;
+  memset(&g, 0, sizeof g);
+  g.nx = p.NX; g.ny = p.NY; g.nz = p.NZ;
+  g.order = p.InterpOrder;
+  g.los = p.LOS;
+  g.interlace = p.DoInterlacing;
+  g.nxtra = p.NX + p.InterpOrder;
+  g.nzc = p.NZ / 2 + 1;
+  g.row = 2LL * g.nzc;
+  g.slice = (long long)p.NY * g.row;
+  g.main_sz = (long long)p.NX * g.slice;
+  g.xmin = p.XMIN; g.ymin = p.YMIN; g.zmin = p.ZMIN;
+  g.xmax = p.XMAX; g.ymax = p.YMAX; g.zmax = p.ZMAX;
+  g.dx = (p.XMAX - p.XMIN) / (double)p.NX;  // src/main.c:1126-1128
+  g.dy = (p.YMAX - p.YMIN) / (double)p.NY;
+  g.dz = (p.ZMAX - p.ZMIN) / (double)p.NZ;
+  g.xmax_l = (double)(0 + p.NX) * g.dx + p.XMIN;  // src/read_data.c:39
+  g.lx = p.XMAX - p.XMIN;
+  g.hx = g.dx / 2.0; g.hy = g.dy / 2.0; g.hz = g.dz / 2.0;
+  g.rsd_opz = 1.0 + p.Redshift;  // src/read_data.c:69
+  g.rsd_den = 100.0 * sqrt(p.Omega_m * pow((1.0 + p.Redshift), 3.0) + 1.0 - p.Omega_m);
+  g.xmin_f = (float)p.XMIN; g.ymin_f = (float)p.YMIN; g.zmin_f = (float)p.ZMIN;
+  g.idx_f = (float)(1.0 / g.dx); g.idy_f = (float)(1.0 / g.dy); g.idz_f = (float)(1.0 / g.dz);
+  g.rsd_f = (float)(g.rsd_opz / g.rsd_den);
+  // FP32 scale error bound in cells: a few ulps of the coordinate over the cell size plus a few
+  // ulps of the scale itself, times a safety factor
+  double cmax = 0;
+  const double c[6] = {p.XMIN, p.XMAX, p.YMIN, p.YMAX, p.ZMIN, p.ZMAX};
+  for (int k = 0; k < 6; k++) cmax = fmax(cmax, fabs(c[k]));
+  double dmin = fmin(g.dx, fmin(g.dy, g.dz));
+  int nmax = p.NX > p.NY ? (p.NX > p.NZ ? p.NX : p.NZ) : (p.NY > p.NZ ? p.NY : p.NZ);
+  double eps = ldexp(1.0, -23);
+  g.margin = (float)(16.0 * eps * (2.0 * cmax / dmin + nmax + 2.0) + 1e-6);
+  return g;
+}
+
+// Fields and spectra of a run (src/read_data.c:91-130, src/main.c:141-148, 214, 406-441).
+static void plan_fields(capow_ctx *c) {
+  const int m = c->p.Momentum;
+  FieldSpec &fs = c->fs;
+  memset(&fs, 0, sizeof fs);
+  BinParams &bp = c->bp;
+  if (c->o.spectra == CAPOW_SPEC_REFERENCE) {
+    static const int tab[9][6] = {  // nfields, ea, eb, imag, mean_sub_a, shot moment
+        {1, 0, 0, 0, 1, 0}, {2, 0, 1, 1, 1, 1}, {1, 1, 0, 0, 0, 2}, {2, 0, 2, 0, 1, 2}, {2, 1, 2, 1, 0, 3},
+        {1, 2, 0, 0, 0, 4}, {2, 0, 3, 1, 1, 3}, {2, 1, 3, 0, 0, 4}, {2, 0, 4, 0, 1, 4}};
+    fs.nfields = tab[m][0];
+    fs.ea = tab[m][1];
+    fs.eb = tab[m][2];
+    bp.nspec = 1;
+    bp.spec[0].x = 0;
+    bp.spec[0].y = fs.nfields == 2 ? 1 : 0;
+    bp.spec[0].imag = tab[m][3];
+    bp.mean_sub_a = tab[m][4];
+    c->shot_moment[0] = tab[m][5];
+    c->spec_kind[0] = 0;
+    c->moments = (m != 0);
+  } else {
+    const int mask = c->o.spectra;
+    const bool needD = mask & (CAPOW_SPEC_DD | CAPOW_SPEC_DP), needP = mask & (CAPOW_SPEC_DP | CAPOW_SPEC_PP);
+    int fd = -1, fp = -1;
+    if (needD && needP) {
+      fs.nfields = 2; fs.ea = 0; fs.eb = 1; fd = 0; fp = 1;
+    } else if (needD) {
+      fs.nfields = 1; fs.ea = 0; fd = 0;
+    } else {
+      fs.nfields = 1; fs.ea = 1; fp = 0;
+    }
+    bp.mean_sub_a = needD ? 1 : 0;
+    int q = 0;
+    if (mask & CAPOW_SPEC_DD) {
+      bp.spec[q] = SpecDef{fd, fd, 0}; c->shot_moment[q] = 0; c->spec_kind[q] = CAPOW_SPEC_DD; q++;
+    }
+    if (mask & CAPOW_SPEC_DP) {
+      bp.spec[q] = SpecDef{fd, fp, 1}; c->shot_moment[q] = 1; c->spec_kind[q] = CAPOW_SPEC_DP; q++;
+    }
+    if (mask & CAPOW_SPEC_PP) {
+      bp.spec[q] = SpecDef{fp, fp, 0}; c->shot_moment[q] = 2; c->spec_kind[q] = CAPOW_SPEC_PP; q++;
+    }
+    bp.nspec = q;
+    c->moments = needP;
+  }
+  fs.moments = c->moments;
+  fs.need_v = fs.moments || c->p.LOS != 0 || fs.ea > 0 || (fs.nfields == 2 && fs.eb > 0);
+  c->nslot = fs.nfields * (c->p.DoInterlacing ? 2 : 1);
+}
+
+static void *dalloc(capow_ctx *c, size_t bytes) {
+  void *p = nullptr;
+  if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+  c->allocs.push_back(p);
+  return p;
+}
+
+extern "C" int capow_create(const capow_params *p, const capow_options *opt, capow_ctx **out) {
+  if (!p || !out) return CAPOW_EINVAL;
+  *out = nullptr;
+  capow_options o;
+  memset(&o, 0, sizeof o);
+  if (opt) o = *opt;
+  else o.precision = CAPOW_FP32_MIXED;
+  capow_ctx *c = new (std::nothrow) capow_ctx();
+  if (!c) return CAPOW_ENOMEM;
+  c->p = *p;
+  c->o = o;
+  int rc = validate(p, &o, c->err, sizeof c->err);
+  if (rc) {
+    fprintf(stderr, "capow_create: %s\n", c->err);
+    delete c;
+    return rc;
+  }
+  c->prec = o.precision;
+  *out = c;  // from here on capow_destroy releases partial state
+  CK(c, cudaSetDevice(o.device));
+  if (o.stream) {
+    c->stream = (cudaStream_t)o.stream;
+    c->own_stream = false;
+  } else {
+    CK(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    c->own_stream = true;
+  }
+  for (int k = 0; k < 4; k++) CK(c, cudaEventCreate(&c->ev[k]));
+  c->g = make_geom(*p);
+  plan_fields(c);
+  const bool f64 = c->prec == CAPOW_FP64;
+  const size_t eb = f64 ? 8 : 4;
+  c->grid_elems = (size_t)c->g.main_sz;
+  c->grid_base = dalloc(c, eb * c->grid_elems * c->nslot);
+  c->st = (DevStats *)dalloc(c, sizeof(DevStats));
+  c->dcv = (double *)dalloc(c, sizeof(double) * 4);
+  c->fixed_scale = (double *)dalloc(c, sizeof(double) * 2);
+  const int nk = p->NK, n2d = p->Output2D ? p->NK * p->NMU : 0;
+  c->bins = (double *)dalloc(c, sizeof(double) * CAPOW_MAX_SPEC * 5 * nk);
+  c->bins2d = (double *)dalloc(c, sizeof(double) * CAPOW_MAX_SPEC * (n2d ? n2d : 1));
+  c->nmodes_d = (unsigned long long *)dalloc(c, sizeof(unsigned long long) * nk);
+  c->nmodes2d_d = (unsigned long long *)dalloc(c, sizeof(unsigned long long) * (n2d ? n2d : 1));
+  if (!c->grid_base || !c->st || !c->dcv || !c->bins || !c->bins2d || !c->nmodes_d || !c->nmodes2d_d)
+    FAIL(c, CAPOW_ENOMEM, "device allocation failed (grids need %.2f GB)", eb * c->grid_elems * c->nslot / 1e9);
+  CK(c, cudaMallocHost((void **)&c->h_bins, sizeof(double) * CAPOW_MAX_SPEC * (5 * nk + n2d)));
+  CK(c, cudaMallocHost((void **)&c->h_st, sizeof(DevStats)));
+  if (!f64) {
+    c->tg = choose_tiles(c->g, c->nslot, c->prec == CAPOW_FP32_DETERMINISTIC);
+    c->pb.counts = (unsigned *)dalloc(c, sizeof(unsigned) * c->tg.ntiles);
+    c->pb.offsets = (unsigned *)dalloc(c, sizeof(unsigned) * (c->tg.ntiles + 1));
+    c->pb.cursor = (unsigned *)dalloc(c, sizeof(unsigned) * c->tg.ntiles);
+    c->pb.fixed_scale = c->fixed_scale;
+    if (!c->pb.counts || !c->pb.offsets || !c->pb.cursor) FAIL(c, CAPOW_ENOMEM, "tile table allocation failed");
+  }
+  // bins: tables, exact edges, one-time mode counts
+  BinParams &bp = c->bp;
+  bp.nx = p->NX; bp.ny = p->NY; bp.nz = p->NZ; bp.nzc = p->NZ / 2 + 1; bp.xhalf = p->NX / 2;
+  bp.nk = nk; bp.nmu = p->NMU; bp.los = p->LOS; bp.interlace = p->DoInterlacing;
+  bp.odd = p->Odd_Multipoles; bp.out2d = p->Output2D; bp.nfields = c->fs.nfields;
+  bp.two_pi = 2.0 * M_PI;
+  if (build_bin_tables(*p, c->g, c->prec, c->bt, c->allocs, c->stream)) FAIL(c, CAPOW_ENOMEM, "bin tables");
+  CK(c, cudaMemsetAsync(c->nmodes_d, 0, sizeof(unsigned long long) * nk, c->stream));
+  CK(c, cudaMemsetAsync(c->nmodes2d_d, 0, sizeof(unsigned long long) * (n2d ? n2d : 1), c->stream));
+  launch_mode_counts(c->stream, bp, c->bt, c->nmodes_d, c->nmodes2d_d, &c->launches);
+  CK(c, cudaGetLastError());
+  c->nmodes.resize(nk);
+  c->nmodes2d.resize(n2d);
+  CK(c, cudaMemcpyAsync(c->nmodes.data(), c->nmodes_d, sizeof(unsigned long long) * nk, cudaMemcpyDeviceToHost,
+                        c->stream));
+  if (n2d)
+    CK(c, cudaMemcpyAsync(c->nmodes2d.data(), c->nmodes2d_d, sizeof(unsigned long long) * n2d,
+                          cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  // one batched in-place r2c plan over all painted grids (replaces the fftw_execute calls,
+  // src/main.c:266-271): forward, unnormalised, padded last dimension
+  int n[3] = {p->NX, p->NY, p->NZ};
+  int inembed[3] = {p->NX, p->NY, 2 * bp.nzc}, onembed[3] = {p->NX, p->NY, bp.nzc};
+  long long idist = (long long)c->grid_elems, odist = (long long)c->grid_elems / 2;
+  if (idist > 0x7fffffffLL) {
+    // cufftPlanMany takes int distances; large grids use one plan per grid instead
+    CKFFT(c, cufftPlan3d(&c->plan, p->NX, p->NY, p->NZ, f64 ? CUFFT_D2Z : CUFFT_R2C));
+  } else {
+    CKFFT(c, cufftPlanMany(&c->plan, 3, n, inembed, 1, (int)idist, onembed, 1, (int)odist,
+                           f64 ? CUFFT_D2Z : CUFFT_R2C, c->nslot));
+  }
+  c->plan_ok = true;
+  CKFFT(c, cufftSetStream(c->plan, c->stream));
+  return CAPOW_OK;
+}
+
+extern "C" int capow_num_spectra(const capow_ctx *c) { return c ? c->bp.nspec : 0; }
+
+extern "C" int64_t capow_kernel_launches(const capow_ctx *c) { return c ? c->launches : 0; }
+
+static int stage_input(capow_ctx *c, const capow_particles *in, capow_particles *dev) {
+  *dev = *in;
+  if (in->on_device) return CAPOW_OK;
+  const size_t eb = in->dtype == CAPOW_F64 ? 8 : 4;
+  const void *src[5] = {in->x, in->y, in->z, in->vlos, in->w};
+  const void **dst[5] = {&dev->x, &dev->y, &dev->z, &dev->vlos, &dev->w};
+  for (int k = 0; k < 5; k++) {
+    if (!src[k]) {
+      *dst[k] = nullptr;
+      continue;
+    }
+    size_t bytes = eb * in->n;
+    if (c->stage_bytes[k] < bytes) {
+      if (c->stage[k]) cudaFree(c->stage[k]);
+      c->stage[k] = nullptr;
+      c->stage_bytes[k] = 0;
+      CK(c, cudaMalloc(&c->stage[k], bytes));
+      c->stage_bytes[k] = bytes;
+    }
+    CK(c, cudaMemcpyAsync(c->stage[k], src[k], bytes, cudaMemcpyHostToDevice, c->stream));
+    *dst[k] = c->stage[k];
+  }
+  dev->on_device = 1;
+  return CAPOW_OK;
+}
+
+static GridPtrs grid_ptrs(capow_ctx *c) {
+  GridPtrs gp;
+  const size_t eb = c->prec == CAPOW_FP64 ? 8 : 4;
+  for (int k = 0; k < 4; k++)
+    gp.g[k] = k < c->nslot ? (void *)((char *)c->grid_base + eb * c->grid_elems * k) : nullptr;
+  return gp;
+}
+
+static int ensure_records(capow_ctx *c, unsigned long long need, bool weights) {
+  if (need <= c->pb.capacity && (!weights || c->pb.recw)) return CAPOW_OK;
+  if (c->pb.recs) cudaFree(c->pb.recs);
+  if (c->pb.recw) cudaFree(c->pb.recw);
+  c->pb.recs = nullptr;
+  c->pb.recw = nullptr;
+  c->pb.capacity = 0;
+  CK(c, cudaMalloc(&c->pb.recs, sizeof(float4) * need));
+  if (weights) CK(c, cudaMalloc(&c->pb.recw, sizeof(float) * need));
+  c->pb.capacity = need;
+  return CAPOW_OK;
+}
+
+static int enqueue_paint(capow_ctx *c, const capow_particles &d) {
+  const long long n = (long long)d.n;
+  GridPtrs gp = grid_ptrs(c);
+  CK(c, cudaMemsetAsync(c->st, 0, sizeof(DevStats), c->stream));
+  CK(c, cudaEventRecord(c->ev[0], c->stream));
+  if (c->prec == CAPOW_FP64) {
+    CK(c, cudaMemsetAsync(c->grid_base, 0, 8 * c->grid_elems * c->nslot, c->stream));
+    launch_paint64(c->stream, c->g, c->fs, d.dtype, d.x, d.y, d.z, d.vlos, d.w, n, gp, c->st, &c->launches);
+  } else {
+    if (c->pb.special_n < (unsigned long long)n + 1) {
+      if (c->pb.special) cudaFree(c->pb.special);
+      c->pb.special = nullptr;
+      c->pb.special_n = 0;
+      CK(c, cudaMalloc(&c->pb.special, sizeof(unsigned) * (n + 1)));
+      c->pb.special_n = n + 1;
+    }
+    unsigned long long want = (unsigned long long)(tile_dup_estimate(c->g, c->tg) * 1.25 * n) + 65536;
+    if (c->pb.capacity < want / 2 || (d.w && !c->pb.recw)) {
+      int rc = ensure_records(c, want, d.w != nullptr);
+      if (rc) return rc;
+    }
+    launch_paint32(c->stream, c->g, c->fs, c->tg, c->prec == CAPOW_FP32_DETERMINISTIC, d.dtype, d.x, d.y, d.z,
+                   d.vlos, d.w, n, gp, c->pb, c->st, &c->launches);
+  }
+  CK(c, cudaGetLastError());
+  CK(c, cudaEventRecord(c->ev[1], c->stream));
+  return CAPOW_OK;
+}
+
+extern "C" int capow_paint(capow_ctx *c, const capow_particles *parts) {
+  if (!c || !parts) return CAPOW_EINVAL;
+  if (!c->plan_ok) FAIL(c, CAPOW_ESTATE, "context not fully created");
+  if (parts->dtype != CAPOW_F32 && parts->dtype != CAPOW_F64) FAIL(c, CAPOW_EINVAL, "dtype must be F32 or F64");
+  if (!parts->x || !parts->y || !parts->z) FAIL(c, CAPOW_EINVAL, "x, y and z are required");
+  if (c->fs.need_v && !parts->vlos) FAIL(c, CAPOW_EINVAL, "vlos is required for LOS != 0 or momentum fields");
+  if (parts->n >= 0xFFFFFFF0ULL) FAIL(c, CAPOW_EINVAL, "too many particles for one paint");
+  CK(c, cudaSetDevice(c->o.device));
+  capow_particles d;
+  int rc = stage_input(c, parts, &d);
+  if (rc) return rc;
+  if (!c->fs.need_v) d.vlos = nullptr;
+  c->last = d;
+  c->painted = true;
+  c->powered = false;
+  return enqueue_paint(c, d);
+}
+
+// Sync, read the counters, repaint once with a larger record buffer when the tile lists
+// overflowed. Returns a status for fatal conditions found by the paint.
+static int settle_paint(capow_ctx *c) {
+  CK(c, cudaMemcpyAsync(c->h_st, c->st, sizeof(DevStats), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  if (c->h_st->overflow) {
+    int rc = ensure_records(c, (unsigned long long)c->h_st->nrecords + 65536, c->last.w != nullptr);
+    if (rc) return rc;
+    rc = enqueue_paint(c, c->last);
+    if (rc) return rc;
+    CK(c, cudaMemcpyAsync(c->h_st, c->st, sizeof(DevStats), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    if (c->h_st->overflow) FAIL(c, CAPOW_ENOMEM, "tile record buffer overflow after resize");
+  }
+  if (c->h_st->nonfinite) FAIL(c, CAPOW_EINVAL, "non-finite particle coordinate, velocity or weight");
+  if (c->h_st->fatal) FAIL(c, CAPOW_EBOUNDS, "particle out of grid bounds with LOS == 0");
+  return CAPOW_OK;
+}
+
+extern "C" int capow_get_stats(capow_ctx *c, capow_stats *out) {
+  if (!c || !out) return CAPOW_EINVAL;
+  if (!c->painted) FAIL(c, CAPOW_ESTATE, "capow_get_stats before capow_paint");
+  int rc = CAPOW_OK;
+  if (!c->powered) rc = settle_paint(c);
+  if (rc != CAPOW_OK && rc != CAPOW_EBOUNDS) return rc;
+  out->nread = c->h_st->nread;
+  out->nout = c->h_st->nout;
+  out->ngrid = c->h_st->ngrid;
+  out->nsq = c->h_st->nsq;
+  for (int k = 0; k < 4; k++) out->vr[k] = c->h_st->vr[k];
+  out->first_out_of_box = c->h_st->fatal ? (int64_t)(~0ULL - c->h_st->fatal_inv) : -1;
+  return rc;
+}
+
+extern "C" int capow_copy_grid(capow_ctx *c, int which, double *host_out) {
+  if (!c || !host_out) return CAPOW_EINVAL;
+  if (!c->painted || c->powered) FAIL(c, CAPOW_ESTATE, "capow_copy_grid is valid between paint and power");
+  int slot = which;
+  if (c->fs.nfields == 1) {
+    if (which == 2 || which == 3) FAIL(c, CAPOW_EINVAL, "field B is not painted in this run");
+    slot = which == 1 ? 1 : 0;
+  }
+  if (!c->p.DoInterlacing && (which & 1)) FAIL(c, CAPOW_EINVAL, "no interlaced grid in this run");
+  if (c->fs.nfields == 2) slot = (which & 1) ? c->fs.nfields + (which >> 1) : (which >> 1);
+  if (slot >= c->nslot) FAIL(c, CAPOW_EINVAL, "grid index out of range");
+  int rc = settle_paint(c);
+  if (rc) return rc;
+  const size_t n = c->grid_elems;
+  if (c->prec == CAPOW_FP64) {
+    CK(c, cudaMemcpy(host_out, (double *)c->grid_base + n * slot, 8 * n, cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<float> tmp(n);
+    CK(c, cudaMemcpy(tmp.data(), (float *)c->grid_base + n * slot, 4 * n, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; i++) host_out[i] = tmp[i];
+  }
+  // padding columns are not part of the FFT input; report them as zero
+  for (long long r = 0; r < (long long)c->p.NX * c->p.NY; r++)
+    for (long long z = c->p.NZ; z < c->g.row; z++) host_out[r * c->g.row + z] = 0.0;
+  return CAPOW_OK;
+}
+
+static int enqueue_power(capow_ctx *c) {
+  const bool f64 = c->prec == CAPOW_FP64;
+  launch_dc_prepare(c->stream, c->st, c->prec == CAPOW_FP32_DETERMINISTIC, c->nslot, c->fs.nfields,
+                    c->bp.mean_sub_a, c->fixed_scale, c->dcv, &c->launches);
+  if (c->grid_elems > 0x7fffffffULL) {
+    const size_t eb = f64 ? 8 : 4;
+    for (int s = 0; s < c->nslot; s++) {
+      char *gp = (char *)c->grid_base + eb * c->grid_elems * s;
+      if (f64) CKFFT(c, cufftExecD2Z(c->plan, (cufftDoubleReal *)gp, (cufftDoubleComplex *)gp));
+      else CKFFT(c, cufftExecR2C(c->plan, (cufftReal *)gp, (cufftComplex *)gp));
+    }
+  } else {
+    if (f64) CKFFT(c, cufftExecD2Z(c->plan, (cufftDoubleReal *)c->grid_base, (cufftDoubleComplex *)c->grid_base));
+    else CKFFT(c, cufftExecR2C(c->plan, (cufftReal *)c->grid_base, (cufftComplex *)c->grid_base));
+  }
+  CK(c, cudaEventRecord(c->ev[2], c->stream));
+  const int nk = c->p.NK, n2d = c->p.Output2D ? c->p.NK * c->p.NMU : 0;
+  CK(c, cudaMemsetAsync(c->bins, 0, sizeof(double) * CAPOW_MAX_SPEC * 5 * nk, c->stream));
+  if (n2d) CK(c, cudaMemsetAsync(c->bins2d, 0, sizeof(double) * CAPOW_MAX_SPEC * n2d, c->stream));
+  void *slots[4];
+  GridPtrs gp = grid_ptrs(c);
+  for (int k = 0; k < 4; k++) slots[k] = gp.g[k];
+  launch_bin(c->stream, c->prec, c->bp, c->bt, slots, c->dcv, c->bins, n2d ? c->bins2d : nullptr, &c->launches);
+  CK(c, cudaGetLastError());
+  CK(c, cudaEventRecord(c->ev[3], c->stream));
+  CK(c, cudaMemcpyAsync(c->h_bins, c->bins, sizeof(double) * c->bp.nspec * 5 * nk, cudaMemcpyDeviceToHost,
+                        c->stream));
+  if (n2d)
+    CK(c, cudaMemcpyAsync(c->h_bins + CAPOW_MAX_SPEC * 5 * nk, c->bins2d, sizeof(double) * c->bp.nspec * n2d,
+                          cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(c->h_st, c->st, sizeof(DevStats), cudaMemcpyDeviceToHost, c->stream));
+  return CAPOW_OK;
+}
+
+extern "C" int capow_power(capow_ctx *c, capow_spectrum *out, int nout) {
+  if (!c) return CAPOW_EINVAL;
+  if (!c->painted) FAIL(c, CAPOW_ESTATE, "capow_power before capow_paint");
+  if (c->powered) FAIL(c, CAPOW_ESTATE, "grids already transformed; paint again");
+  if (nout < c->bp.nspec || !out) FAIL(c, CAPOW_EINVAL, "need room for %d spectra", c->bp.nspec);
+  CK(c, cudaSetDevice(c->o.device));
+  int rc = enqueue_power(c);
+  if (rc) return rc;
+  c->powered = true;
+  CK(c, cudaStreamSynchronize(c->stream));
+  if (c->h_st->overflow) {  // rare: tile lists outgrew the estimate; repaint and redo
+    c->powered = false;
+    rc = ensure_records(c, (unsigned long long)c->h_st->nrecords + 65536, c->last.w != nullptr);
+    if (rc) return rc;
+    rc = enqueue_paint(c, c->last);
+    if (rc) return rc;
+    rc = enqueue_power(c);
+    if (rc) return rc;
+    c->powered = true;
+    CK(c, cudaStreamSynchronize(c->stream));
+    if (c->h_st->overflow) FAIL(c, CAPOW_ENOMEM, "tile record buffer overflow after resize");
+  }
+  if (c->h_st->nonfinite) FAIL(c, CAPOW_EINVAL, "non-finite particle coordinate, velocity or weight");
+  if (c->h_st->fatal) FAIL(c, CAPOW_EBOUNDS, "particle out of grid bounds with LOS == 0");
+  // shot noise and normalisation, src/main.c:117-148 (one rank: NTask = 1)
+  const DevStats &st = *c->h_st;
+  const capow_params &p = c->p;
+  const double N = st.ngrid;
+  const double alpha = N / ((double)p.NX * (double)p.NY * (double)p.NZ);
+  const double nbar = N / ((p.XMAX - p.XMIN) * (p.YMAX - p.YMIN) * (p.ZMAX - p.ZMIN));
+  const double norm = nbar * N;
+  double vr[5] = {1.0, 0, 0, 0, 0};
+  if (c->moments) {
+    const double nsq = st.nsq / 1.0;
+    for (int k = 0; k < 4; k++) vr[k + 1] = st.vr[k] / (nsq * 1.0);
+  }
+  const int nk = p.NK, n2d = p.Output2D ? p.NK * p.NMU : 0;
+  for (int q = 0; q < c->bp.nspec; q++) {
+    capow_spectrum &s = out[q];
+    const int m = c->shot_moment[q];
+    s.shot = m == 0 ? N : vr[m] * N;
+    s.norm = norm;
+    s.alpha = alpha;
+    s.kind = c->spec_kind[q];
+    s.last_bin = -1;
+    for (int l = 0; l < 5; l++) {
+      if (!s.pk[l]) continue;
+      if ((l == 1 || l == 3) && !p.Odd_Multipoles) {
+        memset(s.pk[l], 0, sizeof(double) * nk);
+        continue;
+      }
+      memcpy(s.pk[l], c->h_bins + (q * 5 + l) * nk, sizeof(double) * nk);
+    }
+    if (s.nmodes)
+      for (int b = 0; b < nk; b++) s.nmodes[b] = (int64_t)c->nmodes[b];
+    if (n2d && s.pk2d) memcpy(s.pk2d, c->h_bins + CAPOW_MAX_SPEC * 5 * nk + q * n2d, sizeof(double) * n2d);
+    if (n2d && s.nmodes2d)
+      for (int b = 0; b < n2d; b++) s.nmodes2d[b] = (int64_t)c->nmodes2d[b];
+  }
+  return CAPOW_OK;
+}
+
+extern "C" int capow_normalise(const capow_params *p, capow_spectrum *s) {
+  if (!p || !s || !s->pk[0] || !s->pk[2] || !s->pk[4] || !s->nmodes) return CAPOW_EINVAL;
+  const int NK = p->NK;
+  std::vector<int> fill(NK, 0);
+  const double shot = s->shot, norm = s->norm;
+  for (int i = 0; i < NK; i++) {  // src/main.c:1021-1033
+    const double nm = (double)s->nmodes[i];
+    if (s->nmodes[i] > 0 && fill[i] == 0) {
+      s->pk[0][i] -= nm * shot;
+      s->pk[0][i] /= nm * norm;
+      s->pk[2][i] *= 5.0 / (nm * norm);
+      s->pk[4][i] *= 9.0 / (nm * norm);
+      if (p->Odd_Multipoles && s->pk[1] && s->pk[3]) {
+        s->pk[1][i] *= 3.0 / (nm * norm);
+        s->pk[3][i] *= 7.0 / (nm * norm);
+      }
+      fill[i] = 1;
+    }
+  }
+  if (p->Output2D && s->pk2d && s->nmodes2d)  // :1034-1040
+    for (int i = 0; i < NK * p->NMU; i++)
+      if (s->nmodes2d[i] > 0) s->pk2d[i] /= (double)s->nmodes2d[i] * norm;
+  s->last_bin = -1;
+  for (int i = NK - 1; i >= 0; i--) {  // :1043-1056
+    if (fill[i] == 1) {
+      if (p->Odd_Multipoles && s->pk[1] && s->pk[3]) {
+        s->pk[1][i] = 0.0;
+        s->pk[3][i] = 0.0;
+      }
+      s->pk[0][i] = 0.0;
+      s->pk[2][i] = 0.0;
+      s->pk[4][i] = 0.0;
+      s->nmodes[i] = 0;
+      s->last_bin = i;
+      break;
+    }
+  }
+  return CAPOW_OK;
+}
+
+extern "C" int capow_stage_ms(capow_ctx *c, float *paint_ms, float *fft_ms, float *bin_ms) {
+  if (!c) return CAPOW_EINVAL;
+  CK(c, cudaEventSynchronize(c->ev[3]));
+  float a = 0, b = 0, d = 0;
+  CK(c, cudaEventElapsedTime(&a, c->ev[0], c->ev[1]));
+  CK(c, cudaEventElapsedTime(&b, c->ev[1], c->ev[2]));
+  CK(c, cudaEventElapsedTime(&d, c->ev[2], c->ev[3]));
+  if (paint_ms) *paint_ms = a;
+  if (fft_ms) *fft_ms = b;
+  if (bin_ms) *bin_ms = d;
+  return CAPOW_OK;
+}
+
+extern "C" void capow_destroy(capow_ctx *c) {
+  if (!c) return;
+  cudaSetDevice(c->o.device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->plan_ok) cufftDestroy(c->plan);
+  for (void *p : c->allocs) cudaFree(p);
+  for (int k = 0; k < 5; k++)
+    if (c->stage[k]) cudaFree(c->stage[k]);
+  if (c->pb.recs) cudaFree(c->pb.recs);
+  if (c->pb.recw) cudaFree(c->pb.recw);
+  if (c->pb.special) cudaFree(c->pb.special);
+  if (c->h_bins) cudaFreeHost(c->h_bins);
+  if (c->h_st) cudaFreeHost(c->h_st);
+  for (int k = 0; k < 4; k++)
+    if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}

@@ -1,0 +1,165 @@
+/* ASCII particle catalogue reader with the reference's format and error behaviour
+ * (src/read_data.c:50-76): one particle per line as `x y z vx vy vz`, lines starting with
+ * '#' skipped, any other line that does not hold six numbers is a fatal error. The line of
+ * sight picks the velocity column (LOS 1 -> vx, 2 -> vy, otherwise vz).
+ *
+ * The file is read in one pass into memory and its lines are parsed by several threads
+ * (strtod, correctly rounded like the reference's sscanf("%lf")), each writing its own
+ * contiguous range, so the particle order of the file is kept. */
+#include <errno.h>
+#include <pthread.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+#include "capow.h"
+
+typedef struct {
+  const char *b, *e; /* [b, e) whole lines */
+  size_t n;          /* particles in this chunk */
+  size_t off;        /* output offset */
+  int los;
+  double *x, *y, *z, *v;
+  const char *bad;   /* first bad line, if any */
+} chunk;
+
+static int is_hspace(char c) { return c == ' ' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; }
+
+/* parse up to six numbers of one line [p, e); returns how many were read */
+static int parse_line(const char *p, const char *e, double out[6]) {
+  int k = 0;
+  while (k < 6) {
+    while (p < e && is_hspace(*p)) p++;
+    if (p >= e) break;
+    char *end;
+    double v = strtod(p, &end);
+    if (end == p || end > e) break;
+    out[k++] = v;
+    p = end;
+  }
+  return k;
+}
+
+static void *count_lines(void *arg) {
+  chunk *c = (chunk *)arg;
+  size_t n = 0;
+  const char *p = c->b;
+  while (p < c->e) {
+    const char *nl = memchr(p, '\n', (size_t)(c->e - p));
+    const char *le = nl ? nl : c->e;
+    if (!(le > p && *p == '#')) n++;
+    p = nl ? nl + 1 : c->e;
+  }
+  c->n = n;
+  return NULL;
+}
+
+static void *parse_chunk(void *arg) {
+  chunk *c = (chunk *)arg;
+  size_t i = c->off;
+  const char *p = c->b;
+  double v[6];
+  while (p < c->e) {
+    const char *nl = memchr(p, '\n', (size_t)(c->e - p));
+    const char *le = nl ? nl : c->e;
+    if (!(le > p && *p == '#')) {
+      if (parse_line(p, le, v) != 6) {
+        c->bad = p;
+        return NULL;
+      }
+      c->x[i] = v[0];
+      c->y[i] = v[1];
+      c->z[i] = v[2];
+      c->v[i] = (c->los == 1) ? v[3] : (c->los == 2 ? v[4] : v[5]);
+      i++;
+    }
+    p = nl ? nl + 1 : c->e;
+  }
+  return NULL;
+}
+
+int capow_read_catalogue(const char *path, int los, size_t *n_out, double **x, double **y, double **z, double **vlos,
+                         char *msg, size_t msglen) {
+  if (msg && msglen) msg[0] = 0;
+  *n_out = 0;
+  *x = *y = *z = *vlos = NULL;
+  FILE *f = fopen(path, "rb");
+  if (!f) { /* src/read_data.c:51 */
+    if (msg) snprintf(msg, msglen, "Task 0 cannot open input file\nFatal Error at line 96 in routine read_data\n");
+    return CAPOW_EINVAL;
+  }
+  if (fseek(f, 0, SEEK_END) != 0) {
+    fclose(f);
+    return CAPOW_EINVAL;
+  }
+  long sz = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  char *buf = (char *)malloc((size_t)sz + 1);
+  if (!buf) {
+    fclose(f);
+    return CAPOW_ENOMEM;
+  }
+  size_t got = fread(buf, 1, (size_t)sz, f);
+  fclose(f);
+  buf[got] = 0;
+  const char *end = buf + got;
+  long ncpu = sysconf(_SC_NPROCESSORS_ONLN);
+  int nt = (int)(ncpu > 0 ? ncpu : 1);
+  if (nt > 32) nt = 32;
+  if (got < (1u << 20)) nt = 1;
+  chunk ch[32];
+  pthread_t th[32];
+  const char *p = buf;
+  for (int t = 0; t < nt; t++) {
+    memset(&ch[t], 0, sizeof ch[t]);
+    ch[t].b = p;
+    const char *q = (t == nt - 1) ? end : buf + (size_t)got * (t + 1) / nt;
+    if (q < p) q = p;
+    if (q < end) {
+      const char *nl = memchr(q, '\n', (size_t)(end - q));
+      q = nl ? nl + 1 : end;
+    }
+    ch[t].e = q;
+    ch[t].los = los;
+    p = q;
+  }
+  for (int t = 0; t < nt; t++) pthread_create(&th[t], NULL, count_lines, &ch[t]);
+  for (int t = 0; t < nt; t++) pthread_join(th[t], NULL);
+  size_t total = 0;
+  for (int t = 0; t < nt; t++) {
+    ch[t].off = total;
+    total += ch[t].n;
+  }
+  double *a = (double *)malloc(sizeof(double) * (total ? total : 1));
+  double *b = (double *)malloc(sizeof(double) * (total ? total : 1));
+  double *c = (double *)malloc(sizeof(double) * (total ? total : 1));
+  double *d = (double *)malloc(sizeof(double) * (total ? total : 1));
+  if (!a || !b || !c || !d) {
+    free(a); free(b); free(c); free(d); free(buf);
+    return CAPOW_ENOMEM;
+  }
+  for (int t = 0; t < nt; t++) {
+    ch[t].x = a; ch[t].y = b; ch[t].z = c; ch[t].v = d;
+    pthread_create(&th[t], NULL, parse_chunk, &ch[t]);
+  }
+  for (int t = 0; t < nt; t++) pthread_join(th[t], NULL);
+  for (int t = 0; t < nt; t++) {
+    if (ch[t].bad) { /* src/read_data.c:64 */
+      const char *le = memchr(ch[t].bad, '\n', (size_t)(end - ch[t].bad));
+      size_t len = le ? (size_t)(le - ch[t].bad + 1) : (size_t)(end - ch[t].bad);
+      if (len > 1999) len = 1999;
+      if (msg)
+        snprintf(msg, msglen, "Task 0 has error reading file: %.*s\nFatal Error at line 102 in routine read_data\n",
+                 (int)len, ch[t].bad);
+      free(a); free(b); free(c); free(d); free(buf);
+      return CAPOW_EINVAL;
+    }
+  }
+  free(buf);
+  *n_out = total;
+  *x = a; *y = b; *z = c; *vlos = d;
+  return CAPOW_OK;
+}
+
+void capow_free(void *p) { free(p); }

@@ -1,0 +1,63 @@
+// Paint-stage interfaces shared by paint.cu and capow_api.cu.
+#pragma once
+#include "common.cuh"
+
+template <typename T>
+struct PIn {
+  const T *x, *y, *z, *v, *w;  // v, w may be null
+};
+
+// Device-side counters of one paint (read back by capow_get_stats / capow_power).
+struct DevStats {
+  double nread, nout, ngrid, nsq;
+  double vr[4];
+  double dc[4];              // sum of every value deposited inside the FFT region, per grid slot
+  double absw[2];            // sum |w v^e| per field: bound used for the fixed-point scale
+  unsigned long long dc_fixed[4];  // deterministic mode: exact integer DC sums
+  unsigned int nspecial;     // particles routed to the exact FP64 rules
+  unsigned int nrecords;     // tile-list records needed
+  unsigned long long fatal_inv;  // max of (~0 - index) over LOS == 0 particles outside the box
+  int fatal;                 // LOS == 0 particle outside the box
+  int nonfinite;             // NaN/inf coordinate
+  int overflow;              // record buffer too small
+  int pad;
+};
+
+// Tile decomposition of the grid for the FP32 path.
+struct TileGeo {
+  int tx, ty, tz;
+  int nbx, nby, nbz;
+  int ntiles;
+};
+
+// Grid slot order: slot = stencil * nfields + field (A normal, B normal, A interlaced, B interlaced
+// for two fields). Pointers to padded [NX][NY][2(NZ/2+1)] grids.
+struct GridPtrs {
+  void *g[4];
+};
+
+struct PaintBufs {
+  unsigned int *counts;    // ntiles
+  unsigned int *offsets;   // ntiles + 1
+  unsigned int *cursor;    // ntiles
+  float4 *recs;            // capacity
+  float *recw;             // capacity (only when weights are given)
+  unsigned int *special;   // n: indices of particles handled by the exact rules
+  unsigned long long special_n;
+  unsigned long long capacity;
+  double *fixed_scale;     // [2] deterministic mode: 2^S per field (device)
+};
+
+// host launchers (paint.cu)
+void launch_paint64(cudaStream_t s, const Geom &g, const FieldSpec &fs, int dtype, const void *x, const void *y,
+                    const void *z, const void *v, const void *w, long long n, const GridPtrs &grids, DevStats *st,
+                    long long *launches);
+
+void launch_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, int deterministic,
+                    int dtype, const void *x, const void *y, const void *z, const void *v, const void *w,
+                    long long n, const GridPtrs &grids, const PaintBufs &b, DevStats *st, long long *launches);
+
+// suggested tile geometry for a grid (and whether two fields are painted)
+TileGeo choose_tiles(const Geom &g, int nslots, int deterministic);
+size_t tile_smem_bytes(const TileGeo &tg, int nslots, int deterministic);
+double tile_dup_estimate(const Geom &g, const TileGeo &tg);

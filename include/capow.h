@@ -1,0 +1,194 @@
+/* capow.h -- C ABI of libcapow_gpu, the GB300 (sm_103a) implementation of CAPOW's
+ * periodic-box power-spectrum path.
+ *
+ * The reference has no plugin interface: its periodic path is a chain of C functions
+ * sharing globals (src/proto.h:25-46, src/vars.h). Each entry point below replaces one
+ * link of that chain; the file:line it replaces is given beside it. Paths are relative
+ * to the CAPOW source tree.
+ *
+ *   reference (src/main.c:28-298, periodic branch)      this library
+ *   ------------------------------------------------      -----------------------------
+ *   read_parameterfile / check_inputs (read_params.c)    capow_params (+ driver parser)
+ *   create_grids            (main.c:1123-1251)           capow_create
+ *   read_periodic_serial_ascii + add_to_grid
+ *                           (read_data.c:32-179, 514-745) capow_paint
+ *   shot / norm             (main.c:106-148)             capow_get_stats + capow_power
+ *   mean subtraction        (main.c:211-225)             capow_power (exact DC correction)
+ *   fftw_execute            (main.c:266-271)             capow_power (cuFFT)
+ *   compute_periodic_power  (main.c:302-468)             capow_power
+ *   output_power arithmetic (main.c:1019-1056)           capow_normalise
+ *   destroy_grids           (main.c:1255-1294)           capow_destroy
+ *
+ * Conventions: every call returns an int status (CAPOW_OK = 0); nothing in the library
+ * exits or aborts (the reference calls FatalError -> MPI_Abort, main.c:1298-1303; the
+ * driver maps a nonzero status to the same message-and-exit). No torch types; plain
+ * pointers and sizes only. A context is not thread-safe; all its GPU work runs on the
+ * context's CUDA stream.
+ */
+#ifndef CAPOW_H
+#define CAPOW_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CAPOW_ABI_VERSION 1
+
+/* ---------------------------------------------------------------- status codes */
+#define CAPOW_OK 0
+#define CAPOW_EINVAL 1   /* bad argument or parameter (read_params.c:294-428 checks) */
+#define CAPOW_ENOMEM 2   /* device or host allocation failed */
+#define CAPOW_ECUDA 3    /* CUDA runtime error */
+#define CAPOW_EBOUNDS 4  /* LOS==0 particle outside the box: the reference aborts (read_data.c:81-85) */
+#define CAPOW_ETIMEOUT 5 /* a bounded device wait gave up */
+#define CAPOW_ESTATE 6   /* call out of order (e.g. capow_power before capow_paint) */
+#define CAPOW_ECUFFT 7   /* cuFFT error */
+#define CAPOW_ENOTSUP 8  /* combination not supported */
+
+/* ---------------------------------------------------------------- parameters */
+/* The run_parameters.dat tags that drive the periodic path (read_params.c:65-227), with the
+ * reference's names and meanings. Survey-only tags are accepted by the driver's parser for
+ * file compatibility and ignored here. */
+typedef struct capow_params {
+  int NX, NY, NZ;                           /* grid cells per axis (vars.h:79-81) */
+  double XMIN, XMAX, YMIN, YMAX, ZMIN, ZMAX; /* box (vars.h:83-85) */
+  int InterpOrder;                          /* 1 NN, 2 CIC, 3 TSC (vars.h:78) */
+  int DoInterlacing;                        /* 0/1 (vars.h:77) */
+  int NK, NMU;                              /* k bins, mu bins for the 2-D output (vars.h:88-89) */
+  int Output2D, OutputLog;                  /* (vars.h:90-91) */
+  double Mink, Maxk;                        /* (vars.h:92-93) */
+  double Omega_m, Redshift;                 /* RSD shift factor (read_data.c:69-75) */
+  int LOS;                                  /* 0 real space (mu about z), 1/2/3 RSD along x/y/z (vars.h:108) */
+  int Momentum;                             /* 0..8: which fields and which spectrum (vars.h:113) */
+  int Odd_Multipoles;                       /* also P1, P3 (vars.h:121) */
+} capow_params;
+
+/* numeric path */
+#define CAPOW_FP64 0          /* plain double path: FP64 grids, FFT and bins */
+#define CAPOW_FP32_MIXED 1    /* FP32 grids and FFT; FP64 per-bin sums, scalars, near-edge indices */
+#define CAPOW_FP32_DETERMINISTIC 2 /* as FP32_MIXED with int64 fixed-point painting: bit-reproducible grids */
+
+/* spectra selection (capow_options.spectra) */
+#define CAPOW_SPEC_REFERENCE 0 /* one spectrum chosen by params.Momentum, as one reference run */
+#define CAPOW_SPEC_DD 1        /* density auto (the reference's Momentum 0)                   */
+#define CAPOW_SPEC_DP 2        /* density x LOS momentum, Im(D* P) (Momentum 1)                */
+#define CAPOW_SPEC_PP 4        /* LOS momentum auto (Momentum 2)                               */
+
+typedef struct capow_options {
+  int precision; /* CAPOW_FP64 / CAPOW_FP32_MIXED / CAPOW_FP32_DETERMINISTIC */
+  int spectra;   /* CAPOW_SPEC_REFERENCE, or an OR of CAPOW_SPEC_DD|DP|PP (one paint, one set of FFTs) */
+  int device;    /* CUDA device ordinal */
+  void *stream;  /* cudaStream_t to run on, or NULL for a stream owned by the context */
+  int reserved[8];
+} capow_options;
+
+/* particle input: structure of arrays */
+#define CAPOW_F32 0
+#define CAPOW_F64 1
+typedef struct capow_particles {
+  size_t n;
+  int dtype;         /* CAPOW_F32 or CAPOW_F64, applies to every array */
+  int on_device;     /* 1: device pointers (resident in HBM); 0: host pointers (copied in) */
+  const void *x, *y, *z; /* positions, box units */
+  const void *vlos;  /* velocity along the line of sight in km/s: the vz column for LOS 0 and 3,
+                        vx for 1, vy for 2 (read_data.c:65-76). May be NULL when no momentum
+                        field is painted and LOS == 0. */
+  const void *w;     /* per-particle weights, or NULL for w = 1 (read_data.c:60) */
+} capow_particles;
+
+/* counters of the paint pass (read_data.c:37, 78-88, 92-138) */
+typedef struct capow_stats {
+  double nread;   /* particles read */
+  double nout;    /* outside the box after the RSD shift (LOS != 0) */
+  double ngrid;   /* sum of w over accepted particles = NPERIODIC (main.c:76) */
+  double nsq;     /* sum of w over all particles */
+  double vr[4];   /* sum of w*v^n, n = 1..4, over all particles */
+  int64_t first_out_of_box; /* LOS == 0: index of the first particle outside the box (the one the
+                               reference reports before aborting, read_data.c:81-84), else -1 */
+} capow_stats;
+
+/* one spectrum. The caller owns every array; NULL arrays are skipped. */
+typedef struct capow_spectrum {
+  double *pk[5];       /* P0..P4, NK each (P1, P3 only when Odd_Multipoles) */
+  int64_t *nmodes;     /* NK */
+  double *pk2d;        /* NK*NMU when Output2D */
+  int64_t *nmodes2d;   /* NK*NMU when Output2D */
+  double shot, norm, alpha; /* filled by capow_power (main.c:117-148) */
+  int last_bin;        /* filled by capow_normalise: the zeroed highest filled bin, or -1 */
+  int kind;            /* filled by capow_power: CAPOW_SPEC_DD / DP / PP, or 0 for a reference Momentum run */
+} capow_spectrum;
+
+typedef struct capow_ctx capow_ctx;
+
+/* create_grids (main.c:1123-1251): validates params (read_params.c:294-428 semantics),
+ * allocates device grids, cuFFT plans and the k-bin threshold tables. */
+int capow_create(const capow_params *p, const capow_options *opt, capow_ctx **out);
+
+/* read_periodic_serial_ascii + add_to_grid (read_data.c:32-179, 514-745): RSD shift,
+ * bounds count, mass assignment of every requested field with the interlaced copy, the
+ * halo fold and the velocity moments, for one catalogue. Replaces any previous paint. */
+int capow_paint(capow_ctx *ctx, const capow_particles *parts);
+
+/* counters from the last paint (ends with a stream synchronisation). The counters are filled
+ * even when the status is CAPOW_EBOUNDS, so the caller can report the offending particle. */
+int capow_get_stats(capow_ctx *ctx, capow_stats *out);
+
+/* mean subtraction, FFT and compute_periodic_power (main.c:211-225, 266-271, 302-468):
+ * raw bin sums (not normalised) for each requested spectrum, in the order DD, DP, PP
+ * (or the single Momentum spectrum). `out` has room for `nout` spectra. Ends with a
+ * stream synchronisation and the device-to-host copy of the bins. */
+int capow_power(capow_ctx *ctx, capow_spectrum *out, int nout);
+
+/* output_power arithmetic (main.c:1019-1056) in place on one spectrum's raw sums. Host only. */
+int capow_normalise(const capow_params *p, capow_spectrum *s);
+
+/* number of spectra capow_power will produce for this context */
+int capow_num_spectra(const capow_ctx *ctx);
+
+/* copy one painted real grid to the host in the reference's padded layout
+ * [NX][NY][2*(NZ/2+1)] as float64 (after the halo fold, before mean subtraction).
+ * which: 0 field A, 1 field A interlaced, 2 field B, 3 field B interlaced. Valid between
+ * capow_paint and capow_power. For parity tests. */
+int capow_copy_grid(capow_ctx *ctx, int which, double *host_out);
+
+/* device milliseconds of the last paint, FFT and bin stages (CUDA events on the context stream) */
+int capow_stage_ms(capow_ctx *ctx, float *paint_ms, float *fft_ms, float *bin_ms);
+
+/* total number of kernels this library launched on the context since creation */
+int64_t capow_kernel_launches(const capow_ctx *ctx);
+
+void capow_destroy(capow_ctx *ctx);
+
+/* ---------------------------------------------------------------- host-side file formats */
+
+/* read_parameterfile + check_inputs (read_params.c:30-428): parse a run_parameters.dat with
+ * the same 41 mandatory tags, `%` comments, duplicate/missing-tag errors and range checks.
+ * On failure returns CAPOW_EINVAL (CAPOW_ENOTSUP for Periodic 0) and writes the reference's
+ * message text into msg. Warnings the reference prints are also appended to msg on success. */
+int capow_read_params(const char *path, capow_params *out, char *msg, size_t msglen);
+
+/* the periodic reader's parse loop (read_data.c:50-76): `x y z vx vy vz` per line, `#` lines
+ * skipped, malformed lines fatal. Returns malloc'd float64 arrays (free with capow_free);
+ * vlos holds the column LOS selects. */
+int capow_read_catalogue(const char *path, int los, size_t *n, double **x, double **y, double **z, double **vlos,
+                         char *msg, size_t msglen);
+void capow_free(void *p);
+
+/* output_power's file format (main.c:1058-1101), plus `<path>_2D` when Output2D. */
+int capow_write_output(const char *path, const capow_params *p, const capow_spectrum *s);
+
+/* centre of k bin i as the output file prints it (main.c:1070-1075) */
+double capow_bin_centre(const capow_params *p, int i);
+
+const char *capow_strerror(int status);
+
+/* text of the last error recorded on this context (e.g. the failing CUDA call) */
+const char *capow_last_error(const capow_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CAPOW_H */

@@ -1,0 +1,161 @@
+"""Generate the golden fixtures in this folder from the UNMODIFIED reference program.
+
+The reference (CAPOW) ships no tests, data or expected outputs, so its own behaviour is captured
+here: oracle/_ref/capow_ref is the reference sources compiled against single-rank MPI / FFTW / GSL
+stand-ins (oracle/Makefile.ref). For each case this script writes a seeded catalogue and a
+run_parameters.dat, runs the reference, and stores
+
+  * the raw bin sums Pk0..Pk4, Nmodes (and 2-D bins) left in its globals by compute_periodic_power,
+  * the scalars that passed through MPI_Allreduce (NPERIODIC, sum w, sum w v^n),
+  * its output file and stdout text,
+  * for the small cases, the painted grids (after the halo fold, before mean subtraction),
+
+plus parameter-file and catalogue error cases (stdout text). Run from the repo root, where the
+reference sources are mounted:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle as orc  # noqa: E402
+
+CASES = [
+    # name, params, n particles, seed, keep grids
+    ("nn_los0", dict(NX=8, NY=8, NZ=8, InterpOrder=1, LOS=0, DoInterlacing=1, Momentum=0, NK=6, Maxk=0.05,
+                     Odd_Multipoles=1), 200, 1, True),
+    ("cic_los0_mom1", dict(NX=8, NY=10, NZ=6, InterpOrder=2, LOS=0, DoInterlacing=1, Momentum=1, NK=6, Maxk=0.05,
+                           Odd_Multipoles=1), 300, 2, True),
+    ("tsc_los3_mom1", dict(NX=12, NY=8, NZ=10, InterpOrder=3, LOS=3, DoInterlacing=1, Momentum=1, NK=8, Maxk=0.06,
+                           Odd_Multipoles=1), 400, 3, True),
+    ("tsc_los0_mom2", dict(NX=10, NY=10, NZ=10, InterpOrder=3, LOS=0, DoInterlacing=1, Momentum=2, NK=8,
+                           Maxk=0.05, Odd_Multipoles=0), 400, 4, True),
+    ("tsc_los1_2d", dict(NX=16, NY=16, NZ=16, InterpOrder=3, LOS=1, DoInterlacing=1, Momentum=0, NK=10, Maxk=0.1,
+                         Output2D=1, NMU=4, Odd_Multipoles=1), 1000, 5, False),
+    ("cic_los2_log", dict(NX=16, NY=12, NZ=20, InterpOrder=2, LOS=2, DoInterlacing=0, Momentum=4, NK=7, Mink=-2.0,
+                          Maxk=-0.8, OutputLog=1, Odd_Multipoles=1), 1000, 6, False),
+    ("tsc_c0like", dict(NX=32, NY=32, NZ=32, InterpOrder=2, LOS=0, DoInterlacing=1, Momentum=0, NK=16, Maxk=0.1,
+                        Odd_Multipoles=0), 20000, 7, False),
+    ("m8_los3", dict(NX=16, NY=16, NZ=16, InterpOrder=3, LOS=3, DoInterlacing=1, Momentum=8, NK=8, Maxk=0.05,
+                     Odd_Multipoles=1), 2000, 8, False),
+]
+
+BOX = dict(XMIN=-3.0, XMAX=997.0, YMIN=0.0, YMAX=1000.0, ZMIN=10.0, ZMAX=510.0)
+
+
+def catalogue(p, n, seed):
+    rng = np.random.default_rng(seed)
+    lo = np.array([p.XMIN, p.YMIN, p.ZMIN])
+    hi = np.array([p.XMAX, p.YMAX, p.ZMAX])
+    N = np.array([p.NX, p.NY, p.NZ])
+    d = (hi - lo) / N
+    pos = rng.uniform(lo[:, None], hi[:, None], size=(3, n))
+    m = max(1, n // 16)
+    for a in range(3):  # nodes and half cells exercise every edge rule
+        pos[a, a * m:(a + 1) * m] = lo[a] + d[a] * rng.integers(0, N[a], m)
+        pos[a, (a + 3) * m:(a + 4) * m] = lo[a] + d[a] * (rng.integers(0, N[a], m) + 0.5)
+    vel = rng.normal(0.0, 300.0, size=(3, n))
+    return pos, vel
+
+
+def main():
+    orc.build()
+    if not orc.ref_available():
+        raise SystemExit("oracle/_ref/capow_ref is not built (reference sources not mounted)")
+    manifest = {}
+    with tempfile.TemporaryDirectory() as td:
+        for name, kw, n, seed, grids in CASES:
+            p = orc.Params(**BOX, **kw)
+            pos, vel = catalogue(p, n, seed)
+            r = orc.run_ref_binary(p, os.path.join(td, name), *pos, *vel, grids=grids)
+            assert r["returncode"] == 0, r["stdout"]
+            d = r["dump"]
+            out = dict(x=pos[0], y=pos[1], z=pos[2], vx=vel[0], vy=vel[1], vz=vel[2],
+                       allreduce=d["allreduce"], Nmodes=d["Nmodes"])
+            for k in ("Pk0", "Pk1", "Pk2", "Pk3", "Pk4", "Pk_2D", "Nmodes_2D"):
+                if k in d:
+                    out[k] = d[k]
+            for k, g in r.get("grids", {}).items():
+                out["grid_" + k] = g
+            np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+            with open(os.path.join(HERE, f"{name}.out"), "w") as f:
+                f.write(r["output"])
+            with open(os.path.join(HERE, f"{name}.stdout"), "w") as f:
+                f.write(r["stdout"])
+            manifest[name] = dict(params=dataclass_dict(p), n=n, seed=seed)
+            with open(os.path.join(HERE, f"{name}.stdout"), "w") as f:
+                f.write(r["stdout"].replace(os.path.join(td, name, "data.txt"), "{DATAFILE}").replace(
+                    os.path.join(td, name, "out.txt"), "{OUTFILE}"))
+        # parameter-file error cases: the reference's stdout for each
+        errs = {}
+        good = orc.Params(**BOX, NX=8, NY=8, NZ=8)
+        base = os.path.join(td, "base.dat")
+        good.write_file(base)
+        with open(base) as f:
+            lines = f.read().splitlines()
+        variants = {
+            "missing_tag": [l for l in lines if not l.startswith("NK ")],
+            "duplicate_tag": lines + ["NX 8"],
+            "unknown_tag": lines + ["InputFormat 1"],
+            "bad_los": [("LOS 7" if l.startswith("LOS ") else l) for l in lines],
+            "bad_order": [("InterpOrder 4" if l.startswith("InterpOrder ") else l) for l in lines],
+            "bad_nk": [("NK 0" if l.startswith("NK ") else l) for l in lines],
+            "bad_box": [("XMAX -5.0" if l.startswith("XMAX ") else l) for l in lines],
+            "bad_k": [("Maxk -1.0" if l.startswith("Maxk ") else l) for l in lines],
+            "nmu_2d": [("Output2D 1" if l.startswith("Output2D ") else ("NMU 0" if l.startswith("NMU ") else l))
+                       for l in lines],
+            "comments_and_short_lines": ["% comment line", "lonely"] + lines + ["   ", "% trailing"],
+        }
+        cat = os.path.join(td, "c.txt")
+        orc.write_catalogue(cat, [1.0], [20.0], [30.0], [0.0], [0.0], [0.0])
+        import subprocess
+
+        for k, ls in variants.items():
+            pf = os.path.join(td, f"{k}.dat")
+            with open(pf, "w") as f:
+                f.write("\n".join(ls) + "\n")
+            r = subprocess.run([orc.REF_BIN, pf, cat, "none", os.path.join(td, "o.txt")], capture_output=True,
+                               text=True)
+            errs[k] = dict(lines=ls, stdout=r.stdout.replace(pf, "{PARAMFILE}").replace(cat, "{DATAFILE}"),
+                           returncode=r.returncode)
+        # catalogue error: a malformed line
+        badcat = os.path.join(td, "bad.txt")
+        with open(badcat, "w") as f:
+            f.write("# header\n1 20 30 4 5 6\n1 20 three 4 5 6\n")
+        r = subprocess.run([orc.REF_BIN, base, badcat, "none", os.path.join(td, "o.txt")], capture_output=True,
+                           text=True)
+        errs["catalogue_bad_line"] = dict(lines=lines, catalogue="# header\n1 20 30 4 5 6\n1 20 three 4 5 6\n",
+                                          stdout=r.stdout.replace(badcat, "{DATAFILE}"), returncode=r.returncode)
+        oobcat = os.path.join(td, "oob.txt")
+        with open(oobcat, "w") as f:
+            f.write("1 20 30 4 5 6\n2 21 31 0 0 0\n-7.5 22 33 1 1 1\n5000 20 20 0 0 0\n")
+        r = subprocess.run([orc.REF_BIN, base, oobcat, "none", os.path.join(td, "o.txt")], capture_output=True,
+                           text=True)
+        errs["catalogue_out_of_box"] = dict(lines=lines, catalogue="1 20 30 4 5 6\n2 21 31 0 0 0\n-7.5 22 33 1 1 1\n"
+                                            "5000 20 20 0 0 0\n", stdout=r.stdout.replace(oobcat, "{DATAFILE}"),
+                                            returncode=r.returncode)
+        r = subprocess.run([orc.REF_BIN, base], capture_output=True, text=True)
+        errs["usage"] = dict(stdout=r.stdout, returncode=r.returncode)
+        with open(os.path.join(HERE, "param_errors.json"), "w") as f:
+            json.dump(errs, f, indent=1)
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
+    print("wrote", len(CASES), "cases")
+
+
+def dataclass_dict(p):
+    import dataclasses
+
+    return dataclasses.asdict(p)
+
+
+if __name__ == "__main__":
+    main()
