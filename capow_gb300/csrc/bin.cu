@@ -250,173 +250,255 @@ __global__ void k_dc_prepare(const DevStats *st, int det, int nslot, int nfields
   }
 }
 
-// The fused bin kernel. grid: x = column blocks over the flattened (y, z) columns of the
-// half-complex grid, y = chunks of the x axis.
-template <typename R>
-__global__ void __launch_bounds__(256) k_bin(BinParams bp, BinTables t, const typename CT<R>::C *g0,
-                                             const typename CT<R>::C *g1, const typename CT<R>::C *g2,
-                                             const typename CT<R>::C *g3, const double *dcv, double *bins,
-                                             double *bins2d, int ichunk) {
+// Shared-memory carving of k_bin, used by the kernel and by its launcher. Every region starts
+// on a 16-byte boundary (double2 tables and double edges need 16 and 8).
+struct BinSmem {
+  unsigned sb, sb2, sE, sElo, sEhi, sfx2, scx, sex, sfl, total;
+};
+
+CAPOW_HD unsigned align16(unsigned x) { return (x + 15u) & ~15u; }
+
+CAPOW_HD BinSmem bin_smem_layout(unsigned rsize, int np, int nk, int n2d_sm, int ichunk) {
+  BinSmem L;
+  unsigned o = 0;
+  L.sb = o;   o = align16(o + rsize * np * 5 * nk);
+  L.sb2 = o;  o = align16(o + rsize * np * n2d_sm);
+  L.sE = o;   o = align16(o + 8u * (nk + 3));
+  L.sElo = o; o = align16(o + 4u * (nk + 3));
+  L.sEhi = o; o = align16(o + 4u * (nk + 3));
+  L.sfx2 = o; o = align16(o + rsize * ichunk);
+  L.scx = o;  o = align16(o + rsize * ichunk);
+  L.sex = o;  o = align16(o + 2u * rsize * ichunk);
+  L.sfl = o;  o = align16(o + rsize * ichunk);
+  L.total = o;
+  return L;
+}
+
+// The fused bin kernel. grid.x: blocks of flattened (y, z) columns of the half-complex grid;
+// grid.y: chunks of the x axis. Each thread walks x for one (y, z) column.
+//
+// NF = 1: one painted field (A, and A interlaced); product |A|^2.
+// NF = 2: fields A and B; products |A|^2, Re(A* B), Im(A* B), |B|^2 are all accumulated and
+//         each requested spectrum reads one of them (src/main.c:435-441).
+// ODD: also the odd multipoles (src/main.c:445-449). OUT2D: the (k, mu) histogram (:453-461).
+// All accumulator indexing is compile-time, so the per-thread sums live in registers.
+template <typename R, int NF, bool ODD, bool OUT2D>
+__global__ void __launch_bounds__(256) k_bin(BinParams bp, BinTables t, const typename CT<R>::C *gA,
+                                             const typename CT<R>::C *gB, const typename CT<R>::C *gAi,
+                                             const typename CT<R>::C *gBi, const double *dcv, double *bins,
+                                             double *bins2d, int ichunk, int sm2d) {
   typedef typename CT<R>::C C;
+  constexpr int NP = NF == 1 ? 1 : 4;
+  constexpr bool F32 = sizeof(R) == 4;
+  const int nk = bp.nk;
+  const int n2d = OUT2D ? nk * bp.nmu : 0;
   extern __shared__ __align__(16) unsigned char smraw[];
-  R *sb = (R *)smraw;                       // [nspec][5][NK]
-  R *sb2 = sb + bp.nspec * 5 * bp.nk;       // [nspec][NK*NMU] when out2d fits
-  const int nk = bp.nk, ns = bp.nspec, nf = bp.nfields;
-  const int n2d = bp.out2d ? nk * bp.nmu : 0;
-  const bool sm2d_fit = n2d * ns * sizeof(R) + 5 * nk * ns * sizeof(R) <= 96 * 1024;
-  for (int c = threadIdx.x; c < ns * (5 * nk + (sm2d_fit ? n2d : 0)); c += blockDim.x) sb[c] = (R)0;
+  // shared layout: bins [NP][5][nk] | 2-D bins [NP][n2d] | E (double, nk+3) | Elo, Ehi (float, nk+3)
+  //                | per-chunk x tables: fx2 (R), cx (R), ex (C), fl (R)
+  const BinSmem L = bin_smem_layout(sizeof(R), NP, nk, sm2d ? n2d : 0, ichunk);
+  R *sb = (R *)(smraw + L.sb);
+  R *sb2 = (R *)(smraw + L.sb2);
+  double *sE = (double *)(smraw + L.sE);
+  float *sElo = (float *)(smraw + L.sElo);
+  float *sEhi = (float *)(smraw + L.sEhi);
+  R *sfx2 = (R *)(smraw + L.sfx2);
+  R *scx = (R *)(smraw + L.scx);
+  C *sex = (C *)(smraw + L.sex);
+  R *sfl = (R *)(smraw + L.sfl);
+  const int i0 = blockIdx.y * ichunk, i1 = min(bp.nx, i0 + ichunk);
+  for (int c = threadIdx.x; c < NP * (5 * nk + (sm2d ? n2d : 0)); c += blockDim.x) sb[c] = (R)0;
+  for (int c = threadIdx.x; c < nk + 3; c += blockDim.x) {
+    sE[c] = t.E[c];
+    sElo[c] = t.Elo[c];
+    sEhi[c] = t.Ehi[c];
+  }
+  for (int c = threadIdx.x; c < i1 - i0; c += blockDim.x) {
+    const int i = i0 + c;
+    if (F32) {
+      sfx2[c] = (R)t.fx2f[i];
+      scx[c] = (R)t.cxf[i];
+      sex[c].x = (R)t.exf[i].x;
+      sex[c].y = (R)t.exf[i].y;
+      sfl[c] = (R)t.fxf[i];
+    } else {
+      sfx2[c] = (R)t.fx2d[i];
+      scx[c] = (R)t.cxd[i];
+      sex[c].x = (R)t.exd[i].x;
+      sex[c].y = (R)t.exd[i].y;
+      sfl[c] = (R)t.fxd[i];
+    }
+  }
   __syncthreads();
 
   const long long cols = (long long)bp.ny * bp.nzc;
   const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const int i0 = blockIdx.y * ichunk, i1 = min(bp.nx, i0 + ichunk);
   if (col < cols) {
     const int j = (int)(col / bp.nzc), k = (int)(col - (long long)j * bp.nzc);
-    const bool isf = sizeof(R) == 4;
     // per-column constants
-    const R syz = isf ? (R)(t.fy2f[j] + t.fz2f[k]) : (R)0;
-    R cyz = isf ? (R)(t.cyf[j] * t.czf[k]) : (R)(t.cyd[j] * t.czd[k]);
+    const R syz = F32 ? (R)(t.fy2f[j] + t.fz2f[k]) : (R)0;
+    const double fyz2d_y = t.fy2d[j], fyz2d_z = t.fz2d[k];
+    R cyz = F32 ? (R)(t.cyf[j] * t.czf[k]) : (R)(t.cyd[j] * t.czd[k]);
     if (bp.interlace) cyz *= (R)0.25;
     C eyz;
-    if (isf) {
-      float2 a = t.eyf[j], b = t.ezf[k];
+    if (F32) {
+      const float2 a = t.eyf[j], b = t.ezf[k];
       eyz.x = (R)(a.x * b.x - a.y * b.y);
       eyz.y = (R)(a.x * b.y + a.y * b.x);
     } else {
-      double2 a = t.eyd[j], b = t.ezd[k];
+      const double2 a = t.eyd[j], b = t.ezd[k];
       eyz.x = (R)(a.x * b.x - a.y * b.y);
       eyz.y = (R)(a.x * b.y + a.y * b.x);
     }
-    const R flos_yz = bp.los == 2 ? (isf ? (R)t.fyf[j] : (R)t.fyd[j]) : (isf ? (R)t.fzf[k] : (R)t.fzd[k]);
+    const R flos_yz = bp.los == 2 ? (F32 ? (R)t.fyf[j] : (R)t.fyd[j]) : (F32 ? (R)t.fzf[k] : (R)t.fzd[k]);
     const long long base = (long long)j * bp.nzc + k;
-    R acc[CAPOW_MAX_SPEC][5];
+    R acc[NP][5];
 #pragma unroll
-    for (int q = 0; q < CAPOW_MAX_SPEC; q++)
+    for (int q = 0; q < NP; q++)
 #pragma unroll
       for (int l = 0; l < 5; l++) acc[q][l] = (R)0;
     int cur = -1;
-    int guess = 0;
+    R lo = (R)1, hi = (R)0;  // current bin's safe interval in s (empty: search)
+    // modes of this column with |fx| beyond the top bin edge (or Nyquist) are never included:
+    // walk only i <= r and i >= NX - r (r rounded up; the exact test below decides each mode)
+    const float top = sElo[nk + 1] - (float)(F32 ? (float)syz : (float)(fyz2d_y + fyz2d_z));
+    const int r = top > 0.0f ? min(bp.xhalf, (int)(sqrtf(top) / bp.fx_step) + 1) : -1;
     for (int i = i0; i < i1; i++) {
-      // ---- bin of this mode
-      int b;
-      double sd = -1.0;
-      if (isf) {
-        const float s32 = t.fx2f[i] + (float)syz;
-        b = guess;
-        while (b < nk && s32 >= t.Elo[b + 2]) b++;
-        while (b > -1 && s32 < t.Ehi[b + 1]) b--;
-        // safe iff s32 lies inside [Elo[b+1], Ehi[b+2])
-        if (!(s32 >= t.Elo[b + 1] && s32 < t.Ehi[b + 2])) {
-          sd = exact_s(t, i, j, k);
-          b = exact_bin(t.E, nk, sd, b);
-        }
-      } else {
-        sd = exact_s(t, i, j, k);
-        b = exact_bin(t.E, nk, sd, guess);
+      if (i > r && i < bp.nx - r) {
+        i = bp.nx - r - 1;
+        continue;
       }
-      guess = b;
-      if (b < 0 || b >= nk) continue;
-      if (b != cur) {
-        if (cur >= 0) {
-          for (int q = 0; q < ns; q++)
-            for (int l = 0; l < 5; l++) {
-              if (acc[q][l] != (R)0) atomicAdd(&sb[(q * 5 + l) * nk + cur], acc[q][l]);
-              acc[q][l] = (R)0;
-            }
+      const int li = i - i0;
+      // ---- bin of this mode (src/main.c:355, 369-375)
+      R s;
+      if (F32) s = sfx2[li] + syz;
+      else s = (R)__dadd_rn(__dadd_rn((double)sfx2[li], fyz2d_y), fyz2d_z);
+      if (!(s >= lo && s < hi)) {
+        int b = cur < -1 ? -1 : cur;
+        if (F32) {
+          const float sf = (float)s;
+          while (b < nk && sf >= sElo[b + 2]) b++;
+          while (b > -1 && sf < sEhi[b + 1]) b--;
+          if (sf >= sElo[b + 1] && sf < sEhi[b + 2]) {
+            lo = (R)sElo[b + 1];
+            hi = (R)sEhi[b + 2];
+          } else {  // within a few ulps of an edge: the exact FP64 s decides
+            const double sd = __dadd_rn(__dadd_rn(t.fx2d[i], fyz2d_y), fyz2d_z);
+            b = exact_bin(sE, nk, sd, b);
+            lo = (R)1;
+            hi = (R)0;
+          }
+        } else {
+          b = exact_bin(sE, nk, (double)s, b);
+          lo = (R)sE[b + 1];
+          hi = (R)sE[b + 2];
         }
-        cur = b;
+        if (b != cur) {
+          if (cur >= 0 && cur < nk) {
+#pragma unroll
+            for (int q = 0; q < NP; q++)
+#pragma unroll
+              for (int l = 0; l < 5; l++) {
+                if ((l == 1 || l == 3) && !ODD) continue;
+                if (acc[q][l] != (R)0) atomicAdd(&sb[(q * 5 + l) * nk + cur], acc[q][l]);
+                acc[q][l] = (R)0;
+              }
+          }
+          cur = b;
+        }
       }
-      // ---- fields at this mode, interlacing combine (src/main.c:392-418)
+      if (cur < 0 || cur >= nk) continue;
+      // ---- fields and interlacing combine (src/main.c:392-418)
       const long long off = (long long)i * cols + base;
-      C F[2];
-      const C *gs[4] = {g0, g1, g2, g3};
-      C e;
-      if (isf) {
-        float2 ex = t.exf[i];
-        e.x = (R)ex.x * eyz.x - (R)ex.y * eyz.y;
-        e.y = (R)ex.x * eyz.y + (R)ex.y * eyz.x;
-      } else {
-        double2 ex = t.exd[i];
-        e.x = (R)ex.x * eyz.x - (R)ex.y * eyz.y;
-        e.y = (R)ex.x * eyz.y + (R)ex.y * eyz.x;
-      }
       const bool dc = (i == 0 && col == 0);
-      for (int f = 0; f < nf; f++) {
-        C a = gs[f][off];
-        if (dc) { a.x = (R)dcv[f]; a.y = (R)0; }
-        if (bp.interlace) {
-          C ai = gs[nf + f][off];
-          if (dc) { ai.x = (R)dcv[nf + f]; ai.y = (R)0; }
-          C r = cmul(ai, e);
-          a.x += r.x;
-          a.y += r.y;
+      C ex = sex[li], e;
+      e.x = ex.x * eyz.x - ex.y * eyz.y;
+      e.y = ex.x * eyz.y + ex.y * eyz.x;
+      C A = gA[off];
+      if (dc) { A.x = (R)dcv[0]; A.y = (R)0; }
+      C B;
+      if (NF == 2) {
+        B = gB[off];
+        if (dc) { B.x = (R)dcv[1]; B.y = (R)0; }
+      }
+      if (bp.interlace) {
+        C a = gAi[off];
+        if (dc) { a.x = (R)dcv[NF]; a.y = (R)0; }
+        A.x += a.x * e.x - a.y * e.y;
+        A.y += a.x * e.y + a.y * e.x;
+        if (NF == 2) {
+          C b2 = gBi[off];
+          if (dc) { b2.x = (R)dcv[NF + 1]; b2.y = (R)0; }
+          B.x += b2.x * e.x - b2.y * e.y;
+          B.y += b2.x * e.y + b2.y * e.x;
         }
-        F[f] = a;
       }
-      // ---- weights: deconvolution, Hermitian multiplicity, Legendre (src/main.c:382-389, 422-449)
-      const R cx = isf ? (R)t.cxf[i] : (R)t.cxd[i];
-      const R gc = cyz * cx * (R)herm_nm(i, j, k, bp.xhalf);
+      // ---- weights (src/main.c:382-389, 422-449)
+      const R gc = cyz * scx[li] * (R)herm_nm(i, j, k, bp.xhalf);
+      const R fl = bp.los == 1 ? sfl[li] : flos_yz;
       R mu;
-      const R fl = bp.los == 1 ? (isf ? (R)t.fxf[i] : (R)t.fxd[i]) : flos_yz;
-      if (isf) {
-        const float s32 = t.fx2f[i] + (float)syz;
-        mu = s32 > 0.0f ? (R)((float)fl * rsqrtf(s32)) : (R)0;
-      } else {
-        double sq = sqrt(sd);
-        mu = sq > 0.0 ? (R)(fl / sq) : (R)0;
-      }
+      if (F32) mu = s > (R)0 ? (R)((float)fl * rsqrtf((float)s)) : (R)0;
+      else mu = s > (R)0 ? (R)(fl / sqrt((double)s)) : (R)0;
       const R mu2 = mu * mu;
       const R L2 = (R)1.5 * mu2 - (R)0.5;
       const R L4 = ((R)4.375 * mu2 - (R)3.75) * mu2 + (R)0.375;
       const R L3 = ((R)2.5 * mu2 - (R)1.5) * mu;
-      for (int q = 0; q < ns; q++) {
-        const C X = F[bp.spec[q].x], Y = F[bp.spec[q].y];
-        R pw = bp.spec[q].imag ? (X.x * Y.y - X.y * Y.x) : (X.x * Y.x + X.y * Y.y);
-        pw *= gc;
-        acc[q][0] += pw;
-        acc[q][2] += pw * L2;
-        acc[q][4] += pw * L4;
-        if (bp.odd) {
-          acc[q][1] += pw * mu;
-          acc[q][3] += pw * L3;
+      R P[NP];
+      P[0] = (A.x * A.x + A.y * A.y) * gc;
+      if (NF == 2) {
+        P[1] = (A.x * B.x + A.y * B.y) * gc;
+        P[2] = (A.x * B.y - A.y * B.x) * gc;
+        P[3] = (B.x * B.x + B.y * B.y) * gc;
+      }
+#pragma unroll
+      for (int q = 0; q < NP; q++) {
+        acc[q][0] += P[q];
+        acc[q][2] += P[q] * L2;
+        acc[q][4] += P[q] * L4;
+        if (ODD) {
+          acc[q][1] += P[q] * mu;
+          acc[q][3] += P[q] * L3;
         }
-        if (bp.out2d) {
-          int mb;
-          const R tq = (mu + (R)1) * (R)0.5 * (R)bp.nmu;
-          const R fr = tq - floor(tq);
-          if (isf && (fr < (R)1e-4 || fr > (R)(1 - 1e-4))) {
-            if (sd < 0) sd = exact_s(t, i, j, k);
-            mb = exact_mubin(bp, t, i, j, k, sd);
-          } else if (!isf) {
-            mb = exact_mubin(bp, t, i, j, k, sd);
-          } else {
-            mb = (int)tq;
-            if (mb >= bp.nmu) mb = bp.nmu - 1;
-          }
-          const int bin = b * bp.nmu + mb;
-          if (bin >= 0 && bin < n2d) {
-            if (sm2d_fit)
-              atomicAdd(&sb2[q * n2d + bin], pw);
-            else
-              atomicAdd(&bins2d[q * n2d + bin], (double)pw);
+      }
+      if (OUT2D) {
+        int mb;
+        const R tq = (mu + (R)1) * (R)0.5 * (R)bp.nmu;
+        const R fr = tq - floor(tq);
+        if (!F32 || fr < (R)1e-4 || fr > (R)(1 - 1e-4)) {
+          const double sd = __dadd_rn(__dadd_rn(t.fx2d[i], fyz2d_y), fyz2d_z);
+          mb = exact_mubin(bp, t, i, j, k, sd);
+        } else {
+          mb = (int)tq;
+          if (mb >= bp.nmu) mb = bp.nmu - 1;
+        }
+        const int bin = cur * bp.nmu + mb;
+        if (bin >= 0 && bin < n2d) {
+#pragma unroll
+          for (int q = 0; q < NP; q++) {
+            if (sm2d) atomicAdd(&sb2[q * n2d + bin], P[q]);
+            else atomicAdd(&bins2d[q * n2d + bin], (double)P[q]);
           }
         }
       }
     }
-    if (cur >= 0)
-      for (int q = 0; q < ns; q++)
-        for (int l = 0; l < 5; l++)
+    if (cur >= 0 && cur < nk) {
+#pragma unroll
+      for (int q = 0; q < NP; q++)
+#pragma unroll
+        for (int l = 0; l < 5; l++) {
+          if ((l == 1 || l == 3) && !ODD) continue;
           if (acc[q][l] != (R)0) atomicAdd(&sb[(q * 5 + l) * nk + cur], acc[q][l]);
+        }
+    }
   }
   __syncthreads();
-  const bool sm2d = n2d * ns * sizeof(R) + 5 * nk * ns * sizeof(R) <= 96 * 1024;
-  for (int c = threadIdx.x; c < ns * 5 * nk; c += blockDim.x) {
-    R v = sb[c];
+  // CTA bins -> global FP64 bins, laid out [product][5][nk]
+  for (int c = threadIdx.x; c < NP * 5 * nk; c += blockDim.x) {
+    const R v = sb[c];
     if (v != (R)0) atomicAdd(&bins[c], (double)v);
   }
-  if (bp.out2d && sm2d)
-    for (int c = 0 + threadIdx.x; c < ns * n2d; c += blockDim.x) {
-      R v = sb2[c];
+  if (OUT2D && sm2d)
+    for (int c = threadIdx.x; c < NP * n2d; c += blockDim.x) {
+      const R v = sb2[c];
       if (v != (R)0) atomicAdd(&bins2d[c], (double)v);
     }
 }
@@ -435,34 +517,54 @@ void launch_dc_prepare(cudaStream_t s, const void *st, int deterministic, int ns
   (*launches)++;
 }
 
-void launch_bin(cudaStream_t s, int precision, const BinParams &bp, const BinTables &t, void *const slots[4],
-                const double *dcv, double *bins, double *bins2d, long long *launches) {
+int bin_products(int nfields) { return nfields == 1 ? 1 : 4; }
+
+template <typename R, int NF, bool ODD, bool OUT2D>
+static void launch_bin_t(cudaStream_t s, const BinParams &bp, const BinTables &t, void *const slots[4],
+                         const double *dcv, double *bins, double *bins2d) {
+  typedef typename CT<R>::C C;
+  constexpr int NP = NF == 1 ? 1 : 4;
   const long long cols = (long long)bp.ny * bp.nzc;
   const int th = 256;
   const int nbx = (int)((cols + th - 1) / th);
-  // enough CTAs to fill the GPU several times over, each thread walking a chunk of x
   int nchunk = (152 * 8 + nbx - 1) / nbx;
   if (nchunk < 1) nchunk = 1;
   if (nchunk > bp.nx) nchunk = bp.nx;
   const int ichunk = (bp.nx + nchunk - 1) / nchunk;
   nchunk = (bp.nx + ichunk - 1) / ichunk;
-  dim3 grid(nbx, nchunk);
-  const int n2d = bp.out2d ? bp.nk * bp.nmu : 0;
-  if (precision == CAPOW_FP64) {
-    size_t eb = sizeof(double);
-    bool sm2d = n2d * bp.nspec * eb + 5 * bp.nk * bp.nspec * eb <= 96 * 1024;
-    size_t smem = eb * bp.nspec * (5 * bp.nk + (sm2d ? n2d : 0));
-    cudaFuncSetAttribute(k_bin<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_bin<double><<<grid, th, smem, s>>>(bp, t, (const double2 *)slots[0], (const double2 *)slots[1],
-                                         (const double2 *)slots[2], (const double2 *)slots[3], dcv, bins, bins2d,
-                                         ichunk);
+  const int n2d = OUT2D ? bp.nk * bp.nmu : 0;
+  const int sm2d = (size_t)(NP * n2d) * sizeof(R) <= 64 * 1024 ? 1 : 0;
+  const size_t smem = bin_smem_layout(sizeof(R), NP, bp.nk, sm2d ? n2d : 0, ichunk).total;
+  cudaFuncSetAttribute(k_bin<R, NF, ODD, OUT2D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // slot order: stencil * nfields + field
+  const C *gA = (const C *)slots[0];
+  const C *gB = NF == 2 ? (const C *)slots[1] : nullptr;
+  const C *gAi = bp.interlace ? (const C *)slots[NF] : nullptr;
+  const C *gBi = (bp.interlace && NF == 2) ? (const C *)slots[NF + 1] : nullptr;
+  k_bin<R, NF, ODD, OUT2D><<<dim3(nbx, nchunk), th, smem, s>>>(bp, t, gA, gB, gAi, gBi, dcv, bins, bins2d, ichunk,
+                                                                sm2d);
+}
+
+template <typename R, int NF>
+static void launch_bin_r(cudaStream_t s, const BinParams &bp, const BinTables &t, void *const slots[4],
+                         const double *dcv, double *bins, double *bins2d) {
+  if (bp.odd) {
+    if (bp.out2d) launch_bin_t<R, NF, true, true>(s, bp, t, slots, dcv, bins, bins2d);
+    else launch_bin_t<R, NF, true, false>(s, bp, t, slots, dcv, bins, bins2d);
   } else {
-    size_t eb = sizeof(float);
-    bool sm2d = n2d * bp.nspec * eb + 5 * bp.nk * bp.nspec * eb <= 96 * 1024;
-    size_t smem = eb * bp.nspec * (5 * bp.nk + (sm2d ? n2d : 0));
-    cudaFuncSetAttribute(k_bin<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_bin<float><<<grid, th, smem, s>>>(bp, t, (const float2 *)slots[0], (const float2 *)slots[1],
-                                        (const float2 *)slots[2], (const float2 *)slots[3], dcv, bins, bins2d, ichunk);
+    if (bp.out2d) launch_bin_t<R, NF, false, true>(s, bp, t, slots, dcv, bins, bins2d);
+    else launch_bin_t<R, NF, false, false>(s, bp, t, slots, dcv, bins, bins2d);
+  }
+}
+
+void launch_bin(cudaStream_t s, int precision, const BinParams &bp, const BinTables &t, void *const slots[4],
+                const double *dcv, double *bins, double *bins2d, long long *launches) {
+  if (precision == CAPOW_FP64) {
+    if (bp.nfields == 1) launch_bin_r<double, 1>(s, bp, t, slots, dcv, bins, bins2d);
+    else launch_bin_r<double, 2>(s, bp, t, slots, dcv, bins, bins2d);
+  } else {
+    if (bp.nfields == 1) launch_bin_r<float, 1>(s, bp, t, slots, dcv, bins, bins2d);
+    else launch_bin_r<float, 2>(s, bp, t, slots, dcv, bins, bins2d);
   }
   (*launches)++;
 }

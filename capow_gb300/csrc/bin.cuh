@@ -37,6 +37,7 @@ struct BinParams {
   SpecDef spec[CAPOW_MAX_SPEC];
   int mean_sub_a;           // field A had the mean subtracted (DC correction)
   double two_pi;
+  float fx_step;            // x frequency spacing 1/((float)NX*dx) (src/main.c:329), for per-column x ranges
 };
 
 // Host: exact k-bin of one |k|^2 value s, following src/main.c:355, 369-375.
@@ -52,6 +53,8 @@ void launch_mode_counts(cudaStream_t s, const BinParams &bp, const BinTables &t,
                         unsigned long long *nmodes2d, long long *launches);
 void launch_bin(cudaStream_t s, int precision, const BinParams &bp, const BinTables &t, void *const slots[4],
                 const double *dcv, double *bins, double *bins2d, long long *launches);
+// products accumulated by the bin kernel: 1 for one field, 4 (|A|^2, Re A*B, Im A*B, |B|^2) for two
+int bin_products(int nfields);
 // DC corrections: dcv[slot] = painted sum (minus NGRID for mean-subtracted field A slots)
 void launch_dc_prepare(cudaStream_t s, const void *st, int deterministic, int nslot, int nfields, int mean_sub_a,
                        const double *fixed_scale, double *dcv, long long *launches);

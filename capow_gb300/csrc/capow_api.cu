@@ -13,6 +13,8 @@
 #include "bin.cuh"
 #include "paint.cuh"
 
+#define NPROD 4  // bin products when two fields are painted
+
 struct capow_ctx {
   capow_params p;
   capow_options o;
@@ -251,13 +253,13 @@ extern "C" int capow_create(const capow_params *p, const capow_options *opt, cap
   c->dcv = (double *)dalloc(c, sizeof(double) * 4);
   c->fixed_scale = (double *)dalloc(c, sizeof(double) * 2);
   const int nk = p->NK, n2d = p->Output2D ? p->NK * p->NMU : 0;
-  c->bins = (double *)dalloc(c, sizeof(double) * CAPOW_MAX_SPEC * 5 * nk);
-  c->bins2d = (double *)dalloc(c, sizeof(double) * CAPOW_MAX_SPEC * (n2d ? n2d : 1));
+  c->bins = (double *)dalloc(c, sizeof(double) * NPROD * 5 * nk);
+  c->bins2d = (double *)dalloc(c, sizeof(double) * NPROD * (n2d ? n2d : 1));
   c->nmodes_d = (unsigned long long *)dalloc(c, sizeof(unsigned long long) * nk);
   c->nmodes2d_d = (unsigned long long *)dalloc(c, sizeof(unsigned long long) * (n2d ? n2d : 1));
   if (!c->grid_base || !c->st || !c->dcv || !c->bins || !c->bins2d || !c->nmodes_d || !c->nmodes2d_d)
     FAIL(c, CAPOW_ENOMEM, "device allocation failed (grids need %.2f GB)", eb * c->grid_elems * c->nslot / 1e9);
-  CK(c, cudaMallocHost((void **)&c->h_bins, sizeof(double) * CAPOW_MAX_SPEC * (5 * nk + n2d)));
+  CK(c, cudaMallocHost((void **)&c->h_bins, sizeof(double) * NPROD * (5 * nk + n2d)));
   CK(c, cudaMallocHost((void **)&c->h_st, sizeof(DevStats)));
   if (!f64) {
     c->tg = choose_tiles(c->g, c->nslot, c->prec == CAPOW_FP32_DETERMINISTIC);
@@ -273,6 +275,7 @@ extern "C" int capow_create(const capow_params *p, const capow_options *opt, cap
   bp.nk = nk; bp.nmu = p->NMU; bp.los = p->LOS; bp.interlace = p->DoInterlacing;
   bp.odd = p->Odd_Multipoles; bp.out2d = p->Output2D; bp.nfields = c->fs.nfields;
   bp.two_pi = 2.0 * M_PI;
+  bp.fx_step = (float)(1.0 / ((float)p->NX * c->g.dx));
   if (build_bin_tables(*p, c->g, c->prec, c->bt, c->allocs, c->stream)) FAIL(c, CAPOW_ENOMEM, "bin tables");
   CK(c, cudaMemsetAsync(c->nmodes_d, 0, sizeof(unsigned long long) * nk, c->stream));
   CK(c, cudaMemsetAsync(c->nmodes2d_d, 0, sizeof(unsigned long long) * (n2d ? n2d : 1), c->stream));
@@ -363,12 +366,13 @@ static int enqueue_paint(capow_ctx *c, const capow_particles &d) {
     CK(c, cudaMemsetAsync(c->grid_base, 0, 8 * c->grid_elems * c->nslot, c->stream));
     launch_paint64(c->stream, c->g, c->fs, d.dtype, d.x, d.y, d.z, d.vlos, d.w, n, gp, c->st, &c->launches);
   } else {
-    if (c->pb.special_n < (unsigned long long)n + 1) {
-      if (c->pb.special) cudaFree(c->pb.special);
-      c->pb.special = nullptr;
-      c->pb.special_n = 0;
-      CK(c, cudaMalloc(&c->pb.special, sizeof(unsigned) * (n + 1)));
-      c->pb.special_n = n + 1;
+    if (!c->pb.edge_count) CK(c, cudaMalloc(&c->pb.edge_count, sizeof(unsigned)));
+    if (c->pb.edge_cap < (unsigned long long)n + 1) {  // every particle could sit on an edge
+      if (c->pb.edge_list) cudaFree(c->pb.edge_list);
+      c->pb.edge_list = nullptr;
+      c->pb.edge_cap = 0;
+      CK(c, cudaMalloc(&c->pb.edge_list, sizeof(unsigned) * (n + 1)));
+      c->pb.edge_cap = n + 1;
     }
     unsigned long long want = (unsigned long long)(tile_dup_estimate(c->g, c->tg) * 1.25 * n) + 65536;
     if (c->pb.capacity < want / 2 || (d.w && !c->pb.recw)) {
@@ -479,19 +483,19 @@ static int enqueue_power(capow_ctx *c) {
   }
   CK(c, cudaEventRecord(c->ev[2], c->stream));
   const int nk = c->p.NK, n2d = c->p.Output2D ? c->p.NK * c->p.NMU : 0;
-  CK(c, cudaMemsetAsync(c->bins, 0, sizeof(double) * CAPOW_MAX_SPEC * 5 * nk, c->stream));
-  if (n2d) CK(c, cudaMemsetAsync(c->bins2d, 0, sizeof(double) * CAPOW_MAX_SPEC * n2d, c->stream));
+  CK(c, cudaMemsetAsync(c->bins, 0, sizeof(double) * NPROD * 5 * nk, c->stream));
+  if (n2d) CK(c, cudaMemsetAsync(c->bins2d, 0, sizeof(double) * NPROD * n2d, c->stream));
   void *slots[4];
   GridPtrs gp = grid_ptrs(c);
   for (int k = 0; k < 4; k++) slots[k] = gp.g[k];
   launch_bin(c->stream, c->prec, c->bp, c->bt, slots, c->dcv, c->bins, n2d ? c->bins2d : nullptr, &c->launches);
   CK(c, cudaGetLastError());
   CK(c, cudaEventRecord(c->ev[3], c->stream));
-  CK(c, cudaMemcpyAsync(c->h_bins, c->bins, sizeof(double) * c->bp.nspec * 5 * nk, cudaMemcpyDeviceToHost,
-                        c->stream));
+  const int np = bin_products(c->fs.nfields);
+  CK(c, cudaMemcpyAsync(c->h_bins, c->bins, sizeof(double) * np * 5 * nk, cudaMemcpyDeviceToHost, c->stream));
   if (n2d)
-    CK(c, cudaMemcpyAsync(c->h_bins + CAPOW_MAX_SPEC * 5 * nk, c->bins2d, sizeof(double) * c->bp.nspec * n2d,
-                          cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaMemcpyAsync(c->h_bins + NPROD * 5 * nk, c->bins2d, sizeof(double) * np * n2d, cudaMemcpyDeviceToHost,
+                          c->stream));
   CK(c, cudaMemcpyAsync(c->h_st, c->st, sizeof(DevStats), cudaMemcpyDeviceToHost, c->stream));
   return CAPOW_OK;
 }
@@ -536,6 +540,9 @@ extern "C" int capow_power(capow_ctx *c, capow_spectrum *out, int nout) {
   for (int q = 0; q < c->bp.nspec; q++) {
     capow_spectrum &s = out[q];
     const int m = c->shot_moment[q];
+    // product of this spectrum in the kernel's [product][5][NK] bins: |A|^2, Re(A*B), Im(A*B), |B|^2
+    const SpecDef &sd = c->bp.spec[q];
+    const int pq = c->fs.nfields == 1 ? 0 : (sd.x == sd.y ? (sd.x == 0 ? 0 : 3) : (sd.imag ? 2 : 1));
     s.shot = m == 0 ? N : vr[m] * N;
     s.norm = norm;
     s.alpha = alpha;
@@ -547,11 +554,11 @@ extern "C" int capow_power(capow_ctx *c, capow_spectrum *out, int nout) {
         memset(s.pk[l], 0, sizeof(double) * nk);
         continue;
       }
-      memcpy(s.pk[l], c->h_bins + (q * 5 + l) * nk, sizeof(double) * nk);
+      memcpy(s.pk[l], c->h_bins + (pq * 5 + l) * nk, sizeof(double) * nk);
     }
     if (s.nmodes)
       for (int b = 0; b < nk; b++) s.nmodes[b] = (int64_t)c->nmodes[b];
-    if (n2d && s.pk2d) memcpy(s.pk2d, c->h_bins + CAPOW_MAX_SPEC * 5 * nk + q * n2d, sizeof(double) * n2d);
+    if (n2d && s.pk2d) memcpy(s.pk2d, c->h_bins + NPROD * 5 * nk + pq * n2d, sizeof(double) * n2d);
     if (n2d && s.nmodes2d)
       for (int b = 0; b < n2d; b++) s.nmodes2d[b] = (int64_t)c->nmodes2d[b];
   }
@@ -621,7 +628,8 @@ extern "C" void capow_destroy(capow_ctx *c) {
     if (c->stage[k]) cudaFree(c->stage[k]);
   if (c->pb.recs) cudaFree(c->pb.recs);
   if (c->pb.recw) cudaFree(c->pb.recw);
-  if (c->pb.special) cudaFree(c->pb.special);
+  if (c->pb.edge_list) cudaFree(c->pb.edge_list);
+  if (c->pb.edge_count) cudaFree(c->pb.edge_count);
   if (c->h_bins) cudaFreeHost(c->h_bins);
   if (c->h_st) cudaFreeHost(c->h_st);
   for (int k = 0; k < 4; k++)

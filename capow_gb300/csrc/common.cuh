@@ -285,18 +285,6 @@ CAPOW_HD void axis32(int order, float s, int kind, int n, int los, AxisTapsF &t)
   else ngp_axis32(s, n, los, t);
 }
 
-// Distance test against every point where the reference's deposit changes discontinuously
-// for this axis (acceptance bounds 0, N, N+1; the TSC low-tap drop at 0.5; the TSC LOS==0
-// x shift at 1; every integer for NN). Conservative: a particle near any of them is painted
-// by the exact FP64 rules instead.
-CAPOW_HD bool near_edge(float s, int n, int order, float m) {
-  float nf = (float)n;
-  bool e = (fabsf(s) < m) || (fabsf(s - 0.5f) < m) || (fabsf(s - 1.0f) < m) || (fabsf(s - nf) < m) ||
-           (fabsf(s - nf - 1.0f) < m) || (s < 0.0f) || (s > nf + 1.0f);
-  if (order == 1) e = e || (fabsf(s - rintf(s)) < m);
-  return e;
-}
-
 // accepted? (FP32, non-edge particles only). s* are the normal-stencil scales after the RSD shift.
 CAPOW_HD bool accept32(const Geom &g, float sx, float sy, float sz) {
   const float nx = (float)g.nx, ny = (float)g.ny, nz = (float)g.nz;

@@ -158,12 +158,12 @@ void launch_paint64(cudaStream_t s, const Geom &g, const FieldSpec &fs, int dtyp
 }
 
 // ===================================================================================== FP32 path
-// Normal-stencil scales of one particle after the RSD shift, in FP32, and whether it must take
-// the exact rules. Explicit round-to-nearest intrinsics keep the result identical in every
-// kernel that recomputes it (count, scatter and tile kernels must agree on the tap set).
+// Normal-stencil scales of one particle after the RSD shift, in FP32. Explicit round-to-nearest
+// intrinsics keep the result identical in every kernel that recomputes it (the count, scatter
+// and tile kernels must agree on each particle's tiles).
 struct Prep {
   float sx, sy, sz, v, w;
-  bool edge;
+  bool fin;
 };
 
 template <typename T>
@@ -178,67 +178,107 @@ __device__ __forceinline__ Prep prep32(const Geom &g, const FieldSpec &fs, const
   p.sx = __fmul_rn(__fsub_rn(x, g.xmin_f), g.idx_f);
   p.sy = __fmul_rn(__fsub_rn(y, g.ymin_f), g.idy_f);
   p.sz = __fmul_rn(__fsub_rn(z, g.zmin_f), g.idz_f);
-  bool fin = isfinite(p.sx) && isfinite(p.sy) && isfinite(p.sz) && isfinite(p.v) && isfinite(p.w);
-  bool e = !fin || near_edge(p.sx, g.nx, g.order, g.margin) || near_edge(p.sy, g.ny, g.order, g.margin) ||
-           near_edge(p.sz, g.nz, g.order, g.margin);
-  if (g.interlace)
-    e = e || near_edge(__fadd_rn(p.sx, 0.5f), g.nx, g.order, g.margin) ||
-        near_edge(__fadd_rn(p.sy, 0.5f), g.ny, g.order, g.margin) ||
-        near_edge(__fadd_rn(p.sz, 0.5f), g.nz, g.order, g.margin);
-  p.edge = e;
+  p.fin = isfinite(p.sx) && isfinite(p.sy) && isfinite(p.sz) && isfinite(p.v) && isfinite(p.w);
   return p;
 }
 
+// A particle within the FP32 error margin of a point where the reference's deposit changes
+// discontinuously (box faces 0 and N, anything outside [0, N], the TSC low-tap drop at 0.5, the
+// TSC LOS==0 x shift at 1, every cell edge for NN) is painted by the exact FP64 rules.
+__device__ __forceinline__ bool edge1(float s, int n, int order, float m) {
+  const float nf = (float)n;
+  bool e = !(s >= m && s <= nf - m) || (fabsf(s - 0.5f) < m) || (fabsf(s - 1.0f) < m);
+  if (order == 1) e = e || (fabsf(s - rintf(s)) < m);
+  return e;
+}
+
+__device__ __forceinline__ bool is_edge(const Geom &g, float sx, float sy, float sz) {
+  bool e = edge1(sx, g.nx, g.order, g.margin) || edge1(sy, g.ny, g.order, g.margin) ||
+           edge1(sz, g.nz, g.order, g.margin);
+  if (g.interlace)
+    e = e || edge1(__fadd_rn(sx, 0.5f), g.nx, g.order, g.margin) ||
+        edge1(__fadd_rn(sy, 0.5f), g.ny, g.order, g.margin) || edge1(__fadd_rn(sz, 0.5f), g.nz, g.order, g.margin);
+  return e;
+}
+
+// Distinct tile coordinates along one axis, in registers (at most three: a footprint spans at
+// most six cells and tiles are at least four cells long, except a short partial last tile).
 struct AxisTiles {
-  int n;
-  int t[4];
+  int t0, t1, t2, n;
 };
 
 __device__ __forceinline__ void add_tile(AxisTiles &a, int v) {
-  for (int k = 0; k < a.n; k++)
-    if (a.t[k] == v) return;
-  if (a.n < 4) a.t[a.n++] = v;
+  if ((a.n > 0 && v == a.t0) || (a.n > 1 && v == a.t1) || (a.n > 2 && v == a.t2)) return;
+  if (a.n == 0) a.t0 = v;
+  else if (a.n == 1) a.t1 = v;
+  else a.t2 = v;
+  a.n = a.n < 3 ? a.n + 1 : 3;
 }
 
-// Per-axis tile coordinates touched by the accepted stencils of a regular particle.
-__device__ __forceinline__ int regular_tiles(const Geom &g, const TileGeo &tg, float sx, float sy, float sz,
-                                             AxisTiles &TX, AxisTiles &TY, AxisTiles &TZ) {
-  TX.n = TY.n = TZ.n = 0;
-  const int nst = g.interlace ? 2 : 1;
-  for (int stn = 0; stn < nst; stn++) {
-    float ax = stn ? __fadd_rn(sx, 0.5f) : sx, ay = stn ? __fadd_rn(sy, 0.5f) : sy, az = stn ? __fadd_rn(sz, 0.5f) : sz;
-    if (!accept32(g, ax, ay, az)) continue;
-    AxisTapsF tx, ty, tz;
-    axis32(g.order, ax, 0, g.nx, g.los, tx);
-    axis32(g.order, ay, 1, g.ny, g.los, ty);
-    axis32(g.order, az, 1, g.nz, g.los, tz);
-    for (int k = 0; k < 3; k++) {
-      if (tx.idx[k] >= 0 && tx.idx[k] < g.nx) add_tile(TX, tx.idx[k] / tg.tx);
-      if (ty.idx[k] >= 0 && ty.idx[k] < g.ny) add_tile(TY, ty.idx[k] / tg.ty);
-      if (tz.idx[k] >= 0 && tz.idx[k] < g.nz) add_tile(TZ, tz.idx[k] / tg.tz);
-    }
-  }
-  return TX.n * TY.n * TZ.n;
-}
+__device__ __forceinline__ int tile_at(const AxisTiles &a, int k) { return k == 0 ? a.t0 : (k == 1 ? a.t1 : a.t2); }
 
 __device__ __forceinline__ int tile_id(const TileGeo &tg, int bx, int by, int bz) {
   return (bx * tg.nby + by) * tg.nbz + bz;
 }
 
-// Warp-aggregated atomic add of 1 to counter[key] for active lanes; returns each lane's slot.
-__device__ __forceinline__ unsigned agg_inc(unsigned *counter, int key, bool active) {
-  const unsigned lane = threadIdx.x & 31;
-  unsigned amask = __ballot_sync(FULL_MASK, active);
-  unsigned res = 0;
-  if (active) {
-    unsigned peers = __match_any_sync(amask, key);
-    int leader = __ffs(peers) - 1;
-    unsigned base = 0;
-    if ((int)lane == leader) base = atomicAdd(counter + key, (unsigned)__popc(peers));
-    base = __shfl_sync(peers, base, leader);
-    res = base + __popc(peers & ((1u << lane) - 1));
+// Cells any accepted stencil (normal and interlaced) of a particle at scale s can write along one
+// axis, widened by the FP32 margin: [floor(s-m)-1, floor(s+m)+2] for TSC, [floor(s-m), floor(s+m)+2]
+// for CIC, [floor(s-m), floor(s+m)+1] for NN. Wrapping axes (LOS == 0: periodic y, z and the x halo
+// fold) take the cells modulo N; other axes clip to the grid. Returns false when nothing of the
+// footprint lies in the grid (the particle is outside the box and rejected).
+__device__ __forceinline__ bool axis_range(float s, int n, bool wrap, int order, float m, int &lo, int &hi) {
+  if (!(s > -4.0f && s < (float)n + 4.0f)) return false;
+  lo = __float2int_rd(__fsub_rn(s, m)) - (order == 3 ? 1 : 0);
+  hi = __float2int_rd(__fadd_rn(s, m)) + (order == 1 ? 1 : 2);
+  if (!wrap) {
+    lo = lo < 0 ? 0 : lo;
+    hi = hi > n - 1 ? n - 1 : hi;
+    return lo <= hi;
   }
-  return res;
+  const int span = hi - lo;
+  while (lo < 0) lo += n;
+  while (lo >= n) lo -= n;
+  hi = lo + span;  // cells beyond n - 1 wrap when used
+  return true;
+}
+
+__device__ __forceinline__ bool axis_footprint(float s, int n, int shift, bool wrap, int order, float m,
+                                               AxisTiles &T) {
+  T.n = 0;
+  T.t0 = T.t1 = T.t2 = 0;
+  int lo, hi;
+  if (!axis_range(s, n, wrap, order, m, lo, hi)) return false;
+  for (int c = lo; c <= hi; c++) {
+    int cc = c;
+    while (cc >= n) cc -= n;
+    add_tile(T, cc >> shift);
+  }
+  return true;
+}
+
+// All tiles of a particle. The first tile of each axis list gives the particle's home tile (the one
+// tile that counts it in the statistics).
+__device__ __forceinline__ bool footprint(const Geom &g, const TileGeo &tg, float sx, float sy, float sz,
+                                          AxisTiles &TX, AxisTiles &TY, AxisTiles &TZ) {
+  const bool wrap = g.los == 0;
+  if (!axis_footprint(sx, g.nx, tg.lx, wrap, g.order, g.margin, TX)) return false;
+  if (!axis_footprint(sy, g.ny, tg.ly, wrap, g.order, g.margin, TY)) return false;
+  if (!axis_footprint(sz, g.nz, tg.lz, wrap, g.order, g.margin, TZ)) return false;
+  // CIC rounding edge: a y index equal to NY makes the reference's linear index land in row 0 of
+  // the next x slice (src/read_data.c:592-593); that row's tile joins the list.
+  if (g.order == 2 && sy > (float)g.ny - 1.5f - g.margin) add_tile(TY, 0);
+  return true;
+}
+
+// The home tile without building the lists: the tile of the first cell of each axis range
+// (the same tile footprint() puts first). Returns -1 when the footprint misses the grid.
+__device__ __forceinline__ int home_of(const Geom &g, const TileGeo &tg, float sx, float sy, float sz) {
+  const bool wrap = g.los == 0;
+  int lx, hx, ly, hy, lz, hz;
+  if (!axis_range(sx, g.nx, wrap, g.order, g.margin, lx, hx)) return -1;
+  if (!axis_range(sy, g.ny, wrap, g.order, g.margin, ly, hy)) return -1;
+  if (!axis_range(sz, g.nz, wrap, g.order, g.margin, lz, hz)) return -1;
+  return tile_id(tg, lx >> tg.lx, ly >> tg.ly, lz >> tg.lz);
 }
 
 // Exact FP64 view of one particle (RSD shift in the reference's order).
@@ -263,139 +303,57 @@ __device__ __forceinline__ void decode(const Geom &g, long long L, int &ix, int 
   iz = (int)(r - (long long)iy * g.row);
 }
 
-// Tiles touched by the exact taps of an edge particle (both stencils), deduplicated.
-// Returns the count; writes at most `cap` ids.
-template <int CAP>
-__device__ int exact_tiles(const Geom &g, const TileGeo &tg, double x, double y, double z, int (&ids)[CAP]) {
-  int n = 0;
-  for (int stn = 0; stn < (g.interlace ? 2 : 1); stn++) {
-    AxisTaps ax, ay, az;
-    double px = stn ? DADD(x, g.hx) : x, py = stn ? DADD(y, g.hy) : y, pz = stn ? DADD(z, g.hz) : z;
-    if (!exact_axes(g, px, py, pz, ax, ay, az)) continue;
-    for (int c = 0; c < az.n; c++)
-      for (int b = 0; b < ay.n; b++)
-        for (int a = 0; a < ax.n; a++) {
-          if (!(ax.on[a] && ay.on[b] && az.on[c])) continue;
-          long long L = canon_index(g, ax.idx[a], ay.idx[b], az.idx[c]);
-          if (L < 0) continue;
-          int ix, iy, iz;
-          decode(g, L, ix, iy, iz);
-          int t = tile_id(tg, ix / tg.tx, iy / tg.ty, iz / tg.tz);
-          bool seen = false;
-          for (int k = 0; k < n; k++) seen |= (ids[k] == t);
-          if (!seen && n < CAP) ids[n++] = t;
-        }
-  }
-  return n;
-}
-
-// Pass 1: statistics, tile counts for regular particles, list of edge particles.
+// Pass 1: tile counts; statistics that need no exact decision (reads, velocity moments, the
+// fixed-point bound); particles whose footprint misses the grid (outside the box, rejected).
 template <typename T>
 __global__ void __launch_bounds__(256) k_count(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in, long long n,
-                                               unsigned *counts, unsigned *special, DevStats *st) {
-  float f_read = 0, f_out = 0, f_grid = 0, f_nsq = 0, f_v[4] = {0, 0, 0, 0}, f_abs[2] = {0, 0};
-  double d_grid = 0, d_out = 0, d_nsq = 0, d_v[4] = {0, 0, 0, 0};
+                                               unsigned *counts, DevStats *st, int split_edge) {
+  float f_read = 0, f_out = 0, f_nsq = 0, f_v[4] = {0, 0, 0, 0}, f_abs[2] = {0, 0};
   int fatal = 0, nonfin = 0;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  const long long nround = (n + stride - 1) / stride * stride;  // warp-uniform trip count
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nround; i += stride) {
-    const bool live = i < n;
-    bool reg = false;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const Prep p = prep32(g, fs, in, i);
+    if (!p.fin) {
+      nonfin = 1;
+      continue;
+    }
+    f_read += 1.0f;
+    if (fs.moments) {  // src/read_data.c:132-138, every particle read
+      f_nsq += p.w;
+      float wv = p.w * p.v;
+      f_v[0] += wv; wv *= p.v;
+      f_v[1] += wv; wv *= p.v;
+      f_v[2] += wv; wv *= p.v;
+      f_v[3] += wv;
+    }
+    float pa = p.w, pb = p.w;
+    for (int e = 0; e < fs.ea; e++) pa *= p.v;
+    for (int e = 0; e < fs.eb; e++) pb *= p.v;
+    f_abs[0] += fabsf(pa);
+    f_abs[1] += fabsf(pb);
     AxisTiles TX, TY, TZ;
-    int ntile = 0;
-    if (live) {
-      Prep p = prep32(g, fs, in, i);
-      if (p.edge) {
-        unsigned slot = atomicAdd(&st->nspecial, 1u);
-        special[slot] = (unsigned)i;
-        double x, y, z, v, w;
-        exact_pos(g, fs, in, i, x, y, z, v, w);
-        if (!(isfinite(x) && isfinite(y) && isfinite(z) && isfinite(v) && isfinite(w))) {
-          nonfin = 1;
-        } else {
-          f_read += 1.0f;
-          bool out = outside_box(g, x, y, z);
-          if (out && g.los == 0) {
-            fatal = 1;
-            atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)i);
-          }
-          if (out) d_out += 1.0;
-          AxisTaps ax, ay, az;
-          if (exact_axes(g, x, y, z, ax, ay, az)) d_grid += w;
-          if (fs.moments) {
-            d_nsq += w;
-            double wv = DMUL(w, v);
-            d_v[0] += wv; wv = DMUL(wv, v);
-            d_v[1] += wv; wv = DMUL(wv, v);
-            d_v[2] += wv; wv = DMUL(wv, v);
-            d_v[3] += wv;
-          }
-          f_abs[0] += (float)fabs(wpow64(w, v, fs.ea));
-          f_abs[1] += (float)fabs(wpow64(w, v, fs.eb));
-        }
-      } else {
-        f_read += 1.0f;
-        const bool out = (p.sx < 0.0f) || (p.sx > (float)g.nx) || (p.sy < 0.0f) || (p.sy > (float)g.ny) ||
-                         (p.sz < 0.0f) || (p.sz > (float)g.nz);
-        if (out && g.los == 0) {
-          fatal = 1;
-          atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)i);
-        }
-        if (out) f_out += 1.0f;
-        if (accept32(g, p.sx, p.sy, p.sz)) f_grid += p.w;
-        if (fs.moments) {
-          f_nsq += p.w;
-          float wv = p.w * p.v;
-          f_v[0] += wv; wv *= p.v;
-          f_v[1] += wv; wv *= p.v;
-          f_v[2] += wv; wv *= p.v;
-          f_v[3] += wv;
-        }
-        float pa = p.w, pb = p.w;
-        for (int e = 0; e < fs.ea; e++) pa *= p.v;
-        for (int e = 0; e < fs.eb; e++) pb *= p.v;
-        f_abs[0] += fabsf(pa);
-        f_abs[1] += fabsf(pb);
-        ntile = regular_tiles(g, tg, p.sx, p.sy, p.sz, TX, TY, TZ);
-        reg = true;
+    if (!footprint(g, tg, p.sx, p.sy, p.sz, TX, TY, TZ)) {
+      f_out += 1.0f;  // outside the box by at least two cells (src/read_data.c:81-88)
+      if (g.los == 0) {
+        fatal = 1;
+        atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)i);
       }
+      continue;
     }
-    // warp-uniform loop over the up-to-8 tiles of each regular particle
-    int maxt = __reduce_max_sync(FULL_MASK, reg ? ntile : 0);
-    for (int k = 0; k < maxt; k++) {
-      bool act = reg && k < ntile;
-      int key = 0;
-      if (act) {
-        int a = k % TX.n, b = (k / TX.n) % TY.n, c = k / (TX.n * TY.n);
-        key = tile_id(tg, TX.t[a], TY.t[b], TZ.t[c]);
-      }
-      agg_inc(counts, key, act);
-    }
+    if (split_edge && is_edge(g, p.sx, p.sy, p.sz)) continue;  // painted by k_edge_fixup
+    for (int a = 0; a < TX.n; a++)
+      for (int b = 0; b < TY.n; b++)
+        for (int c = 0; c < TZ.n; c++)
+          atomicAdd(counts + tile_id(tg, tile_at(TX, a), tile_at(TY, b), tile_at(TZ, c)), 1u);
   }
-  // FP32 partials are per thread over ~n/(grid threads) particles; promoted to FP64 per warp
-  const double vals[10] = {(double)f_read, d_out + (double)f_out, d_grid + (double)f_grid, d_nsq + (double)f_nsq,
-                           d_v[0] + (double)f_v[0], d_v[1] + (double)f_v[1], d_v[2] + (double)f_v[2],
-                           d_v[3] + (double)f_v[3], (double)f_abs[0], (double)f_abs[1]};
-  double *const dst[10] = {&st->nread, &st->nout, &st->ngrid, &st->nsq, &st->vr[0], &st->vr[1], &st->vr[2], &st->vr[3],
-                           &st->absw[0], &st->absw[1]};
-  block_add<10>(vals, dst);
+  // FP32 per-thread partials over ~n/(grid threads) particles, FP64 across threads
+  const double vals[9] = {(double)f_read, (double)f_out, (double)f_nsq, (double)f_v[0], (double)f_v[1],
+                          (double)f_v[2], (double)f_v[3], (double)f_abs[0], (double)f_abs[1]};
+  double *const dst[9] = {&st->nread, &st->nout, &st->nsq, &st->vr[0], &st->vr[1], &st->vr[2], &st->vr[3],
+                          &st->absw[0], &st->absw[1]};
+  block_add<9>(vals, dst);
   if (fatal) atomicOr(&st->fatal, 1);
   if (nonfin) atomicOr(&st->nonfinite, 1);
-}
-
-// Pass 1b: tile counts of the edge particles (exact taps).
-template <typename T>
-__global__ void k_count_special(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in, const unsigned *special, DevStats *st,
-                                unsigned *counts) {
-  const unsigned ns = st->nspecial;
-  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += gridDim.x * blockDim.x) {
-    double x, y, z, v, w;
-    exact_pos(g, fs, in, special[k], x, y, z, v, w);
-    if (!(isfinite(x) && isfinite(y) && isfinite(z) && isfinite(v) && isfinite(w))) continue;
-    int ids[64];
-    int nt = exact_tiles<64>(g, tg, x, y, z, ids);
-    for (int t = 0; t < nt; t++) atomicAdd(counts + ids[t], 1u);
-  }
 }
 
 // Pass 2: exclusive scan of the tile counts (one CTA), cursor copy, record total, fixed-point scales.
@@ -437,257 +395,566 @@ __global__ void __launch_bounds__(1024) k_scan(const unsigned *counts, int ntile
 
 #define SPECIAL_MARK (-3.0e38f)
 
-// Pass 3: scatter regular particles into their tiles' lists.
+// Pass 3: scatter particles into their tiles' lists. A record holds the normal-stencil scales and
+// the velocity, or, for a particle taking the exact rules, a mark and the particle index.
 template <typename T>
 __global__ void __launch_bounds__(256) k_scatter(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in, long long n,
                                                  unsigned *cursor, float4 *recs, float *recw,
-                                                 unsigned long long capacity) {
+                                                 unsigned long long capacity, unsigned *edge_list,
+                                                 unsigned *edge_count) {
   const long long stride = (long long)gridDim.x * blockDim.x;
-  const long long nround = (n + stride - 1) / stride * stride;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nround; i += stride) {
-    bool reg = false;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const Prep p = prep32(g, fs, in, i);
+    if (!p.fin) continue;
     AxisTiles TX, TY, TZ;
-    int ntile = 0;
-    Prep p;
-    if (i < n) {
-      p = prep32(g, fs, in, i);
-      if (!p.edge) {
-        reg = true;
-        ntile = regular_tiles(g, tg, p.sx, p.sy, p.sz, TX, TY, TZ);
-      }
+    if (!footprint(g, tg, p.sx, p.sy, p.sz, TX, TY, TZ)) continue;
+    const bool edge = is_edge(g, p.sx, p.sy, p.sz);
+    if (edge && edge_list) {  // painted by k_edge_fixup after the tiles
+      edge_list[atomicAdd(edge_count, 1u)] = (unsigned)i;
+      continue;
     }
-    int maxt = __reduce_max_sync(FULL_MASK, reg ? ntile : 0);
-    for (int k = 0; k < maxt; k++) {
-      bool act = reg && k < ntile;
-      int key = 0;
-      if (act) {
-        int a = k % TX.n, b = (k / TX.n) % TY.n, c = k / (TX.n * TY.n);
-        key = tile_id(tg, TX.t[a], TY.t[b], TZ.t[c]);
-      }
-      unsigned slot = agg_inc(cursor, key, act);
-      if (act && slot < capacity) {
-        recs[slot] = make_float4(p.sx, p.sy, p.sz, p.v);
-        if (recw) recw[slot] = p.w;
-      }
-    }
+    const float4 rec = edge ? make_float4(SPECIAL_MARK, __uint_as_float((unsigned)i), 0.0f, 0.0f)
+                            : make_float4(p.sx, p.sy, p.sz, p.v);
+    for (int a = 0; a < TX.n; a++)
+      for (int b = 0; b < TY.n; b++)
+        for (int c = 0; c < TZ.n; c++) {
+          const unsigned slot = atomicAdd(cursor + tile_id(tg, tile_at(TX, a), tile_at(TY, b), tile_at(TZ, c)), 1u);
+          if (slot < capacity) {
+            recs[slot] = rec;
+            if (recw) recw[slot] = p.w;
+          }
+        }
   }
 }
 
-// Pass 3b: scatter edge particles (record carries the particle index).
-template <typename T>
-__global__ void k_scatter_special(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in, const unsigned *special,
-                                  const DevStats *st, unsigned *cursor, float4 *recs, unsigned long long capacity) {
-  const unsigned ns = st->nspecial;
-  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += gridDim.x * blockDim.x) {
-    const unsigned idx = special[k];
-    double x, y, z, v, w;
-    exact_pos(g, fs, in, idx, x, y, z, v, w);
-    if (!(isfinite(x) && isfinite(y) && isfinite(z) && isfinite(v) && isfinite(w))) continue;
-    int ids[64];
-    int nt = exact_tiles<64>(g, tg, x, y, z, ids);
-    for (int t = 0; t < nt; t++) {
-      unsigned slot = atomicAdd(cursor + ids[t], 1u);
-      if (slot < capacity) recs[slot] = make_float4(SPECIAL_MARK, __uint_as_float(idx), 0.0f, 0.0f);
-    }
+// Pass 4: one CTA per tile. Shared memory holds the tile of every grid slot; taps outside the
+// tile are skipped (another tile owns them). The particle's home tile also adds it to the
+// statistics that need exact decisions: NGRID, the out-of-box count and the LOS == 0 error.
+// FP32 accumulation adds the float; the deterministic variant adds round(value * 2^S) as an integer.
+__device__ __forceinline__ void acc_add(float *p, float v, double) { atomicAdd(p, v); }
+__device__ __forceinline__ void acc_add(unsigned long long *p, float v, double scale) {
+  atomicAdd(p, (unsigned long long)__double2ll_rn((double)v * scale));
+}
+__device__ __forceinline__ void acc_add64(float *p, double v, double) { atomicAdd(p, (float)v); }
+__device__ __forceinline__ void acc_add64(unsigned long long *p, double v, double scale) {
+  atomicAdd(p, (unsigned long long)__double2ll_rn(v * scale));
+}
+
+#define TAP_RB 32  // records a warp stages at a time
+
+// One axis of a record's stencil for the lane-per-tap deposit: the taps' offsets in the shared tile
+// (index within the tile times the axis pitch) and weights; a tap that the reference drops or that
+// lies outside this tile gets weight 0.
+__device__ __forceinline__ void stage_axis32(const AxisTapsF &t, int origin, int extent, int pitch, float *W,
+                                             int *O) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int l = t.idx[k] - origin;
+    const bool ok = t.idx[k] >= 0 && l >= 0 && l < extent;
+    W[k] = ok ? t.w[k] : 0.0f;
+    O[k] = ok ? l * pitch : 0;
   }
 }
 
-// Pass 4: one CTA per tile. Shared memory holds the tile of every grid slot; taps outside
-// the tile are skipped (another tile owns them).
-template <typename Acc>
-struct TileAcc;
-template <>
-struct TileAcc<float> {
-  __device__ static void add(float *p, double vd, float vf, double) { atomicAdd(p, vf); (void)vd; }
-};
-template <>
-struct TileAcc<unsigned long long> {
-  __device__ static void add(unsigned long long *p, double vd, float, double scale) {
-    atomicAdd(p, (unsigned long long)__double2ll_rn(vd * scale));
+// Same for exact taps in the reference's index space. x: halo slices fold onto 0.. (LOS == 0) or are
+// dropped; z: the padding column (a CIC rounding edge) is dropped; y == NY (a CIC rounding edge) is
+// the aliased write handled by the caller.
+__device__ __forceinline__ void stage_axis64(const Geom &g, const AxisTaps &t, int axis, int origin, int extent,
+                                             int pitch, float *W, int *O) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    int idx = t.idx[k];
+    bool ok = k < t.n && t.on[k];
+    const int n = axis == 0 ? g.nx : (axis == 1 ? g.ny : g.nz);
+    if (axis == 0 && idx >= n) {
+      if (g.los == 0 && idx < n + g.order) idx -= n;
+      else ok = false;
+    }
+    if (idx < 0 || idx >= n) ok = false;
+    const int l = idx - origin;
+    ok = ok && l >= 0 && l < extent;
+    W[k] = ok ? (float)t.w[k] : 0.0f;
+    O[k] = ok ? l * pitch : 0;
   }
-};
+}
 
+// Pass 4: one CTA per tile; shared memory holds the tile of every grid slot with bank-spreading
+// pitches. Each warp stages 32 records at a time (lane = record: tap offsets and weights per axis),
+// then deposits them one record after another with lane = tap, so the 27 shared-memory atomics of
+// a record hit 27 different banks. The particle's home tile also adds it to the statistics that need
+// exact decisions: NGRID, the out-of-box count and the LOS == 0 error.
 template <typename T, typename Acc>
-__global__ void __launch_bounds__(256) k_tile_paint(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in,
+__global__ void __launch_bounds__(256, 2) k_tile_paint(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in,
                                                     long long n, const unsigned *offsets, const float4 *recs,
                                                     const float *recw, unsigned long long capacity, GridPtrs grids,
                                                     const double *fixed_scale, DevStats *st) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  Acc *sm = (Acc *)smraw;
   const int nf = fs.nfields, nst = g.interlace ? 2 : 1, nslot = nf * nst;
-  const int tsz = tg.tx * tg.ty * tg.tz;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  Acc *sm = (Acc *)smraw;
+  const size_t tile_bytes = ((size_t)nslot * tg.slot * sizeof(Acc) + 15) & ~(size_t)15;
+  float *Wst = (float *)(smraw + tile_bytes) + warp * (TAP_RB * 9);
+  int *Ost = (int *)(smraw + tile_bytes) + nwarps * (TAP_RB * 9) + warp * (TAP_RB * 9);
+  float2 *Vst = (float2 *)((int *)(smraw + tile_bytes) + 2 * nwarps * (TAP_RB * 9)) + warp * TAP_RB;
   const int tile = blockIdx.x;
   const int bz = tile % tg.nbz, by = (tile / tg.nbz) % tg.nby, bx = tile / (tg.nbz * tg.nby);
   const int x0 = bx * tg.tx, y0 = by * tg.ty, z0 = bz * tg.tz;
   const int ex = min(tg.tx, g.nx - x0), ey = min(tg.ty, g.ny - y0), ez = min(tg.tz, g.nz - z0);
-  for (int c = threadIdx.x; c < nslot * tsz; c += blockDim.x) sm[c] = (Acc)0;
+  for (int c = threadIdx.x; c < nslot * tg.slot; c += blockDim.x) sm[c] = (Acc)0;
   __syncthreads();
   const double sc0 = fixed_scale ? fixed_scale[0] : 1.0, sc1 = fixed_scale ? fixed_scale[1] : 1.0;
+  // this lane's tap in the deposit phase
+  const int K = g.order;
+  const bool tap_on = lane < K * K * K;
+  const int tdx = tap_on ? lane / (K * K) : 0, tdy = tap_on ? (lane / K) % K : 0, tdz = tap_on ? lane % K : 0;
+  float f_grid = 0.0f;
+  double d_grid = 0.0, d_out = 0.0;
+  int fatal = 0;
   unsigned rb = offsets[tile], re = offsets[tile + 1];
   if (re > capacity) re = (unsigned)capacity;
   if (rb > re) rb = re;
-  for (unsigned r = rb + threadIdx.x; r < re; r += blockDim.x) {
-    const float4 rec = recs[r];
-    if (rec.x == SPECIAL_MARK) {  // exact FP64 rules
-      const unsigned idx = __float_as_uint(rec.y);
-      if ((long long)idx >= n) continue;
-      double x, y, z, v, w;
-      exact_pos(g, fs, in, idx, x, y, z, v, w);
-      const double val[2] = {wpow64(w, v, fs.ea), wpow64(w, v, fs.eb)};
-      for (int stn = 0; stn < nst; stn++) {
-        AxisTaps ax, ay, az;
-        double px = stn ? DADD(x, g.hx) : x, py = stn ? DADD(y, g.hy) : y, pz = stn ? DADD(z, g.hz) : z;
-        if (!exact_axes(g, px, py, pz, ax, ay, az)) continue;
-        for (int c = 0; c < az.n; c++)
-          for (int b = 0; b < ay.n; b++)
-            for (int a = 0; a < ax.n; a++) {
-              if (!(ax.on[a] && ay.on[b] && az.on[c])) continue;
-              long long L = canon_index(g, ax.idx[a], ay.idx[b], az.idx[c]);
-              if (L < 0) continue;
-              int ix, iy, iz;
-              decode(g, L, ix, iy, iz);
-              ix -= x0; iy -= y0; iz -= z0;
-              if (ix < 0 || ix >= ex || iy < 0 || iy >= ey || iz < 0 || iz >= ez) continue;
-              const int cell = (ix * tg.ty + iy) * tg.tz + iz;
-              for (int f = 0; f < nf; f++) {
-                double d = DMUL(DMUL(DMUL(val[f], ax.w[a]), ay.w[b]), az.w[c]);
-                TileAcc<Acc>::add(sm + (stn * nf + f) * tsz + cell, d, (float)d, f ? sc1 : sc0);
+  for (unsigned base = rb + warp * TAP_RB; base < re; base += nwarps * TAP_RB) {
+    const unsigned r = base + lane;
+    const bool have = r < re;
+    const int cnt = min((unsigned)TAP_RB, re - base);
+    // ---- this lane's record
+    float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
+    float w = 1.0f;
+    bool special = false;
+    unsigned idx = 0;
+    double x = 0, y = 0, z = 0, v = 0, wd = 1;
+    if (have) {
+      rec = recs[r];
+      special = rec.x == SPECIAL_MARK;
+      if (special) {
+        idx = __float_as_uint(rec.y);
+        if ((long long)idx >= n) {
+          special = false;
+          rec.x = rec.y = rec.z = -1.0e30f;  // taps nowhere
+        } else {
+          exact_pos(g, fs, in, idx, x, y, z, v, wd);
+          const Prep p = prep32(g, fs, in, idx);
+          if (home_of(g, tg, p.sx, p.sy, p.sz) == tile) {  // statistics with exact decisions
+            if (outside_box(g, x, y, z)) {                   // src/read_data.c:81-88
+              d_out += 1.0;
+              if (g.los == 0) {
+                fatal = 1;
+                atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)idx);
               }
             }
-      }
-      continue;
-    }
-    const float w = recw ? recw[r] : 1.0f;
-    float va = w, vb = w;
-    for (int e = 0; e < fs.ea; e++) va *= rec.w;
-    for (int e = 0; e < fs.eb; e++) vb *= rec.w;
-    for (int stn = 0; stn < nst; stn++) {
-      float sx = stn ? __fadd_rn(rec.x, 0.5f) : rec.x, sy = stn ? __fadd_rn(rec.y, 0.5f) : rec.y,
-            sz = stn ? __fadd_rn(rec.z, 0.5f) : rec.z;
-      if (!accept32(g, sx, sy, sz)) continue;
-      AxisTapsF tx, ty, tz;
-      axis32(g.order, sx, 0, g.nx, g.los, tx);
-      axis32(g.order, sy, 1, g.ny, g.los, ty);
-      axis32(g.order, sz, 1, g.nz, g.los, tz);
-      int lx[3], ly[3], lz[3];
-#pragma unroll
-      for (int k = 0; k < 3; k++) {
-        int a = tx.idx[k] - x0, b = ty.idx[k] - y0, c = tz.idx[k] - z0;
-        lx[k] = (tx.idx[k] >= 0 && a >= 0 && a < ex) ? a : -1;
-        ly[k] = (ty.idx[k] >= 0 && b >= 0 && b < ey) ? b : -1;
-        lz[k] = (tz.idx[k] >= 0 && c >= 0 && c < ez) ? c : -1;
-      }
-      Acc *s0 = sm + (stn * nf) * tsz;
-#pragma unroll
-      for (int a = 0; a < 3; a++) {
-        if (lx[a] < 0) continue;
-        const float wa = tx.w[a];
-#pragma unroll
-        for (int b = 0; b < 3; b++) {
-          if (ly[b] < 0) continue;
-          const float wab = wa * ty.w[b];
-          const int rowc = (lx[a] * tg.ty + ly[b]) * tg.tz;
-#pragma unroll
-          for (int c = 0; c < 3; c++) {
-            if (lz[c] < 0) continue;
-            const float wt = wab * tz.w[c];
-            const int cell = rowc + lz[c];
-            TileAcc<Acc>::add(s0 + cell, (double)(va * wt), va * wt, sc0);
-            if (nf == 2) TileAcc<Acc>::add(s0 + tsz + cell, (double)(vb * wt), vb * wt, sc1);
+            AxisTaps ax, ay, az;
+            if (exact_axes(g, x, y, z, ax, ay, az)) d_grid += wd;
           }
         }
+      } else {
+        w = recw ? recw[r] : 1.0f;
+        if (home_of(g, tg, rec.x, rec.y, rec.z) == tile && accept32(g, rec.x, rec.y, rec.z)) f_grid += w;
       }
     }
+    float va, vb;
+    if (special) {
+      va = (float)wpow64(wd, v, fs.ea);
+      vb = (float)wpow64(wd, v, fs.eb);
+    } else {
+      va = w;
+      vb = w;
+      for (int e = 0; e < fs.ea; e++) va *= rec.w;
+      for (int e = 0; e < fs.eb; e++) vb *= rec.w;
+    }
+    Vst[lane] = make_float2(va, vb);
+    for (int stn = 0; stn < nst; stn++) {
+      float *W = Wst + lane * 9;
+      int *O = Ost + lane * 9;
+      if (!have) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) { W[k] = 0.0f; O[k] = 0; }
+      } else if (special) {
+        AxisTaps ax, ay, az;
+        const double px = stn ? DADD(x, g.hx) : x, py = stn ? DADD(y, g.hy) : y, pz = stn ? DADD(z, g.hz) : z;
+        const bool acc = exact_axes(g, px, py, pz, ax, ay, az);
+        if (!acc) {
+#pragma unroll
+          for (int k = 0; k < 9; k++) { W[k] = 0.0f; O[k] = 0; }
+        } else {
+          stage_axis64(g, ax, 0, x0, ex, tg.px, W, O);
+          stage_axis64(g, ay, 1, y0, ey, tg.py, W + 3, O + 3);
+          stage_axis64(g, az, 2, z0, ez, 1, W + 6, O + 6);
+          // CIC rounding edge: y index NY lands in row 0 of the next x slice (src/read_data.c:592-593);
+          // deposited here directly (a handful of taps at most)
+          if (g.order == 2 && ay.n > 0 && ay.idx[0] == g.ny && ay.on[0]) {
+            for (int a = 0; a < ax.n; a++)
+              for (int c = 0; c < az.n; c++) {
+                if (!(ax.on[a] && az.on[c])) continue;
+                long long L = canon_index(g, ax.idx[a], ay.idx[0], az.idx[c]);
+                if (L < 0) continue;
+                int ix, iy, iz;
+                decode(g, L, ix, iy, iz);
+                ix -= x0; iy -= y0; iz -= z0;
+                if (ix < 0 || ix >= ex || iy < 0 || iy >= ey || iz < 0 || iz >= ez) continue;
+                const int cell = ix * tg.px + iy * tg.py + iz;
+                const double tw = DMUL(DMUL(ax.w[a], ay.w[0]), az.w[c]);
+                acc_add64(sm + (stn * nf) * tg.slot + cell, DMUL(wpow64(wd, v, fs.ea), tw), sc0);
+                if (nf == 2) acc_add64(sm + (stn * nf + 1) * tg.slot + cell, DMUL(wpow64(wd, v, fs.eb), tw), sc1);
+              }
+          }
+        }
+      } else {
+        const float sx = stn ? __fadd_rn(rec.x, 0.5f) : rec.x, sy = stn ? __fadd_rn(rec.y, 0.5f) : rec.y,
+                    sz = stn ? __fadd_rn(rec.z, 0.5f) : rec.z;
+        if (!accept32(g, sx, sy, sz)) {
+#pragma unroll
+          for (int k = 0; k < 9; k++) { W[k] = 0.0f; O[k] = 0; }
+        } else {
+          AxisTapsF tx, ty, tz;
+          axis32(g.order, sx, 0, g.nx, g.los, tx);
+          axis32(g.order, sy, 1, g.ny, g.los, ty);
+          axis32(g.order, sz, 1, g.nz, g.los, tz);
+          stage_axis32(tx, x0, ex, tg.px, W, O);
+          stage_axis32(ty, y0, ey, tg.py, W + 3, O + 3);
+          stage_axis32(tz, z0, ez, 1, W + 6, O + 6);
+        }
+      }
+      __syncwarp();
+      // ---- deposit: lane = tap, one record after another
+      Acc *sA = sm + (stn * nf) * tg.slot, *sB = sA + tg.slot;
+      for (int j = 0; j < cnt; j++) {
+        const float *Wj = Wst + j * 9;
+        const int *Oj = Ost + j * 9;
+        const float wt = Wj[tdx] * Wj[3 + tdy] * Wj[6 + tdz];
+        if (tap_on && wt != 0.0f) {
+          const int off = Oj[tdx] + Oj[3 + tdy] + Oj[6 + tdz];
+          const float2 vv = Vst[j];
+          acc_add(sA + off, vv.x * wt, sc0);
+          if (nf == 2) acc_add(sB + off, vv.y * wt, sc1);
+        }
+      }
+      __syncwarp();
+    }
   }
-  __syncthreads();
-  // write the tile: rows along z are contiguous in the padded layout
-  double dc[4] = {0, 0, 0, 0};
-  unsigned long long dcf[4] = {0, 0, 0, 0};
-  const int rows = ex * ey;
+  {
+    const double vals[2] = {d_grid + (double)f_grid, d_out};
+    double *const dst[2] = {&st->ngrid, &st->nout};
+    block_add<2>(vals, dst);
+    if (fatal) atomicOr(&st->fatal, 1);
+  }
+  // ---- write the tile: pairs of cells along z as float2 (rows start 8-byte aligned in global
+  // memory: the padded row length 2*(NZ/2+1) is even)
+  const int tsz = tg.tx * tg.ty * tg.tz;
+  const int npair = tsz >> 1;
   for (int slot = 0; slot < nslot; slot++) {
     float *gp = (float *)grids.g[slot];
-    const Acc *s = sm + slot * tsz;
+    const Acc *s = sm + slot * tg.slot;
     const double inv = (slot % nf) ? 1.0 / sc1 : 1.0 / sc0;
-    for (int q = threadIdx.x; q < rows * ez; q += blockDim.x) {
-      const int rz = q % ez, rr = q / ez;
-      const int ly = rr % ey, lx = rr / ey;
-      const Acc a = s[(lx * tg.ty + ly) * tg.tz + rz];
-      float val;
+    float dsum = 0.0f;  // FP32 over this thread's cells; FP64 across threads
+    unsigned long long fsum = 0;
+    for (int q = threadIdx.x; q < npair; q += blockDim.x) {
+      const int c = q << 1;
+      const int rz = c & (tg.tz - 1), ly = (c >> tg.lz) & (tg.ty - 1), lx = c >> (tg.lz + tg.ly);
+      if (lx >= ex || ly >= ey || rz >= ez) continue;
+      const int sidx = lx * tg.px + ly * tg.py + rz;
+      const Acc a0 = s[sidx], a1 = s[sidx + 1];
+      float v0, v1;
       if (sizeof(Acc) == 8) {
-        val = (float)((double)(long long)a * inv);
-        dcf[slot] += (unsigned long long)a;
+        v0 = (float)((double)(long long)a0 * inv);
+        v1 = (float)((double)(long long)a1 * inv);
+        fsum += (unsigned long long)a0 + (rz + 1 < ez ? (unsigned long long)a1 : 0ULL);
       } else {
-        val = (float)a;
-        dc[slot] += (double)val;
+        v0 = (float)a0;
+        v1 = (float)a1;
+        dsum += v0 + (rz + 1 < ez ? v1 : 0.0f);
       }
-      gp[(long long)(x0 + lx) * g.slice + (long long)(y0 + ly) * g.row + z0 + rz] = val;
+      float *dst = gp + (long long)(x0 + lx) * g.slice + (long long)(y0 + ly) * g.row + z0 + rz;
+      if (rz + 1 < ez) *reinterpret_cast<float2 *>(dst) = make_float2(v0, v1);
+      else dst[0] = v0;
+    }
+    if (sizeof(Acc) == 8) {
+      for (int o = 16; o > 0; o >>= 1) fsum += __shfl_xor_sync(FULL_MASK, fsum, o);
+      if ((threadIdx.x & 31) == 0 && fsum) atomicAdd(&st->dc_fixed[slot], fsum);
+    } else {
+      const double vals[1] = {(double)dsum};
+      double *const dst1[1] = {&st->dc[slot]};
+      block_add<1>(vals, dst1);
     }
   }
-  if (sizeof(Acc) == 8) {
-    for (int slot = 0; slot < nslot; slot++) {
-      unsigned long long v = dcf[slot];
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
-      if ((threadIdx.x & 31) == 0 && v) atomicAdd(&st->dc_fixed[slot], v);
+}
+
+// Compile-time-order FP32 taps of one axis (kind 0: x, 1: y or z).
+template <int K>
+__device__ __forceinline__ void axis32k(float s, int kind, int n, int los, AxisTapsF &t) {
+  if (K == 3) tsc_axis32(s, kind, n, los, t);
+  else if (K == 2) cic_axis32(s, kind, n, los, t);
+  else ngp_axis32(s, n, los, t);
+}
+
+// FP32 tile kernel for particles away from every edge of the reference's rules (those are painted
+// by k_edge_fixup). One CTA per (tile, stencil): shared memory holds the stencil's one or two grid
+// slots, so three CTAs fit per SM. Lane = record while staging, lane = tap while depositing.
+#define LEAN_RB 16  // records a warp stages at a time in the lean kernel
+
+// FP32 tile kernel for particles away from every edge of the reference's rules (those are painted
+// by k_edge_fixup). One CTA per (tile, stencil): shared memory holds the stencil's one or two grid
+// slots, so three CTAs fit per SM. Each warp stages 16 records (lane = record): the 9 products
+// va*wx*wy, vb*wx*wy with their x+y tile offsets and the 3 z weights with their offsets; then it
+// deposits them one record after another with lane = tap, two shared loads and two atomics per tap.
+template <int K, int NF>
+__global__ void __launch_bounds__(256, 3) k_tile_lean(Geom g, FieldSpec fs, TileGeo tg, const unsigned *offsets,
+                                                      const float4 *recs, const float *recw,
+                                                      unsigned long long capacity, GridPtrs grids, DevStats *st) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int stn = blockIdx.y;
+  float *sm = (float *)smraw;
+  const size_t tile_bytes = ((size_t)NF * tg.slot * sizeof(float) + 15) & ~(size_t)15;
+  float4 *XY = (float4 *)(smraw + tile_bytes) + warp * (LEAN_RB * 9);
+  float2 *ZZ = (float2 *)((float4 *)(smraw + tile_bytes) + (blockDim.x >> 5) * (LEAN_RB * 9)) + warp * (LEAN_RB * 3);
+  const int tile = blockIdx.x;
+  const int bz = tile % tg.nbz, by = (tile / tg.nbz) % tg.nby, bx = tile / (tg.nbz * tg.nby);
+  const int x0 = bx * tg.tx, y0 = by * tg.ty, z0 = bz * tg.tz;
+  const int ex = min(tg.tx, g.nx - x0), ey = min(tg.ty, g.ny - y0), ez = min(tg.tz, g.nz - z0);
+  for (int c = threadIdx.x; c < NF * tg.slot; c += blockDim.x) sm[c] = 0.0f;
+  __syncthreads();
+  constexpr int NT = K * K * K;
+  const bool tap_on = lane < NT;
+  const int txy = tap_on ? (lane / (K * K)) * 3 + (lane / K) % K : 0, tz = tap_on ? lane % K : 0;
+  float f_grid = 0.0f;
+  unsigned rb = offsets[tile], re = offsets[tile + 1];
+  if (re > capacity) re = (unsigned)capacity;
+  if (rb > re) rb = re;
+  const int nwarps = blockDim.x >> 5;
+  for (unsigned base = rb + warp * LEAN_RB; base < re; base += nwarps * LEAN_RB) {
+    const unsigned r = base + lane;
+    const int cnt = min((unsigned)LEAN_RB, re - base);
+    if (lane < LEAN_RB) {
+      float wx[3] = {0, 0, 0}, wy[3] = {0, 0, 0}, wz[3] = {0, 0, 0};
+      int ox[3] = {0, 0, 0}, oy[3] = {0, 0, 0}, oz[3] = {0, 0, 0};
+      float va = 0.0f, vb = 0.0f;
+      if (r < re) {
+        const float4 rec = recs[r];
+        const float w = recw ? recw[r] : 1.0f;
+        if (stn == 0 && home_of(g, tg, rec.x, rec.y, rec.z) == tile && accept32(g, rec.x, rec.y, rec.z)) f_grid += w;
+        va = w;
+        vb = w;
+        for (int e = 0; e < fs.ea; e++) va *= rec.w;
+        for (int e = 0; e < fs.eb; e++) vb *= rec.w;
+        const float sx = stn ? __fadd_rn(rec.x, 0.5f) : rec.x, sy = stn ? __fadd_rn(rec.y, 0.5f) : rec.y,
+                    sz = stn ? __fadd_rn(rec.z, 0.5f) : rec.z;
+        if (accept32(g, sx, sy, sz)) {
+          AxisTapsF ax, ay, az;
+          axis32k<K>(sx, 0, g.nx, g.los, ax);
+          axis32k<K>(sy, 1, g.ny, g.los, ay);
+          axis32k<K>(sz, 1, g.nz, g.los, az);
+          stage_axis32(ax, x0, ex, tg.px, wx, ox);
+          stage_axis32(ay, y0, ey, tg.py, wy, oy);
+          stage_axis32(az, z0, ez, 1, wz, oz);
+        }
+      }
+      float4 *xy = XY + lane * 9;
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b2 = 0; b2 < 3; b2++) {
+          const float wxy = wx[a] * wy[b2];
+          xy[a * 3 + b2] = make_float4(va * wxy, vb * wxy, __int_as_float(ox[a] + oy[b2]), 0.0f);
+        }
+      float2 *zz = ZZ + lane * 3;
+#pragma unroll
+      for (int c = 0; c < 3; c++) zz[c] = make_float2(wz[c], __int_as_float(oz[c]));
     }
+    __syncwarp();
+    float *sA = sm, *sB = sm + tg.slot;
+    for (int j = 0; j < cnt; j++) {
+      const float4 e = XY[j * 9 + txy];
+      const float2 f = ZZ[j * 3 + tz];
+      if (tap_on && f.x != 0.0f && (e.x != 0.0f || e.y != 0.0f)) {
+        const int off = __float_as_int(e.z) + __float_as_int(f.y);
+        atomicAdd(sA + off, e.x * f.x);
+        if (NF == 2) atomicAdd(sB + off, e.y * f.x);
+      }
+    }
+    __syncwarp();
+  }
+  if (stn == 0) {
+    const double vals[1] = {(double)f_grid};
+    double *const dst[1] = {&st->ngrid};
+    block_add<1>(vals, dst);
   } else {
-    const double vals[4] = {dc[0], dc[1], dc[2], dc[3]};
-    double *const dst[4] = {&st->dc[0], &st->dc[1], &st->dc[2], &st->dc[3]};
-    block_add<4>(vals, dst);
+    __syncthreads();
   }
+  // write the stencil's slots: pairs of cells along z as float2 (8-byte aligned global rows)
+  const int tsz = tg.tx * tg.ty * tg.tz;
+  const int npair = tsz >> 1;
+  for (int f = 0; f < NF; f++) {
+    const int slot = stn * NF + f;
+    float *gp = (float *)grids.g[slot];
+    const float *sl = sm + f * tg.slot;
+    float dsum = 0.0f;
+    for (int q = threadIdx.x; q < npair; q += blockDim.x) {
+      const int c = q << 1;
+      const int rz = c & (tg.tz - 1), ly = (c >> tg.lz) & (tg.ty - 1), lx = c >> (tg.lz + tg.ly);
+      if (lx >= ex || ly >= ey || rz >= ez) continue;
+      const int sidx = lx * tg.px + ly * tg.py + rz;
+      const float v0 = sl[sidx], v1 = sl[sidx + 1];
+      dsum += v0 + (rz + 1 < ez ? v1 : 0.0f);
+      float *dst = gp + (long long)(x0 + lx) * g.slice + (long long)(y0 + ly) * g.row + z0 + rz;
+      if (rz + 1 < ez) *reinterpret_cast<float2 *>(dst) = make_float2(v0, v1);
+      else dst[0] = v0;
+    }
+    const double vals[1] = {(double)dsum};
+    double *const dst1[1] = {&st->dc[slot]};
+    block_add<1>(vals, dst1);
+  }
+}
+
+// Particles near an edge of the reference's rules, painted after the tiles with the exact FP64
+// rules and global atomics into the FP32 grids; their exact statistics (NGRID, the out-of-box
+// count, the LOS == 0 error) are added here.
+template <typename T>
+__global__ void __launch_bounds__(128) k_edge_fixup(Geom g, FieldSpec fs, PIn<T> in, const unsigned *edge_list,
+                                                    const unsigned *edge_count, GridPtrs grids, DevStats *st) {
+  const unsigned ne = *edge_count;
+  const int nf = fs.nfields, nst = g.interlace ? 2 : 1;
+  double d_grid = 0.0, d_out = 0.0, l_dc[4] = {0, 0, 0, 0};
+  int fatal = 0;
+  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < ne; k += gridDim.x * blockDim.x) {
+    const unsigned idx = edge_list[k];
+    double x, y, z, v, w;
+    exact_pos(g, fs, in, idx, x, y, z, v, w);
+    if (outside_box(g, x, y, z)) {  // src/read_data.c:81-88
+      d_out += 1.0;
+      if (g.los == 0) {
+        fatal = 1;
+        atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)idx);
+        continue;
+      }
+    }
+    const double val[2] = {wpow64(w, v, fs.ea), wpow64(w, v, fs.eb)};
+    for (int stn = 0; stn < nst; stn++) {
+      AxisTaps ax, ay, az;
+      const double px = stn ? DADD(x, g.hx) : x, py = stn ? DADD(y, g.hy) : y, pz = stn ? DADD(z, g.hz) : z;
+      if (!exact_axes(g, px, py, pz, ax, ay, az)) continue;
+      if (stn == 0) d_grid += w;
+      for (int c = 0; c < az.n; c++)
+        for (int b = 0; b < ay.n; b++)
+          for (int a = 0; a < ax.n; a++) {
+            if (!(ax.on[a] && ay.on[b] && az.on[c])) continue;
+            const long long L = canon_index(g, ax.idx[a], ay.idx[b], az.idx[c]);
+            if (L < 0) continue;
+            const double tw = DMUL(DMUL(ax.w[a], ay.w[b]), az.w[c]);
+            for (int f = 0; f < nf; f++) {
+              const float d = (float)DMUL(val[f], tw);
+              atomicAdd((float *)grids.g[stn * nf + f] + L, d);
+              l_dc[stn * nf + f] += (double)d;
+            }
+          }
+    }
+  }
+  const double vals[6] = {d_grid, d_out, l_dc[0], l_dc[1], l_dc[2], l_dc[3]};
+  double *const dst[6] = {&st->ngrid, &st->nout, &st->dc[0], &st->dc[1], &st->dc[2], &st->dc[3]};
+  block_add<6>(vals, dst);
+  if (fatal) atomicOr(&st->fatal, 1);
+}
+
+static int pow2_at_least(int n) {
+  int p = 1;
+  while (p < n) p <<= 1;
+  return p;
+}
+
+static int log2i(int p) {
+  int l = 0;
+  while ((1 << l) < p) l++;
+  return l;
 }
 
 TileGeo choose_tiles(const Geom &g, int nslots, int deterministic) {
   TileGeo t;
   // 4 grid slots x 8x16x32 floats = 64 KB (three CTAs per SM); the int64 variant halves the volume.
+  // Tile edges are powers of two (tile coordinates are shifts); a grid edge shorter than the tile
+  // uses the next power of two and the tile is partial.
   t.tx = 8;
   t.ty = 16;
   t.tz = 32;
   if (deterministic) t.tx = (nslots > 2) ? 4 : 8;
   else if (nslots <= 2) t.tx = 16;
-  if (t.tz > g.nz) t.tz = g.nz;
-  if (t.ty > g.ny) t.ty = g.ny;
-  if (t.tx > g.nx) t.tx = g.nx;
+  t.tz = t.tz < pow2_at_least(g.nz) ? t.tz : pow2_at_least(g.nz);
+  t.ty = t.ty < pow2_at_least(g.ny) ? t.ty : pow2_at_least(g.ny);
+  t.tx = t.tx < pow2_at_least(g.nx) ? t.tx : pow2_at_least(g.nx);
+  t.lx = log2i(t.tx);
+  t.ly = log2i(t.ty);
+  t.lz = log2i(t.tz);
   t.nbx = (g.nx + t.tx - 1) / t.tx;
   t.nby = (g.ny + t.ty - 1) / t.ty;
   t.nbz = (g.nz + t.tz - 1) / t.tz;
   t.ntiles = t.nbx * t.nby * t.nbz;
+  t.py = t.tz + 1;  // >= tz + 1 so a z pair never straddles rows; = 3 (mod 32)
+  while (t.py % 32 != 3) t.py++;
+  t.px = t.ty * t.py;
+  while (t.px % 32 != 9) t.px++;
+  t.slot = t.px * t.tx;
   return t;
 }
 
 size_t tile_smem_bytes(const TileGeo &tg, int nslots, int deterministic) {
-  return (size_t)nslots * tg.tx * tg.ty * tg.tz * (deterministic ? 8 : 4);
+  const size_t tile = ((size_t)nslots * tg.slot * (deterministic ? 8 : 4) + 15) & ~(size_t)15;
+  const size_t stage = (size_t)(256 / 32) * TAP_RB * (9 * 4 + 9 * 4 + 8);
+  return tile + stage;
+}
+
+size_t lean_smem_bytes(const TileGeo &tg, int nf) {
+  const size_t tile = ((size_t)nf * tg.slot * 4 + 15) & ~(size_t)15;
+  return tile + (size_t)(256 / 32) * LEAN_RB * (9 * 16 + 3 * 8);
 }
 
 double tile_dup_estimate(const Geom &g, const TileGeo &tg) {
-  // a particle is listed in a neighbour tile when it lies within ~2.5 cells of the face
-  double m = (g.order == 3) ? 2.5 : (g.order == 2 ? 1.5 : 0.5);
-  if (!g.interlace) m -= 0.5;
-  return (1.0 + m / tg.tx) * (1.0 + m / tg.ty) * (1.0 + m / tg.tz);
+  // a footprint spans 4 (TSC, CIC) or 2 (NN) cells plus the margin; it crosses into the next tile
+  // with probability (span - 1) / tile edge
+  const double span = (g.order == 1 ? 2.0 : (g.order == 2 ? 3.0 : 4.0)) + 2.0 * g.margin;
+  return (1.0 + (span - 1.0) / tg.tx) * (1.0 + (span - 1.0) / tg.ty) * (1.0 + (span - 1.0) / tg.tz);
+}
+
+template <int K, int NF>
+static void launch_lean(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, const PaintBufs &b,
+                        bool weights, const GridPtrs &grids, DevStats *st) {
+  const size_t smem = lean_smem_bytes(tg, NF);
+  cudaFuncSetAttribute(k_tile_lean<K, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_tile_lean<K, NF><<<dim3(tg.ntiles, g.interlace ? 2 : 1), 256, smem, s>>>(
+      g, fs, tg, b.offsets, b.recs, weights ? b.recw : nullptr, b.capacity, grids, st);
+}
+
+template <int K>
+static void launch_lean_nf(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, const PaintBufs &b,
+                           bool weights, const GridPtrs &grids, DevStats *st) {
+  if (fs.nfields == 2) launch_lean<K, 2>(s, g, fs, tg, b, weights, grids, st);
+  else launch_lean<K, 1>(s, g, fs, tg, b, weights, grids, st);
 }
 
 template <typename T>
 static void run_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, int det, PIn<T> in,
                         long long n, const GridPtrs &grids, const PaintBufs &b, DevStats *st, long long *launches) {
   const int th = 256, nb = grid_blocks(n, th) * 2;
+  const bool split = !det;  // FP32: edge particles go to k_edge_fixup; deterministic: exact rules in the tiles
   cudaMemsetAsync(b.counts, 0, sizeof(unsigned) * tg.ntiles, s);
-  k_count<T><<<nb, th, 0, s>>>(g, fs, tg, in, n, b.counts, b.special, st);
-  k_count_special<T><<<152, 128, 0, s>>>(g, fs, tg, in, b.special, st, b.counts);
+  if (split) cudaMemsetAsync(b.edge_count, 0, sizeof(unsigned), s);
+  k_count<T><<<nb, th, 0, s>>>(g, fs, tg, in, n, b.counts, st, split ? 1 : 0);
   k_scan<<<1, 1024, 0, s>>>(b.counts, tg.ntiles, b.offsets, b.cursor, st, b.capacity, b.fixed_scale);
-  k_scatter<T><<<nb, th, 0, s>>>(g, fs, tg, in, n, b.cursor, b.recs, in.w ? b.recw : nullptr, b.capacity);
-  k_scatter_special<T><<<152, 128, 0, s>>>(g, fs, tg, in, b.special, st, b.cursor, b.recs, b.capacity);
-  const int nslot = fs.nfields * (g.interlace ? 2 : 1);
-  const size_t smem = tile_smem_bytes(tg, nslot, det);
+  k_scatter<T><<<nb, th, 0, s>>>(g, fs, tg, in, n, b.cursor, b.recs, in.w ? b.recw : nullptr, b.capacity,
+                                 split ? b.edge_list : nullptr, b.edge_count);
   if (det) {
+    const int nslot = fs.nfields * (g.interlace ? 2 : 1);
+    const size_t smem = tile_smem_bytes(tg, nslot, 1);
     cudaFuncSetAttribute(k_tile_paint<T, unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_tile_paint<T, unsigned long long><<<tg.ntiles, 256, smem, s>>>(g, fs, tg, in, n, b.offsets, b.recs,
                                                                       in.w ? b.recw : nullptr, b.capacity, grids,
                                                                       b.fixed_scale, st);
+    *launches += 4;
   } else {
-    cudaFuncSetAttribute(k_tile_paint<T, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_tile_paint<T, float><<<tg.ntiles, 256, smem, s>>>(g, fs, tg, in, n, b.offsets, b.recs, in.w ? b.recw : nullptr,
-                                                        b.capacity, grids, nullptr, st);
+    const bool wts = in.w != nullptr;
+    if (g.order == 3) launch_lean_nf<3>(s, g, fs, tg, b, wts, grids, st);
+    else if (g.order == 2) launch_lean_nf<2>(s, g, fs, tg, b, wts, grids, st);
+    else launch_lean_nf<1>(s, g, fs, tg, b, wts, grids, st);
+    k_edge_fixup<T><<<152 * 2, 128, 0, s>>>(g, fs, in, b.edge_list, b.edge_count, grids, st);
+    *launches += 5;
   }
-  *launches += 6;
 }
 
 void launch_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, int deterministic,

@@ -25,9 +25,13 @@ struct DevStats {
 
 // Tile decomposition of the grid for the FP32 path.
 struct TileGeo {
-  int tx, ty, tz;
+  int tx, ty, tz;  // powers of two
+  int lx, ly, lz;  // log2 of the tile edges
   int nbx, nby, nbz;
   int ntiles;
+  // shared-memory tile pitches (elements): row pitch py = 3 (mod 32) and plane pitch px = 9 (mod 32)
+  // put the 27 taps of one stencil in 27 distinct banks; slot = px * tx elements
+  int py, px, slot;
 };
 
 // Grid slot order: slot = stencil * nfields + field (A normal, B normal, A interlaced, B interlaced
@@ -42,10 +46,11 @@ struct PaintBufs {
   unsigned int *cursor;    // ntiles
   float4 *recs;            // capacity
   float *recw;             // capacity (only when weights are given)
-  unsigned int *special;   // n: indices of particles handled by the exact rules
-  unsigned long long special_n;
   unsigned long long capacity;
   double *fixed_scale;     // [2] deterministic mode: 2^S per field (device)
+  unsigned int *edge_list; // FP32: indices of particles painted by the exact rules after the tiles
+  unsigned int *edge_count;
+  unsigned long long edge_cap;
 };
 
 // host launchers (paint.cu)
@@ -60,4 +65,5 @@ void launch_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, const Ti
 // suggested tile geometry for a grid (and whether two fields are painted)
 TileGeo choose_tiles(const Geom &g, int nslots, int deterministic);
 size_t tile_smem_bytes(const TileGeo &tg, int nslots, int deterministic);
+size_t lean_smem_bytes(const TileGeo &tg, int nf);
 double tile_dup_estimate(const Geom &g, const TileGeo &tg);
