@@ -84,7 +84,7 @@ EXPORTS = [
     "capow_create", "capow_paint", "capow_get_stats", "capow_power", "capow_normalise", "capow_num_spectra",
     "capow_copy_grid", "capow_stage_ms", "capow_kernel_launches", "capow_destroy", "capow_read_params",
     "capow_read_catalogue", "capow_free", "capow_write_output", "capow_bin_centre", "capow_strerror",
-    "capow_last_error",
+    "capow_last_error", "capow_paint_noalloc",
 ]
 
 _lib = None
@@ -103,6 +103,7 @@ def lib() -> ctypes.CDLL:
     P, O = ctypes.POINTER(_Params), ctypes.POINTER(_Options)
     L.capow_create.argtypes = [P, O, ctypes.POINTER(vp)]
     L.capow_paint.argtypes = [vp, ctypes.POINTER(_Particles)]
+    L.capow_paint_noalloc.argtypes = [vp, ctypes.POINTER(_Particles)]
     L.capow_get_stats.argtypes = [vp, ctypes.POINTER(_Stats)]
     L.capow_power.argtypes = [vp, ctypes.POINTER(_Spectrum), ip]
     L.capow_normalise.argtypes = [P, ctypes.POINTER(_Spectrum)]
@@ -262,6 +263,21 @@ class PowerSpectrum:
         self._keep = [p[3] for p in parts]
         pc = _Particles(n, codes.pop(), devs.pop(), *[p[0] for p in parts])
         self._check(lib().capow_paint(self._ctx, ctypes.byref(pc)), "capow_paint")
+
+    def paint_noalloc(self, x, y, z, vlos=None, w=None) -> None:
+        """capow_paint_noalloc: the paint of an FP32 context from device-resident arrays, with no
+        device allocation (its scratch is the library's fixed per-device array). For callers that
+        cannot allocate at paint time; calls that overlap on the GPU share that array and race."""
+        parts = [_ptr_of(a) for a in (x, y, z, vlos, w)]
+        codes = {p[1] for p in parts if p[0] is not None}
+        if len(codes) != 1 or any(p[2] != 1 for p in parts if p[0] is not None):
+            raise ValueError("capow_paint_noalloc takes device arrays of one dtype")
+        n = len(parts[0][3])
+        if any(p[0] is not None and len(p[3]) != n for p in parts):
+            raise ValueError("particle arrays differ in length")
+        self._keep = [p[3] for p in parts]
+        pc = _Particles(n, codes.pop(), 1, *[p[0] for p in parts])
+        self._check(lib().capow_paint_noalloc(self._ctx, ctypes.byref(pc)), "capow_paint_noalloc")
 
     def stats(self) -> dict:
         s = _Stats()

@@ -10,70 +10,7 @@
 
 #include <vector>
 
-#include "bin.cuh"
-#include "paint.cuh"
-
-#define NPROD 4  // bin products when two fields are painted
-
-struct capow_ctx {
-  capow_params p;
-  capow_options o;
-  int prec;
-  Geom g;
-  FieldSpec fs;
-  TileGeo tg;
-  BinParams bp;
-  BinTables bt;
-  int nslot;
-  int spec_kind[CAPOW_MAX_SPEC];
-  int shot_moment[CAPOW_MAX_SPEC];  // 0: N, n: <v^n> N
-  int moments;
-  cudaStream_t stream;
-  bool own_stream;
-  // device buffers
-  void *grid_base;      // nslot padded grids, contiguous
-  size_t grid_elems;    // reals per padded grid
-  DevStats *st;
-  PaintBufs pb;
-  double *fixed_scale;
-  double *dcv;
-  double *bins, *bins2d;
-  unsigned long long *nmodes_d, *nmodes2d_d;
-  std::vector<unsigned long long> nmodes, nmodes2d;
-  cufftHandle plan;
-  bool plan_ok;
-  // staging for host particle input
-  void *stage[5];
-  size_t stage_bytes[5];
-  capow_particles last;   // device view of the last painted catalogue
-  bool painted, powered;
-  // host pinned readback
-  double *h_bins;
-  DevStats *h_st;
-  std::vector<void *> allocs;
-  cudaEvent_t ev[4];
-  long long launches;
-  char err[512];
-};
-
-#define FAIL(ctx, code, ...)                                        \
-  do {                                                              \
-    if (ctx) snprintf((ctx)->err, sizeof((ctx)->err), __VA_ARGS__); \
-    return (code);                                                  \
-  } while (0)
-
-#define CK(ctx, call)                                                                                       \
-  do {                                                                                                      \
-    cudaError_t e_ = (call);                                                                                \
-    if (e_ != cudaSuccess) FAIL(ctx, CAPOW_ECUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
-                                __LINE__);                                                                  \
-  } while (0)
-
-#define CKFFT(ctx, call)                                                         \
-  do {                                                                           \
-    cufftResult r_ = (call);                                                     \
-    if (r_ != CUFFT_SUCCESS) FAIL(ctx, CAPOW_ECUFFT, "%s failed: cufft status %d", #call, (int)r_); \
-  } while (0)
+#include "ctx.cuh"
 
 extern "C" const char *capow_strerror(int s) {
   switch (s) {

@@ -132,6 +132,28 @@ int capow_create(const capow_params *p, const capow_options *opt, capow_ctx **ou
  * halo fold and the velocity moments, for one catalogue. Replaces any previous paint. */
 int capow_paint(capow_ctx *ctx, const capow_particles *parts);
 
+/* Size of the fixed device scratch of capow_paint_noalloc: 64 MiB per device, reserved when the
+ * first call on that device loads it. */
+#define CAPOW_NOALLOC_SCRATCH_BYTES (64ull << 20)
+
+/* capow_paint without any device allocation. No counterpart in the reference (its paint runs on
+ * the host). capow_paint grows its scratch buffers with the catalogue (cudaMalloc, and cudaFree,
+ * which waits for the whole device); a caller that paints between the steps of a simulation
+ * running on the same GPU, with the rest of the device held by its own memory pool, can neither
+ * allocate nor stall the simulation's streams. This call paints the same grids, with the same
+ * statistics, as capow_paint on an FP32 context, taking its scratch from one fixed device array of
+ * CAPOW_NOALLOC_SCRATCH_BYTES instead; it calls no cudaMalloc, cudaFree or allocating library.
+ * - particles must be device-resident (on_device = 1); FP64 contexts return CAPOW_ENOTSUP;
+ * - n beyond what the array holds for this grid (worst-case tile records per particle) returns
+ *   CAPOW_EINVAL before any device work; capow_last_error names the largest n that fits
+ *   (about 500000 unweighted particles for a 512^3 TSC grid);
+ * - the first call on each device looks up the array's address and loads its code: make it
+ *   before any stream capture begins;
+ * - every call on a device shares the one array: calls that overlap on the GPU (other streams,
+ *   other contexts on the same device) race; order them, e.g. on one stream.
+ * capow_get_stats, capow_copy_grid and capow_power then work as after capow_paint. */
+int capow_paint_noalloc(capow_ctx *ctx, const capow_particles *parts);
+
 /* counters from the last paint (ends with a stream synchronisation). The counters are filled
  * even when the status is CAPOW_EBOUNDS, so the caller can report the offending particle. */
 int capow_get_stats(capow_ctx *ctx, capow_stats *out);
