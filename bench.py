@@ -203,6 +203,27 @@ def cpu_reference(steps: int, warmup: int, parts, log=print) -> dict:
 
 
 # ------------------------------------------------------------------------------------------ GPU
+def profile_case(args):
+    """The workload scaled down by 8 for profiler captures: 128^3 Zel'dovich particles (2,097,152, f32) on
+    a 256^3 TSC grid with the same settings otherwise (grids 270 MB: above L2, a few hundred MB on the
+    device). Runs warm-up + steps evaluations and prints the last one's stage times; no JSON line."""
+    import torch
+
+    import capow_gb300 as cg
+    from capow_gb300 import synth
+
+    dev = torch.device("cuda", 0)
+    x, y, z, vx, vy, vz = synth.zeldovich(N_SIDE // 2, L=1000.0, mesh=256, rms_cells=1.5, seed=SEED,
+                                          torch_device=dev)
+    d = [torch.from_numpy(a).to(dev) for a in (x, y, z, vz)]
+    params = cg.Params(**dict(PARAMS, NX=256, NY=256, NZ=256, NK=81, Maxk=0.81))
+    with cg.PowerSpectrum(params, precision="fp32", spectra=["dd", "dp", "pp"]) as ps:
+        for _ in range(args.warmup + args.steps):
+            ps.paint(*d)
+            ps.power()
+        print("profile case (2,097,152 particles, 256^3): paint %.3f ms, fft %.3f ms, bin %.3f ms" % ps.stage_ms())
+
+
 def gpu_bench(args, world, rank, local):
     import torch
 
@@ -314,8 +335,13 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="run the 8x smaller workload for profiler captures (prints stage times only)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.profile_case:
+        profile_case(args)
+        return
     world, rank, local = dist_init()
     log = (lambda *a: print(*a, file=sys.stderr, flush=True))
 

@@ -686,118 +686,139 @@ __device__ __forceinline__ void axis32k(float s, int kind, int n, int los, AxisT
   else ngp_axis32(s, n, los, t);
 }
 
-// FP32 tile kernel for particles away from every edge of the reference's rules (those are painted
-// by k_edge_fixup). One CTA per (tile, stencil): shared memory holds the stencil's one or two grid
-// slots, so three CTAs fit per SM. Lane = record while staging, lane = tap while depositing.
-#define LEAN_RB 16  // records a warp stages at a time in the lean kernel
+// Power-of-two scale 2^S for a tile's int32 fixed-point cells. A record's taps add at most |w v^e|
+// to one slot, so no cell of the slot exceeds the tile's sum of |w v^e| over its records; that sum
+// (FP32, raised by 0.1 % for its own rounding) times 2^S <= 2^30 keeps every partial sum, with the
+// half-unit rounding of each deposit (one per record and cell), inside int32.
+__device__ __forceinline__ int tile_scale_exp(float sum_abs) {
+  const float bound = sum_abs * 1.001f;
+  if (!(bound > 0.0f) || !isfinite(bound)) return 0;
+  const int e = ilogbf(bound);  // bound < 2^(e+1)
+  const int S = 29 - e;
+  return S > 100 ? 100 : (S < -100 ? -100 : S);
+}
 
 // FP32 tile kernel for particles away from every edge of the reference's rules (those are painted
-// by k_edge_fixup). One CTA per (tile, stencil): shared memory holds the stencil's one or two grid
-// slots, so three CTAs fit per SM. Each warp stages 16 records (lane = record): the 9 products
-// va*wx*wy, vb*wx*wy with their x+y tile offsets and the 3 z weights with their offsets; then it
-// deposits them one record after another with lane = tap, two shared loads and two atomics per tap.
-template <int K, int NF>
-__global__ void __launch_bounds__(256, 3) k_tile_lean(Geom g, FieldSpec fs, TileGeo tg, const unsigned *offsets,
-                                                      const float4 *recs, const float *recw,
-                                                      unsigned long long capacity, GridPtrs grids, DevStats *st) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int stn = blockIdx.y;
-  float *sm = (float *)smraw;
-  const size_t tile_bytes = ((size_t)NF * tg.slot * sizeof(float) + 15) & ~(size_t)15;
-  float4 *XY = (float4 *)(smraw + tile_bytes) + warp * (LEAN_RB * 9);
-  float2 *ZZ = (float2 *)((float4 *)(smraw + tile_bytes) + (blockDim.x >> 5) * (LEAN_RB * 9)) + warp * (LEAN_RB * 3);
+// by k_edge_fixup). One CTA per tile; shared memory holds the tile of every grid slot, both
+// stencils, unpadded [tx][ty][tz], as int32 fixed point with a per-tile power-of-two scale, so
+// every deposit is one native integer shared-memory atomic. Lane = record: each thread reads one
+// record, derives its taps once per stencil and adds the K^3 products, so a record is read once
+// and nothing is staged. The cells are converted back to FP32 when the tile is written. The
+// particle's home tile counts it in NGRID.
+template <int K, int NF, bool IL>
+__global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileGeo tg, const unsigned *offsets,
+                                                     const float4 *recs, const float *recw,
+                                                     unsigned long long capacity, GridPtrs grids, DevStats *st) {
+  extern __shared__ __align__(16) int smi[];
+  constexpr int NS = IL ? 2 : 1;
+  const int tsz = tg.tx * tg.ty * tg.tz;
+  const int pyz = tg.ty * tg.tz;
   const int tile = blockIdx.x;
   const int bz = tile % tg.nbz, by = (tile / tg.nbz) % tg.nby, bx = tile / (tg.nbz * tg.nby);
   const int x0 = bx * tg.tx, y0 = by * tg.ty, z0 = bz * tg.tz;
   const int ex = min(tg.tx, g.nx - x0), ey = min(tg.ty, g.ny - y0), ez = min(tg.tz, g.nz - z0);
-  for (int c = threadIdx.x; c < NF * tg.slot; c += blockDim.x) sm[c] = 0.0f;
+  int4 *sm4 = reinterpret_cast<int4 *>(smi);
+  for (int c = threadIdx.x; c < (NS * NF * tsz) >> 2; c += blockDim.x) sm4[c] = make_int4(0, 0, 0, 0);
   __syncthreads();
-  constexpr int NT = K * K * K;
-  const bool tap_on = lane < NT;
-  const int txy = tap_on ? (lane / (K * K)) * 3 + (lane / K) % K : 0, tz = tap_on ? lane % K : 0;
   float f_grid = 0.0f;
   unsigned rb = offsets[tile], re = offsets[tile + 1];
   if (re > capacity) re = (unsigned)capacity;
   if (rb > re) rb = re;
-  const int nwarps = blockDim.x >> 5;
-  for (unsigned base = rb + warp * LEAN_RB; base < re; base += nwarps * LEAN_RB) {
-    const unsigned r = base + lane;
-    const int cnt = min((unsigned)LEAN_RB, re - base);
-    if (lane < LEAN_RB) {
-      float wx[3] = {0, 0, 0}, wy[3] = {0, 0, 0}, wz[3] = {0, 0, 0};
-      int ox[3] = {0, 0, 0}, oy[3] = {0, 0, 0}, oz[3] = {0, 0, 0};
-      float va = 0.0f, vb = 0.0f;
-      if (r < re) {
-        const float4 rec = recs[r];
-        const float w = recw ? recw[r] : 1.0f;
-        if (stn == 0 && home_of(g, tg, rec.x, rec.y, rec.z) == tile && accept32(g, rec.x, rec.y, rec.z)) f_grid += w;
-        va = w;
-        vb = w;
-        for (int e = 0; e < fs.ea; e++) va *= rec.w;
-        for (int e = 0; e < fs.eb; e++) vb *= rec.w;
-        const float sx = stn ? __fadd_rn(rec.x, 0.5f) : rec.x, sy = stn ? __fadd_rn(rec.y, 0.5f) : rec.y,
-                    sz = stn ? __fadd_rn(rec.z, 0.5f) : rec.z;
-        if (accept32(g, sx, sy, sz)) {
-          AxisTapsF ax, ay, az;
-          axis32k<K>(sx, 0, g.nx, g.los, ax);
-          axis32k<K>(sy, 1, g.ny, g.los, ay);
-          axis32k<K>(sz, 1, g.nz, g.los, az);
-          stage_axis32(ax, x0, ex, tg.px, wx, ox);
-          stage_axis32(ay, y0, ey, tg.py, wy, oy);
-          stage_axis32(az, z0, ez, 1, wz, oz);
-        }
-      }
-      float4 *xy = XY + lane * 9;
-#pragma unroll
-      for (int a = 0; a < 3; a++)
-#pragma unroll
-        for (int b2 = 0; b2 < 3; b2++) {
-          const float wxy = wx[a] * wy[b2];
-          xy[a * 3 + b2] = make_float4(va * wxy, vb * wxy, __int_as_float(ox[a] + oy[b2]), 0.0f);
-        }
-      float2 *zz = ZZ + lane * 3;
-#pragma unroll
-      for (int c = 0; c < 3; c++) zz[c] = make_float2(wz[c], __int_as_float(oz[c]));
+  // pre-pass over the tile's records: sum |w v^e| per field (the records stay in L1 for the deposits)
+  __shared__ float red_abs[2][32];
+  {
+    float la = 0.0f, lb = 0.0f;
+    for (unsigned r = rb + threadIdx.x; r < re; r += blockDim.x) {
+      const float4 rec = recs[r];
+      const float w = recw ? recw[r] : 1.0f;
+      float va = w, vb = w;
+      for (int e = 0; e < fs.ea; e++) va *= rec.w;
+      for (int e = 0; e < fs.eb; e++) vb *= rec.w;
+      la += fabsf(va);
+      lb += fabsf(vb);
     }
-    __syncwarp();
-    float *sA = sm, *sB = sm + tg.slot;
-    for (int j = 0; j < cnt; j++) {
-      const float4 e = XY[j * 9 + txy];
-      const float2 f = ZZ[j * 3 + tz];
-      if (tap_on && f.x != 0.0f && (e.x != 0.0f || e.y != 0.0f)) {
-        const int off = __float_as_int(e.z) + __float_as_int(f.y);
-        atomicAdd(sA + off, e.x * f.x);
-        if (NF == 2) atomicAdd(sB + off, e.y * f.x);
-      }
+    la = warp_sum_f(la);
+    lb = warp_sum_f(lb);
+    if ((threadIdx.x & 31) == 0) {
+      red_abs[0][threadIdx.x >> 5] = la;
+      red_abs[1][threadIdx.x >> 5] = lb;
     }
-    __syncwarp();
-  }
-  if (stn == 0) {
-    const double vals[1] = {(double)f_grid};
-    double *const dst[1] = {&st->ngrid};
-    block_add<1>(vals, dst);
-  } else {
     __syncthreads();
   }
-  // write the stencil's slots: pairs of cells along z as float2 (8-byte aligned global rows)
-  const int tsz = tg.tx * tg.ty * tg.tz;
+  float ta = 0.0f, tb = 0.0f;
+  for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+    ta += red_abs[0][k];
+    tb += red_abs[1][k];
+  }
+  const int SA = tile_scale_exp(ta), SB = tile_scale_exp(tb);
+  const float scA = ldexpf(1.0f, SA), scB = ldexpf(1.0f, SB);
+  for (unsigned r = rb + threadIdx.x; r < re; r += blockDim.x) {
+    const float4 rec = recs[r];
+    const float w = recw ? recw[r] : 1.0f;
+    if (home_of(g, tg, rec.x, rec.y, rec.z) == tile && accept32(g, rec.x, rec.y, rec.z)) f_grid += w;
+    float va = w, vb = w;
+    for (int e = 0; e < fs.ea; e++) va *= rec.w;
+    for (int e = 0; e < fs.eb; e++) vb *= rec.w;
+    va *= scA;
+    vb *= scB;
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+      const float sx = s ? __fadd_rn(rec.x, 0.5f) : rec.x, sy = s ? __fadd_rn(rec.y, 0.5f) : rec.y,
+                  sz = s ? __fadd_rn(rec.z, 0.5f) : rec.z;
+      if (!accept32(g, sx, sy, sz)) continue;
+      AxisTapsF ax, ay, az;
+      axis32k<K>(sx, 0, g.nx, g.los, ax);
+      axis32k<K>(sy, 1, g.ny, g.los, ay);
+      axis32k<K>(sz, 1, g.nz, g.los, az);
+      float wx[3], wy[3], wz[3];
+      int ox[3], oy[3], oz[3];
+      stage_axis32(ax, x0, ex, pyz, wx, ox);
+      stage_axis32(ay, y0, ey, tg.tz, wy, oy);
+      stage_axis32(az, z0, ez, 1, wz, oz);
+      int *sA = smi + (s * NF) * tsz;
+#pragma unroll
+      for (int a = 0; a < K; a++)
+#pragma unroll
+        for (int b2 = 0; b2 < K; b2++) {
+          const float wxy = wx[a] * wy[b2];
+          const float pa = va * wxy, pb = vb * wxy;
+          const int oxy = ox[a] + oy[b2];
+#pragma unroll
+          for (int c = 0; c < K; c++) {
+            if (wxy != 0.0f && wz[c] != 0.0f) {
+              atomicAdd(sA + oxy + oz[c], __float2int_rn(pa * wz[c]));
+              if (NF == 2) atomicAdd(sA + tsz + oxy + oz[c], __float2int_rn(pb * wz[c]));
+            }
+          }
+        }
+    }
+  }
+  {
+    const double vals[1] = {(double)f_grid};
+    double *const dst[1] = {&st->ngrid};
+    block_add<1>(vals, dst);  // ends with a barrier: the tiles are complete
+  }
+  // write every slot: pairs of cells along z as float2 (8-byte aligned global rows)
   const int npair = tsz >> 1;
-  for (int f = 0; f < NF; f++) {
-    const int slot = stn * NF + f;
+  for (int slot = 0; slot < NS * NF; slot++) {
     float *gp = (float *)grids.g[slot];
-    const float *sl = sm + f * tg.slot;
+    const int *sl = smi + slot * tsz;
+    const float inv = ldexpf(1.0f, -((slot % NF) == 0 ? SA : SB));
     float dsum = 0.0f;
     for (int q = threadIdx.x; q < npair; q += blockDim.x) {
       const int c = q << 1;
       const int rz = c & (tg.tz - 1), ly = (c >> tg.lz) & (tg.ty - 1), lx = c >> (tg.lz + tg.ly);
       if (lx >= ex || ly >= ey || rz >= ez) continue;
-      const int sidx = lx * tg.px + ly * tg.py + rz;
-      const float v0 = sl[sidx], v1 = sl[sidx + 1];
-      dsum += v0 + (rz + 1 < ez ? v1 : 0.0f);
+      const int2 iv = *reinterpret_cast<const int2 *>(sl + c);
+      const float2 v = make_float2((float)iv.x * inv, (float)iv.y * inv);
       float *dst = gp + (long long)(x0 + lx) * g.slice + (long long)(y0 + ly) * g.row + z0 + rz;
-      if (rz + 1 < ez) *reinterpret_cast<float2 *>(dst) = make_float2(v0, v1);
-      else dst[0] = v0;
+      if (rz + 1 < ez) {
+        dsum += v.x + v.y;
+        *reinterpret_cast<float2 *>(dst) = v;
+      } else {
+        dsum += v.x;
+        dst[0] = v.x;
+      }
     }
     const double vals[1] = {(double)dsum};
     double *const dst1[1] = {&st->dc[slot]};
@@ -900,10 +921,7 @@ size_t tile_smem_bytes(const TileGeo &tg, int nslots, int deterministic) {
   return tile + stage;
 }
 
-size_t lean_smem_bytes(const TileGeo &tg, int nf) {
-  const size_t tile = ((size_t)nf * tg.slot * 4 + 15) & ~(size_t)15;
-  return tile + (size_t)(256 / 32) * LEAN_RB * (9 * 16 + 3 * 8);
-}
+size_t rec_smem_bytes(const TileGeo &tg, int nslots) { return (size_t)nslots * tg.tx * tg.ty * tg.tz * 4; }
 
 double tile_dup_estimate(const Geom &g, const TileGeo &tg) {
   // a footprint spans 4 (TSC, CIC) or 2 (NN) cells plus the margin; it crosses into the next tile
@@ -912,20 +930,25 @@ double tile_dup_estimate(const Geom &g, const TileGeo &tg) {
   return (1.0 + (span - 1.0) / tg.tx) * (1.0 + (span - 1.0) / tg.ty) * (1.0 + (span - 1.0) / tg.tz);
 }
 
-template <int K, int NF>
-static void launch_lean(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, const PaintBufs &b,
-                        bool weights, const GridPtrs &grids, DevStats *st) {
-  const size_t smem = lean_smem_bytes(tg, NF);
-  cudaFuncSetAttribute(k_tile_lean<K, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_tile_lean<K, NF><<<dim3(tg.ntiles, g.interlace ? 2 : 1), 256, smem, s>>>(
-      g, fs, tg, b.offsets, b.recs, weights ? b.recw : nullptr, b.capacity, grids, st);
+template <int K, int NF, bool IL>
+static void launch_rec(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, const PaintBufs &b,
+                       bool weights, const GridPtrs &grids, DevStats *st) {
+  const size_t smem = rec_smem_bytes(tg, NF * (IL ? 2 : 1));
+  cudaFuncSetAttribute(k_tile_rec<K, NF, IL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_tile_rec<K, NF, IL><<<tg.ntiles, 256, smem, s>>>(g, fs, tg, b.offsets, b.recs, weights ? b.recw : nullptr,
+                                                     b.capacity, grids, st);
 }
 
 template <int K>
-static void launch_lean_nf(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, const PaintBufs &b,
-                           bool weights, const GridPtrs &grids, DevStats *st) {
-  if (fs.nfields == 2) launch_lean<K, 2>(s, g, fs, tg, b, weights, grids, st);
-  else launch_lean<K, 1>(s, g, fs, tg, b, weights, grids, st);
+static void launch_rec_k(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, const PaintBufs &b,
+                         bool weights, const GridPtrs &grids, DevStats *st) {
+  if (fs.nfields == 2) {
+    if (g.interlace) launch_rec<K, 2, true>(s, g, fs, tg, b, weights, grids, st);
+    else launch_rec<K, 2, false>(s, g, fs, tg, b, weights, grids, st);
+  } else {
+    if (g.interlace) launch_rec<K, 1, true>(s, g, fs, tg, b, weights, grids, st);
+    else launch_rec<K, 1, false>(s, g, fs, tg, b, weights, grids, st);
+  }
 }
 
 template <typename T>
@@ -949,9 +972,9 @@ static void run_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, cons
     *launches += 4;
   } else {
     const bool wts = in.w != nullptr;
-    if (g.order == 3) launch_lean_nf<3>(s, g, fs, tg, b, wts, grids, st);
-    else if (g.order == 2) launch_lean_nf<2>(s, g, fs, tg, b, wts, grids, st);
-    else launch_lean_nf<1>(s, g, fs, tg, b, wts, grids, st);
+    if (g.order == 3) launch_rec_k<3>(s, g, fs, tg, b, wts, grids, st);
+    else if (g.order == 2) launch_rec_k<2>(s, g, fs, tg, b, wts, grids, st);
+    else launch_rec_k<1>(s, g, fs, tg, b, wts, grids, st);
     k_edge_fixup<T><<<152 * 2, 128, 0, s>>>(g, fs, in, b.edge_list, b.edge_count, grids, st);
     *launches += 5;
   }

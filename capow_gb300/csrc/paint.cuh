@@ -65,5 +65,5 @@ void launch_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, const Ti
 // suggested tile geometry for a grid (and whether two fields are painted)
 TileGeo choose_tiles(const Geom &g, int nslots, int deterministic);
 size_t tile_smem_bytes(const TileGeo &tg, int nslots, int deterministic);
-size_t lean_smem_bytes(const TileGeo &tg, int nf);
+size_t rec_smem_bytes(const TileGeo &tg, int nslots);
 double tile_dup_estimate(const Geom &g, const TileGeo &tg);
