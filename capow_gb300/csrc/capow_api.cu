@@ -181,6 +181,9 @@ extern "C" int capow_create(const capow_params *p, const capow_options *opt, cap
   }
   for (int k = 0; k < 4; k++) CK(c, cudaEventCreate(&c->ev[k]));
   c->g = make_geom(*p);
+  if (c->prec != CAPOW_FP64 && !(c->g.margin < 0.25f))  // FP32 positions cannot resolve the cells
+    FAIL(c, CAPOW_ENOTSUP, "box coordinates too large for FP32 cell positions (error margin %.3g cells); use FP64",
+         (double)c->g.margin);
   plan_fields(c);
   const bool f64 = c->prec == CAPOW_FP64;
   const size_t eb = f64 ? 8 : 4;

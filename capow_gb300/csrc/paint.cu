@@ -185,19 +185,20 @@ __device__ __forceinline__ Prep prep32(const Geom &g, const FieldSpec &fs, const
 // A particle within the FP32 error margin of a point where the reference's deposit changes
 // discontinuously (box faces 0 and N, anything outside [0, N], the TSC low-tap drop at 0.5, the
 // TSC LOS==0 x shift at 1, every cell edge for NN) is painted by the exact FP64 rules.
+// (Bitwise logic throughout: every test is cheap, so evaluating all of them beats branching.)
 __device__ __forceinline__ bool edge1(float s, int n, int order, float m) {
   const float nf = (float)n;
-  bool e = !(s >= m && s <= nf - m) || (fabsf(s - 0.5f) < m) || (fabsf(s - 1.0f) < m);
-  if (order == 1) e = e || (fabsf(s - rintf(s)) < m);
+  bool e = !(s >= m) | !(s <= nf - m) | (fabsf(s - 0.5f) < m) | (fabsf(s - 1.0f) < m);
+  if (order == 1) e |= (fabsf(s - rintf(s)) < m);
   return e;
 }
 
 __device__ __forceinline__ bool is_edge(const Geom &g, float sx, float sy, float sz) {
-  bool e = edge1(sx, g.nx, g.order, g.margin) || edge1(sy, g.ny, g.order, g.margin) ||
+  bool e = edge1(sx, g.nx, g.order, g.margin) | edge1(sy, g.ny, g.order, g.margin) |
            edge1(sz, g.nz, g.order, g.margin);
   if (g.interlace)
-    e = e || edge1(__fadd_rn(sx, 0.5f), g.nx, g.order, g.margin) ||
-        edge1(__fadd_rn(sy, 0.5f), g.ny, g.order, g.margin) || edge1(__fadd_rn(sz, 0.5f), g.nz, g.order, g.margin);
+    e |= edge1(__fadd_rn(sx, 0.5f), g.nx, g.order, g.margin) | edge1(__fadd_rn(sy, 0.5f), g.ny, g.order, g.margin) |
+         edge1(__fadd_rn(sz, 0.5f), g.nz, g.order, g.margin);
   return e;
 }
 
@@ -208,11 +209,12 @@ struct AxisTiles {
 };
 
 __device__ __forceinline__ void add_tile(AxisTiles &a, int v) {
-  if ((a.n > 0 && v == a.t0) || (a.n > 1 && v == a.t1) || (a.n > 2 && v == a.t2)) return;
-  if (a.n == 0) a.t0 = v;
-  else if (a.n == 1) a.t1 = v;
-  else a.t2 = v;
-  a.n = a.n < 3 ? a.n + 1 : 3;
+  const bool dup = ((a.n > 0) & (v == a.t0)) | ((a.n > 1) & (v == a.t1)) | ((a.n > 2) & (v == a.t2));
+  const bool put = !dup;
+  a.t0 = (put & (a.n == 0)) ? v : a.t0;
+  a.t1 = (put & (a.n == 1)) ? v : a.t1;
+  a.t2 = (put & (a.n >= 2)) ? v : a.t2;
+  a.n = (put & (a.n < 3)) ? a.n + 1 : a.n;
 }
 
 __device__ __forceinline__ int tile_at(const AxisTiles &a, int k) { return k == 0 ? a.t0 : (k == 1 ? a.t1 : a.t2); }
@@ -236,22 +238,31 @@ __device__ __forceinline__ bool axis_range(float s, int n, bool wrap, int order,
     return lo <= hi;
   }
   const int span = hi - lo;
-  while (lo < 0) lo += n;
-  while (lo >= n) lo -= n;
+  // s > -4 and margin < 0.25 give -6 <= lo <= n + 2, and n >= 4: these corrections bring lo into [0, n)
+  lo += lo < 0 ? n : 0;
+  lo += lo < 0 ? n : 0;
+  lo -= lo >= n ? n : 0;
   hi = lo + span;  // cells beyond n - 1 wrap when used
   return true;
 }
 
+// The tiles of the cells lo..hi (hi may pass n - 1 on a wrapping axis): the piece inside the grid
+// covers tiles lo >> shift .. min(hi, n - 1) >> shift, the wrapped piece 0 .. (hi - n) >> shift.
 __device__ __forceinline__ bool axis_footprint(float s, int n, int shift, bool wrap, int order, float m,
                                                AxisTiles &T) {
   T.n = 0;
   T.t0 = T.t1 = T.t2 = 0;
   int lo, hi;
   if (!axis_range(s, n, wrap, order, m, lo, hi)) return false;
-  for (int c = lo; c <= hi; c++) {
-    int cc = c;
-    while (cc >= n) cc -= n;
-    add_tile(T, cc >> shift);
+  const int top = hi < n - 1 ? hi : n - 1;
+  const int a0 = lo >> shift, a1 = top >> shift;  // a1 - a0 <= 2: the footprint spans at most 6 cells
+  T.t0 = a0;
+  T.t1 = a0 + 1;
+  T.t2 = a0 + 2;
+  T.n = a1 - a0 + 1;
+  if (hi >= n) {  // the wrapped piece (rare: a periodic axis near its last cell)
+    const int wtop = hi - n < n - 1 ? hi - n : n - 1;
+    for (int t = 0; t <= (wtop >> shift); t++) add_tile(T, t);
   }
   return true;
 }
@@ -303,55 +314,95 @@ __device__ __forceinline__ void decode(const Geom &g, long long L, int &ix, int 
   iz = (int)(r - (long long)iy * g.row);
 }
 
+// Warp-aggregated tile counters over runs: consecutive lanes naming the same tile form a run and
+// share one atomic, issued by the run's first lane (particles that arrive in spatial order form
+// long runs; any order stays correct). Every lane of the warp must call this; lanes with key < 0
+// take no slot. Returns the lane's slot: the counter's old value plus its offset in the run.
+__device__ __forceinline__ unsigned warp_run_add(unsigned *counter, int key, bool want_slot) {
+  const int lane = threadIdx.x & 31;
+  const int prev = __shfl_up_sync(FULL_MASK, key, 1);
+  const unsigned heads = __ballot_sync(FULL_MASK, lane == 0 || key != prev);
+  const unsigned after = heads & ~((2u << lane) - 1u);  // run heads above this lane (0 for lane 31)
+  const int head = 31 - __clz(heads & ((2u << lane) - 1u));
+  unsigned base = 0;
+  if (head == lane && key >= 0) base = atomicAdd(counter + key, (unsigned)((after ? __ffs(after) - 1 : 32) - lane));
+  if (!want_slot) return 0;
+  base = __shfl_sync(FULL_MASK, base, head);
+  return base + (unsigned)(lane - head);
+}
+
+// Tile id of the lane's (a, b, c)-th footprint tile, or -1 when the lane has none there.
+__device__ __forceinline__ int tile_key(const TileGeo &tg, bool has, const AxisTiles &TX, const AxisTiles &TY,
+                                        const AxisTiles &TZ, int a, int b, int c) {
+  const int id = tile_id(tg, tile_at(TX, a), tile_at(TY, b), tile_at(TZ, c));
+  return (has & (a < TX.n) & (b < TY.n) & (c < TZ.n)) ? id : -1;
+}
+
 // Pass 1: tile counts; statistics that need no exact decision (reads, velocity moments, the
 // fixed-point bound); particles whose footprint misses the grid (outside the box, rejected).
+// The particle loop is warp-uniform (lanes past n take part without a particle) so the tile counters
+// can be aggregated over runs of lanes: particles that arrive in spatial order share their tiles.
 template <typename T>
 __global__ void __launch_bounds__(256) k_count(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in, long long n,
                                                unsigned *counts, DevStats *st, int split_edge) {
-  float f_read = 0, f_out = 0, f_nsq = 0, f_v[4] = {0, 0, 0, 0}, f_abs[2] = {0, 0};
+  float f_read = 0, f_out = 0, f_nsq = 0, f_v[4] = {0, 0, 0, 0}, f_abs[2] = {0, 0}, f_grid = 0;
   int fatal = 0, nonfin = 0;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
-    const Prep p = prep32(g, fs, in, i);
-    if (!p.fin) {
-      nonfin = 1;
-      continue;
-    }
-    f_read += 1.0f;
-    if (fs.moments) {  // src/read_data.c:132-138, every particle read
-      f_nsq += p.w;
-      float wv = p.w * p.v;
-      f_v[0] += wv; wv *= p.v;
-      f_v[1] += wv; wv *= p.v;
-      f_v[2] += wv; wv *= p.v;
-      f_v[3] += wv;
-    }
-    float pa = p.w, pb = p.w;
-    for (int e = 0; e < fs.ea; e++) pa *= p.v;
-    for (int e = 0; e < fs.eb; e++) pb *= p.v;
-    f_abs[0] += fabsf(pa);
-    f_abs[1] += fabsf(pb);
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); i0 < n; i0 += stride) {
+    const long long i = i0 + (threadIdx.x & 31);
+    bool has = false;
     AxisTiles TX, TY, TZ;
-    if (!footprint(g, tg, p.sx, p.sy, p.sz, TX, TY, TZ)) {
-      f_out += 1.0f;  // outside the box by at least two cells (src/read_data.c:81-88)
-      if (g.los == 0) {
-        fatal = 1;
-        atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)i);
+    TX.n = TY.n = TZ.n = 0;
+    if (i < n) {
+      const Prep p = prep32(g, fs, in, i);
+      if (!p.fin) {
+        nonfin = 1;
+      } else {
+        f_read += 1.0f;
+        if (fs.moments) {  // src/read_data.c:132-138, every particle read
+          f_nsq += p.w;
+          float wv = p.w * p.v;
+          f_v[0] += wv; wv *= p.v;
+          f_v[1] += wv; wv *= p.v;
+          f_v[2] += wv; wv *= p.v;
+          f_v[3] += wv;
+        }
+        float pa = p.w, pb = p.w;
+        for (int e = 0; e < fs.ea; e++) pa *= p.v;
+        for (int e = 0; e < fs.eb; e++) pb *= p.v;
+        f_abs[0] += fabsf(pa);
+        f_abs[1] += fabsf(pb);
+        if (!footprint(g, tg, p.sx, p.sy, p.sz, TX, TY, TZ)) {
+          f_out += 1.0f;  // outside the box by at least two cells (src/read_data.c:81-88)
+          if (g.los == 0) {
+            fatal = 1;
+            atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)i);
+          }
+        } else if (split_edge && is_edge(g, p.sx, p.sy, p.sz)) {
+          // painted and counted by k_edge_fixup
+        } else {
+          has = true;
+          // NGRID (src/read_data.c:92-126): exact for particles away from every edge
+          if (split_edge && accept32(g, p.sx, p.sy, p.sz)) f_grid += p.w;
+        }
       }
-      continue;
     }
-    if (split_edge && is_edge(g, p.sx, p.sy, p.sz)) continue;  // painted by k_edge_fixup
-    for (int a = 0; a < TX.n; a++)
-      for (int b = 0; b < TY.n; b++)
-        for (int c = 0; c < TZ.n; c++)
-          atomicAdd(counts + tile_id(tg, tile_at(TX, a), tile_at(TY, b), tile_at(TZ, c)), 1u);
+    const int na = __reduce_max_sync(FULL_MASK, has ? TX.n : 0), nb = __reduce_max_sync(FULL_MASK, has ? TY.n : 0),
+              nc = __reduce_max_sync(FULL_MASK, has ? TZ.n : 0);
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+          if (a < na && b < nb && c < nc) warp_run_add(counts, tile_key(tg, has, TX, TY, TZ, a, b, c), false);
   }
   // FP32 per-thread partials over ~n/(grid threads) particles, FP64 across threads
-  const double vals[9] = {(double)f_read, (double)f_out, (double)f_nsq, (double)f_v[0], (double)f_v[1],
-                          (double)f_v[2], (double)f_v[3], (double)f_abs[0], (double)f_abs[1]};
-  double *const dst[9] = {&st->nread, &st->nout, &st->nsq, &st->vr[0], &st->vr[1], &st->vr[2], &st->vr[3],
-                          &st->absw[0], &st->absw[1]};
-  block_add<9>(vals, dst);
+  const double vals[10] = {(double)f_read, (double)f_out, (double)f_nsq, (double)f_v[0], (double)f_v[1],
+                           (double)f_v[2], (double)f_v[3], (double)f_abs[0], (double)f_abs[1], (double)f_grid};
+  double *const dst[10] = {&st->nread, &st->nout, &st->nsq, &st->vr[0], &st->vr[1], &st->vr[2], &st->vr[3],
+                           &st->absw[0], &st->absw[1], &st->ngrid};
+  block_add<10>(vals, dst);
   if (fatal) atomicOr(&st->fatal, 1);
   if (nonfin) atomicOr(&st->nonfinite, 1);
 }
@@ -396,32 +447,49 @@ __global__ void __launch_bounds__(1024) k_scan(const unsigned *counts, int ntile
 #define SPECIAL_MARK (-3.0e38f)
 
 // Pass 3: scatter particles into their tiles' lists. A record holds the normal-stencil scales and
-// the velocity, or, for a particle taking the exact rules, a mark and the particle index.
+// the velocity, or, for a particle taking the exact rules, a mark and the particle index. Same
+// warp-uniform loop and run aggregation of the tile cursors as k_count.
 template <typename T>
 __global__ void __launch_bounds__(256) k_scatter(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in, long long n,
                                                  unsigned *cursor, float4 *recs, float *recw,
                                                  unsigned long long capacity, unsigned *edge_list,
                                                  unsigned *edge_count) {
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
-    const Prep p = prep32(g, fs, in, i);
-    if (!p.fin) continue;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); i0 < n; i0 += stride) {
+    const long long i = i0 + (threadIdx.x & 31);
+    bool has = false;
     AxisTiles TX, TY, TZ;
-    if (!footprint(g, tg, p.sx, p.sy, p.sz, TX, TY, TZ)) continue;
-    const bool edge = is_edge(g, p.sx, p.sy, p.sz);
-    if (edge && edge_list) {  // painted by k_edge_fixup after the tiles
-      edge_list[atomicAdd(edge_count, 1u)] = (unsigned)i;
-      continue;
+    TX.n = TY.n = TZ.n = 0;
+    float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
+    float w = 1.0f;
+    if (i < n) {
+      const Prep p = prep32(g, fs, in, i);
+      if (p.fin && footprint(g, tg, p.sx, p.sy, p.sz, TX, TY, TZ)) {
+        const bool edge = is_edge(g, p.sx, p.sy, p.sz);
+        if (edge && edge_list) {  // painted by k_edge_fixup after the tiles
+          edge_list[atomicAdd(edge_count, 1u)] = (unsigned)i;
+        } else {
+          has = true;
+          w = p.w;
+          rec = edge ? make_float4(SPECIAL_MARK, __uint_as_float((unsigned)i), 0.0f, 0.0f)
+                     : make_float4(p.sx, p.sy, p.sz, p.v);
+        }
+      }
     }
-    const float4 rec = edge ? make_float4(SPECIAL_MARK, __uint_as_float((unsigned)i), 0.0f, 0.0f)
-                            : make_float4(p.sx, p.sy, p.sz, p.v);
-    for (int a = 0; a < TX.n; a++)
-      for (int b = 0; b < TY.n; b++)
-        for (int c = 0; c < TZ.n; c++) {
-          const unsigned slot = atomicAdd(cursor + tile_id(tg, tile_at(TX, a), tile_at(TY, b), tile_at(TZ, c)), 1u);
-          if (slot < capacity) {
+    const int na = __reduce_max_sync(FULL_MASK, has ? TX.n : 0), nb = __reduce_max_sync(FULL_MASK, has ? TY.n : 0),
+              nc = __reduce_max_sync(FULL_MASK, has ? TZ.n : 0);
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          if (!(a < na && b < nb && c < nc)) continue;  // warp-uniform
+          const int key = tile_key(tg, has, TX, TY, TZ, a, b, c);
+          const unsigned slot = warp_run_add(cursor, key, true);
+          if (key >= 0 && slot < capacity) {
             recs[slot] = rec;
-            if (recw) recw[slot] = p.w;
+            if (recw) recw[slot] = w;
           }
         }
   }
@@ -703,8 +771,8 @@ __device__ __forceinline__ int tile_scale_exp(float sum_abs) {
 // stencils, unpadded [tx][ty][tz], as int32 fixed point with a per-tile power-of-two scale, so
 // every deposit is one native integer shared-memory atomic. Lane = record: each thread reads one
 // record, derives its taps once per stencil and adds the K^3 products, so a record is read once
-// and nothing is staged. The cells are converted back to FP32 when the tile is written. The
-// particle's home tile counts it in NGRID.
+// and nothing is staged. The cells are converted back to FP32 when the tile is written. (NGRID of
+// these particles is counted by k_count.)
 template <int K, int NF, bool IL>
 __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileGeo tg, const unsigned *offsets,
                                                      const float4 *recs, const float *recw,
@@ -720,7 +788,6 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
   int4 *sm4 = reinterpret_cast<int4 *>(smi);
   for (int c = threadIdx.x; c < (NS * NF * tsz) >> 2; c += blockDim.x) sm4[c] = make_int4(0, 0, 0, 0);
   __syncthreads();
-  float f_grid = 0.0f;
   unsigned rb = offsets[tile], re = offsets[tile + 1];
   if (re > capacity) re = (unsigned)capacity;
   if (rb > re) rb = re;
@@ -755,7 +822,6 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
   for (unsigned r = rb + threadIdx.x; r < re; r += blockDim.x) {
     const float4 rec = recs[r];
     const float w = recw ? recw[r] : 1.0f;
-    if (home_of(g, tg, rec.x, rec.y, rec.z) == tile && accept32(g, rec.x, rec.y, rec.z)) f_grid += w;
     float va = w, vb = w;
     for (int e = 0; e < fs.ea; e++) va *= rec.w;
     for (int e = 0; e < fs.eb; e++) vb *= rec.w;
@@ -793,11 +859,7 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
         }
     }
   }
-  {
-    const double vals[1] = {(double)f_grid};
-    double *const dst[1] = {&st->ngrid};
-    block_add<1>(vals, dst);  // ends with a barrier: the tiles are complete
-  }
+  __syncthreads();
   // write every slot: pairs of cells along z as float2 (8-byte aligned global rows)
   const int npair = tsz >> 1;
   for (int slot = 0; slot < NS * NF; slot++) {
@@ -954,7 +1016,9 @@ static void launch_rec_k(cudaStream_t s, const Geom &g, const FieldSpec &fs, con
 template <typename T>
 static void run_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, int det, PIn<T> in,
                         long long n, const GridPtrs &grids, const PaintBufs &b, DevStats *st, long long *launches) {
-  const int th = 256, nb = grid_blocks(n, th) * 2;
+  const int th = 256;
+  long long nbl = (n + th - 1) / th;
+  const int nb = (int)(nbl < 1 ? 1 : (nbl > 152 * 8 ? 152 * 8 : nbl));  // one resident wave of 256-thread blocks
   const bool split = !det;  // FP32: edge particles go to k_edge_fixup; deterministic: exact rules in the tiles
   cudaMemsetAsync(b.counts, 0, sizeof(unsigned) * tg.ntiles, s);
   if (split) cudaMemsetAsync(b.edge_count, 0, sizeof(unsigned), s);
