@@ -34,6 +34,7 @@ OK, EINVAL, ENOMEM, ECUDA, EBOUNDS, ETIMEOUT, ESTATE, ECUFFT, ENOTSUP = range(9)
 FP64, FP32_MIXED, FP32_DETERMINISTIC = 0, 1, 2
 SPEC_REFERENCE, SPEC_DD, SPEC_DP, SPEC_PP = 0, 1, 2, 4
 F32, F64 = 0, 1
+FFT_AUTO, FFT_3D = 0, 1
 PRECISIONS = {"fp64": FP64, "fp32": FP32_MIXED, "det": FP32_DETERMINISTIC}
 
 
@@ -58,7 +59,7 @@ class _Params(ctypes.Structure):
 
 class _Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("spectra", ctypes.c_int), ("device", ctypes.c_int),
-                ("stream", ctypes.c_void_p), ("reserved", ctypes.c_int * 8)]
+                ("stream", ctypes.c_void_p), ("fft_path", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
 
 
 class _Particles(ctypes.Structure):
@@ -218,18 +219,21 @@ class PowerSpectrum:
     """One capow context: paint a catalogue, then P_l(k) for the requested spectra.
 
     precision: "fp32" (FP32-mixed, default), "fp64" (plain double path), "det" (int64 fixed-point grids).
+    fft_path:  "auto" (fused x-axis FFT + binning where it applies) or "3d" (3-D cuFFT + binning kernel).
     spectra:   None -> one spectrum chosen by params.Momentum (one reference run); or any of
                ("dd", "dp", "pp") computed from one paint and one set of FFTs.
     """
 
-    def __init__(self, params: Params, precision: str = "fp32", spectra=None, device: int = 0, stream=None):
+    def __init__(self, params: Params, precision: str = "fp32", spectra=None, device: int = 0, stream=None,
+                 fft_path: str = "auto"):
         self.params = params
         self._pc = params.to_c()
         mask = 0
         for s in (spectra or []):
             mask |= {"dd": SPEC_DD, "dp": SPEC_DP, "pp": SPEC_PP}[s]
         self.spectra_mask = mask
-        opt = _Options(PRECISIONS[precision], mask, device, ctypes.c_void_p(stream or 0))
+        opt = _Options(PRECISIONS[precision], mask, device, ctypes.c_void_p(stream or 0),
+                       {"auto": FFT_AUTO, "3d": FFT_3D}[fft_path])
         self._ctx = ctypes.c_void_p()
         rc = lib().capow_create(ctypes.byref(self._pc), ctypes.byref(opt), ctypes.byref(self._ctx))
         if rc != OK:

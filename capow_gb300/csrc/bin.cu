@@ -149,6 +149,16 @@ int build_bin_tables(const capow_params &p, const Geom &g, int precision, BinTab
   t.E = upload(E, allocs, s);
   t.Elo = upload(Elo, allocs, s);
   t.Ehi = upload(Ehi, allocs, s);
+  t.twx = nullptr;
+  if (nx >= 2 && (nx & (nx - 1)) == 0) {  // twiddles of the fused x-axis FFT (forward, sign -1)
+    std::vector<float2> tw(nx);
+    for (int q = 0; q < nx; q++) {
+      const double a = -2.0 * M_PI * (double)q / (double)nx;
+      tw[q] = make_float2((float)cos(a), (float)sin(a));
+    }
+    t.twx = upload(tw, allocs, s);
+    if (!t.twx) return 1;
+  }
   return (t.E && t.Elo && t.Ehi && t.ezf) ? 0 : 1;
 }
 
@@ -332,6 +342,10 @@ __global__ void __launch_bounds__(256) k_bin(BinParams bp, BinTables t, const ty
 
   const long long cols = (long long)bp.ny * bp.nzc;
   const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  // DC values converted once per thread (for R = float each conversion is an FP64-pipe slot)
+  const int nsl = NF * (bp.interlace ? 2 : 1);
+  const R dc0 = (R)dcv[0], dc1 = nsl > 1 ? (R)dcv[1] : (R)0, dc2 = nsl > 2 ? (R)dcv[2] : (R)0,
+          dc3 = nsl > 3 ? (R)dcv[3] : (R)0;
   if (col < cols) {
     const int j = (int)(col / bp.nzc), k = (int)(col - (long long)j * bp.nzc);
     // per-column constants
@@ -414,20 +428,20 @@ __global__ void __launch_bounds__(256) k_bin(BinParams bp, BinTables t, const ty
       e.x = ex.x * eyz.x - ex.y * eyz.y;
       e.y = ex.x * eyz.y + ex.y * eyz.x;
       C A = gA[off];
-      if (dc) { A.x = (R)dcv[0]; A.y = (R)0; }
+      if (dc) { A.x = dc0; A.y = (R)0; }
       C B;
       if (NF == 2) {
         B = gB[off];
-        if (dc) { B.x = (R)dcv[1]; B.y = (R)0; }
+        if (dc) { B.x = dc1; B.y = (R)0; }
       }
       if (bp.interlace) {
         C a = gAi[off];
-        if (dc) { a.x = (R)dcv[NF]; a.y = (R)0; }
+        if (dc) { a.x = NF == 2 ? dc2 : dc1; a.y = (R)0; }
         A.x += a.x * e.x - a.y * e.y;
         A.y += a.x * e.y + a.y * e.x;
         if (NF == 2) {
           C b2 = gBi[off];
-          if (dc) { b2.x = (R)dcv[NF + 1]; b2.y = (R)0; }
+          if (dc) { b2.x = dc3; b2.y = (R)0; }
           B.x += b2.x * e.x - b2.y * e.y;
           B.y += b2.x * e.y + b2.y * e.x;
         }
@@ -501,6 +515,352 @@ __global__ void __launch_bounds__(256) k_bin(BinParams bp, BinTables t, const ty
       const R v = sb2[c];
       if (v != (R)0) atomicAdd(&bins2d[c], (double)v);
     }
+}
+
+// ------------------------------------------------------------ fused x-axis FFT + binning (FP32)
+// cuFFT has transformed every x-plane of every grid over (y, z); what is left of the 3-D transform
+// (src/main.c:266-271) is the length-NX DFT along x of every (ky, kz) column, and its only consumer
+// is the binning (src/main.c:302-468). One pass does both: a CTA loads a block of columns into
+// shared memory, transforms them along x there and bins the modes from there, so the x-transformed
+// grids never go to HBM. Columns whose smallest |k| lies beyond the top k-bin edge are not loaded.
+//
+// Shared layout of a block: row x (the position along x) holds ncol complex values, column
+// c = slot * kc + (kz - k0) stored at c ^ (x & (ncol - 1)): a row is contiguous for the loads and
+// the FFT, and the XOR spreads the rows the binning reads at once over the banks.
+struct XbinSmem {
+  unsigned sd, sb, sE, sElo, sEhi, total;
+};
+
+CAPOW_HD XbinSmem xbin_smem_layout(int n, int ncol, int np, int nl, int nk) {
+  XbinSmem L;
+  unsigned o = 0;
+  L.sd = o;   o = align16(o + 8u * (unsigned)n * ncol);
+  L.sb = o;   o = align16(o + 4u * np * nl * nk);
+  L.sE = o;   o = align16(o + 8u * (nk + 3));
+  L.sElo = o; o = align16(o + 4u * (nk + 3));
+  L.sEhi = o; o = align16(o + 4u * (nk + 3));
+  L.total = o;
+  return L;
+}
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cmul_mi(float2 a) { return make_float2(a.y, -a.x); }  // a * (-i)
+
+// In-place DIF butterflies of one stage, forward sign. Inputs a[q] at span/R spacing; outputs X[p]
+// (p in natural order) times the twiddle w^(p*j) are written back at position p.
+__device__ __forceinline__ void dft8(float2 *a) {
+  const float h = 0.70710678118654752f;
+  float2 b0 = cadd(a[0], a[4]), b4 = csub(a[0], a[4]);
+  float2 b1 = cadd(a[1], a[5]), t5 = csub(a[1], a[5]);
+  float2 b2 = cadd(a[2], a[6]), t6 = csub(a[2], a[6]);
+  float2 b3 = cadd(a[3], a[7]), t7 = csub(a[3], a[7]);
+  const float2 b5 = make_float2((t5.x + t5.y) * h, (t5.y - t5.x) * h);    // * e^{-i pi/4}
+  const float2 b6 = cmul_mi(t6);                                           // * e^{-i pi/2}
+  const float2 b7 = make_float2((t7.y - t7.x) * h, -(t7.x + t7.y) * h);   // * e^{-3i pi/4}
+  const float2 c0 = cadd(b0, b2), c2 = csub(b0, b2), c1 = cadd(b1, b3), c3 = cmul_mi(csub(b1, b3));
+  const float2 c4 = cadd(b4, b6), c6 = csub(b4, b6), c5 = cadd(b5, b7), c7 = cmul_mi(csub(b5, b7));
+  a[0] = cadd(c0, c1);
+  a[4] = csub(c0, c1);
+  a[2] = cadd(c2, c3);
+  a[6] = csub(c2, c3);
+  a[1] = cadd(c4, c5);
+  a[5] = csub(c4, c5);
+  a[3] = cadd(c6, c7);
+  a[7] = csub(c6, c7);
+}
+
+__device__ __forceinline__ void dft4(float2 *a) {
+  const float2 b0 = cadd(a[0], a[2]), b2 = csub(a[0], a[2]), b1 = cadd(a[1], a[3]), b3 = cmul_mi(csub(a[1], a[3]));
+  a[0] = cadd(b0, b1);
+  a[2] = csub(b0, b1);
+  a[1] = cadd(b2, b3);
+  a[3] = csub(b2, b3);
+}
+
+template <int R>
+__device__ __forceinline__ void xfft_stage(float2 *sd, const float2 *__restrict__ tw, int n, int ncol, int log2ncol,
+                                           int span, int log2q, int twstep) {
+  const int Q = span / R;
+  const int nbf = ncol * (n / R);
+  for (int u = threadIdx.x; u < nbf; u += blockDim.x) {
+    const int c = u & (ncol - 1), v = u >> log2ncol;
+    const int b = v >> log2q, jj = v & (Q - 1);
+    const int base = b * span + jj;
+    float2 a[R];
+#pragma unroll
+    for (int q = 0; q < R; q++) {
+      const int row = base + q * Q;
+      a[q] = sd[row * ncol + (c ^ (row & (ncol - 1)))];
+    }
+    if (R == 8) dft8(a);
+    else if (R == 4) dft4(a);
+    else {
+      const float2 t0 = a[0];
+      a[0] = cadd(t0, a[1]);
+      a[1] = csub(t0, a[1]);
+    }
+#pragma unroll
+    for (int p = 0; p < R; p++) {
+      float2 y = a[p];
+      if (p > 0 && jj > 0) y = cmulf(y, __ldg(tw + ((p * jj * twstep) & (n - 1))));
+      const int row = base + p * Q;
+      sd[row * ncol + (c ^ (row & (ncol - 1)))] = y;
+    }
+  }
+}
+
+// Position along x, after the in-place DIF stages (log2n / 3 of radix 8, then one of radix
+// 2^(log2n % 3) when that is not 1), of frequency index i: its base-8 digits reversed.
+__device__ __forceinline__ int xfft_pos(int log2n, int i) {
+  int pos = 0, shift = log2n, rem = i;
+  for (int st = 0; st < log2n / 3; st++) {
+    shift -= 3;
+    pos += (rem & 7) << shift;
+    rem >>= 3;
+  }
+  return pos + rem;  // the last digit has span 1
+}
+
+template <int NF, bool IL, bool ODD>
+__global__ void __launch_bounds__(256) k_xfft_bin(BinParams bp, BinTables t, XbinGeo xg, const float2 *g0,
+                                                  const float2 *g1, const float2 *g2, const float2 *g3,
+                                                  const double *dcv, double *bins) {
+  constexpr int NS = NF * (IL ? 2 : 1);
+  constexpr int NP = NF == 1 ? 1 : 4;
+  constexpr int NL = ODD ? 5 : 3;  // stored multipoles: l = 0, 2, 4 (+ 1, 3)
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int n = 1 << xg.log2n, ncol = xg.ncol, kc_n = xg.kc, nk = bp.nk;
+  const XbinSmem L = xbin_smem_layout(n, ncol, NP, NL, nk);
+  float2 *sd = (float2 *)(smraw + L.sd);
+  float *sb = (float *)(smraw + L.sb);
+  double *sE = (double *)(smraw + L.sE);
+  float *sElo = (float *)(smraw + L.sElo);
+  float *sEhi = (float *)(smraw + L.sEhi);
+  for (int c = threadIdx.x; c < NP * NL * nk; c += blockDim.x) sb[c] = 0.0f;
+  for (int c = threadIdx.x; c < nk + 3; c += blockDim.x) {
+    sE[c] = t.E[c];
+    sElo[c] = t.Elo[c];
+    sEhi[c] = t.Ehi[c];
+  }
+  const float topf32 = (float)t.E[nk + 1] * 1.0001f;
+  // DC values of the slots, converted once (a conversion from FP64 costs an FP64-pipe slot)
+  const float dcf0 = (float)dcv[0], dcf1 = NS > 1 ? (float)dcv[1] : 0.0f, dcf2 = NS > 2 ? (float)dcv[2] : 0.0f,
+              dcf3 = NS > 3 ? (float)dcv[3] : 0.0f;
+  const int tpc = blockDim.x >> xg.log2kc;       // threads per column
+  const int mpt = n / tpc > 0 ? n / tpc : 1;      // modes (kx) per thread
+  const int my_kc = threadIdx.x / tpc, my_ch = threadIdx.x - my_kc * tpc;
+  for (int blk = blockIdx.x; blk < xg.nblocks; blk += gridDim.x) {
+    const int j = blk / xg.nkb, k0 = (blk - j * xg.nkb) * kc_n;
+    // every mode of the block has s >= fy^2 + fz(k0)^2: skip the block when that is clearly beyond
+    // the top edge (a block kept near the edge only costs work; each mode is tested exactly)
+    if (t.fy2f[j] + t.fz2f[k0] > topf32) continue;
+    __syncthreads();  // the previous block's binning has read sd
+    for (int idx = threadIdx.x; idx < n * ncol; idx += blockDim.x) {
+      const int c = idx & (ncol - 1), x = idx >> xg.log2ncol;
+      const int sl = c >> xg.log2kc, kz = k0 + (c & (kc_n - 1));
+      float2 v = make_float2(0.0f, 0.0f);
+      const float2 *g = sl == 0 ? g0 : (sl == 1 ? g1 : (sl == 2 ? g2 : g3));
+      if (sl < NS && kz < bp.nzc) v = g[((long long)x * bp.ny + j) * bp.nzc + kz];
+      sd[x * ncol + (c ^ (x & (ncol - 1)))] = v;
+    }
+    __syncthreads();
+    int log2span = xg.log2n;
+    while (log2span >= 3) {  // radix-8 stages
+      xfft_stage<8>(sd, t.twx, n, ncol, xg.log2ncol, 1 << log2span, log2span - 3, n >> log2span);
+      __syncthreads();
+      log2span -= 3;
+    }
+    if (log2span == 2) xfft_stage<4>(sd, t.twx, n, ncol, xg.log2ncol, 4, 0, n >> 2);
+    else if (log2span == 1) xfft_stage<2>(sd, t.twx, n, ncol, xg.log2ncol, 2, 0, n >> 1);
+    __syncthreads();
+    // ---- binning (the math of k_bin, src/main.c:355-449), one run of consecutive kx per thread
+    const int kz = k0 + my_kc;
+    if (kz < bp.nzc && my_ch * mpt < n) {
+      const float syz = t.fy2f[j] + t.fz2f[kz];
+      float cyz = t.cyf[j] * t.czf[kz];
+      if (IL) cyz *= 0.25f;
+      float2 eyz = make_float2(0.0f, 0.0f);
+      if (IL) eyz = cmulf(t.eyf[j], t.ezf[kz]);
+      const float flos_yz = bp.los == 2 ? t.fyf[j] : t.fzf[kz];
+      const float topf = sElo[nk + 1] - syz;
+      const int r = topf > 0.0f ? min(bp.xhalf, (int)(sqrtf(topf) / bp.fx_step) + 1) : -1;
+      // this thread's kx run [i0, i0 + mpt) lies in [0, xhalf) or in [xhalf, NX) (xhalf is a multiple
+      // of mpt); keep its modes with i <= r or i >= NX - r (r <= xhalf; the others can not reach the
+      // top bin): a prefix of a run in the first half, a suffix in the second
+      const int i0 = my_ch * mpt;
+      int m_lo = 0, m_hi = mpt;
+      if (i0 < bp.xhalf) m_hi = min(mpt, r + 1 - i0);
+      else m_lo = max(0, bp.nx - r - i0);
+      float acc[NP][NL];
+#pragma unroll
+      for (int qq = 0; qq < NP; qq++)
+#pragma unroll
+        for (int l = 0; l < NL; l++) acc[qq][l] = 0.0f;
+      int cur = -2;  // no bin yet: the first mode bisects the edges, later ones walk from the last
+      float lo = 1.0f, hi = 0.0f;
+      for (int m = m_lo; m < m_hi; m++) {
+        const int i = i0 + m;
+        const float s = t.fx2f[i] + syz;
+        if (!(s >= lo && s < hi)) {
+          int b = cur;
+          if (b == -2) {  // sElo[a] <= s < sElo[z] (sElo[0] = -inf, sElo[nk + 2] = +inf)
+            int a = 0, z = nk + 2;
+            while (z - a > 1) {
+              const int mid = (a + z) >> 1;
+              if (sElo[mid] <= s) a = mid;
+              else z = mid;
+            }
+            b = a - 1;
+          }
+          while (b < nk && s >= sElo[b + 2]) b++;
+          while (b > -1 && s < sEhi[b + 1]) b--;
+          if (s >= sElo[b + 1] && s < sEhi[b + 2]) {
+            lo = sElo[b + 1];
+            hi = sEhi[b + 2];
+          } else {  // within a few ulps of an edge: the exact FP64 s decides
+            const double sd2 = __dadd_rn(__dadd_rn(t.fx2d[i], t.fy2d[j]), t.fz2d[kz]);
+            b = exact_bin(sE, nk, sd2, b);
+            lo = 1.0f;
+            hi = 0.0f;
+          }
+          if (b != cur) {
+            if (cur >= 0 && cur < nk) {
+#pragma unroll
+              for (int qq = 0; qq < NP; qq++)
+#pragma unroll
+                for (int l = 0; l < NL; l++) {
+                  if (acc[qq][l] != 0.0f) atomicAdd(&sb[(qq * NL + l) * nk + cur], acc[qq][l]);
+                  acc[qq][l] = 0.0f;
+                }
+            }
+            cur = b;
+          }
+        }
+        if (cur < 0 || cur >= nk) continue;
+        const int row = xfft_pos(xg.log2n, i);
+        const int rb = row * ncol, sw = row & (ncol - 1);
+        const bool dc = (i == 0 && j == 0 && kz == 0);
+        float2 A = sd[rb + ((0 * kc_n + my_kc) ^ sw)];
+        if (dc) A = make_float2(dcf0, 0.0f);
+        float2 B = make_float2(0.0f, 0.0f);
+        if (NF == 2) {
+          B = sd[rb + ((1 * kc_n + my_kc) ^ sw)];
+          if (dc) B = make_float2(dcf1, 0.0f);
+        }
+        if (IL) {
+          const float2 e = cmulf(t.exf[i], eyz);
+          float2 a = sd[rb + ((NF * kc_n + my_kc) ^ sw)];
+          if (dc) a = make_float2(NF == 2 ? dcf2 : dcf1, 0.0f);
+          A = cadd(A, cmulf(a, e));
+          if (NF == 2) {
+            float2 b2 = sd[rb + (((NF + 1) * kc_n + my_kc) ^ sw)];
+            if (dc) b2 = make_float2(dcf3, 0.0f);
+            B = cadd(B, cmulf(b2, e));
+          }
+        }
+        const float gc = cyz * t.cxf[i] * (float)herm_nm(i, j, kz, bp.xhalf);
+        const float fl = bp.los == 1 ? t.fxf[i] : flos_yz;
+        const float mu = s > 0.0f ? fl * rsqrtf(s) : 0.0f;
+        const float mu2 = mu * mu;
+        const float L2 = 1.5f * mu2 - 0.5f;
+        const float L4 = (4.375f * mu2 - 3.75f) * mu2 + 0.375f;
+        float P[NP];
+        P[0] = (A.x * A.x + A.y * A.y) * gc;
+        if (NF == 2) {
+          P[1] = (A.x * B.x + A.y * B.y) * gc;
+          P[2] = (A.x * B.y - A.y * B.x) * gc;
+          P[3] = (B.x * B.x + B.y * B.y) * gc;
+        }
+#pragma unroll
+        for (int qq = 0; qq < NP; qq++) {
+          acc[qq][0] += P[qq];
+          acc[qq][1] += P[qq] * L2;
+          acc[qq][2] += P[qq] * L4;
+          if (ODD) {
+            acc[qq][NL - 2] += P[qq] * mu;
+            acc[qq][NL - 1] += P[qq] * ((2.5f * mu2 - 1.5f) * mu);
+          }
+        }
+      }
+      if (cur >= 0 && cur < nk) {
+#pragma unroll
+        for (int qq = 0; qq < NP; qq++)
+#pragma unroll
+          for (int l = 0; l < NL; l++)
+            if (acc[qq][l] != 0.0f) atomicAdd(&sb[(qq * NL + l) * nk + cur], acc[qq][l]);
+      }
+    }
+  }
+  __syncthreads();
+  // CTA bins -> global FP64 bins [product][5][nk]; stored multipole index -> l
+  for (int c = threadIdx.x; c < NP * NL * nk; c += blockDim.x) {
+    const float v = sb[c];
+    if (v == 0.0f) continue;
+    const int b = c % nk, ql = c / nk, qq = ql / NL, li = ql - qq * NL;
+    const int l = li == 0 ? 0 : (li == 1 ? 2 : (li == 2 ? 4 : (li == 3 ? 1 : 3)));
+    atomicAdd(&bins[(qq * 5 + l) * nk + b], (double)v);
+  }
+}
+
+static int ilog2i(int v) {
+  int l = 0;
+  while ((1 << l) < v) l++;
+  return l;
+}
+
+bool xbin_plan(const BinParams &bp, int nslot, XbinGeo &xg) {
+  const int n = bp.nx;
+  if (n < 16 || n > 2048 || (n & (n - 1)) != 0 || bp.out2d) return false;
+  memset(&xg, 0, sizeof xg);
+  xg.log2n = ilog2i(n);
+  xg.ncol = n <= 512 ? 16 : (n == 1024 ? 8 : 4);
+  if (nslot > xg.ncol) return false;
+  xg.log2ncol = ilog2i(xg.ncol);
+  const int ns = nslot == 3 ? 4 : nslot;
+  xg.kc = xg.ncol / ns;
+  xg.log2kc = ilog2i(xg.kc);
+  xg.nkb = (bp.nzc + xg.kc - 1) / xg.kc;
+  xg.nblocks = bp.ny * xg.nkb;
+  const int np = bp.nfields == 1 ? 1 : 4, nl = bp.odd ? 5 : 3;
+  return xbin_smem_layout(n, xg.ncol, np, nl, bp.nk).total <= 100 * 1024;
+}
+
+template <int NF, bool IL, bool ODD>
+static void launch_xbin_t(cudaStream_t s, const BinParams &bp, const BinTables &t, const XbinGeo &xg,
+                          void *const slots[4], const double *dcv, double *bins) {
+  constexpr int NP = NF == 1 ? 1 : 4, NL = ODD ? 5 : 3;
+  const size_t smem = xbin_smem_layout(1 << xg.log2n, xg.ncol, NP, NL, bp.nk).total;
+  cudaFuncSetAttribute(k_xfft_bin<NF, IL, ODD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_xfft_bin<NF, IL, ODD>, 256, smem);
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  int grid = (per_sm > 0 ? per_sm : 1) * nsm;
+  if (grid > xg.nblocks) grid = xg.nblocks;
+  k_xfft_bin<NF, IL, ODD><<<grid, 256, smem, s>>>(bp, t, xg, (const float2 *)slots[0], (const float2 *)slots[1],
+                                                  (const float2 *)slots[2], (const float2 *)slots[3], dcv, bins);
+}
+
+void launch_xbin(cudaStream_t s, const BinParams &bp, const BinTables &t, const XbinGeo &xg, void *const slots[4],
+                 const double *dcv, double *bins, long long *launches) {
+  const bool il = bp.interlace != 0, odd = bp.odd != 0;
+  if (bp.nfields == 2) {
+    if (il) odd ? launch_xbin_t<2, true, true>(s, bp, t, xg, slots, dcv, bins)
+            : launch_xbin_t<2, true, false>(s, bp, t, xg, slots, dcv, bins);
+    else odd ? launch_xbin_t<2, false, true>(s, bp, t, xg, slots, dcv, bins)
+             : launch_xbin_t<2, false, false>(s, bp, t, xg, slots, dcv, bins);
+  } else {
+    if (il) odd ? launch_xbin_t<1, true, true>(s, bp, t, xg, slots, dcv, bins)
+            : launch_xbin_t<1, true, false>(s, bp, t, xg, slots, dcv, bins);
+    else odd ? launch_xbin_t<1, false, true>(s, bp, t, xg, slots, dcv, bins)
+             : launch_xbin_t<1, false, false>(s, bp, t, xg, slots, dcv, bins);
+  }
+  (*launches)++;
 }
 
 void launch_mode_counts(cudaStream_t s, const BinParams &bp, const BinTables &t, unsigned long long *nmodes,

@@ -28,6 +28,13 @@ struct BinTables {
   // merged k-bin edges E[0..NK] in s (bin b iff E[b] <= s < E[b+1]) and FP32 safe edges
   double *E;
   float *Elo, *Ehi;  // E[b]*(1+eps), E[b]*(1-eps) rounded outward/inward: safe FP32 tests
+  float2 *twx;       // exp(-2 pi i q / NX), q < NX (fused x-axis FFT; power-of-two NX only)
+};
+
+// Geometry of the fused x-axis FFT + binning pass (k_xfft_bin): blocks of `ncol` columns of the
+// (y, z)-transformed grids, `kc` consecutive kz of one ky in each of the nslot grids.
+struct XbinGeo {
+  int log2n, ncol, log2ncol, kc, log2kc, nkb, nblocks;
 };
 
 struct BinParams {
@@ -55,6 +62,13 @@ void launch_bin(cudaStream_t s, int precision, const BinParams &bp, const BinTab
                 const double *dcv, double *bins, double *bins2d, long long *launches);
 // products accumulated by the bin kernel: 1 for one field, 4 (|A|^2, Re A*B, Im A*B, |B|^2) for two
 int bin_products(int nfields);
+
+// Fused path: plan for a grid (returns false when NX is not a power of two in [16, 2048], the 2-D
+// bins are requested, or the shared-memory bins do not fit), and its launcher. The slots hold the
+// (y, z)-transformed grids: [NX][NY][NZ/2+1] complex, x in real space.
+bool xbin_plan(const BinParams &bp, int nslot, XbinGeo &xg);
+void launch_xbin(cudaStream_t s, const BinParams &bp, const BinTables &t, const XbinGeo &xg, void *const slots[4],
+                 const double *dcv, double *bins, long long *launches);
 // DC corrections: dcv[slot] = painted sum (minus NGRID for mean-subtracted field A slots)
 void launch_dc_prepare(cudaStream_t s, const void *st, int deterministic, int nslot, int nfields, int mean_sub_a,
                        const double *fixed_scale, double *dcv, long long *launches);

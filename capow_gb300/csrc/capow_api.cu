@@ -229,6 +229,18 @@ extern "C" int capow_create(const capow_params *p, const capow_options *opt, cap
     CK(c, cudaMemcpyAsync(c->nmodes2d.data(), c->nmodes2d_d, sizeof(unsigned long long) * n2d,
                           cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
+  // FP32 with a power-of-two NX: cuFFT transforms every x-plane over (y, z), and k_xfft_bin does the
+  // x axis together with the binning (CAPOW_FFT_3D keeps the 3-D transform and k_bin)
+  c->fused = !f64 && o.fft_path != CAPOW_FFT_3D && c->bt.twx && xbin_plan(bp, c->nslot, c->xg);
+  if (c->fused) {
+    int n2[2] = {p->NY, p->NZ};
+    int in2[2] = {p->NY, 2 * bp.nzc}, on2[2] = {p->NY, bp.nzc};
+    CKFFT(c, cufftPlanMany(&c->plan, 2, n2, in2, 1, p->NY * 2 * bp.nzc, on2, 1, p->NY * bp.nzc, CUFFT_R2C,
+                           p->NX * c->nslot));
+    c->plan_ok = true;
+    CKFFT(c, cufftSetStream(c->plan, c->stream));
+    return CAPOW_OK;
+  }
   // one batched in-place r2c plan over all painted grids (replaces the fftw_execute calls,
   // src/main.c:266-271): forward, unnormalised, padded last dimension
   int n[3] = {p->NX, p->NY, p->NZ};
@@ -410,6 +422,22 @@ static int enqueue_power(capow_ctx *c) {
   const bool f64 = c->prec == CAPOW_FP64;
   launch_dc_prepare(c->stream, c->st, c->prec == CAPOW_FP32_DETERMINISTIC, c->nslot, c->fs.nfields,
                     c->bp.mean_sub_a, c->fixed_scale, c->dcv, &c->launches);
+  if (c->fused) {
+    CKFFT(c, cufftExecR2C(c->plan, (cufftReal *)c->grid_base, (cufftComplex *)c->grid_base));
+    CK(c, cudaEventRecord(c->ev[2], c->stream));
+    const int nk = c->p.NK;
+    CK(c, cudaMemsetAsync(c->bins, 0, sizeof(double) * NPROD * 5 * nk, c->stream));
+    void *slots[4];
+    GridPtrs gp = grid_ptrs(c);
+    for (int k = 0; k < 4; k++) slots[k] = gp.g[k];
+    launch_xbin(c->stream, c->bp, c->bt, c->xg, slots, c->dcv, c->bins, &c->launches);
+    CK(c, cudaGetLastError());
+    CK(c, cudaEventRecord(c->ev[3], c->stream));
+    CK(c, cudaMemcpyAsync(c->h_bins, c->bins, sizeof(double) * bin_products(c->fs.nfields) * 5 * nk,
+                          cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaMemcpyAsync(c->h_st, c->st, sizeof(DevStats), cudaMemcpyDeviceToHost, c->stream));
+    return CAPOW_OK;
+  }
   if (c->grid_elems > 0x7fffffffULL) {
     const size_t eb = f64 ? 8 : 4;
     for (int s = 0; s < c->nslot; s++) {

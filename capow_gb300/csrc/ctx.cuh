@@ -39,6 +39,8 @@ struct capow_ctx {
   std::vector<unsigned long long> nmodes, nmodes2d;
   cufftHandle plan;
   bool plan_ok;
+  bool fused;           // FP32: 2-D (y, z) cuFFT + fused x-axis FFT and binning (k_xfft_bin)
+  XbinGeo xg;
   // staging for host particle input
   void *stage[5];
   size_t stage_bytes[5];

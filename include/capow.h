@@ -82,8 +82,16 @@ typedef struct capow_options {
   int spectra;   /* CAPOW_SPEC_REFERENCE, or an OR of CAPOW_SPEC_DD|DP|PP (one paint, one set of FFTs) */
   int device;    /* CUDA device ordinal */
   void *stream;  /* cudaStream_t to run on, or NULL for a stream owned by the context */
-  int reserved[8];
+  int fft_path;  /* CAPOW_FFT_AUTO or CAPOW_FFT_3D (below) */
+  int reserved[7];
 } capow_options;
+
+/* FFT and binning path (capow_options.fft_path). AUTO: FP32 contexts with a power-of-two NX in
+ * [16, 2048] and no 2-D output transform each x-plane over (y, z) with cuFFT and do the x axis
+ * together with the binning in one kernel; everything else, or 3D, runs the full 3-D cuFFT
+ * transform and a separate binning kernel. Both give the same spectra within FP32 rounding. */
+#define CAPOW_FFT_AUTO 0
+#define CAPOW_FFT_3D 1
 
 /* particle input: structure of arrays */
 #define CAPOW_F32 0

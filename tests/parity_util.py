@@ -67,10 +67,10 @@ def oracle_run(po, parts, momentum):
     return out
 
 
-def gpu_run(pc, parts, precision, spectra=None, grids=False):
+def gpu_run(pc, parts, precision, spectra=None, grids=False, fft_path="auto"):
     x, y, z, vx, vy, vz = parts
     v = vlos_of(pc.LOS, vx, vy, vz)
-    with cg.PowerSpectrum(pc, precision=precision, spectra=spectra) as ps:
+    with cg.PowerSpectrum(pc, precision=precision, spectra=spectra, fft_path=fft_path) as ps:
         ps.paint(x, y, z, v)
         st = ps.stats()
         g = None

@@ -44,6 +44,31 @@ def test_reference_run_parity(gpu, precision, order, los, il, mom):
     assert_spectrum(r, raw, norm0, precision, odd=True, label=label)
 
 
+FUSED = [(3, 3, 1, 1, 1, 64, 48, 40), (3, 0, 1, 0, 0, 128, 24, 30), (2, 3, 0, 2, 1, 64, 40, 48),
+         (1, 0, 0, 1, 0, 16, 20, 18), (3, 1, 1, 1, 1, 256, 16, 12), (2, 2, 1, 0, 1, 2048, 8, 6)]
+
+
+@pytest.mark.parametrize("precision", ["fp32", "det"])
+@pytest.mark.parametrize("order,los,il,mom,odd,nx,ny,nz", FUSED)
+def test_fused_x_fft_bin_parity(gpu, precision, order, los, il, mom, odd, nx, ny, nz):
+    """Power-of-two NX: (y, z) cuFFT + the fused x-axis FFT and binning, against the oracle and
+    against the 3-D cuFFT + binning kernel path on the same paint."""
+    kw = dict(BASE, Odd_Multipoles=odd)
+    po, pc = params_pair(NX=nx, NY=ny, NZ=nz, InterpOrder=order, LOS=los, DoInterlacing=il, Momentum=mom, **kw)
+    parts = particles(po, 4000, seed=300 + nx + order * 7 + mom)
+    ref = oracle_run(po, parts, mom)
+    res, _, _, _ = gpu_run(pc, parts, precision)
+    res3, _, _, _ = gpu_run(pc, parts, precision, fft_path="3d")
+    label = f"fused {precision} nx={nx} order={order} los={los} il={il} mom={mom} odd={odd}"
+    raw = ref["raw"]
+    if mom == 1:
+        norm0 = np.sqrt(np.abs(oracle_run(po, parts, 0)["raw"]["Pk0"] * oracle_run(po, parts, 2)["raw"]["Pk0"]))
+    else:
+        norm0 = np.abs(raw["Pk0"])
+    assert_spectrum(res[0], raw, norm0, precision, odd=bool(odd), label=label)
+    assert_spectrum(res[0], res3[0], norm0, precision, odd=bool(odd), label=label + " vs 3d")
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_combined_spectra_equal_three_reference_runs(gpu, precision):
     """dd, dp, pp from one paint equal Momentum 0, 1, 2 reference runs."""
