@@ -465,6 +465,7 @@ __global__ void __launch_bounds__(256) k_bin(BinParams bp, BinTables t, const ty
       }
 #pragma unroll
       for (int q = 0; q < NP; q++) {
+        if (!(bp.pmask & (1 << q))) continue;  // a product no requested spectrum reads
         acc[q][0] += P[q];
         acc[q][2] += P[q] * L2;
         acc[q][4] += P[q] * L4;
@@ -777,6 +778,7 @@ __global__ void __launch_bounds__(256) k_xfft_bin(BinParams bp, BinTables t, Xbi
         }
 #pragma unroll
         for (int qq = 0; qq < NP; qq++) {
+          if (!(bp.pmask & (1 << qq))) continue;  // a product no requested spectrum reads
           acc[qq][0] += P[qq];
           acc[qq][1] += P[qq] * L2;
           acc[qq][2] += P[qq] * L4;

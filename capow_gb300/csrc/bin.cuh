@@ -43,6 +43,7 @@ struct BinParams {
   int nspec, nfields;
   SpecDef spec[CAPOW_MAX_SPEC];
   int mean_sub_a;           // field A had the mean subtracted (DC correction)
+  int pmask;                // products the spectra read (bit q: |A|^2, Re A*B, Im A*B, |B|^2)
   double two_pi;
   float fx_step;            // x frequency spacing 1/((float)NX*dx) (src/main.c:329), for per-column x ranges
 };

@@ -94,6 +94,11 @@ static Geom make_geom(const capow_params &p) {
   return g;
 }
 
+// Product of one spectrum in the bin kernels' [product][5][NK] sums: |A|^2, Re(A*B), Im(A*B), |B|^2.
+static int spectrum_product(int nfields, const SpecDef &sd) {
+  return nfields == 1 ? 0 : (sd.x == sd.y ? (sd.x == 0 ? 0 : 3) : (sd.imag ? 2 : 1));
+}
+
 // Fields and spectra of a run (src/read_data.c:91-130, src/main.c:141-148, 214, 406-441).
 static void plan_fields(capow_ctx *c) {
   const int m = c->p.Momentum;
@@ -142,6 +147,8 @@ static void plan_fields(capow_ctx *c) {
   }
   fs.moments = c->moments;
   fs.need_v = fs.moments || c->p.LOS != 0 || fs.ea > 0 || (fs.nfields == 2 && fs.eb > 0);
+  bp.pmask = 0;
+  for (int q = 0; q < bp.nspec; q++) bp.pmask |= 1 << spectrum_product(fs.nfields, bp.spec[q]);
   c->nslot = fs.nfields * (c->p.DoInterlacing ? 2 : 1);
 }
 
@@ -509,8 +516,7 @@ extern "C" int capow_power(capow_ctx *c, capow_spectrum *out, int nout) {
     capow_spectrum &s = out[q];
     const int m = c->shot_moment[q];
     // product of this spectrum in the kernel's [product][5][NK] bins: |A|^2, Re(A*B), Im(A*B), |B|^2
-    const SpecDef &sd = c->bp.spec[q];
-    const int pq = c->fs.nfields == 1 ? 0 : (sd.x == sd.y ? (sd.x == 0 ? 0 : 3) : (sd.imag ? 2 : 1));
+    const int pq = spectrum_product(c->fs.nfields, c->bp.spec[q]);
     s.shot = m == 0 ? N : vr[m] * N;
     s.norm = norm;
     s.alpha = alpha;
