@@ -73,6 +73,11 @@ class _Stats(ctypes.Structure):
                 ("nsq", ctypes.c_double), ("vr", ctypes.c_double * 4), ("first_out_of_box", ctypes.c_int64)]
 
 
+class _Grads(ctypes.Structure):
+    _fields_ = [("on_device", ctypes.c_int), ("dtype", ctypes.c_int), ("dx", ctypes.c_void_p), ("dy", ctypes.c_void_p),
+                ("dz", ctypes.c_void_p), ("dvlos", ctypes.c_void_p), ("dw", ctypes.c_void_p)]
+
+
 class _Spectrum(ctypes.Structure):
     _fields_ = [("pk", ctypes.POINTER(ctypes.c_double) * 5), ("nmodes", ctypes.POINTER(ctypes.c_int64)),
                 ("pk2d", ctypes.POINTER(ctypes.c_double)), ("nmodes2d", ctypes.POINTER(ctypes.c_int64)),
@@ -85,7 +90,7 @@ EXPORTS = [
     "capow_create", "capow_paint", "capow_get_stats", "capow_power", "capow_normalise", "capow_num_spectra",
     "capow_copy_grid", "capow_stage_ms", "capow_kernel_launches", "capow_destroy", "capow_read_params",
     "capow_read_catalogue", "capow_free", "capow_write_output", "capow_bin_centre", "capow_strerror",
-    "capow_last_error", "capow_paint_noalloc",
+    "capow_last_error", "capow_paint_noalloc", "capow_backward",
 ]
 
 _lib = None
@@ -106,6 +111,7 @@ def lib() -> ctypes.CDLL:
     L.capow_paint.argtypes = [vp, ctypes.POINTER(_Particles)]
     L.capow_paint_noalloc.argtypes = [vp, ctypes.POINTER(_Particles)]
     L.capow_get_stats.argtypes = [vp, ctypes.POINTER(_Stats)]
+    L.capow_backward.argtypes = [vp, ctypes.POINTER(ctypes.POINTER(ctypes.c_double) * 5), ctypes.POINTER(_Grads)]
     L.capow_power.argtypes = [vp, ctypes.POINTER(_Spectrum), ip]
     L.capow_normalise.argtypes = [P, ctypes.POINTER(_Spectrum)]
     L.capow_num_spectra.argtypes = [vp]
@@ -328,6 +334,31 @@ class PowerSpectrum:
                 d["Nmodes_2D"] = n2[:n2d]
             out.append(d)
         return out
+
+    def backward(self, dL_dP: dict, out=None) -> dict:
+        """capow_backward: gradients of a loss with respect to the last painted catalogue.
+
+        dL_dP maps "Pk0".."Pk4" to arrays of NK (missing keys: zero). Returns a dict of float64
+        host arrays dx, dy, dz, dvlos, dw; or pass `out`, a dict of contiguous device arrays
+        (torch tensors) of the particles' dtype, to receive them on the device."""
+        p = self.params
+        arrs = [np.ascontiguousarray(dL_dP.get(f"Pk{l}", np.zeros(p.NK)), dtype=np.float64) for l in range(5)]
+        ptrs = (ctypes.POINTER(ctypes.c_double) * 5)(*[a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+                                                        for a in arrs])
+        names = ("dx", "dy", "dz", "dvlos", "dw")
+        if out is not None:
+            t = next(iter(out.values()))
+            code = F64 if "float64" in str(t.dtype) else F32
+            g = _Grads(1, code, *[out[k].data_ptr() if k in out else None for k in names])
+            self._check(lib().capow_backward(self._ctx, ptrs, ctypes.byref(g)), "capow_backward")
+            return out
+        keep = self._keep[0]
+        n = len(keep)
+        dt = np.float64 if ("float64" in str(keep.dtype)) else np.float32
+        host = {k: np.zeros(n, dtype=dt) for k in names}
+        g = _Grads(0, F64 if dt == np.float64 else F32, *[host[k].ctypes.data for k in names])
+        self._check(lib().capow_backward(self._ctx, ptrs, ctypes.byref(g)), "capow_backward")
+        return {k: v.astype(np.float64) for k, v in host.items()}
 
     def normalise(self, raw: dict) -> dict:
         """capow_normalise (output_power arithmetic) on a copy of one raw spectrum."""

@@ -346,6 +346,15 @@ static int enqueue_paint(capow_ctx *c, const capow_particles &d) {
   return CAPOW_OK;
 }
 
+int enqueue_backward_paint(capow_ctx *c) {
+  int rc = enqueue_paint(c, c->last);
+  if (rc) return rc;
+  launch_dc_prepare(c->stream, c->st, c->prec == CAPOW_FP32_DETERMINISTIC, c->nslot, c->fs.nfields,
+                    c->bp.mean_sub_a, c->fixed_scale, c->dcv, &c->launches);
+  CK(c, cudaGetLastError());
+  return CAPOW_OK;
+}
+
 extern "C" int capow_paint(capow_ctx *c, const capow_particles *parts) {
   if (!c || !parts) return CAPOW_EINVAL;
   if (!c->plan_ok) FAIL(c, CAPOW_ESTATE, "context not fully created");
@@ -597,6 +606,13 @@ extern "C" void capow_destroy(capow_ctx *c) {
   cudaSetDevice(c->o.device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->plan_ok) cufftDestroy(c->plan);
+  if (c->adj_plans) {
+    cufftDestroy(c->adj_fwd);
+    cufftDestroy(c->adj_inv);
+  }
+  if (c->adj_coef) cudaFree(c->adj_coef);
+  for (int k = 0; k < 5; k++)
+    if (c->adj_stage[k]) cudaFree(c->adj_stage[k]);
   for (void *p : c->allocs) cudaFree(p);
   for (int k = 0; k < 5; k++)
     if (c->stage[k]) cudaFree(c->stage[k]);

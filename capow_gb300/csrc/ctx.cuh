@@ -41,6 +41,12 @@ struct capow_ctx {
   bool plan_ok;
   bool fused;           // FP32: 2-D (y, z) cuFFT + fused x-axis FFT and binning (k_xfft_bin)
   XbinGeo xg;
+  // capow_backward (created on first use): full 3-D plans, bin coefficients, host-output staging
+  bool adj_plans;
+  cufftHandle adj_fwd, adj_inv;
+  double *adj_coef;
+  void *adj_stage[5];
+  size_t adj_stage_bytes[5];
   // staging for host particle input
   void *stage[5];
   size_t stage_bytes[5];
@@ -73,3 +79,6 @@ struct capow_ctx {
     cufftResult r_ = (call);                                                     \
     if (r_ != CUFFT_SUCCESS) FAIL(ctx, CAPOW_ECUFFT, "%s failed: cufft status %d", #call, (int)r_); \
   } while (0)
+
+// capow_api.cu: paint the last catalogue again and prepare the DC values (capow_backward).
+int enqueue_backward_paint(capow_ctx *c);

@@ -172,6 +172,26 @@ int capow_get_stats(capow_ctx *ctx, capow_stats *out);
  * stream synchronisation and the device-to-host copy of the bins. */
 int capow_power(capow_ctx *ctx, capow_spectrum *out, int nout);
 
+/* gradients of a loss with respect to every particle of the last paint (capow_backward) */
+typedef struct capow_grads {
+  int on_device;     /* 1: device pointers; 0: host pointers (copied out at the end of the call) */
+  int dtype;         /* CAPOW_F32 / CAPOW_F64: must match the painted particles */
+  void *dx, *dy, *dz; /* dL/d(position), n each; NULL to skip one */
+  void *dvlos;       /* dL/d(v_los): through the RSD shift (LOS != 0) */
+  void *dw;          /* dL/d(weight), including its effect on NGRID (norm, shot, mean subtraction) */
+} capow_grads;
+
+/* Adjoint of capow_power + capow_normalise for the density auto-spectrum (Momentum 0, or
+ * spectra = CAPOW_SPEC_DD): given dL/dP_l(k) of the normalised multipoles (dL_dP[l] = double[NK],
+ * l = 0..4; NULL for a multipole the loss does not use), writes dL/dx, dL/dy, dL/dz, dL/dv_los
+ * and dL/dw of every particle of the last capow_paint. The reference has no adjoint; this inverts
+ * read_data.c:32-179, 514-745 and main.c:106-148, 211-225, 266-271, 302-468, 1019-1056: repaint,
+ * full 3-D R2C, per-mode dL/dF, Hermitian completion, C2R, and the transposed deposit with the
+ * weight derivatives. Call after capow_power; it leaves the grids holding dL/dgrid, so paint
+ * again before the next capow_power. The output_power rule that zeroes the highest filled bin
+ * makes that bin's gradient zero. */
+int capow_backward(capow_ctx *ctx, const double *const dL_dP[5], const capow_grads *out);
+
 /* output_power arithmetic (main.c:1019-1056) in place on one spectrum's raw sums. Host only. */
 int capow_normalise(const capow_params *p, capow_spectrum *s);
 

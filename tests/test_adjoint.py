@@ -1,0 +1,206 @@
+"""capow_backward (adjoint of the density multipoles) against torch autograd through a dense FP64
+restatement of the forward, against central finite differences, and FP32 against FP64 at the
+C3 workload size. The loss is sum over l in {0, 2} and k of (P_l(k) - T_l(k))^2, T from a second
+seeded realisation."""
+import numpy as np
+import pytest
+
+import capow_gb300 as cg
+
+pytestmark = pytest.mark.gpu
+
+
+def rsd_factor(p):
+    return (1.0 + p.Redshift) / (100.0 * np.sqrt(p.Omega_m * (1.0 + p.Redshift) ** 3 + 1.0 - p.Omega_m))
+
+
+def mode_tables(p):
+    """Per half-space mode: k-bin (-1 when excluded), mu, NM * grid_cor (* 0.25 when interlaced) and
+    the interlace phase, following the binning loop of src/main.c:302-468 (bin from the float
+    quantity (float)(fktot - Mink) / binwidth, Nyquist cut, Hermitian weights)."""
+    n = (p.NX, p.NY, p.NZ)
+    d = [(p.XMAX - p.XMIN) / n[0], (p.YMAX - p.YMIN) / n[1], (p.ZMAX - p.ZMIN) / n[2]]
+    f = []
+    for a in range(3):
+        sc = 1.0 / (np.float64(np.float32(n[a])) * d[a])
+        idx = np.arange(n[a] if a < 2 else n[a] // 2 + 1)
+        fr = np.where(idx <= n[a] // 2, idx, idx - n[a]).astype(np.float64) * sc if a < 2 else idx * sc
+        f.append(fr)
+    fx, fy, fz = np.meshgrid(f[0], f[1], f[2], indexing="ij")
+    fktot = 2.0 * np.pi * np.sqrt(fx * fx + fy * fy + fz * fz)
+    mu = np.where(fktot > 0, 2.0 * np.pi * fz / np.where(fktot > 0, fktot, 1.0), 0.0)
+    bw = (p.Maxk - p.Mink) / p.NK
+    kb = np.trunc(np.float32(fktot - p.Mink).astype(np.float64) / bw).astype(np.int64)
+    ny = min(np.pi / d[0], np.pi / d[1], np.pi / d[2])
+    kb = np.where((kb >= 0) & (kb < p.NK) & (fktot <= ny), kb, -1)
+    ax, ay, az = np.pi * fx * d[0], np.pi * fy * d[1], np.pi * fz * d[2]
+    sinc = lambda t: np.where(t != 0, np.sin(t) / np.where(t != 0, t, 1.0), 1.0)
+    gc = (1.0 / (sinc(ax) * sinc(ay) * sinc(az))) ** (2 * p.InterpOrder)
+    i, j, k = np.meshgrid(np.arange(n[0]), np.arange(n[1]), np.arange(n[2] // 2 + 1), indexing="ij")
+    nm = np.where(k != 0, 2, np.where(j == 0, np.where((i != 0) & (i != n[0] // 2), 1, 2),
+                                      np.where(i != n[0] // 2, 1, 2)))
+    if p.DoInterlacing:
+        gc = gc * 0.25
+    kh = ax + ay + az
+    return kb, mu, nm * gc, np.cos(kh) + 1j * np.sin(kh), nm
+
+
+def dense_multipoles(torch, p, x, y, z, v, w, tab):
+    """P0, P2 of the density field (TSC, interlaced, LOS = z), normalised as output_power does, for
+    particles whose every tap lies inside the grid (then the reference deposit is plain TSC)."""
+    n = p.NX
+    d = (p.XMAX - p.XMIN) / n
+    zs = z + v * rsd_factor(p)
+
+    def paint(px, py, pz):
+        g = torch.zeros(n * n * n, dtype=torch.float64, device=x.device)
+        s = [(px - p.XMIN) / d, (py - p.YMIN) / d, (pz - p.ZMIN) / d]
+        i = [torch.floor(t + 0.5).detach().long() for t in s]
+        dd = [t - ii.to(t.dtype) for t, ii in zip(s, i)]
+        W = [[0.5 * (0.5 - e) ** 2, 0.75 - e * e, 0.5 * (0.5 + e) ** 2] for e in dd]
+        for a in range(3):
+            for b in range(3):
+                for c in range(3):
+                    idx = ((i[0] + a - 1) * n + (i[1] + b - 1)) * n + (i[2] + c - 1)
+                    g = g.index_add(0, idx, w * W[0][a] * W[1][b] * W[2][c])
+        return g.view(n, n, n)
+
+    N = w.sum()
+    h = 0.5 * d
+    g, gi = paint(x, y, zs), paint(x + h, y + h, zs + h)
+    kb, mu, wgt, e, nm = tab
+    dc = torch.zeros(kb.shape, dtype=torch.float64, device=x.device)
+    dc[0, 0, 0] = 1.0
+    F = torch.fft.rfftn(g)
+    Fi = torch.fft.rfftn(gi)
+    F = F * (1 - dc) + dc * (g.sum() - N)
+    Fi = Fi * (1 - dc) + dc * (gi.sum() - N)
+    Fp = F + torch.as_tensor(e, device=x.device) * Fi
+    power = torch.as_tensor(wgt, device=x.device) * (Fp.real ** 2 + Fp.imag ** 2)
+    m = torch.as_tensor(kb >= 0, device=x.device)
+    kbt = torch.as_tensor(np.where(kb >= 0, kb, 0), device=x.device)[m]
+    mut = torch.as_tensor(mu, device=x.device)[m]
+    S0 = torch.zeros(p.NK, dtype=torch.float64, device=x.device).index_add(0, kbt, power[m])
+    S2 = torch.zeros(p.NK, dtype=torch.float64, device=x.device).index_add(0, kbt, power[m] * (1.5 * mut ** 2 - 0.5))
+    Nm = np.zeros(p.NK)
+    np.add.at(Nm, kb[kb >= 0], nm[kb >= 0])
+    V = (p.XMAX - p.XMIN) * (p.YMAX - p.YMIN) * (p.ZMAX - p.ZMIN)
+    norm = N * N / V
+    Nmt = torch.as_tensor(np.where(Nm > 0, Nm, 1.0), device=x.device)
+    keep = Nm > 0
+    keep[np.nonzero(Nm > 0)[0].max()] = False  # output_power zeroes the highest filled bin
+    kt = torch.as_tensor(keep.astype(np.float64), device=x.device)
+    P0 = (S0 - Nmt * N) / (Nmt * norm) * kt
+    P2 = 5.0 * S2 / (Nmt * norm) * kt
+    return P0, P2
+
+
+def lib_multipoles(p, parts, precision):
+    x, y, z, vz, w = parts
+    with cg.PowerSpectrum(p, precision=precision) as ps:
+        ps.paint(x, y, z, vz, w)
+        r = ps.normalise(ps.power()[0])
+    return r["Pk0"], r["Pk2"]
+
+
+def lib_grads(p, parts, precision, T0, T2):
+    x, y, z, vz, w = parts
+    with cg.PowerSpectrum(p, precision=precision) as ps:
+        ps.paint(x, y, z, vz, w)
+        r = ps.normalise(ps.power()[0])
+        P0, P2 = r["Pk0"], r["Pk2"]
+        gr = ps.backward({"Pk0": 2 * (P0 - T0), "Pk2": 2 * (P2 - T2)})
+    return gr, P0, P2
+
+
+def interior_particles(p, n, seed, margin=3.0):
+    rng = np.random.default_rng(seed)
+    d = (p.XMAX - p.XMIN) / p.NX
+    lo, hi = p.XMIN + margin * d, p.XMAX - margin * d
+    x, y, z = (rng.uniform(lo, hi, n) for _ in range(3))
+    vz = rng.normal(0.0, 50.0, n)
+    w = rng.uniform(0.5, 1.5, n)
+    return x, y, z, vz, w
+
+
+BASE = dict(XMIN=0.0, XMAX=1000.0, YMIN=0.0, YMAX=1000.0, ZMIN=0.0, ZMAX=1000.0, InterpOrder=3,
+            DoInterlacing=1, LOS=3, Momentum=0)
+
+
+def test_backward_matches_dense_torch_autograd(gpu):
+    torch = pytest.importorskip("torch")
+    p = cg.Params(NX=64, NY=64, NZ=64, NK=30, Maxk=0.3, **BASE)
+    parts = interior_particles(p, 32 ** 3, seed=41)
+    T0, T2 = lib_multipoles(p, interior_particles(p, 32 ** 3, seed=42), "fp64")
+    gr, P0, P2 = lib_grads(p, parts, "fp64", T0, T2)
+    tab = mode_tables(p)
+    t = [torch.tensor(a, dtype=torch.float64, device=gpu, requires_grad=True) for a in parts]
+    D0, D2 = dense_multipoles(torch, p, *t, tab)
+    scale0 = np.abs(P0).max()
+    assert np.abs(D0.detach().cpu().numpy() - P0).max() <= 1e-10 * scale0
+    assert np.abs(D2.detach().cpu().numpy() - P2).max() <= 1e-10 * scale0
+    loss = ((D0 - torch.as_tensor(T0, device=gpu)) ** 2).sum() + ((D2 - torch.as_tensor(T2, device=gpu)) ** 2).sum()
+    loss.backward()
+    for name, tt in zip(("dx", "dy", "dz", "dvlos", "dw"), t):
+        ref = tt.grad.cpu().numpy()
+        err = np.abs(gr[name] - ref).max() / np.abs(ref).max()
+        assert err <= 1e-8, f"{name}: {err:.2e}"
+
+
+def test_backward_central_differences(gpu):
+    p = cg.Params(NX=32, NY=32, NZ=32, NK=15, Maxk=0.15, **BASE)
+    parts = [a.copy() for a in interior_particles(p, 20000, seed=51, margin=0.0)]
+    T0, T2 = lib_multipoles(p, interior_particles(p, 20000, seed=52, margin=0.0), "fp64")
+    gr, _, _ = lib_grads(p, parts, "fp64", T0, T2)
+
+    def loss():
+        P0, P2 = lib_multipoles(p, parts, "fp64")
+        return float(((P0 - T0) ** 2).sum() + ((P2 - T2) ** 2).sum())
+
+    d = (p.XMAX - p.XMIN) / p.NX
+    rng = np.random.default_rng(53)
+    picks = rng.choice(len(parts[0]), 64, replace=False)
+    steps = {"dx": 1e-3 * d, "dy": 1e-3 * d, "dz": 1e-3 * d, "dvlos": 1e-3 * d / rsd_factor(p), "dw": 1e-3}
+    for a, name in enumerate(("dx", "dy", "dz", "dvlos", "dw")):
+        fd = []
+        for i in picks:
+            v0 = parts[a][i]
+            parts[a][i] = v0 + steps[name]
+            lp = loss()
+            parts[a][i] = v0 - steps[name]
+            lm = loss()
+            parts[a][i] = v0
+            fd.append((lp - lm) / (2 * steps[name]))
+        fd = np.array(fd)
+        an = gr[name][picks]
+        scale = np.abs(fd).max()
+        bad = np.abs(an - fd) > 2e-3 * scale
+        # a central difference that straddles a TSC kink (a cell face) is off by O(h): allow two
+        assert bad.sum() <= 2, f"{name}: {np.c_[an[bad], fd[bad]]}"
+
+
+def test_backward_fp32_matches_fp64_at_c3_size(gpu):
+    """The C3 workload: 256^3 Zel'dovich particles (f32, unit weights), TSC 256^3, interlaced, LOS = z."""
+    import torch
+
+    from capow_gb300 import synth
+
+    p = cg.Params(NX=256, NY=256, NZ=256, NK=80, Maxk=0.8, **BASE)
+    x, y, z, vx, vy, vz = synth.zeldovich(256, L=1000.0, mesh=512, rms_cells=1.5, seed=2, torch_device=gpu)
+    d = [torch.from_numpy(a).to(gpu) for a in (x, y, z, vz)]
+    t = synth.zeldovich(256, L=1000.0, mesh=512, rms_cells=1.5, seed=3, torch_device=gpu)
+    with cg.PowerSpectrum(p, precision="fp64") as ps:
+        ps.paint(*[torch.from_numpy(a).to(gpu) for a in (t[0], t[1], t[2], t[5])])
+        rt = ps.normalise(ps.power()[0])
+    out = {}
+    for prec in ("fp32", "fp64"):
+        with cg.PowerSpectrum(p, precision=prec) as ps:
+            ps.paint(*d)
+            r = ps.normalise(ps.power()[0])
+            g = {k: torch.empty_like(d[0]) for k in ("dx", "dy", "dz", "dvlos", "dw")}
+            ps.backward({"Pk0": 2 * (r["Pk0"] - rt["Pk0"]), "Pk2": 2 * (r["Pk2"] - rt["Pk2"])}, out=g)
+            out[prec] = {k: v.double().cpu().numpy() for k, v in g.items()}
+    for k in out["fp64"]:
+        a, b = out["fp32"][k], out["fp64"][k]
+        rel = np.linalg.norm(a - b) / np.linalg.norm(b)
+        assert rel <= 2e-3, f"{k}: relative L2 difference {rel:.2e}"
