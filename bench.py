@@ -240,7 +240,11 @@ def gpu_bench(args, world, rank, local):
     params = cg.Params(**PARAMS)
     d = [torch.from_numpy(a).to(dev) for a in (x, y, z, vz)]
     host = [torch.from_numpy(a).pin_memory() for a in (x, y, z, vz)]
-    ps = cg.PowerSpectrum(params, precision="fp32", spectra=["dd", "dp", "pp"], device=local)
+    torch.cuda.synchronize()
+    # every context runs on this stream, and every CUDA event below is recorded on it
+    ts = torch.cuda.Stream(device=dev)
+    sh = ts.cuda_stream
+    ps = cg.PowerSpectrum(params, precision="fp32", spectra=["dd", "dp", "pp"], device=local, stream=sh)
 
     def step_device():
         ps.paint(*d)
@@ -257,15 +261,15 @@ def gpu_bench(args, world, rank, local):
     barrier(world)
     torch.cuda.synchronize()
     launches0 = ps.kernel_launches()
-    with ClockSampler(local) as clk:
+    with ClockSampler(local) as clk, torch.cuda.stream(ts):
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
-        ev0.record()
+        ev0.record(ts)
         stage_acc = np.zeros(3)
         for _ in range(args.steps):
             res = step_device()
             stage_acc += np.array(ps.stage_ms())
-        ev1.record()
+        ev1.record(ts)
         torch.cuda.synchronize()
         wall = (time.perf_counter() - t0) * 1e3
     launches = ps.kernel_launches() - launches0
@@ -288,22 +292,47 @@ def gpu_bench(args, world, rank, local):
     e2e_ms = max_over_ranks(world, e2e_ms, dev) / (args.steps * world)
     h2d = sum(int(h.numel() * h.element_size()) for h in host)
     d2h = 3 * 5 * PARAMS["NK"] * 8
+    # ---- adjoint (C3 workload): the same particles, density multipoles on a 256^3 TSC grid; forward
+    # (paint + power) and capow_backward timed separately with CUDA events
+    adj = None
+    try:
+        p3 = cg.Params(**dict(PARAMS, NX=256, NY=256, NZ=256, NK=80, Maxk=0.8))
+        with cg.PowerSpectrum(p3, precision="fp32", device=local, stream=sh) as pa:
+            gbuf = {k: torch.empty_like(d[0]) for k in ("dx", "dy", "dz", "dvlos", "dw")}
+            torch.cuda.synchronize()
+            fw, bw = [], []
+            for it in range(4):
+                e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+                e0.record(ts)
+                pa.paint(*d)
+                r3 = pa.normalise(pa.power()[0])
+                e1.record(ts)
+                pa.backward({"Pk0": 2 * r3["Pk0"], "Pk2": 2 * r3["Pk2"]}, out=gbuf)
+                e2.record(ts)
+                torch.cuda.synchronize()
+                if it:
+                    fw.append(e0.elapsed_time(e1))
+                    bw.append(e1.elapsed_time(e2))
+        adj = {"workload": "same 16,777,216 particles, TSC 256^3, interlaced, LOS=z, loss sum_l (P_l)^2, l=0,2",
+               "forward_ms": round(statistics.median(fw), 3), "backward_ms": round(statistics.median(bw), 3)}
+    except cg.CapowError as e:  # pragma: no cover
+        adj = {"error": str(e)}
     # ---- FP64 GPU path on the same workload (fewer steps: it is the slow baseline)
     ps.close()
     fp64_ms = None
     acc = None
     try:
-        p64 = cg.PowerSpectrum(params, precision="fp64", spectra=["dd", "dp", "pp"], device=local)
+        p64 = cg.PowerSpectrum(params, precision="fp64", spectra=["dd", "dp", "pp"], device=local, stream=sh)
         p64.paint(*d)
         r64 = p64.power()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         k64 = max(1, min(3, args.steps))
-        e0.record()
+        e0.record(ts)
         for _ in range(k64):
             p64.paint(*d)
             r64 = p64.power()
-        e1.record()
+        e1.record(ts)
         torch.cuda.synchronize()
         fp64_ms = e0.elapsed_time(e1) / k64
         p64.close()
@@ -326,7 +355,7 @@ def gpu_bench(args, world, rank, local):
     return {
         "ms_per": ms_per, "wall_ms": wall, "stage_ms": stage_ms, "launches": launches, "e2e_ms": e2e_ms, "h2d": h2d,
         "d2h": d2h, "fp64_ms": fp64_ms, "acc": acc, "B32": B32, "B64": B64, "peaks": pk, "clocks": clk.summary(),
-        "n": n, "parts": parts,
+        "n": n, "parts": parts, "adjoint": adj,
     }
 
 
@@ -392,6 +421,7 @@ def main():
                           "peak_source": pk["source"]},
         "fp64_gpu": {"ms": round(r["fp64_ms"], 3) if r["fp64_ms"] else None, "algorithmic_bytes": r["B64"]},
         "accuracy_fp32_vs_fp64_gpu": r["acc"],
+        "adjoint_c3": r["adjoint"],
         "clocks": r["clocks"],
         "cpu_baseline": ({k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")} if cpu else None),
     }
