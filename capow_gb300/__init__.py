@@ -85,12 +85,19 @@ class _Spectrum(ctypes.Structure):
                 ("last_bin", ctypes.c_int), ("kind", ctypes.c_int)]
 
 
+class _Mock(ctypes.Structure):
+    _fields_ = [("params", _Params), ("parts", _Particles), ("out", ctypes.POINTER(_Spectrum)), ("status", ctypes.c_int)]
+
+
+BATCH_GRAPH, BATCH_AUTOTUNE = 1, 2
+
+
 # every entry point include/capow.h declares
 EXPORTS = [
     "capow_create", "capow_paint", "capow_get_stats", "capow_power", "capow_normalise", "capow_num_spectra",
     "capow_copy_grid", "capow_stage_ms", "capow_kernel_launches", "capow_destroy", "capow_read_params",
     "capow_read_catalogue", "capow_free", "capow_write_output", "capow_bin_centre", "capow_strerror",
-    "capow_last_error", "capow_paint_noalloc", "capow_backward",
+    "capow_last_error", "capow_paint_noalloc", "capow_backward", "capow_batch",
 ]
 
 _lib = None
@@ -111,6 +118,7 @@ def lib() -> ctypes.CDLL:
     L.capow_paint.argtypes = [vp, ctypes.POINTER(_Particles)]
     L.capow_paint_noalloc.argtypes = [vp, ctypes.POINTER(_Particles)]
     L.capow_get_stats.argtypes = [vp, ctypes.POINTER(_Stats)]
+    L.capow_batch.argtypes = [ctypes.POINTER(_Mock), ip, O, ip]
     L.capow_backward.argtypes = [vp, ctypes.POINTER(ctypes.POINTER(ctypes.c_double) * 5), ctypes.POINTER(_Grads)]
     L.capow_power.argtypes = [vp, ctypes.POINTER(_Spectrum), ip]
     L.capow_normalise.argtypes = [P, ctypes.POINTER(_Spectrum)]
@@ -410,3 +418,54 @@ def run(params: Params, x, y, z, vlos=None, w=None, precision: str = "fp32", spe
     with PowerSpectrum(params, precision=precision, spectra=spectra, device=device) as ps:
         ps.paint(x, y, z, vlos, w)
         return ps.power()
+
+
+def run_batch(mocks, precision: str = "fp32", spectra=None, graph: bool = False, autotune: bool = False,
+              device: int = 0, stream=None):
+    """capow_batch: many independent mocks in one call.
+
+    mocks: list of (Params, (x, y, z, vlos, w)) with device arrays (vlos, w may be None).
+    Returns a list of (status, [spectrum dict, ...]) in input order; the dicts hold raw sums as
+    PowerSpectrum.power returns them (normalise with PowerSpectrum.normalise or capow_normalise)."""
+    mask = 0
+    for sp in (spectra or []):
+        mask |= {"dd": SPEC_DD, "dp": SPEC_DP, "pp": SPEC_PP}[sp]
+    nspec = 1 if mask == 0 else bin(mask).count("1")
+    arr = (_Mock * len(mocks))()
+    keep = []
+    for i, (prm, parts) in enumerate(mocks):
+        ptrs = [_ptr_of(a) for a in parts]
+        codes = {q[1] for q in ptrs if q[0] is not None}
+        if len(codes) != 1 or any(q[2] != 1 for q in ptrs if q[0] is not None):
+            raise ValueError("capow_batch takes device arrays of one dtype per mock")
+        n = len(ptrs[0][3])
+        keep.append([q[3] for q in ptrs])
+        specs = (_Spectrum * nspec)()
+        bufs = []
+        for q in range(nspec):
+            pk = [np.zeros(prm.NK) for _ in range(5)]
+            nm = np.zeros(prm.NK, np.int64)
+            for l in range(5):
+                specs[q].pk[l] = pk[l].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+            specs[q].nmodes = nm.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+            bufs.append((pk, nm))
+        keep.append((specs, bufs))
+        arr[i].params = prm.to_c()
+        arr[i].parts = _Particles(n, codes.pop(), 1, *[q[0] for q in ptrs])
+        arr[i].out = ctypes.cast(specs, ctypes.POINTER(_Spectrum))
+    opt = _Options(PRECISIONS[precision], mask, device, ctypes.c_void_p(stream or 0), FFT_AUTO)
+    flags = (BATCH_GRAPH if graph else 0) | (BATCH_AUTOTUNE if autotune else 0)
+    rc = lib().capow_batch(arr, len(mocks), ctypes.byref(opt), flags)
+    if rc != OK:
+        raise CapowError(rc, f"capow_batch: {lib().capow_strerror(rc).decode()}")
+    out = []
+    for i in range(len(mocks)):
+        specs, bufs = keep[2 * i + 1]
+        res = []
+        for q in range(nspec if arr[i].status == OK else 0):
+            pk, nm = bufs[q]
+            res.append({"Pk0": pk[0], "Pk1": pk[1], "Pk2": pk[2], "Pk3": pk[3], "Pk4": pk[4], "Nmodes": nm,
+                        "shot": specs[q].shot, "norm": specs[q].norm, "alpha": specs[q].alpha,
+                        "kind": {0: "ref", SPEC_DD: "dd", SPEC_DP: "dp", SPEC_PP: "pp"}[specs[q].kind]})
+        out.append((arr[i].status, res))
+    return out

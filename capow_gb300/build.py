@@ -22,7 +22,7 @@ BIN = os.path.join(HERE, "bin")
 LIB = os.path.join(BUILD, "libcapow_gpu.so")
 DRIVER = os.path.join(BIN, "capow")
 
-CU_SOURCES = ["capow_api.cu", "paint.cu", "bin.cu", "noalloc.cu", "adjoint.cu"]
+CU_SOURCES = ["capow_api.cu", "paint.cu", "bin.cu", "noalloc.cu", "adjoint.cu", "batch.cu"]
 C_SOURCES = ["params.c", "catalogue.c", "output.c"]
 DRIVER_SOURCES = ["main.c"]
 

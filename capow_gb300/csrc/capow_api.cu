@@ -57,7 +57,7 @@ static int validate(const capow_params *p, const capow_options *o, char *err, si
 #undef BAD
 }
 
-static Geom make_geom(const capow_params &p) {
+Geom make_geom(const capow_params &p) {
   Geom g;
   memset(&g, 0, sizeof g);
   g.nx = p.NX; g.ny = p.NY; g.nz = p.NZ;
@@ -316,11 +316,11 @@ static int ensure_records(capow_ctx *c, unsigned long long need, bool weights) {
   return CAPOW_OK;
 }
 
-static int enqueue_paint(capow_ctx *c, const capow_particles &d) {
+int enqueue_paint(capow_ctx *c, const capow_particles &d) {
   const long long n = (long long)d.n;
   GridPtrs gp = grid_ptrs(c);
   CK(c, cudaMemsetAsync(c->st, 0, sizeof(DevStats), c->stream));
-  CK(c, cudaEventRecord(c->ev[0], c->stream));
+  if (!c->quiet) CK(c, cudaEventRecord(c->ev[0], c->stream));
   if (c->prec == CAPOW_FP64) {
     CK(c, cudaMemsetAsync(c->grid_base, 0, 8 * c->grid_elems * c->nslot, c->stream));
     launch_paint64(c->stream, c->g, c->fs, d.dtype, d.x, d.y, d.z, d.vlos, d.w, n, gp, c->st, &c->launches);
@@ -342,8 +342,24 @@ static int enqueue_paint(capow_ctx *c, const capow_particles &d) {
                    d.vlos, d.w, n, gp, c->pb, c->st, &c->launches);
   }
   CK(c, cudaGetLastError());
-  CK(c, cudaEventRecord(c->ev[1], c->stream));
+  if (!c->quiet) CK(c, cudaEventRecord(c->ev[1], c->stream));
   return CAPOW_OK;
+}
+
+// Size the FP32 record and edge buffers for catalogues of up to nmax particles (so that a later
+// enqueue_paint allocates nothing).
+int prepare_paint_buffers(capow_ctx *c, unsigned long long nmax, bool weights) {
+  if (c->prec == CAPOW_FP64) return CAPOW_OK;
+  if (!c->pb.edge_count) CK(c, cudaMalloc(&c->pb.edge_count, sizeof(unsigned)));
+  if (c->pb.edge_cap < nmax + 1) {
+    if (c->pb.edge_list) cudaFree(c->pb.edge_list);
+    c->pb.edge_list = nullptr;
+    c->pb.edge_cap = 0;
+    CK(c, cudaMalloc(&c->pb.edge_list, sizeof(unsigned) * (nmax + 1)));
+    c->pb.edge_cap = nmax + 1;
+  }
+  const unsigned long long want = (unsigned long long)(tile_dup_estimate(c->g, c->tg) * 1.25 * nmax) + 65536;
+  return ensure_records(c, want, weights);
 }
 
 int enqueue_backward_paint(capow_ctx *c) {
@@ -434,13 +450,14 @@ extern "C" int capow_copy_grid(capow_ctx *c, int which, double *host_out) {
   return CAPOW_OK;
 }
 
-static int enqueue_power(capow_ctx *c) {
+// The kernels of capow_power (DC values, FFT, binning into c->bins); no read-back, no sync.
+int enqueue_power_kernels(capow_ctx *c) {
   const bool f64 = c->prec == CAPOW_FP64;
   launch_dc_prepare(c->stream, c->st, c->prec == CAPOW_FP32_DETERMINISTIC, c->nslot, c->fs.nfields,
                     c->bp.mean_sub_a, c->fixed_scale, c->dcv, &c->launches);
   if (c->fused) {
     CKFFT(c, cufftExecR2C(c->plan, (cufftReal *)c->grid_base, (cufftComplex *)c->grid_base));
-    CK(c, cudaEventRecord(c->ev[2], c->stream));
+    if (!c->quiet) CK(c, cudaEventRecord(c->ev[2], c->stream));
     const int nk = c->p.NK;
     CK(c, cudaMemsetAsync(c->bins, 0, sizeof(double) * NPROD * 5 * nk, c->stream));
     void *slots[4];
@@ -448,10 +465,7 @@ static int enqueue_power(capow_ctx *c) {
     for (int k = 0; k < 4; k++) slots[k] = gp.g[k];
     launch_xbin(c->stream, c->bp, c->bt, c->xg, slots, c->dcv, c->bins, &c->launches);
     CK(c, cudaGetLastError());
-    CK(c, cudaEventRecord(c->ev[3], c->stream));
-    CK(c, cudaMemcpyAsync(c->h_bins, c->bins, sizeof(double) * bin_products(c->fs.nfields) * 5 * nk,
-                          cudaMemcpyDeviceToHost, c->stream));
-    CK(c, cudaMemcpyAsync(c->h_st, c->st, sizeof(DevStats), cudaMemcpyDeviceToHost, c->stream));
+    if (!c->quiet) CK(c, cudaEventRecord(c->ev[3], c->stream));
     return CAPOW_OK;
   }
   if (c->grid_elems > 0x7fffffffULL) {
@@ -465,7 +479,7 @@ static int enqueue_power(capow_ctx *c) {
     if (f64) CKFFT(c, cufftExecD2Z(c->plan, (cufftDoubleReal *)c->grid_base, (cufftDoubleComplex *)c->grid_base));
     else CKFFT(c, cufftExecR2C(c->plan, (cufftReal *)c->grid_base, (cufftComplex *)c->grid_base));
   }
-  CK(c, cudaEventRecord(c->ev[2], c->stream));
+  if (!c->quiet) CK(c, cudaEventRecord(c->ev[2], c->stream));
   const int nk = c->p.NK, n2d = c->p.Output2D ? c->p.NK * c->p.NMU : 0;
   CK(c, cudaMemsetAsync(c->bins, 0, sizeof(double) * NPROD * 5 * nk, c->stream));
   if (n2d) CK(c, cudaMemsetAsync(c->bins2d, 0, sizeof(double) * NPROD * n2d, c->stream));
@@ -474,7 +488,14 @@ static int enqueue_power(capow_ctx *c) {
   for (int k = 0; k < 4; k++) slots[k] = gp.g[k];
   launch_bin(c->stream, c->prec, c->bp, c->bt, slots, c->dcv, c->bins, n2d ? c->bins2d : nullptr, &c->launches);
   CK(c, cudaGetLastError());
-  CK(c, cudaEventRecord(c->ev[3], c->stream));
+  if (!c->quiet) CK(c, cudaEventRecord(c->ev[3], c->stream));
+  return CAPOW_OK;
+}
+
+static int enqueue_power(capow_ctx *c) {
+  int rc = enqueue_power_kernels(c);
+  if (rc) return rc;
+  const int nk = c->p.NK, n2d = c->p.Output2D ? c->p.NK * c->p.NMU : 0;
   const int np = bin_products(c->fs.nfields);
   CK(c, cudaMemcpyAsync(c->h_bins, c->bins, sizeof(double) * np * 5 * nk, cudaMemcpyDeviceToHost, c->stream));
   if (n2d)
@@ -508,9 +529,14 @@ extern "C" int capow_power(capow_ctx *c, capow_spectrum *out, int nout) {
   }
   if (c->h_st->nonfinite) FAIL(c, CAPOW_EINVAL, "non-finite particle coordinate, velocity or weight");
   if (c->h_st->fatal) FAIL(c, CAPOW_EBOUNDS, "particle out of grid bounds with LOS == 0");
-  // shot noise and normalisation, src/main.c:117-148 (one rank: NTask = 1)
-  const DevStats &st = *c->h_st;
-  const capow_params &p = c->p;
+  fill_spectra(c, c->p, *c->h_st, c->h_bins, c->nmodes.data(), c->nmodes2d.data(), out);
+  return CAPOW_OK;
+}
+
+// Host side of capow_power for one catalogue: shot noise and normalisation (src/main.c:117-148,
+// one rank: NTask = 1) and the raw sums of each spectrum out of the [product][5][NK] bins.
+void fill_spectra(const capow_ctx *c, const capow_params &p, const DevStats &st, const double *h_bins,
+                  const unsigned long long *nmodes, const unsigned long long *nmodes2d, capow_spectrum *out) {
   const double N = st.ngrid;
   const double alpha = N / ((double)p.NX * (double)p.NY * (double)p.NZ);
   const double nbar = N / ((p.XMAX - p.XMIN) * (p.YMAX - p.YMIN) * (p.ZMAX - p.ZMIN));
@@ -537,15 +563,14 @@ extern "C" int capow_power(capow_ctx *c, capow_spectrum *out, int nout) {
         memset(s.pk[l], 0, sizeof(double) * nk);
         continue;
       }
-      memcpy(s.pk[l], c->h_bins + (pq * 5 + l) * nk, sizeof(double) * nk);
+      memcpy(s.pk[l], h_bins + (pq * 5 + l) * nk, sizeof(double) * nk);
     }
     if (s.nmodes)
-      for (int b = 0; b < nk; b++) s.nmodes[b] = (int64_t)c->nmodes[b];
-    if (n2d && s.pk2d) memcpy(s.pk2d, c->h_bins + NPROD * 5 * nk + pq * n2d, sizeof(double) * n2d);
+      for (int b = 0; b < nk; b++) s.nmodes[b] = (int64_t)nmodes[b];
+    if (n2d && s.pk2d) memcpy(s.pk2d, h_bins + NPROD * 5 * nk + pq * n2d, sizeof(double) * n2d);
     if (n2d && s.nmodes2d)
-      for (int b = 0; b < n2d; b++) s.nmodes2d[b] = (int64_t)c->nmodes2d[b];
+      for (int b = 0; b < n2d; b++) s.nmodes2d[b] = (int64_t)nmodes2d[b];
   }
-  return CAPOW_OK;
 }
 
 extern "C" int capow_normalise(const capow_params *p, capow_spectrum *s) {

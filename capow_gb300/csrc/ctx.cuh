@@ -42,6 +42,7 @@ struct capow_ctx {
   bool fused;           // FP32: 2-D (y, z) cuFFT + fused x-axis FFT and binning (k_xfft_bin)
   XbinGeo xg;
   // capow_backward (created on first use): full 3-D plans, bin coefficients, host-output staging
+  bool quiet;           // skip the stage-timing event records (batched enqueue, graph capture)
   bool adj_plans;
   cufftHandle adj_fwd, adj_inv;
   double *adj_coef;
@@ -82,3 +83,11 @@ struct capow_ctx {
 
 // capow_api.cu: paint the last catalogue again and prepare the DC values (capow_backward).
 int enqueue_backward_paint(capow_ctx *c);
+
+// capow_api.cu pieces shared with batch.cu
+Geom make_geom(const capow_params &p);
+int enqueue_paint(capow_ctx *c, const capow_particles &d);
+int enqueue_power_kernels(capow_ctx *c);
+int prepare_paint_buffers(capow_ctx *c, unsigned long long nmax, bool weights);
+void fill_spectra(const capow_ctx *c, const capow_params &p, const DevStats &st, const double *h_bins,
+                  const unsigned long long *nmodes, const unsigned long long *nmodes2d, capow_spectrum *out);

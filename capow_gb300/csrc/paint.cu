@@ -950,15 +950,18 @@ static int log2i(int p) {
 }
 
 TileGeo choose_tiles(const Geom &g, int nslots, int deterministic) {
-  TileGeo t;
   // 4 grid slots x 8x16x32 floats = 64 KB (three CTAs per SM); the int64 variant halves the volume.
-  // Tile edges are powers of two (tile coordinates are shifts); a grid edge shorter than the tile
-  // uses the next power of two and the tile is partial.
-  t.tx = 8;
-  t.ty = 16;
-  t.tz = 32;
-  if (deterministic) t.tx = (nslots > 2) ? 4 : 8;
-  else if (nslots <= 2) t.tx = 16;
+  if (deterministic) return make_tiles(g, (nslots > 2) ? 4 : 8, 16, 32);
+  return make_tiles(g, nslots <= 2 ? 16 : 8, 16, 32);
+}
+
+// Tile edges are powers of two (tile coordinates are shifts); a grid edge shorter than the tile
+// uses the next power of two and the tile is partial.
+TileGeo make_tiles(const Geom &g, int tx, int ty, int tz) {
+  TileGeo t;
+  t.tx = tx;
+  t.ty = ty;
+  t.tz = tz;
   t.tz = t.tz < pow2_at_least(g.nz) ? t.tz : pow2_at_least(g.nz);
   t.ty = t.ty < pow2_at_least(g.ny) ? t.ty : pow2_at_least(g.ny);
   t.tx = t.tx < pow2_at_least(g.nx) ? t.tx : pow2_at_least(g.nx);

@@ -64,6 +64,7 @@ void launch_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, const Ti
 
 // suggested tile geometry for a grid (and whether two fields are painted)
 TileGeo choose_tiles(const Geom &g, int nslots, int deterministic);
+TileGeo make_tiles(const Geom &g, int tx, int ty, int tz);  // tx, ty, tz powers of two (>= 4)
 size_t tile_smem_bytes(const TileGeo &tg, int nslots, int deterministic);
 size_t rec_smem_bytes(const TileGeo &tg, int nslots);
 double tile_dup_estimate(const Geom &g, const TileGeo &tg);

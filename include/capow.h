@@ -192,6 +192,26 @@ typedef struct capow_grads {
  * makes that bin's gradient zero. */
 int capow_backward(capow_ctx *ctx, const double *const dL_dP[5], const capow_grads *out);
 
+/* ---------------------------------------------------------------- batched mocks */
+/* One mock of a batch: its own parameters (box, grid, order, ...) and device-resident catalogue.
+ * `out` has room for capow_num_spectra entries (the spectra selected by the batch's options);
+ * the call fills them as capow_power does (raw sums, shot, norm, alpha, Nmodes) and sets status. */
+typedef struct capow_mock {
+  capow_params params;
+  capow_particles parts; /* on_device = 1 */
+  capow_spectrum *out;
+  int status;            /* CAPOW_OK or this mock's error (e.g. CAPOW_EBOUNDS) */
+} capow_mock;
+
+#define CAPOW_BATCH_GRAPH 1    /* capture the whole batch as one CUDA graph and launch it once */
+#define CAPOW_BATCH_AUTOTUNE 2 /* time candidate tile shapes of the FP32 paint per grid shape first */
+
+/* Run many independent mocks (the reference runs one per process, main.c:28-298). Mocks with the
+ * same grid shape share grids, plans and record buffers; every mock is enqueued on one stream
+ * with no host synchronisation and read back once. Output2D is not supported here. Returns
+ * CAPOW_OK when the batch ran; per-mock errors are in mocks[i].status. */
+int capow_batch(capow_mock *mocks, int nmocks, const capow_options *opt, int flags);
+
 /* output_power arithmetic (main.c:1019-1056) in place on one spectrum's raw sums. Host only. */
 int capow_normalise(const capow_params *p, capow_spectrum *s);
 
