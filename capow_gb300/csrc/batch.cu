@@ -13,6 +13,7 @@
 #include <string.h>
 
 #include <map>
+#include <mutex>
 #include <tuple>
 #include <vector>
 
@@ -69,6 +70,10 @@ int time_paint(capow_ctx *c, const capow_particles &d, float *ms) {
   return rc;
 }
 
+// tile shapes chosen by the autotuner, per grid shape, for the life of the process
+std::mutex g_tuned_mu;
+std::map<ShapeKey, TileGeo> g_tuned;
+
 }  // namespace
 
 extern "C" int capow_batch(capow_mock *mocks, int nmocks, const capow_options *opt, int flags) {
@@ -118,7 +123,9 @@ extern "C" int capow_batch(capow_mock *mocks, int nmocks, const capow_options *o
   // ---- per-mock tables and output buffers (one device arena for the small per-mock arrays)
   const size_t per = ((sizeof(DevStats) + 255) & ~(size_t)255) + 256;  // counters + 4 DC values
   std::vector<MockDev> md(nmocks);
-  std::vector<std::vector<void *>> tab_allocs(nmocks);
+  std::vector<unsigned char> blob;  // every mock's bin tables, uploaded once
+  std::vector<size_t> tab_off(nmocks, 0);
+  void *tab_dev = nullptr;
   size_t bins_total = 0, nm_total = 0;
   std::vector<size_t> bins_off(nmocks, 0), nm_off(nmocks, 0);
   for (int i = 0; i < nmocks; i++) {
@@ -150,22 +157,42 @@ extern "C" int capow_batch(capow_mock *mocks, int nmocks, const capow_options *o
     }
     m.bp = c->bp;
     m.bp.fx_step = (float)(1.0 / ((float)p.NX * m.g.dx));
-    if (build_bin_tables(p, m.g, c->prec, m.bt, tab_allocs[i], stream)) {
+    tab_off[i] = (blob.size() + 255) & ~(size_t)255;
+    blob.resize(tab_off[i]);
+    std::vector<unsigned char> one;
+    if (build_bin_tables_packed(p, m.g, c->prec, m.bt, one)) {
       mocks[i].status = CAPOW_ENOMEM;
       ctx_of[i] = nullptr;
       continue;
     }
+    blob.insert(blob.end(), one.begin(), one.end());
     m.st = (DevStats *)(arena + per * i);
     m.dcv = (double *)(arena + per * i + ((sizeof(DevStats) + 255) & ~(size_t)255));
     m.bins = bins_d + bins_off[i];
     m.nmodes = nm_d + nm_off[i];
   }
-  // ---- record buffers for the largest catalogue of each shape; the tile autotuner
+  if (!rc && !blob.empty()) {
+    if (cudaMalloc(&tab_dev, blob.size()) != cudaSuccess ||
+        cudaMemcpyAsync(tab_dev, blob.data(), blob.size(), cudaMemcpyHostToDevice, stream) != cudaSuccess)
+      rc = CAPOW_ENOMEM;
+    for (int i = 0; i < nmocks && !rc; i++)
+      if (ctx_of[i]) relocate_bin_tables(md[i].bt, (const char *)tab_dev + tab_off[i]);
+  }
+  // ---- record buffers for the largest catalogue of each shape; the tile autotuner (its choice is
+  // kept per grid shape for later calls)
   for (auto &kv : ctxs) {
     if (rc) break;
     capow_ctx *c = kv.second;
     rc = prepare_paint_buffers(c, nmax[kv.first], wts[kv.first]);
     if (rc || !(flags & CAPOW_BATCH_AUTOTUNE) || c->prec != CAPOW_FP32_MIXED) continue;
+    {
+      std::lock_guard<std::mutex> lock(g_tuned_mu);
+      auto it = g_tuned.find(kv.first);
+      if (it != g_tuned.end()) {
+        c->tg = it->second;
+        continue;
+      }
+    }
     int first = -1;
     for (int i = 0; i < nmocks; i++)
       if (ctx_of[i] == c) {
@@ -191,6 +218,8 @@ extern "C" int capow_batch(capow_mock *mocks, int nmocks, const capow_options *o
     }
     c->tg = best;
     c->pb = keep_pb;
+    std::lock_guard<std::mutex> lock(g_tuned_mu);
+    g_tuned[kv.first] = best;
   }
   // ---- enqueue every mock (optionally captured as one graph)
   cudaGraph_t graph = nullptr;
@@ -278,8 +307,7 @@ extern "C" int capow_batch(capow_mock *mocks, int nmocks, const capow_options *o
   if (exec) cudaGraphExecDestroy(exec);
   if (graph) cudaGraphDestroy(graph);
   for (auto &kv : ctxs) capow_destroy(kv.second);  // restores nothing: the contexts are private
-  for (auto &v : tab_allocs)
-    for (void *p : v) cudaFree(p);
+  if (tab_dev) cudaFree(tab_dev);
   if (arena) cudaFree(arena);
   if (own_stream) cudaStreamDestroy(stream);
   return rc;

@@ -56,8 +56,19 @@ static double edge_for(int b, double mink, double bw, int nk, int lg, double ny)
   return from_bits(hi);
 }
 
+// When set, upload() appends to this host blob instead (16-byte aligned) and returns the offset as
+// a pointer; relocate_bin_tables then rebases every table on the blob's device copy.
+static thread_local std::vector<unsigned char> *g_pack = nullptr;
+
 template <typename T>
 static T *upload(const std::vector<T> &h, std::vector<void *> &allocs, cudaStream_t s) {
+  if (g_pack) {
+    size_t off = (g_pack->size() + 15) & ~(size_t)15;
+    if (off == 0) off = 16;  // no table at offset 0: a null pointer means "missing"
+    g_pack->resize(off + sizeof(T) * (h.size() ? h.size() : 1), 0);
+    if (!h.empty()) memcpy(g_pack->data() + off, h.data(), sizeof(T) * h.size());
+    return (T *)(uintptr_t)off;
+  }
   T *d = nullptr;
   if (cudaMalloc(&d, sizeof(T) * (h.size() ? h.size() : 1)) != cudaSuccess) return nullptr;
   allocs.push_back(d);
@@ -160,6 +171,26 @@ int build_bin_tables(const capow_params &p, const Geom &g, int precision, BinTab
     if (!t.twx) return 1;
   }
   return (t.E && t.Elo && t.Ehi && t.ezf) ? 0 : 1;
+}
+
+int build_bin_tables_packed(const capow_params &p, const Geom &g, int precision, BinTables &t,
+                            std::vector<unsigned char> &blob) {
+  std::vector<void *> none;
+  g_pack = &blob;
+  const int rc = build_bin_tables(p, g, precision, t, none, nullptr);
+  g_pack = nullptr;
+  return rc;
+}
+
+void relocate_bin_tables(BinTables &t, const void *base) {
+  void **f[] = {(void **)&t.fx2d, (void **)&t.fy2d, (void **)&t.fz2d, (void **)&t.fx2f, (void **)&t.fy2f,
+                (void **)&t.fz2f, (void **)&t.fxd,  (void **)&t.fyd,  (void **)&t.fzd,  (void **)&t.fxf,
+                (void **)&t.fyf,  (void **)&t.fzf,  (void **)&t.cxd,  (void **)&t.cyd,  (void **)&t.czd,
+                (void **)&t.cxf,  (void **)&t.cyf,  (void **)&t.czf,  (void **)&t.exd,  (void **)&t.eyd,
+                (void **)&t.ezd,  (void **)&t.exf,  (void **)&t.eyf,  (void **)&t.ezf,  (void **)&t.E,
+                (void **)&t.Elo,  (void **)&t.Ehi,  (void **)&t.twx};
+  for (void **q : f)
+    if (*q) *q = (void *)((const char *)base + (uintptr_t)*q);
 }
 
 // ---------------------------------------------------------------------------------- device side

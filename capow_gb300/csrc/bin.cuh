@@ -56,6 +56,12 @@ int host_kbin_of_s(double s, double mink, double binwidth, int nk, int output_lo
 int build_bin_tables(const capow_params &p, const Geom &g, int precision, BinTables &t, std::vector<void *> &allocs,
                      cudaStream_t s);
 
+// The same tables appended to a host blob (offsets in place of pointers), for many grids in one
+// allocation; relocate_bin_tables rebases them on the blob's device copy.
+int build_bin_tables_packed(const capow_params &p, const Geom &g, int precision, BinTables &t,
+                            std::vector<unsigned char> &blob);
+void relocate_bin_tables(BinTables &t, const void *base);
+
 // launchers
 void launch_mode_counts(cudaStream_t s, const BinParams &bp, const BinTables &t, unsigned long long *nmodes,
                         unsigned long long *nmodes2d, long long *launches);
