@@ -284,6 +284,56 @@ def batch_bench(args):
     print(json.dumps(line), flush=True)
 
 
+def scale_bench(args):
+    """The large single-mock workload: a 512^3 Zel'dovich lattice (134,217,728 particles, f32), L = 2000 Mpc/h,
+    CIC on a 1024^3 grid, interlaced, density and LOS-momentum multipoles (dd, dp, pp). FP32-mixed and
+    deterministic int64 modes timed and compared bin by bin with the FP64 path. Prints one JSON line."""
+    import torch
+
+    import capow_gb300 as cg
+    from capow_gb300 import synth
+
+    dev = torch.device("cuda", 0)
+    x, y, z, vx, vy, vz = synth.zeldovich(512, L=2000.0, mesh=1024, rms_cells=1.5, seed=2, torch_device=dev)
+    d = [torch.from_numpy(a).to(dev) for a in (x, y, z, vz)]
+    del x, y, z, vx, vy
+    p = cg.Params(**dict(PARAMS, NX=1024, NY=1024, NZ=1024, XMAX=2000.0, YMAX=2000.0, ZMAX=2000.0, InterpOrder=2,
+                         NK=160, Maxk=1.6))
+    ts = torch.cuda.Stream(device=dev)
+    res, ms = {}, {}
+    for prec in ("fp32", "det", "fp64"):
+        with cg.PowerSpectrum(p, precision=prec, spectra=["dd", "dp", "pp"], stream=ts.cuda_stream) as ps:
+            reps = 2 if prec == "fp64" else 4
+            times = []
+            for it in range(reps + 1):
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(ts)
+                ps.paint(*d)
+                r = ps.power()
+                e1.record(ts)
+                torch.cuda.synchronize()
+                if it:
+                    times.append(e0.elapsed_time(e1))
+            res[prec], ms[prec] = r, statistics.median(times)
+    acc = {}
+    for prec in ("fp32", "det"):
+        acc[prec] = {}
+        for q, name in enumerate(("dd", "dp", "pp")):
+            r, r64 = res[prec][q], res["fp64"][q]
+            m = np.asarray(r64["Nmodes"]) > 0
+            n0 = np.abs(r64["Pk0"]) if name != "dp" else np.sqrt(np.abs(res["fp64"][0]["Pk0"] * res["fp64"][2]["Pk0"]))
+            acc[prec][name] = {f"l{l}": float(np.max((2 * l + 1) * np.abs(r[f"Pk{l}"][m] - r64[f"Pk{l}"][m]) / n0[m]))
+                               for l in (0, 2, 4)}
+            acc[prec][name]["nmodes_equal"] = bool(np.array_equal(r["Nmodes"], r64["Nmodes"]))
+    line = {"metric": "ms per dd+dp+pp P0/2/4(k), 1024^3 CIC, 134M particles", "unit": "ms", "higher_is_better": False,
+            "fp32_ms": round(ms["fp32"], 2), "det_ms": round(ms["det"], 2), "fp64_ms": round(ms["fp64"], 2),
+            "accuracy_vs_fp64": acc, "n_gpus": 1, "data": "synthetic (seeded Zel'dovich lattice, f32)",
+            "config": {"workload": "512^3 lattice (134,217,728 particles), L=2000 Mpc/h, CIC 1024^3, interlaced, "
+                                   "dd+dp+pp, LOS=z, NK=160 to k=1.6"}}
+    print(json.dumps(line), flush=True)
+
+
 def gpu_bench(args, world, rank, local):
     import torch
 
@@ -426,6 +476,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--batch", action="store_true", help="run the batched-mocks workload instead (mocks/s)")
     ap.add_argument("--mocks", type=int, default=256)
+    ap.add_argument("--scale", action="store_true", help="run the 1024^3 / 134M-particle workload instead")
     ap.add_argument("--profile-case", action="store_true",
                     help="run the 8x smaller workload for profiler captures (prints stage times only)")
     args = ap.parse_args()
@@ -435,6 +486,9 @@ def main():
         return
     if args.batch:
         batch_bench(args)
+        return
+    if args.scale:
+        scale_bench(args)
         return
     world, rank, local = dist_init()
     log = (lambda *a: print(*a, file=sys.stderr, flush=True))
