@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "ctx.cuh"
+#include "paint_dev.cuh"
 
 template <typename R>
 struct AdjC;
@@ -176,71 +177,160 @@ __device__ __forceinline__ void adj_axis_deriv(int order, double scale, double *
   }
 }
 
-// Step 4: per particle, the transpose of its deposit.
+// dL/d(particle) from the deposit's gradient sums: g0 = sum G W, gs = sum G dW/dscale per axis.
+template <typename T>
+__device__ __forceinline__ void adj_store(const Geom &g, const FieldSpec &fs, double v, double w, double g0,
+                                          const double *gs, bool accepted, double dLdN, long long p, T *ox, T *oy,
+                                          T *oz, T *ov, T *ow) {
+  const int e = fs.ea;
+  double ve = 1.0;
+  for (int k = 0; k < e; k++) ve *= v;
+  const double val = w * ve;  // deposit value w v^e (field A)
+  const double dxr = val * gs[0] / g.dx, dyr = val * gs[1] / g.dy, dzr = val * gs[2] / g.dz;
+  const double dw = ve * g0 + (accepted ? dLdN : 0.0);
+  double dv = 0.0;
+  if (e > 0) {
+    double vm = 1.0;
+    for (int k = 0; k < e - 1; k++) vm *= v;
+    dv = w * (double)e * vm * g0;
+  }
+  const double rsd = g.rsd_opz / g.rsd_den;  // d(shifted LOS coordinate)/dv
+  if (g.los == 1) dv += rsd * dxr;
+  else if (g.los == 2) dv += rsd * dyr;
+  else if (g.los == 3) dv += rsd * dzr;
+  if (ox) ox[p] = (T)dxr;
+  if (oy) oy[p] = (T)dyr;
+  if (oz) oz[p] = (T)dzr;
+  if (ov) ov[p] = (T)dv;
+  if (ow) ow[p] = (T)dw;
+}
+
+// Step 4 for one particle by the exact FP64 rules: the transpose of its deposit (same taps, halo
+// fold and dropped writes) read from dL/dgrid with the weight derivatives.
+template <typename T, typename R>
+__device__ __forceinline__ void adj_particle_exact(const Geom &g, const FieldSpec &fs, const PIn<T> &in, long long p,
+                                                   const R *gA, const R *gAi, double dLdN, T *ox, T *oy, T *oz,
+                                                   T *ov, T *ow) {
+  double x = (double)in.x[p], y = (double)in.y[p], z = (double)in.z[p];
+  const double v = fs.need_v ? (double)in.v[p] : 0.0, w = in.w ? (double)in.w[p] : 1.0;
+  if (g.los == 1) x = rsd_shift64(g, x, v);
+  else if (g.los == 2) y = rsd_shift64(g, y, v);
+  else if (g.los == 3) z = rsd_shift64(g, z, v);
+  double g0 = 0.0, gs[3] = {0.0, 0.0, 0.0};
+  bool accepted = false;
+  if (!outside_box(g, x, y, z)) {
+    const int nst = g.interlace ? 2 : 1;
+    for (int st = 0; st < nst; st++) {
+      const double px = st ? DADD(x, g.hx) : x, py = st ? DADD(y, g.hy) : y, pz = st ? DADD(z, g.hz) : z;
+      AxisTaps ax, ay, az;
+      if (!exact_axes(g, px, py, pz, ax, ay, az)) continue;
+      if (st == 0) accepted = true;
+      // the scales exact_axes used (TSC with LOS == 0 maps x - XMIN < dx to x + L first)
+      double qx = px;
+      if (g.order == 3 && g.los == 0 && DSUB(qx, g.xmin) < g.dx) qx = DADD(qx, g.lx);
+      double dx3[3], dy3[3], dz3[3];
+      adj_axis_deriv(g.order, DDIV(DSUB(qx, g.xmin), g.dx), dx3);
+      adj_axis_deriv(g.order, DDIV(DSUB(py, g.ymin), g.dy), dy3);
+      adj_axis_deriv(g.order, DDIV(DSUB(pz, g.zmin), g.dz), dz3);
+      const R *gr = st ? gAi : gA;
+      for (int c = 0; c < az.n; c++)
+        for (int b = 0; b < ay.n; b++)
+          for (int a = 0; a < ax.n; a++) {
+            if (!(ax.on[a] && ay.on[b] && az.on[c])) continue;
+            const long long L = canon_index(g, ax.idx[a], ay.idx[b], az.idx[c]);
+            if (L < 0) continue;
+            const double G = (double)gr[L];
+            g0 += G * ax.w[a] * ay.w[b] * az.w[c];
+            gs[0] += G * dx3[a] * ay.w[b] * az.w[c];
+            gs[1] += G * ax.w[a] * dy3[b] * az.w[c];
+            gs[2] += G * ax.w[a] * ay.w[b] * dz3[c];
+          }
+    }
+  }
+  adj_store(g, fs, v, w, g0, gs, accepted, dLdN, p, ox, oy, oz, ov, ow);
+}
+
 template <typename T, typename R>
 __global__ void __launch_bounds__(128) k_adj_readout(Geom g, FieldSpec fs, PIn<T> in, long long n, const R *gA,
                                                      const R *gAi, double dLdN_host, const double *gamma0,
                                                      T *ox, T *oy, T *oz, T *ov, T *ow) {
   const double dLdN = dLdN_host - gamma0[0] - (g.interlace ? gamma0[1] : 0.0);
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x)
+    adj_particle_exact<T, R>(g, fs, in, p, gA, gAi, dLdN, ox, oy, oz, ov, ow);
+}
+
+// FP32 per-axis weight derivatives of the taps axis32k produced (same offset d).
+template <int K>
+__device__ __forceinline__ void adj_axis_deriv32(float s, int kind, int n, int los, float *dw) {
+  if (K == 3) {
+    if (kind == 0 && los == 0 && s < 1.0f) s += (float)n;  // the x shift of tsc_axis32
+    const int i = (int)(s + 0.5f);
+    const float d = s - (float)i;
+    dw[0] = -2.0f * d;
+    dw[1] = -(0.5f - d);
+    dw[2] = 0.5f + d;
+  } else if (K == 2) {
+    dw[0] = -1.0f;
+    dw[1] = 1.0f;
+    dw[2] = 0.0f;
+  } else {
+    dw[0] = dw[1] = dw[2] = 0.0f;
+  }
+}
+
+// Step 4 for FP32 contexts: particles away from every edge of the reference's rules gather their
+// taps with the FP32 rules of the paint (the same ones that deposited them); the others take the
+// exact FP64 path.
+template <int K, typename T>
+__global__ void __launch_bounds__(128) k_adj_readout32(Geom g, FieldSpec fs, PIn<T> in, long long n,
+                                                       const float *gA, const float *gAi, double dLdN_host,
+                                                       const double *gamma0, T *ox, T *oy, T *oz, T *ov, T *ow) {
+  const double dLdN = dLdN_host - gamma0[0] - (g.interlace ? gamma0[1] : 0.0);
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
-    double x = (double)in.x[p], y = (double)in.y[p], z = (double)in.z[p];
-    const double v = fs.need_v ? (double)in.v[p] : 0.0, w = in.w ? (double)in.w[p] : 1.0;
-    if (g.los == 1) x = rsd_shift64(g, x, v);
-    else if (g.los == 2) y = rsd_shift64(g, y, v);
-    else if (g.los == 3) z = rsd_shift64(g, z, v);
-    double g0 = 0.0, gs[3] = {0.0, 0.0, 0.0};
+    const Prep pr = prep32(g, fs, in, p);
+    if (!pr.fin || is_edge(g, pr.sx, pr.sy, pr.sz)) {
+      adj_particle_exact<T, float>(g, fs, in, p, gA, gAi, dLdN, ox, oy, oz, ov, ow);
+      continue;
+    }
+    float g0 = 0.0f, gs[3] = {0.0f, 0.0f, 0.0f};
     bool accepted = false;
-    if (!outside_box(g, x, y, z)) {
-      const int nst = g.interlace ? 2 : 1;
-      for (int st = 0; st < nst; st++) {
-        const double px = st ? DADD(x, g.hx) : x, py = st ? DADD(y, g.hy) : y, pz = st ? DADD(z, g.hz) : z;
-        AxisTaps ax, ay, az;
-        if (!exact_axes(g, px, py, pz, ax, ay, az)) continue;
-        if (st == 0) accepted = true;
-        // the scales exact_axes used (TSC with LOS == 0 maps x - XMIN < dx to x + L first)
-        double qx = px;
-        if (g.order == 3 && g.los == 0 && DSUB(qx, g.xmin) < g.dx) qx = DADD(qx, g.lx);
-        double dx3[3], dy3[3], dz3[3];
-        adj_axis_deriv(g.order, DDIV(DSUB(qx, g.xmin), g.dx), dx3);
-        adj_axis_deriv(g.order, DDIV(DSUB(py, g.ymin), g.dy), dy3);
-        adj_axis_deriv(g.order, DDIV(DSUB(pz, g.zmin), g.dz), dz3);
-        const R *gr = st ? gAi : gA;
-        for (int c = 0; c < az.n; c++)
-          for (int b = 0; b < ay.n; b++)
-            for (int a = 0; a < ax.n; a++) {
-              if (!(ax.on[a] && ay.on[b] && az.on[c])) continue;
-              const long long L = canon_index(g, ax.idx[a], ay.idx[b], az.idx[c]);
-              if (L < 0) continue;
-              const double G = (double)gr[L];
-              g0 += G * ax.w[a] * ay.w[b] * az.w[c];
-              gs[0] += G * dx3[a] * ay.w[b] * az.w[c];
-              gs[1] += G * ax.w[a] * dy3[b] * az.w[c];
-              gs[2] += G * ax.w[a] * ay.w[b] * dz3[c];
-            }
+    const int nst = g.interlace ? 2 : 1;
+    for (int st = 0; st < nst; st++) {
+      const float sx = st ? __fadd_rn(pr.sx, 0.5f) : pr.sx, sy = st ? __fadd_rn(pr.sy, 0.5f) : pr.sy,
+                  sz = st ? __fadd_rn(pr.sz, 0.5f) : pr.sz;
+      if (!accept32(g, sx, sy, sz)) continue;
+      if (st == 0) accepted = true;
+      AxisTapsF ax, ay, az;
+      axis32k<K>(sx, 0, g.nx, g.los, ax);
+      axis32k<K>(sy, 1, g.ny, g.los, ay);
+      axis32k<K>(sz, 1, g.nz, g.los, az);
+      float dx3[3], dy3[3], dz3[3];
+      adj_axis_deriv32<K>(sx, 0, g.nx, g.los, dx3);
+      adj_axis_deriv32<K>(sy, 1, g.ny, g.los, dy3);
+      adj_axis_deriv32<K>(sz, 1, g.nz, g.los, dz3);
+      const float *gr = st ? gAi : gA;
+#pragma unroll
+      for (int a = 0; a < K; a++) {
+        if (ax.idx[a] < 0) continue;
+#pragma unroll
+        for (int b = 0; b < K; b++) {
+          if (ay.idx[b] < 0) continue;
+          const long long rowb = ((long long)ax.idx[a] * g.ny + ay.idx[b]) * g.row;
+#pragma unroll
+          for (int c = 0; c < K; c++) {
+            if (az.idx[c] < 0) continue;
+            const float G = gr[rowb + az.idx[c]];
+            const float wyz = ay.w[b] * az.w[c];
+            g0 += G * ax.w[a] * wyz;
+            gs[0] += G * dx3[a] * wyz;
+            gs[1] += G * ax.w[a] * dy3[b] * az.w[c];
+            gs[2] += G * ax.w[a] * ay.w[b] * dz3[c];
+          }
+        }
       }
     }
-    // deposit value w v^e (field A); its derivatives
-    const int e = fs.ea;
-    double ve = 1.0;
-    for (int k = 0; k < e; k++) ve *= v;
-    const double val = w * ve;
-    const double dxr = val * gs[0] / g.dx, dyr = val * gs[1] / g.dy, dzr = val * gs[2] / g.dz;
-    double dw = ve * g0 + (accepted ? dLdN : 0.0);
-    double dv = 0.0;
-    if (e > 0) {
-      double vm = 1.0;
-      for (int k = 0; k < e - 1; k++) vm *= v;
-      dv = w * (double)e * vm * g0;
-    }
-    const double rsd = g.rsd_opz / g.rsd_den;  // d(shifted LOS coordinate)/dv
-    if (g.los == 1) dv += rsd * dxr;
-    else if (g.los == 2) dv += rsd * dyr;
-    else if (g.los == 3) dv += rsd * dzr;
-    if (ox) ox[p] = (T)dxr;
-    if (oy) oy[p] = (T)dyr;
-    if (oz) oz[p] = (T)dzr;
-    if (ov) ov[p] = (T)dv;
-    if (ow) ow[p] = (T)dw;
+    const double gsd[3] = {(double)gs[0], (double)gs[1], (double)gs[2]};
+    adj_store(g, fs, (double)pr.v, (double)pr.w, (double)g0, gsd, accepted, dLdN, p, ox, oy, oz, ov, ow);
   }
 }
 
@@ -365,21 +455,33 @@ extern "C" int capow_backward(capow_ctx *c, const double *const dL_dP[5], const 
   }
   const capow_particles &d = c->last;
   const int nb = (int)((n + 127) / 128 > 152 * 16 ? 152 * 16 : ((n + 127) / 128 < 1 ? 1 : (n + 127) / 128));
-#define ADJ_RUN(TI, TO, R)                                                                                       \
-  k_adj_readout<TI, R><<<nb, 128, 0, c->stream>>>(                                                               \
-      c->g, c->fs, PIn<TI>{(const TI *)d.x, (const TI *)d.y, (const TI *)d.z, (const TI *)d.vlos, (const TI *)d.w}, \
-      n, (const R *)gA, (const R *)gAi, dLdN, gamma0, (TO *)dev[0], (TO *)dev[1], (TO *)dev[2], (TO *)dev[3],     \
-      (TO *)dev[4])
+#define ADJ_IN(TI) \
+  PIn<TI> { (const TI *)d.x, (const TI *)d.y, (const TI *)d.z, (const TI *)d.vlos, (const TI *)d.w }
+#define ADJ_OUT(TO) (TO *)dev[0], (TO *)dev[1], (TO *)dev[2], (TO *)dev[3], (TO *)dev[4]
+#define ADJ_RUN64(T) \
+  k_adj_readout<T, double><<<nb, 128, 0, c->stream>>>(c->g, c->fs, ADJ_IN(T), n, (const double *)gA, \
+                                                      (const double *)gAi, dLdN, gamma0, ADJ_OUT(T))
+#define ADJ_RUN32(K, T) \
+  k_adj_readout32<K, T><<<nb, 128, 0, c->stream>>>(c->g, c->fs, ADJ_IN(T), n, (const float *)gA, \
+                                                   (const float *)gAi, dLdN, gamma0, ADJ_OUT(T))
   if (d.dtype != out->dtype)
     FAIL(c, CAPOW_EINVAL, "capow_backward: gradient dtype must match the painted particles' dtype");
-  if (d.dtype == CAPOW_F64) {
-    if (f64) ADJ_RUN(double, double, double);
-    else ADJ_RUN(double, double, float);
+  if (f64) {
+    if (d.dtype == CAPOW_F64) ADJ_RUN64(double);
+    else ADJ_RUN64(float);
+  } else if (d.dtype == CAPOW_F64) {
+    if (p.InterpOrder == 3) ADJ_RUN32(3, double);
+    else if (p.InterpOrder == 2) ADJ_RUN32(2, double);
+    else ADJ_RUN32(1, double);
   } else {
-    if (f64) ADJ_RUN(float, float, double);
-    else ADJ_RUN(float, float, float);
+    if (p.InterpOrder == 3) ADJ_RUN32(3, float);
+    else if (p.InterpOrder == 2) ADJ_RUN32(2, float);
+    else ADJ_RUN32(1, float);
   }
-#undef ADJ_RUN
+#undef ADJ_IN
+#undef ADJ_OUT
+#undef ADJ_RUN64
+#undef ADJ_RUN32
   c->launches++;
   CK(c, cudaGetLastError());
   if (!out->on_device)
