@@ -114,6 +114,7 @@ extern "C" int capow_batch(capow_mock *mocks, int nmocks, const capow_options *o
         continue;
       }
       c->quiet = true;
+      c->two_pass = true;  // record buffers sized once per shape (prepare_paint_buffers)
       ctxs[k] = c;
     }
     ctx_of[i] = ctxs[k];

@@ -333,10 +333,36 @@ int enqueue_paint(capow_ctx *c, const capow_particles &d) {
       CK(c, cudaMalloc(&c->pb.edge_list, sizeof(unsigned) * (n + 1)));
       c->pb.edge_cap = n + 1;
     }
-    unsigned long long want = (unsigned long long)(tile_dup_estimate(c->g, c->tg) * 1.25 * n) + 65536;
-    if (c->pb.capacity < want / 2 || (d.w && !c->pb.recw)) {
-      int rc = ensure_records(c, want, d.w != nullptr);
+    c->pb.bucket_cap = 0;
+    if (c->prec == CAPOW_FP32_MIXED && !c->two_pass) {
+      // bucket mode: each tile gets twice its mean share of the records (plus slack); the overflow
+      // list takes up to a quarter of the catalogue; beyond that the paint falls back to two passes
+      const double mean = tile_dup_estimate(c->g, c->tg) * (double)n / (double)c->tg.ntiles;
+      const unsigned cap = ((unsigned)(2.0 * mean) + 64 + 31) & ~31u;
+      int rc = ensure_records(c, (unsigned long long)cap * c->tg.ntiles, d.w != nullptr);
       if (rc) return rc;
+      const unsigned long long ocap = (unsigned long long)n / 4 + 65536;
+      if (!c->pb.ovf_count) CK(c, cudaMalloc(&c->pb.ovf_count, sizeof(unsigned)));
+      if (c->pb.ovf_cap < ocap || (d.w && !c->pb.ovf_w)) {
+        if (c->pb.ovf_recs) cudaFree(c->pb.ovf_recs);
+        if (c->pb.ovf_w) cudaFree(c->pb.ovf_w);
+        if (c->pb.ovf_tile) cudaFree(c->pb.ovf_tile);
+        c->pb.ovf_recs = nullptr;
+        c->pb.ovf_w = nullptr;
+        c->pb.ovf_tile = nullptr;
+        c->pb.ovf_cap = 0;
+        CK(c, cudaMalloc(&c->pb.ovf_recs, sizeof(float4) * ocap));
+        CK(c, cudaMalloc(&c->pb.ovf_tile, sizeof(unsigned) * ocap));
+        if (d.w) CK(c, cudaMalloc(&c->pb.ovf_w, sizeof(float) * ocap));
+        c->pb.ovf_cap = ocap;
+      }
+      c->pb.bucket_cap = cap;
+    } else {
+      unsigned long long want = (unsigned long long)(tile_dup_estimate(c->g, c->tg) * 1.25 * n) + 65536;
+      if (c->pb.capacity < want / 2 || (d.w && !c->pb.recw)) {
+        int rc = ensure_records(c, want, d.w != nullptr);
+        if (rc) return rc;
+      }
     }
     launch_paint32(c->stream, c->g, c->fs, c->tg, c->prec == CAPOW_FP32_DETERMINISTIC, d.dtype, d.x, d.y, d.z,
                    d.vlos, d.w, n, gp, c->pb, c->st, &c->launches);
@@ -394,6 +420,13 @@ extern "C" int capow_paint(capow_ctx *c, const capow_particles *parts) {
 static int settle_paint(capow_ctx *c) {
   CK(c, cudaMemcpyAsync(c->h_st, c->st, sizeof(DevStats), cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
+  if (c->h_st->overflow && c->pb.bucket_cap) {  // the overflow list filled: two passes from now on
+    c->two_pass = true;
+    int rc = enqueue_paint(c, c->last);
+    if (rc) return rc;
+    CK(c, cudaMemcpyAsync(c->h_st, c->st, sizeof(DevStats), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+  }
   if (c->h_st->overflow) {
     int rc = ensure_records(c, (unsigned long long)c->h_st->nrecords + 65536, c->last.w != nullptr);
     if (rc) return rc;
@@ -517,7 +550,8 @@ extern "C" int capow_power(capow_ctx *c, capow_spectrum *out, int nout) {
   CK(c, cudaStreamSynchronize(c->stream));
   if (c->h_st->overflow) {  // rare: tile lists outgrew the estimate; repaint and redo
     c->powered = false;
-    rc = ensure_records(c, (unsigned long long)c->h_st->nrecords + 65536, c->last.w != nullptr);
+    if (c->pb.bucket_cap) c->two_pass = true;  // the bucket overflow list filled
+    else rc = ensure_records(c, (unsigned long long)c->h_st->nrecords + 65536, c->last.w != nullptr);
     if (rc) return rc;
     rc = enqueue_paint(c, c->last);
     if (rc) return rc;
@@ -645,6 +679,10 @@ extern "C" void capow_destroy(capow_ctx *c) {
   if (c->pb.recw) cudaFree(c->pb.recw);
   if (c->pb.edge_list) cudaFree(c->pb.edge_list);
   if (c->pb.edge_count) cudaFree(c->pb.edge_count);
+  if (c->pb.ovf_recs) cudaFree(c->pb.ovf_recs);
+  if (c->pb.ovf_w) cudaFree(c->pb.ovf_w);
+  if (c->pb.ovf_tile) cudaFree(c->pb.ovf_tile);
+  if (c->pb.ovf_count) cudaFree(c->pb.ovf_count);
   if (c->h_bins) cudaFreeHost(c->h_bins);
   if (c->h_st) cudaFreeHost(c->h_st);
   for (int k = 0; k < 4; k++)

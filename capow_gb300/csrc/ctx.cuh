@@ -43,6 +43,7 @@ struct capow_ctx {
   XbinGeo xg;
   // capow_backward (created on first use): full 3-D plans, bin coefficients, host-output staging
   bool quiet;           // skip the stage-timing event records (batched enqueue, graph capture)
+  bool two_pass;        // FP32 paint: count/scan/scatter instead of the one-pass buckets
   bool adj_plans;
   cufftHandle adj_fwd, adj_inv;
   double *adj_coef;

@@ -455,6 +455,98 @@ __global__ void __launch_bounds__(256) k_scatter(Geom g, FieldSpec fs, TileGeo t
   }
 }
 
+// Bucket mode, passes 1-3 in one: the statistics of k_count and the records of k_scatter, each
+// written into its tile's fixed-capacity bucket (slot from the run-aggregated tile counter); a
+// record that finds its bucket full goes to the overflow list with its tile.
+template <typename T>
+__global__ void __launch_bounds__(256) k_bucket(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in, long long n,
+                                                unsigned *counts, float4 *recs, float *recw, unsigned cap,
+                                                unsigned *edge_list, unsigned *edge_count, float4 *ovf_recs,
+                                                float *ovf_w, unsigned *ovf_tile, unsigned *ovf_count,
+                                                unsigned long long ovf_cap, DevStats *st) {
+  float f_read = 0, f_out = 0, f_nsq = 0, f_v[4] = {0, 0, 0, 0}, f_abs[2] = {0, 0}, f_grid = 0;
+  int fatal = 0, nonfin = 0, ovf_full = 0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); i0 < n; i0 += stride) {
+    const long long i = i0 + (threadIdx.x & 31);
+    bool has = false;
+    AxisTiles TX, TY, TZ;
+    TX.n = TY.n = TZ.n = 0;
+    float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
+    float w = 1.0f;
+    if (i < n) {
+      const Prep p = prep32(g, fs, in, i);
+      if (!p.fin) {
+        nonfin = 1;
+      } else {
+        f_read += 1.0f;
+        if (fs.moments) {  // src/read_data.c:132-138, every particle read
+          f_nsq += p.w;
+          float wv = p.w * p.v;
+          f_v[0] += wv; wv *= p.v;
+          f_v[1] += wv; wv *= p.v;
+          f_v[2] += wv; wv *= p.v;
+          f_v[3] += wv;
+        }
+        float pa = p.w, pb = p.w;
+        for (int e = 0; e < fs.ea; e++) pa *= p.v;
+        for (int e = 0; e < fs.eb; e++) pb *= p.v;
+        f_abs[0] += fabsf(pa);
+        f_abs[1] += fabsf(pb);
+        if (!footprint(g, tg, p.sx, p.sy, p.sz, TX, TY, TZ)) {
+          f_out += 1.0f;  // outside the box by at least two cells (src/read_data.c:81-88)
+          if (g.los == 0) {
+            fatal = 1;
+            atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)i);
+          }
+        } else if (is_edge(g, p.sx, p.sy, p.sz)) {
+          edge_list[atomicAdd(edge_count, 1u)] = (unsigned)i;  // painted and counted by k_edge_fixup
+        } else {
+          has = true;
+          w = p.w;
+          rec = make_float4(p.sx, p.sy, p.sz, p.v);
+          if (accept32(g, p.sx, p.sy, p.sz)) f_grid += p.w;  // NGRID (src/read_data.c:92-126)
+        }
+      }
+    }
+    const int na = __reduce_max_sync(FULL_MASK, has ? TX.n : 0), nb = __reduce_max_sync(FULL_MASK, has ? TY.n : 0),
+              nc = __reduce_max_sync(FULL_MASK, has ? TZ.n : 0);
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          if (!(a < na && b < nb && c < nc)) continue;  // warp-uniform
+          const int key = tile_key(tg, has, TX, TY, TZ, a, b, c);
+          const unsigned slot = warp_run_add(counts, key, true);
+          if (key < 0) continue;
+          if (slot < cap) {
+            const unsigned long long r = (unsigned long long)key * cap + slot;
+            recs[r] = rec;
+            if (recw) recw[r] = w;
+          } else {
+            const unsigned o = atomicAdd(ovf_count, 1u);
+            if (o < ovf_cap) {
+              ovf_recs[o] = rec;
+              if (ovf_w) ovf_w[o] = w;
+              ovf_tile[o] = (unsigned)key;
+            } else {
+              ovf_full = 1;
+            }
+          }
+        }
+  }
+  const double vals[10] = {(double)f_read, (double)f_out, (double)f_nsq, (double)f_v[0], (double)f_v[1],
+                           (double)f_v[2], (double)f_v[3], (double)f_abs[0], (double)f_abs[1], (double)f_grid};
+  double *const dst[10] = {&st->nread, &st->nout, &st->nsq, &st->vr[0], &st->vr[1], &st->vr[2], &st->vr[3],
+                           &st->absw[0], &st->absw[1], &st->ngrid};
+  block_add<10>(vals, dst);
+  if (fatal) atomicOr(&st->fatal, 1);
+  if (nonfin) atomicOr(&st->nonfinite, 1);
+  if (ovf_full) atomicOr(&st->overflow, 1);
+}
+
 // Pass 4: one CTA per tile. Shared memory holds the tile of every grid slot; taps outside the
 // tile are skipped (another tile owns them). The particle's home tile also adds it to the
 // statistics that need exact decisions: NGRID, the out-of-box count and the LOS == 0 error.
@@ -719,6 +811,81 @@ __device__ __forceinline__ int tile_scale_exp(float sum_abs) {
   return S > 100 ? 100 : (S < -100 ? -100 : S);
 }
 
+// The int32 quantum of a tile is about 2^-30 of the tile's total |w v^e|, and a cell sums up to one
+// rounded deposit per record: the cells' relative error grows with the record count. A tile with
+// more records than this (a dense clump; uniform catalogues put about a thousand records in a
+// tile) is accumulated in int64 with 2^61 headroom instead, one grid slot and one shared-memory
+// chunk of cells per pass over its records (the records are re-read from L2 for each pass).
+#define TILE_PRECISE_RECORDS 16384
+
+template <int K, int NF, bool IL>
+__device__ void tile_paint_precise(const Geom &g, const FieldSpec &fs, const TileGeo &tg, const float4 *recs,
+                                   const float *recw, unsigned long long rb, unsigned long long re, float ta, float tb,
+                                   int x0, int y0, int z0, int ex, int ey, int ez, int pyz, int tsz,
+                                   long long *sm64, int chunk, GridPtrs grids, DevStats *st) {
+  constexpr int NS = IL ? 2 : 1;
+  const int S64a = 60 - ilogbf(fmaxf(ta * 1.001f, 1e-30f)), S64b = 60 - ilogbf(fmaxf(tb * 1.001f, 1e-30f));
+  for (int slot = 0; slot < NS * NF; slot++) {
+    const int sten = slot / NF, fld = slot % NF;
+    const int S64 = fld == 0 ? S64a : S64b;
+    const float sc = ldexpf(1.0f, S64 > 100 ? 100 : S64);
+    float dsum = 0.0f;
+    for (int c0 = 0; c0 < tsz; c0 += chunk) {
+      const int c1 = min(tsz, c0 + chunk);
+      for (int c = threadIdx.x; c < c1 - c0; c += blockDim.x) sm64[c] = 0;
+      __syncthreads();
+      for (unsigned long long r = rb + threadIdx.x; r < re; r += blockDim.x) {
+        const float4 rec = recs[r];
+        const float w = recw ? recw[r] : 1.0f;
+        float v = w;
+        const int e_n = fld == 0 ? fs.ea : fs.eb;
+        for (int e = 0; e < e_n; e++) v *= rec.w;
+        v *= sc;
+        const float sx = sten ? __fadd_rn(rec.x, 0.5f) : rec.x, sy = sten ? __fadd_rn(rec.y, 0.5f) : rec.y,
+                    sz = sten ? __fadd_rn(rec.z, 0.5f) : rec.z;
+        if (!accept32(g, sx, sy, sz)) continue;
+        AxisTapsF ax, ay, az;
+        axis32k<K>(sx, 0, g.nx, g.los, ax);
+        axis32k<K>(sy, 1, g.ny, g.los, ay);
+        axis32k<K>(sz, 1, g.nz, g.los, az);
+        float wx[3], wy[3], wz[3];
+        int ox[3], oy[3], oz[3];
+        stage_axis32(ax, x0, ex, pyz, wx, ox);
+        stage_axis32(ay, y0, ey, tg.tz, wy, oy);
+        stage_axis32(az, z0, ez, 1, wz, oz);
+#pragma unroll
+        for (int a = 0; a < K; a++)
+#pragma unroll
+          for (int b2 = 0; b2 < K; b2++) {
+            const float wxy = wx[a] * wy[b2];
+            const float pv = v * wxy;
+            const int oxy = ox[a] + oy[b2];
+#pragma unroll
+            for (int c = 0; c < K; c++) {
+              const int off = oxy + oz[c] - c0;
+              if (wxy != 0.0f && wz[c] != 0.0f && off >= 0 && off < c1 - c0)
+                atomicAdd((unsigned long long *)(sm64 + off), (unsigned long long)__float2ll_rn(pv * wz[c]));
+            }
+          }
+      }
+      __syncthreads();
+      const double inv = ldexp(1.0, -(S64 > 100 ? 100 : S64));
+      float *gp = (float *)grids.g[slot];
+      for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+        const int rz = c & (tg.tz - 1), ly = (c >> tg.lz) & (tg.ty - 1), lx = c >> (tg.lz + tg.ly);
+        if (lx >= ex || ly >= ey || rz >= ez) continue;
+        const float val = (float)((double)sm64[c - c0] * inv);
+        gp[(long long)(x0 + lx) * g.slice + (long long)(y0 + ly) * g.row + z0 + rz] = val;
+        dsum += val;
+      }
+      __syncthreads();
+    }
+    const double vals[1] = {(double)dsum};
+    double *const dst1[1] = {&st->dc[slot]};
+    block_add<1>(vals, dst1);
+  }
+}
+
 // FP32 tile kernel for particles away from every edge of the reference's rules (those are painted
 // by k_edge_fixup). One CTA per tile; shared memory holds the tile of every grid slot, both
 // stencils, unpadded [tx][ty][tz], as int32 fixed point with a per-tile power-of-two scale, so
@@ -728,8 +895,9 @@ __device__ __forceinline__ int tile_scale_exp(float sum_abs) {
 // these particles is counted by k_count.)
 template <int K, int NF, bool IL>
 __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileGeo tg, const unsigned *offsets,
-                                                     const float4 *recs, const float *recw,
-                                                     unsigned long long capacity, GridPtrs grids, DevStats *st) {
+                                                     const unsigned *counts, unsigned cap, const float4 *recs,
+                                                     const float *recw, unsigned long long capacity, GridPtrs grids,
+                                                     DevStats *st) {
   extern __shared__ __align__(16) int smi[];
   constexpr int NS = IL ? 2 : 1;
   const int tsz = tg.tx * tg.ty * tg.tz;
@@ -741,14 +909,21 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
   int4 *sm4 = reinterpret_cast<int4 *>(smi);
   for (int c = threadIdx.x; c < (NS * NF * tsz) >> 2; c += blockDim.x) sm4[c] = make_int4(0, 0, 0, 0);
   __syncthreads();
-  unsigned rb = offsets[tile], re = offsets[tile + 1];
-  if (re > capacity) re = (unsigned)capacity;
+  unsigned long long rb, re;
+  if (cap) {  // bucket mode: the tile's own bucket
+    rb = (unsigned long long)tile * cap;
+    re = rb + min(counts[tile], cap);
+  } else {
+    rb = offsets[tile];
+    re = offsets[tile + 1];
+  }
+  if (re > capacity) re = capacity;
   if (rb > re) rb = re;
   // pre-pass over the tile's records: sum |w v^e| per field (the records stay in L1 for the deposits)
   __shared__ float red_abs[2][32];
   {
     float la = 0.0f, lb = 0.0f;
-    for (unsigned r = rb + threadIdx.x; r < re; r += blockDim.x) {
+    for (unsigned long long r = rb + threadIdx.x; r < re; r += blockDim.x) {
       const float4 rec = recs[r];
       const float w = recw ? recw[r] : 1.0f;
       float va = w, vb = w;
@@ -771,8 +946,14 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
     tb += red_abs[1][k];
   }
   const int SA = tile_scale_exp(ta), SB = tile_scale_exp(tb);
+  if (re - rb > TILE_PRECISE_RECORDS) {  // a dense tile (uniform over the CTA)
+    const int words = NS * NF * tsz;  // the int32 tile area, reused as int64 cells
+    tile_paint_precise<K, NF, IL>(g, fs, tg, recs, recw, rb, re, ta, tb, x0, y0, z0, ex, ey, ez, pyz, tsz,
+                                  reinterpret_cast<long long *>(smi), words / 2, grids, st);
+    return;
+  }
   const float scA = ldexpf(1.0f, SA), scB = ldexpf(1.0f, SB);
-  for (unsigned r = rb + threadIdx.x; r < re; r += blockDim.x) {
+  for (unsigned long long r = rb + threadIdx.x; r < re; r += blockDim.x) {
     const float4 rec = recs[r];
     const float w = recw ? recw[r] : 1.0f;
     float va = w, vb = w;
@@ -839,6 +1020,67 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
     double *const dst1[1] = {&st->dc[slot]};
     block_add<1>(vals, dst1);
   }
+}
+
+// Bucket mode: records that found their tile's bucket full, deposited after the tiles were written
+// (FP32 global atomics), each restricted to the taps inside its own tile, with their DC sums.
+template <int K, int NF, bool IL>
+__global__ void __launch_bounds__(128) k_ovf_paint(Geom g, FieldSpec fs, TileGeo tg, const float4 *ovf_recs,
+                                                   const float *ovf_w, const unsigned *ovf_tile,
+                                                   const unsigned *ovf_count, unsigned long long ovf_cap,
+                                                   GridPtrs grids, DevStats *st) {
+  constexpr int NS = IL ? 2 : 1;
+  const unsigned long long no = min((unsigned long long)*ovf_count, ovf_cap);
+  double l_dc[4] = {0, 0, 0, 0};
+  for (unsigned long long o = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; o < no;
+       o += (unsigned long long)gridDim.x * blockDim.x) {
+    const float4 rec = ovf_recs[o];
+    const float w = ovf_w ? ovf_w[o] : 1.0f;
+    const int tile = (int)ovf_tile[o];
+    const int bz = tile % tg.nbz, by = (tile / tg.nbz) % tg.nby, bx = tile / (tg.nbz * tg.nby);
+    const int x0 = bx * tg.tx, y0 = by * tg.ty, z0 = bz * tg.tz;
+    const int ex = min(tg.tx, g.nx - x0), ey = min(tg.ty, g.ny - y0), ez = min(tg.tz, g.nz - z0);
+    float va = w, vb = w;
+    for (int e = 0; e < fs.ea; e++) va *= rec.w;
+    for (int e = 0; e < fs.eb; e++) vb *= rec.w;
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+      const float sx = s ? __fadd_rn(rec.x, 0.5f) : rec.x, sy = s ? __fadd_rn(rec.y, 0.5f) : rec.y,
+                  sz = s ? __fadd_rn(rec.z, 0.5f) : rec.z;
+      if (!accept32(g, sx, sy, sz)) continue;
+      AxisTapsF ax, ay, az;
+      axis32k<K>(sx, 0, g.nx, g.los, ax);
+      axis32k<K>(sy, 1, g.ny, g.los, ay);
+      axis32k<K>(sz, 1, g.nz, g.los, az);
+      float wx[3], wy[3], wz[3];
+      int lx[3], ly[3], lz[3];
+      stage_axis32(ax, x0, ex, 1, wx, lx);
+      stage_axis32(ay, y0, ey, 1, wy, ly);
+      stage_axis32(az, z0, ez, 1, wz, lz);
+#pragma unroll
+      for (int a = 0; a < K; a++)
+#pragma unroll
+        for (int b2 = 0; b2 < K; b2++) {
+          const float wxy = wx[a] * wy[b2];
+          const long long rowb = ((long long)(x0 + lx[a]) * g.ny + (y0 + ly[b2])) * g.row + z0;
+#pragma unroll
+          for (int c = 0; c < K; c++) {
+            if (wxy == 0.0f || wz[c] == 0.0f) continue;
+            const float da = (va * wxy) * wz[c];
+            atomicAdd((float *)grids.g[s * NF] + rowb + lz[c], da);
+            l_dc[s * NF] += (double)da;
+            if (NF == 2) {
+              const float db = (vb * wxy) * wz[c];
+              atomicAdd((float *)grids.g[s * NF + 1] + rowb + lz[c], db);
+              l_dc[s * NF + 1] += (double)db;
+            }
+          }
+        }
+    }
+  }
+  const double vals[4] = {l_dc[0], l_dc[1], l_dc[2], l_dc[3]};
+  double *const dst[4] = {&st->dc[0], &st->dc[1], &st->dc[2], &st->dc[3]};
+  block_add<4>(vals, dst);
 }
 
 // Particles near an edge of the reference's rules, painted after the tiles with the exact FP64
@@ -953,8 +1195,11 @@ static void launch_rec(cudaStream_t s, const Geom &g, const FieldSpec &fs, const
                        bool weights, const GridPtrs &grids, DevStats *st) {
   const size_t smem = rec_smem_bytes(tg, NF * (IL ? 2 : 1));
   cudaFuncSetAttribute(k_tile_rec<K, NF, IL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_tile_rec<K, NF, IL><<<tg.ntiles, 256, smem, s>>>(g, fs, tg, b.offsets, b.recs, weights ? b.recw : nullptr,
-                                                     b.capacity, grids, st);
+  k_tile_rec<K, NF, IL><<<tg.ntiles, 256, smem, s>>>(g, fs, tg, b.offsets, b.counts, b.bucket_cap, b.recs,
+                                                     weights ? b.recw : nullptr, b.capacity, grids, st);
+  if (b.bucket_cap)
+    k_ovf_paint<K, NF, IL><<<152 * 2, 128, 0, s>>>(g, fs, tg, b.ovf_recs, weights ? b.ovf_w : nullptr, b.ovf_tile,
+                                                   b.ovf_count, b.ovf_cap, grids, st);
 }
 
 template <int K>
@@ -978,6 +1223,19 @@ static void run_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, cons
   const bool split = !det;  // FP32: edge particles go to k_edge_fixup; deterministic: exact rules in the tiles
   cudaMemsetAsync(b.counts, 0, sizeof(unsigned) * tg.ntiles, s);
   if (split) cudaMemsetAsync(b.edge_count, 0, sizeof(unsigned), s);
+  if (!det && b.bucket_cap) {  // bucket mode: one pass to the tiles' buckets, overflow after the tiles
+    cudaMemsetAsync(b.ovf_count, 0, sizeof(unsigned), s);
+    k_bucket<T><<<nb, th, 0, s>>>(g, fs, tg, in, n, b.counts, b.recs, in.w ? b.recw : nullptr, b.bucket_cap,
+                                  b.edge_list, b.edge_count, b.ovf_recs, in.w ? b.ovf_w : nullptr, b.ovf_tile,
+                                  b.ovf_count, b.ovf_cap, st);
+    const bool wts = in.w != nullptr;
+    if (g.order == 3) launch_rec_k<3>(s, g, fs, tg, b, wts, grids, st);
+    else if (g.order == 2) launch_rec_k<2>(s, g, fs, tg, b, wts, grids, st);
+    else launch_rec_k<1>(s, g, fs, tg, b, wts, grids, st);
+    k_edge_fixup<T><<<152 * 2, 128, 0, s>>>(g, fs, in, b.edge_list, b.edge_count, grids, st);
+    *launches += 4;
+    return;
+  }
   k_count<T><<<nb, th, 0, s>>>(g, fs, tg, in, n, b.counts, st, split ? 1 : 0);
   k_scan<<<1, 1024, 0, s>>>(b.counts, tg.ntiles, b.offsets, b.cursor, st, b.capacity, b.fixed_scale);
   k_scatter<T><<<nb, th, 0, s>>>(g, fs, tg, in, n, b.cursor, b.recs, in.w ? b.recw : nullptr, b.capacity,

@@ -51,6 +51,15 @@ struct PaintBufs {
   unsigned int *edge_list; // FP32: indices of particles painted by the exact rules after the tiles
   unsigned int *edge_count;
   unsigned long long edge_cap;
+  // bucket mode (bucket_cap > 0): one pass writes each tile's records into its own fixed-capacity
+  // bucket recs[tile * bucket_cap ...]; records beyond a full bucket go to the overflow list with
+  // their tile and are deposited with global atomics after the tiles
+  unsigned bucket_cap;
+  float4 *ovf_recs;
+  float *ovf_w;
+  unsigned *ovf_tile;
+  unsigned *ovf_count;
+  unsigned long long ovf_cap;
 };
 
 // host launchers (paint.cu)

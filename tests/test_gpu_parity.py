@@ -149,3 +149,39 @@ def test_nonfinite_is_an_error(gpu):
             with pytest.raises(cg.CapowError) as e:
                 ps.power()
             assert e.value.status == cg.EINVAL
+
+
+def _clumped(po, n, frac, seed, width):
+    """Uniform particles with a fraction packed into a small cube (a few cells wide)."""
+    x, y, z, vx, vy, vz = particles(po, n, seed=seed, edges=False)
+    rng = np.random.default_rng(seed + 1)
+    m = int(n * frac)
+    d = (po.XMAX - po.XMIN) / po.NX
+    c = np.array([po.XMIN + 0.37 * (po.XMAX - po.XMIN), po.YMIN + 0.41 * (po.YMAX - po.YMIN),
+                  po.ZMIN + 0.43 * (po.ZMAX - po.ZMIN)])
+    for a, arr in enumerate((x, y, z)):
+        arr[:m] = c[a] + rng.uniform(-width / 2, width / 2, m) * d
+    return x, y, z, vx, vy, vz
+
+
+@pytest.mark.parametrize("frac,n", [(0.3, 40000), (0.95, 300000)])
+def test_fp32_bucket_overflow_parity(gpu, frac, n):
+    """A clump overflows its tiles' buckets: the overflow list (first case) or, when that fills too,
+    the fall-back to the two-pass paint (second case) must paint exactly what the oracle paints."""
+    po, pc = params_pair(NX=64, NY=64, NZ=64, InterpOrder=3, LOS=3, DoInterlacing=1, Momentum=1, **BASE)
+    parts = _clumped(po, n, frac, seed=61 + n, width=3.0)
+    ref = oracle_run(po, parts, 1)
+    res, st, grids, _ = gpu_run(pc, parts, "fp32", grids=True)
+    assert st["ngrid"] == ref["stats"]["ngrid"]
+    # an FP32 cell of the clump sums ~n*frac deposits, each rounded at about 2^-24 of the cell (the
+    # int32 tile quantum is of the same order): the error grows as sqrt(deposits)
+    tol = max(1e-5, 4.0 * 2.0 ** -24 * np.sqrt(n * frac) * 2.0)
+    row = 2 * (po.NZ // 2 + 1)
+    for k, g in grids.items():
+        a = g.reshape(po.NX, po.NY, row)[:, :, :po.NZ]
+        b = ref["painted"][k][: po.NX * po.NY * row].reshape(po.NX, po.NY, row)[:, :, :po.NZ]
+        err = np.abs(a - b).max() / np.abs(b).max()
+        assert err <= tol, f"clump {frac} {k}: {err:.3e} > {tol:.3e}"
+    dd = oracle_run(po, parts, 0)["raw"]["Pk0"]
+    pp = oracle_run(po, parts, 2)["raw"]["Pk0"]
+    assert_spectrum(res[0], ref["raw"], np.sqrt(np.abs(dd * pp)), "fp32", odd=True, label=f"clump {frac}")
