@@ -218,7 +218,7 @@ __device__ __forceinline__ void adj_particle_exact(const Geom &g, const FieldSpe
   else if (g.los == 3) z = rsd_shift64(g, z, v);
   double g0 = 0.0, gs[3] = {0.0, 0.0, 0.0};
   bool accepted = false;
-  if (!outside_box(g, x, y, z)) {
+  {  // a particle outside the box (LOS != 0) is still painted where a stencil accepts it (src/read_data.c:81-97)
     const int nst = g.interlace ? 2 : 1;
     for (int st = 0; st < nst; st++) {
       const double px = st ? DADD(x, g.hx) : x, py = st ? DADD(y, g.hy) : y, pz = st ? DADD(z, g.hz) : z;

@@ -177,6 +177,46 @@ CAPOW_HD bool exact_axes(const Geom &g, double x, double y, double z, AxisTaps &
   return true;
 }
 
+// One axis of exact_axes (0 x, 1 y, 2 z): that axis's acceptance test and taps. A particle is
+// accepted when all three axes accept it, so the three can be evaluated independently.
+CAPOW_HD bool exact_axis(const Geom &g, int a, double c, AxisTaps &t) {
+  const double mn = a == 0 ? g.xmin : (a == 1 ? g.ymin : g.zmin);
+  const double mx = a == 0 ? g.xmax_l : (a == 1 ? g.ymax : g.zmax);
+  const double d = a == 0 ? g.dx : (a == 1 ? g.dy : g.dz);
+  const int n = a == 0 ? g.nx : (a == 1 ? g.ny : g.nz);
+  if (g.order == 1) {  // src/read_data.c:519-541
+    if ((c < mn) || (c >= mx)) return false;
+    int i = (int)DDIV(DSUB(c, mn), d);
+    if (a == 0) {
+      if (i == g.nxtra) i = g.nxtra - 1;
+    } else if (i == n) {
+      i = n - 1;
+    }
+    t.n = 1;
+    t.idx[0] = i;
+    t.w[0] = 1.0;
+    t.on[0] = 1;
+    return true;
+  }
+  if (g.order == 2) {  // src/read_data.c:544-605
+    if ((c < mn) || (c >= mx)) return false;
+    cic_axis64(DDIV(DSUB(c, mn), d), a == 0, n, g.nxtra, g.los, t);
+    return true;
+  }
+  if (a == 0) {  // TSC, src/read_data.c:608-619
+    if (g.los == 0) {
+      if (DSUB(c, g.xmin) < g.dx) c = DADD(c, g.lx);
+      if ((c < DADD(mn, g.dx)) || (c >= DADD(mx, g.dx))) return false;
+    } else if ((c < mn) || (c >= DADD(mx, g.dx))) {
+      return false;
+    }
+  } else if ((c < mn) || (c >= mx)) {
+    return false;
+  }
+  tsc_axis64(DDIV(DSUB(c, mn), d), a == 0, n, g.nxtra, g.los, t);
+  return true;
+}
+
 // Linear padded index of a reference write (src/read_data.c:536 form), then the halo fold:
 // indices in the halo slices map onto slice 0.. when LOS == 0 and are dropped otherwise.
 // Writes into the padding columns (z >= NZ, reachable only by a rounding edge) are dropped:
@@ -189,7 +229,7 @@ CAPOW_HD long long canon_index(const Geom &g, int ix, int iy, int iz) {
     L -= (unsigned long long)g.main_sz;
     if (L >= (unsigned long long)g.order * (unsigned long long)g.slice) return -1;
   }
-  if ((long long)(L % (unsigned long long)g.row) >= g.nz) return -1;
+  if (iz >= g.nz) return -1;  // iz < row, so iz is L % row before and after the halo fold
   return (long long)L;
 }
 

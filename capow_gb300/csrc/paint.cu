@@ -31,6 +31,27 @@ __device__ __forceinline__ float warp_sum_f(float v) {
   return v;
 }
 
+// Reduce `nv` per-thread floats over the block in FP32 within each warp (32 terms) and in FP64
+// across warps, and add them to global `dst` (one FP64 atomic per value and block).
+template <int NV>
+__device__ void block_add_f(const float (&v)[NV], double *const (&dst)[NV]) {
+  __shared__ double redf[32][NV];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  float t[NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++) t[k] = warp_sum_f(v[k]);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; k++) redf[wid][k] = (double)t[k];
+  __syncthreads();
+  if (wid == 0 && lane < NV) {
+    double a = 0.0;
+    for (int w = 0; w < nw; w++) a += redf[w][lane];
+    if (a != 0.0) atomicAdd(dst[lane], a);
+  }
+  __syncthreads();
+}
+
 // Reduce `nv` per-thread doubles over the block and add them to global `dst`.
 template <int NV>
 __device__ void block_add(const double (&v)[NV], double *const (&dst)[NV]) {
@@ -188,8 +209,14 @@ __device__ __forceinline__ int tile_id(const TileGeo &tg, int bx, int by, int bz
 // for CIC, [floor(s-m), floor(s+m)+1] for NN. Wrapping axes (LOS == 0: periodic y, z and the x halo
 // fold) take the cells modulo N; other axes clip to the grid. Returns false when nothing of the
 // footprint lies in the grid (the particle is outside the box and rejected).
-__device__ __forceinline__ bool axis_range(float s, int n, bool wrap, int order, float m, int &lo, int &hi) {
+// [low, lim): where either stencil of a particle at s is accepted along a non-wrapping axis (lim = n,
+// or n + 1 for the TSC x axis; low = 0, or -1/2 when the interlaced copy at s + 1/2 is painted too).
+// A particle beyond that range by more than the margin is rejected by both and lies outside the box,
+// so it is counted out without the exact rules.
+__device__ __forceinline__ bool axis_range(float s, int n, bool wrap, int order, float m, float low, float lim,
+                                           int &lo, int &hi) {
   if (!(s > -4.0f && s < (float)n + 4.0f)) return false;
+  if (!wrap && (s < low - m || s >= lim + m)) return false;
   lo = __float2int_rd(__fsub_rn(s, m)) - (order == 3 ? 1 : 0);
   hi = __float2int_rd(__fadd_rn(s, m)) + (order == 1 ? 1 : 2);
   if (!wrap) {
@@ -208,12 +235,12 @@ __device__ __forceinline__ bool axis_range(float s, int n, bool wrap, int order,
 
 // The tiles of the cells lo..hi (hi may pass n - 1 on a wrapping axis): the piece inside the grid
 // covers tiles lo >> shift .. min(hi, n - 1) >> shift, the wrapped piece 0 .. (hi - n) >> shift.
-__device__ __forceinline__ bool axis_footprint(float s, int n, int shift, bool wrap, int order, float m,
-                                               AxisTiles &T) {
+__device__ __forceinline__ bool axis_footprint(float s, int n, int shift, bool wrap, int order, float m, float low,
+                                               float lim, AxisTiles &T) {
   T.n = 0;
   T.t0 = T.t1 = T.t2 = 0;
   int lo, hi;
-  if (!axis_range(s, n, wrap, order, m, lo, hi)) return false;
+  if (!axis_range(s, n, wrap, order, m, low, lim, lo, hi)) return false;
   const int top = hi < n - 1 ? hi : n - 1;
   const int a0 = lo >> shift, a1 = top >> shift;  // a1 - a0 <= 2: the footprint spans at most 6 cells
   T.t0 = a0;
@@ -232,9 +259,11 @@ __device__ __forceinline__ bool axis_footprint(float s, int n, int shift, bool w
 __device__ __forceinline__ bool footprint(const Geom &g, const TileGeo &tg, float sx, float sy, float sz,
                                           AxisTiles &TX, AxisTiles &TY, AxisTiles &TZ) {
   const bool wrap = g.los == 0;
-  if (!axis_footprint(sx, g.nx, tg.lx, wrap, g.order, g.margin, TX)) return false;
-  if (!axis_footprint(sy, g.ny, tg.ly, wrap, g.order, g.margin, TY)) return false;
-  if (!axis_footprint(sz, g.nz, tg.lz, wrap, g.order, g.margin, TZ)) return false;
+  const float limx = (float)g.nx + (g.order == 3 ? 1.0f : 0.0f);  // src/read_data.c:618-619
+  const float low = g.interlace ? -0.5f : 0.0f;
+  if (!axis_footprint(sx, g.nx, tg.lx, wrap, g.order, g.margin, low, limx, TX)) return false;
+  if (!axis_footprint(sy, g.ny, tg.ly, wrap, g.order, g.margin, low, (float)g.ny, TY)) return false;
+  if (!axis_footprint(sz, g.nz, tg.lz, wrap, g.order, g.margin, low, (float)g.nz, TZ)) return false;
   // CIC rounding edge: a y index equal to NY makes the reference's linear index land in row 0 of
   // the next x slice (src/read_data.c:592-593); that row's tile joins the list.
   if (g.order == 2 && sy > (float)g.ny - 1.5f - g.margin) add_tile(TY, 0);
@@ -246,9 +275,11 @@ __device__ __forceinline__ bool footprint(const Geom &g, const TileGeo &tg, floa
 __device__ __forceinline__ int home_of(const Geom &g, const TileGeo &tg, float sx, float sy, float sz) {
   const bool wrap = g.los == 0;
   int lx, hx, ly, hy, lz, hz;
-  if (!axis_range(sx, g.nx, wrap, g.order, g.margin, lx, hx)) return -1;
-  if (!axis_range(sy, g.ny, wrap, g.order, g.margin, ly, hy)) return -1;
-  if (!axis_range(sz, g.nz, wrap, g.order, g.margin, lz, hz)) return -1;
+  const float limx = (float)g.nx + (g.order == 3 ? 1.0f : 0.0f);
+  const float low = g.interlace ? -0.5f : 0.0f;
+  if (!axis_range(sx, g.nx, wrap, g.order, g.margin, low, limx, lx, hx)) return -1;
+  if (!axis_range(sy, g.ny, wrap, g.order, g.margin, low, (float)g.ny, ly, hy)) return -1;
+  if (!axis_range(sz, g.nz, wrap, g.order, g.margin, low, (float)g.nz, lz, hz)) return -1;
   return tile_id(tg, lx >> tg.lx, ly >> tg.ly, lz >> tg.lz);
 }
 
@@ -333,7 +364,7 @@ __global__ void __launch_bounds__(256) k_count(Geom g, FieldSpec fs, TileGeo tg,
         f_abs[0] += fabsf(pa);
         f_abs[1] += fabsf(pb);
         if (!footprint(g, tg, p.sx, p.sy, p.sz, TX, TY, TZ)) {
-          f_out += 1.0f;  // outside the box by at least two cells (src/read_data.c:81-88)
+          f_out += 1.0f;  // clearly outside the box (src/read_data.c:81-88)
           if (g.los == 0) {
             fatal = 1;
             atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)i);
@@ -342,8 +373,9 @@ __global__ void __launch_bounds__(256) k_count(Geom g, FieldSpec fs, TileGeo tg,
           // painted and counted by k_edge_fixup
         } else {
           has = true;
-          // NGRID (src/read_data.c:92-126): exact for particles away from every edge
+          // NGRID (src/read_data.c:92-126) and NOUT: exact for particles away from every edge
           if (split_edge && accept32(g, p.sx, p.sy, p.sz)) f_grid += p.w;
+          if (split_edge && outside32(g, p.sx, p.sy, p.sz)) f_out += 1.0f;
         }
       }
     }
@@ -357,12 +389,11 @@ __global__ void __launch_bounds__(256) k_count(Geom g, FieldSpec fs, TileGeo tg,
         for (int c = 0; c < 3; c++)
           if (a < na && b < nb && c < nc) warp_run_add(counts, tile_key(tg, has, TX, TY, TZ, a, b, c), false);
   }
-  // FP32 per-thread partials over ~n/(grid threads) particles, FP64 across threads
-  const double vals[10] = {(double)f_read, (double)f_out, (double)f_nsq, (double)f_v[0], (double)f_v[1],
-                           (double)f_v[2], (double)f_v[3], (double)f_abs[0], (double)f_abs[1], (double)f_grid};
+  // FP32 per-thread partials and warp sums, FP64 across warps
+  const float vals[10] = {f_read, f_out, f_nsq, f_v[0], f_v[1], f_v[2], f_v[3], f_abs[0], f_abs[1], f_grid};
   double *const dst[10] = {&st->nread, &st->nout, &st->nsq, &st->vr[0], &st->vr[1], &st->vr[2], &st->vr[3],
                            &st->absw[0], &st->absw[1], &st->ngrid};
-  block_add<10>(vals, dst);
+  block_add_f<10>(vals, dst);
   if (fatal) atomicOr(&st->fatal, 1);
   if (nonfin) atomicOr(&st->nonfinite, 1);
 }
@@ -494,7 +525,7 @@ __global__ void __launch_bounds__(256) k_bucket(Geom g, FieldSpec fs, TileGeo tg
         f_abs[0] += fabsf(pa);
         f_abs[1] += fabsf(pb);
         if (!footprint(g, tg, p.sx, p.sy, p.sz, TX, TY, TZ)) {
-          f_out += 1.0f;  // outside the box by at least two cells (src/read_data.c:81-88)
+          f_out += 1.0f;  // clearly outside the box (src/read_data.c:81-88)
           if (g.los == 0) {
             fatal = 1;
             atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)i);
@@ -506,6 +537,7 @@ __global__ void __launch_bounds__(256) k_bucket(Geom g, FieldSpec fs, TileGeo tg
           w = p.w;
           rec = make_float4(p.sx, p.sy, p.sz, p.v);
           if (accept32(g, p.sx, p.sy, p.sz)) f_grid += p.w;  // NGRID (src/read_data.c:92-126)
+          if (outside32(g, p.sx, p.sy, p.sz)) f_out += 1.0f;  // src/read_data.c:81-88
         }
       }
     }
@@ -537,11 +569,10 @@ __global__ void __launch_bounds__(256) k_bucket(Geom g, FieldSpec fs, TileGeo tg
           }
         }
   }
-  const double vals[10] = {(double)f_read, (double)f_out, (double)f_nsq, (double)f_v[0], (double)f_v[1],
-                           (double)f_v[2], (double)f_v[3], (double)f_abs[0], (double)f_abs[1], (double)f_grid};
+  const float vals[10] = {f_read, f_out, f_nsq, f_v[0], f_v[1], f_v[2], f_v[3], f_abs[0], f_abs[1], f_grid};
   double *const dst[10] = {&st->nread, &st->nout, &st->nsq, &st->vr[0], &st->vr[1], &st->vr[2], &st->vr[3],
                            &st->absw[0], &st->absw[1], &st->ngrid};
-  block_add<10>(vals, dst);
+  block_add_f<10>(vals, dst);
   if (fatal) atomicOr(&st->fatal, 1);
   if (nonfin) atomicOr(&st->nonfinite, 1);
   if (ovf_full) atomicOr(&st->overflow, 1);
@@ -627,7 +658,7 @@ __global__ void __launch_bounds__(256, 2) k_tile_paint(Geom g, FieldSpec fs, Til
   const int K = g.order;
   const bool tap_on = lane < K * K * K;
   const int tdx = tap_on ? lane / (K * K) : 0, tdy = tap_on ? (lane / K) % K : 0, tdz = tap_on ? lane % K : 0;
-  float f_grid = 0.0f;
+  float f_grid = 0.0f, f_out = 0.0f;
   double d_grid = 0.0, d_out = 0.0;
   int fatal = 0;
   unsigned rb = offsets[tile], re = offsets[tile + 1];
@@ -668,7 +699,10 @@ __global__ void __launch_bounds__(256, 2) k_tile_paint(Geom g, FieldSpec fs, Til
         }
       } else {
         w = recw ? recw[r] : 1.0f;
-        if (home_of(g, tg, rec.x, rec.y, rec.z) == tile && accept32(g, rec.x, rec.y, rec.z)) f_grid += w;
+        if (home_of(g, tg, rec.x, rec.y, rec.z) == tile) {
+          if (accept32(g, rec.x, rec.y, rec.z)) f_grid += w;
+          if (outside32(g, rec.x, rec.y, rec.z)) f_out += 1.0f;  // src/read_data.c:81-88
+        }
       }
     }
     float va, vb;
@@ -752,7 +786,7 @@ __global__ void __launch_bounds__(256, 2) k_tile_paint(Geom g, FieldSpec fs, Til
     }
   }
   {
-    const double vals[2] = {d_grid + (double)f_grid, d_out};
+    const double vals[2] = {d_grid + (double)f_grid, d_out + (double)f_out};
     double *const dst[2] = {&st->ngrid, &st->nout};
     block_add<2>(vals, dst);
     if (fatal) atomicOr(&st->fatal, 1);
@@ -1085,45 +1119,65 @@ __global__ void __launch_bounds__(128) k_ovf_paint(Geom g, FieldSpec fs, TileGeo
 
 // Particles near an edge of the reference's rules, painted after the tiles with the exact FP64
 // rules and global atomics into the FP32 grids; their exact statistics (NGRID, the out-of-box
-// count, the LOS == 0 error) are added here.
+// count, the LOS == 0 error) are added here. One warp per particle: lanes 0-2 take the taps of the
+// three axes, then lane t deposits tap t (each a serial chain of FP64 steps otherwise).
 template <typename T>
 __global__ void __launch_bounds__(128) k_edge_fixup(Geom g, FieldSpec fs, PIn<T> in, const unsigned *edge_list,
                                                     const unsigned *edge_count, GridPtrs grids, DevStats *st) {
   const unsigned ne = *edge_count;
   const int nf = fs.nfields, nst = g.interlace ? 2 : 1;
+  const int lane = threadIdx.x & 31;
+  const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nwarp = (gridDim.x * blockDim.x) >> 5;
   double d_grid = 0.0, d_out = 0.0, l_dc[4] = {0, 0, 0, 0};
   int fatal = 0;
-  for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < ne; k += gridDim.x * blockDim.x) {
+  for (unsigned k = warp; k < ne; k += nwarp) {
     const unsigned idx = edge_list[k];
     double x, y, z, v, w;
     exact_pos(g, fs, in, idx, x, y, z, v, w);
     if (outside_box(g, x, y, z)) {  // src/read_data.c:81-88
-      d_out += 1.0;
+      if (lane == 0) d_out += 1.0;
       if (g.los == 0) {
         fatal = 1;
-        atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)idx);
+        if (lane == 0) atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)idx);
         continue;
       }
     }
     const double val[2] = {wpow64(w, v, fs.ea), wpow64(w, v, fs.eb)};
     for (int stn = 0; stn < nst; stn++) {
-      AxisTaps ax, ay, az;
       const double px = stn ? DADD(x, g.hx) : x, py = stn ? DADD(y, g.hy) : y, pz = stn ? DADD(z, g.hz) : z;
-      if (!exact_axes(g, px, py, pz, ax, ay, az)) continue;
-      if (stn == 0) d_grid += w;
-      for (int c = 0; c < az.n; c++)
-        for (int b = 0; b < ay.n; b++)
-          for (int a = 0; a < ax.n; a++) {
-            if (!(ax.on[a] && ay.on[b] && az.on[c])) continue;
-            const long long L = canon_index(g, ax.idx[a], ay.idx[b], az.idx[c]);
-            if (L < 0) continue;
-            const double tw = DMUL(DMUL(ax.w[a], ay.w[b]), az.w[c]);
-            for (int f = 0; f < nf; f++) {
-              const float d = (float)DMUL(val[f], tw);
-              atomicAdd((float *)grids.g[stn * nf + f] + L, d);
-              l_dc[stn * nf + f] += (double)d;
-            }
-          }
+      AxisTaps t;
+      t.n = 0;
+      bool acc = true;
+      if (lane < 3) acc = exact_axis(g, lane, lane == 0 ? px : (lane == 1 ? py : pz), t);
+      if (__ballot_sync(FULL_MASK, !acc)) continue;  // rejected by some axis
+      if (stn == 0 && lane == 0) d_grid += w;
+      // this lane's tap (a, b, c) of a 3 x 3 x 3 block; the axes' taps from lanes 0, 1, 2
+      const int ta = lane / 9, tb = (lane / 3) % 3, tc = lane % 3;
+      const int nx_ = __shfl_sync(FULL_MASK, t.n, 0), ny_ = __shfl_sync(FULL_MASK, t.n, 1),
+                nz_ = __shfl_sync(FULL_MASK, t.n, 2);
+      int ix = 0, iy = 0, iz = 0, on = 1;
+      double wx = 0.0, wy = 0.0, wz = 0.0;
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        const int i0 = __shfl_sync(FULL_MASK, t.idx[q], 0), i1 = __shfl_sync(FULL_MASK, t.idx[q], 1),
+                  i2 = __shfl_sync(FULL_MASK, t.idx[q], 2);
+        const int o0 = __shfl_sync(FULL_MASK, (int)t.on[q], 0), o1 = __shfl_sync(FULL_MASK, (int)t.on[q], 1),
+                  o2 = __shfl_sync(FULL_MASK, (int)t.on[q], 2);
+        const double w0 = __shfl_sync(FULL_MASK, t.w[q], 0), w1 = __shfl_sync(FULL_MASK, t.w[q], 1),
+                     w2 = __shfl_sync(FULL_MASK, t.w[q], 2);
+        if (ta == q) { ix = i0; wx = w0; on &= o0; }
+        if (tb == q) { iy = i1; wy = w1; on &= o1; }
+        if (tc == q) { iz = i2; wz = w2; on &= o2; }
+      }
+      if (lane >= 27 || ta >= nx_ || tb >= ny_ || tc >= nz_ || !on) continue;
+      const long long L = canon_index(g, ix, iy, iz);
+      if (L < 0) continue;
+      const double tw = DMUL(DMUL(wx, wy), wz);
+      for (int f = 0; f < nf; f++) {
+        const float dep = (float)DMUL(val[f], tw);
+        atomicAdd((float *)grids.g[stn * nf + f] + L, dep);
+        l_dc[stn * nf + f] += (double)dep;
+      }
     }
   }
   const double vals[6] = {d_grid, d_out, l_dc[0], l_dc[1], l_dc[2], l_dc[3]};

@@ -26,23 +26,38 @@ __device__ __forceinline__ Prep prep32(const Geom &g, const FieldSpec &fs, const
 }
 
 // A particle within the FP32 error margin of a point where the reference's deposit changes
-// discontinuously (box faces 0 and N, anything outside [0, N], the TSC low-tap drop at 0.5, the
-// TSC LOS==0 x shift at 1, every cell edge for NN) is painted by the exact FP64 rules.
+// discontinuously is painted by the exact FP64 rules. Along one axis, for one stencil's scale s:
+// the acceptance ends 0 and lim (n, or n + 1 for the TSC x axis), the grid end n (halo and wrap
+// rules), the TSC low-tap drop at 0.5, the TSC LOS == 0 x shift at 1, and every cell edge for NN.
+// On a periodic axis (LOS == 0) anything outside [m, n - m] is an edge too: such a particle is the
+// reference's fatal error, which the exact rules report. Elsewhere a stencil clearly outside the
+// acceptance is simply not painted (accept32), and the particle is counted out (outside32).
 // (Bitwise logic throughout: every test is cheap, so evaluating all of them beats branching.)
-__device__ __forceinline__ bool edge1(float s, int n, int order, float m) {
+__device__ __forceinline__ bool edge1(float s, int n, float lim, int order, float m, bool wrap) {
   const float nf = (float)n;
-  bool e = !(s >= m) | !(s <= nf - m) | (fabsf(s - 0.5f) < m) | (fabsf(s - 1.0f) < m);
+  bool e = (fabsf(s) < m) | (fabsf(s - nf) < m) | (fabsf(s - lim) < m) | (fabsf(s - 0.5f) < m) |
+           (fabsf(s - 1.0f) < m);
+  if (wrap) e |= !(s >= m) | !(s <= nf - m);
   if (order == 1) e |= (fabsf(s - rintf(s)) < m);
   return e;
 }
 
 __device__ __forceinline__ bool is_edge(const Geom &g, float sx, float sy, float sz) {
-  bool e = edge1(sx, g.nx, g.order, g.margin) | edge1(sy, g.ny, g.order, g.margin) |
-           edge1(sz, g.nz, g.order, g.margin);
+  const bool wrap = g.los == 0;
+  const float limx = (float)g.nx + (g.order == 3 ? 1.0f : 0.0f);
+  bool e = edge1(sx, g.nx, limx, g.order, g.margin, wrap) | edge1(sy, g.ny, (float)g.ny, g.order, g.margin, wrap) |
+           edge1(sz, g.nz, (float)g.nz, g.order, g.margin, wrap);
   if (g.interlace)
-    e |= edge1(__fadd_rn(sx, 0.5f), g.nx, g.order, g.margin) | edge1(__fadd_rn(sy, 0.5f), g.ny, g.order, g.margin) |
-         edge1(__fadd_rn(sz, 0.5f), g.nz, g.order, g.margin);
+    e |= edge1(__fadd_rn(sx, 0.5f), g.nx, limx, g.order, g.margin, wrap) |
+         edge1(__fadd_rn(sy, 0.5f), g.ny, (float)g.ny, g.order, g.margin, wrap) |
+         edge1(__fadd_rn(sz, 0.5f), g.nz, (float)g.nz, g.order, g.margin, wrap);
   return e;
+}
+
+// Outside the box (src/read_data.c:81), for a particle that is not an edge particle: no scale is
+// within the margin of 0 or n, so the FP32 test decides exactly.
+__device__ __forceinline__ bool outside32(const Geom &g, float sx, float sy, float sz) {
+  return (sx < 0.0f) | (sx > (float)g.nx) | (sy < 0.0f) | (sy > (float)g.ny) | (sz < 0.0f) | (sz > (float)g.nz);
 }
 
 template <int K>

@@ -179,6 +179,49 @@ def test_backward_central_differences(gpu):
         assert bad.sum() <= 2, f"{name}: {np.c_[an[bad], fd[bad]]}"
 
 
+def test_backward_particles_outside_the_box(gpu):
+    """Particles that the RSD shift puts just below z = 0 are outside the box. The reader counts
+    them in NOUT and still calls add_to_grid for both stencils (src/read_data.c:76-97): the normal
+    stencil is rejected (z < ZMIN), the interlaced copy at z + dz/2 is painted when it lands at or
+    above ZMIN. So the first group's gradient is its interlaced copy's and the second group's is 0."""
+    p = cg.Params(NX=32, NY=32, NZ=32, NK=15, Maxk=0.15, **BASE)
+    parts = [a.copy() for a in interior_particles(p, 20000, seed=71, margin=0.0)]
+    d = (p.XMAX - p.XMIN) / p.NX
+    rng = np.random.default_rng(72)
+    live, dead = np.arange(0, 8), np.arange(8, 16)
+    u = rng.uniform(0.05, 0.4, 16)
+    target = np.r_[rng.uniform(-0.45, -0.05, 8), rng.uniform(-0.95, -0.6, 8)]  # shifted z / dz
+    parts[2][:16] = p.ZMIN + u * d
+    parts[3][:16] = (target - u) * d / rsd_factor(p)
+    T0, T2 = lib_multipoles(p, interior_particles(p, 20000, seed=73, margin=0.0), "fp64")
+
+    def loss():
+        P0, P2 = lib_multipoles(p, parts, "fp64")
+        return float(((P0 - T0) ** 2).sum() + ((P2 - T2) ** 2).sum())
+
+    h = 1e-2 * d
+    fd = {}
+    for a, name in ((0, "dx"), (1, "dy"), (2, "dz")):
+        vals = []
+        for i in live:
+            v0 = parts[a][i]
+            parts[a][i] = v0 + h
+            lp = loss()
+            parts[a][i] = v0 - h
+            lm = loss()
+            parts[a][i] = v0
+            vals.append((lp - lm) / (2 * h))
+        fd[name] = np.array(vals)
+    for prec in ("fp64", "fp32"):
+        gr, _, _ = lib_grads(p, parts, prec, T0, T2)
+        for name in ("dx", "dy", "dz", "dvlos", "dw"):
+            assert np.all(gr[name][dead] == 0.0), (prec, name, gr[name][dead])
+        for name, f in fd.items():
+            assert np.abs(f).max() > 0.0
+            an = gr[name][live]
+            assert np.all(np.abs(an - f) <= 1e-2 * np.abs(f).max()), (prec, name, np.c_[an, f])
+
+
 def test_backward_fp32_matches_fp64_at_c3_size(gpu):
     """The C3 workload: 256^3 Zel'dovich particles (f32, unit weights), TSC 256^3, interlaced, LOS = z."""
     import torch
