@@ -552,21 +552,42 @@ __global__ void __launch_bounds__(256) k_bin(BinParams bp, BinTables t, const ty
 // ------------------------------------------------------------ fused x-axis FFT + binning (FP32)
 // cuFFT has transformed every x-plane of every grid over (y, z); what is left of the 3-D transform
 // (src/main.c:266-271) is the length-NX DFT along x of every (ky, kz) column, and its only consumer
-// is the binning (src/main.c:302-468). One pass does both: a CTA loads a block of columns into
-// shared memory, transforms them along x there and bins the modes from there, so the x-transformed
-// grids never go to HBM. Columns whose smallest |k| lies beyond the top k-bin edge are not loaded.
+// is the binning (src/main.c:302-468). One pass does both: a CTA transforms a block of columns
+// along x in shared memory and bins the modes from there, so the x-transformed grids never go to
+// HBM. Columns whose smallest |k| lies beyond the top k-bin edge are not loaded.
 //
-// Shared layout of a block: row x (the position along x) holds ncol complex values, column
-// c = slot * kc + (kz - k0) stored at c ^ (x & (ncol - 1)): a row is contiguous for the loads and
-// the FFT, and the XOR spreads the rows the binning reads at once over the banks.
+// A block is `kc` consecutive kz of one ky in each of the nslot grids: 8 kz (64 contiguous bytes
+// of every x-row of every grid) for NX <= 512. One CTA of XBIN_THREADS threads per SM. The first
+// radix-8 stage reads its inputs straight from HBM; the others work in shared memory, where row x
+// holds the block's ncol columns (c = slot * kc + kz - k0) with a pitch of ncol + 1: a butterfly's
+// rows are one base plus a fixed stride, a warp's accesses are whole rows, and the pad spreads the
+// rows the binning reads at once over the banks.
+constexpr int XBIN_THREADS = 512;
+
 struct XbinSmem {
-  unsigned sd, sb, sE, sElo, sEhi, total;
+  unsigned sd, stw, sxt, sfx, sb, sE, sElo, sEhi, total;
 };
 
-CAPOW_HD XbinSmem xbin_smem_layout(int n, int ncol, int np, int nl, int nk) {
+// Twiddle-table entries of the radix-8 stages that have more than one butterfly per group: a
+// stage of span 2^l has 2^(l-3) of them, each with its 8 factors w^(p jj NX/span), p < 8.
+CAPOW_HD unsigned xbin_tw_entries(int log2n) {
+  unsigned e = 0;
+  for (int l = log2n; l >= 4; l -= 3) e += 8u << (l - 3);
+  return e;
+}
+
+// Position in the x-table of kx index i: one pad entry per 64 spreads the starts of the binning
+// runs over the banks.
+__device__ __forceinline__ int xt_index(int i) { return i + (i >> 6); }
+
+CAPOW_HD XbinSmem xbin_smem_layout(int log2n, int ncol, int np, int nl, int nk) {
+  const unsigned n = 1u << log2n;
   XbinSmem L;
   unsigned o = 0;
-  L.sd = o;   o = align16(o + 8u * (unsigned)n * ncol);
+  L.sd = o;   o = align16(o + 8u * n * (ncol + 1));
+  L.stw = o;  o = align16(o + 8u * xbin_tw_entries(log2n));
+  L.sxt = o;  o = align16(o + 16u * (n + (n >> 6) + 1));
+  L.sfx = o;  o = align16(o + 4u * n);
   L.sb = o;   o = align16(o + 4u * np * nl * nk);
   L.sE = o;   o = align16(o + 8u * (nk + 3));
   L.sElo = o; o = align16(o + 4u * (nk + 3));
@@ -581,6 +602,14 @@ __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 __device__ __forceinline__ float2 cmul_mi(float2 a) { return make_float2(a.y, -a.x); }  // a * (-i)
+
+// A column element read once: no L1 allocation, and an L2 fetch of the surrounding 256 bytes (the
+// neighbouring kz blocks of the same row, which other CTAs read next).
+__device__ __forceinline__ float2 ld_col(const float2 *p) {
+  float2 v;
+  asm("ld.global.nc.L1::no_allocate.L2::256B.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+  return v;
+}
 
 // In-place DIF butterflies of one stage, forward sign. Inputs a[q] at span/R spacing; outputs X[p]
 // (p in natural order) times the twiddle w^(p*j) are written back at position p.
@@ -613,36 +642,17 @@ __device__ __forceinline__ void dft4(float2 *a) {
   a[3] = csub(b2, b3);
 }
 
-template <int R>
-__device__ __forceinline__ void xfft_stage(float2 *sd, const float2 *__restrict__ tw, int n, int ncol, int log2ncol,
-                                           int span, int log2q, int twstep) {
-  const int Q = span / R;
-  const int nbf = ncol * (n / R);
-  for (int u = threadIdx.x; u < nbf; u += blockDim.x) {
-    const int c = u & (ncol - 1), v = u >> log2ncol;
-    const int b = v >> log2q, jj = v & (Q - 1);
-    const int base = b * span + jj;
-    float2 a[R];
-#pragma unroll
-    for (int q = 0; q < R; q++) {
-      const int row = base + q * Q;
-      a[q] = sd[row * ncol + (c ^ (row & (ncol - 1)))];
-    }
-    if (R == 8) dft8(a);
-    else if (R == 4) dft4(a);
-    else {
-      const float2 t0 = a[0];
-      a[0] = cadd(t0, a[1]);
-      a[1] = csub(t0, a[1]);
-    }
-#pragma unroll
-    for (int p = 0; p < R; p++) {
-      float2 y = a[p];
-      if (p > 0 && jj > 0) y = cmulf(y, __ldg(tw + ((p * jj * twstep) & (n - 1))));
-      const int row = base + p * Q;
-      sd[row * ncol + (c ^ (row & (ncol - 1)))] = y;
-    }
-  }
+// a[p] *= w[p], p = 1..7, w one 16-byte aligned row of a stage's twiddle table (w[0] = 1)
+__device__ __forceinline__ void twiddle8(float2 *a, const float2 *w) {
+  const float4 *w4 = (const float4 *)w;
+  const float4 t01 = w4[0], t23 = w4[1], t45 = w4[2], t67 = w4[3];
+  a[1] = cmulf(a[1], make_float2(t01.z, t01.w));
+  a[2] = cmulf(a[2], make_float2(t23.x, t23.y));
+  a[3] = cmulf(a[3], make_float2(t23.z, t23.w));
+  a[4] = cmulf(a[4], make_float2(t45.x, t45.y));
+  a[5] = cmulf(a[5], make_float2(t45.z, t45.w));
+  a[6] = cmulf(a[6], make_float2(t67.x, t67.y));
+  a[7] = cmulf(a[7], make_float2(t67.z, t67.w));
 }
 
 // Position along x, after the in-place DIF stages (log2n / 3 of radix 8, then one of radix
@@ -658,16 +668,20 @@ __device__ __forceinline__ int xfft_pos(int log2n, int i) {
 }
 
 template <int NF, bool IL, bool ODD>
-__global__ void __launch_bounds__(256) k_xfft_bin(BinParams bp, BinTables t, XbinGeo xg, const float2 *g0,
-                                                  const float2 *g1, const float2 *g2, const float2 *g3,
-                                                  const double *dcv, double *bins) {
+__global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTables t, XbinGeo xg, const float2 *g0,
+                                                           const float2 *g1, const float2 *g2, const float2 *g3,
+                                                           const double *dcv, double *bins) {
   constexpr int NS = NF * (IL ? 2 : 1);
   constexpr int NP = NF == 1 ? 1 : 4;
   constexpr int NL = ODD ? 5 : 3;  // stored multipoles: l = 0, 2, 4 (+ 1, 3)
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int n = 1 << xg.log2n, ncol = xg.ncol, kc_n = xg.kc, nk = bp.nk;
-  const XbinSmem L = xbin_smem_layout(n, ncol, NP, NL, nk);
+  const int log2n = xg.log2n, n = 1 << log2n, ncol = xg.ncol, kc_n = xg.kc, nk = bp.nk;
+  const int P = ncol + 1;  // row pitch of sd
+  const XbinSmem L = xbin_smem_layout(log2n, ncol, NP, NL, nk);
   float2 *sd = (float2 *)(smraw + L.sd);
+  float2 *stw = (float2 *)(smraw + L.stw);
+  float4 *sxt = (float4 *)(smraw + L.sxt);  // per kx: fx^2, deconvolution factor, interlace phase
+  float *sfx = (float *)(smraw + L.sfx);    // per kx: fx (the mu numerator when LOS = x)
   float *sb = (float *)(smraw + L.sb);
   double *sE = (double *)(smraw + L.sE);
   float *sElo = (float *)(smraw + L.sElo);
@@ -678,40 +692,98 @@ __global__ void __launch_bounds__(256) k_xfft_bin(BinParams bp, BinTables t, Xbi
     sElo[c] = t.Elo[c];
     sEhi[c] = t.Ehi[c];
   }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const float2 e = IL ? t.exf[i] : make_float2(0.0f, 0.0f);
+    sxt[xt_index(i)] = make_float4(t.fx2f[i], t.cxf[i], e.x, e.y);
+    sfx[i] = t.fxf[i];
+  }
+  for (int l = log2n, off = 0; l >= 4; off += 8 << (l - 3), l -= 3) {
+    const int step = n >> l;  // NX / span
+    for (int e = threadIdx.x; e < (8 << (l - 3)); e += blockDim.x)
+      stw[off + e] = t.twx[((e & 7) * (e >> 3) * step) & (n - 1)];
+  }
   const float topf32 = (float)t.E[nk + 1] * 1.0001f;
-  // DC values of the slots, converted once (a conversion from FP64 costs an FP64-pipe slot)
-  const float dcf0 = (float)dcv[0], dcf1 = NS > 1 ? (float)dcv[1] : 0.0f, dcf2 = NS > 2 ? (float)dcv[2] : 0.0f,
-              dcf3 = NS > 3 ? (float)dcv[3] : 0.0f;
-  const int tpc = blockDim.x >> xg.log2kc;       // threads per column
-  const int mpt = n / tpc > 0 ? n / tpc : 1;      // modes (kx) per thread
-  const int my_kc = threadIdx.x / tpc, my_ch = threadIdx.x - my_kc * tpc;
+  // binning work items: (kz column of the block, run of mpt consecutive kx), mpt <= 8 chosen so that
+  // the kc * NX / mpt items keep every thread busy. Within a column the run index is rotated by 3
+  // bits, so that the 16 lanes of a half-warp start runs whose rows differ in their low 4 bits (the
+  // shared reads of a run step are then conflict-free at NX = 512).
+  const int log2mpt = min(3, max(0, log2n + xg.log2kc - (31 - __clz(blockDim.x))));
+  const int mpt = 1 << log2mpt, log2nr = log2n - log2mpt, nitems = kc_n << log2nr;
+  const long long xstride = (long long)bp.ny * bp.nzc;
+  const int Q1 = n >> 3, nbf1 = ncol << (log2n - 3);
+  const long long qstep = (long long)Q1 * xstride;
+  __syncthreads();
   for (int blk = blockIdx.x; blk < xg.nblocks; blk += gridDim.x) {
     const int j = blk / xg.nkb, k0 = (blk - j * xg.nkb) * kc_n;
     // every mode of the block has s >= fy^2 + fz(k0)^2: skip the block when that is clearly beyond
     // the top edge (a block kept near the edge only costs work; each mode is tested exactly)
     if (t.fy2f[j] + t.fz2f[k0] > topf32) continue;
     __syncthreads();  // the previous block's binning has read sd
-    for (int idx = threadIdx.x; idx < n * ncol; idx += blockDim.x) {
-      const int c = idx & (ncol - 1), x = idx >> xg.log2ncol;
+    // first DIF stage (span NX) straight from HBM: butterfly (column c, jj) reads rows jj + q NX/8
+    for (int u = threadIdx.x; u < nbf1; u += blockDim.x) {
+      const int c = u & (ncol - 1), jj = u >> xg.log2ncol;
       const int sl = c >> xg.log2kc, kz = k0 + (c & (kc_n - 1));
-      float2 v = make_float2(0.0f, 0.0f);
+      const bool live = sl < NS && kz < bp.nzc;
       const float2 *g = sl == 0 ? g0 : (sl == 1 ? g1 : (sl == 2 ? g2 : g3));
-      if (sl < NS && kz < bp.nzc) v = g[((long long)x * bp.ny + j) * bp.nzc + kz];
-      sd[x * ncol + (c ^ (x & (ncol - 1)))] = v;
+      const float2 *gp = g + (live ? (long long)jj * xstride + (long long)j * bp.nzc + kz : 0ll);
+      float2 a[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) a[q] = live ? ld_col(gp + q * qstep) : make_float2(0.0f, 0.0f);
+      dft8(a);
+      if (jj > 0) twiddle8(a, stw + 8 * jj);
+      float2 *p = sd + jj * P + c;
+#pragma unroll
+      for (int q = 0; q < 8; q++) p[q * Q1 * P] = a[q];
     }
     __syncthreads();
-    int log2span = xg.log2n;
-    while (log2span >= 3) {  // radix-8 stages
-      xfft_stage<8>(sd, t.twx, n, ncol, xg.log2ncol, 1 << log2span, log2span - 3, n >> log2span);
+    int l = log2n - 3, twoff = 8 * Q1;
+    for (; l >= 3; l -= 3) {  // the other radix-8 stages
+      const int log2q = l - 3, Q = 1 << log2q, qs = Q * P;
+      for (int u = threadIdx.x; u < nbf1; u += blockDim.x) {
+        const int c = u & (ncol - 1), v = u >> xg.log2ncol;
+        const int jj = v & (Q - 1);
+        float2 *p = sd + (((v >> log2q) << l) + jj) * P + c;
+        float2 a[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) a[q] = p[q * qs];
+        dft8(a);
+        if (jj > 0) twiddle8(a, stw + twoff + 8 * jj);
+#pragma unroll
+        for (int q = 0; q < 8; q++) p[q * qs] = a[q];
+      }
       __syncthreads();
-      log2span -= 3;
+      if (Q > 1) twoff += 8 * Q;
     }
-    if (log2span == 2) xfft_stage<4>(sd, t.twx, n, ncol, xg.log2ncol, 4, 0, n >> 2);
-    else if (log2span == 1) xfft_stage<2>(sd, t.twx, n, ncol, xg.log2ncol, 2, 0, n >> 1);
-    __syncthreads();
-    // ---- binning (the math of k_bin, src/main.c:355-449), one run of consecutive kx per thread
-    const int kz = k0 + my_kc;
-    if (kz < bp.nzc && my_ch * mpt < n) {
+    if (l == 2) {  // a last radix-4 stage (span 4: no twiddles)
+      for (int u = threadIdx.x; u < (ncol << (log2n - 2)); u += blockDim.x) {
+        float2 *p = sd + ((u >> xg.log2ncol) << 2) * P + (u & (ncol - 1));
+        float2 a[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) a[q] = p[q * P];
+        dft4(a);
+#pragma unroll
+        for (int q = 0; q < 4; q++) p[q * P] = a[q];
+      }
+      __syncthreads();
+    } else if (l == 1) {  // a last radix-2 stage
+      for (int u = threadIdx.x; u < (ncol << (log2n - 1)); u += blockDim.x) {
+        float2 *p = sd + ((u >> xg.log2ncol) << 1) * P + (u & (ncol - 1));
+        const float2 a0 = p[0], a1 = p[P];
+        p[0] = cadd(a0, a1);
+        p[P] = csub(a0, a1);
+      }
+      __syncthreads();
+    }
+    // ---- binning (the math of k_bin, src/main.c:355-449), runs of consecutive kx
+    for (int w = threadIdx.x; w < nitems; w += blockDim.x) {
+      const int my_kc = w >> log2nr, rr = w & ((1 << log2nr) - 1);
+      const int ch = log2nr >= 3 ? (((rr & 7) << (log2nr - 3)) | (rr >> 3)) : rr;
+      const int i0 = ch << log2mpt;
+      // rows of the run: the digit reversal is a permutation of bit positions and i0, m < mpt <= 8
+      // have disjoint bits, so row(i0 + m) = row(i0) + row(m) = row(i0) + m NX/8
+      const int rowb = xfft_pos(log2n, i0);
+      const int kz = k0 + my_kc;
+      if (kz >= bp.nzc) continue;
       const float syz = t.fy2f[j] + t.fz2f[kz];
       float cyz = t.cyf[j] * t.czf[kz];
       if (IL) cyz *= 0.25f;
@@ -723,20 +795,34 @@ __global__ void __launch_bounds__(256) k_xfft_bin(BinParams bp, BinTables t, Xbi
       // this thread's kx run [i0, i0 + mpt) lies in [0, xhalf) or in [xhalf, NX) (xhalf is a multiple
       // of mpt); keep its modes with i <= r or i >= NX - r (r <= xhalf; the others can not reach the
       // top bin): a prefix of a run in the first half, a suffix in the second
-      const int i0 = my_ch * mpt;
       int m_lo = 0, m_hi = mpt;
       if (i0 < bp.xhalf) m_hi = min(mpt, r + 1 - i0);
       else m_lo = max(0, bp.nx - r - i0);
+      // Hermitian multiplicity NM (src/main.c:422-429): 2 off the kz = 0 plane; on it 1, except at
+      // kx = NX/2 and, on ky = 0, at kx = 0; a run holds at most one of those
+      const float cyzn = kz != 0 ? 2.0f * cyz : cyz;
+      int isp = -1;
+      if (kz == 0) {
+        if (bp.xhalf >= i0 && bp.xhalf < i0 + mpt) isp = bp.xhalf;
+        else if (j == 0 && i0 == 0) isp = 0;
+      }
+      if (j == 0 && kz == 0 && i0 == 0) {  // the DC mode: the slots' exact DC values replace F(0)
+        float2 *pd = sd + rowb * P + my_kc;
+#pragma unroll
+        for (int sl = 0; sl < NS; sl++) pd[sl * kc_n] = make_float2((float)dcv[sl], 0.0f);
+      }
       float acc[NP][NL];
 #pragma unroll
       for (int qq = 0; qq < NP; qq++)
 #pragma unroll
-        for (int l = 0; l < NL; l++) acc[qq][l] = 0.0f;
+        for (int l2 = 0; l2 < NL; l2++) acc[qq][l2] = 0.0f;
       int cur = -2;  // no bin yet: the first mode bisects the edges, later ones walk from the last
       float lo = 1.0f, hi = 0.0f;
       for (int m = m_lo; m < m_hi; m++) {
         const int i = i0 + m;
-        const float s = t.fx2f[i] + syz;
+        const float2 *pm = sd + (rowb + m * (n >> 3)) * P + my_kc;
+        const float4 xt = sxt[xt_index(i)];
+        const float s = xt.x + syz;
         if (!(s >= lo && s < hi)) {
           int b = cur;
           if (b == -2) {  // sElo[a] <= s < sElo[z] (sElo[0] = -inf, sElo[nk + 2] = +inf)
@@ -764,58 +850,45 @@ __global__ void __launch_bounds__(256) k_xfft_bin(BinParams bp, BinTables t, Xbi
 #pragma unroll
               for (int qq = 0; qq < NP; qq++)
 #pragma unroll
-                for (int l = 0; l < NL; l++) {
-                  if (acc[qq][l] != 0.0f) atomicAdd(&sb[(qq * NL + l) * nk + cur], acc[qq][l]);
-                  acc[qq][l] = 0.0f;
+                for (int l2 = 0; l2 < NL; l2++) {
+                  if (acc[qq][l2] != 0.0f && ((bp.pmask >> qq) & 1)) atomicAdd(&sb[(qq * NL + l2) * nk + cur], acc[qq][l2]);
+                  acc[qq][l2] = 0.0f;
                 }
             }
             cur = b;
           }
         }
         if (cur < 0 || cur >= nk) continue;
-        const int row = xfft_pos(xg.log2n, i);
-        const int rb = row * ncol, sw = row & (ncol - 1);
-        const bool dc = (i == 0 && j == 0 && kz == 0);
-        float2 A = sd[rb + ((0 * kc_n + my_kc) ^ sw)];
-        if (dc) A = make_float2(dcf0, 0.0f);
+        float2 A = pm[0];
         float2 B = make_float2(0.0f, 0.0f);
-        if (NF == 2) {
-          B = sd[rb + ((1 * kc_n + my_kc) ^ sw)];
-          if (dc) B = make_float2(dcf1, 0.0f);
-        }
+        if (NF == 2) B = pm[kc_n];
         if (IL) {
-          const float2 e = cmulf(t.exf[i], eyz);
-          float2 a = sd[rb + ((NF * kc_n + my_kc) ^ sw)];
-          if (dc) a = make_float2(NF == 2 ? dcf2 : dcf1, 0.0f);
-          A = cadd(A, cmulf(a, e));
-          if (NF == 2) {
-            float2 b2 = sd[rb + (((NF + 1) * kc_n + my_kc) ^ sw)];
-            if (dc) b2 = make_float2(dcf3, 0.0f);
-            B = cadd(B, cmulf(b2, e));
-          }
+          const float2 e = cmulf(make_float2(xt.z, xt.w), eyz);
+          A = cadd(A, cmulf(pm[NF * kc_n], e));
+          if (NF == 2) B = cadd(B, cmulf(pm[3 * kc_n], e));
         }
-        const float gc = cyz * t.cxf[i] * (float)herm_nm(i, j, kz, bp.xhalf);
-        const float fl = bp.los == 1 ? t.fxf[i] : flos_yz;
+        float gc = cyzn * xt.y;
+        if (i == isp) gc *= 2.0f;
+        const float fl = bp.los == 1 ? sfx[i] : flos_yz;
         const float mu = s > 0.0f ? fl * rsqrtf(s) : 0.0f;
         const float mu2 = mu * mu;
         const float L2 = 1.5f * mu2 - 0.5f;
         const float L4 = (4.375f * mu2 - 3.75f) * mu2 + 0.375f;
-        float P[NP];
-        P[0] = (A.x * A.x + A.y * A.y) * gc;
+        float Pq[NP];
+        Pq[0] = (A.x * A.x + A.y * A.y) * gc;
         if (NF == 2) {
-          P[1] = (A.x * B.x + A.y * B.y) * gc;
-          P[2] = (A.x * B.y - A.y * B.x) * gc;
-          P[3] = (B.x * B.x + B.y * B.y) * gc;
+          Pq[1] = (A.x * B.x + A.y * B.y) * gc;
+          Pq[2] = (A.x * B.y - A.y * B.x) * gc;
+          Pq[3] = (B.x * B.x + B.y * B.y) * gc;
         }
 #pragma unroll
         for (int qq = 0; qq < NP; qq++) {
-          if (!(bp.pmask & (1 << qq))) continue;  // a product no requested spectrum reads
-          acc[qq][0] += P[qq];
-          acc[qq][1] += P[qq] * L2;
-          acc[qq][2] += P[qq] * L4;
+          acc[qq][0] += Pq[qq];
+          acc[qq][1] += Pq[qq] * L2;
+          acc[qq][2] += Pq[qq] * L4;
           if (ODD) {
-            acc[qq][NL - 2] += P[qq] * mu;
-            acc[qq][NL - 1] += P[qq] * ((2.5f * mu2 - 1.5f) * mu);
+            acc[qq][NL - 2] += Pq[qq] * mu;
+            acc[qq][NL - 1] += Pq[qq] * ((2.5f * mu2 - 1.5f) * mu);
           }
         }
       }
@@ -823,8 +896,8 @@ __global__ void __launch_bounds__(256) k_xfft_bin(BinParams bp, BinTables t, Xbi
 #pragma unroll
         for (int qq = 0; qq < NP; qq++)
 #pragma unroll
-          for (int l = 0; l < NL; l++)
-            if (acc[qq][l] != 0.0f) atomicAdd(&sb[(qq * NL + l) * nk + cur], acc[qq][l]);
+          for (int l2 = 0; l2 < NL; l2++)
+            if (acc[qq][l2] != 0.0f && ((bp.pmask >> qq) & 1)) atomicAdd(&sb[(qq * NL + l2) * nk + cur], acc[qq][l2]);
       }
     }
   }
@@ -850,7 +923,7 @@ bool xbin_plan(const BinParams &bp, int nslot, XbinGeo &xg) {
   if (n < 16 || n > 2048 || (n & (n - 1)) != 0 || bp.out2d) return false;
   memset(&xg, 0, sizeof xg);
   xg.log2n = ilog2i(n);
-  xg.ncol = n <= 512 ? 16 : (n == 1024 ? 8 : 4);
+  xg.ncol = n <= 512 ? 32 : (n == 1024 ? 16 : 4);
   if (nslot > xg.ncol) return false;
   xg.log2ncol = ilog2i(xg.ncol);
   const int ns = nslot == 3 ? 4 : nslot;
@@ -859,24 +932,25 @@ bool xbin_plan(const BinParams &bp, int nslot, XbinGeo &xg) {
   xg.nkb = (bp.nzc + xg.kc - 1) / xg.kc;
   xg.nblocks = bp.ny * xg.nkb;
   const int np = bp.nfields == 1 ? 1 : 4, nl = bp.odd ? 5 : 3;
-  return xbin_smem_layout(n, xg.ncol, np, nl, bp.nk).total <= 100 * 1024;
+  return xbin_smem_layout(xg.log2n, xg.ncol, np, nl, bp.nk).total <= 220 * 1024;
 }
 
 template <int NF, bool IL, bool ODD>
 static void launch_xbin_t(cudaStream_t s, const BinParams &bp, const BinTables &t, const XbinGeo &xg,
                           void *const slots[4], const double *dcv, double *bins) {
   constexpr int NP = NF == 1 ? 1 : 4, NL = ODD ? 5 : 3;
-  const size_t smem = xbin_smem_layout(1 << xg.log2n, xg.ncol, NP, NL, bp.nk).total;
+  const size_t smem = xbin_smem_layout(xg.log2n, xg.ncol, NP, NL, bp.nk).total;
   cudaFuncSetAttribute(k_xfft_bin<NF, IL, ODD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_xfft_bin<NF, IL, ODD>, 256, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_xfft_bin<NF, IL, ODD>, XBIN_THREADS, smem);
   int dev = 0, nsm = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   int grid = (per_sm > 0 ? per_sm : 1) * nsm;
   if (grid > xg.nblocks) grid = xg.nblocks;
-  k_xfft_bin<NF, IL, ODD><<<grid, 256, smem, s>>>(bp, t, xg, (const float2 *)slots[0], (const float2 *)slots[1],
-                                                  (const float2 *)slots[2], (const float2 *)slots[3], dcv, bins);
+  k_xfft_bin<NF, IL, ODD><<<grid, XBIN_THREADS, smem, s>>>(bp, t, xg, (const float2 *)slots[0],
+                                                            (const float2 *)slots[1], (const float2 *)slots[2],
+                                                            (const float2 *)slots[3], dcv, bins);
 }
 
 void launch_xbin(cudaStream_t s, const BinParams &bp, const BinTables &t, const XbinGeo &xg, void *const slots[4],
