@@ -97,7 +97,7 @@ EXPORTS = [
     "capow_create", "capow_paint", "capow_get_stats", "capow_power", "capow_normalise", "capow_num_spectra",
     "capow_copy_grid", "capow_stage_ms", "capow_kernel_launches", "capow_destroy", "capow_read_params",
     "capow_read_catalogue", "capow_free", "capow_write_output", "capow_bin_centre", "capow_strerror",
-    "capow_last_error", "capow_paint_noalloc", "capow_backward", "capow_batch",
+    "capow_last_error", "capow_paint_noalloc", "capow_backward", "capow_batch", "capow_tile_kernel_ms",
 ]
 
 _lib = None
@@ -126,6 +126,7 @@ def lib() -> ctypes.CDLL:
     L.capow_copy_grid.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_double)]
     L.capow_stage_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
                                  ctypes.POINTER(ctypes.c_float)]
+    L.capow_tile_kernel_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int64)]
     L.capow_kernel_launches.argtypes = [vp]
     L.capow_kernel_launches.restype = ctypes.c_int64
     L.capow_destroy.argtypes = [vp]
@@ -391,6 +392,12 @@ class PowerSpectrum:
         self._check(lib().capow_stage_ms(self._ctx, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
                     "capow_stage_ms")
         return a.value, b.value, c.value
+
+    def tile_kernel_ms(self):
+        """(device ms of the last FP32 paint's tile-deposit kernel, particle records it deposited)."""
+        ms, rec = ctypes.c_float(), ctypes.c_int64()
+        self._check(lib().capow_tile_kernel_ms(self._ctx, ctypes.byref(ms), ctypes.byref(rec)), "capow_tile_kernel_ms")
+        return ms.value, rec.value
 
     def kernel_launches(self) -> int:
         return int(lib().capow_kernel_launches(self._ctx))

@@ -187,6 +187,8 @@ extern "C" int capow_create(const capow_params *p, const capow_options *opt, cap
     c->own_stream = true;
   }
   for (int k = 0; k < 4; k++) CK(c, cudaEventCreate(&c->ev[k]));
+  CK(c, cudaEventCreate(&c->ev_tile[0]));
+  CK(c, cudaEventCreate(&c->ev_tile[1]));
   c->g = make_geom(*p);
   if (c->prec != CAPOW_FP64 && !(c->g.margin < 0.25f))  // FP32 positions cannot resolve the cells
     FAIL(c, CAPOW_ENOTSUP, "box coordinates too large for FP32 cell positions (error margin %.3g cells); use FP64",
@@ -364,8 +366,12 @@ int enqueue_paint(capow_ctx *c, const capow_particles &d) {
         if (rc) return rc;
       }
     }
+    PaintBufs pb = c->pb;
+    pb.tile_ev0 = c->quiet ? nullptr : c->ev_tile[0];
+    pb.tile_ev1 = c->quiet ? nullptr : c->ev_tile[1];
+    c->tile_timed = !c->quiet;
     launch_paint32(c->stream, c->g, c->fs, c->tg, c->prec == CAPOW_FP32_DETERMINISTIC, d.dtype, d.x, d.y, d.z,
-                   d.vlos, d.w, n, gp, c->pb, c->st, &c->launches);
+                   d.vlos, d.w, n, gp, pb, c->st, &c->launches);
   }
   CK(c, cudaGetLastError());
   if (!c->quiet) CK(c, cudaEventRecord(c->ev[1], c->stream));
@@ -660,6 +666,24 @@ extern "C" int capow_stage_ms(capow_ctx *c, float *paint_ms, float *fft_ms, floa
   return CAPOW_OK;
 }
 
+extern "C" int capow_tile_kernel_ms(capow_ctx *c, float *ms, int64_t *records) {
+  if (!c) return CAPOW_EINVAL;
+  if (c->prec == CAPOW_FP64 || !c->tile_timed)
+    FAIL(c, CAPOW_ESTATE, "no timed FP32 tile deposit: paint an FP32 context first");
+  CK(c, cudaEventSynchronize(c->ev_tile[1]));
+  float t = 0.0f;
+  CK(c, cudaEventElapsedTime(&t, c->ev_tile[0], c->ev_tile[1]));
+  if (ms) *ms = t;
+  if (records) {
+    std::vector<unsigned> cnt(c->tg.ntiles);
+    CK(c, cudaMemcpy(cnt.data(), c->pb.counts, sizeof(unsigned) * cnt.size(), cudaMemcpyDeviceToHost));
+    long long tot = 0;
+    for (unsigned v : cnt) tot += c->pb.bucket_cap ? (v < c->pb.bucket_cap ? v : c->pb.bucket_cap) : v;
+    *records = tot;
+  }
+  return CAPOW_OK;
+}
+
 extern "C" void capow_destroy(capow_ctx *c) {
   if (!c) return;
   cudaSetDevice(c->o.device);
@@ -687,6 +711,8 @@ extern "C" void capow_destroy(capow_ctx *c) {
   if (c->h_st) cudaFreeHost(c->h_st);
   for (int k = 0; k < 4; k++)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  for (int k = 0; k < 2; k++)
+    if (c->ev_tile[k]) cudaEventDestroy(c->ev_tile[k]);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

@@ -59,6 +59,8 @@ struct capow_ctx {
   DevStats *h_st;
   std::vector<void *> allocs;
   cudaEvent_t ev[4];
+  cudaEvent_t ev_tile[2];  // around the FP32 tile-deposit kernel of the last paint
+  bool tile_timed;         // the last FP32 paint recorded ev_tile
   long long launches;
   char err[512];
 };

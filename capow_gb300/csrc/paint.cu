@@ -1283,9 +1283,11 @@ static void run_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, cons
                                   b.edge_list, b.edge_count, b.ovf_recs, in.w ? b.ovf_w : nullptr, b.ovf_tile,
                                   b.ovf_count, b.ovf_cap, st);
     const bool wts = in.w != nullptr;
+    if (b.tile_ev0) cudaEventRecord(b.tile_ev0, s);
     if (g.order == 3) launch_rec_k<3>(s, g, fs, tg, b, wts, grids, st);
     else if (g.order == 2) launch_rec_k<2>(s, g, fs, tg, b, wts, grids, st);
     else launch_rec_k<1>(s, g, fs, tg, b, wts, grids, st);
+    if (b.tile_ev1) cudaEventRecord(b.tile_ev1, s);
     k_edge_fixup<T><<<152 * 2, 128, 0, s>>>(g, fs, in, b.edge_list, b.edge_count, grids, st);
     *launches += 4;
     return;
@@ -1298,15 +1300,19 @@ static void run_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, cons
     const int nslot = fs.nfields * (g.interlace ? 2 : 1);
     const size_t smem = tile_smem_bytes(tg, nslot, 1);
     cudaFuncSetAttribute(k_tile_paint<T, unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (b.tile_ev0) cudaEventRecord(b.tile_ev0, s);
     k_tile_paint<T, unsigned long long><<<tg.ntiles, 256, smem, s>>>(g, fs, tg, in, n, b.offsets, b.recs,
                                                                       in.w ? b.recw : nullptr, b.capacity, grids,
                                                                       b.fixed_scale, st);
+    if (b.tile_ev1) cudaEventRecord(b.tile_ev1, s);
     *launches += 4;
   } else {
     const bool wts = in.w != nullptr;
+    if (b.tile_ev0) cudaEventRecord(b.tile_ev0, s);
     if (g.order == 3) launch_rec_k<3>(s, g, fs, tg, b, wts, grids, st);
     else if (g.order == 2) launch_rec_k<2>(s, g, fs, tg, b, wts, grids, st);
     else launch_rec_k<1>(s, g, fs, tg, b, wts, grids, st);
+    if (b.tile_ev1) cudaEventRecord(b.tile_ev1, s);
     k_edge_fixup<T><<<152 * 2, 128, 0, s>>>(g, fs, in, b.edge_list, b.edge_count, grids, st);
     *launches += 5;
   }

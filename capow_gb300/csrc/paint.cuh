@@ -60,6 +60,8 @@ struct PaintBufs {
   unsigned *ovf_tile;
   unsigned *ovf_count;
   unsigned long long ovf_cap;
+  // when set, recorded on the stream just before and after the tile-deposit kernel
+  cudaEvent_t tile_ev0, tile_ev1;
 };
 
 // host launchers (paint.cu)

@@ -227,6 +227,12 @@ int capow_copy_grid(capow_ctx *ctx, int which, double *host_out);
 /* device milliseconds of the last paint, FFT and bin stages (CUDA events on the context stream) */
 int capow_stage_ms(capow_ctx *ctx, float *paint_ms, float *fft_ms, float *bin_ms);
 
+/* device milliseconds of the tile-deposit kernel of the last FP32 paint (CUDA events on the context
+ * stream, around that one launch) and the number of particle records it deposited (each record is
+ * one particle's footprint within one tile). For roofline measurements; no reference counterpart.
+ * CAPOW_ESTATE on FP64 contexts or before an FP32 paint. */
+int capow_tile_kernel_ms(capow_ctx *ctx, float *ms, int64_t *records);
+
 /* total number of kernels this library launched on the context since creation */
 int64_t capow_kernel_launches(const capow_ctx *ctx);
 

@@ -185,3 +185,26 @@ def test_fp32_bucket_overflow_parity(gpu, frac, n):
     dd = oracle_run(po, parts, 0)["raw"]["Pk0"]
     pp = oracle_run(po, parts, 2)["raw"]["Pk0"]
     assert_spectrum(res[0], ref["raw"], np.sqrt(np.abs(dd * pp)), "fp32", odd=True, label=f"clump {frac}")
+
+
+def test_tile_kernel_timing(gpu):
+    """capow_tile_kernel_ms: the tile-deposit kernel's event time and record count of the last FP32
+    paint (every particle has at least one record, at most one per tile its two stencils reach);
+    FP64 contexts have no tile kernel."""
+    p = cg.Params(NX=64, NY=64, NZ=64, NK=20, Maxk=0.3, XMIN=0.0, XMAX=1000.0, YMIN=0.0, YMAX=1000.0,
+                  ZMIN=0.0, ZMAX=1000.0, InterpOrder=3, DoInterlacing=1, LOS=3, Momentum=0)
+    rng = np.random.default_rng(5)
+    n = 50000
+    x, y, z = (rng.uniform(1.0, 999.0, n) for _ in range(3))
+    v = rng.normal(0.0, 10.0, n)
+    with cg.PowerSpectrum(p, precision="fp32") as ps:
+        with pytest.raises(cg.CapowError):
+            ps.tile_kernel_ms()
+        ps.paint(x, y, z, v)
+        ms, rec = ps.tile_kernel_ms()
+        assert ms > 0.0
+        assert n <= rec <= 8 * n
+    with cg.PowerSpectrum(p, precision="fp64") as ps:
+        ps.paint(x, y, z, v)
+        with pytest.raises(cg.CapowError):
+            ps.tile_kernel_ms()
