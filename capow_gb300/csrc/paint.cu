@@ -845,6 +845,25 @@ __device__ __forceinline__ int tile_scale_exp(float sum_abs) {
   return S > 100 ? 100 : (S < -100 ? -100 : S);
 }
 
+// Scale exponent S of a tile that also keeps every single deposit below 2^22 in magnitude
+// (|w v^e| 2^S < 2^22, tap weights <= 1), so that rint_small can round it exactly.
+__device__ __forceinline__ int tile_scale_exp2(float sum_abs, float max_abs) {
+  int S = tile_scale_exp(sum_abs);
+  const float mb = max_abs * 1.001f;
+  if (mb > 0.0f && isfinite(mb)) {
+    const int Sm = 21 - ilogbf(mb);
+    if (Sm < S) S = Sm;
+  }
+  return S < -100 ? -100 : S;
+}
+
+// Round-to-nearest-even of a * b as an int32, for |a * b| < 2^22: the fused multiply-add rounds the
+// exact product plus 1.5 * 2^23 to an integer, whose FP32 bit pattern is 0x4B400000 + that integer.
+// (Two FP32/integer-pipe instructions instead of a conversion.)
+__device__ __forceinline__ int rint_small(float a, float b) {
+  return __float_as_int(__fmaf_rn(a, b, 12582912.0f)) - 0x4B400000;
+}
+
 // The int32 quantum of a tile is about 2^-30 of the tile's total |w v^e|, and a cell sums up to one
 // rounded deposit per record: the cells' relative error grows with the record count. A tile with
 // more records than this (a dense clump; uniform catalogues put about a thousand records in a
@@ -923,10 +942,11 @@ __device__ void tile_paint_precise(const Geom &g, const FieldSpec &fs, const Til
 // FP32 tile kernel for particles away from every edge of the reference's rules (those are painted
 // by k_edge_fixup). One CTA per tile; shared memory holds the tile of every grid slot, both
 // stencils, unpadded [tx][ty][tz], as int32 fixed point with a per-tile power-of-two scale, so
-// every deposit is one native integer shared-memory atomic. Lane = record: each thread reads one
-// record, derives its taps once per stencil and adds the K^3 products, so a record is read once
-// and nothing is staged. The cells are converted back to FP32 when the tile is written. (NGRID of
-// these particles is counted by k_count.)
+// every deposit is one native integer shared-memory atomic (the scale also keeps each deposit below
+// 2^22, where rint_small rounds it). Lane = record: each thread reads one record, derives its taps
+// once per stencil and adds the K^3 products, so a record is read once and nothing is staged. The
+// cells are converted back to FP32 when the tile is written. (NGRID of these particles is counted
+// by k_bucket or k_count.)
 template <int K, int NF, bool IL>
 __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileGeo tg, const unsigned *offsets,
                                                      const unsigned *counts, unsigned cap, const float4 *recs,
@@ -954,9 +974,9 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
   if (re > capacity) re = capacity;
   if (rb > re) rb = re;
   // pre-pass over the tile's records: sum |w v^e| per field (the records stay in L1 for the deposits)
-  __shared__ float red_abs[2][32];
+  __shared__ float red_abs[4][32];
   {
-    float la = 0.0f, lb = 0.0f;
+    float la = 0.0f, lb = 0.0f, ma = 0.0f, mb = 0.0f;
     for (unsigned long long r = rb + threadIdx.x; r < re; r += blockDim.x) {
       const float4 rec = recs[r];
       const float w = recw ? recw[r] : 1.0f;
@@ -965,21 +985,32 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
       for (int e = 0; e < fs.eb; e++) vb *= rec.w;
       la += fabsf(va);
       lb += fabsf(vb);
+      ma = fmaxf(ma, fabsf(va));
+      mb = fmaxf(mb, fabsf(vb));
     }
     la = warp_sum_f(la);
     lb = warp_sum_f(lb);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      ma = fmaxf(ma, __shfl_xor_sync(0xffffffffu, ma, o));
+      mb = fmaxf(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+    }
     if ((threadIdx.x & 31) == 0) {
       red_abs[0][threadIdx.x >> 5] = la;
       red_abs[1][threadIdx.x >> 5] = lb;
+      red_abs[2][threadIdx.x >> 5] = ma;
+      red_abs[3][threadIdx.x >> 5] = mb;
     }
     __syncthreads();
   }
-  float ta = 0.0f, tb = 0.0f;
+  float ta = 0.0f, tb = 0.0f, xa = 0.0f, xb = 0.0f;
   for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
     ta += red_abs[0][k];
     tb += red_abs[1][k];
+    xa = fmaxf(xa, red_abs[2][k]);
+    xb = fmaxf(xb, red_abs[3][k]);
   }
-  const int SA = tile_scale_exp(ta), SB = tile_scale_exp(tb);
+  const int SA = tile_scale_exp2(ta, xa), SB = tile_scale_exp2(tb, xb);
   if (re - rb > TILE_PRECISE_RECORDS) {  // a dense tile (uniform over the CTA)
     const int words = NS * NF * tsz;  // the int32 tile area, reused as int64 cells
     tile_paint_precise<K, NF, IL>(g, fs, tg, recs, recw, rb, re, ta, tb, x0, y0, z0, ex, ey, ez, pyz, tsz,
@@ -1017,11 +1048,13 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
           const float wxy = wx[a] * wy[b2];
           const float pa = va * wxy, pb = vb * wxy;
           const int oxy = ox[a] + oy[b2];
+          // one test per (x, y) tap pair: an x or y tap outside the tile has weight 0. A z tap outside
+          // it (the z edge of a tile is 32 cells: rare) has weight 0 and offset 0 and adds 0 there.
+          if (wxy != 0.0f) {
 #pragma unroll
-          for (int c = 0; c < K; c++) {
-            if (wxy != 0.0f && wz[c] != 0.0f) {
-              atomicAdd(sA + oxy + oz[c], __float2int_rn(pa * wz[c]));
-              if (NF == 2) atomicAdd(sA + tsz + oxy + oz[c], __float2int_rn(pb * wz[c]));
+            for (int c = 0; c < K; c++) {
+              atomicAdd(sA + oxy + oz[c], rint_small(pa, wz[c]));
+              if (NF == 2) atomicAdd(sA + tsz + oxy + oz[c], rint_small(pb, wz[c]));
             }
           }
         }
