@@ -562,7 +562,7 @@ __global__ void __launch_bounds__(256) k_bin(BinParams bp, BinTables t, const ty
 // holds the block's ncol columns (c = slot * kc + kz - k0) with a pitch of ncol + 1: a butterfly's
 // rows are one base plus a fixed stride, a warp's accesses are whole rows, and the pad spreads the
 // rows the binning reads at once over the banks.
-constexpr int XBIN_THREADS = 512;
+constexpr int XBIN_THREADS = 1024;
 
 struct XbinSmem {
   unsigned sd, stw, sxt, sfx, sb, sE, sElo, sEhi, total;
@@ -705,8 +705,8 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
   const float topf32 = (float)t.E[nk + 1] * 1.0001f;
   // binning work items: (kz column of the block, run of mpt consecutive kx), mpt <= 8 chosen so that
   // the kc * NX / mpt items keep every thread busy. Within a column the run index is rotated by 3
-  // bits, so that the 16 lanes of a half-warp start runs whose rows differ in their low 4 bits (the
-  // shared reads of a run step are then conflict-free at NX = 512).
+  // bits, so that neighbouring lanes start runs far apart in x and their rows (digit-reversed)
+  // spread over the shared-memory banks.
   const int log2mpt = min(3, max(0, log2n + xg.log2kc - (31 - __clz(blockDim.x))));
   const int mpt = 1 << log2mpt, log2nr = log2n - log2mpt, nitems = kc_n << log2nr;
   const long long xstride = (long long)bp.ny * bp.nzc;

@@ -381,13 +381,13 @@ __global__ void __launch_bounds__(256) k_count(Geom g, FieldSpec fs, TileGeo tg,
     }
     const int na = __reduce_max_sync(FULL_MASK, has ? TX.n : 0), nb = __reduce_max_sync(FULL_MASK, has ? TY.n : 0),
               nc = __reduce_max_sync(FULL_MASK, has ? TZ.n : 0);
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-      for (int b = 0; b < 3; b++)
-#pragma unroll
-        for (int c = 0; c < 3; c++)
-          if (a < na && b < nb && c < nc) warp_run_add(counts, tile_key(tg, has, TX, TY, TZ, a, b, c), false);
+    // runtime loops over the warp's footprint tiles (warp-uniform bounds): one copy of the body
+#pragma unroll 1
+    for (int a = 0; a < na; a++)
+#pragma unroll 1
+      for (int b = 0; b < nb; b++)
+#pragma unroll 1
+        for (int c = 0; c < nc; c++) warp_run_add(counts, tile_key(tg, has, TX, TY, TZ, a, b, c), false);
   }
   // FP32 per-thread partials and warp sums, FP64 across warps
   const float vals[10] = {f_read, f_out, f_nsq, f_v[0], f_v[1], f_v[2], f_v[3], f_abs[0], f_abs[1], f_grid};
@@ -469,13 +469,13 @@ __global__ void __launch_bounds__(256) k_scatter(Geom g, FieldSpec fs, TileGeo t
     }
     const int na = __reduce_max_sync(FULL_MASK, has ? TX.n : 0), nb = __reduce_max_sync(FULL_MASK, has ? TY.n : 0),
               nc = __reduce_max_sync(FULL_MASK, has ? TZ.n : 0);
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-      for (int b = 0; b < 3; b++)
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          if (!(a < na && b < nb && c < nc)) continue;  // warp-uniform
+    // runtime loops over the warp's footprint tiles (warp-uniform bounds): one copy of the body
+#pragma unroll 1
+    for (int a = 0; a < na; a++)
+#pragma unroll 1
+      for (int b = 0; b < nb; b++)
+#pragma unroll 1
+        for (int c = 0; c < nc; c++) {
           const int key = tile_key(tg, has, TX, TY, TZ, a, b, c);
           const unsigned slot = warp_run_add(cursor, key, true);
           if (key >= 0 && slot < capacity) {
@@ -543,13 +543,13 @@ __global__ void __launch_bounds__(256) k_bucket(Geom g, FieldSpec fs, TileGeo tg
     }
     const int na = __reduce_max_sync(FULL_MASK, has ? TX.n : 0), nb = __reduce_max_sync(FULL_MASK, has ? TY.n : 0),
               nc = __reduce_max_sync(FULL_MASK, has ? TZ.n : 0);
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-      for (int b = 0; b < 3; b++)
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          if (!(a < na && b < nb && c < nc)) continue;  // warp-uniform
+    // runtime loops over the warp's footprint tiles (warp-uniform bounds): one copy of the body
+#pragma unroll 1
+    for (int a = 0; a < na; a++)
+#pragma unroll 1
+      for (int b = 0; b < nb; b++)
+#pragma unroll 1
+        for (int c = 0; c < nc; c++) {
           const int key = tile_key(tg, has, TX, TY, TZ, a, b, c);
           const unsigned slot = warp_run_add(counts, key, true);
           if (key < 0) continue;
