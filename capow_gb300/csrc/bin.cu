@@ -170,6 +170,23 @@ int build_bin_tables(const capow_params &p, const Geom &g, int precision, BinTab
     t.twx = upload(tw, allocs, s);
     if (!t.twx) return 1;
   }
+  t.twz = t.tpz = nullptr;
+  const int nzp = p.NZ;
+  if (nzp >= 32 && nzp <= 2048 && (nzp & (nzp - 1)) == 0) {  // z pass of the transposed fused path
+    const int m = nzp / 2;
+    std::vector<float2> tz(m), tp(m + 1);
+    for (int q = 0; q < m; q++) {
+      const double a = -2.0 * M_PI * (double)q / (double)m;
+      tz[q] = make_float2((float)cos(a), (float)sin(a));
+    }
+    for (int k = 0; k <= m; k++) {
+      const double a = -2.0 * M_PI * (double)k / (double)nzp;
+      tp[k] = make_float2((float)cos(a), (float)sin(a));
+    }
+    t.twz = upload(tz, allocs, s);
+    t.tpz = upload(tp, allocs, s);
+    if (!t.twz || !t.tpz) return 1;
+  }
   return (t.E && t.Elo && t.Ehi && t.ezf) ? 0 : 1;
 }
 
@@ -188,7 +205,7 @@ void relocate_bin_tables(BinTables &t, const void *base) {
                 (void **)&t.fyf,  (void **)&t.fzf,  (void **)&t.cxd,  (void **)&t.cyd,  (void **)&t.czd,
                 (void **)&t.cxf,  (void **)&t.cyf,  (void **)&t.czf,  (void **)&t.exd,  (void **)&t.eyd,
                 (void **)&t.ezd,  (void **)&t.exf,  (void **)&t.eyf,  (void **)&t.ezf,  (void **)&t.E,
-                (void **)&t.Elo,  (void **)&t.Ehi,  (void **)&t.twx};
+                (void **)&t.Elo,  (void **)&t.Ehi,  (void **)&t.twx,  (void **)&t.twz,  (void **)&t.tpz};
   for (void **q : f)
     if (*q) *q = (void *)((const char *)base + (uintptr_t)*q);
 }
@@ -709,23 +726,26 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
   // spread over the shared-memory banks.
   const int log2mpt = min(3, max(0, log2n + xg.log2kc - (31 - __clz(blockDim.x))));
   const int mpt = 1 << log2mpt, log2nr = log2n - log2mpt, nitems = kc_n << log2nr;
-  const long long xstride = (long long)bp.ny * bp.nzc;
+  const long long xstride = (long long)bp.ny * bp.nzc;  // = n_outer * n_inner
   const int Q1 = n >> 3, nbf1 = ncol << (log2n - 3);
   const long long qstep = (long long)Q1 * xstride;
   __syncthreads();
   for (int blk = blockIdx.x; blk < xg.nblocks; blk += gridDim.x) {
-    const int j = blk / xg.nkb, k0 = (blk - j * xg.nkb) * kc_n;
-    // every mode of the block has s >= fy^2 + fz(k0)^2: skip the block when that is clearly beyond
-    // the top edge (a block kept near the edge only costs work; each mode is tested exactly)
-    if (t.fy2f[j] + t.fz2f[k0] > topf32) continue;
+    const int bo = blk / xg.nkb, bi0 = (blk - bo * xg.nkb) * kc_n;  // outer index, first inner index
+    // every mode of the block has s >= the block's smallest fy^2 + fz^2 (fz^2 grows with kz; fy^2
+    // rises to ky = NY/2 and falls after it, so over a run of ky it is smallest at an end): skip the
+    // block when that is clearly beyond the top edge (each kept mode is tested exactly)
+    const float smin = xg.tr ? t.fz2f[bo] + fminf(t.fy2f[bi0], t.fy2f[min(bi0 + kc_n, bp.ny) - 1])
+                             : t.fy2f[bo] + t.fz2f[bi0];
+    if (smin > topf32) continue;
     __syncthreads();  // the previous block's binning has read sd
     // first DIF stage (span NX) straight from HBM: butterfly (column c, jj) reads rows jj + q NX/8
     for (int u = threadIdx.x; u < nbf1; u += blockDim.x) {
       const int c = u & (ncol - 1), jj = u >> xg.log2ncol;
-      const int sl = c >> xg.log2kc, kz = k0 + (c & (kc_n - 1));
-      const bool live = sl < NS && kz < bp.nzc;
+      const int sl = c >> xg.log2kc, inner = bi0 + (c & (kc_n - 1));
+      const bool live = sl < NS && inner < xg.n_inner;
       const float2 *g = sl == 0 ? g0 : (sl == 1 ? g1 : (sl == 2 ? g2 : g3));
-      const float2 *gp = g + (live ? (long long)jj * xstride + (long long)j * bp.nzc + kz : 0ll);
+      const float2 *gp = g + (live ? (long long)jj * xstride + (long long)bo * xg.n_inner + inner : 0ll);
       float2 a[8];
 #pragma unroll
       for (int q = 0; q < 8; q++) a[q] = live ? ld_col(gp + q * qstep) : make_float2(0.0f, 0.0f);
@@ -782,8 +802,9 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
       // rows of the run: the digit reversal is a permutation of bit positions and i0, m < mpt <= 8
       // have disjoint bits, so row(i0 + m) = row(i0) + row(m) = row(i0) + m NX/8
       const int rowb = xfft_pos(log2n, i0);
-      const int kz = k0 + my_kc;
-      if (kz >= bp.nzc) continue;
+      const int inner = bi0 + my_kc;
+      if (inner >= xg.n_inner) continue;
+      const int j = xg.tr ? inner : bo, kz = xg.tr ? bo : inner;
       const float syz = t.fy2f[j] + t.fz2f[kz];
       float cyz = t.cyf[j] * t.czf[kz];
       if (IL) cyz *= 0.25f;
@@ -912,13 +933,171 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
   }
 }
 
+// ------------------------------------------------------------ z-axis real-to-complex DFT (FP32)
+// The first axis of the 3-D transform (src/main.c:266-271) on the transposed fused path: every
+// (x, y) row of NZ reals of every painted grid, as the M = NZ/2-point complex DFT Z of
+// z[n] = x[2n] + i x[2n+1] followed by the real-input split
+//   X[k] = (Z[k] + Z*[M-k]) / 2 - (i/2) e^{-2 pi i k/NZ} (Z[k] - Z*[M-k]),  k = 0..M (Z[M] = Z[0]).
+// Written out of place and transposed, [NX][NZ/2+1][NY]: the y axis is then a contiguous row for
+// the batched cuFFT C2C that follows, and ZB consecutive ky at one kz are contiguous for the fused
+// x-axis pass. A CTA transforms ZB consecutive rows (one x) in shared memory: coalesced row reads,
+// the same in-place radix-8 DIF stages as the x-axis pass (rows padded to ZB + 1), and ZB * 8 byte
+// segments written per kz.
+constexpr int ZR_THREADS = 256;
+
+// twiddle-table entries of the radix-8 stages of an M = 2^log2m point DIF with more than one
+// butterfly per group
+CAPOW_HD unsigned zr2c_tw_entries(int log2m) {
+  unsigned e = 0;
+  for (int l = log2m; l >= 4; l -= 3) e += 8u << (l - 3);
+  return e;
+}
+
+struct ZrGeo {
+  int log2m, nx, ny, nzc, row, nyb, ns;
+  long long slice, in_slot, out_slot;
+};
+
+template <int ZB>
+__global__ void __launch_bounds__(ZR_THREADS) k_zr2c(ZrGeo zg, BinTables t, const float *in, float2 *out) {
+  constexpr int LZB = ZB == 16 ? 4 : 3;
+  extern __shared__ __align__(16) unsigned char smz[];
+  const int log2m = zg.log2m, M = 1 << log2m, P = ZB + 1, Q1 = M >> 3;
+  float2 *sd = (float2 *)smz;                                      // [M][ZB + 1]
+  float2 *stw = (float2 *)(smz + align16(8u * (unsigned)M * P));  // radix-8 stage twiddle tables
+  int *spos = (int *)(smz + align16(8u * (unsigned)M * P) + 8u * zr2c_tw_entries(log2m));  // row of Z[k]
+  for (int k = threadIdx.x; k < M; k += blockDim.x) spos[k] = xfft_pos(log2m, k);
+  for (int l = log2m, off = 0; l >= 4; off += 8 << (l - 3), l -= 3) {
+    const int step = M >> l;  // M / span
+    for (int e = threadIdx.x; e < (8 << (l - 3)); e += blockDim.x)
+      stw[off + e] = t.twz[((e & 7) * (e >> 3) * step) & (M - 1)];
+  }
+  const int per_slot = zg.nx * zg.nyb, nblk = per_slot * zg.ns;
+  for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {  // (slot, x, block of ZB rows)
+    const int sl = blk / per_slot, rem = blk - sl * per_slot;
+    const int x = rem / zg.nyb, y0 = (rem - x * zg.nyb) * ZB;
+    const float *src = in + sl * zg.in_slot + (long long)x * zg.slice;
+    __syncthreads();  // tables written; the previous block's output has read sd
+    // first DIF stage (span M) straight from the rows: butterfly (row r, jj) reads z[jj + q M/8];
+    // lanes run along a row, so each of a warp's 8 loads is one contiguous 256-byte piece
+    for (int u = threadIdx.x; u < (ZB << (log2m - 3)); u += blockDim.x) {
+      const int jj = u & (Q1 - 1), r = u >> (log2m - 3), y = y0 + r;
+      const float2 *rp = reinterpret_cast<const float2 *>(src + (long long)(y < zg.ny ? y : 0) * zg.row) + jj;
+      float2 a[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) a[q] = y < zg.ny ? __ldcs(rp + q * Q1) : make_float2(0.0f, 0.0f);
+      dft8(a);
+      if (jj > 0) twiddle8(a, stw + 8 * jj);
+      float2 *p = sd + jj * P + r;
+#pragma unroll
+      for (int q = 0; q < 8; q++) p[q * Q1 * P] = a[q];
+    }
+    __syncthreads();
+    int l = log2m - 3, twoff = 8 * Q1;
+    for (; l >= 3; l -= 3) {  // the other radix-8 DIF stages
+      const int log2q = l - 3, Q = 1 << log2q, qs = Q * P;
+      for (int u = threadIdx.x; u < (ZB << (log2m - 3)); u += blockDim.x) {
+        const int c = u & (ZB - 1), v = u >> LZB;
+        const int jj = v & (Q - 1);
+        float2 *p = sd + (((v >> log2q) << l) + jj) * P + c;
+        float2 a[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) a[q] = p[q * qs];
+        dft8(a);
+        if (jj > 0) twiddle8(a, stw + twoff + 8 * jj);
+#pragma unroll
+        for (int q = 0; q < 8; q++) p[q * qs] = a[q];
+      }
+      __syncthreads();
+      if (Q > 1) twoff += 8 * Q;
+    }
+    if (l == 2) {  // a last radix-4 stage (span 4: no twiddles)
+      for (int u = threadIdx.x; u < (ZB << (log2m - 2)); u += blockDim.x) {
+        float2 *p = sd + ((u >> LZB) << 2) * P + (u & (ZB - 1));
+        float2 a[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) a[q] = p[q * P];
+        dft4(a);
+#pragma unroll
+        for (int q = 0; q < 4; q++) p[q * P] = a[q];
+      }
+      __syncthreads();
+    } else if (l == 1) {  // a last radix-2 stage
+      for (int u = threadIdx.x; u < (ZB << (log2m - 1)); u += blockDim.x) {
+        float2 *p = sd + ((u >> LZB) << 1) * P + (u & (ZB - 1));
+        const float2 a0 = p[0], a1 = p[P];
+        p[0] = cadd(a0, a1);
+        p[P] = csub(a0, a1);
+      }
+      __syncthreads();
+    }
+    // real-input split and transposed store; the thread's row r is the same on every step
+    const int r = threadIdx.x & (ZB - 1), y = y0 + r;
+    if (y < zg.ny) {
+      float2 *dst = out + sl * zg.out_slot + (long long)x * zg.nzc * zg.ny + y;
+      for (int k = threadIdx.x >> LZB; k <= M; k += blockDim.x >> LZB) {
+        const float2 zk = sd[spos[k & (M - 1)] * P + r];
+        const float2 zm = sd[spos[(M - k) & (M - 1)] * P + r];
+        const float2 A = make_float2(zk.x + zm.x, zk.y - zm.y);  // Z[k] + conj Z[M-k]
+        const float2 B = make_float2(zk.x - zm.x, zk.y + zm.y);  // Z[k] - conj Z[M-k]
+        const float2 wB = cmulf(__ldg(t.tpz + k), B);
+        dst[(long long)k * zg.ny] = make_float2(0.5f * (A.x + wB.y), 0.5f * (A.y - wB.x));
+      }
+    }
+  }
+}
+
+bool zr2c_supported(const BinParams &bp) {
+  return bp.nz >= 32 && bp.nz <= 2048 && (bp.nz & (bp.nz - 1)) == 0;
+}
+
+template <int ZB>
+static void launch_zr2c_t(cudaStream_t s, const ZrGeo &zg, const BinTables &t, int nslot, const float *in,
+                          float2 *out) {
+  const int M = 1 << zg.log2m;
+  const size_t smem = align16(8u * (unsigned)M * (ZB + 1)) + 8u * zr2c_tw_entries(zg.log2m) + 4u * M;
+  cudaFuncSetAttribute(k_zr2c<ZB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 1, dev = 0, nsm = 152;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zr2c<ZB>, ZR_THREADS, smem);
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const long long nblk = (long long)zg.nx * zg.nyb * nslot;
+  long long grid = (long long)(per_sm > 0 ? per_sm : 1) * nsm;
+  if (grid > nblk) grid = nblk;
+  k_zr2c<ZB><<<(unsigned)grid, ZR_THREADS, smem, s>>>(zg, t, in, out);
+}
+
+void launch_zr2c(cudaStream_t s, const BinParams &bp, const BinTables &t, int nslot, const float *in,
+                 long long in_slot, int row, float2 *out, long long out_slot, long long *launches) {
+  ZrGeo zg;
+  int lm = 0;
+  while ((2 << lm) < bp.nz) lm++;  // M = NZ / 2 = 2^lm
+  zg.log2m = lm;
+  zg.nx = bp.nx;
+  zg.ny = bp.ny;
+  zg.nzc = bp.nzc;
+  zg.row = row;
+  zg.slice = (long long)bp.ny * row;
+  zg.in_slot = in_slot;
+  zg.out_slot = out_slot;
+  zg.ns = nslot;
+  if (bp.nz <= 512) {  // 16 rows per CTA: 128-byte segments per kz
+    zg.nyb = (bp.ny + 15) / 16;
+    launch_zr2c_t<16>(s, zg, t, nslot, in, out);
+  } else {  // 8 rows per CTA keeps the shared rows within 80 KB
+    zg.nyb = (bp.ny + 7) / 8;
+    launch_zr2c_t<8>(s, zg, t, nslot, in, out);
+  }
+  (*launches)++;
+}
+
 static int ilog2i(int v) {
   int l = 0;
   while ((1 << l) < v) l++;
   return l;
 }
 
-bool xbin_plan(const BinParams &bp, int nslot, XbinGeo &xg) {
+bool xbin_plan(const BinParams &bp, int nslot, XbinGeo &xg, bool transposed) {
   const int n = bp.nx;
   if (n < 16 || n > 2048 || (n & (n - 1)) != 0 || bp.out2d) return false;
   memset(&xg, 0, sizeof xg);
@@ -929,8 +1108,11 @@ bool xbin_plan(const BinParams &bp, int nslot, XbinGeo &xg) {
   const int ns = nslot == 3 ? 4 : nslot;
   xg.kc = xg.ncol / ns;
   xg.log2kc = ilog2i(xg.kc);
-  xg.nkb = (bp.nzc + xg.kc - 1) / xg.kc;
-  xg.nblocks = bp.ny * xg.nkb;
+  xg.tr = transposed ? 1 : 0;
+  xg.n_outer = transposed ? bp.nzc : bp.ny;
+  xg.n_inner = transposed ? bp.ny : bp.nzc;
+  xg.nkb = (xg.n_inner + xg.kc - 1) / xg.kc;
+  xg.nblocks = xg.n_outer * xg.nkb;
   const int np = bp.nfields == 1 ? 1 : 4, nl = bp.odd ? 5 : 3;
   return xbin_smem_layout(xg.log2n, xg.ncol, np, nl, bp.nk).total <= 220 * 1024;
 }

@@ -29,12 +29,18 @@ struct BinTables {
   double *E;
   float *Elo, *Ehi;  // E[b]*(1+eps), E[b]*(1-eps) rounded outward/inward: safe FP32 tests
   float2 *twx;       // exp(-2 pi i q / NX), q < NX (fused x-axis FFT; power-of-two NX only)
+  // z-axis pass of the fused path (power-of-two NZ >= 32 only): exp(-2 pi i q / M), q < M = NZ/2,
+  // for the M-point complex DFT, and exp(-2 pi i k / NZ), k <= M, for its real-input split
+  float2 *twz, *tpz;
 };
 
 // Geometry of the fused x-axis FFT + binning pass (k_xfft_bin): blocks of `ncol` columns of the
-// (y, z)-transformed grids, `kc` consecutive kz of one ky in each of the nslot grids.
+// (y, z)-transformed grids, `kc` consecutive "inner" indices of one "outer" index in each of the
+// nslot grids. Layout [NX][outer][inner]: tr = 0, [NX][NY][NZ/2+1] (outer ky, inner kz, after the
+// cuFFT 2-D transform); tr = 1, [NX][NZ/2+1][NY] (outer kz, inner ky, after k_zr2c and the y pass).
 struct XbinGeo {
   int log2n, ncol, log2ncol, kc, log2kc, nkb, nblocks;
+  int tr, n_outer, n_inner;
 };
 
 struct BinParams {
@@ -72,8 +78,14 @@ int bin_products(int nfields);
 
 // Fused path: plan for a grid (returns false when NX is not a power of two in [16, 2048], the 2-D
 // bins are requested, or the shared-memory bins do not fit), and its launcher. The slots hold the
-// (y, z)-transformed grids: [NX][NY][NZ/2+1] complex, x in real space.
-bool xbin_plan(const BinParams &bp, int nslot, XbinGeo &xg);
+// (y, z)-transformed grids, x in real space, in the layout xg.tr names.
+bool xbin_plan(const BinParams &bp, int nslot, XbinGeo &xg, bool transposed);
+// The z-axis pass of the transposed fused layout: true when NZ is a power of two in [32, 2048].
+bool zr2c_supported(const BinParams &bp);
+// Real-to-complex DFT along z of every row of every painted grid (in: [NX][NY][row] floats, slot
+// stride in_slot floats), out of place into out (slot stride out_slot complex) as [NX][NZ/2+1][NY].
+void launch_zr2c(cudaStream_t s, const BinParams &bp, const BinTables &t, int nslot, const float *in,
+                 long long in_slot, int row, float2 *out, long long out_slot, long long *launches);
 void launch_xbin(cudaStream_t s, const BinParams &bp, const BinTables &t, const XbinGeo &xg, void *const slots[4],
                  const double *dcv, double *bins, long long *launches);
 // DC corrections: dcv[slot] = painted sum (minus NGRID for mean-subtracted field A slots)

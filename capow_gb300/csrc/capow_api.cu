@@ -238,9 +238,27 @@ extern "C" int capow_create(const capow_params *p, const capow_options *opt, cap
     CK(c, cudaMemcpyAsync(c->nmodes2d.data(), c->nmodes2d_d, sizeof(unsigned long long) * n2d,
                           cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
-  // FP32 with a power-of-two NX: cuFFT transforms every x-plane over (y, z), and k_xfft_bin does the
-  // x axis together with the binning (CAPOW_FFT_3D keeps the 3-D transform and k_bin)
-  c->fused = !f64 && o.fft_path != CAPOW_FFT_3D && c->bt.twx && xbin_plan(bp, c->nslot, c->xg);
+  // FP32 with a power-of-two NX: the (y, z) axes first, then k_xfft_bin does the x axis together
+  // with the binning (CAPOW_FFT_3D keeps the 3-D transform and k_bin). With a power-of-two NZ the z
+  // axis is k_zr2c, out of place and transposed to [NX][NZ/2+1][NY], and the y axis a contiguous
+  // batched cuFFT C2C; otherwise one cuFFT 2-D R2C over every x-plane, in place.
+  const bool want_fused = !f64 && o.fft_path != CAPOW_FFT_3D && c->bt.twx;
+  const bool tr = want_fused && c->bt.twz && zr2c_supported(bp);
+  c->fused = want_fused && xbin_plan(bp, c->nslot, c->xg, tr);
+  if (c->fused && tr) {
+    c->xtr = true;
+    c->tslot = (long long)p->NX * bp.nzc * p->NY;
+    c->tbuf = (float2 *)dalloc(c, sizeof(float2) * (size_t)c->tslot * c->nslot);
+    if (!c->tbuf) FAIL(c, CAPOW_ENOMEM, "transposed FFT buffer allocation failed");
+    int ny = p->NY;
+    const long long rows = (long long)c->nslot * p->NX * bp.nzc;
+    if (rows > 0x7fffffffLL) FAIL(c, CAPOW_ENOTSUP, "too many rows for one batched y-axis FFT");
+    CKFFT(c, cufftPlanMany(&c->yplan, 1, &ny, nullptr, 1, ny, nullptr, 1, ny, CUFFT_C2C, (int)rows));
+    c->yplan_ok = true;
+    CKFFT(c, cufftSetStream(c->yplan, c->stream));
+    c->plan_ok = true;  // the context is complete (c->plan is not used on this path)
+    return CAPOW_OK;
+  }
   if (c->fused) {
     int n2[2] = {p->NY, p->NZ};
     int in2[2] = {p->NY, 2 * bp.nzc}, on2[2] = {p->NY, bp.nzc};
@@ -495,13 +513,20 @@ int enqueue_power_kernels(capow_ctx *c) {
   launch_dc_prepare(c->stream, c->st, c->prec == CAPOW_FP32_DETERMINISTIC, c->nslot, c->fs.nfields,
                     c->bp.mean_sub_a, c->fixed_scale, c->dcv, &c->launches);
   if (c->fused) {
-    CKFFT(c, cufftExecR2C(c->plan, (cufftReal *)c->grid_base, (cufftComplex *)c->grid_base));
+    void *slots[4];
+    if (c->xtr) {
+      launch_zr2c(c->stream, c->bp, c->bt, c->nslot, (const float *)c->grid_base, (long long)c->grid_elems, c->g.row,
+                  c->tbuf, c->tslot, &c->launches);
+      CKFFT(c, cufftExecC2C(c->yplan, (cufftComplex *)c->tbuf, (cufftComplex *)c->tbuf, CUFFT_FORWARD));
+      for (int k = 0; k < 4; k++) slots[k] = k < c->nslot ? (void *)(c->tbuf + c->tslot * k) : nullptr;
+    } else {
+      CKFFT(c, cufftExecR2C(c->plan, (cufftReal *)c->grid_base, (cufftComplex *)c->grid_base));
+      GridPtrs gp = grid_ptrs(c);
+      for (int k = 0; k < 4; k++) slots[k] = gp.g[k];
+    }
     if (!c->quiet) CK(c, cudaEventRecord(c->ev[2], c->stream));
     const int nk = c->p.NK;
     CK(c, cudaMemsetAsync(c->bins, 0, sizeof(double) * NPROD * 5 * nk, c->stream));
-    void *slots[4];
-    GridPtrs gp = grid_ptrs(c);
-    for (int k = 0; k < 4; k++) slots[k] = gp.g[k];
     launch_xbin(c->stream, c->bp, c->bt, c->xg, slots, c->dcv, c->bins, &c->launches);
     CK(c, cudaGetLastError());
     if (!c->quiet) CK(c, cudaEventRecord(c->ev[3], c->stream));
@@ -688,7 +713,8 @@ extern "C" void capow_destroy(capow_ctx *c) {
   if (!c) return;
   cudaSetDevice(c->o.device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  if (c->plan_ok) cufftDestroy(c->plan);
+  if (c->plan_ok && !c->xtr) cufftDestroy(c->plan);
+  if (c->yplan_ok) cufftDestroy(c->yplan);
   if (c->adj_plans) {
     cufftDestroy(c->adj_fwd);
     cufftDestroy(c->adj_inv);

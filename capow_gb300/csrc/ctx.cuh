@@ -39,6 +39,13 @@ struct capow_ctx {
   std::vector<unsigned long long> nmodes, nmodes2d;
   cufftHandle plan;
   bool plan_ok;
+  // transposed fused path (power-of-two NZ): k_zr2c writes [NX][NZ/2+1][NY] complex per slot into
+  // tbuf, yplan is the batched C2C along y over it
+  bool xtr;
+  float2 *tbuf;
+  long long tslot;  // complex values per slot of tbuf
+  cufftHandle yplan;
+  bool yplan_ok;
   bool fused;           // FP32: 2-D (y, z) cuFFT + fused x-axis FFT and binning (k_xfft_bin)
   XbinGeo xg;
   // capow_backward (created on first use): full 3-D plans, bin coefficients, host-output staging

@@ -45,14 +45,18 @@ def test_reference_run_parity(gpu, precision, order, los, il, mom):
 
 
 FUSED = [(3, 3, 1, 1, 1, 64, 48, 40), (3, 0, 1, 0, 0, 128, 24, 30), (2, 3, 0, 2, 1, 64, 40, 48),
-         (1, 0, 0, 1, 0, 16, 20, 18), (3, 1, 1, 1, 1, 256, 16, 12), (2, 2, 1, 0, 1, 2048, 8, 6)]
+         (1, 0, 0, 1, 0, 16, 20, 18), (3, 1, 1, 1, 1, 256, 16, 12), (2, 2, 1, 0, 1, 2048, 8, 6),
+         # power-of-two NZ: the z axis by k_zr2c into the transposed layout, the y axis by cuFFT C2C
+         (3, 3, 1, 1, 1, 64, 48, 32), (2, 0, 1, 2, 0, 32, 20, 64), (1, 1, 0, 0, 1, 16, 12, 128),
+         (3, 2, 1, 1, 0, 128, 36, 32), (2, 3, 1, 0, 0, 64, 8, 2048)]
 
 
 @pytest.mark.parametrize("precision", ["fp32", "det"])
 @pytest.mark.parametrize("order,los,il,mom,odd,nx,ny,nz", FUSED)
 def test_fused_x_fft_bin_parity(gpu, precision, order, los, il, mom, odd, nx, ny, nz):
-    """Power-of-two NX: (y, z) cuFFT + the fused x-axis FFT and binning, against the oracle and
-    against the 3-D cuFFT + binning kernel path on the same paint."""
+    """Power-of-two NX: the (y, z) axes (cuFFT 2-D, or k_zr2c + cuFFT C2C along y for a power-of-two
+    NZ) + the fused x-axis FFT and binning, against the oracle and against the 3-D cuFFT + binning
+    kernel path on the same paint."""
     kw = dict(BASE, Odd_Multipoles=odd)
     po, pc = params_pair(NX=nx, NY=ny, NZ=nz, InterpOrder=order, LOS=los, DoInterlacing=il, Momentum=mom, **kw)
     parts = particles(po, 4000, seed=300 + nx + order * 7 + mom)
