@@ -1031,17 +1031,20 @@ __global__ void __launch_bounds__(ZR_THREADS) k_zr2c(ZrGeo zg, BinTables t, cons
       }
       __syncthreads();
     }
-    // real-input split and transposed store; the thread's row r is the same on every step
+    // real-input split and transposed store, X[k] and X[M-k] from the same pair: with
+    // A = Z[k] + conj Z[M-k], B = Z[k] - conj Z[M-k] and w^M = -1, X[k] = (A + (-i) w^k B) / 2 and
+    // X[M-k] = (conj A + (-i) conj(w^k B)) / 2. The thread's row r is the same on every step.
     const int r = threadIdx.x & (ZB - 1), y = y0 + r;
     if (y < zg.ny) {
       float2 *dst = out + sl * zg.out_slot + (long long)x * zg.nzc * zg.ny + y;
-      for (int k = threadIdx.x >> LZB; k <= M; k += blockDim.x >> LZB) {
+      for (int k = threadIdx.x >> LZB; k <= (M >> 1); k += blockDim.x >> LZB) {
         const float2 zk = sd[spos[k & (M - 1)] * P + r];
         const float2 zm = sd[spos[(M - k) & (M - 1)] * P + r];
-        const float2 A = make_float2(zk.x + zm.x, zk.y - zm.y);  // Z[k] + conj Z[M-k]
-        const float2 B = make_float2(zk.x - zm.x, zk.y + zm.y);  // Z[k] - conj Z[M-k]
+        const float2 A = make_float2(zk.x + zm.x, zk.y - zm.y);
+        const float2 B = make_float2(zk.x - zm.x, zk.y + zm.y);
         const float2 wB = cmulf(__ldg(t.tpz + k), B);
         dst[(long long)k * zg.ny] = make_float2(0.5f * (A.x + wB.y), 0.5f * (A.y - wB.x));
+        if (2 * k != M) dst[(long long)(M - k) * zg.ny] = make_float2(0.5f * (A.x - wB.y), -0.5f * (A.y + wB.x));
       }
     }
   }
