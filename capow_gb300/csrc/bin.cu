@@ -597,7 +597,7 @@ CAPOW_HD unsigned xbin_tw_entries(int log2n) {
 // runs over the banks.
 __device__ __forceinline__ int xt_index(int i) { return i + (i >> 6); }
 
-CAPOW_HD XbinSmem xbin_smem_layout(int log2n, int ncol, int np, int nl, int nk) {
+CAPOW_HD XbinSmem xbin_smem_layout(int log2n, int ncol, int np, int nl, int nk, int nbc) {
   const unsigned n = 1u << log2n;
   XbinSmem L;
   unsigned o = 0;
@@ -605,7 +605,7 @@ CAPOW_HD XbinSmem xbin_smem_layout(int log2n, int ncol, int np, int nl, int nk) 
   L.stw = o;  o = align16(o + 8u * xbin_tw_entries(log2n));
   L.sxt = o;  o = align16(o + 16u * (n + (n >> 6) + 1));
   L.sfx = o;  o = align16(o + 4u * n);
-  L.sb = o;   o = align16(o + 4u * np * nl * nk);
+  L.sb = o;   o = align16(o + 4u * np * nl * nk * nbc);
   L.sE = o;   o = align16(o + 8u * (nk + 3));
   L.sElo = o; o = align16(o + 4u * (nk + 3));
   L.sEhi = o; o = align16(o + 4u * (nk + 3));
@@ -694,7 +694,7 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
   extern __shared__ __align__(16) unsigned char smraw[];
   const int log2n = xg.log2n, n = 1 << log2n, ncol = xg.ncol, kc_n = xg.kc, nk = bp.nk;
   const int P = ncol + 1;  // row pitch of sd
-  const XbinSmem L = xbin_smem_layout(log2n, ncol, NP, NL, nk);
+  const XbinSmem L = xbin_smem_layout(log2n, ncol, NP, NL, nk, xg.nbc);
   float2 *sd = (float2 *)(smraw + L.sd);
   float2 *stw = (float2 *)(smraw + L.stw);
   float4 *sxt = (float4 *)(smraw + L.sxt);  // per kx: fx^2, deconvolution factor, interlace phase
@@ -703,7 +703,10 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
   double *sE = (double *)(smraw + L.sE);
   float *sElo = (float *)(smraw + L.sElo);
   float *sEhi = (float *)(smraw + L.sEhi);
-  for (int c = threadIdx.x; c < NP * NL * nk; c += blockDim.x) sb[c] = 0.0f;
+  const int nbins = NP * NL * nk;
+  for (int c = threadIdx.x; c < nbins * xg.nbc; c += blockDim.x) sb[c] = 0.0f;
+  // this warp's copy of the bins (flushes from different warps then rarely meet on one address)
+  float *sbw = sb + ((threadIdx.x >> 5) & (xg.nbc - 1)) * nbins;
   for (int c = threadIdx.x; c < nk + 3; c += blockDim.x) {
     sE[c] = t.E[c];
     sElo[c] = t.Elo[c];
@@ -872,7 +875,7 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
               for (int qq = 0; qq < NP; qq++)
 #pragma unroll
                 for (int l2 = 0; l2 < NL; l2++) {
-                  if (acc[qq][l2] != 0.0f && ((bp.pmask >> qq) & 1)) atomicAdd(&sb[(qq * NL + l2) * nk + cur], acc[qq][l2]);
+                  if (acc[qq][l2] != 0.0f && ((bp.pmask >> qq) & 1)) atomicAdd(&sbw[(qq * NL + l2) * nk + cur], acc[qq][l2]);
                   acc[qq][l2] = 0.0f;
                 }
             }
@@ -918,14 +921,15 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
         for (int qq = 0; qq < NP; qq++)
 #pragma unroll
           for (int l2 = 0; l2 < NL; l2++)
-            if (acc[qq][l2] != 0.0f && ((bp.pmask >> qq) & 1)) atomicAdd(&sb[(qq * NL + l2) * nk + cur], acc[qq][l2]);
+            if (acc[qq][l2] != 0.0f && ((bp.pmask >> qq) & 1)) atomicAdd(&sbw[(qq * NL + l2) * nk + cur], acc[qq][l2]);
       }
     }
   }
   __syncthreads();
-  // CTA bins -> global FP64 bins [product][5][nk]; stored multipole index -> l
-  for (int c = threadIdx.x; c < NP * NL * nk; c += blockDim.x) {
-    const float v = sb[c];
+  // CTA bins (the sum of the copies) -> global FP64 bins [product][5][nk]; stored multipole index -> l
+  for (int c = threadIdx.x; c < nbins; c += blockDim.x) {
+    float v = 0.0f;
+    for (int k = 0; k < xg.nbc; k++) v += sb[c + k * nbins];
     if (v == 0.0f) continue;
     const int b = c % nk, ql = c / nk, qq = ql / NL, li = ql - qq * NL;
     const int l = li == 0 ? 0 : (li == 1 ? 2 : (li == 2 ? 4 : (li == 3 ? 1 : 3)));
@@ -1117,14 +1121,16 @@ bool xbin_plan(const BinParams &bp, int nslot, XbinGeo &xg, bool transposed) {
   xg.nkb = (xg.n_inner + xg.kc - 1) / xg.kc;
   xg.nblocks = xg.n_outer * xg.nkb;
   const int np = bp.nfields == 1 ? 1 : 4, nl = bp.odd ? 5 : 3;
-  return xbin_smem_layout(xg.log2n, xg.ncol, np, nl, bp.nk).total <= 220 * 1024;
+  for (xg.nbc = 4; xg.nbc > 1; xg.nbc >>= 1)  // up to 4 bin copies as fit (8 measured slower: less L1)
+    if (xbin_smem_layout(xg.log2n, xg.ncol, np, nl, bp.nk, xg.nbc).total <= 220 * 1024) break;
+  return xbin_smem_layout(xg.log2n, xg.ncol, np, nl, bp.nk, xg.nbc).total <= 220 * 1024;
 }
 
 template <int NF, bool IL, bool ODD>
 static void launch_xbin_t(cudaStream_t s, const BinParams &bp, const BinTables &t, const XbinGeo &xg,
                           void *const slots[4], const double *dcv, double *bins) {
   constexpr int NP = NF == 1 ? 1 : 4, NL = ODD ? 5 : 3;
-  const size_t smem = xbin_smem_layout(xg.log2n, xg.ncol, NP, NL, bp.nk).total;
+  const size_t smem = xbin_smem_layout(xg.log2n, xg.ncol, NP, NL, bp.nk, xg.nbc).total;
   cudaFuncSetAttribute(k_xfft_bin<NF, IL, ODD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int per_sm = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_xfft_bin<NF, IL, ODD>, XBIN_THREADS, smem);

@@ -41,6 +41,7 @@ struct BinTables {
 struct XbinGeo {
   int log2n, ncol, log2ncol, kc, log2kc, nkb, nblocks;
   int tr, n_outer, n_inner;
+  int nbc;  // copies of the CTA's bins in shared memory (warps spread over them), a power of two
 };
 
 struct BinParams {
