@@ -970,7 +970,9 @@ __global__ void __launch_bounds__(ZR_THREADS) k_zr2c(ZrGeo zg, BinTables t, cons
   float2 *sd = (float2 *)smz;                                      // [M][ZB + 1]
   float2 *stw = (float2 *)(smz + align16(8u * (unsigned)M * P));  // radix-8 stage twiddle tables
   int *spos = (int *)(smz + align16(8u * (unsigned)M * P) + 8u * zr2c_tw_entries(log2m));  // row of Z[k]
+  float2 *stp = (float2 *)(smz + align16(8u * (unsigned)M * P) + 8u * zr2c_tw_entries(log2m) + align16(4u * M));
   for (int k = threadIdx.x; k < M; k += blockDim.x) spos[k] = xfft_pos(log2m, k);
+  for (int k = threadIdx.x; k <= M; k += blockDim.x) stp[k] = t.tpz[k];
   for (int l = log2m, off = 0; l >= 4; off += 8 << (l - 3), l -= 3) {
     const int step = M >> l;  // M / span
     for (int e = threadIdx.x; e < (8 << (l - 3)); e += blockDim.x)
@@ -1046,7 +1048,7 @@ __global__ void __launch_bounds__(ZR_THREADS) k_zr2c(ZrGeo zg, BinTables t, cons
         const float2 zm = sd[spos[(M - k) & (M - 1)] * P + r];
         const float2 A = make_float2(zk.x + zm.x, zk.y - zm.y);
         const float2 B = make_float2(zk.x - zm.x, zk.y + zm.y);
-        const float2 wB = cmulf(__ldg(t.tpz + k), B);
+        const float2 wB = cmulf(stp[k], B);
         dst[(long long)k * zg.ny] = make_float2(0.5f * (A.x + wB.y), 0.5f * (A.y - wB.x));
         if (2 * k != M) dst[(long long)(M - k) * zg.ny] = make_float2(0.5f * (A.x - wB.y), -0.5f * (A.y + wB.x));
       }
@@ -1062,7 +1064,7 @@ template <int ZB>
 static void launch_zr2c_t(cudaStream_t s, const ZrGeo &zg, const BinTables &t, int nslot, const float *in,
                           float2 *out) {
   const int M = 1 << zg.log2m;
-  const size_t smem = align16(8u * (unsigned)M * (ZB + 1)) + 8u * zr2c_tw_entries(zg.log2m) + 4u * M;
+  const size_t smem = align16(8u * (unsigned)M * (ZB + 1)) + 8u * zr2c_tw_entries(zg.log2m) + align16(4u * M) + 8u * (M + 1);
   cudaFuncSetAttribute(k_zr2c<ZB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int per_sm = 1, dev = 0, nsm = 152;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zr2c<ZB>, ZR_THREADS, smem);

@@ -941,7 +941,8 @@ __device__ void tile_paint_precise(const Geom &g, const FieldSpec &fs, const Til
 
 // FP32 tile kernel for particles away from every edge of the reference's rules (those are painted
 // by k_edge_fixup). One CTA per tile; shared memory holds the tile of every grid slot, both
-// stencils, unpadded [tx][ty][tz], as int32 fixed point with a per-tile power-of-two scale, so
+// stencils, [tx][ty][tz] with the padded pitches py = 3, px = 9 (mod 32) so that deposits at equal z
+// spread over the banks, as int32 fixed point with a per-tile power-of-two scale, so
 // every deposit is one native integer shared-memory atomic (the scale also keeps each deposit below
 // 2^22, where rint_small rounds it). Lane = record: each thread reads one record, derives its taps
 // once per stencil and adds the K^3 products, so a record is read once and nothing is staged. The
@@ -961,7 +962,9 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
   const int x0 = bx * tg.tx, y0 = by * tg.ty, z0 = bz * tg.tz;
   const int ex = min(tg.tx, g.nx - x0), ey = min(tg.ty, g.ny - y0), ez = min(tg.tz, g.nz - z0);
   int4 *sm4 = reinterpret_cast<int4 *>(smi);
-  for (int c = threadIdx.x; c < (NS * NF * tsz) >> 2; c += blockDim.x) sm4[c] = make_int4(0, 0, 0, 0);
+  const int slotw = tg.slot;  // words per padded slot
+  for (int c = threadIdx.x; c < (NS * NF * slotw) >> 2; c += blockDim.x) sm4[c] = make_int4(0, 0, 0, 0);
+  for (int c = ((NS * NF * slotw) & ~3) + threadIdx.x; c < NS * NF * slotw; c += blockDim.x) smi[c] = 0;
   __syncthreads();
   unsigned long long rb, re;
   if (cap) {  // bucket mode: the tile's own bucket
@@ -1037,10 +1040,10 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
       axis32k<K>(sz, 1, g.nz, g.los, az);
       float wx[3], wy[3], wz[3];
       int ox[3], oy[3], oz[3];
-      stage_axis32(ax, x0, ex, pyz, wx, ox);
-      stage_axis32(ay, y0, ey, tg.tz, wy, oy);
+      stage_axis32(ax, x0, ex, tg.px, wx, ox);
+      stage_axis32(ay, y0, ey, tg.py, wy, oy);
       stage_axis32(az, z0, ez, 1, wz, oz);
-      int *sA = smi + (s * NF) * tsz;
+      int *sA = smi + (s * NF) * slotw;
 #pragma unroll
       for (int a = 0; a < K; a++)
 #pragma unroll
@@ -1054,7 +1057,7 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
 #pragma unroll
             for (int c = 0; c < K; c++) {
               atomicAdd(sA + oxy + oz[c], rint_small(pa, wz[c]));
-              if (NF == 2) atomicAdd(sA + tsz + oxy + oz[c], rint_small(pb, wz[c]));
+              if (NF == 2) atomicAdd(sA + slotw + oxy + oz[c], rint_small(pb, wz[c]));
             }
           }
         }
@@ -1065,14 +1068,15 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
   const int npair = tsz >> 1;
   for (int slot = 0; slot < NS * NF; slot++) {
     float *gp = (float *)grids.g[slot];
-    const int *sl = smi + slot * tsz;
+    const int *sl = smi + slot * slotw;
     const float inv = ldexpf(1.0f, -((slot % NF) == 0 ? SA : SB));
     float dsum = 0.0f;
     for (int q = threadIdx.x; q < npair; q += blockDim.x) {
       const int c = q << 1;
       const int rz = c & (tg.tz - 1), ly = (c >> tg.lz) & (tg.ty - 1), lx = c >> (tg.lz + tg.ly);
       if (lx >= ex || ly >= ey || rz >= ez) continue;
-      const int2 iv = *reinterpret_cast<const int2 *>(sl + c);
+      const int cp = lx * tg.px + ly * tg.py + rz;
+      const int2 iv = make_int2(sl[cp], sl[cp + 1]);
       const float2 v = make_float2((float)iv.x * inv, (float)iv.y * inv);
       float *dst = gp + (long long)(x0 + lx) * g.slice + (long long)(y0 + ly) * g.row + z0 + rz;
       if (rz + 1 < ez) {
@@ -1268,7 +1272,7 @@ size_t tile_smem_bytes(const TileGeo &tg, int nslots, int deterministic) {
   return tile + stage;
 }
 
-size_t rec_smem_bytes(const TileGeo &tg, int nslots) { return (size_t)nslots * tg.tx * tg.ty * tg.tz * 4; }
+size_t rec_smem_bytes(const TileGeo &tg, int nslots) { return (size_t)nslots * tg.slot * 4; }
 
 double tile_dup_estimate(const Geom &g, const TileGeo &tg) {
   // a footprint spans 4 (TSC, CIC) or 2 (NN) cells plus the margin; it crosses into the next tile
