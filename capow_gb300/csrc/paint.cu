@@ -1064,8 +1064,11 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
     }
   }
   __syncthreads();
-  // write every slot: pairs of cells along z as float2 (8-byte aligned global rows)
+  // write every slot: pairs of cells along z as float2 (8-byte aligned global rows); the slots' DC
+  // sums go to one block reduction at the end (FP32 per thread and warp, FP64 across warps)
   const int npair = tsz >> 1;
+  float dsums[NS * NF];
+#pragma unroll
   for (int slot = 0; slot < NS * NF; slot++) {
     float *gp = (float *)grids.g[slot];
     const int *sl = smi + slot * slotw;
@@ -1087,10 +1090,12 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
         dst[0] = v.x;
       }
     }
-    const double vals[1] = {(double)dsum};
-    double *const dst1[1] = {&st->dc[slot]};
-    block_add<1>(vals, dst1);
+    dsums[slot] = dsum;
   }
+  double *dsts[NS * NF];
+#pragma unroll
+  for (int slot = 0; slot < NS * NF; slot++) dsts[slot] = &st->dc[slot];
+  block_add_f<NS * NF>(dsums, dsts);
 }
 
 // Bucket mode: records that found their tile's bucket full, deposited after the tiles were written
