@@ -243,21 +243,29 @@ extern "C" int capow_create(const capow_params *p, const capow_options *opt, cap
   // axis is k_zr2c, out of place and transposed to [NX][NZ/2+1][NY], and the y axis a contiguous
   // batched cuFFT C2C; otherwise one cuFFT 2-D R2C over every x-plane, in place.
   const bool want_fused = !f64 && o.fft_path != CAPOW_FFT_3D && c->bt.twx;
-  const bool tr = want_fused && c->bt.twz && zr2c_supported(bp);
+  const long long yrows = (long long)c->nslot * p->NX * bp.nzc;
+  const bool tr = want_fused && c->bt.twz && zr2c_supported(bp) && yrows <= 0x7fffffffLL;
   c->fused = want_fused && xbin_plan(bp, c->nslot, c->xg, tr);
   if (c->fused && tr) {
-    c->xtr = true;
+    // the transposed layout needs a second grid-sized buffer and a cuFFT workspace; when the device
+    // has no room for them the context keeps the in-place 2-D cuFFT layout instead
     c->tslot = (long long)p->NX * bp.nzc * p->NY;
-    c->tbuf = (float2 *)dalloc(c, sizeof(float2) * (size_t)c->tslot * c->nslot);
-    if (!c->tbuf) FAIL(c, CAPOW_ENOMEM, "transposed FFT buffer allocation failed");
+    void *tb = nullptr;
     int ny = p->NY;
-    const long long rows = (long long)c->nslot * p->NX * bp.nzc;
-    if (rows > 0x7fffffffLL) FAIL(c, CAPOW_ENOTSUP, "too many rows for one batched y-axis FFT");
-    CKFFT(c, cufftPlanMany(&c->yplan, 1, &ny, nullptr, 1, ny, nullptr, 1, ny, CUFFT_C2C, (int)rows));
-    c->yplan_ok = true;
-    CKFFT(c, cufftSetStream(c->yplan, c->stream));
-    c->plan_ok = true;  // the context is complete (c->plan is not used on this path)
-    return CAPOW_OK;
+    if (cudaMalloc(&tb, sizeof(float2) * (size_t)c->tslot * c->nslot) == cudaSuccess) {
+      if (cufftPlanMany(&c->yplan, 1, &ny, nullptr, 1, ny, nullptr, 1, ny, CUFFT_C2C, (int)yrows) == CUFFT_SUCCESS) {
+        c->allocs.push_back(tb);
+        c->tbuf = (float2 *)tb;
+        c->xtr = true;
+        c->yplan_ok = true;
+        CKFFT(c, cufftSetStream(c->yplan, c->stream));
+        c->plan_ok = true;  // the context is complete (c->plan is not used on this path)
+        return CAPOW_OK;
+      }
+      cudaFree(tb);
+    }
+    (void)cudaGetLastError();  // clear the failed allocation
+    c->fused = xbin_plan(bp, c->nslot, c->xg, false);
   }
   if (c->fused) {
     int n2[2] = {p->NY, p->NZ};

@@ -845,16 +845,11 @@ __device__ __forceinline__ int tile_scale_exp(float sum_abs) {
   return S > 100 ? 100 : (S < -100 ? -100 : S);
 }
 
-// Scale exponent S of a tile that also keeps every single deposit below 2^22 in magnitude
-// (|w v^e| 2^S < 2^22, tap weights <= 1), so that rint_small can round it exactly.
-__device__ __forceinline__ int tile_scale_exp2(float sum_abs, float max_abs) {
-  int S = tile_scale_exp(sum_abs);
+// Largest scale exponent that keeps every single deposit of a tile below 2^22 in magnitude
+// (|w v^e| 2^S < 2^22, tap weights <= 1), where rint_small rounds exactly.
+__device__ __forceinline__ int tile_scale_max(float max_abs) {
   const float mb = max_abs * 1.001f;
-  if (mb > 0.0f && isfinite(mb)) {
-    const int Sm = 21 - ilogbf(mb);
-    if (Sm < S) S = Sm;
-  }
-  return S < -100 ? -100 : S;
+  return (mb > 0.0f && isfinite(mb)) ? 21 - ilogbf(mb) : 100;
 }
 
 // Round-to-nearest-even of a * b as an int32, for |a * b| < 2^22: the fused multiply-add rounds the
@@ -939,12 +934,66 @@ __device__ void tile_paint_precise(const Geom &g, const FieldSpec &fs, const Til
   }
 }
 
+// The deposits of a tile's records (lane = record; both stencils) into the int32 shared tile.
+// FASTR: rounded by rint_small (every deposit below 2^22); otherwise by conversion.
+template <int K, int NF, bool IL, bool FASTR>
+__device__ __forceinline__ void tile_rec_deposit(const Geom &g, const FieldSpec &fs, const TileGeo &tg,
+                                                 const float4 *recs, const float *recw, unsigned long long rb,
+                                                 unsigned long long re, float scA, float scB, int x0, int y0,
+                                                 int z0, int ex, int ey, int ez, int *smi) {
+  constexpr int NS = IL ? 2 : 1;
+  const int slotw = tg.slot;
+  for (unsigned long long r = rb + threadIdx.x; r < re; r += blockDim.x) {
+    const float4 rec = recs[r];
+    const float w = recw ? recw[r] : 1.0f;
+    float va = w, vb = w;
+    for (int e = 0; e < fs.ea; e++) va *= rec.w;
+    for (int e = 0; e < fs.eb; e++) vb *= rec.w;
+    va *= scA;
+    vb *= scB;
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+      const float sx = s ? __fadd_rn(rec.x, 0.5f) : rec.x, sy = s ? __fadd_rn(rec.y, 0.5f) : rec.y,
+                  sz = s ? __fadd_rn(rec.z, 0.5f) : rec.z;
+      if (!accept32(g, sx, sy, sz)) continue;
+      AxisTapsF ax, ay, az;
+      axis32k<K>(sx, 0, g.nx, g.los, ax);
+      axis32k<K>(sy, 1, g.ny, g.los, ay);
+      axis32k<K>(sz, 1, g.nz, g.los, az);
+      float wx[3], wy[3], wz[3];
+      int ox[3], oy[3], oz[3];
+      stage_axis32(ax, x0, ex, tg.px, wx, ox);
+      stage_axis32(ay, y0, ey, tg.py, wy, oy);
+      stage_axis32(az, z0, ez, 1, wz, oz);
+      int *sA = smi + (s * NF) * slotw;
+#pragma unroll
+      for (int a = 0; a < K; a++)
+#pragma unroll
+        for (int b2 = 0; b2 < K; b2++) {
+          const float wxy = wx[a] * wy[b2];
+          const float pa = va * wxy, pb = vb * wxy;
+          const int oxy = ox[a] + oy[b2];
+          // one test per (x, y) tap pair: an x or y tap outside the tile has weight 0. A z tap outside
+          // it (the z edge of a tile is 32 cells: rare) has weight 0 and offset 0 and adds 0 there.
+          if (wxy != 0.0f) {
+#pragma unroll
+            for (int c = 0; c < K; c++) {
+              atomicAdd(sA + oxy + oz[c], FASTR ? rint_small(pa, wz[c]) : __float2int_rn(pa * wz[c]));
+              if (NF == 2)
+                atomicAdd(sA + slotw + oxy + oz[c], FASTR ? rint_small(pb, wz[c]) : __float2int_rn(pb * wz[c]));
+            }
+          }
+        }
+    }
+  }
+}
+
 // FP32 tile kernel for particles away from every edge of the reference's rules (those are painted
 // by k_edge_fixup). One CTA per tile; shared memory holds the tile of every grid slot, both
 // stencils, [tx][ty][tz] with the padded pitches py = 3, px = 9 (mod 32) so that deposits at equal z
 // spread over the banks, as int32 fixed point with a per-tile power-of-two scale, so
-// every deposit is one native integer shared-memory atomic (the scale also keeps each deposit below
-// 2^22, where rint_small rounds it). Lane = record: each thread reads one record, derives its taps
+// every deposit is one native integer shared-memory atomic (an ordinary tile's scale also keeps each
+// deposit below 2^22, where rint_small rounds it). Lane = record: each thread reads one record, derives its taps
 // once per stencil and adds the K^3 products, so a record is read once and nothing is staged. The
 // cells are converted back to FP32 when the tile is written. (NGRID of these particles is counted
 // by k_bucket or k_count.)
@@ -1013,7 +1062,14 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
     xa = fmaxf(xa, red_abs[2][k]);
     xb = fmaxf(xb, red_abs[3][k]);
   }
-  const int SA = tile_scale_exp2(ta, xa), SB = tile_scale_exp2(tb, xb);
+  // The tile's scale is set by its sum (tile_scale_exp). When keeping every deposit below 2^22 costs
+  // it at most 2 bits (an ordinary tile: hundreds of comparable records), the tile takes that scale
+  // and the fast rounding; otherwise (few records, or one dominant record) it keeps the sum's scale
+  // and rounds by conversion.
+  const int SAs = tile_scale_exp(ta), SBs = tile_scale_exp(tb);
+  const int SAf = min(SAs, tile_scale_max(xa)), SBf = min(SBs, tile_scale_max(xb));
+  const bool fast = (SAs - SAf <= 2) && (NF == 1 || SBs - SBf <= 2);
+  const int SA = fast ? SAf : SAs, SB = fast ? SBf : SBs;
   if (re - rb > TILE_PRECISE_RECORDS) {  // a dense tile (uniform over the CTA)
     const int words = NS * NF * tsz;  // the int32 tile area, reused as int64 cells
     tile_paint_precise<K, NF, IL>(g, fs, tg, recs, recw, rb, re, ta, tb, x0, y0, z0, ex, ey, ez, pyz, tsz,
@@ -1021,48 +1077,8 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
     return;
   }
   const float scA = ldexpf(1.0f, SA), scB = ldexpf(1.0f, SB);
-  for (unsigned long long r = rb + threadIdx.x; r < re; r += blockDim.x) {
-    const float4 rec = recs[r];
-    const float w = recw ? recw[r] : 1.0f;
-    float va = w, vb = w;
-    for (int e = 0; e < fs.ea; e++) va *= rec.w;
-    for (int e = 0; e < fs.eb; e++) vb *= rec.w;
-    va *= scA;
-    vb *= scB;
-#pragma unroll
-    for (int s = 0; s < NS; s++) {
-      const float sx = s ? __fadd_rn(rec.x, 0.5f) : rec.x, sy = s ? __fadd_rn(rec.y, 0.5f) : rec.y,
-                  sz = s ? __fadd_rn(rec.z, 0.5f) : rec.z;
-      if (!accept32(g, sx, sy, sz)) continue;
-      AxisTapsF ax, ay, az;
-      axis32k<K>(sx, 0, g.nx, g.los, ax);
-      axis32k<K>(sy, 1, g.ny, g.los, ay);
-      axis32k<K>(sz, 1, g.nz, g.los, az);
-      float wx[3], wy[3], wz[3];
-      int ox[3], oy[3], oz[3];
-      stage_axis32(ax, x0, ex, tg.px, wx, ox);
-      stage_axis32(ay, y0, ey, tg.py, wy, oy);
-      stage_axis32(az, z0, ez, 1, wz, oz);
-      int *sA = smi + (s * NF) * slotw;
-#pragma unroll
-      for (int a = 0; a < K; a++)
-#pragma unroll
-        for (int b2 = 0; b2 < K; b2++) {
-          const float wxy = wx[a] * wy[b2];
-          const float pa = va * wxy, pb = vb * wxy;
-          const int oxy = ox[a] + oy[b2];
-          // one test per (x, y) tap pair: an x or y tap outside the tile has weight 0. A z tap outside
-          // it (the z edge of a tile is 32 cells: rare) has weight 0 and offset 0 and adds 0 there.
-          if (wxy != 0.0f) {
-#pragma unroll
-            for (int c = 0; c < K; c++) {
-              atomicAdd(sA + oxy + oz[c], rint_small(pa, wz[c]));
-              if (NF == 2) atomicAdd(sA + slotw + oxy + oz[c], rint_small(pb, wz[c]));
-            }
-          }
-        }
-    }
-  }
+  if (fast) tile_rec_deposit<K, NF, IL, true>(g, fs, tg, recs, recw, rb, re, scA, scB, x0, y0, z0, ex, ey, ez, smi);
+  else tile_rec_deposit<K, NF, IL, false>(g, fs, tg, recs, recw, rb, re, scA, scB, x0, y0, z0, ex, ey, ez, smi);
   __syncthreads();
   // write every slot: pairs of cells along z as float2 (8-byte aligned global rows); the slots' DC
   // sums go to one block reduction at the end (FP32 per thread and warp, FP64 across warps)

@@ -212,3 +212,67 @@ def test_tile_kernel_timing(gpu):
         ps.paint(x, y, z, v)
         with pytest.raises(cg.CapowError):
             ps.tile_kernel_ms()
+
+
+def test_fp32_tile_scale_heavy_weights(gpu):
+    """Weights over six decades plus a few dominant particles: FP32 tiles whose scale is set by the
+    largest deposit (each deposit below 2^22, rounded by the FFMA magic-number add) as well as by the
+    tile sum. Grids and spectra against the FP64 path (weights are a library extension; the FP64
+    path is pinned to the oracle elsewhere)."""
+    p = cg.Params(NX=64, NY=64, NZ=64, NK=20, Maxk=0.3, XMIN=0.0, XMAX=1000.0, YMIN=0.0, YMAX=1000.0,
+                  ZMIN=0.0, ZMAX=1000.0, InterpOrder=3, DoInterlacing=1, LOS=3, Momentum=0)
+    rng = np.random.default_rng(17)
+    n = 200000
+    x, y, z = (rng.uniform(20.0, 980.0, n) for _ in range(3))
+    v = rng.normal(0.0, 300.0, n)
+    w = 10.0 ** rng.uniform(-3.0, 3.0, n)
+    w[:5] = 1.0e6
+    out = {}
+    for prec in ("fp64", "fp32"):
+        with cg.PowerSpectrum(p, precision=prec, spectra=["dd", "dp", "pp"]) as ps:
+            ps.paint(x, y, z, v, w)
+            g = [ps.grid(k) for k in range(4)]
+            out[prec] = (g, ps.power())
+    for k in range(4):
+        grid_close(out["fp32"][0][k], out["fp64"][0][k], p, "fp32", label=f"slot {k}")
+    r32, r64 = out["fp32"][1], out["fp64"][1]
+    for q, name in ((0, "dd"), (2, "pp")):
+        assert_spectrum(r32[q], r64[q], np.abs(np.asarray(r64[q]["Pk0"])), "fp32", odd=False, label=name)
+
+
+def test_transposed_path_falls_back_when_memory_is_short(gpu):
+    """A power-of-two NZ takes the transposed (y,z) pass, which needs a second grid-sized buffer.
+    With the device nearly full (a bounded filler allocation leaves room for the grids but not for
+    that buffer), capow_create keeps the in-place 2-D cuFFT layout: one library kernel fewer per
+    capow_power (no k_zr2c), same spectra."""
+    torch = pytest.importorskip("torch")
+    p = cg.Params(NX=256, NY=256, NZ=256, NK=40, Maxk=0.6, XMIN=0.0, XMAX=1000.0, YMIN=0.0, YMAX=1000.0,
+                  ZMIN=0.0, ZMAX=1000.0, InterpOrder=3, DoInterlacing=1, LOS=3, Momentum=0)
+    rng = np.random.default_rng(23)
+    n = 300000
+    x, y, z = (rng.uniform(1.0, 999.0, n) for _ in range(3))
+    v = rng.normal(0.0, 100.0, n)
+
+    def run():
+        with cg.PowerSpectrum(p, precision="fp32", spectra=["dd", "dp", "pp"]) as ps:
+            ps.paint(x, y, z, v)
+            l0 = ps.kernel_launches()
+            r = ps.power()
+            return r, ps.kernel_launches() - l0
+
+    r_normal, k_normal = run()
+    grids = 4 * 256 * 256 * 258 * 4  # the painted slots; the transposed buffer is as large
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    free, _ = torch.cuda.mem_get_info()
+    # leave room for the grids and 0.9 of them (plans, tables, records), not for a second copy
+    filler = torch.empty(max(0, free - int(1.9 * grids)), dtype=torch.uint8, device=gpu)
+    try:
+        r_short, k_short = run()
+    finally:
+        del filler
+        torch.cuda.empty_cache()
+    assert k_short == k_normal - 1, (k_short, k_normal)
+    pdd, ppp = (np.abs(np.asarray(r_normal[q]["Pk0"])) for q in (0, 2))
+    for q, norm0 in ((0, pdd), (1, np.sqrt(pdd * ppp)), (2, ppp)):
+        assert_spectrum(r_short[q], r_normal[q], norm0, "fp32", odd=False, label=f"spectrum {q}")
