@@ -488,9 +488,10 @@ __global__ void __launch_bounds__(256) k_scatter(Geom g, FieldSpec fs, TileGeo t
 
 // Bucket mode, passes 1-3 in one: the statistics of k_count and the records of k_scatter, each
 // written into its tile's fixed-capacity bucket (slot from the run-aggregated tile counter); a
-// record that finds its bucket full goes to the overflow list with its tile.
+// record that finds its bucket full goes to the overflow list with its tile. (Four CTAs per SM:
+// 64 registers, which the overlapped reservations below need without spilling.)
 template <typename T>
-__global__ void __launch_bounds__(256) k_bucket(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in, long long n,
+__global__ void __launch_bounds__(256, 4) k_bucket(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in, long long n,
                                                 unsigned *counts, float4 *recs, float *recw, unsigned cap,
                                                 unsigned *edge_list, unsigned *edge_count, float4 *ovf_recs,
                                                 float *ovf_w, unsigned *ovf_tile, unsigned *ovf_count,
@@ -543,31 +544,66 @@ __global__ void __launch_bounds__(256) k_bucket(Geom g, FieldSpec fs, TileGeo tg
     }
     const int na = __reduce_max_sync(FULL_MASK, has ? TX.n : 0), nb = __reduce_max_sync(FULL_MASK, has ? TY.n : 0),
               nc = __reduce_max_sync(FULL_MASK, has ? TZ.n : 0);
-    // runtime loops over the warp's footprint tiles (warp-uniform bounds): one copy of the body
-#pragma unroll 1
-    for (int a = 0; a < na; a++)
-#pragma unroll 1
-      for (int b = 0; b < nb; b++)
-#pragma unroll 1
-        for (int c = 0; c < nc; c++) {
-          const int key = tile_key(tg, has, TX, TY, TZ, a, b, c);
-          const unsigned slot = warp_run_add(counts, key, true);
-          if (key < 0) continue;
-          if (slot < cap) {
-            const unsigned long long r = (unsigned long long)key * cap + slot;
-            recs[r] = rec;
-            if (recw) recw[r] = w;
-          } else {
-            const unsigned o = atomicAdd(ovf_count, 1u);
-            if (o < ovf_cap) {
-              ovf_recs[o] = rec;
-              if (ovf_w) ovf_w[o] = w;
-              ovf_tile[o] = (unsigned)key;
-            } else {
-              ovf_full = 1;
-            }
-          }
+    auto put = [&](int key, unsigned slot) {
+      if (key < 0) return;
+      if (slot < cap) {
+        const unsigned long long r = (unsigned long long)key * cap + slot;
+        recs[r] = rec;
+        if (recw) recw[r] = w;
+      } else {
+        const unsigned o = atomicAdd(ovf_count, 1u);
+        if (o < ovf_cap) {
+          ovf_recs[o] = rec;
+          if (ovf_w) ovf_w[o] = w;
+          ovf_tile[o] = (unsigned)key;
+        } else {
+          ovf_full = 1;
         }
+      }
+    };
+    if (na <= 2 && nb <= 2 && nc <= 2) {
+      // every (a, b, c) reservation of the warp first (their atomics in flight together), then the
+      // records: lane slot = the run head's returned base + the lane's place in its run
+      const int lane = threadIdx.x & 31;
+      int keys[8], hd[8];
+      unsigned base[8];
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const int a = t >> 2, b = (t >> 1) & 1, c = t & 1;
+        keys[t] = -1;
+        hd[t] = 0;
+        base[t] = 0;
+        if (a < na && b < nb && c < nc) {  // warp-uniform
+          const int key = tile_key(tg, has, TX, TY, TZ, a, b, c);
+          const int prev = __shfl_up_sync(FULL_MASK, key, 1);
+          const unsigned heads = __ballot_sync(FULL_MASK, lane == 0 || key != prev);
+          const unsigned after = heads & ~((2u << lane) - 1u);
+          const int head = 31 - __clz(heads & ((2u << lane) - 1u));
+          if (head == lane && key >= 0) base[t] = atomicAdd(counts + key, (unsigned)((after ? __ffs(after) - 1 : 32) - lane));
+          keys[t] = key;
+          hd[t] = head;
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const int a = t >> 2, b = (t >> 1) & 1, c = t & 1;
+        if (a < na && b < nb && c < nc) {
+          const unsigned b0 = __shfl_sync(FULL_MASK, base[t], hd[t]);
+          put(keys[t], b0 + (unsigned)(lane - hd[t]));
+        }
+      }
+    } else {
+      // runtime loops over the warp's footprint tiles (warp-uniform bounds): one copy of the body
+#pragma unroll 1
+      for (int a = 0; a < na; a++)
+#pragma unroll 1
+        for (int b = 0; b < nb; b++)
+#pragma unroll 1
+          for (int c = 0; c < nc; c++) {
+            const int key = tile_key(tg, has, TX, TY, TZ, a, b, c);
+            put(key, warp_run_add(counts, key, true));
+          }
+    }
   }
   const float vals[10] = {f_read, f_out, f_nsq, f_v[0], f_v[1], f_v[2], f_v[3], f_abs[0], f_abs[1], f_grid};
   double *const dst[10] = {&st->nread, &st->nout, &st->nsq, &st->vr[0], &st->vr[1], &st->vr[2], &st->vr[3],
