@@ -67,6 +67,11 @@ struct capow_ctx {
   std::vector<void *> allocs;
   cudaEvent_t ev[4];
   cudaEvent_t ev_tile[2];  // around the FP32 tile-deposit kernel of the last paint
+  // host catalogues of FP32 bucket-mode paints are copied in CAPOW_CHUNKS chunks on copy_stream, and
+  // the bucket pass of each chunk starts when its copy lands (chunk_ev); nchunk > 1 for that paint
+  cudaStream_t copy_stream;
+  cudaEvent_t chunk_ev[4], copy_start;
+  int nchunk;
   bool tile_timed;         // the last FP32 paint recorded ev_tile
   long long launches;
   char err[512];

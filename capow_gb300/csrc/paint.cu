@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(256) k_scatter(Geom g, FieldSpec fs, TileGeo t
 // 64 registers, which the overlapped reservations below need without spilling.)
 template <typename T>
 __global__ void __launch_bounds__(256, 4) k_bucket(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in, long long n,
-                                                unsigned *counts, float4 *recs, float *recw, unsigned cap,
+                                                   long long ibase, unsigned *counts, float4 *recs, float *recw, unsigned cap,
                                                 unsigned *edge_list, unsigned *edge_count, float4 *ovf_recs,
                                                 float *ovf_w, unsigned *ovf_tile, unsigned *ovf_count,
                                                 unsigned long long ovf_cap, DevStats *st) {
@@ -529,10 +529,10 @@ __global__ void __launch_bounds__(256, 4) k_bucket(Geom g, FieldSpec fs, TileGeo
           f_out += 1.0f;  // clearly outside the box (src/read_data.c:81-88)
           if (g.los == 0) {
             fatal = 1;
-            atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)i);
+            atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)(ibase + i));
           }
         } else if (is_edge(g, p.sx, p.sy, p.sz)) {
-          edge_list[atomicAdd(edge_count, 1u)] = (unsigned)i;  // painted and counted by k_edge_fixup
+          edge_list[atomicAdd(edge_count, 1u)] = (unsigned)(ibase + i);  // painted and counted by k_edge_fixup
         } else {
           has = true;
           w = p.w;
@@ -1373,9 +1373,18 @@ static void run_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, cons
   if (split) cudaMemsetAsync(b.edge_count, 0, sizeof(unsigned), s);
   if (!det && b.bucket_cap) {  // bucket mode: one pass to the tiles' buckets, overflow after the tiles
     cudaMemsetAsync(b.ovf_count, 0, sizeof(unsigned), s);
-    k_bucket<T><<<nb, th, 0, s>>>(g, fs, tg, in, n, b.counts, b.recs, in.w ? b.recw : nullptr, b.bucket_cap,
-                                  b.edge_list, b.edge_count, b.ovf_recs, in.w ? b.ovf_w : nullptr, b.ovf_tile,
-                                  b.ovf_count, b.ovf_cap, st);
+    const int nch = b.nchunk > 1 ? b.nchunk : 1;
+    for (int k = 0; k < nch; k++) {  // one launch per copied chunk of a host catalogue (else one)
+      const long long c0 = n * k / nch, c1 = n * (k + 1) / nch;
+      if (nch > 1) cudaStreamWaitEvent(s, b.chunk_ev[k], 0);
+      PIn<T> ink{in.x + c0, in.y + c0, in.z + c0, in.v ? in.v + c0 : nullptr, in.w ? in.w + c0 : nullptr};
+      const long long nbk = (c1 - c0 + th - 1) / th;
+      const int nbc = (int)(nbk < 1 ? 1 : (nbk > 152 * 8 ? 152 * 8 : nbk));
+      k_bucket<T><<<nbc, th, 0, s>>>(g, fs, tg, ink, c1 - c0, c0, b.counts, b.recs, in.w ? b.recw : nullptr,
+                                     b.bucket_cap, b.edge_list, b.edge_count, b.ovf_recs, in.w ? b.ovf_w : nullptr,
+                                     b.ovf_tile, b.ovf_count, b.ovf_cap, st);
+    }
+    *launches += nch - 1;
     const bool wts = in.w != nullptr;
     if (b.tile_ev0) cudaEventRecord(b.tile_ev0, s);
     if (g.order == 3) launch_rec_k<3>(s, g, fs, tg, b, wts, grids, st);

@@ -62,6 +62,10 @@ struct PaintBufs {
   unsigned long long ovf_cap;
   // when set, recorded on the stream just before and after the tile-deposit kernel
   cudaEvent_t tile_ev0, tile_ev1;
+  // bucket mode with host input copied in chunks: the bucket pass runs per chunk k (particles
+  // [k n / nchunk, (k + 1) n / nchunk)), each launch after chunk_ev[k]
+  int nchunk;
+  const cudaEvent_t *chunk_ev;
 };
 
 // host launchers (paint.cu)

@@ -276,3 +276,50 @@ def test_transposed_path_falls_back_when_memory_is_short(gpu):
     pdd, ppp = (np.abs(np.asarray(r_normal[q]["Pk0"])) for q in (0, 2))
     for q, norm0 in ((0, pdd), (1, np.sqrt(pdd * ppp)), (2, ppp)):
         assert_spectrum(r_short[q], r_normal[q], norm0, "fp32", odd=False, label=f"spectrum {q}")
+
+
+def test_host_catalogue_in_chunks_matches_device_input(gpu):
+    """A host catalogue of >= 4M particles is copied in chunks that the bucket pass consumes as they
+    land. Against the same catalogue passed on the device (one bucket launch): equal grids, counters
+    and spectra, with edge particles in every chunk (their indices go through the chunk's base) and,
+    for LOS = 0, the first out-of-box particle planted in the last chunk reported by its index."""
+    torch = pytest.importorskip("torch")
+    p = cg.Params(NX=64, NY=64, NZ=64, NK=20, Maxk=0.3, XMIN=0.0, XMAX=1000.0, YMIN=0.0, YMAX=1000.0,
+                  ZMIN=0.0, ZMAX=1000.0, InterpOrder=3, DoInterlacing=1, LOS=3, Momentum=1)
+    rng = np.random.default_rng(31)
+    n = 5_000_000
+    d = 1000.0 / 64
+    x, y, z = (rng.uniform(2.0, 998.0, n).astype(np.float32) for _ in range(3))
+    v = rng.normal(0.0, 100.0, n).astype(np.float32)
+    picks = rng.choice(n, 400, replace=False)  # on cell edges (the exact-rules path), all chunks
+    x[picks] = (np.floor(x[picks] / d) * d).astype(np.float32)
+    out = {}
+    for where in ("host", "device"):
+        arrs = [x, y, z, v] if where == "host" else [torch.from_numpy(a).to(gpu) for a in (x, y, z, v)]
+        with cg.PowerSpectrum(p, precision="fp32", spectra=["dd", "dp", "pp"]) as ps:
+            ps.paint(*arrs)
+            g = [ps.grid(k) for k in range(4)]
+            st = ps.stats()
+            out[where] = (g, st, ps.power())
+    gh, sh, rh = out["host"]
+    gd, sd, rd = out["device"]
+    for k in range(4):
+        scale = np.abs(gd[k]).max()
+        assert np.abs(gh[k] - gd[k]).max() <= 1e-6 * scale, k
+    for key in ("nread", "nout", "ngrid", "nsq"):
+        assert sh[key] == sd[key], key
+    pdd, ppp = (np.abs(np.asarray(rd[q]["Pk0"])) for q in (0, 2))
+    for q, norm0 in ((0, pdd), (1, np.sqrt(pdd * ppp)), (2, ppp)):
+        assert_spectrum(rh[q], rd[q], norm0, "fp32", odd=False, label=f"spectrum {q}")
+    # LOS = 0: a particle outside the box in the last chunk is the reference's fatal error
+    p0 = cg.Params(NX=64, NY=64, NZ=64, NK=20, Maxk=0.3, XMIN=0.0, XMAX=1000.0, YMIN=0.0, YMAX=1000.0,
+                   ZMIN=0.0, ZMAX=1000.0, InterpOrder=3, DoInterlacing=1, LOS=0, Momentum=0)
+    bad = n - 1234
+    xb = x.copy()
+    xb[bad] = np.float32(1003.0)
+    with cg.PowerSpectrum(p0, precision="fp32") as ps:
+        ps.paint(xb, y, z)
+        with pytest.raises(cg.CapowError) as e:
+            ps.power()
+        assert e.value.status == cg.EBOUNDS
+        assert ps.stats()["first_out_of_box"] == bad
