@@ -1116,33 +1116,41 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
   if (fast) tile_rec_deposit<K, NF, IL, true>(g, fs, tg, recs, recw, rb, re, scA, scB, x0, y0, z0, ex, ey, ez, smi);
   else tile_rec_deposit<K, NF, IL, false>(g, fs, tg, recs, recw, rb, re, scA, scB, x0, y0, z0, ex, ey, ez, smi);
   __syncthreads();
-  // write every slot: pairs of cells along z as float2 (8-byte aligned global rows); the slots' DC
-  // sums go to one block reduction at the end (FP32 per thread and warp, FP64 across warps)
-  const int npair = tsz >> 1;
-  float dsums[NS * NF];
+  // write every slot: pairs of cells along z as float2 (8-byte aligned global rows). A thread keeps
+  // one (y, z) pair of the tile's x-planes and walks x, all slots per step: the pair's address in
+  // shared memory and in the grid only advance by px and the grid slice. The slots' DC sums go to
+  // one block reduction at the end (FP32 per thread and warp, FP64 across warps).
+  float dsums[NS * NF], invs[NS * NF];
 #pragma unroll
   for (int slot = 0; slot < NS * NF; slot++) {
-    float *gp = (float *)grids.g[slot];
-    const int *sl = smi + slot * slotw;
-    const float inv = ldexpf(1.0f, -((slot % NF) == 0 ? SA : SB));
-    float dsum = 0.0f;
-    for (int q = threadIdx.x; q < npair; q += blockDim.x) {
-      const int c = q << 1;
-      const int rz = c & (tg.tz - 1), ly = (c >> tg.lz) & (tg.ty - 1), lx = c >> (tg.lz + tg.ly);
-      if (lx >= ex || ly >= ey || rz >= ez) continue;
-      const int cp = lx * tg.px + ly * tg.py + rz;
-      const int2 iv = make_int2(sl[cp], sl[cp + 1]);
-      const float2 v = make_float2((float)iv.x * inv, (float)iv.y * inv);
-      float *dst = gp + (long long)(x0 + lx) * g.slice + (long long)(y0 + ly) * g.row + z0 + rz;
-      if (rz + 1 < ez) {
-        dsum += v.x + v.y;
-        *reinterpret_cast<float2 *>(dst) = v;
-      } else {
-        dsum += v.x;
-        dst[0] = v.x;
+    dsums[slot] = 0.0f;
+    invs[slot] = ldexpf(1.0f, -((slot % NF) == 0 ? SA : SB));
+  }
+  const int ppl = (tg.ty * tg.tz) >> 1;  // pairs per x-plane
+  for (int w = threadIdx.x; w < ppl; w += blockDim.x) {
+    const int c = w << 1;
+    const int rz = c & (tg.tz - 1), ly = c >> tg.lz;
+    if (ly >= ey || rz >= ez) continue;
+    const bool two = rz + 1 < ez;
+    const int cb = ly * tg.py + rz;
+    const long long gb = (long long)x0 * g.slice + (long long)(y0 + ly) * g.row + z0 + rz;
+    for (int lx = 0; lx < ex; lx++) {
+      const int cp = cb + lx * tg.px;
+      const long long go = gb + (long long)lx * g.slice;
+#pragma unroll
+      for (int slot = 0; slot < NS * NF; slot++) {
+        const int *sl = smi + slot * slotw + cp;
+        const float a0 = (float)sl[0] * invs[slot], a1 = (float)sl[1] * invs[slot];
+        float *dst = (float *)grids.g[slot] + go;
+        if (two) {
+          dsums[slot] += a0 + a1;
+          *reinterpret_cast<float2 *>(dst) = make_float2(a0, a1);
+        } else {
+          dsums[slot] += a0;
+          dst[0] = a0;
+        }
       }
     }
-    dsums[slot] = dsum;
   }
   double *dsts[NS * NF];
 #pragma unroll
