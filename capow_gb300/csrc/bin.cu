@@ -567,18 +567,20 @@ __global__ void __launch_bounds__(256) k_bin(BinParams bp, BinTables t, const ty
 }
 
 // ------------------------------------------------------------ fused x-axis FFT + binning (FP32)
-// cuFFT has transformed every x-plane of every grid over (y, z); what is left of the 3-D transform
-// (src/main.c:266-271) is the length-NX DFT along x of every (ky, kz) column, and its only consumer
-// is the binning (src/main.c:302-468). One pass does both: a CTA transforms a block of columns
-// along x in shared memory and bins the modes from there, so the x-transformed grids never go to
-// HBM. Columns whose smallest |k| lies beyond the top k-bin edge are not loaded.
+// Every x-plane of every grid has been transformed over (y, z) (by cuFFT in place, or by k_zr2c and
+// the y-axis C2C into the transposed layout); what is left of the 3-D transform (src/main.c:266-271)
+// is the length-NX DFT along x of every (ky, kz) column, and its only consumer is the binning
+// (src/main.c:302-468). One pass does both: a CTA transforms a block of columns along x in shared
+// memory and bins the modes from there, so the x-transformed grids never go to HBM. Columns whose
+// smallest |k| lies beyond the top k-bin edge are not loaded.
 //
-// A block is `kc` consecutive kz of one ky in each of the nslot grids: 8 kz (64 contiguous bytes
-// of every x-row of every grid) for NX <= 512. One CTA of XBIN_THREADS threads per SM. The first
-// radix-8 stage reads its inputs straight from HBM; the others work in shared memory, where row x
-// holds the block's ncol columns (c = slot * kc + kz - k0) with a pitch of ncol + 1: a butterfly's
-// rows are one base plus a fixed stride, a warp's accesses are whole rows, and the pad spreads the
-// rows the binning reads at once over the banks.
+// A block is `kc` consecutive inner indices (kz of one ky, or ky of one kz on the transposed layout)
+// in each of the nslot grids: 8 of them (64 contiguous bytes of every x-row of every grid) for
+// NX <= 512. One CTA of XBIN_THREADS threads per SM. The first radix-8 stage reads its inputs
+// straight from HBM; the others work in shared memory, where row x holds the block's ncol columns
+// (c = slot * kc + inner - first inner) with a pitch of ncol + 1: a butterfly's rows are one base
+// plus a fixed stride, a warp's accesses are whole rows, and the pad spreads the rows the binning
+// reads at once over the banks.
 constexpr int XBIN_THREADS = 1024;
 
 struct XbinSmem {
