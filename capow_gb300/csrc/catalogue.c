@@ -3,11 +3,14 @@
  * '#' skipped, any other line that does not hold six numbers is a fatal error. The line of
  * sight picks the velocity column (LOS 1 -> vx, 2 -> vy, otherwise vz).
  *
- * The file is read in one pass into memory and its lines are parsed by several threads
- * (strtod, correctly rounded like the reference's sscanf("%lf")), each writing its own
- * contiguous range, so the particle order of the file is kept. */
+ * The file is read in one pass into memory and its lines are parsed by several threads, each
+ * writing its own contiguous range, so the particle order of the file is kept. Numbers are
+ * correctly rounded like the reference's sscanf("%lf"): Clinger's fast path where it is exact
+ * (at most 19 significant digits, mantissa <= 2^53, |decimal exponent| <= 22: one IEEE multiply or
+ * divide of two exact doubles), strtod for everything else. */
 #include <errno.h>
 #include <pthread.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -26,14 +29,77 @@ typedef struct {
 
 static int is_hspace(char c) { return c == ' ' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; }
 
+static const double pow10_exact[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
+                                       1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+
+/* One decimal number at p (no leading space), ending before e. Sets *end to the first character
+ * after it (p when there is none), with strtod's result. */
+static double parse_number(const char *p, const char *e, const char **end) {
+  const char *s = p;
+  int neg = 0;
+  if (s < e && (*s == '+' || *s == '-')) neg = *s++ == '-';
+  uint64_t m = 0;
+  int nd = 0, exp10 = 0, digits = 0, exact = 1;
+  while (s < e && *s >= '0' && *s <= '9') {
+    if (nd < 19) {
+      m = m * 10 + (uint64_t)(*s - '0');
+      if (m) nd++;
+    } else {
+      exact = 0;
+    }
+    digits++;
+    s++;
+  }
+  if (s < e && *s == '.') {
+    s++;
+    while (s < e && *s >= '0' && *s <= '9') {
+      if (nd < 19) {
+        m = m * 10 + (uint64_t)(*s - '0');
+        if (m) nd++;
+        exp10--;
+      } else {
+        exact = 0;
+      }
+      digits++;
+      s++;
+    }
+  }
+  if (digits && s < e && (*s == 'e' || *s == 'E')) {
+    const char *t = s + 1;
+    int eneg = 0, ev = 0, ed = 0;
+    if (t < e && (*t == '+' || *t == '-')) eneg = *t++ == '-';
+    while (t < e && *t >= '0' && *t <= '9') {
+      if (ev < 100000) ev = ev * 10 + (*t - '0');
+      ed++;
+      t++;
+    }
+    if (ed) {  /* otherwise the 'e' is not part of the number */
+      exp10 += eneg ? -ev : ev;
+      s = t;
+    }
+  }
+  /* hex, inf and nan (x, i, n after the digits or none), long mantissas and large exponents */
+  const int plain = digits && !(s < e && (*s == 'x' || *s == 'X' || *s == 'i' || *s == 'I' || *s == 'n' || *s == 'N'));
+  if (plain && exact && m <= (1ULL << 53) && exp10 >= -22 && exp10 <= 22) {
+    double d = (double)m;
+    d = exp10 < 0 ? d / pow10_exact[-exp10] : d * pow10_exact[exp10];
+    *end = s;
+    return neg ? -d : d;
+  }
+  char *q;
+  const double d = strtod(p, &q);
+  *end = q;
+  return d;
+}
+
 /* parse up to six numbers of one line [p, e); returns how many were read */
 static int parse_line(const char *p, const char *e, double out[6]) {
   int k = 0;
   while (k < 6) {
     while (p < e && is_hspace(*p)) p++;
     if (p >= e) break;
-    char *end;
-    double v = strtod(p, &end);
+    const char *end;
+    double v = parse_number(p, e, &end);
     if (end == p || end > e) break;
     out[k++] = v;
     p = end;

@@ -129,6 +129,35 @@ def test_catalogue_reader_large_parallel(tmp_path):
     assert np.array_equal(x, ref[:, 0]) and np.array_equal(v, ref[:, 5])
 
 
+def test_catalogue_number_parsing_is_correctly_rounded(tmp_path):
+    """The reader's fast path (exact mantissa and power of ten) and its strtod fallback both give the
+    correctly rounded double of every token, as the reference's sscanf("%lf") does: against Python's
+    float() over many formats, signs, exponent ranges, long mantissas, subnormals, hex and inf/nan."""
+    rng = np.random.default_rng(11)
+    vals = np.concatenate([rng.normal(0, 300, 4000), rng.uniform(-1e-3, 1e-3, 2000),
+                           10.0 ** rng.uniform(-310, 308, 2000) * rng.choice([-1.0, 1.0], 2000),
+                           rng.integers(-(1 << 60), 1 << 60, 1000).astype(np.float64)])
+    toks = []
+    fmts = ["%.9g", "%.17g", "%.6f", "%.3e", "%.15e", "%g", "%.20g", "%.25f", "%+.8f"]
+    for i, v in enumerate(vals):
+        toks.append(fmts[i % len(fmts)] % v)
+    toks += ["0", "-0", "-0.0", "+0.5", ".5", "5.", "-.25", "1e5", "1.E-5", "1e+22", "1e23", "9007199254740993",
+             "9007199254740992", "123456789012345678901234", "0.1", "0.3", "2.2250738585072011e-308",
+             "4.9e-324", "1e-400", "1.7976931348623157e308", "0x1.8p3", "-0X10", "inf", "-Infinity", "nan",
+             "00000000000000000000000123.5", "0.000000000000000000000000000123", "7e-22", "7e22", "3.0e-23"]
+    while len(toks) % 6:
+        toks.append("1")
+    f = tmp_path / "nums.txt"
+    with open(f, "w") as fh:
+        for k in range(0, len(toks), 6):
+            fh.write(" ".join(toks[k:k + 6]) + "\n")
+    x, y, z, v = cg.read_catalogue(str(f), 1)  # LOS 1: the fourth column
+    got = np.stack([x, y, z, v], axis=1).ravel()
+    ref = np.array([float.fromhex(t) if "x" in t.lower() else float(t) for t in toks]).reshape(-1, 6)[:, :4].ravel()
+    same = (got.view(np.uint64) == ref.view(np.uint64)) | (np.isnan(got) & np.isnan(ref))
+    assert same.all(), [(toks[6 * (i // 4) + i % 4], got[i], ref[i]) for i in np.nonzero(~same)[0][:5]]
+
+
 def test_catalogue_bad_line_message(tmp_path):
     e = ERRS["catalogue_bad_line"]
     f = tmp_path / "bad.txt"
