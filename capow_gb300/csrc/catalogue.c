@@ -7,7 +7,8 @@
  * writing its own contiguous range, so the particle order of the file is kept. Numbers are
  * correctly rounded like the reference's sscanf("%lf"): Clinger's fast path where it is exact
  * (at most 19 significant digits, mantissa <= 2^53, |decimal exponent| <= 22: one IEEE multiply or
- * divide of two exact doubles), strtod for everything else. */
+ * divide of two exact doubles), else the Eisel-Lemire method for up to 19 digits (a 192-bit product
+ * with a 128-bit significand of 5^q), and strtod wherever those cannot decide. */
 #include <errno.h>
 #include <pthread.h>
 #include <stdint.h>
@@ -17,6 +18,7 @@
 #include <unistd.h>
 
 #include "capow.h"
+#include "pow5_table.h"
 
 typedef struct {
   const char *b, *e; /* [b, e) whole lines */
@@ -31,6 +33,44 @@ static int is_hspace(char c) { return c == ' ' || c == '\t' || c == '\r' || c ==
 
 static const double pow10_exact[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
                                        1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+
+/* w * 10^q correctly rounded, w != 0 with at most 19 digits (Eisel-Lemire). With F the 128-bit
+ * significand of 5^q (5^q = F 2^(e5 - 127), e5 = floor(log2 5^q)) and wn = w << lz normalised,
+ * w 10^q = P 2^(e5 - 127 + q - lz) for the 192-bit product P = wn F, whose leading bit is bit
+ * 190 + u (u = 0 or 1). The top 54 bits of P give the 53-bit significand and its round bit. F is
+ * exact for 0 <= q <= 55; otherwise it is truncated and the true product lies in [P, P + 2^64), so
+ * a carry into the kept bits (every bit from 64 to the round bit set) or an apparent tie cannot be
+ * decided here. Returns 0 then, and for subnormal, zero or infinite results (strtod decides). */
+static int eisel_lemire(uint64_t w, int q, int neg, double *out) {
+  if (q < POW5_QMIN || q > POW5_QMAX) return 0;
+  const int lz = __builtin_clzll(w);
+  const uint64_t wn = w << lz;
+  const uint64_t fh = pow5_128[q - POW5_QMIN][0], fl = pow5_128[q - POW5_QMIN][1];
+  const unsigned __int128 a = (unsigned __int128)wn * fh, b = (unsigned __int128)wn * fl;
+  const uint64_t p0 = (uint64_t)b;
+  const unsigned __int128 t = (unsigned __int128)(uint64_t)a + (uint64_t)(b >> 64);
+  const uint64_t p1 = (uint64_t)t;
+  const uint64_t p2 = (uint64_t)(a >> 64) + (uint64_t)(t >> 64);
+  const int u = (int)(p2 >> 63);
+  const int sh = 9 + u;  /* bits of p2 below the 54 kept ones */
+  const uint64_t m54 = p2 >> sh, below = p2 & ((1ULL << sh) - 1);
+  if (!(q >= 0 && q <= 55)) {
+    if (below == (1ULL << sh) - 1 && p1 == ~0ULL) return 0;
+    if ((m54 & 1) && below == 0 && p1 == 0 && p0 == 0) return 0;
+  }
+  uint64_t m = m54 >> 1;
+  int e2 = 63 + u + (((217706 * q) >> 16) - q) + q - lz;  /* binary exponent of the leading bit */
+  if ((m54 & 1) && (below != 0 || p1 != 0 || p0 != 0 || (m & 1))) m++;
+  if (m == (1ULL << 53)) {
+    m >>= 1;
+    e2++;
+  }
+  const int be = e2 + 1023;
+  if (be < 1 || be > 2046) return 0;
+  const uint64_t bits = ((uint64_t)(neg ? 1 : 0) << 63) | ((uint64_t)be << 52) | (m & ((1ULL << 52) - 1));
+  memcpy(out, &bits, sizeof bits);
+  return 1;
+}
 
 /* One decimal number at p (no leading space), ending before e. Sets *end to the first character
  * after it (p when there is none), with strtod's result. */
@@ -85,6 +125,13 @@ static double parse_number(const char *p, const char *e, const char **end) {
     d = exp10 < 0 ? d / pow10_exact[-exp10] : d * pow10_exact[exp10];
     *end = s;
     return neg ? -d : d;
+  }
+  if (plain && exact && m != 0) {
+    double d;
+    if (eisel_lemire(m, exp10, neg, &d)) {
+      *end = s;
+      return d;
+    }
   }
   char *q;
   const double d = strtod(p, &q);

@@ -158,6 +158,43 @@ def test_catalogue_number_parsing_is_correctly_rounded(tmp_path):
     assert same.all(), [(toks[6 * (i // 4) + i % 4], got[i], ref[i]) for i in np.nonzero(~same)[0][:5]]
 
 
+def test_catalogue_long_mantissas_and_near_ties(tmp_path):
+    """Up to 19 significant digits over the whole exponent range (the Eisel-Lemire path), decimals
+    cut from the exact midpoints between adjacent doubles (and one unit either side), and exact ties
+    that fit in 19 digits: bit-identical to correctly rounded parsing (Python's float())."""
+    import random
+    import struct
+    from decimal import Decimal, getcontext
+    getcontext().prec = 1200
+    rnd = random.Random(7)
+    toks = []
+    for _ in range(60000):
+        nd = rnd.randint(15, 19)
+        toks.append(f"{rnd.randint(10 ** (nd - 1), 10 ** nd - 1)}e{rnd.randint(-345, 310)}")
+    for _ in range(8000):
+        d = struct.unpack("<d", struct.pack("<Q", rnd.getrandbits(63)))[0]
+        if not 2.3e-308 < abs(d) < 1.7e308:
+            continue
+        mid = (Decimal(d) + Decimal(float(np.nextafter(d, np.inf)))) / 2
+        for nd in (17, 18, 19):
+            t = f"{mid:.{nd - 1}e}"
+            mant, ex = t.split("e")
+            k = int(mant.replace(".", ""))
+            toks += [t, f"{k - 1}e{int(ex) - (nd - 1)}", f"{k + 1}e{int(ex) - (nd - 1)}"]
+    toks += [str((2 ** 53 + o) * 2 ** k) for k in range(0, 10) for o in range(1, 400, 2)]
+    while len(toks) % 6:
+        toks.append("1")
+    f = tmp_path / "long.txt"
+    with open(f, "w") as fh:
+        for k in range(0, len(toks), 6):
+            fh.write(" ".join(toks[k:k + 6]) + "\n")
+    x, y, z, v = cg.read_catalogue(str(f), 1)
+    got = np.stack([x, y, z, v], axis=1).ravel()
+    ref = np.array([float(t) for t in toks]).reshape(-1, 6)[:, :4].ravel()
+    bad = np.nonzero(got.view(np.uint64) != ref.view(np.uint64))[0]
+    assert bad.size == 0, [(toks[6 * (i // 4) + i % 4], got[i], ref[i]) for i in bad[:5]]
+
+
 def test_catalogue_bad_line_message(tmp_path):
     e = ERRS["catalogue_bad_line"]
     f = tmp_path / "bad.txt"
