@@ -43,6 +43,8 @@ PARAMS = dict(NX=512, NY=512, NZ=512, XMIN=0.0, XMAX=1000.0, YMIN=0.0, YMAX=1000
               Omega_m=0.3089, Redshift=0.1, LOS=3, Momentum=0, Odd_Multipoles=0)
 N_SIDE = 256
 SEED = 2
+PRECISION = ("fp32-mixed: FP32 grids, FFT, per-thread bin runs and per-CTA bin copies; FP64 global bin sums, "
+             "scalars and near-edge indices; exact k-bins")
 # DRAM read + write bytes of one launch at this workload, from one ncu capture of it
 TRAFFIC_TILE_REC = 512893000 + 2119952000
 TRAFFIC_XFFT_BIN = 1768743000 + 3229000
@@ -112,10 +114,11 @@ def peaks() -> dict:
         return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def make_particles(torch, device):
+def make_particles():
+    """The workload's particles, generated on the host (both arms get the same values)."""
     from capow_gb300 import synth
 
-    return synth.zeldovich(N_SIDE, L=1000.0, mesh=512, rms_cells=1.5, seed=SEED, torch_device=device)
+    return synth.zeldovich(N_SIDE, L=1000.0, mesh=512, rms_cells=1.5, seed=SEED)
 
 
 def dist_init():
@@ -149,60 +152,84 @@ def max_over_ranks(world, v: float, device) -> float:
 
 
 # ------------------------------------------------------------------------------------------ CPU
+def cpu_model() -> dict:
+    """Host cores and CPU model of this box (for the reference arm's line)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not model:
+        import platform
+
+        model = platform.processor() or platform.machine()
+    return {"nproc": os.cpu_count(), "model": model}
+
+
+def config_dict(n_particles: int) -> dict:
+    return {"workload": WORKLOAD, "grid": 512, "particles": n_particles, "interp": "TSC", "interlacing": True,
+            "spectra": ["dd", "dp", "pp"], "l2": "inputs larger than L2 (grids 2.15 GB, particles 268 MB)",
+            "parallelism": "replicas"}
+
+
 def cpu_reference(steps: int, warmup: int, parts, log=print) -> dict:
-    """The reference algorithm on the host cores (CPU oracle restatement; 1 core, as the reference's
-    periodic path is single threaded without MPI). Each step is a bounded sample of the workload scaled
-    to one full evaluation: paint of a 1/16 particle subsample (x16), one 512^3 double r2c FFT (x8: the
-    three reference runs Momentum 0, 1, 2 need 2 + 4 + 2 transforms) and the full binning loop of one
-    grid pair (x3 runs)."""
+    """The reference's algorithm on the host cores: the CPU oracle (the periodic path of the reference
+    restated in C, single threaded as the reference's periodic path is without MPI). One step is one
+    full evaluation of the workload: the three reference runs that give dd, dp and pp (Momentum 0, 1,
+    2), each with its own paint, mean subtraction, FFTs, binning and normalisation, run side by side as
+    three single-threaded processes. The FFT is scipy's pocketfft (the reference links FFTW, absent
+    here). The step time is the longest of the three runs (they start together); particle loading is
+    outside it, as the GPU arm's particles are resident. Returns the median step and the runs' raw sums
+    of the last step."""
+    import tempfile
+
     import oracle as orc
 
-    try:
-        import scipy.fft as sfft
-
-        def fft(g, p):
-            row = 2 * (p.NZ // 2 + 1)
-            a = g[: p.NX * p.NY * row].reshape(p.NX, p.NY, row)
-            c = sfft.rfftn(a[:, :, : p.NZ], workers=1)
-            a[:] = c.view(np.float64).reshape(p.NX, p.NY, row)
-        fft_name = "scipy.fft (pocketfft, 1 thread; the reference links FFTW)"
-    except Exception:  # pragma: no cover
-        def fft(g, p):
-            orc.fft_r2c_inplace(g, p.NX, p.NY, p.NZ)
-        fft_name = "oracle C FFT"
-    orc.build()
     p = orc.Params(**{k: v for k, v in PARAMS.items() if k in orc.Params.__dataclass_fields__})
-    x, y, z, vx, vy, vz = [np.asarray(a, dtype=np.float64) for a in parts]
-    n = len(x)
-    sub = slice(0, n // 16)
-    samples = []
-    for it in range(warmup + steps):
-        t0 = time.perf_counter()
-        g, st = orc.paint(p, x[sub], y[sub], z[sub], vx[sub], vy[sub], vz[sub], momentum=1)  # 4 grids
-        t1 = time.perf_counter()
-        fft(g["ddg"], p)
-        t2 = time.perf_counter()
-        g["ddg_interlace"][:] = g["ddg"]
-        g["ddg_mom"][:] = g["ddg"]
-        g["ddg_mom_interlace"][:] = g["ddg"]
-        t3 = time.perf_counter()
-        orc.compute_power(p, g, momentum=1)
-        t4 = time.perf_counter()
-        # Momentum 0 and 2 runs paint 2 grids each, Momentum 1 paints 4: 8 grid-paints = 2x the 4-grid paint
-        paint_ms = (t1 - t0) * 16 * 2 * 1e3
-        fft_ms = (t2 - t1) * 8 * 1e3
-        bin_ms = (t4 - t3) * 3 * 1e3
-        total = paint_ms + fft_ms + bin_ms
-        if it >= warmup:
-            samples.append((total, paint_ms, fft_ms, bin_ms))
-        log(f"cpu step {it}: est {total:.0f} ms (paint {paint_ms:.0f}, fft {fft_ms:.0f}, bin {bin_ms:.0f})")
-    tot = statistics.median(s[0] for s in samples)
-    return {"value": tot, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": ("per step: paint of 1/16 of the particles (x16, x2 for the three Momentum runs' 8 grids), "
-                       f"one 512^3 float64 r2c FFT x8 [{fft_name}], one full binning pass x3"),
-            "stages_ms": {"paint": statistics.median(s[1] for s in samples),
-                          "fft": statistics.median(s[2] for s in samples),
-                          "bin": statistics.median(s[3] for s in samples)}}
+    samples, last = [], None
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "parts.npz")
+        orc.save_particles(path, *parts)
+        with orc.ParallelRuns(3) as pool:
+            for it in range(warmup + steps):
+                t0 = time.perf_counter()
+                out = pool.run(p, path, [0, 1, 2], timeout=1800)
+                wall = (time.perf_counter() - t0) * 1e3
+                per = [o[1] * 1e3 for o in out]
+                if it >= warmup:
+                    samples.append((max(per), wall, per))
+                last = out
+                log(f"cpu step {it}{' (warm-up)' if it < warmup else ''}: {max(per):.0f} ms "
+                    f"(Momentum 0/1/2 runs {per[0]:.0f} / {per[1]:.0f} / {per[2]:.0f} ms, wall {wall:.0f} ms)")
+    val = statistics.median(s[0] for s in samples)
+    info = cpu_model()
+    return {"value": val, "unit": UNIT, "cores": 3, "kind": "port",
+            "sample": ("per step: one full evaluation, the three reference runs for dd, dp, pp (Momentum 0, 1, 2) "
+                       "of all 16,777,216 particles on the 512^3 TSC grid, each single threaded, run side by side; "
+                       "FFT scipy.fft pocketfft (the reference links FFTW)"),
+            "runs_ms": {f"momentum_{m}": statistics.median(s[2][m] for s in samples) for m in (0, 1, 2)},
+            "wall_ms": statistics.median(s[1] for s in samples), "nproc": info["nproc"], "cpu_model": info["model"],
+            "raw": {m: last[m][0] for m in (0, 1, 2)}}
+
+
+def accuracy_vs_oracle(res, raw) -> dict:
+    """Max over bins of the normalised |P_l(GPU) - P_l(oracle)| per spectrum (parity_util's measure: l = 0
+    against P0 + shot/norm, l = 2, 4 times (2l+1); dp normalised by sqrt(P_dd P_pp)), and whether the
+    mode counts are equal."""
+    dd, pp = np.abs(raw[0]["raw"]["Pk0"]), np.abs(raw[2]["raw"]["Pk0"])
+    acc = {}
+    for q, (name, norm0) in enumerate((("dd", dd), ("dp", np.sqrt(dd * pp)), ("pp", pp))):
+        ref = raw[q]["raw"]
+        m = (np.asarray(ref["Nmodes"]) > 0) & (norm0 > 0)
+        acc[name] = {f"l{l}": float(np.max((2 * l + 1) * np.abs(np.asarray(res[q][f"Pk{l}"])[m] - ref[f"Pk{l}"][m])
+                                            / norm0[m])) for l in (0, 2, 4)}
+        acc[name]["nmodes_equal"] = bool(np.array_equal(np.asarray(res[q]["Nmodes"], np.int64),
+                                                        np.asarray(ref["Nmodes"], np.int64)))
+    return acc
 
 
 # ------------------------------------------------------------------------------------------ GPU
@@ -341,7 +368,7 @@ def gpu_bench(args, world, rank, local):
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    parts = make_particles(torch, dev)
+    parts = make_particles()
     x, y, z, vx, vy, vz = parts
     n = len(x)
     params = cg.Params(**PARAMS)
@@ -435,6 +462,7 @@ def gpu_bench(args, world, rank, local):
     ps.close()
     fp64_ms = None
     acc = None
+    r64 = None
     try:
         p64 = cg.PowerSpectrum(params, precision="fp64", spectra=["dd", "dp", "pp"], device=local, stream=sh)
         p64.paint(*d)
@@ -470,6 +498,7 @@ def gpu_bench(args, world, rank, local):
         "ms_per": ms_per, "wall_ms": wall, "stage_ms": stage_ms, "launches": launches, "e2e_ms": e2e_ms, "h2d": h2d,
         "d2h": d2h, "fp64_ms": fp64_ms, "acc": acc, "B32": B32, "B64": B64, "peaks": pk, "clocks": clk.summary(),
         "n": n, "parts": parts, "adjoint": adj, "tile_ms": tile_ms, "tile_records": tile_records,
+        "res": res, "r64": r64,
     }
 
 
@@ -503,17 +532,17 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        from capow_gb300 import synth
-
-        parts = synth.zeldovich(N_SIDE, L=1000.0, mesh=512, rms_cells=1.5, seed=SEED)
-        cpu = cpu_reference(args.steps, 1, parts, log)
-        line = {"metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-                "warmup": 1, "ms_per_step": cpu["value"], "higher_is_better": False, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Zel'dovich lattice)",
-                "config": {"workload": WORKLOAD, "grid": 512, "particles": N_SIDE ** 3}, "impl": "reference",
-                "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
-                "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-                "stages_ms": cpu["stages_ms"]}
+        parts = make_particles()
+        cpu = cpu_reference(args.steps, args.warmup, parts, log)
+        line = {"metric": METRIC, "value": round(cpu["value"], 1), "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(cpu["value"], 1),
+                "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded Zel'dovich lattice, float32 positions/velocities)",
+                "config": config_dict(len(parts[0])), "impl": "reference",
+                "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "nproc", "cpu_model")},
+                "e2e": {"value": round(cpu["value"], 1), "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0},
+                "runs_ms": cpu["runs_ms"], "wall_ms": cpu["wall_ms"]}
         print(json.dumps(line), flush=True)
         return
 
@@ -531,9 +560,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": round(r["ms_per"] * world, 4), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Zel'dovich lattice, float32 positions/velocities)",
-        "config": {"workload": WORKLOAD, "grid": 512, "particles": r["n"], "interp": "TSC", "interlacing": True,
-                   "spectra": ["dd", "dp", "pp"], "precision": "fp32-mixed (FP64 bin sums, exact k-bins)",
-                   "l2": "inputs larger than L2 (grids 2.15 GB, particles 268 MB)", "parallelism": "replicas"},
+        "config": config_dict(r["n"]),
+        "precision": PRECISION,
         "e2e": {"value": round(r["e2e_ms"], 4), "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"]},
         "gpu_launches": int(r["launches"]),
@@ -546,8 +574,13 @@ def main():
         "accuracy_fp32_vs_fp64_gpu": r["acc"],
         "adjoint_c3": r["adjoint"],
         "clocks": r["clocks"],
-        "cpu_baseline": ({k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")} if cpu else None),
+        "cpu_baseline": ({k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "nproc", "cpu_model")}
+                         if cpu else None),
     }
+    if cpu:  # the same particles through the oracle: the headline's error against the reference's algorithm
+        line["accuracy_vs_oracle"] = {"fp32": accuracy_vs_oracle(r["res"], cpu["raw"])}
+        if r["r64"]:
+            line["accuracy_vs_oracle"]["fp64"] = accuracy_vs_oracle(r["r64"], cpu["raw"])
     # the two largest kernels, each timed by the library's CUDA events on the context stream:
     # k_tile_rec (the FP32 tile deposit; events around its one launch) and k_xfft_bin (x-axis FFT
     # fused with the binning: the whole "bin" stage). "roofline" is the one that took longer.

@@ -117,6 +117,21 @@ extern "C" int capow_paint_noalloc(capow_ctx *c, const capow_particles *parts) {
   if (!parts->on_device) FAIL(c, CAPOW_EINVAL, "capow_paint_noalloc takes device-resident particles only");
   if (!parts->x || !parts->y || !parts->z) FAIL(c, CAPOW_EINVAL, "x, y and z are required");
   if (c->fs.need_v && !parts->vlos) FAIL(c, CAPOW_EINVAL, "vlos is required for LOS != 0 or momentum fields");
+  // every input must be device memory of this context's device (another device's memory would be
+  // read through peer access or fault, with no clear error)
+  {
+    const void *arrs[5] = {parts->x, parts->y, parts->z, c->fs.need_v ? parts->vlos : nullptr, parts->w};
+    for (int k = 0; k < 5; k++) {
+      if (!arrs[k]) continue;
+      cudaPointerAttributes a;
+      if (cudaPointerGetAttributes(&a, arrs[k]) != cudaSuccess) {
+        (void)cudaGetLastError();
+        FAIL(c, CAPOW_EINVAL, "capow_paint_noalloc: input array %d is not device memory", k);
+      }
+      if (a.type != cudaMemoryTypeDevice || a.device != c->o.device)
+        FAIL(c, CAPOW_EINVAL, "capow_paint_noalloc: input array %d is not device memory of device %d", k, c->o.device);
+    }
+  }
   const bool det = c->prec == CAPOW_FP32_DETERMINISTIC, weights = parts->w != nullptr;
   const unsigned long long n = parts->n, per = records_per_particle(c->g, c->tg);
   const unsigned long long limit = CAPOW_NOALLOC_SCRATCH_BYTES;
@@ -153,6 +168,10 @@ extern "C" int capow_paint_noalloc(capow_ctx *c, const capow_particles *parts) {
   c->last = d;
   c->painted = true;
   c->powered = false;
+  // per-paint state of capow_paint that this paint does not produce: no timed tile launch (the record
+  // counts live in the shared array, not the context's tables) and no chunked host copy
+  c->tile_timed = false;
+  c->nchunk = 0;
   GridPtrs gp;
   for (int k = 0; k < 4; k++)
     gp.g[k] = k < c->nslot ? (void *)((float *)c->grid_base + c->grid_elems * k) : nullptr;

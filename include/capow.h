@@ -140,8 +140,10 @@ int capow_create(const capow_params *p, const capow_options *opt, capow_ctx **ou
  * halo fold and the velocity moments, for one catalogue. Replaces any previous paint. */
 int capow_paint(capow_ctx *ctx, const capow_particles *parts);
 
-/* Size of the fixed device scratch of capow_paint_noalloc: 64 MiB per device, reserved when the
- * first call on that device loads it. */
+/* Size of the fixed device scratch of capow_paint_noalloc: 64 MiB per device. With lazy module
+ * loading (the CUDA default since 12.2) it is reserved when the first call on a device loads it;
+ * with CUDA_MODULE_LOADING=EAGER every process that links the library holds it on every device it
+ * uses from context creation on. */
 #define CAPOW_NOALLOC_SCRATCH_BYTES (64ull << 20)
 
 /* capow_paint without any device allocation. No counterpart in the reference (its paint runs on
@@ -159,7 +161,13 @@ int capow_paint(capow_ctx *ctx, const capow_particles *parts);
  *   before any stream capture begins;
  * - every call on a device shares the one array: calls that overlap on the GPU (other streams,
  *   other contexts on the same device) race; order them, e.g. on one stream.
- * capow_get_stats, capow_copy_grid and capow_power then work as after capow_paint. */
+ * - every input array must be device memory of the context's device (CAPOW_EINVAL otherwise).
+ * capow_get_stats, capow_copy_grid and capow_power then work as after capow_paint and allocate
+ * nothing (the worst-case bound keeps the record lists from overflowing, so the repaint that
+ * capow_power does after an overflow cannot happen). capow_backward is not covered: it repaints the
+ * catalogue through capow_paint's buffers, which it allocates on first use, so a caller that cannot
+ * allocate must not call it on a context painted this way. capow_tile_kernel_ms returns
+ * CAPOW_ESTATE after this paint (its tile launch is not timed). */
 int capow_paint_noalloc(capow_ctx *ctx, const capow_particles *parts);
 
 /* counters from the last paint (ends with a stream synchronisation). The counters are filled

@@ -30,22 +30,25 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liborc.so")
 REF_BIN = os.path.join(HERE, "_ref", "capow_ref")
-REF_SRC = "/root/reference"
+# Where the CAPOW sources are mounted (only where the reference binary is to be built); no default.
+REF_SRC_ENV = "CAPOW_REFERENCE_SRC"
 
 _CFLAGS = ["-O2", "-std=gnu99", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", "-Wno-unused-function"]
 
 
-def build(force: bool = False) -> str:
-    """Compile liborc.so (and, where the reference sources exist, oracle/_ref/capow_ref)."""
+def build(force: bool = False, ref_src: Optional[str] = None) -> str:
+    """Compile liborc.so, and oracle/_ref/capow_ref when the reference sources are given (``ref_src``
+    or the CAPOW_REFERENCE_SRC environment variable) and present."""
     os.makedirs(BUILD, exist_ok=True)
     srcs = [os.path.join(HERE, f) for f in ("capow_oracle.c", "orc_fft.c")]
     hdrs = [os.path.join(HERE, f) for f in ("capow_oracle.h", "orc_fft.h")]
     newest = max(os.path.getmtime(f) for f in srcs + hdrs)
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
         subprocess.check_call(["gcc", *_CFLAGS, "-o", LIB, *srcs, "-lm"])
-    if os.path.isdir(os.path.join(REF_SRC, "src")):
+    ref_src = ref_src or os.environ.get(REF_SRC_ENV)
+    if ref_src and os.path.isdir(os.path.join(ref_src, "src")):
         subprocess.check_call(
-            ["make", "-s", "-f", os.path.join("oracle", "Makefile.ref"), f"REF={REF_SRC}"],
+            ["make", "-s", "-f", os.path.join("oracle", "Makefile.ref"), f"REF={ref_src}"],
             cwd=os.path.dirname(HERE),
         )
     return LIB
@@ -263,6 +266,70 @@ def run(p: Params, x, y, z, vx, vy, vz, w=None, momentum: Optional[int] = None, 
 
 def fft_r2c_inplace(grid: np.ndarray, nx: int, ny: int, nz: int) -> None:
     lib().orc_fft_r2c_3d_inplace(nx, ny, nz, _dp(grid))
+
+
+def fft_scipy(grid: np.ndarray, p: Params) -> None:
+    """In-place forward r2c of a padded grid with scipy's pocketfft (one thread): the same transform as
+    the oracle FFT (sign -1, unnormalised, src/main.c:266-271), several times faster at 512^3."""
+    import scipy.fft as sfft
+
+    row = 2 * (p.NZ // 2 + 1)
+    a = grid[: p.NX * p.NY * row].reshape(p.NX, p.NY, row)
+    c = sfft.rfftn(a[:, :, : p.NZ], workers=1)
+    a[:] = c.view(np.float64).reshape(p.NX, p.NY, row)
+
+
+def _summary(res: dict) -> dict:
+    """What a parity check or a timing needs from run(): everything but the grids."""
+    return {k: v for k, v in res.items() if k != "grids"}
+
+
+def _load_particles(path: str):
+    d = np.load(path)
+    return tuple(np.asarray(d[k], dtype=np.float64) for k in ("x", "y", "z", "vx", "vy", "vz"))
+
+
+def _run_from_file(args):
+    import time
+
+    pdict, path, momentum, use_scipy = args
+    parts = _load_particles(path)
+    t0 = time.perf_counter()
+    res = run(Params(**pdict), *parts, momentum=momentum, fft=fft_scipy if use_scipy else None)
+    return _summary(res), time.perf_counter() - t0
+
+
+def save_particles(path: str, x, y, z, vx, vy, vz) -> None:
+    """Write a catalogue for run_parallel (one .npz of the six columns)."""
+    np.savez(path, x=x, y=y, z=z, vx=vx, vy=vy, vz=vz)
+
+
+class ParallelRuns:
+    """Single-threaded oracle runs of one catalogue for several Momentum values, one process each, as
+    the reference is run once per spectrum (src/main.c:28-298). Processes are started with `spawn`
+    (never forked from a process that has used the GPU); a worker that dies raises instead of being
+    restarted. Each run() call returns, per Momentum, the run() results without the grids and that
+    run's seconds."""
+
+    def __init__(self, nproc: int):
+        import concurrent.futures as cf
+        import multiprocessing as mp
+
+        build()
+        self.pool = cf.ProcessPoolExecutor(max_workers=nproc, mp_context=mp.get_context("spawn"))
+
+    def run(self, p: Params, path: str, momenta, use_scipy: bool = True, timeout: Optional[float] = None):
+        pdict = dataclasses.asdict(p)
+        return list(self.pool.map(_run_from_file, [(pdict, path, m, use_scipy) for m in momenta], timeout=timeout))
+
+    def close(self):
+        self.pool.shutdown(wait=True, cancel_futures=True)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def real_view(p: Params, grid: np.ndarray) -> np.ndarray:

@@ -147,6 +147,31 @@ def test_backward_matches_dense_torch_autograd(gpu):
         assert err <= 1e-8, f"{name}: {err:.2e}"
 
 
+def test_autograd_function_matches_dense_torch_autograd(gpu):
+    """The same loss written in torch over the multipoles of the test-only autograd.Function (whose
+    backward is capow_backward), against autograd through the dense FP64 restatement."""
+    torch = pytest.importorskip("torch")
+    from capow_autograd import density_multipoles
+
+    p = cg.Params(NX=64, NY=64, NZ=64, NK=30, Maxk=0.3, **BASE)
+    parts = interior_particles(p, 32 ** 3, seed=43)
+    T0, T2 = (torch.as_tensor(a, device=gpu) for a in lib_multipoles(p, interior_particles(p, 32 ** 3, seed=44),
+                                                                          "fp64"))
+    t = [torch.tensor(a, dtype=torch.float64, device=gpu, requires_grad=True) for a in parts]
+    P = density_multipoles(torch, p, "fp64", *t)
+    loss = ((P[0] - T0) ** 2).sum() + ((P[2] - T2) ** 2).sum()
+    loss.backward()
+    got = [tt.grad.cpu().numpy() for tt in t]
+    u = [torch.tensor(a, dtype=torch.float64, device=gpu, requires_grad=True) for a in parts]
+    D0, D2 = dense_multipoles(torch, p, *u, mode_tables(p))
+    assert np.abs(P[0].detach().cpu().numpy() - D0.detach().cpu().numpy()).max() <= 1e-10 * D0.abs().max().item()
+    ((D0 - T0) ** 2).sum().add(((D2 - T2) ** 2).sum()).backward()
+    for name, g, uu in zip(("dx", "dy", "dz", "dvlos", "dw"), got, u):
+        ref = uu.grad.cpu().numpy()
+        err = np.abs(g - ref).max() / np.abs(ref).max()
+        assert err <= 1e-8, f"{name}: {err:.2e}"
+
+
 def test_backward_central_differences(gpu):
     p = cg.Params(NX=32, NY=32, NZ=32, NK=15, Maxk=0.15, **BASE)
     parts = [a.copy() for a in interior_particles(p, 20000, seed=51, margin=0.0)]

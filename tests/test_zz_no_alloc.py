@@ -35,7 +35,8 @@ def test_noalloc_matches_paint_twice(gpu, precision, order, los, mom):
     p = cg.Params(NX=64, NY=48, NZ=40, InterpOrder=order, LOS=los, Momentum=mom, **BASE)
     nfields = 2 if mom == 1 else 1
     with cg.PowerSpectrum(p, precision) as ref, cg.PowerSpectrum(p, precision) as na:
-        for call, (n, seed) in enumerate(((150000, 31), (40000, 32))):
+        # ascending sizes: the second, larger catalogue is the one capow_paint would grow its buffers for
+        for call, (n, seed) in enumerate(((40000, 31), (150000, 32))):
             dev = _device(particles(p, n, seed), los, gpu)
             ref.paint(*dev)
             torch.cuda.synchronize()
@@ -85,9 +86,14 @@ def test_noalloc_rejects_beyond_limit(gpu):
         assert m, str(e.value)
         fit = int(m.group(1))
         assert 100_000 < fit < big
-        # exactly the limit is accepted and matches capow_paint
+        # exactly the limit is accepted, allocates nothing and matches capow_paint
         sub = [a[:fit].contiguous() for a in pos]
+        ps.paint_noalloc(*[a[:1000] for a in sub])  # loads the array on this device before the measured call
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
         ps.paint_noalloc(*sub)
+        ps.stats()
+        assert torch.cuda.mem_get_info()[0] == free0
         ref.paint(*sub)
         s, r = ps.stats(), ref.stats()
         assert s["nread"] == fit and s["ngrid"] == r["ngrid"]
@@ -114,3 +120,9 @@ def test_noalloc_argument_errors(gpu):
         rc = cg.lib().capow_paint_noalloc(ps._ctx, ctypes.byref(pc))
         assert rc == cg.EINVAL
         assert "device-resident" in cg.lib().capow_last_error(ps._ctx).decode()
+        # pinned host memory handed over as if it were device memory: refused by its pointer attributes
+        h = torch.tensor(x).pin_memory()
+        pc = cg._Particles(len(x), cg.F64, 1, h.data_ptr(), h.data_ptr(), h.data_ptr(), None, None)
+        rc = cg.lib().capow_paint_noalloc(ps._ctx, ctypes.byref(pc))
+        assert rc == cg.EINVAL
+        assert "not device memory" in cg.lib().capow_last_error(ps._ctx).decode()
