@@ -89,4 +89,4 @@ def test_headline_workload_against_oracle(gpu, headline_case, precision):
         nm = np.asarray(refs[m]["raw"]["Nmodes"], dtype=np.float64)
         k = nm > 0
         moved = np.max(np.abs(r["shot"] - refs[m]["shot"]) * nm[k] / norm0[k])
-        assert moved <= (1e-12 if precision == "fp64" else 1e-5), (label, r["kind"], moved)
+        assert moved <= (1e-10 if precision == "fp64" else 1e-5), (label, r["kind"], moved)
