@@ -158,6 +158,7 @@ extern "C" int capow_batch(capow_mock *mocks, int nmocks, const capow_options *o
     }
     m.bp = c->bp;
     m.bp.fx_step = (float)(1.0 / ((float)p.NX * m.g.dx));
+    bin_params_kguess(m.bp, p);
     tab_off[i] = (blob.size() + 255) & ~(size_t)255;
     blob.resize(tab_off[i]);
     std::vector<unsigned char> one;

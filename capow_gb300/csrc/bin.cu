@@ -584,7 +584,18 @@ __global__ void __launch_bounds__(256) k_bin(BinParams bp, BinTables t, const ty
 constexpr int XBIN_THREADS = 1024;
 
 struct XbinSmem {
-  unsigned sd, stw, sxt, sfx, sb, sE, sElo, sEhi, total;
+  unsigned sd, stw, sxt, sfx, sb, sbd, scol, srow, sE, sElo, sEhi, total;
+};
+
+// Per-column quantities of the block being binned (one entry per inner index of the block), written
+// by kc threads during the first FFT stage: everything of a mode that does not depend on kx.
+struct XCol {
+  float syz;    // fy^2 + fz^2 (FP32)
+  float cyzn;   // y, z deconvolution factors, x 0.25 when interlaced, x 2 off the kz = 0 plane (NM)
+  float flos;   // mu numerator when the LOS is y or z (fy or fz)
+  int r;        // |kx| index beyond which no mode reaches the top bin edge (-1: none does)
+  float2 eyz;   // y, z interlace phase
+  int j, kz;    // ky index (-1: inner index beyond the grid), kz index
 };
 
 // Twiddle-table entries of the radix-8 stages that have more than one butterfly per group: a
@@ -608,6 +619,9 @@ CAPOW_HD XbinSmem xbin_smem_layout(int log2n, int ncol, int np, int nl, int nk, 
   L.sxt = o;  o = align16(o + 16u * (n + (n >> 6) + 1));
   L.sfx = o;  o = align16(o + 4u * n);
   L.sb = o;   o = align16(o + 4u * np * nl * nk * nbc);
+  L.sbd = o;  o = align16(o + 8u * np * nl * nk);
+  L.scol = o; o = align16(o + (unsigned)sizeof(XCol) * ncol);
+  L.srow = o; o = align16(o + 4u * n);
   L.sE = o;   o = align16(o + 8u * (nk + 3));
   L.sElo = o; o = align16(o + 4u * (nk + 3));
   L.sEhi = o; o = align16(o + 4u * (nk + 3));
@@ -686,7 +700,26 @@ __device__ __forceinline__ int xfft_pos(int log2n, int i) {
   return pos + rem;  // the last digit has span 1
 }
 
-template <int NF, bool IL, bool ODD>
+// First guess of the bin of an FP32 s (linear bins: from sqrtf(s); log bins: bisection over the safe
+// edges). It only starts the walk over the safe edges, which ends on the same bin from any start.
+__device__ __forceinline__ int guess_bin(const BinParams &bp, const float *sElo, float s) {
+  const int nk = bp.nk;
+  if (!bp.lg) {
+    const float v = sqrtf(s) * bp.kscale + bp.koff;
+    return v < 0.0f ? -1 : (v >= (float)nk ? nk : (int)v);
+  }
+  int a = 0, z = nk + 2;  // sElo[a] <= s < sElo[z] (sElo[0] = -inf, sElo[nk + 2] = +inf)
+  while (z - a > 1) {
+    const int mid = (a + z) >> 1;
+    if (sElo[mid] <= s) a = mid;
+    else z = mid;
+  }
+  return a - 1;
+}
+
+// PM: the products accumulated (bit q: |A|^2, Re A*B, Im A*B, |B|^2); the launcher passes a superset
+// of the products the spectra read.
+template <int NF, bool IL, bool ODD, int PM>
 __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTables t, XbinGeo xg, const float2 *g0,
                                                            const float2 *g1, const float2 *g2, const float2 *g3,
                                                            const double *dcv, double *bins) {
@@ -701,13 +734,17 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
   float2 *stw = (float2 *)(smraw + L.stw);
   float4 *sxt = (float4 *)(smraw + L.sxt);  // per kx: fx^2, deconvolution factor, interlace phase
   float *sfx = (float *)(smraw + L.sfx);    // per kx: fx (the mu numerator when LOS = x)
-  float *sb = (float *)(smraw + L.sb);
+  float *sb = (float *)(smraw + L.sb);      // this block's bins, FP32, xg.nbc copies
+  double *sbd = (double *)(smraw + L.sbd);  // the CTA's bins, FP64
+  XCol *scol = (XCol *)(smraw + L.scol);
+  int *srow = (int *)(smraw + L.srow);
   double *sE = (double *)(smraw + L.sE);
   float *sElo = (float *)(smraw + L.sElo);
   float *sEhi = (float *)(smraw + L.sEhi);
   const int nbins = NP * NL * nk;
   for (int c = threadIdx.x; c < nbins * xg.nbc; c += blockDim.x) sb[c] = 0.0f;
-  // this warp's copy of the bins (flushes from different warps then rarely meet on one address)
+  for (int c = threadIdx.x; c < nbins; c += blockDim.x) sbd[c] = 0.0;
+  // this warp's copy of the block bins (flushes from different warps then rarely meet on one address)
   float *sbw = sb + ((threadIdx.x >> 5) & (xg.nbc - 1)) * nbins;
   for (int c = threadIdx.x; c < nk + 3; c += blockDim.x) {
     sE[c] = t.E[c];
@@ -728,12 +765,16 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
   // binning work items: (kz column of the block, run of mpt consecutive kx), mpt <= 8 chosen so that
   // the kc * NX / mpt items keep every thread busy. Within a column the run index is rotated by 3
   // bits, so that neighbouring lanes start runs far apart in x and their rows (digit-reversed)
-  // spread over the shared-memory banks.
+  // spread over the shared-memory banks. srow[ch]: row of kx = ch * mpt after the DIF stages; the
+  // digit reversal is a permutation of bit positions and the run's offsets m < mpt <= 8 have bits
+  // disjoint from ch * mpt, so row(ch * mpt + m) = srow[ch] + m NX/8.
   const int log2mpt = min(3, max(0, log2n + xg.log2kc - (31 - __clz(blockDim.x))));
   const int mpt = 1 << log2mpt, log2nr = log2n - log2mpt, nitems = kc_n << log2nr;
+  for (int ch = threadIdx.x; ch < (1 << log2nr); ch += blockDim.x) srow[ch] = xfft_pos(log2n, ch << log2mpt);
   const long long xstride = (long long)bp.ny * bp.nzc;  // = n_outer * n_inner
   const int Q1 = n >> 3, nbf1 = ncol << (log2n - 3);
   const long long qstep = (long long)Q1 * xstride;
+  int nproc = 0;
   __syncthreads();
   for (int blk = blockIdx.x; blk < xg.nblocks; blk += gridDim.x) {
     const int bo = blk / xg.nkb, bi0 = (blk - bo * xg.nkb) * kc_n;  // outer index, first inner index
@@ -743,7 +784,31 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
     const float smin = xg.tr ? t.fz2f[bo] + fminf(t.fy2f[bi0], t.fy2f[min(bi0 + kc_n, bp.ny) - 1])
                              : t.fy2f[bo] + t.fz2f[bi0];
     if (smin > topf32) continue;
-    __syncthreads();  // the previous block's binning has read sd
+    __syncthreads();  // the previous block's binning has read sd and scol
+    if (threadIdx.x < kc_n) {  // the block's column table (src/main.c:335-389 for the y, z factors)
+      XCol col;
+      const int inner = bi0 + threadIdx.x;
+      if (inner < xg.n_inner) {
+        const int j = xg.tr ? inner : bo, kz = xg.tr ? bo : inner;
+        col.syz = t.fy2f[j] + t.fz2f[kz];
+        float cyz = t.cyf[j] * t.czf[kz];
+        if (IL) cyz *= 0.25f;
+        col.cyzn = kz != 0 ? 2.0f * cyz : cyz;  // Hermitian multiplicity off the kz = 0 plane (:422-429)
+        col.eyz = IL ? cmulf(t.eyf[j], t.ezf[kz]) : make_float2(0.0f, 0.0f);
+        col.flos = bp.los == 2 ? t.fyf[j] : t.fzf[kz];
+        const float topf = sElo[nk + 1] - col.syz;
+        col.r = topf > 0.0f ? min(bp.xhalf, (int)(sqrtf(topf) / bp.fx_step) + 1) : -1;
+        col.j = j;
+        col.kz = kz;
+      } else {
+        col.syz = col.cyzn = col.flos = 0.0f;
+        col.eyz = make_float2(0.0f, 0.0f);
+        col.r = -1;
+        col.j = -1;
+        col.kz = 0;
+      }
+      scol[threadIdx.x] = col;
+    }
     // first DIF stage (span NX) straight from HBM: butterfly (column c, jj) reads rows jj + q NX/8
     for (int u = threadIdx.x; u < nbf1; u += blockDim.x) {
       const int c = u & (ncol - 1), jj = u >> xg.log2ncol;
@@ -804,69 +869,49 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
       const int my_kc = w >> log2nr, rr = w & ((1 << log2nr) - 1);
       const int ch = log2nr >= 3 ? (((rr & 7) << (log2nr - 3)) | (rr >> 3)) : rr;
       const int i0 = ch << log2mpt;
-      // rows of the run: the digit reversal is a permutation of bit positions and i0, m < mpt <= 8
-      // have disjoint bits, so row(i0 + m) = row(i0) + row(m) = row(i0) + m NX/8
-      const int rowb = xfft_pos(log2n, i0);
-      const int inner = bi0 + my_kc;
-      if (inner >= xg.n_inner) continue;
-      const int j = xg.tr ? inner : bo, kz = xg.tr ? bo : inner;
-      const float syz = t.fy2f[j] + t.fz2f[kz];
-      float cyz = t.cyf[j] * t.czf[kz];
-      if (IL) cyz *= 0.25f;
-      float2 eyz = make_float2(0.0f, 0.0f);
-      if (IL) eyz = cmulf(t.eyf[j], t.ezf[kz]);
-      const float flos_yz = bp.los == 2 ? t.fyf[j] : t.fzf[kz];
-      const float topf = sElo[nk + 1] - syz;
-      const int r = topf > 0.0f ? min(bp.xhalf, (int)(sqrtf(topf) / bp.fx_step) + 1) : -1;
+      const XCol col = scol[my_kc];
+      if (col.j < 0) continue;
+      const int rowb = srow[ch];
+      if (col.j == 0 && col.kz == 0 && i0 == 0) {  // the DC mode: the slots' exact DC values replace F(0)
+        float2 *pd = sd + rowb * P + my_kc;
+#pragma unroll
+        for (int sl = 0; sl < NS; sl++) pd[sl * kc_n] = make_float2((float)dcv[sl], 0.0f);
+      }
       // this thread's kx run [i0, i0 + mpt) lies in [0, xhalf) or in [xhalf, NX) (xhalf is a multiple
       // of mpt); keep its modes with i <= r or i >= NX - r (r <= xhalf; the others can not reach the
       // top bin): a prefix of a run in the first half, a suffix in the second
       int m_lo = 0, m_hi = mpt;
-      if (i0 < bp.xhalf) m_hi = min(mpt, r + 1 - i0);
-      else m_lo = max(0, bp.nx - r - i0);
-      // Hermitian multiplicity NM (src/main.c:422-429): 2 off the kz = 0 plane; on it 1, except at
-      // kx = NX/2 and, on ky = 0, at kx = 0; a run holds at most one of those
-      const float cyzn = kz != 0 ? 2.0f * cyz : cyz;
+      if (i0 < bp.xhalf) m_hi = min(mpt, col.r + 1 - i0);
+      else m_lo = max(0, bp.nx - col.r - i0);
+      if (m_lo >= m_hi) continue;
+      // Hermitian multiplicity NM (src/main.c:422-429): 2 off the kz = 0 plane (in cyzn); on it 1,
+      // except at kx = NX/2 and, on ky = 0, at kx = 0; a run holds at most one of those
       int isp = -1;
-      if (kz == 0) {
+      if (col.kz == 0) {
         if (bp.xhalf >= i0 && bp.xhalf < i0 + mpt) isp = bp.xhalf;
-        else if (j == 0 && i0 == 0) isp = 0;
-      }
-      if (j == 0 && kz == 0 && i0 == 0) {  // the DC mode: the slots' exact DC values replace F(0)
-        float2 *pd = sd + rowb * P + my_kc;
-#pragma unroll
-        for (int sl = 0; sl < NS; sl++) pd[sl * kc_n] = make_float2((float)dcv[sl], 0.0f);
+        else if (col.j == 0 && i0 == 0) isp = 0;
       }
       float acc[NP][NL];
 #pragma unroll
       for (int qq = 0; qq < NP; qq++)
 #pragma unroll
         for (int l2 = 0; l2 < NL; l2++) acc[qq][l2] = 0.0f;
-      int cur = -2;  // no bin yet: the first mode bisects the edges, later ones walk from the last
+      int cur = -2;  // no bin yet: the first mode guesses, later ones walk from the last
       float lo = 1.0f, hi = 0.0f;
       for (int m = m_lo; m < m_hi; m++) {
         const int i = i0 + m;
         const float2 *pm = sd + (rowb + m * (n >> 3)) * P + my_kc;
         const float4 xt = sxt[xt_index(i)];
-        const float s = xt.x + syz;
+        const float s = xt.x + col.syz;
         if (!(s >= lo && s < hi)) {
-          int b = cur;
-          if (b == -2) {  // sElo[a] <= s < sElo[z] (sElo[0] = -inf, sElo[nk + 2] = +inf)
-            int a = 0, z = nk + 2;
-            while (z - a > 1) {
-              const int mid = (a + z) >> 1;
-              if (sElo[mid] <= s) a = mid;
-              else z = mid;
-            }
-            b = a - 1;
-          }
+          int b = cur == -2 ? guess_bin(bp, sElo, s) : cur;
           while (b < nk && s >= sElo[b + 2]) b++;
           while (b > -1 && s < sEhi[b + 1]) b--;
           if (s >= sElo[b + 1] && s < sEhi[b + 2]) {
             lo = sElo[b + 1];
             hi = sEhi[b + 2];
           } else {  // within a few ulps of an edge: the exact FP64 s decides
-            const double sd2 = __dadd_rn(__dadd_rn(t.fx2d[i], t.fy2d[j]), t.fz2d[kz]);
+            const double sd2 = __dadd_rn(__dadd_rn(t.fx2d[i], t.fy2d[col.j]), t.fz2d[col.kz]);
             b = exact_bin(sE, nk, sd2, b);
             lo = 1.0f;
             hi = 0.0f;
@@ -875,11 +920,12 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
             if (cur >= 0 && cur < nk) {
 #pragma unroll
               for (int qq = 0; qq < NP; qq++)
+                if ((PM >> qq) & 1)
 #pragma unroll
-                for (int l2 = 0; l2 < NL; l2++) {
-                  if (acc[qq][l2] != 0.0f && ((bp.pmask >> qq) & 1)) atomicAdd(&sbw[(qq * NL + l2) * nk + cur], acc[qq][l2]);
-                  acc[qq][l2] = 0.0f;
-                }
+                  for (int l2 = 0; l2 < NL; l2++) {
+                    atomicAdd(&sbw[(qq * NL + l2) * nk + cur], acc[qq][l2]);
+                    acc[qq][l2] = 0.0f;
+                  }
             }
             cur = b;
           }
@@ -889,26 +935,27 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
         float2 B = make_float2(0.0f, 0.0f);
         if (NF == 2) B = pm[kc_n];
         if (IL) {
-          const float2 e = cmulf(make_float2(xt.z, xt.w), eyz);
+          const float2 e = cmulf(make_float2(xt.z, xt.w), col.eyz);
           A = cadd(A, cmulf(pm[NF * kc_n], e));
           if (NF == 2) B = cadd(B, cmulf(pm[3 * kc_n], e));
         }
-        float gc = cyzn * xt.y;
+        float gc = col.cyzn * xt.y;
         if (i == isp) gc *= 2.0f;
-        const float fl = bp.los == 1 ? sfx[i] : flos_yz;
+        const float fl = bp.los == 1 ? sfx[i] : col.flos;
         const float mu = s > 0.0f ? fl * rsqrtf(s) : 0.0f;
         const float mu2 = mu * mu;
         const float L2 = 1.5f * mu2 - 0.5f;
         const float L4 = (4.375f * mu2 - 3.75f) * mu2 + 0.375f;
         float Pq[NP];
-        Pq[0] = (A.x * A.x + A.y * A.y) * gc;
+        if (PM & 1) Pq[0] = (A.x * A.x + A.y * A.y) * gc;
         if (NF == 2) {
-          Pq[1] = (A.x * B.x + A.y * B.y) * gc;
-          Pq[2] = (A.x * B.y - A.y * B.x) * gc;
-          Pq[3] = (B.x * B.x + B.y * B.y) * gc;
+          if (PM & 2) Pq[1] = (A.x * B.x + A.y * B.y) * gc;
+          if (PM & 4) Pq[2] = (A.x * B.y - A.y * B.x) * gc;
+          if (PM & 8) Pq[3] = (B.x * B.x + B.y * B.y) * gc;
         }
 #pragma unroll
         for (int qq = 0; qq < NP; qq++) {
+          if (!((PM >> qq) & 1)) continue;
           acc[qq][0] += Pq[qq];
           acc[qq][1] += Pq[qq] * L2;
           acc[qq][2] += Pq[qq] * L4;
@@ -921,21 +968,34 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
       if (cur >= 0 && cur < nk) {
 #pragma unroll
         for (int qq = 0; qq < NP; qq++)
+          if ((PM >> qq) & 1)
 #pragma unroll
-          for (int l2 = 0; l2 < NL; l2++)
-            if (acc[qq][l2] != 0.0f && ((bp.pmask >> qq) & 1)) atomicAdd(&sbw[(qq * NL + l2) * nk + cur], acc[qq][l2]);
+            for (int l2 = 0; l2 < NL; l2++) atomicAdd(&sbw[(qq * NL + l2) * nk + cur], acc[qq][l2]);
+      }
+    }
+    // every 4 blocks, the FP32 block bins (a few hundred modes per bin at most) are added into the
+    // CTA's FP64 bins and cleared; the next block's first barrier orders the clearing before its flushes
+    if ((++nproc & 3) == 0) {
+      __syncthreads();
+      for (int c = threadIdx.x; c < nbins; c += blockDim.x) {
+        float v = 0.0f;
+        for (int k = 0; k < xg.nbc; k++) {
+          v += sb[c + k * nbins];
+          sb[c + k * nbins] = 0.0f;
+        }
+        sbd[c] += (double)v;
       }
     }
   }
   __syncthreads();
-  // CTA bins (the sum of the copies) -> global FP64 bins [product][5][nk]; stored multipole index -> l
+  // CTA bins (FP64) -> global FP64 bins [product][5][nk]; stored multipole index -> l
   for (int c = threadIdx.x; c < nbins; c += blockDim.x) {
-    float v = 0.0f;
-    for (int k = 0; k < xg.nbc; k++) v += sb[c + k * nbins];
-    if (v == 0.0f) continue;
+    double v = sbd[c];
+    for (int k = 0; k < xg.nbc; k++) v += (double)sb[c + k * nbins];
+    if (v == 0.0) continue;
     const int b = c % nk, ql = c / nk, qq = ql / NL, li = ql - qq * NL;
     const int l = li == 0 ? 0 : (li == 1 ? 2 : (li == 2 ? 4 : (li == 3 ? 1 : 3)));
-    atomicAdd(&bins[(qq * 5 + l) * nk + b], (double)v);
+    atomicAdd(&bins[(qq * 5 + l) * nk + b], v);
   }
 }
 
@@ -1130,39 +1190,54 @@ bool xbin_plan(const BinParams &bp, int nslot, XbinGeo &xg, bool transposed) {
   return xbin_smem_layout(xg.log2n, xg.ncol, np, nl, bp.nk, xg.nbc).total <= 220 * 1024;
 }
 
-template <int NF, bool IL, bool ODD>
+template <int NF, bool IL, bool ODD, int PM>
 static void launch_xbin_t(cudaStream_t s, const BinParams &bp, const BinTables &t, const XbinGeo &xg,
                           void *const slots[4], const double *dcv, double *bins) {
   constexpr int NP = NF == 1 ? 1 : 4, NL = ODD ? 5 : 3;
   const size_t smem = xbin_smem_layout(xg.log2n, xg.ncol, NP, NL, bp.nk, xg.nbc).total;
-  cudaFuncSetAttribute(k_xfft_bin<NF, IL, ODD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(k_xfft_bin<NF, IL, ODD, PM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_xfft_bin<NF, IL, ODD>, XBIN_THREADS, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_xfft_bin<NF, IL, ODD, PM>, XBIN_THREADS, smem);
   int dev = 0, nsm = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   int grid = (per_sm > 0 ? per_sm : 1) * nsm;
   if (grid > xg.nblocks) grid = xg.nblocks;
-  k_xfft_bin<NF, IL, ODD><<<grid, XBIN_THREADS, smem, s>>>(bp, t, xg, (const float2 *)slots[0],
-                                                            (const float2 *)slots[1], (const float2 *)slots[2],
-                                                            (const float2 *)slots[3], dcv, bins);
+  k_xfft_bin<NF, IL, ODD, PM><<<grid, XBIN_THREADS, smem, s>>>(bp, t, xg, (const float2 *)slots[0],
+                                                                (const float2 *)slots[1], (const float2 *)slots[2],
+                                                                (const float2 *)slots[3], dcv, bins);
+}
+
+// Two fields: the products dd + dp + pp read (|A|^2, Im A*B, |B|^2), or all four.
+template <bool IL, bool ODD>
+static void launch_xbin_f2(cudaStream_t s, const BinParams &bp, const BinTables &t, const XbinGeo &xg,
+                           void *const slots[4], const double *dcv, double *bins) {
+  if ((bp.pmask & ~0xD) == 0) launch_xbin_t<2, IL, ODD, 0xD>(s, bp, t, xg, slots, dcv, bins);
+  else launch_xbin_t<2, IL, ODD, 0xF>(s, bp, t, xg, slots, dcv, bins);
 }
 
 void launch_xbin(cudaStream_t s, const BinParams &bp, const BinTables &t, const XbinGeo &xg, void *const slots[4],
                  const double *dcv, double *bins, long long *launches) {
   const bool il = bp.interlace != 0, odd = bp.odd != 0;
   if (bp.nfields == 2) {
-    if (il) odd ? launch_xbin_t<2, true, true>(s, bp, t, xg, slots, dcv, bins)
-            : launch_xbin_t<2, true, false>(s, bp, t, xg, slots, dcv, bins);
-    else odd ? launch_xbin_t<2, false, true>(s, bp, t, xg, slots, dcv, bins)
-             : launch_xbin_t<2, false, false>(s, bp, t, xg, slots, dcv, bins);
+    if (il) odd ? launch_xbin_f2<true, true>(s, bp, t, xg, slots, dcv, bins)
+            : launch_xbin_f2<true, false>(s, bp, t, xg, slots, dcv, bins);
+    else odd ? launch_xbin_f2<false, true>(s, bp, t, xg, slots, dcv, bins)
+             : launch_xbin_f2<false, false>(s, bp, t, xg, slots, dcv, bins);
   } else {
-    if (il) odd ? launch_xbin_t<1, true, true>(s, bp, t, xg, slots, dcv, bins)
-            : launch_xbin_t<1, true, false>(s, bp, t, xg, slots, dcv, bins);
-    else odd ? launch_xbin_t<1, false, true>(s, bp, t, xg, slots, dcv, bins)
-             : launch_xbin_t<1, false, false>(s, bp, t, xg, slots, dcv, bins);
+    if (il) odd ? launch_xbin_t<1, true, true, 1>(s, bp, t, xg, slots, dcv, bins)
+            : launch_xbin_t<1, true, false, 1>(s, bp, t, xg, slots, dcv, bins);
+    else odd ? launch_xbin_t<1, false, true, 1>(s, bp, t, xg, slots, dcv, bins)
+             : launch_xbin_t<1, false, false, 1>(s, bp, t, xg, slots, dcv, bins);
   }
   (*launches)++;
+}
+
+void bin_params_kguess(BinParams &bp, const capow_params &p) {
+  const double bw = (p.Maxk - p.Mink) / (double)p.NK;
+  bp.lg = p.OutputLog ? 1 : 0;
+  bp.kscale = (float)(2.0 * M_PI / bw);
+  bp.koff = (float)(-p.Mink / bw);
 }
 
 void launch_mode_counts(cudaStream_t s, const BinParams &bp, const BinTables &t, unsigned long long *nmodes,

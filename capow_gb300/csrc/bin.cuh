@@ -53,7 +53,15 @@ struct BinParams {
   int pmask;                // products the spectra read (bit q: |A|^2, Re A*B, Im A*B, |B|^2)
   double two_pi;
   float fx_step;            // x frequency spacing 1/((float)NX*dx) (src/main.c:329), for per-column x ranges
+  // first guess of a mode's bin from FP32 s = |f|^2 for linear bins: (int)(sqrtf(s) * kscale + koff), i.e.
+  // (2 pi |f| - Mink) / binwidth (src/main.c:369-373); lg = 1 (log bins) bisects instead. The guess only
+  // starts the walk over the safe FP32 edges, so its rounding does not matter.
+  float kscale, koff;
+  int lg;
 };
+
+// Fill kscale, koff and lg of bp for a run's k binning.
+void bin_params_kguess(BinParams &bp, const capow_params &p);
 
 // Host: exact k-bin of one |k|^2 value s, following src/main.c:355, 369-375.
 // Returns -1 (below), 0..NK-1, or NK (above or beyond Nyquist).

@@ -225,6 +225,7 @@ extern "C" int capow_create(const capow_params *p, const capow_options *opt, cap
   bp.odd = p->Odd_Multipoles; bp.out2d = p->Output2D; bp.nfields = c->fs.nfields;
   bp.two_pi = 2.0 * M_PI;
   bp.fx_step = (float)(1.0 / ((float)p->NX * c->g.dx));
+  bin_params_kguess(bp, *p);
   if (build_bin_tables(*p, c->g, c->prec, c->bt, c->allocs, c->stream)) FAIL(c, CAPOW_ENOMEM, "bin tables");
   CK(c, cudaMemsetAsync(c->nmodes_d, 0, sizeof(unsigned long long) * nk, c->stream));
   CK(c, cudaMemsetAsync(c->nmodes2d_d, 0, sizeof(unsigned long long) * (n2d ? n2d : 1), c->stream));
