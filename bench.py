@@ -258,8 +258,9 @@ def batch_bench(args):
     """The batched-mocks workload: 256 mocks, box L ~ U[500, 1500] Mpc/h, grid from {128^3, 192^3, 256^3},
     particle counts log-uniform in [0.5M, 8M] (cube lattices), Zel'dovich-displaced as the main workload
     (rms 1.5 cells of each grid), CIC and TSC alternating, interlaced, density P0/P2/P4 with LOS = z,
-    FP32. One capow_batch call (CUDA graph + tile autotuner) against 256 sequential plain-path runs
-    (create, paint, power, destroy per mock). Prints one JSON line in mocks per second."""
+    FP32. capow_batch calls (tile autotuner; direct enqueue and the cached CUDA graph; the first call,
+    which sets the batch up, timed apart) against 256 sequential plain-path runs (create, paint, power,
+    destroy per mock). Prints one JSON line in mocks per second."""
     import torch
 
     import capow_gb300 as cg
@@ -280,15 +281,25 @@ def batch_bench(args):
         mocks.append((p, parts))
     npart = sum(len(m[1][0]) for m in mocks)
     torch.cuda.synchronize()
-    # warm-up: module loading, and the autotuner's choice per grid shape (kept for later calls)
-    cg.run_batch(mocks, precision="fp32", graph=False, autotune=True)
-    times = {}
-    for graph in (False, True):
+
+    def timed(graph):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         out = cg.run_batch(mocks, precision="fp32", graph=graph, autotune=True)
         torch.cuda.synchronize()
-        times[graph] = time.perf_counter() - t0
+        return time.perf_counter() - t0, out
+
+    # the first call sets up the batch (shared contexts, tables, the autotuner's tile choice); later
+    # calls with the same mocks reuse that state; the first graph call also captures the graph
+    cg.release_batch()
+    t_cold, _ = timed(False)
+    t_direct = statistics.median(timed(False)[0] for _ in range(3))
+    t_graph_first, _ = timed(True)
+    reps = [timed(True) for _ in range(3)]
+    t_graph = statistics.median(r[0] for r in reps)
+    out = reps[-1][1]
+    cg.release_batch()
+    times = {False: t_direct, True: t_graph}
     graph_best = times[True] < times[False]
     t_batch = times[graph_best]
     ok = sum(1 for s, _ in out if s == cg.OK)
@@ -302,7 +313,8 @@ def batch_bench(args):
     line = {"metric": "mocks per second, 256 uneven periodic mocks (batched)", "value": round(len(mocks) / t_batch, 2),
             "unit": "mocks/s", "higher_is_better": True, "n_gpus": 1, "mocks": len(mocks), "mocks_ok": ok,
             "particles": int(npart), "batch_s": round(t_batch, 3), "batch_s_graph": round(times[True], 3),
-            "batch_s_direct": round(times[False], 3), "sequential_s": round(t_seq, 3),
+            "batch_s_direct": round(times[False], 3), "batch_s_first_call": round(t_cold, 3),
+            "batch_s_first_graph_call": round(t_graph_first, 3), "sequential_s": round(t_seq, 3),
             "sequential_mocks_per_s": round(len(mocks) / t_seq, 2), "speedup": round(t_seq / t_batch, 2),
             "data": "synthetic (seeded Zel'dovich lattices)", "dtype": "f32",
             "config": {"workload": "256 mocks, L~U[500,1500], grid in {128,192,256}^3, N_p log-uniform 0.5M-8M, "

@@ -34,7 +34,7 @@ OK, EINVAL, ENOMEM, ECUDA, EBOUNDS, ETIMEOUT, ESTATE, ECUFFT, ENOTSUP = range(9)
 FP64, FP32_MIXED, FP32_DETERMINISTIC = 0, 1, 2
 SPEC_REFERENCE, SPEC_DD, SPEC_DP, SPEC_PP = 0, 1, 2, 4
 F32, F64 = 0, 1
-FFT_AUTO, FFT_3D = 0, 1
+FFT_AUTO, FFT_3D, FFT_ONE_LAUNCH = 0, 1, 2
 PRECISIONS = {"fp64": FP64, "fp32": FP32_MIXED, "det": FP32_DETERMINISTIC}
 
 
@@ -98,6 +98,7 @@ EXPORTS = [
     "capow_copy_grid", "capow_stage_ms", "capow_kernel_launches", "capow_destroy", "capow_read_params",
     "capow_read_catalogue", "capow_free", "capow_write_output", "capow_bin_centre", "capow_strerror",
     "capow_last_error", "capow_paint_noalloc", "capow_backward", "capow_batch", "capow_tile_kernel_ms",
+    "capow_batch_release",
 ]
 
 _lib = None
@@ -119,6 +120,8 @@ def lib() -> ctypes.CDLL:
     L.capow_paint_noalloc.argtypes = [vp, ctypes.POINTER(_Particles)]
     L.capow_get_stats.argtypes = [vp, ctypes.POINTER(_Stats)]
     L.capow_batch.argtypes = [ctypes.POINTER(_Mock), ip, O, ip]
+    L.capow_batch_release.restype = None
+    L.capow_batch_release.argtypes = []
     L.capow_backward.argtypes = [vp, ctypes.POINTER(ctypes.POINTER(ctypes.c_double) * 5), ctypes.POINTER(_Grads)]
     L.capow_power.argtypes = [vp, ctypes.POINTER(_Spectrum), ip]
     L.capow_normalise.argtypes = [P, ctypes.POINTER(_Spectrum)]
@@ -234,7 +237,8 @@ class PowerSpectrum:
     """One capow context: paint a catalogue, then P_l(k) for the requested spectra.
 
     precision: "fp32" (FP32-mixed, default), "fp64" (plain double path), "det" (int64 fixed-point grids).
-    fft_path:  "auto" (fused x-axis FFT + binning where it applies) or "3d" (3-D cuFFT + binning kernel).
+    fft_path:  "auto" (fused x-axis FFT + binning where it applies), "3d" (3-D cuFFT + binning kernel) or
+               "one_launch" (as auto, with the z and y axes in one launch where NY and NZ are powers of two).
     spectra:   None -> one spectrum chosen by params.Momentum (one reference run); or any of
                ("dd", "dp", "pp") computed from one paint and one set of FFTs.
     """
@@ -248,7 +252,7 @@ class PowerSpectrum:
             mask |= {"dd": SPEC_DD, "dp": SPEC_DP, "pp": SPEC_PP}[s]
         self.spectra_mask = mask
         opt = _Options(PRECISIONS[precision], mask, device, ctypes.c_void_p(stream or 0),
-                       {"auto": FFT_AUTO, "3d": FFT_3D}[fft_path])
+                       {"auto": FFT_AUTO, "3d": FFT_3D, "one_launch": FFT_ONE_LAUNCH}[fft_path])
         self._ctx = ctypes.c_void_p()
         rc = lib().capow_create(ctypes.byref(self._pc), ctypes.byref(opt), ctypes.byref(self._ctx))
         if rc != OK:
@@ -427,9 +431,15 @@ def run(params: Params, x, y, z, vlos=None, w=None, precision: str = "fp32", spe
         return ps.power()
 
 
+def release_batch() -> None:
+    """capow_batch_release: free the device state capow_batch keeps between calls."""
+    lib().capow_batch_release()
+
+
 def run_batch(mocks, precision: str = "fp32", spectra=None, graph: bool = False, autotune: bool = False,
               device: int = 0, stream=None):
-    """capow_batch: many independent mocks in one call.
+    """capow_batch: many independent mocks in one call (the device state and graph of the batch are kept
+    for a later call with the same mocks' parameters and sizes; release_batch frees them).
 
     mocks: list of (Params, (x, y, z, vlos, w)) with device arrays (vlos, w may be None).
     Returns a list of (status, [spectrum dict, ...]) in input order; the dicts hold raw sums as

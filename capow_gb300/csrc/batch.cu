@@ -21,11 +21,13 @@
 
 namespace {
 
-typedef std::tuple<int, int, int, int, int, int, int, int, int, int, int, double, double> ShapeKey;
+// What the shared device resources of a context depend on: the grid shape (grids, plans, tile tables),
+// the painted fields (LOS, Momentum) and the binning kernel's variant (odd multipoles). The box, the
+// interpolation order and the k bins are per mock (geometry, tables and bins are bound per mock).
+typedef std::tuple<int, int, int, int, int, int, int> ShapeKey;
 
 ShapeKey shape_of(const capow_params &p) {
-  return ShapeKey(p.NX, p.NY, p.NZ, p.InterpOrder, p.DoInterlacing, p.NK, p.LOS, p.Momentum, p.Odd_Multipoles,
-                  p.Output2D, p.OutputLog, p.Mink, p.Maxk);
+  return ShapeKey(p.NX, p.NY, p.NZ, p.DoInterlacing, p.LOS, p.Momentum, p.Odd_Multipoles);
 }
 
 struct MockDev {
@@ -35,6 +37,7 @@ struct MockDev {
   unsigned long long *nmodes;
   Geom g;
   BinParams bp;
+  XbinGeo xg;  // the fused binning pass's blocks for this mock's bins
 };
 
 // Candidate tile shapes for the FP32 paint: the int32 tiles of every slot within 64 KB per CTA.
@@ -50,6 +53,7 @@ void bind_mock(capow_ctx *c, const capow_params &p, const MockDev &m) {
   c->g = m.g;
   c->bp = m.bp;
   c->bt = m.bt;
+  if (c->fused) c->xg = m.xg;
   c->st = m.st;
   c->dcv = m.dcv;
   c->bins = m.bins;
@@ -74,119 +78,199 @@ int time_paint(capow_ctx *c, const capow_particles &d, float *ms) {
 std::mutex g_tuned_mu;
 std::map<ShapeKey, TileGeo> g_tuned;
 
-}  // namespace
-
-extern "C" int capow_batch(capow_mock *mocks, int nmocks, const capow_options *opt, int flags) {
-  if (!mocks || nmocks < 0) return CAPOW_EINVAL;
-  if (nmocks == 0) return CAPOW_OK;
-  capow_options o;
-  memset(&o, 0, sizeof o);
-  if (opt) o = *opt;
-  else o.precision = CAPOW_FP32_MIXED;
-  if (cudaSetDevice(o.device) != cudaSuccess) return CAPOW_ECUDA;
-  for (int i = 0; i < nmocks; i++) {
-    mocks[i].status = CAPOW_OK;
-    if (!mocks[i].parts.on_device || !mocks[i].out || mocks[i].params.Output2D) mocks[i].status = CAPOW_EINVAL;
-  }
-  // ---- one context per grid shape, on one stream
-  cudaStream_t stream = (cudaStream_t)o.stream;
+// The device state of one batch signature (the mocks' parameters, sizes and array kinds, the options
+// and flags): shared contexts, per-mock tables and outputs, and the instantiated graph. It is kept
+// after the call, so that a later call with the same signature (new particle values, or new arrays of
+// the same sizes) only launches: the graph as it is when the arrays are the same, or updated in place
+// (cudaGraphExecUpdate) when they moved. A call with another signature, or capow_batch_release,
+// frees it.
+struct BatchState {
+  std::vector<unsigned char> sig;
+  cudaStream_t stream = nullptr;
   bool own_stream = false;
-  if (!stream) {
-    if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return CAPOW_ECUDA;
-    own_stream = true;
+  std::map<ShapeKey, capow_ctx *> ctxs;
+  std::vector<capow_ctx *> ctx_of;
+  std::vector<int> status0;  // per-mock status found while setting up (e.g. CAPOW_ENOTSUP)
+  std::vector<MockDev> md;
+  std::vector<size_t> bins_off, nm_off;
+  size_t per = 0, bins_total = 0, nm_total = 0;
+  char *arena = nullptr;
+  double *bins_d = nullptr;
+  unsigned long long *nm_d = nullptr;
+  void *tab_dev = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<const void *> ptrs;  // the particle arrays the graph holds
+};
+
+std::mutex g_batch_mu;
+BatchState *g_batch = nullptr;
+
+void free_batch_state(BatchState *b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (auto &kv : b->ctxs) capow_destroy(kv.second);
+  if (b->tab_dev) cudaFree(b->tab_dev);
+  if (b->arena) cudaFree(b->arena);
+  if (b->own_stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+template <typename T>
+void put(std::vector<unsigned char> &v, const T &x) {
+  const unsigned char *p = (const unsigned char *)&x;
+  v.insert(v.end(), p, p + sizeof(T));
+}
+
+std::vector<unsigned char> batch_signature(const capow_mock *mocks, int nmocks, const capow_options &o, int flags) {
+  std::vector<unsigned char> s;
+  put(s, o.precision);
+  put(s, o.spectra);
+  put(s, o.device);
+  put(s, o.stream);
+  put(s, o.fft_path);
+  put(s, flags & CAPOW_BATCH_AUTOTUNE);
+  put(s, nmocks);
+  for (int i = 0; i < nmocks; i++) {
+    const capow_params &p = mocks[i].params;  // field by field: the struct's padding is not compared
+    const int ints[] = {p.NX, p.NY, p.NZ, p.InterpOrder, p.DoInterlacing, p.NK, p.NMU, p.Output2D, p.OutputLog,
+                        p.LOS, p.Momentum, p.Odd_Multipoles};
+    const double dbls[] = {p.XMIN, p.XMAX, p.YMIN, p.YMAX, p.ZMIN, p.ZMAX, p.Mink, p.Maxk, p.Omega_m, p.Redshift};
+    put(s, ints);
+    put(s, dbls);
+    put(s, mocks[i].parts.n);
+    put(s, mocks[i].parts.dtype);
+    put(s, mocks[i].parts.on_device);
+    put(s, mocks[i].parts.vlos != nullptr);
+    put(s, mocks[i].parts.w != nullptr);
+  }
+  return s;
+}
+
+std::vector<const void *> batch_pointers(const capow_mock *mocks, int nmocks) {
+  std::vector<const void *> p;
+  for (int i = 0; i < nmocks; i++) {
+    p.push_back(mocks[i].parts.x);
+    p.push_back(mocks[i].parts.y);
+    p.push_back(mocks[i].parts.z);
+    p.push_back(mocks[i].parts.vlos);
+    p.push_back(mocks[i].parts.w);
+  }
+  return p;
+}
+
+// Contexts, tables, buffers and tuning of a new signature. Returns a status; per-mock problems go to
+// b->status0.
+int setup_batch(BatchState *b, const capow_mock *mocks, int nmocks, const capow_options &o, int flags) {
+  b->status0.assign(nmocks, CAPOW_OK);
+  for (int i = 0; i < nmocks; i++)
+    if (!mocks[i].parts.on_device || !mocks[i].out || mocks[i].params.Output2D) b->status0[i] = CAPOW_EINVAL;
+  b->stream = (cudaStream_t)o.stream;
+  if (!b->stream) {
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return CAPOW_ECUDA;
+    b->own_stream = true;
   }
   capow_options so = o;
-  so.stream = stream;
-  std::map<ShapeKey, capow_ctx *> ctxs;
+  so.stream = b->stream;
   std::map<ShapeKey, unsigned long long> nmax;
   std::map<ShapeKey, bool> wts;
-  std::vector<capow_ctx *> ctx_of(nmocks, nullptr);
-  int rc = CAPOW_OK;
+  b->ctx_of.assign(nmocks, nullptr);
+  // the shared context of a shape is created for its largest interpolation order (the record buffers
+  // are sized for the widest footprint)
+  std::map<ShapeKey, int> max_order;
+  for (int i = 0; i < nmocks; i++)
+    if (!b->status0[i]) {
+      int &mo = max_order[shape_of(mocks[i].params)];
+      mo = std::max(mo, mocks[i].params.InterpOrder);
+    }
   for (int i = 0; i < nmocks; i++) {
-    if (mocks[i].status) continue;
+    if (b->status0[i]) continue;
     const ShapeKey k = shape_of(mocks[i].params);
-    if (!ctxs.count(k)) {
+    if (!b->ctxs.count(k)) {
       capow_ctx *c = nullptr;
-      const int r = capow_create(&mocks[i].params, &so, &c);
+      capow_params cp = mocks[i].params;
+      cp.InterpOrder = max_order[k];
+      const int r = capow_create(&cp, &so, &c);
       if (r) {
         if (c) capow_destroy(c);
-        mocks[i].status = r;
+        b->status0[i] = r;
         continue;
       }
       c->quiet = true;
       c->two_pass = true;  // record buffers sized once per shape (prepare_paint_buffers)
-      ctxs[k] = c;
+      b->ctxs[k] = c;
     }
-    ctx_of[i] = ctxs[k];
+    b->ctx_of[i] = b->ctxs[k];
     nmax[k] = std::max(nmax[k], (unsigned long long)mocks[i].parts.n);
     wts[k] = wts[k] || mocks[i].parts.w != nullptr;
   }
   // ---- per-mock tables and output buffers (one device arena for the small per-mock arrays)
-  const size_t per = ((sizeof(DevStats) + 255) & ~(size_t)255) + 256;  // counters + 4 DC values
-  std::vector<MockDev> md(nmocks);
+  b->per = ((sizeof(DevStats) + 255) & ~(size_t)255) + 256;  // counters + 4 DC values
+  b->md.assign(nmocks, MockDev());
   std::vector<unsigned char> blob;  // every mock's bin tables, uploaded once
   std::vector<size_t> tab_off(nmocks, 0);
-  void *tab_dev = nullptr;
-  size_t bins_total = 0, nm_total = 0;
-  std::vector<size_t> bins_off(nmocks, 0), nm_off(nmocks, 0);
+  b->bins_off.assign(nmocks, 0);
+  b->nm_off.assign(nmocks, 0);
   for (int i = 0; i < nmocks; i++) {
-    if (!ctx_of[i]) continue;
-    bins_off[i] = bins_total;
-    nm_off[i] = nm_total;
-    bins_total += (size_t)NPROD * 5 * mocks[i].params.NK;
-    nm_total += mocks[i].params.NK;
+    if (!b->ctx_of[i]) continue;
+    b->bins_off[i] = b->bins_total;
+    b->nm_off[i] = b->nm_total;
+    b->bins_total += (size_t)NPROD * 5 * mocks[i].params.NK;
+    b->nm_total += mocks[i].params.NK;
   }
-  char *arena = nullptr;
-  double *bins_d = nullptr;
-  unsigned long long *nm_d = nullptr;
-  const size_t arena_bytes = per * nmocks + 8 * bins_total + 8 * nm_total + 512;
-  if (cudaMalloc(&arena, arena_bytes) != cudaSuccess) rc = CAPOW_ENOMEM;
-  if (!rc) {
-    bins_d = (double *)(arena + ((per * nmocks + 255) & ~(size_t)255));
-    nm_d = (unsigned long long *)(bins_d + bins_total);
-  }
-  for (int i = 0; i < nmocks && !rc; i++) {
-    capow_ctx *c = ctx_of[i];
+  const size_t arena_bytes = b->per * nmocks + 8 * b->bins_total + 8 * b->nm_total + 512;
+  if (cudaMalloc((void **)&b->arena, arena_bytes) != cudaSuccess) return CAPOW_ENOMEM;
+  b->bins_d = (double *)(b->arena + ((b->per * nmocks + 255) & ~(size_t)255));
+  b->nm_d = (unsigned long long *)(b->bins_d + b->bins_total);
+  for (int i = 0; i < nmocks; i++) {
+    capow_ctx *c = b->ctx_of[i];
     if (!c) continue;
     const capow_params &p = mocks[i].params;
-    MockDev &m = md[i];
+    MockDev &m = b->md[i];
     m.g = make_geom(p);
     if (c->prec != CAPOW_FP64 && !(m.g.margin < 0.25f)) {
-      mocks[i].status = CAPOW_ENOTSUP;
-      ctx_of[i] = nullptr;
+      b->status0[i] = CAPOW_ENOTSUP;
+      b->ctx_of[i] = nullptr;
       continue;
     }
     m.bp = c->bp;
+    m.bp.nk = p.NK;
+    m.bp.out2d = p.Output2D;
     m.bp.fx_step = (float)(1.0 / ((float)p.NX * m.g.dx));
     bin_params_kguess(m.bp, p);
+    if (c->fused && !xbin_plan(m.bp, c->nslot, m.xg, c->xtr)) {  // this mock's bins do not fit the pass
+      b->status0[i] = CAPOW_ENOTSUP;
+      b->ctx_of[i] = nullptr;
+      continue;
+    }
     tab_off[i] = (blob.size() + 255) & ~(size_t)255;
     blob.resize(tab_off[i]);
     std::vector<unsigned char> one;
     if (build_bin_tables_packed(p, m.g, c->prec, m.bt, one)) {
-      mocks[i].status = CAPOW_ENOMEM;
-      ctx_of[i] = nullptr;
+      b->status0[i] = CAPOW_ENOMEM;
+      b->ctx_of[i] = nullptr;
       continue;
     }
     blob.insert(blob.end(), one.begin(), one.end());
-    m.st = (DevStats *)(arena + per * i);
-    m.dcv = (double *)(arena + per * i + ((sizeof(DevStats) + 255) & ~(size_t)255));
-    m.bins = bins_d + bins_off[i];
-    m.nmodes = nm_d + nm_off[i];
+    m.st = (DevStats *)(b->arena + b->per * i);
+    m.dcv = (double *)(b->arena + b->per * i + ((sizeof(DevStats) + 255) & ~(size_t)255));
+    m.bins = b->bins_d + b->bins_off[i];
+    m.nmodes = b->nm_d + b->nm_off[i];
   }
-  if (!rc && !blob.empty()) {
-    if (cudaMalloc(&tab_dev, blob.size()) != cudaSuccess ||
-        cudaMemcpyAsync(tab_dev, blob.data(), blob.size(), cudaMemcpyHostToDevice, stream) != cudaSuccess)
-      rc = CAPOW_ENOMEM;
-    for (int i = 0; i < nmocks && !rc; i++)
-      if (ctx_of[i]) relocate_bin_tables(md[i].bt, (const char *)tab_dev + tab_off[i]);
+  if (!blob.empty()) {
+    if (cudaMalloc(&b->tab_dev, blob.size()) != cudaSuccess ||
+        cudaMemcpyAsync(b->tab_dev, blob.data(), blob.size(), cudaMemcpyHostToDevice, b->stream) != cudaSuccess)
+      return CAPOW_ENOMEM;
+    for (int i = 0; i < nmocks; i++)
+      if (b->ctx_of[i]) relocate_bin_tables(b->md[i].bt, (const char *)b->tab_dev + tab_off[i]);
   }
   // ---- record buffers for the largest catalogue of each shape; the tile autotuner (its choice is
   // kept per grid shape for later calls)
-  for (auto &kv : ctxs) {
-    if (rc) break;
+  for (auto &kv : b->ctxs) {
     capow_ctx *c = kv.second;
-    rc = prepare_paint_buffers(c, nmax[kv.first], wts[kv.first]);
-    if (rc || !(flags & CAPOW_BATCH_AUTOTUNE) || c->prec != CAPOW_FP32_MIXED) continue;
+    int rc = prepare_paint_buffers(c, nmax[kv.first], wts[kv.first]);
+    if (rc) return rc;
+    if (!(flags & CAPOW_BATCH_AUTOTUNE) || c->prec != CAPOW_FP32_MIXED) continue;
     {
       std::lock_guard<std::mutex> lock(g_tuned_mu);
       auto it = g_tuned.find(kv.first);
@@ -197,14 +281,14 @@ extern "C" int capow_batch(capow_mock *mocks, int nmocks, const capow_options *o
     }
     int first = -1;
     for (int i = 0; i < nmocks; i++)
-      if (ctx_of[i] == c) {
+      if (b->ctx_of[i] == c) {
         first = i;
         break;
       }
     if (first < 0) continue;
     const TileGeo keep = c->tg;
     const PaintBufs keep_pb = c->pb;
-    bind_mock(c, mocks[first].params, md[first]);
+    bind_mock(c, mocks[first].params, b->md[first]);
     TileGeo best = keep;
     float best_ms = 1e30f;
     for (auto &cand : tile_candidates(c->nslot)) {
@@ -223,94 +307,150 @@ extern "C" int capow_batch(capow_mock *mocks, int nmocks, const capow_options *o
     std::lock_guard<std::mutex> lock(g_tuned_mu);
     g_tuned[kv.first] = best;
   }
-  // ---- enqueue every mock (optionally captured as one graph)
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  bool captured = false;
-  if (!rc && (flags & CAPOW_BATCH_GRAPH)) {
-    // one uncaptured pass over the first mock of each shape: every kernel and plan the graph will
-    // hold has run once before the capture starts
-    for (auto &kv : ctxs) {
+  // ---- one uncaptured pass over the first mock of each shape: every kernel and plan a graph holds
+  // has run once before a capture starts
+  if (flags & CAPOW_BATCH_GRAPH) {
+    for (auto &kv : b->ctxs) {
       capow_ctx *c = kv.second;
       for (int i = 0; i < nmocks; i++) {
-        if (ctx_of[i] != c) continue;
-        bind_mock(c, mocks[i].params, md[i]);
+        if (b->ctx_of[i] != c) continue;
+        bind_mock(c, mocks[i].params, b->md[i]);
         capow_particles d = mocks[i].parts;
         if (!c->fs.need_v) d.vlos = nullptr;
-        launch_mode_counts(stream, c->bp, c->bt, md[i].nmodes, nullptr, &c->launches);
-        rc = enqueue_paint(c, d);
+        launch_mode_counts(b->stream, c->bp, c->bt, b->md[i].nmodes, nullptr, &c->launches);
+        int rc = enqueue_paint(c, d);
         if (!rc) rc = enqueue_power_kernels(c);
+        if (rc) return rc;
         break;
       }
-      if (rc) break;
     }
   }
-  if (!rc) {
-    cudaStreamSynchronize(stream);  // table uploads, tuning and warm-up done
-    if ((flags & CAPOW_BATCH_GRAPH) &&
-        cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess)
-      captured = true;
-    for (int i = 0; i < nmocks && !rc; i++) {
-      capow_ctx *c = ctx_of[i];
-      if (!c) continue;
-      bind_mock(c, mocks[i].params, md[i]);
-      const int nk = mocks[i].params.NK;
-      cudaMemsetAsync(md[i].nmodes, 0, sizeof(unsigned long long) * nk, stream);
-      launch_mode_counts(stream, c->bp, c->bt, md[i].nmodes, nullptr, &c->launches);
-      capow_particles d = mocks[i].parts;
-      if (!c->fs.need_v) d.vlos = nullptr;
-      int r = enqueue_paint(c, d);
-      if (!r) r = enqueue_power_kernels(c);
-      if (r) mocks[i].status = r;
-    }
-    if (captured) {
-      const cudaError_t e = cudaStreamEndCapture(stream, &graph);
-      if (e != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess ||
-          cudaGraphLaunch(exec, stream) != cudaSuccess)
-        rc = CAPOW_ECUDA;
-    }
-    if (!rc && cudaStreamSynchronize(stream) != cudaSuccess) rc = CAPOW_ECUDA;
+  return cudaStreamSynchronize(b->stream) == cudaSuccess ? CAPOW_OK : CAPOW_ECUDA;
+}
+
+// Every mock's kernels on the batch stream (no host synchronisation, no allocation).
+int enqueue_batch(BatchState *b, capow_mock *mocks, int nmocks) {
+  for (int i = 0; i < nmocks; i++) {
+    capow_ctx *c = b->ctx_of[i];
+    if (!c) continue;
+    bind_mock(c, mocks[i].params, b->md[i]);
+    const int nk = mocks[i].params.NK;
+    cudaMemsetAsync(b->md[i].nmodes, 0, sizeof(unsigned long long) * nk, b->stream);
+    launch_mode_counts(b->stream, c->bp, c->bt, b->md[i].nmodes, nullptr, &c->launches);
+    capow_particles d = mocks[i].parts;
+    if (!c->fs.need_v) d.vlos = nullptr;
+    int r = enqueue_paint(c, d);
+    if (!r) r = enqueue_power_kernels(c);
+    if (r) mocks[i].status = r;
   }
+  return CAPOW_OK;
+}
+
+}  // namespace
+
+extern "C" int capow_batch(capow_mock *mocks, int nmocks, const capow_options *opt, int flags) {
+  if (!mocks || nmocks < 0) return CAPOW_EINVAL;
+  if (nmocks == 0) return CAPOW_OK;
+  capow_options o;
+  memset(&o, 0, sizeof o);
+  if (opt) o = *opt;
+  else o.precision = CAPOW_FP32_MIXED;
+  if (cudaSetDevice(o.device) != cudaSuccess) return CAPOW_ECUDA;
+  std::lock_guard<std::mutex> lock(g_batch_mu);
+  const std::vector<unsigned char> sig = batch_signature(mocks, nmocks, o, flags);
+  BatchState *b = g_batch;
+  int rc = CAPOW_OK;
+  if (!b || b->sig != sig) {  // a new signature: the old state goes, this one is set up
+    free_batch_state(g_batch);
+    g_batch = nullptr;
+    b = new (std::nothrow) BatchState();
+    if (!b) return CAPOW_ENOMEM;
+    b->sig = sig;
+    rc = setup_batch(b, mocks, nmocks, o, flags);
+    if (rc) {
+      free_batch_state(b);
+      return rc;
+    }
+    g_batch = b;
+  }
+  for (int i = 0; i < nmocks; i++) mocks[i].status = b->status0[i];
+  // ---- enqueue every mock: directly, or as the cached graph (captured on first use, updated in
+  // place when the particle arrays moved)
+  if (flags & CAPOW_BATCH_GRAPH) {
+    const std::vector<const void *> ptrs = batch_pointers(mocks, nmocks);
+    if (!b->exec || ptrs != b->ptrs) {
+      cudaGraph_t graph = nullptr;
+      if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return CAPOW_ECUDA;
+      enqueue_batch(b, mocks, nmocks);
+      if (cudaStreamEndCapture(b->stream, &graph) != cudaSuccess) return CAPOW_ECUDA;
+      bool ok = false;
+      if (b->exec) {
+        cudaGraphExecUpdateResultInfo info;
+        ok = cudaGraphExecUpdate(b->exec, graph, &info) == cudaSuccess;
+        if (!ok) {
+          (void)cudaGetLastError();
+          cudaGraphExecDestroy(b->exec);
+          b->exec = nullptr;
+        }
+      }
+      if (!ok) ok = cudaGraphInstantiate(&b->exec, graph, 0) == cudaSuccess;
+      cudaGraphDestroy(graph);
+      if (!ok) {
+        b->exec = nullptr;
+        return CAPOW_ECUDA;
+      }
+      b->ptrs = ptrs;
+      for (int i = 0; i < nmocks; i++)  // statuses set while enqueueing under capture
+        if (mocks[i].status) b->status0[i] = mocks[i].status;
+    }
+    if (cudaGraphLaunch(b->exec, b->stream) != cudaSuccess) return CAPOW_ECUDA;
+  } else {
+    enqueue_batch(b, mocks, nmocks);
+  }
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return CAPOW_ECUDA;
   // ---- read back and fill every mock's spectra (the host side of capow_power)
-  if (!rc) {
-    std::vector<unsigned char> hst(per * nmocks);
-    std::vector<double> hb(bins_total);
-    std::vector<unsigned long long> hnm(nm_total);
-    if (cudaMemcpy(hst.data(), arena, per * nmocks, cudaMemcpyDeviceToHost) != cudaSuccess ||
-        cudaMemcpy(hb.data(), bins_d, 8 * bins_total, cudaMemcpyDeviceToHost) != cudaSuccess ||
-        cudaMemcpy(hnm.data(), nm_d, 8 * nm_total, cudaMemcpyDeviceToHost) != cudaSuccess)
-      rc = CAPOW_ECUDA;
-    for (int i = 0; i < nmocks && !rc; i++) {
-      capow_ctx *c = ctx_of[i];
-      if (!c || mocks[i].status) continue;
-      const DevStats &st = *(const DevStats *)(hst.data() + per * i);
-      if (st.overflow) {  // rare: the record estimate was short; a context of its own repaints this mock
-        capow_ctx *c1 = nullptr;
-        capow_options o1 = o;
-        o1.stream = nullptr;
-        int r = capow_create(&mocks[i].params, &o1, &c1);
-        if (!r) r = capow_paint(c1, &mocks[i].parts);
-        if (!r) r = capow_power(c1, mocks[i].out, capow_num_spectra(c1));
-        if (c1) capow_destroy(c1);
-        mocks[i].status = r;
-        continue;
-      }
-      if (st.nonfinite) {
-        mocks[i].status = CAPOW_EINVAL;
-        continue;
-      }
-      if (st.fatal) {
-        mocks[i].status = CAPOW_EBOUNDS;
-        continue;
-      }
-      fill_spectra(c, mocks[i].params, st, hb.data() + bins_off[i], hnm.data() + nm_off[i], nullptr, mocks[i].out);
+  std::vector<unsigned char> hst(b->per * nmocks);
+  std::vector<double> hb(b->bins_total);
+  std::vector<unsigned long long> hnm(b->nm_total);
+  if (cudaMemcpy(hst.data(), b->arena, b->per * nmocks, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(hb.data(), b->bins_d, 8 * b->bins_total, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(hnm.data(), b->nm_d, 8 * b->nm_total, cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = CAPOW_ECUDA;
+  for (int i = 0; i < nmocks && !rc; i++) {
+    capow_ctx *c = b->ctx_of[i];
+    if (!c || mocks[i].status) continue;
+    const DevStats &st = *(const DevStats *)(hst.data() + b->per * i);
+    if (st.overflow) {  // rare: the record estimate was short; a context of its own repaints this mock
+      capow_ctx *c1 = nullptr;
+      capow_options o1 = o;
+      o1.stream = nullptr;
+      int r = capow_create(&mocks[i].params, &o1, &c1);
+      if (!r) r = capow_paint(c1, &mocks[i].parts);
+      if (!r) r = capow_power(c1, mocks[i].out, capow_num_spectra(c1));
+      if (c1) capow_destroy(c1);
+      mocks[i].status = r;
+      continue;
     }
+    if (st.nonfinite) {
+      mocks[i].status = CAPOW_EINVAL;
+      continue;
+    }
+    if (st.fatal) {
+      mocks[i].status = CAPOW_EBOUNDS;
+      continue;
+    }
+    if (st.timeout) {
+      mocks[i].status = CAPOW_ETIMEOUT;
+      continue;
+    }
+    fill_spectra(c, mocks[i].params, st, hb.data() + b->bins_off[i], hnm.data() + b->nm_off[i], nullptr,
+                 mocks[i].out);
   }
-  if (exec) cudaGraphExecDestroy(exec);
-  if (graph) cudaGraphDestroy(graph);
-  for (auto &kv : ctxs) capow_destroy(kv.second);  // restores nothing: the contexts are private
-  if (tab_dev) cudaFree(tab_dev);
-  if (arena) cudaFree(arena);
-  if (own_stream) cudaStreamDestroy(stream);
   return rc;
+}
+
+extern "C" void capow_batch_release(void) {
+  std::lock_guard<std::mutex> lock(g_batch_mu);
+  free_batch_state(g_batch);
+  g_batch = nullptr;
 }

@@ -170,6 +170,16 @@ int build_bin_tables(const capow_params &p, const Geom &g, int precision, BinTab
     t.twx = upload(tw, allocs, s);
     if (!t.twx) return 1;
   }
+  t.twy = nullptr;
+  if (ny >= 16 && ny <= 2048 && (ny & (ny - 1)) == 0) {  // y pass of the one-launch z + y transform
+    std::vector<float2> tw(ny);
+    for (int q = 0; q < ny; q++) {
+      const double a = -2.0 * M_PI * (double)q / (double)ny;
+      tw[q] = make_float2((float)cos(a), (float)sin(a));
+    }
+    t.twy = upload(tw, allocs, s);
+    if (!t.twy) return 1;
+  }
   t.twz = t.tpz = nullptr;
   const int nzp = p.NZ;
   if (nzp >= 32 && nzp <= 2048 && (nzp & (nzp - 1)) == 0) {  // z pass of the transposed fused path
@@ -205,7 +215,8 @@ void relocate_bin_tables(BinTables &t, const void *base) {
                 (void **)&t.fyf,  (void **)&t.fzf,  (void **)&t.cxd,  (void **)&t.cyd,  (void **)&t.czd,
                 (void **)&t.cxf,  (void **)&t.cyf,  (void **)&t.czf,  (void **)&t.exd,  (void **)&t.eyd,
                 (void **)&t.ezd,  (void **)&t.exf,  (void **)&t.eyf,  (void **)&t.ezf,  (void **)&t.E,
-                (void **)&t.Elo,  (void **)&t.Ehi,  (void **)&t.twx,  (void **)&t.twz,  (void **)&t.tpz};
+                (void **)&t.Elo,  (void **)&t.Ehi,  (void **)&t.twx,  (void **)&t.twz,  (void **)&t.tpz,
+                (void **)&t.twy};
   for (void **q : f)
     if (*q) *q = (void *)((const char *)base + (uintptr_t)*q);
 }
@@ -1024,96 +1035,306 @@ struct ZrGeo {
   long long slice, in_slot, out_slot;
 };
 
-template <int ZB>
-__global__ void __launch_bounds__(ZR_THREADS) k_zr2c(ZrGeo zg, BinTables t, const float *in, float2 *out) {
-  constexpr int LZB = ZB == 16 ? 4 : 3;
-  extern __shared__ __align__(16) unsigned char smz[];
-  const int log2m = zg.log2m, M = 1 << log2m, P = ZB + 1, Q1 = M >> 3;
-  float2 *sd = (float2 *)smz;                                      // [M][ZB + 1]
-  float2 *stw = (float2 *)(smz + align16(8u * (unsigned)M * P));  // radix-8 stage twiddle tables
-  int *spos = (int *)(smz + align16(8u * (unsigned)M * P) + 8u * zr2c_tw_entries(log2m));  // row of Z[k]
-  float2 *stp = (float2 *)(smz + align16(8u * (unsigned)M * P) + 8u * zr2c_tw_entries(log2m) + align16(4u * M));
-  for (int k = threadIdx.x; k < M; k += blockDim.x) spos[k] = xfft_pos(log2m, k);
-  for (int k = threadIdx.x; k <= M; k += blockDim.x) stp[k] = t.tpz[k];
+// Shared tables of the z pass: radix-8 twiddles (stw), the row of Z[k] after the DIF stages (spos)
+// and the real-input split twiddles (stp), carved after a data area of `data_bytes`.
+struct ZrTables {
+  float2 *stw;
+  int *spos;
+  float2 *stp;
+};
+
+CAPOW_HD unsigned zr2c_tables_bytes(int log2m) {
+  const unsigned M = 1u << log2m;
+  return align16(8u * zr2c_tw_entries(log2m)) + align16(4u * M) + align16(8u * (M + 1));
+}
+
+__device__ ZrTables zr2c_load_tables(const BinTables &t, int log2m, unsigned char *base) {
+  const int M = 1 << log2m;
+  ZrTables z;
+  z.stw = (float2 *)base;
+  z.spos = (int *)(base + align16(8u * zr2c_tw_entries(log2m)));
+  z.stp = (float2 *)(base + align16(8u * zr2c_tw_entries(log2m)) + align16(4u * M));
+  for (int k = threadIdx.x; k < M; k += blockDim.x) z.spos[k] = xfft_pos(log2m, k);
+  for (int k = threadIdx.x; k <= M; k += blockDim.x) z.stp[k] = t.tpz[k];
   for (int l = log2m, off = 0; l >= 4; off += 8 << (l - 3), l -= 3) {
     const int step = M >> l;  // M / span
     for (int e = threadIdx.x; e < (8 << (l - 3)); e += blockDim.x)
-      stw[off + e] = t.twz[((e & 7) * (e >> 3) * step) & (M - 1)];
+      z.stw[off + e] = t.twz[((e & 7) * (e >> 3) * step) & (M - 1)];
   }
+  return z;
+}
+
+// One block of the z pass: ZB rows y0.. of plane x of slot sl, through the shared data area sd
+// ([M][ZB + 1]). The caller has synchronised after the tables were written and after any earlier use
+// of sd.
+template <int ZB>
+__device__ __forceinline__ void zr2c_block(const ZrGeo &zg, const ZrTables &z, const float *in, float2 *out,
+                                           float2 *sd, int sl, int x, int y0) {
+  constexpr int LZB = ZB == 16 ? 4 : 3;
+  const int log2m = zg.log2m, M = 1 << log2m, P = ZB + 1, Q1 = M >> 3;
+  const float *src = in + sl * zg.in_slot + (long long)x * zg.slice;
+  // first DIF stage (span M) straight from the rows: butterfly (row r, jj) reads z[jj + q M/8];
+  // lanes run along a row, so each of a warp's 8 loads is one contiguous 256-byte piece
+  for (int u = threadIdx.x; u < (ZB << (log2m - 3)); u += blockDim.x) {
+    const int jj = u & (Q1 - 1), r = u >> (log2m - 3), y = y0 + r;
+    const float2 *rp = reinterpret_cast<const float2 *>(src + (long long)(y < zg.ny ? y : 0) * zg.row) + jj;
+    float2 a[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) a[q] = y < zg.ny ? __ldcs(rp + q * Q1) : make_float2(0.0f, 0.0f);
+    dft8(a);
+    if (jj > 0) twiddle8(a, z.stw + 8 * jj);
+    float2 *p = sd + jj * P + r;
+#pragma unroll
+    for (int q = 0; q < 8; q++) p[q * Q1 * P] = a[q];
+  }
+  __syncthreads();
+  int l = log2m - 3, twoff = 8 * Q1;
+  for (; l >= 3; l -= 3) {  // the other radix-8 DIF stages
+    const int log2q = l - 3, Q = 1 << log2q, qs = Q * P;
+    for (int u = threadIdx.x; u < (ZB << (log2m - 3)); u += blockDim.x) {
+      const int c = u & (ZB - 1), v = u >> LZB;
+      const int jj = v & (Q - 1);
+      float2 *p = sd + (((v >> log2q) << l) + jj) * P + c;
+      float2 a[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) a[q] = p[q * qs];
+      dft8(a);
+      if (jj > 0) twiddle8(a, z.stw + twoff + 8 * jj);
+#pragma unroll
+      for (int q = 0; q < 8; q++) p[q * qs] = a[q];
+    }
+    __syncthreads();
+    if (Q > 1) twoff += 8 * Q;
+  }
+  if (l == 2) {  // a last radix-4 stage (span 4: no twiddles)
+    for (int u = threadIdx.x; u < (ZB << (log2m - 2)); u += blockDim.x) {
+      float2 *p = sd + ((u >> LZB) << 2) * P + (u & (ZB - 1));
+      float2 a[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) a[q] = p[q * P];
+      dft4(a);
+#pragma unroll
+      for (int q = 0; q < 4; q++) p[q * P] = a[q];
+    }
+    __syncthreads();
+  } else if (l == 1) {  // a last radix-2 stage
+    for (int u = threadIdx.x; u < (ZB << (log2m - 1)); u += blockDim.x) {
+      float2 *p = sd + ((u >> LZB) << 1) * P + (u & (ZB - 1));
+      const float2 a0 = p[0], a1 = p[P];
+      p[0] = cadd(a0, a1);
+      p[P] = csub(a0, a1);
+    }
+    __syncthreads();
+  }
+  // real-input split and transposed store, X[k] and X[M-k] from the same pair: with
+  // A = Z[k] + conj Z[M-k], B = Z[k] - conj Z[M-k] and w^M = -1, X[k] = (A + (-i) w^k B) / 2 and
+  // X[M-k] = (conj A + (-i) conj(w^k B)) / 2. The thread's row r is the same on every step.
+  const int r = threadIdx.x & (ZB - 1), y = y0 + r;
+  if (y < zg.ny) {
+    float2 *dst = out + sl * zg.out_slot + (long long)x * zg.nzc * zg.ny + y;
+    for (int k = threadIdx.x >> LZB; k <= (M >> 1); k += blockDim.x >> LZB) {
+      const float2 zk = sd[z.spos[k & (M - 1)] * P + r];
+      const float2 zm = sd[z.spos[(M - k) & (M - 1)] * P + r];
+      const float2 A = make_float2(zk.x + zm.x, zk.y - zm.y);
+      const float2 B = make_float2(zk.x - zm.x, zk.y + zm.y);
+      const float2 wB = cmulf(z.stp[k], B);
+      dst[(long long)k * zg.ny] = make_float2(0.5f * (A.x + wB.y), 0.5f * (A.y - wB.x));
+      if (2 * k != M) dst[(long long)(M - k) * zg.ny] = make_float2(0.5f * (A.x - wB.y), -0.5f * (A.y + wB.x));
+    }
+  }
+}
+
+template <int ZB>
+__global__ void __launch_bounds__(ZR_THREADS) k_zr2c(ZrGeo zg, BinTables t, const float *in, float2 *out) {
+  extern __shared__ __align__(16) unsigned char smz[];
+  const int M = 1 << zg.log2m;
+  float2 *sd = (float2 *)smz;  // [M][ZB + 1]
+  const ZrTables z = zr2c_load_tables(t, zg.log2m, smz + align16(8u * (unsigned)M * (ZB + 1)));
   const int per_slot = zg.nx * zg.nyb, nblk = per_slot * zg.ns;
   for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {  // (slot, x, block of ZB rows)
     const int sl = blk / per_slot, rem = blk - sl * per_slot;
     const int x = rem / zg.nyb, y0 = (rem - x * zg.nyb) * ZB;
-    const float *src = in + sl * zg.in_slot + (long long)x * zg.slice;
     __syncthreads();  // tables written; the previous block's output has read sd
-    // first DIF stage (span M) straight from the rows: butterfly (row r, jj) reads z[jj + q M/8];
-    // lanes run along a row, so each of a warp's 8 loads is one contiguous 256-byte piece
-    for (int u = threadIdx.x; u < (ZB << (log2m - 3)); u += blockDim.x) {
-      const int jj = u & (Q1 - 1), r = u >> (log2m - 3), y = y0 + r;
-      const float2 *rp = reinterpret_cast<const float2 *>(src + (long long)(y < zg.ny ? y : 0) * zg.row) + jj;
+    zr2c_block<ZB>(zg, z, in, out, sd, sl, x, y0);
+  }
+}
+
+// ------------------------------------------------------------ z and y axes in one launch (FP32)
+// The z pass above followed by the y-axis C2C over the transposed layout [NX][NZ/2+1][NY], in one
+// persistent launch so that each x-plane's z output is read back by its y transforms from L2 and
+// overwritten in place, instead of going to HBM and back (4 bytes of grid traffic per real cell less
+// in each direction). Work items come from one queue counter in a fixed order: the z items of the
+// first `lead` planes, then for each plane p its y items followed by the z items of plane p + lead.
+// A y item of plane p (KB consecutive kz rows of one slot) waits until all z items of that plane and
+// slot are done (a per-(slot, plane) counter). Every item it waits for was taken from the queue before
+// it by a running CTA and waits for nothing, so the wait always ends; it is still bounded: a wait that
+// runs out sets the abort flag (every CTA then stops at its next item) and the error flag of the
+// paint statistics, which capow_power reports as CAPOW_ETIMEOUT.
+constexpr int ZY_KB = 8;                     // kz rows per y item
+constexpr unsigned ZY_WAIT_LIMIT = 1u << 22;  // polls of about 0.2 us: about a second
+
+struct ZyGeo {
+  ZrGeo zg;
+  int log2ny;     // NY = 2^log2ny
+  int nkb;        // y items per (plane, slot)
+  int lead;       // planes of z items issued ahead of the y items
+  int stall;      // test switch: y items wait for one z item more than exists (their waits run out)
+  long long nitems;
+};
+
+CAPOW_HD unsigned zy_ytables_bytes(int log2ny) {
+  return align16(8u * xbin_tw_entries(log2ny)) + align16(4u * (1u << log2ny));
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// One y item: rows kz0 .. kz0 + ZY_KB - 1 (those below NZ/2+1) of plane x of slot sl, each NY complex
+// values along y, transformed in place (forward, unnormalised) through sd ([NY][ZY_KB + 1]).
+__device__ __forceinline__ void yfft_block(const ZyGeo &yg, const float2 *stwy, const int *sposy, float2 *out,
+                                           float2 *sd, int sl, int x, int kz0) {
+  constexpr int KB = ZY_KB, LKB = 3, P = KB + 1;
+  const int log2n = yg.log2ny, n = 1 << log2n, Q1 = n >> 3;
+  const int nrow = min(KB, yg.zg.nzc - kz0);
+  float2 *rows = out + sl * yg.zg.out_slot + ((long long)x * yg.zg.nzc + kz0) * n;
+  // first DIF stage (span NY) from the rows, lanes along a row (written by other CTAs of this launch:
+  // read through L2, never from a stale L1 line)
+  for (int u = threadIdx.x; u < (KB << (log2n - 3)); u += blockDim.x) {
+    const int jj = u & (Q1 - 1), r = u >> (log2n - 3);
+    const float2 *rp = rows + (long long)(r < nrow ? r : 0) * n + jj;
+    float2 a[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) a[q] = r < nrow ? __ldcg(rp + q * Q1) : make_float2(0.0f, 0.0f);
+    dft8(a);
+    if (jj > 0) twiddle8(a, stwy + 8 * jj);
+    float2 *p = sd + jj * P + r;
+#pragma unroll
+    for (int q = 0; q < 8; q++) p[q * Q1 * P] = a[q];
+  }
+  __syncthreads();
+  int l = log2n - 3, twoff = 8 * Q1;
+  for (; l >= 3; l -= 3) {
+    const int log2q = l - 3, Q = 1 << log2q, qs = Q * P;
+    for (int u = threadIdx.x; u < (KB << (log2n - 3)); u += blockDim.x) {
+      const int c = u & (KB - 1), v = u >> LKB;
+      const int jj = v & (Q - 1);
+      float2 *p = sd + (((v >> log2q) << l) + jj) * P + c;
       float2 a[8];
 #pragma unroll
-      for (int q = 0; q < 8; q++) a[q] = y < zg.ny ? __ldcs(rp + q * Q1) : make_float2(0.0f, 0.0f);
+      for (int q = 0; q < 8; q++) a[q] = p[q * qs];
       dft8(a);
-      if (jj > 0) twiddle8(a, stw + 8 * jj);
-      float2 *p = sd + jj * P + r;
+      if (jj > 0) twiddle8(a, stwy + twoff + 8 * jj);
 #pragma unroll
-      for (int q = 0; q < 8; q++) p[q * Q1 * P] = a[q];
+      for (int q = 0; q < 8; q++) p[q * qs] = a[q];
     }
     __syncthreads();
-    int l = log2m - 3, twoff = 8 * Q1;
-    for (; l >= 3; l -= 3) {  // the other radix-8 DIF stages
-      const int log2q = l - 3, Q = 1 << log2q, qs = Q * P;
-      for (int u = threadIdx.x; u < (ZB << (log2m - 3)); u += blockDim.x) {
-        const int c = u & (ZB - 1), v = u >> LZB;
-        const int jj = v & (Q - 1);
-        float2 *p = sd + (((v >> log2q) << l) + jj) * P + c;
-        float2 a[8];
+    if (Q > 1) twoff += 8 * Q;
+  }
+  if (l == 2) {
+    for (int u = threadIdx.x; u < (KB << (log2n - 2)); u += blockDim.x) {
+      float2 *p = sd + ((u >> LKB) << 2) * P + (u & (KB - 1));
+      float2 a[4];
 #pragma unroll
-        for (int q = 0; q < 8; q++) a[q] = p[q * qs];
-        dft8(a);
-        if (jj > 0) twiddle8(a, stw + twoff + 8 * jj);
+      for (int q = 0; q < 4; q++) a[q] = p[q * P];
+      dft4(a);
 #pragma unroll
-        for (int q = 0; q < 8; q++) p[q * qs] = a[q];
-      }
-      __syncthreads();
-      if (Q > 1) twoff += 8 * Q;
+      for (int q = 0; q < 4; q++) p[q * P] = a[q];
     }
-    if (l == 2) {  // a last radix-4 stage (span 4: no twiddles)
-      for (int u = threadIdx.x; u < (ZB << (log2m - 2)); u += blockDim.x) {
-        float2 *p = sd + ((u >> LZB) << 2) * P + (u & (ZB - 1));
-        float2 a[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) a[q] = p[q * P];
-        dft4(a);
-#pragma unroll
-        for (int q = 0; q < 4; q++) p[q * P] = a[q];
-      }
-      __syncthreads();
-    } else if (l == 1) {  // a last radix-2 stage
-      for (int u = threadIdx.x; u < (ZB << (log2m - 1)); u += blockDim.x) {
-        float2 *p = sd + ((u >> LZB) << 1) * P + (u & (ZB - 1));
-        const float2 a0 = p[0], a1 = p[P];
-        p[0] = cadd(a0, a1);
-        p[P] = csub(a0, a1);
-      }
-      __syncthreads();
+    __syncthreads();
+  } else if (l == 1) {
+    for (int u = threadIdx.x; u < (KB << (log2n - 1)); u += blockDim.x) {
+      float2 *p = sd + ((u >> LKB) << 1) * P + (u & (KB - 1));
+      const float2 a0 = p[0], a1 = p[P];
+      p[0] = cadd(a0, a1);
+      p[P] = csub(a0, a1);
     }
-    // real-input split and transposed store, X[k] and X[M-k] from the same pair: with
-    // A = Z[k] + conj Z[M-k], B = Z[k] - conj Z[M-k] and w^M = -1, X[k] = (A + (-i) w^k B) / 2 and
-    // X[M-k] = (conj A + (-i) conj(w^k B)) / 2. The thread's row r is the same on every step.
-    const int r = threadIdx.x & (ZB - 1), y = y0 + r;
-    if (y < zg.ny) {
-      float2 *dst = out + sl * zg.out_slot + (long long)x * zg.nzc * zg.ny + y;
-      for (int k = threadIdx.x >> LZB; k <= (M >> 1); k += blockDim.x >> LZB) {
-        const float2 zk = sd[spos[k & (M - 1)] * P + r];
-        const float2 zm = sd[spos[(M - k) & (M - 1)] * P + r];
-        const float2 A = make_float2(zk.x + zm.x, zk.y - zm.y);
-        const float2 B = make_float2(zk.x - zm.x, zk.y + zm.y);
-        const float2 wB = cmulf(stp[k], B);
-        dst[(long long)k * zg.ny] = make_float2(0.5f * (A.x + wB.y), 0.5f * (A.y - wB.x));
-        if (2 * k != M) dst[(long long)(M - k) * zg.ny] = make_float2(0.5f * (A.x - wB.y), -0.5f * (A.y + wB.x));
+    __syncthreads();
+  }
+  // natural order out: lanes along ky (coalesced rows); sposy[ky] is the row of Y[ky] in sd
+  for (int u = threadIdx.x; u < nrow * n; u += blockDim.x) {
+    const int ky = u & (n - 1), r = u >> log2n;
+    rows[(long long)r * n + ky] = sd[sposy[ky] * P + r];
+  }
+}
+
+template <int ZB>
+__global__ void __launch_bounds__(ZR_THREADS) k_zy(ZyGeo yg, BinTables t, const float *in, float2 *out,
+                                                   unsigned *ctr, DevStats *st) {
+  extern __shared__ __align__(16) unsigned char smz[];
+  const ZrGeo &zg = yg.zg;
+  const int M = 1 << zg.log2m, ny = 1 << yg.log2ny;
+  const unsigned zdata = align16(8u * (unsigned)M * (ZB + 1)), ydata = align16(8u * (unsigned)ny * (ZY_KB + 1));
+  float2 *sd = (float2 *)smz;  // the data area of whichever item runs
+  unsigned char *tb = smz + (zdata > ydata ? zdata : ydata);
+  const ZrTables z = zr2c_load_tables(t, zg.log2m, tb);
+  tb += zr2c_tables_bytes(zg.log2m);
+  float2 *stwy = (float2 *)tb;
+  int *sposy = (int *)(tb + align16(8u * xbin_tw_entries(yg.log2ny)));
+  for (int l = yg.log2ny, off = 0; l >= 4; off += 8 << (l - 3), l -= 3) {
+    const int step = ny >> l;
+    for (int e = threadIdx.x; e < (8 << (l - 3)); e += blockDim.x)
+      stwy[off + e] = t.twy[((e & 7) * (e >> 3) * step) & (ny - 1)];
+  }
+  for (int k = threadIdx.x; k < ny; k += blockDim.x) sposy[k] = xfft_pos(yg.log2ny, k);
+  __shared__ long long s_item;
+  __shared__ int s_ok;
+  unsigned *done = ctr + 2;  // [slot][plane]: finished z items
+  const long long nzp = (long long)zg.ns * zg.nyb, nyp = (long long)zg.ns * yg.nkb;
+  const long long lead = yg.lead, s0 = lead * nzp, per = nzp + nyp, nper = zg.nx - lead;
+  for (;;) {
+    __syncthreads();  // the previous item is done with sd (and the tables are written)
+    if (threadIdx.x == 0) {
+      const unsigned abort = *(volatile unsigned *)(ctr + 1);
+      s_item = abort ? yg.nitems : (long long)atomicAdd(ctr, 1u);
+    }
+    __syncthreads();
+    const long long item = s_item;
+    if (item >= yg.nitems) break;
+    // decode: z items of the first `lead` planes, then (y items of p, z items of p + lead) per plane
+    bool is_y;
+    long long plane, r;
+    if (item < s0) {
+      is_y = false;
+      plane = item / nzp;
+      r = item - plane * nzp;
+    } else if (item - s0 < nper * per) {
+      const long long t2 = item - s0, q = t2 / per;
+      r = t2 - q * per;
+      is_y = r < nyp;
+      plane = is_y ? q : q + lead;
+      if (!is_y) r -= nyp;
+    } else {
+      const long long t3 = item - s0 - nper * per;
+      is_y = true;
+      plane = nper + t3 / nyp;
+      r = t3 - (plane - nper) * nyp;
+    }
+    if (!is_y) {
+      const int sl = (int)(r / zg.nyb), y0 = (int)(r - (long long)sl * zg.nyb) * ZB;
+      zr2c_block<ZB>(zg, z, in, out, sd, sl, (int)plane, y0);
+      __threadfence();  // this thread's stores, before the item is counted done
+      __syncthreads();
+      if (threadIdx.x == 0) atomicAdd(done + (long long)sl * zg.nx + plane, 1u);
+    } else {
+      const int sl = (int)(r / yg.nkb), kz0 = (int)(r - (long long)sl * yg.nkb) * ZY_KB;
+      if (threadIdx.x == 0) {
+        const unsigned *cnt = done + (long long)sl * zg.nx + plane;
+        unsigned polls = 0;
+        const unsigned need = (unsigned)(zg.nyb + yg.stall);
+        while (ld_acquire_u32(cnt) < need && ++polls < ZY_WAIT_LIMIT && !*(volatile unsigned *)(ctr + 1))
+          __nanosleep(200);
+        s_ok = polls < ZY_WAIT_LIMIT && !*(volatile unsigned *)(ctr + 1);
+        if (!s_ok) {
+          atomicExch(ctr + 1, 1u);
+          atomicExch(&st->timeout, 1);
+        }
       }
+      __syncthreads();
+      if (!s_ok) break;
+      yfft_block(yg, stwy, sposy, out, sd, sl, (int)plane, kz0);
     }
   }
 }
@@ -1126,7 +1347,7 @@ template <int ZB>
 static void launch_zr2c_t(cudaStream_t s, const ZrGeo &zg, const BinTables &t, int nslot, const float *in,
                           float2 *out) {
   const int M = 1 << zg.log2m;
-  const size_t smem = align16(8u * (unsigned)M * (ZB + 1)) + 8u * zr2c_tw_entries(zg.log2m) + align16(4u * M) + 8u * (M + 1);
+  const size_t smem = align16(8u * (unsigned)M * (ZB + 1)) + zr2c_tables_bytes(zg.log2m);
   cudaFuncSetAttribute(k_zr2c<ZB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int per_sm = 1, dev = 0, nsm = 152;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zr2c<ZB>, ZR_THREADS, smem);
@@ -1159,6 +1380,58 @@ void launch_zr2c(cudaStream_t s, const BinParams &bp, const BinTables &t, int ns
     zg.nyb = (bp.ny + 7) / 8;
     launch_zr2c_t<8>(s, zg, t, nslot, in, out);
   }
+  (*launches)++;
+}
+
+bool zy_supported(const BinParams &bp, const BinTables &t) {
+  return zr2c_supported(bp) && t.twy && bp.ny >= 16 && bp.ny <= 2048 && (bp.ny & (bp.ny - 1)) == 0;
+}
+
+size_t zy_counter_words(const BinParams &bp, int nslot) { return 2 + (size_t)nslot * bp.nx; }
+
+template <int ZB>
+static void launch_zy_t(cudaStream_t s, const ZyGeo &yg, const BinTables &t, const float *in, float2 *out,
+                        unsigned *ctr, DevStats *st) {
+  const unsigned M = 1u << yg.zg.log2m, ny = 1u << yg.log2ny;
+  const unsigned zdata = align16(8u * M * (ZB + 1)), ydata = align16(8u * ny * (ZY_KB + 1));
+  const size_t smem = (zdata > ydata ? zdata : ydata) + zr2c_tables_bytes(yg.zg.log2m) + zy_ytables_bytes(yg.log2ny);
+  cudaFuncSetAttribute(k_zy<ZB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 1, dev = 0, nsm = 152;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zy<ZB>, ZR_THREADS, smem);
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  long long grid = (long long)(per_sm > 0 ? per_sm : 1) * nsm;
+  if (grid > yg.nitems) grid = yg.nitems;
+  k_zy<ZB><<<(unsigned)grid, ZR_THREADS, smem, s>>>(yg, t, in, out, ctr, st);
+}
+
+void launch_zy(cudaStream_t s, const BinParams &bp, const BinTables &t, int nslot, const float *in, long long in_slot,
+               int row, float2 *out, long long out_slot, unsigned *ctr, DevStats *st, int stall,
+               long long *launches) {
+  ZyGeo yg;
+  ZrGeo &zg = yg.zg;
+  int lm = 0;
+  while ((2 << lm) < bp.nz) lm++;  // M = NZ / 2 = 2^lm
+  zg.log2m = lm;
+  zg.nx = bp.nx;
+  zg.ny = bp.ny;
+  zg.nzc = bp.nzc;
+  zg.row = row;
+  zg.slice = (long long)bp.ny * row;
+  zg.in_slot = in_slot;
+  zg.out_slot = out_slot;
+  zg.ns = nslot;
+  const int zb = bp.nz <= 512 ? 16 : 8;
+  zg.nyb = (bp.ny + zb - 1) / zb;
+  yg.log2ny = 0;
+  while ((1 << yg.log2ny) < bp.ny) yg.log2ny++;
+  yg.nkb = (bp.nzc + ZY_KB - 1) / ZY_KB;
+  yg.lead = bp.nx < 8 ? bp.nx : 8;
+  yg.stall = stall ? 1 : 0;
+  yg.nitems = (long long)bp.nx * nslot * (zg.nyb + yg.nkb);
+  cudaMemsetAsync(ctr, 0, sizeof(unsigned) * zy_counter_words(bp, nslot), s);
+  if (zb == 16) launch_zy_t<16>(s, yg, t, in, out, ctr, st);
+  else launch_zy_t<8>(s, yg, t, in, out, ctr, st);
   (*launches)++;
 }
 

@@ -29,6 +29,7 @@ struct BinTables {
   double *E;
   float *Elo, *Ehi;  // E[b]*(1+eps), E[b]*(1-eps) rounded outward/inward: safe FP32 tests
   float2 *twx;       // exp(-2 pi i q / NX), q < NX (fused x-axis FFT; power-of-two NX only)
+  float2 *twy;       // exp(-2 pi i q / NY), q < NY (y pass of the one-launch z + y transform; power-of-two NY)
   // z-axis pass of the fused path (power-of-two NZ >= 32 only): exp(-2 pi i q / M), q < M = NZ/2,
   // for the M-point complex DFT, and exp(-2 pi i k / NZ), k <= M, for its real-input split
   float2 *twz, *tpz;
@@ -91,6 +92,15 @@ int bin_products(int nfields);
 bool xbin_plan(const BinParams &bp, int nslot, XbinGeo &xg, bool transposed);
 // The z-axis pass of the transposed fused layout: true when NZ is a power of two in [32, 2048].
 bool zr2c_supported(const BinParams &bp);
+// The z pass and the y-axis C2C of the transposed layout in one launch (power-of-two NZ and NY, the
+// tables' twy present). ctr: 2 + nslot * NX device counters, cleared by the launcher; a wait that gave
+// up sets st->timeout. stall != 0 (tests of the timeout path only) makes every wait run out.
+struct DevStats;
+bool zy_supported(const BinParams &bp, const BinTables &t);
+size_t zy_counter_words(const BinParams &bp, int nslot);
+void launch_zy(cudaStream_t s, const BinParams &bp, const BinTables &t, int nslot, const float *in, long long in_slot,
+               int row, float2 *out, long long out_slot, unsigned *ctr, DevStats *st, int stall,
+               long long *launches);
 // Real-to-complex DFT along z of every row of every painted grid (in: [NX][NY][row] floats, slot
 // stride in_slot floats), out of place into out (slot stride out_slot complex) as [NX][NZ/2+1][NY].
 void launch_zr2c(cudaStream_t s, const BinParams &bp, const BinTables &t, int nslot, const float *in,

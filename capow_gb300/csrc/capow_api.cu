@@ -48,6 +48,7 @@ static int validate(const capow_params *p, const capow_options *o, char *err, si
   if (p->Maxk < p->Mink) BAD("Maxk is less than Mink");
   if (p->Momentum < 0 || p->Momentum > 8) BAD("Momentum must be 0..8");
   if (o->precision < 0 || o->precision > 2) BAD("unknown precision");
+  if (o->fft_path < CAPOW_FFT_AUTO || o->fft_path > CAPOW_FFT_ONE_LAUNCH) BAD("unknown fft_path");
   if (o->spectra < 0 || o->spectra > 7) BAD("unknown spectra mask");
   if (o->precision != CAPOW_FP64 && (p->NX < 4 || p->NY < 4 || p->NZ < 4))
     BAD("the FP32 paths need NX, NY, NZ >= 4");
@@ -253,6 +254,20 @@ extern "C" int capow_create(const capow_params *p, const capow_options *opt, cap
     c->tslot = (long long)p->NX * bp.nzc * p->NY;
     void *tb = nullptr;
     int ny = p->NY;
+    if (o.fft_path == CAPOW_FFT_ONE_LAUNCH && zy_supported(bp, c->bt)) {  // z and y axes in one launch
+      const char *stall = getenv("CAPOW_TEST_STALL_ZY");
+      c->zy_stall = stall && stall[0] == '1';
+      c->zy_ctr = (unsigned *)dalloc(c, sizeof(unsigned) * zy_counter_words(bp, c->nslot));
+      if (c->zy_ctr && cudaMalloc(&tb, sizeof(float2) * (size_t)c->tslot * c->nslot) == cudaSuccess) {
+        c->allocs.push_back(tb);
+        c->tbuf = (float2 *)tb;
+        c->xtr = true;
+        c->zy = true;
+        c->plan_ok = true;
+        return CAPOW_OK;
+      }
+      tb = nullptr;
+    }
     if (cudaMalloc(&tb, sizeof(float2) * (size_t)c->tslot * c->nslot) == cudaSuccess) {
       if (cufftPlanMany(&c->yplan, 1, &ny, nullptr, 1, ny, nullptr, 1, ny, CUFFT_C2C, (int)yrows) == CUFFT_SUCCESS) {
         c->allocs.push_back(tb);
@@ -556,7 +571,12 @@ int enqueue_power_kernels(capow_ctx *c) {
                     c->bp.mean_sub_a, c->fixed_scale, c->dcv, &c->launches);
   if (c->fused) {
     void *slots[4];
-    if (c->xtr) {
+    if (c->xtr && c->zy) {
+      launch_zy(c->stream, c->bp, c->bt, c->nslot, (const float *)c->grid_base, (long long)c->grid_elems, c->g.row,
+                c->tbuf, c->tslot, c->zy_ctr, c->st, c->zy_stall, &c->launches);
+      CK(c, cudaGetLastError());
+      for (int k = 0; k < 4; k++) slots[k] = k < c->nslot ? (void *)(c->tbuf + c->tslot * k) : nullptr;
+    } else if (c->xtr) {
       launch_zr2c(c->stream, c->bp, c->bt, c->nslot, (const float *)c->grid_base, (long long)c->grid_elems, c->g.row,
                   c->tbuf, c->tslot, &c->launches);
       CKFFT(c, cufftExecC2C(c->yplan, (cufftComplex *)c->tbuf, (cufftComplex *)c->tbuf, CUFFT_FORWARD));
@@ -636,6 +656,7 @@ extern "C" int capow_power(capow_ctx *c, capow_spectrum *out, int nout) {
   }
   if (c->h_st->nonfinite) FAIL(c, CAPOW_EINVAL, "non-finite particle coordinate, velocity or weight");
   if (c->h_st->fatal) FAIL(c, CAPOW_EBOUNDS, "particle out of grid bounds with LOS == 0");
+  if (c->h_st->timeout) FAIL(c, CAPOW_ETIMEOUT, "a bounded wait of the z + y transform gave up");
   fill_spectra(c, c->p, *c->h_st, c->h_bins, c->nmodes.data(), c->nmodes2d.data(), out);
   return CAPOW_OK;
 }

@@ -46,6 +46,11 @@ struct capow_ctx {
   long long tslot;  // complex values per slot of tbuf
   cufftHandle yplan;
   bool yplan_ok;
+  // power-of-two NY as well: the z pass and the y axis in one launch (k_zy) instead of k_zr2c + yplan;
+  // zy_ctr holds its work-queue and per-plane counters
+  bool zy;
+  unsigned *zy_ctr;
+  int zy_stall;  // CAPOW_TEST_STALL_ZY=1 at creation: k_zy's waits run out (the timeout path's test)
   bool fused;           // FP32: 2-D (y, z) cuFFT + fused x-axis FFT and binning (k_xfft_bin)
   XbinGeo xg;
   // capow_backward (created on first use): full 3-D plans, bin coefficients, host-output staging

@@ -20,7 +20,7 @@ struct DevStats {
   int fatal;                 // LOS == 0 particle outside the box
   int nonfinite;             // NaN/inf coordinate
   int overflow;              // record buffer too small
-  int pad;
+  int timeout;               // a bounded device wait of the power stage gave up (CAPOW_ETIMEOUT)
 };
 
 // Tile decomposition of the grid for the FP32 path.

@@ -82,7 +82,7 @@ typedef struct capow_options {
   int spectra;   /* CAPOW_SPEC_REFERENCE, or an OR of CAPOW_SPEC_DD|DP|PP (one paint, one set of FFTs) */
   int device;    /* CUDA device ordinal */
   void *stream;  /* cudaStream_t to run on, or NULL for a stream owned by the context */
-  int fft_path;  /* CAPOW_FFT_AUTO or CAPOW_FFT_3D (below) */
+  int fft_path;  /* CAPOW_FFT_AUTO, CAPOW_FFT_3D or CAPOW_FFT_ONE_LAUNCH (below) */
   int reserved[7];
 } capow_options;
 
@@ -92,6 +92,11 @@ typedef struct capow_options {
  * transform and a separate binning kernel. Both give the same spectra within FP32 rounding. */
 #define CAPOW_FFT_AUTO 0
 #define CAPOW_FFT_3D 1
+/* ONE_LAUNCH: as AUTO, but where NY and NZ are powers of two (NY in [16, 2048], NZ in [32, 2048]) the
+ * z and y axes run in one launch of the library's own kernel, each x-plane's z output read back from
+ * L2 by its y transforms (no HBM round trip between the axes) instead of the z kernel followed by
+ * cuFFT along y. Same spectra within FP32 rounding. */
+#define CAPOW_FFT_ONE_LAUNCH 2
 
 /* particle input: structure of arrays */
 #define CAPOW_F32 0
@@ -215,10 +220,19 @@ typedef struct capow_mock {
 #define CAPOW_BATCH_AUTOTUNE 2 /* time candidate tile shapes of the FP32 paint per grid shape first */
 
 /* Run many independent mocks (the reference runs one per process, main.c:28-298). Mocks with the
- * same grid shape share grids, plans and record buffers; every mock is enqueued on one stream
- * with no host synchronisation and read back once. Output2D is not supported here. Returns
- * CAPOW_OK when the batch ran; per-mock errors are in mocks[i].status. */
+ * same grid shape (NX, NY, NZ, interlacing, LOS, Momentum, odd multipoles) share grids, plans and
+ * record buffers whatever their boxes, orders and k bins; every mock is enqueued on one stream with
+ * no host synchronisation and read back once. Output2D is not supported here. Returns CAPOW_OK when
+ * the batch ran; per-mock errors are in mocks[i].status.
+ * The device state of the batch (contexts, tables, outputs and, with CAPOW_BATCH_GRAPH, the
+ * instantiated graph) is kept for the next call: a call with the same signature (parameters,
+ * particle counts and array kinds of every mock, options and flags) only launches, the graph as it
+ * is or updated in place when the particle arrays moved. A call with another signature replaces it;
+ * capow_batch_release frees it. Calls are serialised by the library. */
 int capow_batch(capow_mock *mocks, int nmocks, const capow_options *opt, int flags);
+
+/* Free the device state capow_batch keeps between calls. No reference counterpart. */
+void capow_batch_release(void);
 
 /* output_power arithmetic (main.c:1019-1056) in place on one spectrum's raw sums. Host only. */
 int capow_normalise(const capow_params *p, capow_spectrum *s);

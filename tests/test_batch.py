@@ -79,3 +79,35 @@ def test_batch_mocks_match_the_oracle(gpu):
         r = res[0]
         assert r["shot"] == ref["shot"] and abs(r["norm"] - ref["normf"]) <= 1e-12 * ref["normf"], p
         assert_spectrum(r, ref["raw"], np.abs(ref["raw"]["Pk0"]), "fp32", odd=False, label=f"batch {p.NX}")
+
+
+def test_batch_state_is_reused_across_calls(gpu):
+    """capow_batch keeps its device state and instantiated graph for the next call with the same
+    signature: new values in the same arrays (the graph relaunched as it is), then new arrays (the
+    graph updated in place), each against single contexts; capow_batch_release frees the state and a
+    later call sets it up again."""
+    import torch
+
+    mocks = make_mocks(torch, gpu, 6, seed=21)
+
+    def check(out, mocks):
+        for (p, parts), (status, res) in zip(mocks, out):
+            assert status == cg.OK
+            with cg.PowerSpectrum(p, precision="fp32") as ps:
+                ps.paint(*parts[:4])
+                ref = ps.power()[0]
+            assert np.array_equal(res[0]["Nmodes"], ref["Nmodes"])
+            scale = np.abs(ref["Pk0"]).max()
+            for l in (0, 2, 4):
+                assert np.abs(res[0][f"Pk{l}"] - ref[f"Pk{l}"]).max() <= TOL["fp32"][0] * scale, (p, l)
+
+    check(cg.run_batch(mocks, precision="fp32", graph=True), mocks)
+    for p, parts in mocks:  # same arrays, new values
+        L = p.XMAX - p.XMIN
+        parts[0].copy_(torch.remainder(parts[0] * 1.37 + 0.1 * L, L))
+    check(cg.run_batch(mocks, precision="fp32", graph=True), mocks)
+    moved = [(p, tuple(None if a is None else a.clone() for a in parts)) for p, parts in mocks]  # new arrays
+    check(cg.run_batch(moved, precision="fp32", graph=True), moved)
+    cg.release_batch()
+    check(cg.run_batch(moved, precision="fp32", graph=False), moved)
+    cg.release_batch()

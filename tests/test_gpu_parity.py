@@ -76,21 +76,25 @@ FUSED = [(3, 3, 1, 1, 1, 64, 48, 40), (3, 0, 1, 0, 0, 128, 24, 30), (2, 3, 0, 2,
          (1, 0, 0, 1, 0, 16, 20, 18), (3, 1, 1, 1, 1, 256, 16, 12), (2, 2, 1, 0, 1, 2048, 8, 6),
          # power-of-two NZ: the z axis by k_zr2c into the transposed layout, the y axis by cuFFT C2C
          (3, 3, 1, 1, 1, 64, 48, 32), (2, 0, 1, 2, 0, 32, 20, 64), (1, 1, 0, 0, 1, 16, 12, 128),
-         (3, 2, 1, 1, 0, 128, 36, 32), (2, 3, 1, 0, 0, 64, 8, 2048)]
+         (3, 2, 1, 1, 0, 128, 36, 32), (2, 3, 1, 0, 0, 64, 8, 2048),
+         # power-of-two NY and NZ: the z and y axes in one launch (k_zy), NY from 16 to 1024
+         (3, 3, 1, 1, 1, 32, 16, 32), (2, 0, 1, 2, 0, 16, 64, 128), (1, 1, 1, 0, 1, 64, 32, 64),
+         (3, 2, 1, 1, 0, 16, 1024, 32), (2, 3, 0, 1, 1, 32, 128, 256)]
 
 
 @pytest.mark.parametrize("precision", ["fp32", "det"])
 @pytest.mark.parametrize("order,los,il,mom,odd,nx,ny,nz", FUSED)
 def test_fused_x_fft_bin_parity(gpu, precision, order, los, il, mom, odd, nx, ny, nz):
     """Power-of-two NX: the (y, z) axes (cuFFT 2-D, or k_zr2c + cuFFT C2C along y for a power-of-two
-    NZ) + the fused x-axis FFT and binning, against the oracle and against the 3-D cuFFT + binning
-    kernel path on the same paint."""
+    NZ, or with fft_path one_launch and power-of-two NY both in one k_zy launch) + the fused x-axis FFT
+    and binning, against the oracle and against the 3-D cuFFT + binning kernel path on the same paint."""
     kw = dict(BASE, Odd_Multipoles=odd)
     po, pc = params_pair(NX=nx, NY=ny, NZ=nz, InterpOrder=order, LOS=los, DoInterlacing=il, Momentum=mom, **kw)
     parts = particles(po, 4000, seed=300 + nx + order * 7 + mom)
     ref = oracle_run(po, parts, mom)
     res, _, _, _ = gpu_run(pc, parts, precision)
     res3, _, _, _ = gpu_run(pc, parts, precision, fft_path="3d")
+    res1, _, _, _ = gpu_run(pc, parts, precision, fft_path="one_launch")
     label = f"fused {precision} nx={nx} order={order} los={los} il={il} mom={mom} odd={odd}"
     raw = ref["raw"]
     if mom == 1:
@@ -99,6 +103,7 @@ def test_fused_x_fft_bin_parity(gpu, precision, order, los, il, mom, odd, nx, ny
         norm0 = np.abs(raw["Pk0"])
     assert_spectrum(res[0], raw, norm0, precision, odd=bool(odd), label=label)
     assert_spectrum(res[0], res3[0], norm0, precision, odd=bool(odd), label=label + " vs 3d")
+    assert_spectrum(res1[0], raw, norm0, precision, odd=bool(odd), label=label + " one launch")
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
@@ -351,3 +356,30 @@ def test_host_catalogue_in_chunks_matches_device_input(gpu):
             ps.power()
         assert e.value.status == cg.EBOUNDS
         assert ps.stats()["first_out_of_box"] == bad
+
+
+def test_zy_wait_that_runs_out_reports_timeout(gpu, monkeypatch):
+    """The one-launch z + y transform (fft_path one_launch) waits, per x-plane, for that plane's z transforms. Each wait is
+    bounded: with the test switch CAPOW_TEST_STALL_ZY=1 every y item waits for one z item more than
+    exists, its wait runs out (about a second), the launch stops, and capow_power returns
+    CAPOW_ETIMEOUT. The device stays usable: a context created without the switch gives the spectra
+    of the 3-D transform path."""
+    p = cg.Params(NX=32, NY=32, NZ=32, NK=12, Maxk=0.3, XMIN=0.0, XMAX=1000.0, YMIN=0.0, YMAX=1000.0,
+                  ZMIN=0.0, ZMAX=1000.0, InterpOrder=3, DoInterlacing=1, LOS=3, Momentum=0)
+    rng = np.random.default_rng(41)
+    x, y, z = (rng.uniform(1.0, 999.0, 20000) for _ in range(3))
+    v = rng.normal(0.0, 100.0, 20000)
+    monkeypatch.setenv("CAPOW_TEST_STALL_ZY", "1")
+    with cg.PowerSpectrum(p, precision="fp32", fft_path="one_launch") as ps:
+        ps.paint(x, y, z, v)
+        with pytest.raises(cg.CapowError) as e:
+            ps.power()
+        assert e.value.status == cg.ETIMEOUT
+    monkeypatch.delenv("CAPOW_TEST_STALL_ZY")
+    with cg.PowerSpectrum(p, precision="fp32", fft_path="one_launch") as ps:
+        ps.paint(x, y, z, v)
+        r = ps.power()[0]
+    with cg.PowerSpectrum(p, precision="fp32", fft_path="3d") as ps:
+        ps.paint(x, y, z, v)
+        r3 = ps.power()[0]
+    assert_spectrum(r, r3, np.abs(np.asarray(r3["Pk0"])), "fp32", odd=False, label="after timeout")
