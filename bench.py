@@ -247,7 +247,7 @@ def profile_case(args):
                                           torch_device=dev)
     d = [torch.from_numpy(a).to(dev) for a in (x, y, z, vz)]
     params = cg.Params(**dict(PARAMS, NX=256, NY=256, NZ=256, NK=81, Maxk=0.81))
-    with cg.PowerSpectrum(params, precision="fp32", spectra=["dd", "dp", "pp"]) as ps:
+    with cg.PowerSpectrum(params, precision="fp32", spectra=["dd", "dp", "pp"], fft_path=args.fft_path) as ps:
         for _ in range(args.warmup + args.steps):
             ps.paint(*d)
             ps.power()
@@ -390,7 +390,8 @@ def gpu_bench(args, world, rank, local):
     # every context runs on this stream, and every CUDA event below is recorded on it
     ts = torch.cuda.Stream(device=dev)
     sh = ts.cuda_stream
-    ps = cg.PowerSpectrum(params, precision="fp32", spectra=["dd", "dp", "pp"], device=local, stream=sh)
+    ps = cg.PowerSpectrum(params, precision="fp32", spectra=["dd", "dp", "pp"], device=local, stream=sh,
+                          fft_path=args.fft_path)
 
     def step_device():
         ps.paint(*d)
@@ -522,6 +523,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fft-path", default="auto", choices=["auto", "3d", "one_launch"],
+                    help="FFT path of the FP32 context (capow_options.fft_path)")
     ap.add_argument("--batch", action="store_true", help="run the batched-mocks workload instead (mocks/s)")
     ap.add_argument("--mocks", type=int, default=256)
     ap.add_argument("--scale", action="store_true", help="run the 1024^3 / 134M-particle workload instead")

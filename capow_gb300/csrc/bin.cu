@@ -1182,9 +1182,7 @@ struct ZyGeo {
   long long nitems;
 };
 
-CAPOW_HD unsigned zy_ytables_bytes(int log2ny) {
-  return align16(8u * xbin_tw_entries(log2ny)) + align16(4u * (1u << log2ny));
-}
+CAPOW_HD unsigned zy_ytables_bytes(int log2ny) { return align16(8u * xbin_tw_entries(log2ny)); }
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
   unsigned v;
@@ -1192,93 +1190,255 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
   return v;
 }
 
-// One y item: rows kz0 .. kz0 + ZY_KB - 1 (those below NZ/2+1) of plane x of slot sl, each NY complex
-// values along y, transformed in place (forward, unnormalised) through sd ([NY][ZY_KB + 1]).
-__device__ __forceinline__ void yfft_block(const ZyGeo &yg, const float2 *stwy, const int *sposy, float2 *out,
-                                           float2 *sd, int sl, int x, int kz0) {
-  constexpr int KB = ZY_KB, LKB = 3, P = KB + 1;
-  const int log2n = yg.log2ny, n = 1 << log2n, Q1 = n >> 3;
-  const int nrow = min(KB, yg.zg.nzc - kz0);
-  float2 *rows = out + sl * yg.zg.out_slot + ((long long)x * yg.zg.nzc + kz0) * n;
-  // first DIF stage (span NY) from the rows, lanes along a row (written by other CTAs of this launch:
-  // read through L2, never from a stale L1 line)
-  for (int u = threadIdx.x; u < (KB << (log2n - 3)); u += blockDim.x) {
-    const int jj = u & (Q1 - 1), r = u >> (log2n - 3);
-    const float2 *rp = rows + (long long)(r < nrow ? r : 0) * n + jj;
+// ------------------------------------------------------------ one row per warp (FP32, forward)
+// Base-8 digit reversal of g over D digits.
+template <int D>
+__device__ __forceinline__ int rev8(int g) {
+  int r = 0;
+#pragma unroll
+  for (int t = 0; t < D; t++) {
+    r = (r << 3) | (g & 7);
+    g >>= 3;
+  }
+  return r;
+}
+
+// Padded position in a warp's row buffer: one pad element per 8 spreads the strided accesses of every
+// stage (and the last stage's runs of 8) over the banks.
+__device__ __forceinline__ int wpad(int i) { return i + (i >> 3); }
+
+// One complex row of N = 2^LOG2N (16 <= N <= 2048) transformed by one warp with no block barrier: the
+// first in-place DIF stage (radix 8, span N) reads src, the middle radix-8 stages work in the warp's
+// buffer wb (N + N/8 values), and the last stage (radix 8, 4 or 2) writes dst in natural order (the
+// output of butterfly g, entry q, is frequency rev8(g) + q N/R). stw: the stage twiddle tables in the
+// layout of xbin_tw_entries. src is read through L2 (other CTAs of a launch may have written it).
+template <int LOG2N>
+__device__ __forceinline__ void warp_fft_row(const float2 *src, float2 *dst, float2 *wb, const float2 *stw,
+                                             int lane) {
+  constexpr int N = 1 << LOG2N;
+  constexpr int LR = LOG2N % 3 == 0 ? 3 : LOG2N % 3;  // log2 of the last stage's radix
+  constexpr int R = 1 << LR;
+  constexpr int S8 = (LOG2N - LR) / 3;  // radix-8 stages before the last (>= 1)
+  constexpr int Q1 = N >> 3;
+  for (int j = lane; j < Q1; j += 32) {
     float2 a[8];
 #pragma unroll
-    for (int q = 0; q < 8; q++) a[q] = r < nrow ? __ldcg(rp + q * Q1) : make_float2(0.0f, 0.0f);
+    for (int q = 0; q < 8; q++) a[q] = __ldcg(src + j + q * Q1);
     dft8(a);
-    if (jj > 0) twiddle8(a, stwy + 8 * jj);
-    float2 *p = sd + jj * P + r;
+    if (j > 0) twiddle8(a, stw + 8 * j);
 #pragma unroll
-    for (int q = 0; q < 8; q++) p[q * Q1 * P] = a[q];
+    for (int q = 0; q < 8; q++) wb[wpad(j + q * Q1)] = a[q];
   }
-  __syncthreads();
-  int l = log2n - 3, twoff = 8 * Q1;
-  for (; l >= 3; l -= 3) {
-    const int log2q = l - 3, Q = 1 << log2q, qs = Q * P;
-    for (int u = threadIdx.x; u < (KB << (log2n - 3)); u += blockDim.x) {
-      const int c = u & (KB - 1), v = u >> LKB;
-      const int jj = v & (Q - 1);
-      float2 *p = sd + (((v >> log2q) << l) + jj) * P + c;
+  __syncwarp();
+  int twoff = 8 * Q1;
+#pragma unroll
+  for (int t = 1; t < S8; t++) {
+    const int l = LOG2N - 3 * t, log2q = l - 3, Q = 1 << log2q;
+    for (int u = lane; u < (N >> 3); u += 32) {
+      const int jj = u & (Q - 1);
+      const int base = ((u >> log2q) << l) + jj;
       float2 a[8];
 #pragma unroll
-      for (int q = 0; q < 8; q++) a[q] = p[q * qs];
+      for (int q = 0; q < 8; q++) a[q] = wb[wpad(base + q * Q)];
       dft8(a);
-      if (jj > 0) twiddle8(a, stwy + twoff + 8 * jj);
+      if (jj > 0) twiddle8(a, stw + twoff + 8 * jj);
 #pragma unroll
-      for (int q = 0; q < 8; q++) p[q * qs] = a[q];
+      for (int q = 0; q < 8; q++) wb[wpad(base + q * Q)] = a[q];
     }
-    __syncthreads();
+    __syncwarp();
     if (Q > 1) twoff += 8 * Q;
   }
-  if (l == 2) {
-    for (int u = threadIdx.x; u < (KB << (log2n - 2)); u += blockDim.x) {
-      float2 *p = sd + ((u >> LKB) << 2) * P + (u & (KB - 1));
-      float2 a[4];
+  constexpr int NG = N / R;
+  for (int g = lane; g < NG; g += 32) {
+    float2 a[R];
 #pragma unroll
-      for (int q = 0; q < 4; q++) a[q] = p[q * P];
+    for (int q = 0; q < R; q++) a[q] = wb[wpad(R * g + q)];
+    if (R == 8) {
+      dft8(a);
+    } else if (R == 4) {
       dft4(a);
+    } else {
+      const float2 a0 = a[0];
+      a[0] = cadd(a0, a[1]);
+      a[1] = csub(a0, a[1]);
+    }
+    const int i0 = rev8<S8>(g);
 #pragma unroll
-      for (int q = 0; q < 4; q++) p[q * P] = a[q];
-    }
-    __syncthreads();
-  } else if (l == 1) {
-    for (int u = threadIdx.x; u < (KB << (log2n - 1)); u += blockDim.x) {
-      float2 *p = sd + ((u >> LKB) << 1) * P + (u & (KB - 1));
-      const float2 a0 = p[0], a1 = p[P];
-      p[0] = cadd(a0, a1);
-      p[P] = csub(a0, a1);
-    }
-    __syncthreads();
+    for (int q = 0; q < R; q++) dst[i0 + q * NG] = a[q];
   }
-  // natural order out: lanes along ky (coalesced rows); sposy[ky] is the row of Y[ky] in sd
-  for (int u = threadIdx.x; u < nrow * n; u += blockDim.x) {
-    const int ky = u & (n - 1), r = u >> log2n;
-    rows[(long long)r * n + ky] = sd[sposy[ky] * P + r];
+  __syncwarp();
+}
+
+// The same transform with the output in natural order in the warp's own row buffer buf (used for the
+// stages with wpad positions; N + N/8 values): the last stage's inputs are all read into registers
+// before any output is written. STREAM: the source is read once (evict-first loads).
+template <int LOG2N, bool STREAM>
+__device__ __forceinline__ void warp_fft_row_buf(const float2 *src, float2 *buf, const float2 *stw, int lane) {
+  constexpr int N = 1 << LOG2N;
+  constexpr int LR = LOG2N % 3 == 0 ? 3 : LOG2N % 3;
+  constexpr int R = 1 << LR;
+  constexpr int S8 = (LOG2N - LR) / 3;
+  constexpr int Q1 = N >> 3;
+  for (int j = lane; j < Q1; j += 32) {
+    float2 a[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) a[q] = STREAM ? __ldcs(src + j + q * Q1) : __ldcg(src + j + q * Q1);
+    dft8(a);
+    if (j > 0) twiddle8(a, stw + 8 * j);
+#pragma unroll
+    for (int q = 0; q < 8; q++) buf[wpad(j + q * Q1)] = a[q];
+  }
+  __syncwarp();
+  int twoff = 8 * Q1;
+#pragma unroll
+  for (int t = 1; t < S8; t++) {
+    const int l = LOG2N - 3 * t, log2q = l - 3, Q = 1 << log2q;
+    for (int u = lane; u < (N >> 3); u += 32) {
+      const int jj = u & (Q - 1);
+      const int base = ((u >> log2q) << l) + jj;
+      float2 a[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) a[q] = buf[wpad(base + q * Q)];
+      dft8(a);
+      if (jj > 0) twiddle8(a, stw + twoff + 8 * jj);
+#pragma unroll
+      for (int q = 0; q < 8; q++) buf[wpad(base + q * Q)] = a[q];
+    }
+    __syncwarp();
+    if (Q > 1) twoff += 8 * Q;
+  }
+  constexpr int NG = N / R, PER = (NG + 31) / 32;  // last-stage butterflies per lane
+  float2 a[PER][R];
+#pragma unroll
+  for (int p = 0; p < PER; p++) {
+    const int g = lane + 32 * p;
+    if (g < NG) {
+#pragma unroll
+      for (int q = 0; q < R; q++) a[p][q] = buf[wpad(R * g + q)];
+      if (R == 8) {
+        dft8(a[p]);
+      } else if (R == 4) {
+        dft4(a[p]);
+      } else {
+        const float2 a0 = a[p][0];
+        a[p][0] = cadd(a0, a[p][1]);
+        a[p][1] = csub(a0, a[p][1]);
+      }
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int p = 0; p < PER; p++) {
+    const int g = lane + 32 * p;
+    if (g < NG) {
+      const int i0 = rev8<S8>(g);
+#pragma unroll
+      for (int q = 0; q < R; q++) buf[i0 + q * NG] = a[p][q];
+    }
+  }
+  __syncwarp();
+}
+
+template <int LOG2N>
+__device__ __forceinline__ void warp_fft_rows(const ZyGeo &yg, const float2 *stwy, float2 *rows, float2 *sd, int nrow) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int N = 1 << LOG2N;
+  for (int r = w; r < nrow; r += (int)(blockDim.x >> 5))
+    warp_fft_row<LOG2N>(rows + (long long)r * N, rows + (long long)r * N, sd + w * (N + N / 8), stwy, lane);
+}
+
+// One y item: rows kz0 .. kz0 + ZY_KB - 1 (those below NZ/2+1) of plane x of slot sl, each NY complex
+// values along y, transformed in place (forward, unnormalised), one row per warp through that warp's
+// part of sd (ZY_KB warps, each NY + NY/8 values).
+__device__ __forceinline__ void yfft_block(const ZyGeo &yg, const float2 *stwy, float2 *out, float2 *sd, int sl,
+                                           int x, int kz0) {
+  const int nrow = min(ZY_KB, yg.zg.nzc - kz0);
+  float2 *rows = out + sl * yg.zg.out_slot + ((long long)x * yg.zg.nzc + kz0) * (1LL << yg.log2ny);
+  switch (yg.log2ny) {
+    case 4: warp_fft_rows<4>(yg, stwy, rows, sd, nrow); break;
+    case 5: warp_fft_rows<5>(yg, stwy, rows, sd, nrow); break;
+    case 6: warp_fft_rows<6>(yg, stwy, rows, sd, nrow); break;
+    case 7: warp_fft_rows<7>(yg, stwy, rows, sd, nrow); break;
+    case 8: warp_fft_rows<8>(yg, stwy, rows, sd, nrow); break;
+    case 9: warp_fft_rows<9>(yg, stwy, rows, sd, nrow); break;
+    case 10: warp_fft_rows<10>(yg, stwy, rows, sd, nrow); break;
+    default: warp_fft_rows<11>(yg, stwy, rows, sd, nrow); break;
+  }
+}
+
+// z items of k_zy with one warp per row (M <= 256): rows of M = 2^LOG2M complex values (z[n] = x[2n] + i x[2n+1])
+// transformed into natural order in their own buffer rows (stride M + M/8 + 1: the split's lanes run
+// across rows), then the real-input split and transposed store of zr2c_block.
+template <int LOG2M>
+__device__ __forceinline__ int zy_zrow_stride() {
+  return (1 << LOG2M) + (1 << LOG2M) / 8 + 1;
+}
+
+CAPOW_HD unsigned zy_zdata_bytes(int log2m, int zb) {
+  const unsigned M = 1u << log2m;
+  return log2m <= 8 ? align16(8u * zb * (M + M / 8 + 1)) : align16(8u * M * (zb + 1));
+}
+
+template <int ZB, int LOG2M>
+__device__ __forceinline__ void zr2c_block_warp(const ZrGeo &zg, const ZrTables &z, const float *in, float2 *out,
+                                                float2 *sd, int sl, int x, int y0) {
+  constexpr int LZB = ZB == 16 ? 4 : 3, M = 1 << LOG2M;
+  const int RS = zy_zrow_stride<LOG2M>();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const float *src = in + sl * zg.in_slot + (long long)x * zg.slice;
+  for (int r = w; r < ZB; r += nw) {
+    const int y = y0 + r;
+    if (y < zg.ny)
+      warp_fft_row_buf<LOG2M, true>(reinterpret_cast<const float2 *>(src + (long long)y * zg.row), sd + r * RS, z.stw,
+                                    lane);
+  }
+  __syncthreads();
+  const int r = threadIdx.x & (ZB - 1), y = y0 + r;
+  if (y < zg.ny) {
+    const float2 *zr = sd + r * RS;
+    float2 *dst = out + sl * zg.out_slot + (long long)x * zg.nzc * zg.ny + y;
+    for (int k = threadIdx.x >> LZB; k <= (M >> 1); k += blockDim.x >> LZB) {
+      const float2 zk = zr[k & (M - 1)];
+      const float2 zm = zr[(M - k) & (M - 1)];
+      const float2 A = make_float2(zk.x + zm.x, zk.y - zm.y);
+      const float2 B = make_float2(zk.x - zm.x, zk.y + zm.y);
+      const float2 wB = cmulf(z.stp[k], B);
+      dst[(long long)k * zg.ny] = make_float2(0.5f * (A.x + wB.y), 0.5f * (A.y - wB.x));
+      if (2 * k != M) dst[(long long)(M - k) * zg.ny] = make_float2(0.5f * (A.x - wB.y), -0.5f * (A.y + wB.x));
+    }
   }
 }
 
 template <int ZB>
-__global__ void __launch_bounds__(ZR_THREADS) k_zy(ZyGeo yg, BinTables t, const float *in, float2 *out,
+__device__ __forceinline__ void zy_zblock(const ZrGeo &zg, const ZrTables &z, const float *in, float2 *out,
+                                          float2 *sd, int sl, int x, int y0) {
+  switch (zg.log2m) {
+    case 4: zr2c_block_warp<ZB, 4>(zg, z, in, out, sd, sl, x, y0); break;
+    case 5: zr2c_block_warp<ZB, 5>(zg, z, in, out, sd, sl, x, y0); break;
+    case 6: zr2c_block_warp<ZB, 6>(zg, z, in, out, sd, sl, x, y0); break;
+    case 7: zr2c_block_warp<ZB, 7>(zg, z, in, out, sd, sl, x, y0); break;
+    case 8: zr2c_block_warp<ZB, 8>(zg, z, in, out, sd, sl, x, y0); break;
+    default: zr2c_block<ZB>(zg, z, in, out, sd, sl, x, y0); break;  // M >= 512: the block stages
+  }
+}
+
+template <int ZB>
+__global__ void __launch_bounds__(ZR_THREADS, 4) k_zy(ZyGeo yg, BinTables t, const float *in, float2 *out,
                                                    unsigned *ctr, DevStats *st) {
   extern __shared__ __align__(16) unsigned char smz[];
   const ZrGeo &zg = yg.zg;
   const int M = 1 << zg.log2m, ny = 1 << yg.log2ny;
-  const unsigned zdata = align16(8u * (unsigned)M * (ZB + 1)), ydata = align16(8u * (unsigned)ny * (ZY_KB + 1));
+  const unsigned zdata = zy_zdata_bytes(zg.log2m, ZB), ydata = align16(8u * ZY_KB * (ny + ny / 8));
   float2 *sd = (float2 *)smz;  // the data area of whichever item runs
   unsigned char *tb = smz + (zdata > ydata ? zdata : ydata);
   const ZrTables z = zr2c_load_tables(t, zg.log2m, tb);
   tb += zr2c_tables_bytes(zg.log2m);
   float2 *stwy = (float2 *)tb;
-  int *sposy = (int *)(tb + align16(8u * xbin_tw_entries(yg.log2ny)));
   for (int l = yg.log2ny, off = 0; l >= 4; off += 8 << (l - 3), l -= 3) {
     const int step = ny >> l;
     for (int e = threadIdx.x; e < (8 << (l - 3)); e += blockDim.x)
       stwy[off + e] = t.twy[((e & 7) * (e >> 3) * step) & (ny - 1)];
   }
-  for (int k = threadIdx.x; k < ny; k += blockDim.x) sposy[k] = xfft_pos(yg.log2ny, k);
   __shared__ long long s_item;
   __shared__ int s_ok;
   unsigned *done = ctr + 2;  // [slot][plane]: finished z items
@@ -1314,7 +1474,7 @@ __global__ void __launch_bounds__(ZR_THREADS) k_zy(ZyGeo yg, BinTables t, const 
     }
     if (!is_y) {
       const int sl = (int)(r / zg.nyb), y0 = (int)(r - (long long)sl * zg.nyb) * ZB;
-      zr2c_block<ZB>(zg, z, in, out, sd, sl, (int)plane, y0);
+      zy_zblock<ZB>(zg, z, in, out, sd, sl, (int)plane, y0);
       __threadfence();  // this thread's stores, before the item is counted done
       __syncthreads();
       if (threadIdx.x == 0) atomicAdd(done + (long long)sl * zg.nx + plane, 1u);
@@ -1334,7 +1494,7 @@ __global__ void __launch_bounds__(ZR_THREADS) k_zy(ZyGeo yg, BinTables t, const 
       }
       __syncthreads();
       if (!s_ok) break;
-      yfft_block(yg, stwy, sposy, out, sd, sl, (int)plane, kz0);
+      yfft_block(yg, stwy, out, sd, sl, (int)plane, kz0);
     }
   }
 }
@@ -1393,7 +1553,7 @@ template <int ZB>
 static void launch_zy_t(cudaStream_t s, const ZyGeo &yg, const BinTables &t, const float *in, float2 *out,
                         unsigned *ctr, DevStats *st) {
   const unsigned M = 1u << yg.zg.log2m, ny = 1u << yg.log2ny;
-  const unsigned zdata = align16(8u * M * (ZB + 1)), ydata = align16(8u * ny * (ZY_KB + 1));
+  const unsigned zdata = zy_zdata_bytes(yg.zg.log2m, ZB), ydata = align16(8u * ZY_KB * (ny + ny / 8));
   const size_t smem = (zdata > ydata ? zdata : ydata) + zr2c_tables_bytes(yg.zg.log2m) + zy_ytables_bytes(yg.log2ny);
   cudaFuncSetAttribute(k_zy<ZB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int per_sm = 1, dev = 0, nsm = 152;
