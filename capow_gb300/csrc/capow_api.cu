@@ -211,8 +211,8 @@ extern "C" int capow_create(const capow_params *p, const capow_options *opt, cap
     FAIL(c, CAPOW_ENOMEM, "device allocation failed (grids need %.2f GB)", eb * c->grid_elems * c->nslot / 1e9);
   CK(c, cudaMallocHost((void **)&c->h_bins, sizeof(double) * NPROD * (5 * nk + n2d)));
   CK(c, cudaMallocHost((void **)&c->h_st, sizeof(DevStats)));
-  {  // tile tables (the FP64 tiles hold 8-byte cells, as the deterministic path's)
-    c->tg = choose_tiles(c->g, c->nslot, c->prec != CAPOW_FP32_MIXED);
+  if (!f64) {
+    c->tg = choose_tiles(c->g, c->nslot, c->prec == CAPOW_FP32_DETERMINISTIC);
     c->pb.counts = (unsigned *)dalloc(c, sizeof(unsigned) * c->tg.ntiles);
     c->pb.offsets = (unsigned *)dalloc(c, sizeof(unsigned) * (c->tg.ntiles + 1));
     c->pb.cursor = (unsigned *)dalloc(c, sizeof(unsigned) * c->tg.ntiles);
@@ -395,18 +395,8 @@ int enqueue_paint(capow_ctx *c, const capow_particles &d) {
   CK(c, cudaMemsetAsync(c->st, 0, sizeof(DevStats), c->stream));
   if (!c->quiet) CK(c, cudaEventRecord(c->ev[0], c->stream));
   if (c->prec == CAPOW_FP64) {
-    // tiles of FP64 cells, every particle by the exact rules; the record buffer holds one index per
-    // (particle, tile touched), sized from the estimate (an overflow repaints with the exact count)
-    if (!c->pb.edge_count) CK(c, cudaMalloc(&c->pb.edge_count, sizeof(unsigned)));
-    const unsigned long long want = (unsigned long long)(tile_dup_estimate(c->g, c->tg) * 1.25 * n) + 65536;
-    if (c->pb.capacity < want / 2) {
-      int rc = ensure_records(c, want, false);
-      if (rc) return rc;
-    }
-    c->pb.bucket_cap = 0;
-    c->tile_timed = false;
-    launch_paint64_tiles(c->stream, c->g, c->fs, c->tg, d.dtype, d.x, d.y, d.z, d.vlos, d.w, n, gp, c->pb, c->st,
-                         &c->launches);
+    CK(c, cudaMemsetAsync(c->grid_base, 0, 8 * c->grid_elems * c->nslot, c->stream));
+    launch_paint64(c->stream, c->g, c->fs, d.dtype, d.x, d.y, d.z, d.vlos, d.w, n, gp, c->st, &c->launches);
   } else {
     if (!c->pb.edge_count) CK(c, cudaMalloc(&c->pb.edge_count, sizeof(unsigned)));
     if (c->pb.edge_cap < (unsigned long long)n + 1) {  // every particle could sit on an edge
@@ -466,7 +456,7 @@ int enqueue_paint(capow_ctx *c, const capow_particles &d) {
 // Size the FP32 record and edge buffers for catalogues of up to nmax particles (so that a later
 // enqueue_paint allocates nothing).
 int prepare_paint_buffers(capow_ctx *c, unsigned long long nmax, bool weights) {
-  if (c->prec == CAPOW_FP64) weights = false;  // the FP64 records are particle indices only
+  if (c->prec == CAPOW_FP64) return CAPOW_OK;
   if (!c->pb.edge_count) CK(c, cudaMalloc(&c->pb.edge_count, sizeof(unsigned)));
   if (c->pb.edge_cap < nmax + 1) {
     if (c->pb.edge_list) cudaFree(c->pb.edge_list);

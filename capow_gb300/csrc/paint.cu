@@ -118,7 +118,6 @@ __global__ void __launch_bounds__(256) k_paint64(Geom g, FieldSpec fs, PIn<T> in
       }
       if (!exact_axes(g, px, py, pz, ax, ay, az)) continue;
       if (stn == 0) l_grid += w;
-      if (!grids.g[0]) continue;  // statistics only (the FP64 tile path deposits in k_tile_paint64)
       for (int f = 0; f < nf; f++) {
         double *gp = (double *)grids.g[stn * nf + f];
         double dsum = 0.0;
@@ -336,10 +335,7 @@ __device__ __forceinline__ int tile_key(const TileGeo &tg, bool has, const AxisT
 // can be aggregated over runs of lanes: particles that arrive in spatial order share their tiles.
 template <typename T>
 __global__ void __launch_bounds__(256) k_count(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in, long long n,
-                                               unsigned *counts, DevStats *st, int mode) {
-  // mode 1: FP32 path (edge particles left to k_edge_fixup); 0: deterministic path (every particle in
-  // the tiles); 2: FP64 tile path (tile counts only: its statistics come from the FP64 pass)
-  const bool split_edge = mode == 1, stats = mode != 2;
+                                               unsigned *counts, DevStats *st, int split_edge) {
   float f_read = 0, f_out = 0, f_nsq = 0, f_v[4] = {0, 0, 0, 0}, f_abs[2] = {0, 0}, f_grid = 0;
   int fatal = 0, nonfin = 0;
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -369,7 +365,7 @@ __global__ void __launch_bounds__(256) k_count(Geom g, FieldSpec fs, TileGeo tg,
         f_abs[1] += fabsf(pb);
         if (!footprint(g, tg, p.sx, p.sy, p.sz, TX, TY, TZ)) {
           f_out += 1.0f;  // clearly outside the box (src/read_data.c:81-88)
-          if (g.los == 0 && stats) {
+          if (g.los == 0) {
             fatal = 1;
             atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)i);
           }
@@ -397,7 +393,6 @@ __global__ void __launch_bounds__(256) k_count(Geom g, FieldSpec fs, TileGeo tg,
   const float vals[10] = {f_read, f_out, f_nsq, f_v[0], f_v[1], f_v[2], f_v[3], f_abs[0], f_abs[1], f_grid};
   double *const dst[10] = {&st->nread, &st->nout, &st->nsq, &st->vr[0], &st->vr[1], &st->vr[2], &st->vr[3],
                            &st->absw[0], &st->absw[1], &st->ngrid};
-  if (!stats) return;
   block_add_f<10>(vals, dst);
   if (fatal) atomicOr(&st->fatal, 1);
   if (nonfin) atomicOr(&st->nonfinite, 1);
@@ -449,7 +444,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_scatter(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in, long long n,
                                                  unsigned *cursor, float4 *recs, float *recw,
                                                  unsigned long long capacity, unsigned *edge_list,
-                                                 unsigned *edge_count, int all_exact) {
+                                                 unsigned *edge_count) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i0 = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); i0 < n; i0 += stride) {
     const long long i = i0 + (threadIdx.x & 31);
@@ -461,7 +456,7 @@ __global__ void __launch_bounds__(256) k_scatter(Geom g, FieldSpec fs, TileGeo t
     if (i < n) {
       const Prep p = prep32(g, fs, in, i);
       if (p.fin && footprint(g, tg, p.sx, p.sy, p.sz, TX, TY, TZ)) {
-        const bool edge = all_exact || is_edge(g, p.sx, p.sy, p.sz);
+        const bool edge = is_edge(g, p.sx, p.sy, p.sz);
         if (edge && edge_list) {  // painted by k_edge_fixup after the tiles
           edge_list[atomicAdd(edge_count, 1u)] = (unsigned)i;
         } else {
@@ -1411,7 +1406,7 @@ static void run_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, cons
   k_count<T><<<nb, th, 0, s>>>(g, fs, tg, in, n, b.counts, st, split ? 1 : 0);
   k_scan<<<1, 1024, 0, s>>>(b.counts, tg.ntiles, b.offsets, b.cursor, st, b.capacity, b.fixed_scale);
   k_scatter<T><<<nb, th, 0, s>>>(g, fs, tg, in, n, b.cursor, b.recs, in.w ? b.recw : nullptr, b.capacity,
-                                 split ? b.edge_list : nullptr, b.edge_count, 0);
+                                 split ? b.edge_list : nullptr, b.edge_count);
   if (det) {
     const int nslot = fs.nfields * (g.interlace ? 2 : 1);
     const size_t smem = tile_smem_bytes(tg, nslot, 1);
@@ -1443,129 +1438,5 @@ void launch_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, const Ti
   } else {
     PIn<float> in{(const float *)x, (const float *)y, (const float *)z, (const float *)v, (const float *)w};
     run_paint32<float>(s, g, fs, tg, deterministic, in, n, grids, b, st, launches);
-  }
-}
-
-// ===================================================================================== FP64 tiles
-// The cell of grid index (ix, iy, iz) as canon_index places it (the CIC y == NY write lands in row 0 of
-// the next x slice, halo slices fold onto x = 0.. for LOS == 0 and are dropped otherwise, z beyond NZ
-// is dropped), as tile-local coordinates; false when dropped.
-__device__ __forceinline__ bool canon_cell(const Geom &g, int ix, int iy, int iz, int &cx, int &cy) {
-  if (iz >= g.nz) return false;
-  if (iy >= g.ny) {
-    iy -= g.ny;
-    ix += 1;
-  }
-  if (ix >= g.nx) {
-    if (g.los != 0 || ix - g.nx >= g.order) return false;
-    ix -= g.nx;
-  }
-  cx = ix;
-  cy = iy;
-  return true;
-}
-
-// FP64 path: one CTA per tile; every record is a particle index (k_scatter with all_exact), painted by
-// the reference's exact FP64 rules (exact_axes: src/read_data.c:514-745 with its quirks) into FP64
-// shared-memory tiles of every slot. Lane = record; each tap is one FP64 shared atomic (the weights
-// multiplied in the order of k_paint64). The tile is written out in FP64 with its slots' DC sums.
-// The statistics of the paint come from k_paint64 run without deposits.
-template <typename T>
-__global__ void __launch_bounds__(256) k_tile_paint64(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in, long long n,
-                                                      const unsigned *offsets, const float4 *recs,
-                                                      unsigned long long capacity, GridPtrs grids, DevStats *st) {
-  extern __shared__ __align__(16) double smd[];
-  const int nf = fs.nfields, nst = g.interlace ? 2 : 1, nslot = nf * nst;
-  const int tile = blockIdx.x;
-  const int bz = tile % tg.nbz, by = (tile / tg.nbz) % tg.nby, bx = tile / (tg.nbz * tg.nby);
-  const int x0 = bx * tg.tx, y0 = by * tg.ty, z0 = bz * tg.tz;
-  const int ex = min(tg.tx, g.nx - x0), ey = min(tg.ty, g.ny - y0), ez = min(tg.tz, g.nz - z0);
-  for (int c = threadIdx.x; c < nslot * tg.slot; c += blockDim.x) smd[c] = 0.0;
-  __syncthreads();
-  unsigned rb = offsets[tile], re = offsets[tile + 1];
-  if (re > capacity) re = (unsigned)capacity;
-  if (rb > re) rb = re;
-  for (unsigned r = rb + threadIdx.x; r < re; r += blockDim.x) {
-    const unsigned idx = __float_as_uint(recs[r].y);
-    if ((long long)idx >= n) continue;
-    double x, y, z, v, w;
-    exact_pos(g, fs, in, idx, x, y, z, v, w);
-    const double val[2] = {wpow64(w, v, fs.ea), wpow64(w, v, fs.eb)};
-    for (int stn = 0; stn < nst; stn++) {
-      AxisTaps ax, ay, az;
-      const double px = stn ? DADD(x, g.hx) : x, py = stn ? DADD(y, g.hy) : y, pz = stn ? DADD(z, g.hz) : z;
-      if (!exact_axes(g, px, py, pz, ax, ay, az)) continue;
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        if (c >= az.n || !az.on[c]) continue;
-        const int lz = az.idx[c] - z0;
-        if (az.idx[c] >= g.nz || lz < 0 || lz >= ez) continue;
-#pragma unroll
-        for (int b = 0; b < 3; b++) {
-          if (b >= ay.n || !ay.on[b]) continue;
-#pragma unroll
-          for (int a = 0; a < 3; a++) {
-            if (a >= ax.n || !ax.on[a]) continue;
-            int cx, cy;
-            if (!canon_cell(g, ax.idx[a], ay.idx[b], az.idx[c], cx, cy)) continue;
-            const int lx = cx - x0, ly = cy - y0;
-            if (lx < 0 || lx >= ex || ly < 0 || ly >= ey) continue;
-            const int cell = lx * tg.px + ly * tg.py + lz;
-            for (int f = 0; f < nf; f++)
-              atomicAdd(smd + (stn * nf + f) * tg.slot + cell, DMUL(DMUL(DMUL(val[f], ax.w[a]), ay.w[b]), az.w[c]));
-          }
-        }
-      }
-    }
-  }
-  __syncthreads();
-  // write the tile (FP64 cells, each cell of the FFT region written once) and the slots' DC sums
-  const int tsz = tg.tx * tg.ty * tg.tz;
-  for (int slot = 0; slot < nslot; slot++) {
-    double *gp = (double *)grids.g[slot];
-    const double *sv = smd + slot * tg.slot;
-    double dsum = 0.0;
-    for (int c = threadIdx.x; c < tsz; c += blockDim.x) {
-      const int rz = c & (tg.tz - 1), ly = (c >> tg.lz) & (tg.ty - 1), lx = c >> (tg.lz + tg.ly);
-      if (lx >= ex || ly >= ey || rz >= ez) continue;
-      const double val = sv[lx * tg.px + ly * tg.py + rz];
-      gp[(long long)(x0 + lx) * g.slice + (long long)(y0 + ly) * g.row + z0 + rz] = val;
-      dsum += val;
-    }
-    const double vals[1] = {dsum};
-    double *const dst1[1] = {&st->dc[slot]};
-    block_add<1>(vals, dst1);
-  }
-}
-
-template <typename T>
-static void run_paint64_tiles(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, PIn<T> in,
-                              long long n, const GridPtrs &grids, const PaintBufs &b, DevStats *st, long long *launches) {
-  const int th = 256;
-  long long nbl = (n + th - 1) / th;
-  const int nb = (int)(nbl < 1 ? 1 : (nbl > 152 * 8 ? 152 * 8 : nbl));
-  GridPtrs none;
-  memset(&none, 0, sizeof none);
-  k_paint64<T><<<grid_blocks(n, th), th, 0, s>>>(g, fs, in, n, none, st);  // FP64 statistics only
-  cudaMemsetAsync(b.counts, 0, sizeof(unsigned) * tg.ntiles, s);
-  k_count<T><<<nb, th, 0, s>>>(g, fs, tg, in, n, b.counts, st, 2);
-  k_scan<<<1, 1024, 0, s>>>(b.counts, tg.ntiles, b.offsets, b.cursor, st, b.capacity, b.fixed_scale);
-  k_scatter<T><<<nb, th, 0, s>>>(g, fs, tg, in, n, b.cursor, b.recs, nullptr, b.capacity, nullptr, b.edge_count, 1);
-  const int nslot = fs.nfields * (g.interlace ? 2 : 1);
-  const size_t smem = sizeof(double) * (size_t)nslot * tg.slot;
-  cudaFuncSetAttribute(k_tile_paint64<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_tile_paint64<T><<<tg.ntiles, th, smem, s>>>(g, fs, tg, in, n, b.offsets, b.recs, b.capacity, grids, st);
-  *launches += 5;
-}
-
-void launch_paint64_tiles(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, int dtype,
-                          const void *x, const void *y, const void *z, const void *v, const void *w, long long n,
-                          const GridPtrs &grids, const PaintBufs &b, DevStats *st, long long *launches) {
-  if (dtype == CAPOW_F64) {
-    PIn<double> in{(const double *)x, (const double *)y, (const double *)z, (const double *)v, (const double *)w};
-    run_paint64_tiles<double>(s, g, fs, tg, in, n, grids, b, st, launches);
-  } else {
-    PIn<float> in{(const float *)x, (const float *)y, (const float *)z, (const float *)v, (const float *)w};
-    run_paint64_tiles<float>(s, g, fs, tg, in, n, grids, b, st, launches);
   }
 }

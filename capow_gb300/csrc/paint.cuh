@@ -73,12 +73,6 @@ void launch_paint64(cudaStream_t s, const Geom &g, const FieldSpec &fs, int dtyp
                     const void *z, const void *v, const void *w, long long n, const GridPtrs &grids, DevStats *st,
                     long long *launches);
 
-// FP64 path through the tiles: exact FP64 statistics (k_paint64 without deposits), the two-pass tile
-// binning with every record a particle index, and k_tile_paint64 (FP64 shared-memory tiles).
-void launch_paint64_tiles(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, int dtype,
-                          const void *x, const void *y, const void *z, const void *v, const void *w, long long n,
-                          const GridPtrs &grids, const PaintBufs &b, DevStats *st, long long *launches);
-
 void launch_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, int deterministic,
                     int dtype, const void *x, const void *y, const void *z, const void *v, const void *w,
                     long long n, const GridPtrs &grids, const PaintBufs &b, DevStats *st, long long *launches);
