@@ -40,11 +40,12 @@ def build(force: bool = False, ref_src: Optional[str] = None) -> str:
     """Compile liborc.so, and oracle/_ref/capow_ref when the reference sources are given (``ref_src``
     or the CAPOW_REFERENCE_SRC environment variable) and present."""
     os.makedirs(BUILD, exist_ok=True)
-    srcs = [os.path.join(HERE, f) for f in ("capow_oracle.c", "orc_fft.c")]
-    hdrs = [os.path.join(HERE, f) for f in ("capow_oracle.h", "orc_fft.h")]
+    srcs = [os.path.join(HERE, f) for f in ("capow_oracle.c", "orc_fft.c", "orc_gsl.c")]
+    hdrs = [os.path.join(HERE, f) for f in ("capow_oracle.h", "orc_fft.h", "shims/gsl/gsl_spline.h",
+                                            "shims/gsl/gsl_integration.h")]
     newest = max(os.path.getmtime(f) for f in srcs + hdrs)
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
-        subprocess.check_call(["gcc", *_CFLAGS, "-o", LIB, *srcs, "-lm"])
+        subprocess.check_call(["gcc", *_CFLAGS, "-I", HERE, "-o", LIB, *srcs, "-lm"])
     ref_src = ref_src or os.environ.get(REF_SRC_ENV)
     if ref_src and os.path.isdir(os.path.join(ref_src, "src")):
         subprocess.check_call(
@@ -99,6 +100,19 @@ class Params:
     LOS: int = 0
     Momentum: int = 0
     Odd_Multipoles: int = 0
+    # survey-mode tags (src/read_params.c:65-227); the periodic path ignores them
+    Periodic: int = 1
+    Coord_Type: int = 0
+    X_Origin: float = 0.0
+    Y_Origin: float = 0.0
+    Z_Origin: float = 0.0
+    REDMININ: float = 0.0
+    REDMAXIN: float = 1.0
+    NOBJ_Max: int = 1
+    NBAR_Column: int = -1
+    SkyArea: float = 1.0
+    FKP_Column: int = -1
+    FKP_Pk: float = 0.0
 
     def to_c(self) -> OrcParams:
         return OrcParams(self.NX, self.NY, self.NZ, self.XMIN, self.XMAX, self.YMIN, self.YMAX, self.ZMIN,
@@ -114,9 +128,12 @@ class Params:
             DoInterlacing=self.DoInterlacing, InterpOrder=self.InterpOrder, NK=self.NK, NMU=self.NMU,
             Output2D=self.Output2D, OutputLog=self.OutputLog, Mink=repr(float(self.Mink)),
             Maxk=repr(float(self.Maxk)), Omega_m=repr(float(self.Omega_m)), Redshift=repr(float(self.Redshift)),
-            Periodic=1, LOS=self.LOS, Survey=0, Momentum=self.Momentum, X_Origin=0, Y_Origin=0, Z_Origin=0,
-            REDMININ=0, REDMAXIN=1, NOBJ_Max=1, Coord_Type=0, x_Column=1, y_Column=2, z_Column=3,
-            NBAR_Column=-1, SkyArea=1, FKP_Column=-1, FKP_Pk=0, FKP_Pk_mom=0, FKP_Pk_cross=0,
+            Periodic=self.Periodic, LOS=self.LOS, Survey=0 if self.Periodic else 1, Momentum=self.Momentum,
+            X_Origin=repr(float(self.X_Origin)), Y_Origin=repr(float(self.Y_Origin)),
+            Z_Origin=repr(float(self.Z_Origin)), REDMININ=repr(float(self.REDMININ)),
+            REDMAXIN=repr(float(self.REDMAXIN)), NOBJ_Max=self.NOBJ_Max, Coord_Type=self.Coord_Type, x_Column=1,
+            y_Column=2, z_Column=3, NBAR_Column=self.NBAR_Column, SkyArea=repr(float(self.SkyArea)),
+            FKP_Column=self.FKP_Column, FKP_Pk=repr(float(self.FKP_Pk)), FKP_Pk_mom=0, FKP_Pk_cross=0,
             Odd_Multipoles=self.Odd_Multipoles,
         )
         with open(path, "w") as f:
@@ -407,3 +424,120 @@ def run_ref_binary(p: Params, workdir: str, x, y, z, vx, vy, vz, grids: bool = F
 if __name__ == "__main__":  # pragma: no cover
     build(force="--force" in sys.argv)
     print(LIB)
+
+
+# --------------------------------------------------------------------------- survey mode
+class OrcSurvey(ctypes.Structure):
+    _fields_ = [("x_origin", ctypes.c_double), ("y_origin", ctypes.c_double), ("z_origin", ctypes.c_double)]
+
+
+def _survey_lib():
+    L = lib()
+    if not getattr(L, "_survey_bound", False):
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        P = ctypes.POINTER(OrcParams)
+        L.orc_survey_paint.restype = ctypes.c_double
+        L.orc_survey_paint.argtypes = [P, ctypes.c_int64, dp, dp, dp, dp, ctypes.c_double, dp, dp]
+        L.orc_survey_power.argtypes = [P, ctypes.POINTER(OrcSurvey), dp, dp, dp, dp, dp, dp, dp, ip]
+        L.orc_survey_redshift.restype = ctypes.c_double
+        L.orc_survey_redshift.argtypes = [ctypes.c_double, ctypes.c_double]
+        L._survey_bound = True
+    return L
+
+
+def _seqsum(a) -> float:
+    """Left-to-right double sum, as the reference's loops add (numpy's sum is pairwise)."""
+    a = np.asarray(a, dtype=np.float64)
+    return float(np.cumsum(a)[-1]) if a.size else 0.0
+
+
+def survey_read(p: Params, path: str, randoms: bool) -> dict:
+    """read_survey_serial_ascii (src/read_data.c:184-361) for Cartesian input (Coord_Type 0) with the number
+    density from its column (NBAR_Column > 0): data lines hold 12 numbers, randoms 8; the weight is the
+    4th, the number density the 5th (the reader copies that column into nbar, :244-250). Objects whose
+    redshift (the distance table's inverse at |x|, :259-266) lies outside [REDMININ, REDMAXIN] are dropped;
+    an object outside the grid less the interpolation margin is the reference's fatal error (:293-299)."""
+    L = _survey_lib()
+    a = np.loadtxt(path, comments="#", ndmin=2)
+    need = 8 if randoms else 12
+    if a.shape[1] < need:
+        raise ValueError(f"survey catalogue {path} has {a.shape[1]} columns, the reference reads {need}")
+    dx, dy, dz = (p.XMAX - p.XMIN) / p.NX, (p.YMAX - p.YMIN) / p.NY, (p.ZMAX - p.ZMIN) / p.NZ
+    xlo, xhi = p.XMIN + (p.InterpOrder - 1) * dx, p.XMAX - (p.InterpOrder - 1) * dx
+    ylo, yhi = p.YMIN + (p.InterpOrder - 1) * dy, p.YMAX - (p.InterpOrder - 1) * dy
+    zlo, zhi = p.ZMIN + (p.InterpOrder - 1) * dz, p.ZMAX - (p.InterpOrder - 1) * dz
+    if p.DoInterlacing:
+        xhi -= 0.5 * dx
+        yhi -= 0.5 * dy
+        zhi -= 0.5 * dz
+    keep = []
+    red = []
+    for i in range(a.shape[0]):
+        tx, ty, tz = a[i, 0], a[i, 1], a[i, 2]
+        tred = L.orc_survey_redshift(p.Omega_m, float(np.sqrt(tx * tx + ty * ty + tz * tz)))
+        if tred < p.REDMININ or tred > p.REDMAXIN:
+            continue
+        if tx < xlo or tx >= xhi or ty < ylo or ty >= yhi or tz < zlo or tz >= zhi:
+            raise ValueError(f"object out of grid bounds for chosen InterpOrder: x={tx}, y={ty}, z={tz}")
+        keep.append(i)
+        red.append(tred)
+    # the reference keeps each object in float fields (struct survey_data, src/vars.h:136-142)
+    k = np.array(keep, dtype=np.int64)
+    f32 = np.float32
+    out = {"x": a[k, 0].astype(f32), "y": a[k, 1].astype(f32), "z": a[k, 2].astype(f32),
+           "weight": a[k, 3].astype(f32), "redshift": np.array(red).astype(f32), "nread": a.shape[0]}
+    out["nbar"] = a[k, 4].astype(f32) if p.NBAR_Column > 0 else np.zeros(len(k), f32)
+    return out
+
+
+def survey_fkp(p: Params, cat: dict) -> None:
+    """compute_fkp for the density (src/read_data.c:450-466): weight *= 1 / (1 + nbar FKP_Pk) in double, stored
+    back into the float weight, in place."""
+    w = cat["weight"].astype(np.float64) * (1.0 / (1.0 + cat["nbar"].astype(np.float64) * p.FKP_Pk))
+    cat["weight"] = w.astype(np.float32)
+
+
+def survey_run(p: Params, data_path: str, rand_path: str, grids: bool = False) -> dict:
+    """The survey branch of main for the density (src/main.c:77-95, 149-204, 226-258, 279-288): read data and
+    randoms, FKP weights, alpha / shot / norm, data minus alpha randoms painted, the Yamamoto multipoles,
+    output_power's normalisation."""
+    L = _survey_lib()
+    data = survey_read(p, data_path, False)
+    rand = survey_read(p, rand_path, True)
+    if p.FKP_Column < 0:
+        survey_fkp(p, data)
+        survey_fkp(p, rand)
+    wd, wr = data["weight"], rand["weight"]  # float32: the products below are float products, as in C
+    data_nbw, data_nbwsq, data_nbsqwsq = _seqsum(wd), _seqsum(wd * wd), _seqsum(wd * wd * data["nbar"])
+    rand_nbw, rand_nbwsq, rand_nbsqwsq = _seqsum(wr), _seqsum(wr * wr), _seqsum(wr * wr * rand["nbar"])
+    wd, wr = wd.astype(np.float64), wr.astype(np.float64)
+    for c in (data, rand):
+        for a in ("x", "y", "z"):
+            c[a] = c[a].astype(np.float64)
+    alpha = data_nbw / rand_nbw
+    rand_nbwsq *= alpha * alpha
+    rand_nbsqwsq *= alpha
+    shot = data_nbwsq + rand_nbwsq
+    norm = rand_nbsqwsq
+    pc = p.to_c()
+    nd = lib().orc_grid_doubles(ctypes.byref(pc))
+    ddg = np.zeros(nd)
+    ddgi = np.zeros(nd) if p.DoInterlacing else None
+    ngrid_d = L.orc_survey_paint(ctypes.byref(pc), len(wd), _dp(data["x"]), _dp(data["y"]), _dp(data["z"]), _dp(wd),
+                                 1.0, _dp(ddg), _dp(ddgi))
+    ngrid_r = L.orc_survey_paint(ctypes.byref(pc), len(wr), _dp(rand["x"]), _dp(rand["y"]), _dp(rand["z"]), _dp(wr),
+                                 -alpha, _dp(ddg), _dp(ddgi))
+    painted = {"ddg": ddg.copy(), "ddg_interlace": None if ddgi is None else ddgi.copy()} if grids else None
+    NK = p.NK
+    pk = [np.zeros(NK) for _ in range(5)]
+    nm = np.zeros(NK, np.int32)
+    sp = OrcSurvey(p.X_Origin, p.Y_Origin, p.Z_Origin)
+    L.orc_survey_power(ctypes.byref(pc), ctypes.byref(sp), _dp(ddg), _dp(ddgi), *[_dp(a) for a in pk], _ip(nm))
+    raw = {"Pk0": pk[0], "Pk1": pk[1], "Pk2": pk[2], "Pk3": pk[3], "Pk4": pk[4], "Nmodes": nm}
+    normed, last = normalise(p, raw, shot, norm)
+    return {"raw": raw, "norm": normed, "last": last, "alpha": alpha, "shot": shot, "normf": norm,
+            "ndata": len(wd), "nrand": len(wr), "ngrid_data": ngrid_d, "ngrid_rand": ngrid_r / -alpha,
+            "sums": {"data_nbw": data_nbw, "data_nbwsq": data_nbwsq, "data_nbsqwsq": data_nbsqwsq,
+                     "rand_nbwsq": rand_nbwsq, "rand_nbsqwsq": rand_nbsqwsq},
+            "data": data, "rand": rand, "painted": painted}

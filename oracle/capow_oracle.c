@@ -3,6 +3,8 @@
  * Local_nx = NX, Local_nxtra = NX + InterpOrder (src/main.c:1131-1135). */
 #include "capow_oracle.h"
 #include "orc_fft.h"
+#include "shims/gsl/gsl_integration.h"
+#include "shims/gsl/gsl_spline.h"
 
 #include <math.h>
 #include <stdlib.h>
@@ -456,4 +458,321 @@ int orc_normalise(const orc_params *p, double shot, double norm, double *pk0, do
   }
   free(fill);
   return last;
+}
+
+/* ------------------------------------------------------------------ survey mode */
+/* add_to_grid with the Survey branches (src/read_data.c:514-745; single rank: the TSC acceptance of
+ * :617-619, the clamps of :577-590 (CIC) and :672-688 (TSC)): a neighbour index reaching the axis
+ * limit (Local_nxtra for x, NY, NZ) is pulled back with the centre, the weights staying those of the
+ * unclamped position. */
+static void cic_axis_s(double scale, int lim, taps *t) {
+  int i = (int)scale;
+  double d = scale - (double)i;
+  int nb = i + 1;
+  if (nb == lim) {
+    nb = lim - 1;
+    i = lim - 2;
+  }
+  t->idx[0] = i;  t->wt[0] = 1.0 - d; t->on[0] = 1;
+  t->idx[1] = nb; t->wt[1] = d;       t->on[1] = 1;
+  t->on[2] = 0;
+}
+
+static void tsc_axis_s(double scale, int is_x, int n, int lim, taps *t) {
+  int i = (int)(scale + 0.5);
+  double d = scale - (double)i;
+  double wc = 0.75 - d * d;
+  double wl = 0.5 * (0.5 - d) * (0.5 - d);
+  double wh = 0.5 * (0.5 + d) * (0.5 + d);
+  int lo = i - 1, hi = i + 1;
+  if (hi == lim) {
+    hi = lim - 1;
+    i = lim - 2;
+    lo = lim - 3;
+  }
+  t->idx[0] = i;  t->wt[0] = wc; t->on[0] = is_x ? 1 : (i < n);
+  t->idx[1] = lo; t->wt[1] = wl; t->on[1] = (lo > 0);
+  t->idx[2] = hi; t->wt[2] = wh; t->on[2] = (hi < lim);
+}
+
+double orc_survey_add(const orc_params *p, double x, double y, double z, double w, double vr, double *density) {
+  const geom g = mk_geom(p);
+  const double xmin = g.xmin_l, xmax = g.xmax_l;
+  const double wvr = w * vr;
+  if (p->interp_order == 1) return orc_add_to_grid(p, x, y, z, w, vr, density); /* NN has no survey branch */
+  taps tx, ty, tz;
+  if (p->interp_order == 2) {
+    if ((x < xmin) || (x >= xmax)) return 0.0;
+    if ((y < p->ymin) || (y >= p->ymax)) return 0.0;
+    if ((z < p->zmin) || (z >= p->zmax)) return 0.0;
+    cic_axis_s((x - xmin) / g.dx, g.nxtra, &tx);
+    cic_axis_s((y - p->ymin) / g.dy, p->ny, &ty);
+    cic_axis_s((z - p->zmin) / g.dz, p->nz, &tz);
+    ty.on[1] = ty.idx[1] < p->ny;
+    tz.on[1] = tz.idx[1] < p->nz;
+    static const int yz[4][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}};
+    for (int q = 0; q < 4; q++) {
+      int a = yz[q][0], b = yz[q][1];
+      if (!ty.on[a] || !tz.on[b]) continue;
+      for (int c = 0; c < 2; c++)
+        put(p, &g, density, tx.idx[c], ty.idx[a], tz.idx[b], wvr * tx.wt[c] * ty.wt[a] * tz.wt[b]);
+    }
+    return w;
+  }
+  if ((x < xmin) || (x >= xmax + g.dx)) return 0.0; /* :617-619, rank 0 */
+  if ((y < p->ymin) || (y >= p->ymax)) return 0.0;
+  if ((z < p->zmin) || (z >= p->zmax)) return 0.0;
+  tsc_axis_s((x - xmin) / g.dx, 1, p->nx, g.nxtra, &tx);
+  tsc_axis_s((y - p->ymin) / g.dy, 0, p->ny, p->ny, &ty);
+  tsc_axis_s((z - p->zmin) / g.dz, 0, p->nz, p->nz, &tz);
+  static const int yz[9][2] = {{0, 0}, {1, 0}, {1, 1}, {1, 2}, {2, 0}, {2, 1}, {2, 2}, {0, 1}, {0, 2}};
+  for (int q = 0; q < 9; q++) {
+    int a = yz[q][0], b = yz[q][1];
+    if (!ty.on[a] || !tz.on[b]) continue;
+    for (int c = 0; c < 3; c++) {
+      if (!tx.on[c]) continue;
+      put(p, &g, density, tx.idx[c], ty.idx[a], tz.idx[b], wvr * tx.wt[c] * ty.wt[a] * tz.wt[b]);
+    }
+  }
+  return w;
+}
+
+/* assign_survey_data for the density (src/read_data.c:471-494, Momentum 0): each object, and its
+ * copy shifted by half a cell into the interlaced grid, with weight prefactor * w. Returns
+ * sum(add_to_grid / w) (the reference's NGRID of the call). */
+double orc_survey_paint(const orc_params *p, int64_t n, const double *x, const double *y, const double *z,
+                        const double *w, double prefactor, double *ddg, double *ddg_interlace) {
+  const geom g = mk_geom(p);
+  double ngrid = 0.0;
+  for (int64_t i = 0; i < n; i++) {
+    ngrid += orc_survey_add(p, x[i], y[i], z[i], prefactor * w[i], 1.0, ddg) / w[i];
+    if (p->do_interlacing)
+      orc_survey_add(p, x[i] + g.dx / 2.0, y[i] + g.dy / 2.0, z[i] + g.dz / 2.0, prefactor * w[i], 1.0,
+                     ddg_interlace);
+  }
+  return ngrid;
+}
+
+/* The unit-vector products of compute_survey_power (src/main.c:472-775) for each multipole: index
+ * triples in the reference's loop order, and the power of r^ they multiply the grid by. */
+static int survey_terms(int l, int t[15][3]) {
+  int n = 0;
+  if (l == 0) { t[0][0] = t[0][1] = t[0][2] = 0; return 1; }
+  if (l == 1) { for (int i = 0; i < 3; i++) { t[n][0] = i; t[n][1] = t[n][2] = 0; n++; } return n; }
+  if (l == 2) {
+    for (int i = 0; i < 3; i++) for (int j = i; j < 3; j++) { t[n][0] = i; t[n][1] = j; t[n][2] = 0; n++; }
+    return n;
+  }
+  if (l == 3) { /* :648-655 */
+    for (int i = 0; i < 3; i++) {
+      int jl = i, jh = i + 1;
+      if (i == 0) jh = i + 2;
+      for (int j = jl; j < jh; j++) {
+        int kl = 0, kh = 3;
+        if (j != i) kl = 2;
+        for (int k = kl; k < kh; k++) { t[n][0] = i; t[n][1] = j; t[n][2] = k; n++; }
+      }
+    }
+    return n;
+  }
+  for (int i = 0; i < 3; i++) /* l == 4, :709-727 */
+    for (int j = 0; j < 3; j++) {
+      int kl = 0, kh = 3;
+      if (j != i) {
+        if (i == 1) kl = 2;
+        else if (i == 2) {
+          if (j == 1) continue;
+          kl = 1;
+          kh = 2;
+        } else kl = j;
+      }
+      for (int k = kl; k < kh; k++) { t[n][0] = i; t[n][1] = j; t[n][2] = k; n++; }
+    }
+  return n;
+}
+
+/* The weighted grid of one term (src/main.c:506-511, 551-559, 604-612, 660-668, 731-742): the first NX
+ * slices of src times the r^ products of the cell corner position relative to the origin. */
+static void survey_weight(const orc_params *p, const orc_survey *sp, int l, const int *ijk, const double *src,
+                          double *dst) {
+  const geom g = mk_geom(p);
+  for (int ix = 0; ix < p->nx; ix++)
+    for (int iy = 0; iy < p->ny; iy++)
+      for (int iz = 0; iz < p->nz; iz++) {
+        long ind = iz + 2 * (p->nz / 2 + 1) * (iy + p->ny * ix);
+        double vec[3] = {ix * g.dx + p->xmin - sp->x_origin, iy * g.dy + p->ymin - sp->y_origin,
+                         iz * g.dz + p->zmin - sp->z_origin};
+        double r2 = vec[0] * vec[0] + vec[1] * vec[1] + vec[2] * vec[2];
+        if (r2 == 0.0) r2 = 1.0;
+        double v = src[ind];
+        if (l == 1) v = src[ind] * vec[ijk[0]] / sqrt(r2);
+        else if (l == 2) v = src[ind] * vec[ijk[0]] * vec[ijk[1]] / r2;
+        else if (l == 3) v = src[ind] * vec[ijk[0]] * vec[ijk[1]] * vec[ijk[2]] / (r2 * sqrt(r2));
+        else if (l == 4) v = src[ind] * vec[ijk[0]] * vec[ijk[0]] * vec[ijk[1]] * vec[ijk[2]] / (r2 * r2);
+        dst[ind] = v;
+      }
+}
+
+/* assign_survey_power for the density (src/main.c:781-967, Momentum 0) over the transformed term grid
+ * dk (and its interlaced copy); multipole 0 stores the combined field in F0. */
+static void survey_assign(const orc_params *p, int l, const int *ijk, const double *d2, const double *d2i, double *F0,
+                          double *pk[5], int *nmodes) {
+  const geom g = mk_geom(p);
+  const int NK = p->nk;
+  const double ny_x = M_PI / g.dx, ny_y = M_PI / g.dy, ny_z = M_PI / g.dz;
+  double min_nyquist = ny_x;
+  if (ny_y < min_nyquist) min_nyquist = ny_y;
+  if (ny_z < min_nyquist) min_nyquist = ny_z;
+  const unsigned long long NX = p->nx, NY = p->ny, NZ = p->nz;
+  const double sx = 1.0 / ((float)NX * g.dx), sy = 1.0 / ((float)NY * g.dy), sz = 1.0 / ((float)NZ * g.dz);
+  const int ii = ijk[0], jj = ijk[1], kk = ijk[2];
+  for (int i = 0; i < p->nx; i++)
+    for (int j = 0; j < p->ny; j++)
+      for (int k = 0; (unsigned long long)k <= NZ / 2; k++) {
+        double fx = ((unsigned long long)i <= NX / 2) ? (float)i * sx : ((float)i - (float)NX) * sx;
+        double fy = ((unsigned long long)j <= NY / 2) ? (float)j * sy : ((float)j - (float)NY) * sy;
+        double fz = (float)k * sz;
+        double fktot = 2.0 * M_PI * sqrt(fx * fx + fy * fy + fz * fz);
+        int kbin = orc_kbin(p, fktot);
+        if (!((kbin >= 0) && (kbin < NK) && (fktot <= min_nyquist))) continue;
+        double sinc_x = 1.0, sinc_y = 1.0, sinc_z = 1.0;
+        double ax = M_PI * fx * g.dx, ay = M_PI * fy * g.dy, az = M_PI * fz * g.dz;
+        if (fx != 0.0) sinc_x = sin(ax) / ax;
+        if (fy != 0.0) sinc_y = sin(ay) / ay;
+        if (fz != 0.0) sinc_z = sin(az) / az;
+        double grid_cor = pow(1.0 / (sinc_x * sinc_y * sinc_z), 2 * p->interp_order);
+        double kvec[3] = {2. * M_PI * fx, 2. * M_PI * fy, 2. * M_PI * fz};
+        long long ind = (2 * k) + 2 * (NZ / 2 + 1) * (j + NY * i);
+        double dkr = d2[ind], dki = d2[ind + 1];
+        if (p->do_interlacing) {
+          grid_cor *= 0.25;
+          double kh = ax + ay + az, sink = sin(kh), cosk = cos(kh);
+          double a = d2i[ind], b = d2i[ind + 1];
+          dkr += a * cosk - b * sink;
+          dki += a * sink + b * cosk;
+        }
+        double power;
+        if (l == 0) {
+          F0[ind] = dkr;
+          F0[ind + 1] = dki;
+          power = (dkr * dkr + dki * dki) * grid_cor;
+        } else if (l % 2) {
+          power = (dkr * F0[ind + 1] - dki * F0[ind]) * grid_cor;
+        } else {
+          power = (dkr * F0[ind] + dki * F0[ind + 1]) * grid_cor;
+        }
+        int NM = 2;
+        if (k == 0) {
+          if (j == 0) {
+            if ((i != 0) && ((unsigned long long)i != NX / 2)) NM = 1;
+          } else {
+            if ((unsigned long long)i != NX / 2) NM = 1;
+          }
+        }
+        power *= NM;
+        if (l == 0) {
+          pk[0][kbin] += power;
+          pk[2][kbin] -= 0.5 * power;
+          pk[4][kbin] += 0.375 * power;
+          nmodes[kbin] += NM;
+        } else if (l == 1) {
+          if (fktot > 0.0) {
+            power *= kvec[ii] / fktot;
+            pk[1][kbin] += power;
+            pk[3][kbin] -= 1.5 * power;
+          }
+        } else if (l == 2) {
+          if (fktot > 0.0) {
+            double kprefac = ii != jj ? 2.0 : 1.0;
+            power *= kprefac * kvec[ii] * kvec[jj] / (fktot * fktot);
+            pk[2][kbin] += 1.5 * power;
+            pk[4][kbin] -= 3.75 * power;
+          }
+        } else if (l == 3) {
+          if (fktot > 0.0) {
+            double kprefac = 1.0;
+            if (ii != kk) kprefac = (ii != jj) ? 6.0 : 3.0;
+            pk[3][kbin] += 2.5 * kprefac * kvec[ii] * kvec[jj] * kvec[kk] / (fktot * fktot * fktot) * power;
+          }
+        } else {
+          if (fktot > 0) {
+            double kprefac = 1.0;
+            if (ii == jj) {
+              if (ii != kk) kprefac = 4.0;
+            } else {
+              kprefac = (jj == kk) ? 6.0 : 12.0;
+            }
+            pk[4][kbin] += 4.375 * kprefac * kvec[ii] * kvec[ii] * kvec[jj] * kvec[kk] /
+                           (fktot * fktot * fktot * fktot) * power;
+          }
+        }
+      }
+}
+
+void orc_survey_power(const orc_params *p, const orc_survey *sp, const double *ddg, const double *ddg_interlace,
+                      double *pk0, double *pk1, double *pk2, double *pk3, double *pk4, int *nmodes) {
+  const int NK = p->nk;
+  double *pk[5] = {pk0, pk1, pk2, pk3, pk4};
+  double dummy[NK > 0 ? NK : 1];
+  for (int l = 0; l < 5; l++) {
+    if (!pk[l]) pk[l] = dummy;
+    memset(pk[l], 0, sizeof(double) * NK);
+  }
+  memset(nmodes, 0, sizeof(int) * NK);
+  const int64_t nd = orc_grid_doubles(p);
+  double *d2 = (double *)calloc((size_t)nd, sizeof(double));
+  double *d2i = p->do_interlacing ? (double *)calloc((size_t)nd, sizeof(double)) : NULL;
+  double *F0 = (double *)calloc((size_t)nd, sizeof(double));
+  const int step = p->odd_multipoles ? 1 : 2; /* src/main.c:490-492 */
+  for (int l = 0; l <= 4; l += step) {
+    int t[15][3];
+    const int nt = survey_terms(l, t);
+    for (int q = 0; q < nt; q++) {
+      survey_weight(p, sp, l, t[q], ddg, d2);
+      orc_fft_r2c_3d_inplace(p->nx, p->ny, p->nz, d2);
+      if (d2i) {
+        survey_weight(p, sp, l, t[q], ddg_interlace, d2i);
+        orc_fft_r2c_3d_inplace(p->nx, p->ny, p->nz, d2i);
+      }
+      survey_assign(p, l, t[q], d2, d2i, F0, pk, nmodes);
+    }
+  }
+  free(d2);
+  free(d2i);
+  free(F0);
+}
+
+/* ---- the redshift-distance table of create_grids (src/main.c:1233-1248) */
+static double orc_hubble_inv(double z, void *par) {
+  const double om = *(const double *)par;
+  return 1.0 / sqrt(om * (1.0 + z) * (1.0 + z) * (1.0 + z) + (1.0 - om)); /* src/read_data.c:376-379 */
+}
+
+double orc_survey_redshift(double omega_m, double r) {
+  static double cached_om = -1.0;
+  static gsl_spline *red_spline = NULL;
+  if (!red_spline || cached_om != omega_m) {
+    const int nbins = 10000;
+    const double redmin = 0.0, redmax = 10.0, redbinwidth = (redmax - redmin) / (double)(nbins - 1);
+    double *zt = (double *)malloc(nbins * sizeof(double)), *rt = (double *)malloc(nbins * sizeof(double));
+    double om = omega_m;
+    gsl_function F;
+    F.function = &orc_hubble_inv;
+    F.params = &om;
+    zt[0] = 0.0;
+    rt[0] = 0.0;
+    for (int i = 1; i < nbins; i++) { /* comoving_distance, src/read_data.c:365-373 */
+      double result, error;
+      zt[i] = i * redbinwidth + redmin;
+      gsl_integration_qags(&F, 0.0, zt[i], 0, 1e-7, 1000, NULL, &result, &error);
+      rt[i] = 299792.458 * result / 100.0;
+    }
+    if (red_spline) gsl_spline_free(red_spline);
+    red_spline = gsl_spline_alloc(gsl_interp_cspline, nbins);
+    gsl_spline_init(red_spline, rt, zt, nbins);
+    free(zt);
+    free(rt);
+    cached_om = omega_m;
+  }
+  return gsl_spline_eval(red_spline, r, NULL);
 }

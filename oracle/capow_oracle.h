@@ -77,6 +77,28 @@ int orc_normalise(const orc_params *p, double shot, double norm, double *pk0, do
 /* the k-bin of one |k| value, src/main.c:369-373 (exposed for tests) */
 int orc_kbin(const orc_params *p, double fktot);
 
+/* ---- survey mode (Periodic 0, Survey 1), density (Momentum 0) */
+typedef struct {
+  double x_origin, y_origin, z_origin; /* observer position (X_Origin, ...) */
+} orc_survey;
+
+/* add_to_grid with the Survey branches (src/read_data.c:514-745) */
+double orc_survey_add(const orc_params *p, double x, double y, double z, double w, double vr, double *density);
+
+/* assign_survey_data (src/read_data.c:471-494): every object with weight prefactor * w, and into the
+ * interlaced grid half a cell up; returns sum(add_to_grid / w) */
+double orc_survey_paint(const orc_params *p, int64_t n, const double *x, const double *y, const double *z,
+                        const double *w, double prefactor, double *ddg, double *ddg_interlace);
+
+/* compute_survey_power + assign_survey_power (src/main.c:472-967, Momentum 0): raw bin sums of the
+ * Yamamoto multipoles from the painted grids (data minus alpha randoms); the oracle FFT in place of FFTW */
+void orc_survey_power(const orc_params *p, const orc_survey *sp, const double *ddg, const double *ddg_interlace,
+                      double *pk0, double *pk1, double *pk2, double *pk3, double *pk4, int *nmodes);
+
+/* the redshift of comoving distance r from the table create_grids builds (src/main.c:1233-1248,
+ * comoving_distance src/read_data.c:365-380), through the GSL stand-ins (orc_gsl.c) */
+double orc_survey_redshift(double omega_m, double r);
+
 #ifdef __cplusplus
 }
 #endif

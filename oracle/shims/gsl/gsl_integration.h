@@ -1,4 +1,4 @@
-/* Stand-in for the GSL integration API (test infrastructure only); inert, see gsl_spline.h. */
+/* Stand-in for the GSL integration API (test infrastructure only): adaptive Gauss-Kronrod (shim.c). */
 #ifndef CAPOW_SHIM_GSL_INTEGRATION_H
 #define CAPOW_SHIM_GSL_INTEGRATION_H
 #include <stddef.h>

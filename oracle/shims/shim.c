@@ -157,37 +157,4 @@ void fftw_execute(const fftw_plan p) { orc_fft_r2c_3d_inplace(p->n0, p->n1, p->n
 
 void fftw_destroy_plan(fftw_plan p) { free(p); }
 
-/* ------------------------------------------------------------------ GSL */
-static const gsl_interp_type g_cspline = {0};
-const gsl_interp_type *gsl_interp_cspline = &g_cspline;
-gsl_interp_accel *gsl_interp_accel_alloc(void) { return (gsl_interp_accel *)calloc(1, sizeof(gsl_interp_accel)); }
-void gsl_interp_accel_free(gsl_interp_accel *a) { free(a); }
-gsl_spline *gsl_spline_alloc(const gsl_interp_type *t, size_t n) {
-  (void)t;
-  gsl_spline *s = (gsl_spline *)calloc(1, sizeof(gsl_spline));
-  s->n = n;
-  return s;
-}
-int gsl_spline_init(gsl_spline *s, const double *x, const double *y, size_t n) {
-  (void)s; (void)x; (void)y; (void)n;
-  return 0;
-}
-double gsl_spline_eval(const gsl_spline *s, double x, gsl_interp_accel *a) {
-  (void)s; (void)x; (void)a;
-  fprintf(stderr, "capow_ref shim: gsl_spline_eval is not available (survey path)\n");
-  exit(3);
-}
-void gsl_spline_free(gsl_spline *s) { free(s); }
-gsl_integration_workspace *gsl_integration_workspace_alloc(size_t n) {
-  gsl_integration_workspace *w = (gsl_integration_workspace *)calloc(1, sizeof *w);
-  w->limit = n;
-  return w;
-}
-void gsl_integration_workspace_free(gsl_integration_workspace *w) { free(w); }
-int gsl_integration_qags(const gsl_function *f, double a, double b, double epsabs, double epsrel, size_t limit,
-                         gsl_integration_workspace *w, double *result, double *abserr) {
-  (void)f; (void)a; (void)b; (void)epsabs; (void)epsrel; (void)limit; (void)w;
-  *result = 0.0;
-  *abserr = 0.0;
-  return 0;
-}
+/* ------------------------------------------------------------------ GSL: oracle/orc_gsl.c */

@@ -151,6 +151,67 @@ def main():
     print("wrote", len(CASES), "cases")
 
 
+# survey-mode cases (Periodic 0, Survey 1, Momentum 0, Cartesian input, number density from its column,
+# FKP weights): name, params, data objects, random objects, seed
+SURVEY_CASES = [
+    ("sv_tsc_il_odd", dict(NX=32, NY=32, NZ=32, XMIN=100.0, XMAX=1100.0, YMIN=-500.0, YMAX=500.0, ZMIN=-500.0,
+                           ZMAX=500.0, InterpOrder=3, DoInterlacing=1, NK=12, Maxk=0.09, Odd_Multipoles=1,
+                           REDMININ=0.0, REDMAXIN=5.0, FKP_Pk=5000.0), 2000, 20000, 11),
+    ("sv_cic_cut", dict(NX=24, NY=20, NZ=16, XMIN=-800.0, XMAX=-200.0, YMIN=300.0, YMAX=800.0, ZMIN=-250.0,
+                        ZMAX=250.0, InterpOrder=2, DoInterlacing=0, NK=10, Maxk=0.12, Odd_Multipoles=0,
+                        REDMININ=0.15, REDMAXIN=0.28, FKP_Pk=10000.0, X_Origin=10.0, Y_Origin=-20.0, Z_Origin=5.0),
+     1500, 15000, 12),
+    ("sv_nn_il", dict(NX=16, NY=16, NZ=16, XMIN=0.0, XMAX=600.0, YMIN=0.0, YMAX=600.0, ZMIN=-100.0, ZMAX=500.0,
+                      InterpOrder=1, DoInterlacing=1, NK=8, Maxk=0.08, Odd_Multipoles=1, REDMININ=0.0, REDMAXIN=5.0,
+                      FKP_Pk=3000.0, X_Origin=300.0, Y_Origin=300.0, Z_Origin=-200.0), 1000, 10000, 13),
+]
+
+
+def survey_catalogue(p, n, ncol, rng):
+    """Objects uniform inside the grid less the reference's interpolation margin (src/read_data.c:193-204),
+    weights in [0.5, 1.5], a smooth number density in the 5th column, zeros in the others."""
+    d = np.array([(p.XMAX - p.XMIN) / p.NX, (p.YMAX - p.YMIN) / p.NY, (p.ZMAX - p.ZMIN) / p.NZ])
+    lo = np.array([p.XMIN, p.YMIN, p.ZMIN]) + (p.InterpOrder - 1) * d
+    hi = np.array([p.XMAX, p.YMAX, p.ZMAX]) - (p.InterpOrder - 1) * d - (0.5 * d if p.DoInterlacing else 0.0)
+    pos = rng.uniform(lo + 1e-3 * d, hi - 1e-3 * d, size=(n, 3))
+    w = rng.uniform(0.5, 1.5, n)
+    nb = 1e-4 * (1.0 + 0.5 * np.sin(np.linalg.norm(pos, axis=1) / 200.0))
+    return np.concatenate([pos, w[:, None], nb[:, None], np.zeros((n, ncol - 5))], axis=1)
+
+
+def main_survey():
+    import subprocess
+
+    orc.build()
+    if not orc.ref_available():
+        raise SystemExit("oracle/_ref/capow_ref is not built (reference sources not mounted)")
+    manifest = {}
+    with tempfile.TemporaryDirectory() as td:
+        for name, kw, nd, nr, seed in SURVEY_CASES:
+            p = orc.Params(**kw, Periodic=0, Coord_Type=0, NBAR_Column=5, FKP_Column=-1,
+                           NOBJ_Max=max(nd, nr) + 10)
+            rng = np.random.default_rng(seed)
+            data, rand = survey_catalogue(p, nd, 12, rng), survey_catalogue(p, nr, 8, rng)
+            pf, df, rf, of, dump = (os.path.join(td, f"{name}.{e}") for e in ("dat", "data", "rand", "out", "dump"))
+            p.write_file(pf)
+            np.savetxt(df, data, fmt="%.17g")
+            np.savetxt(rf, rand, fmt="%.17g")
+            r = subprocess.run([orc.REF_BIN, pf, df, rf, of], capture_output=True, text=True,
+                               env=dict(os.environ, CAPOW_REF_DUMP=dump))
+            assert r.returncode == 0, r.stdout
+            dd = orc.parse_dump(dump)
+            np.savez_compressed(os.path.join(HERE, f"{name}.npz"), data=data, rand=rand, Nmodes=dd["Nmodes"],
+                                **{k: dd[k] for k in ("Pk0", "Pk1", "Pk2", "Pk3", "Pk4")})
+            with open(os.path.join(HERE, f"{name}.out"), "w") as f:
+                f.write(open(of).read())
+            with open(os.path.join(HERE, f"{name}.stdout"), "w") as f:
+                f.write(r.stdout.replace(df, "{DATAFILE}").replace(rf, "{RANDFILE}").replace(of, "{OUTFILE}"))
+            manifest[name] = dict(params=dataclass_dict(p), ndata=nd, nrand=nr, seed=seed)
+    with open(os.path.join(HERE, "survey_manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
+    print("wrote", len(SURVEY_CASES), "survey cases")
+
+
 def dataclass_dict(p):
     import dataclasses
 
@@ -158,4 +219,7 @@ def dataclass_dict(p):
 
 
 if __name__ == "__main__":
-    main()
+    if "--survey" in sys.argv:
+        main_survey()
+    else:
+        main()
