@@ -92,13 +92,41 @@ class _Mock(ctypes.Structure):
 BATCH_GRAPH, BATCH_AUTOTUNE = 1, 2
 
 
+class _SurveyParams(ctypes.Structure):
+    _fields_ = [("Periodic", ctypes.c_int), ("Survey", ctypes.c_int), ("Coord_Type", ctypes.c_int),
+                ("X_Origin", ctypes.c_double), ("Y_Origin", ctypes.c_double), ("Z_Origin", ctypes.c_double),
+                ("REDMININ", ctypes.c_double), ("REDMAXIN", ctypes.c_double), ("NOBJ_Max", ctypes.c_longlong),
+                ("NBAR_Column", ctypes.c_int), ("SkyArea", ctypes.c_double), ("FKP_Column", ctypes.c_int),
+                ("FKP_Pk", ctypes.c_double), ("FKP_Pk_mom", ctypes.c_double), ("FKP_Pk_cross", ctypes.c_double)]
+
+
+class _SurveyCatalogue(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_size_t), ("dtype", ctypes.c_int), ("on_device", ctypes.c_int),
+                ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("z", ctypes.c_void_p),
+                ("w", ctypes.c_void_p), ("nbar", ctypes.c_void_p)]
+
+
+class _SurveyStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in ("ngrid_data", "ngrid_rand", "data_nbw", "data_nbwsq", "data_nbsqwsq",
+                                               "rand_nbw", "rand_nbwsq", "rand_nbsqwsq")]
+
+
+class _SurveyObjects(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_size_t), ("nread", ctypes.c_ulonglong)] + [
+        (k, ctypes.POINTER(ctypes.c_float)) for k in ("x", "y", "z", "w", "nbar", "redshift")] + [
+        ("lo", ctypes.c_double * 3), ("hi", ctypes.c_double * 3), ("redmin", ctypes.c_double),
+        ("redmax", ctypes.c_double), ("log", ctypes.c_void_p)]
+
+
 # every entry point include/capow.h declares
 EXPORTS = [
     "capow_create", "capow_paint", "capow_get_stats", "capow_power", "capow_normalise", "capow_num_spectra",
     "capow_copy_grid", "capow_stage_ms", "capow_kernel_launches", "capow_destroy", "capow_read_params",
     "capow_read_catalogue", "capow_free", "capow_write_output", "capow_bin_centre", "capow_strerror",
     "capow_last_error", "capow_paint_noalloc", "capow_backward", "capow_batch", "capow_tile_kernel_ms",
-    "capow_batch_release",
+    "capow_batch_release", "capow_survey_create", "capow_survey_power", "capow_survey_copy_grid",
+    "capow_survey_stage_ms", "capow_survey_kernel_launches", "capow_survey_last_error", "capow_survey_destroy",
+    "capow_read_survey_params", "capow_read_survey", "capow_survey_objects_free",
 ]
 
 _lib = None
@@ -147,6 +175,24 @@ def lib() -> ctypes.CDLL:
     L.capow_strerror.restype = ctypes.c_char_p
     L.capow_last_error.argtypes = [vp]
     L.capow_last_error.restype = ctypes.c_char_p
+    SP = ctypes.POINTER(_SurveyParams)
+    L.capow_survey_create.argtypes = [P, SP, O, ctypes.POINTER(vp)]
+    L.capow_survey_power.argtypes = [vp, ctypes.POINTER(_SurveyCatalogue), ctypes.POINTER(_SurveyCatalogue),
+                                     ctypes.POINTER(_Spectrum), ctypes.POINTER(_SurveyStats)]
+    L.capow_survey_copy_grid.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_double)]
+    L.capow_survey_stage_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
+                                        ctypes.POINTER(ctypes.c_int)]
+    L.capow_survey_kernel_launches.argtypes = [vp]
+    L.capow_survey_kernel_launches.restype = ctypes.c_int64
+    L.capow_survey_last_error.argtypes = [vp]
+    L.capow_survey_last_error.restype = ctypes.c_char_p
+    L.capow_survey_destroy.argtypes = [vp]
+    L.capow_survey_destroy.restype = None
+    L.capow_read_survey_params.argtypes = [ctypes.c_char_p, P, SP, ctypes.c_char_p, ctypes.c_size_t]
+    L.capow_read_survey.argtypes = [ctypes.c_char_p, P, SP, ip, ctypes.POINTER(_SurveyObjects), ctypes.c_char_p,
+                                    ctypes.c_size_t]
+    L.capow_survey_objects_free.argtypes = [ctypes.POINTER(_SurveyObjects)]
+    L.capow_survey_objects_free.restype = None
     _lib = L
     return L
 
@@ -486,3 +532,183 @@ def run_batch(mocks, precision: str = "fp32", spectra=None, graph: bool = False,
                         "kind": {0: "ref", SPEC_DD: "dd", SPEC_DP: "dp", SPEC_PP: "pp"}[specs[q].kind]})
         out.append((arr[i].status, res))
     return out
+
+
+# ---------------------------------------------------------------------------------------- survey mode
+@dataclasses.dataclass
+class SurveyParams:
+    """capow_survey_params: the survey tags of run_parameters.dat (src/read_params.c:145-222)."""
+    Periodic: int = 0
+    Survey: int = 1
+    Coord_Type: int = 0
+    X_Origin: float = 0.0
+    Y_Origin: float = 0.0
+    Z_Origin: float = 0.0
+    REDMININ: float = 0.0
+    REDMAXIN: float = 10.0
+    NOBJ_Max: int = 1 << 40
+    NBAR_Column: int = 5
+    SkyArea: float = 1.0
+    FKP_Column: int = -1
+    FKP_Pk: float = 5000.0
+    FKP_Pk_mom: float = 0.0
+    FKP_Pk_cross: float = 0.0
+
+    def to_c(self) -> _SurveyParams:
+        return _SurveyParams(**{f.name: getattr(self, f.name) for f in dataclasses.fields(self)})
+
+    @classmethod
+    def from_c(cls, c: _SurveyParams) -> "SurveyParams":
+        return cls(**{f.name: getattr(c, f.name) for f in dataclasses.fields(cls)})
+
+
+def read_survey_params(path: str):
+    """capow_read_survey_params: (Params, SurveyParams) of a periodic or survey parameter file."""
+    c, s = _Params(), _SurveyParams()
+    msg = ctypes.create_string_buffer(8192)
+    rc = lib().capow_read_survey_params(path.encode(), ctypes.byref(c), ctypes.byref(s), msg, len(msg))
+    if rc != OK:
+        raise CapowError(rc, msg.value.decode())
+    return Params.from_c(c), SurveyParams.from_c(s)
+
+
+def read_survey(path: str, params: Params, survey: SurveyParams, randoms: bool) -> dict:
+    """capow_read_survey: the objects read_survey_serial_ascii keeps (float32 arrays) and its counters."""
+    L = lib()
+    o = _SurveyObjects()
+    msg = ctypes.create_string_buffer(8192)
+    pc, sc = params.to_c(), survey.to_c()
+    rc = L.capow_read_survey(path.encode(), ctypes.byref(pc), ctypes.byref(sc), int(randoms), ctypes.byref(o), msg,
+                             len(msg))
+    log = ctypes.string_at(o.log).decode() if o.log else ""
+    if rc != OK:
+        L.capow_survey_objects_free(ctypes.byref(o))
+        err = CapowError(rc, msg.value.decode())
+        err.log = log
+        raise err
+    out = {k: (np.ctypeslib.as_array(getattr(o, k), shape=(o.n,)).copy() if o.n else np.zeros(0, np.float32))
+           for k in ("x", "y", "z", "w", "nbar", "redshift")}
+    out.update(n=o.n, nread=o.nread, lo=list(o.lo), hi=list(o.hi), redmin=o.redmin, redmax=o.redmax, log=log)
+    L.capow_survey_objects_free(ctypes.byref(o))
+    return out
+
+
+def _survey_cat(cat):
+    """A capow_survey_catalogue for a dict (or tuple) of x, y, z, w, nbar arrays (numpy: host; CUDA tensors:
+    device), plus the arrays to keep alive."""
+    arrs = [cat[k] for k in ("x", "y", "z", "w", "nbar")] if isinstance(cat, dict) else list(cat)
+    ptrs = [_ptr_of(a) for a in arrs]
+    codes = {p[1] for p in ptrs}
+    devs = {p[2] for p in ptrs}
+    if len(codes) != 1 or len(devs) != 1:
+        raise ValueError("survey catalogue arrays must share one dtype and one location")
+    n = len(ptrs[0][3])
+    if any(len(p[3]) != n for p in ptrs):
+        raise ValueError("survey catalogue arrays differ in length")
+    return _SurveyCatalogue(n, codes.pop(), devs.pop(), *[p[0] for p in ptrs]), [p[3] for p in ptrs]
+
+
+class SurveySpectrum:
+    """One capow survey context (capow_survey_create): the survey estimator's P_l(k) from data and randoms.
+
+    precision: "fp64" (plain double path) or "fp32" (FP32 grids and FFTs, FP64 sums and bins)."""
+
+    def __init__(self, params: Params, survey: SurveyParams, precision: str = "fp64", device: int = 0, stream=None):
+        self.params, self.survey = params, survey
+        self._pc, self._sc = params.to_c(), survey.to_c()
+        opt = _Options(PRECISIONS[precision], 0, device, ctypes.c_void_p(stream or 0), FFT_AUTO)
+        self._ctx = ctypes.c_void_p()
+        rc = lib().capow_survey_create(ctypes.byref(self._pc), ctypes.byref(self._sc), ctypes.byref(opt),
+                                       ctypes.byref(self._ctx))
+        if rc != OK:
+            err = self._err()
+            self.close()
+            raise CapowError(rc, f"capow_survey_create: {lib().capow_strerror(rc).decode()}: {err}")
+
+    def _err(self) -> str:
+        return lib().capow_survey_last_error(self._ctx).decode() if self._ctx else ""
+
+    def _check(self, rc: int, what: str):
+        if rc != OK:
+            raise CapowError(rc, f"{what}: {lib().capow_strerror(rc).decode()}: {self._err()}")
+
+    def power(self, data, rand) -> dict:
+        """Raw bin sums, Nmodes, shot, norm, alpha and the survey counters (capow_survey_power)."""
+        p = self.params
+        dc, keep_d = _survey_cat(data)
+        rc_, keep_r = _survey_cat(rand)
+        pk = [np.zeros(p.NK) for _ in range(5)]
+        nm = np.zeros(p.NK, np.int64)
+        n2d = p.NK * p.NMU if p.Output2D else 0
+        p2, n2 = np.zeros(max(n2d, 1)), np.zeros(max(n2d, 1), np.int64)
+        s = _Spectrum()
+        for l in range(5):
+            s.pk[l] = pk[l].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        s.nmodes = nm.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        if n2d:
+            s.pk2d = p2.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+            s.nmodes2d = n2.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        st = _SurveyStats()
+        self._check(lib().capow_survey_power(self._ctx, ctypes.byref(dc), ctypes.byref(rc_), ctypes.byref(s),
+                                             ctypes.byref(st)), "capow_survey_power")
+        del keep_d, keep_r
+        out = {"Pk0": pk[0], "Pk1": pk[1], "Pk2": pk[2], "Pk3": pk[3], "Pk4": pk[4], "Nmodes": nm,
+               "shot": s.shot, "norm": s.norm, "alpha": s.alpha, "kind": "ref",
+               "stats": {k: getattr(st, k) for k, _ in _SurveyStats._fields_}}
+        if n2d:
+            out["Pk_2D"], out["Nmodes_2D"] = p2[:n2d], n2[:n2d]
+        return out
+
+    def normalise(self, raw: dict) -> dict:
+        """capow_normalise (output_power arithmetic) on a copy of one raw spectrum."""
+        p = self.params
+        d = {k: (np.array(v, copy=True) if isinstance(v, np.ndarray) else v) for k, v in raw.items()}
+        s = _Spectrum()
+        for l in range(5):
+            s.pk[l] = d[f"Pk{l}"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        s.nmodes = d["Nmodes"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        if p.Output2D:
+            s.pk2d = d["Pk_2D"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+            s.nmodes2d = d["Nmodes_2D"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        s.shot, s.norm = d["shot"], d["norm"]
+        rc = lib().capow_normalise(ctypes.byref(self._pc), ctypes.byref(s))
+        if rc != OK:
+            raise CapowError(rc, "capow_normalise")
+        d["last_bin"] = s.last_bin
+        return d
+
+    def grid(self, which: int) -> np.ndarray:
+        """The painted grid (0) or its interlaced copy (1) of the last evaluation, padded reference layout."""
+        p = self.params
+        out = np.zeros(p.NX * p.NY * 2 * (p.NZ // 2 + 1))
+        self._check(lib().capow_survey_copy_grid(self._ctx, which,
+                                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+                    "capow_survey_copy_grid")
+        return out
+
+    def stage_ms(self):
+        """(paint ms, multipole ms, FFT sets) of the last evaluation."""
+        a, b, n = ctypes.c_float(), ctypes.c_float(), ctypes.c_int()
+        self._check(lib().capow_survey_stage_ms(self._ctx, ctypes.byref(a), ctypes.byref(b), ctypes.byref(n)),
+                    "capow_survey_stage_ms")
+        return a.value, b.value, n.value
+
+    def kernel_launches(self) -> int:
+        return int(lib().capow_survey_kernel_launches(self._ctx))
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            lib().capow_survey_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

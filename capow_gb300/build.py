@@ -22,8 +22,8 @@ BIN = os.path.join(HERE, "bin")
 LIB = os.path.join(BUILD, "libcapow_gpu.so")
 DRIVER = os.path.join(BIN, "capow")
 
-CU_SOURCES = ["capow_api.cu", "paint.cu", "bin.cu", "noalloc.cu", "adjoint.cu", "batch.cu"]
-C_SOURCES = ["params.c", "catalogue.c", "output.c"]
+CU_SOURCES = ["capow_api.cu", "paint.cu", "bin.cu", "noalloc.cu", "adjoint.cu", "batch.cu", "survey.cu"]
+C_SOURCES = ["params.c", "catalogue.c", "output.c", "survey_io.c"]
 DRIVER_SOURCES = ["main.c"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

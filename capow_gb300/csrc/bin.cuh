@@ -61,6 +61,25 @@ struct BinParams {
   int lg;
 };
 
+// bin in [-1, NK] of an exact s: E[b+1] <= s < E[b+2]
+__device__ __forceinline__ int exact_bin(const double *E, int nk, double s, int guess) {
+  int b = guess < -1 ? -1 : (guess > nk ? nk : guess);
+  while (b < nk && s >= E[b + 2]) b++;
+  while (b > -1 && s < E[b + 1]) b--;
+  return b;
+}
+
+__device__ __forceinline__ double exact_s(const BinTables &t, int i, int j, int k) {
+  return __dadd_rn(__dadd_rn(t.fx2d[i], t.fy2d[j]), t.fz2d[k]);
+}
+
+// Hermitian multiplicity NM, src/main.c:422-429
+__device__ __forceinline__ int herm_nm(int i, int j, int k, int xhalf) {
+  if (k != 0) return 2;
+  if (j == 0) return ((i != 0) && (i != xhalf)) ? 1 : 2;
+  return (i != xhalf) ? 1 : 2;
+}
+
 // Fill kscale, koff and lg of bp for a run's k binning.
 void bin_params_kguess(BinParams &bp, const capow_params &p);
 

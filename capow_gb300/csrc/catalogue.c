@@ -73,8 +73,8 @@ static int eisel_lemire(uint64_t w, int q, int neg, double *out) {
 }
 
 /* One decimal number at p (no leading space), ending before e. Sets *end to the first character
- * after it (p when there is none), with strtod's result. */
-static double parse_number(const char *p, const char *e, const char **end) {
+ * after it (p when there is none), with strtod's result. Shared with the survey reader, not exported. */
+__attribute__((visibility("hidden"))) double capow_parse_number(const char *p, const char *e, const char **end) {
   const char *s = p;
   int neg = 0;
   if (s < e && (*s == '+' || *s == '-')) neg = *s++ == '-';
@@ -146,7 +146,7 @@ static int parse_line(const char *p, const char *e, double out[6]) {
     while (p < e && is_hspace(*p)) p++;
     if (p >= e) break;
     const char *end;
-    double v = parse_number(p, e, &end);
+    double v = capow_parse_number(p, e, &end);
     if (end == p || end > e) break;
     out[k++] = v;
     p = end;

@@ -3,8 +3,8 @@
  *
  * The tag set and the message texts are kept identical on purpose: the same parameter file
  * must drive both the reference and this build, and scripts that parse the reference's
- * stdout keep working. Survey-only tags are parsed and ignored (the survey estimator is not
- * part of this library). */
+ * stdout keep working. capow_read_params serves the periodic path and refuses a survey run;
+ * capow_read_survey_params accepts both and also returns the survey tags. */
 #include <stddef.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -60,7 +60,7 @@ static void append(char *msg, size_t len, const char *s) {
   snprintf(msg + u, len - u, "%s", s);
 }
 
-int capow_read_params(const char *fname, capow_params *out, char *msg, size_t msglen) {
+static int read_all(const char *fname, capow_params *out, capow_survey_params *sv, char *msg, size_t msglen) {
   int ival[I_COUNT];
   double dval[D_COUNT];
   int used[64];
@@ -163,9 +163,27 @@ int capow_read_params(const char *fname, capow_params *out, char *msg, size_t ms
   if (dval[D_Maxk] < dval[D_Mink])
     FATAL("\nERROR: `Maxk' is less than `Mink'.\n        Please set `Maxk' > `Mink'.\n\n", 427);
 #undef FATAL
-  if (!ival[I_Periodic]) {
-    append(msg, msglen, "\nERROR: only the periodic-box estimator (Periodic 1) is provided by this build.\n\n");
+  if (!ival[I_Periodic] && !sv) {
+    append(msg, msglen, "\nERROR: a survey run (Periodic 0) needs capow_read_survey_params.\n\n");
     return CAPOW_ENOTSUP;
+  }
+  if (sv) {
+    memset(sv, 0, sizeof *sv);
+    sv->Periodic = ival[I_Periodic];
+    sv->Survey = ival[I_Survey];
+    sv->Coord_Type = ival[I_Coord_Type];
+    sv->X_Origin = dval[D_X_Origin];
+    sv->Y_Origin = dval[D_Y_Origin];
+    sv->Z_Origin = dval[D_Z_Origin];
+    sv->REDMININ = dval[D_REDMININ];
+    sv->REDMAXIN = dval[D_REDMAXIN];
+    sv->NOBJ_Max = ival[I_NOBJ_Max];
+    sv->NBAR_Column = ival[I_NBAR_Column];
+    sv->SkyArea = dval[D_SkyArea];
+    sv->FKP_Column = ival[I_FKP_Column];
+    sv->FKP_Pk = dval[D_FKP_Pk];
+    sv->FKP_Pk_mom = dval[D_FKP_Pk_mom];
+    sv->FKP_Pk_cross = dval[D_FKP_Pk_cross];
   }
   if (out) {
     memset(out, 0, sizeof *out);
@@ -190,4 +208,14 @@ int capow_read_params(const char *fname, capow_params *out, char *msg, size_t ms
     out->Odd_Multipoles = ival[I_Odd_Multipoles];
   }
   return CAPOW_OK;
+}
+
+int capow_read_params(const char *fname, capow_params *out, char *msg, size_t msglen) {
+  return read_all(fname, out, NULL, msg, msglen);
+}
+
+int capow_read_survey_params(const char *fname, capow_params *out, capow_survey_params *sv, char *msg,
+                             size_t msglen) {
+  if (!sv) return CAPOW_EINVAL;
+  return read_all(fname, out, sv, msg, msglen);
 }

@@ -1,0 +1,1011 @@
+// Survey-mode estimator (Periodic 0, Survey 1, density) on one GB300: the C ABI's capow_survey_*.
+//
+// Reference semantics (single rank; paths relative to the CAPOW source tree):
+//   src/read_data.c:450-466  compute_fkp: weight *= 1/(1 + nbar FKP_Pk), stored back in the float field
+//   src/main.c:149-204       sums over data and randoms, alpha, shot, norm
+//   src/read_data.c:471-494  assign_survey_data: data with prefactor 1, randoms with -alpha, each object
+//                            and its copy shifted by half a cell (interlacing)
+//   src/read_data.c:514-745  add_to_grid's Survey branches: no wrap; a neighbour that reaches the axis
+//                            limit pulls the stencil back by one cell (:577-590, :672-688); the halo
+//                            slices past NX are discarded (no neighbour rank, src/main.c:1162-1188)
+//   src/main.c:472-775       compute_survey_power: the density times products of the unit vector r^
+//                            from the observer to every cell corner, one FFT per product
+//   src/main.c:781-967       assign_survey_power: interlacing combine, deconvolution, the products'
+//                            k^ factors, crossed with F0 (the monopole field) and binned
+//
+// Multipoles through solid harmonics. For a unit k^, the reference builds
+//   F_l(k) = sum_r L_l(k^.r^) delta(r) e^{-ik.r}
+// from the Cartesian products r^_i r^_j ... (1, 3, 6, 10, 15 FFTs for l = 0..4). By the addition
+// theorem L_l(k^.u) = sum_m c_lm h_lm(k^) h_lm(u) with h_lm the 2l+1 real harmonic polynomials of
+// degree l (below), so F_l = sum_m c_lm h_lm(k^) FFT[h_lm(r^) delta] takes 1, 3, 5, 7, 9 FFTs. The two
+// forms agree on every cell with |r^| = 1. The cell whose corner is the observer (r2 == 0, where the
+// reference sets r2 = 1 and all its products vanish) enters the reference's P2 and P4 through the
+// constant terms of L_2 and L_4 only: L_l(0) delta_o e^{-ik.r_o}, added here in closed form. At k = 0
+// the reference skips every l > 0 product and keeps L_l(0) |F0|^2.
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <math.h>
+#include <stddef.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <new>
+#include <vector>
+
+#include "ctx.cuh"
+
+// ------------------------------------------------------------------------------------ device state
+struct SvStats {
+  double wsum[2], w2sum[2], w2nsum[2];  // [0] data, [1] randoms: sum w, w^2, w^2 nbar (src/main.c:151-163)
+  double ngrid[2];                      // sum of add_to_grid(...)/weight (src/read_data.c:488)
+  double dc[2];                         // FP64 sum of the deposits reaching the FFT input: main, interlaced
+  int nonfinite;                        // a non-finite coordinate, weight or number density
+  int pad;
+};
+
+template <typename T>
+struct SvIn {
+  const T *x, *y, *z, *w, *nbar;
+};
+
+// Real harmonic polynomials of degree l (m = 0 .. 2l) and the factors c_lm of
+// L_l(n.u) = sum_m c_lm h_lm(n) h_lm(u) for unit n and u.
+template <typename R>
+__device__ __forceinline__ R harm(int l, int m, R x, R y, R z) {
+  const R x2 = x * x, y2 = y * y, z2 = z * z;
+  switch (l) {
+    case 1:
+      return m == 0 ? x : (m == 1 ? y : z);
+    case 2:
+      switch (m) {
+        case 0: return x * y;
+        case 1: return y * z;
+        case 2: return x * z;
+        case 3: return x2 - y2;
+        default: return (R)2 * z2 - x2 - y2;
+      }
+    case 3:
+      switch (m) {
+        case 0: return x * (x2 - (R)3 * y2);
+        case 1: return y * ((R)3 * x2 - y2);
+        case 2: return z * (x2 - y2);
+        case 3: return x * y * z;
+        case 4: return x * ((R)4 * z2 - x2 - y2);
+        case 5: return y * ((R)4 * z2 - x2 - y2);
+        default: return z * ((R)2 * z2 - (R)3 * x2 - (R)3 * y2);
+      }
+    default: {
+      const R p = x2 + y2;
+      switch (m) {
+        case 0: return x * y * (x2 - y2);
+        case 1: return x2 * x2 - (R)6 * x2 * y2 + y2 * y2;
+        case 2: return y * z * ((R)3 * x2 - y2);
+        case 3: return x * z * (x2 - (R)3 * y2);
+        case 4: return x * y * ((R)6 * z2 - p);
+        case 5: return (x2 - y2) * ((R)6 * z2 - p);
+        case 6: return y * z * ((R)4 * z2 - (R)3 * p);
+        case 7: return x * z * ((R)4 * z2 - (R)3 * p);
+        default: return (R)8 * z2 * z2 - (R)24 * z2 * p + (R)3 * p * p;
+      }
+    }
+  }
+}
+
+static double harm_coef(int l, int m) {
+  static const double c1[3] = {1, 1, 1};
+  static const double c2[5] = {3, 3, 3, 0.75, 0.25};
+  static const double c3[7] = {0.625, 0.625, 3.75, 15, 0.375, 0.375, 0.25};
+  static const double c4[9] = {8.75, 35.0 / 64.0, 4.375, 4.375, 1.25, 0.3125, 0.625, 0.625, 1.0 / 64.0};
+  const double *c[5] = {nullptr, c1, c2, c3, c4};
+  return l == 0 ? 1.0 : c[l][m];
+}
+
+// -------------------------------------------------------------------------- paint (exact FP64 rules)
+// One axis of add_to_grid's Survey branch. CIC (src/read_data.c:554-590): ix = (int)scale, neighbour
+// ix + 1; TSC (:629-688): ix = (int)(scale + 0.5), neighbours ix -/+ 1. When the upper neighbour
+// equals lim (Local_nxtra along x, NY or NZ) the stencil moves down one cell, weights unchanged.
+// Write guards (:592-605, :690-742): CIC y/z neighbour < N; TSC centre y/z < N, low > 0, high < lim.
+__device__ __forceinline__ void sv_cic(double scale, bool is_x, int n, int lim, AxisTaps &t) {
+  int i = (int)scale;
+  const double d = DSUB(scale, (double)i);
+  int nb = i + 1;
+  if (nb == lim) {
+    nb = lim - 1;
+    i = lim - 2;
+  }
+  t.n = 2;
+  t.idx[0] = i;  t.w[0] = DSUB(1.0, d); t.on[0] = 1;
+  t.idx[1] = nb; t.w[1] = d;            t.on[1] = is_x ? 1 : (nb < n);
+  t.on[2] = 0;
+}
+
+__device__ __forceinline__ void sv_tsc(double scale, bool is_x, int n, int lim, AxisTaps &t) {
+  int i = (int)DADD(scale, 0.5);
+  const double d = DSUB(scale, (double)i);
+  const double wc = DSUB(0.75, DMUL(d, d));
+  const double a = DSUB(0.5, d), b = DADD(0.5, d);
+  const double wl = DMUL(DMUL(0.5, a), a);
+  const double wh = DMUL(DMUL(0.5, b), b);
+  int lo = i - 1, hi = i + 1;
+  if (hi == lim) {
+    hi = lim - 1;
+    i = lim - 2;
+    lo = lim - 3;
+  }
+  t.n = 3;
+  t.idx[0] = i;  t.w[0] = wc; t.on[0] = is_x ? 1 : (i < n);
+  t.idx[1] = lo; t.w[1] = wl; t.on[1] = (lo > 0);
+  t.idx[2] = hi; t.w[2] = wh; t.on[2] = (hi < lim);
+}
+
+// Acceptance and taps of one Survey add_to_grid call (rank 0 of one: x in [XMIN, XMAX) for NN and
+// CIC, [XMIN, XMAX + dx) for TSC, :519-527, :546-552, :617-619). NN has no Survey branch.
+__device__ __forceinline__ bool sv_axes(const Geom &g, double x, double y, double z, AxisTaps &ax, AxisTaps &ay,
+                                        AxisTaps &az) {
+  if (g.order == 1) return exact_axes(g, x, y, z, ax, ay, az);
+  const double xmin = g.xmin, xmax = g.xmax_l;
+  if (g.order == 2) {
+    if ((x < xmin) || (x >= xmax)) return false;
+  } else if ((x < xmin) || (x >= DADD(xmax, g.dx))) {
+    return false;
+  }
+  if ((y < g.ymin) || (y >= g.ymax)) return false;
+  if ((z < g.zmin) || (z >= g.zmax)) return false;
+  const double sx = DDIV(DSUB(x, xmin), g.dx), sy = DDIV(DSUB(y, g.ymin), g.dy), sz = DDIV(DSUB(z, g.zmin), g.dz);
+  if (g.order == 2) {
+    sv_cic(sx, true, g.nx, g.nxtra, ax);
+    sv_cic(sy, false, g.ny, g.ny, ay);
+    sv_cic(sz, false, g.nz, g.nz, az);
+  } else {
+    sv_tsc(sx, true, g.nx, g.nxtra, ax);
+    sv_tsc(sy, false, g.ny, g.ny, ay);
+    sv_tsc(sz, false, g.nz, g.nz, az);
+  }
+  return true;
+}
+
+// Linear index of a write (src/read_data.c:536 form) that reaches the FFT input, else -1: the halo
+// slices are discarded, the padding columns are not read by the transform, and an index the
+// reference would place before the grid (NY or NZ below 3 with a pulled-back TSC stencil) is dropped.
+__device__ __forceinline__ long long sv_index(const Geom &g, int ix, int iy, int iz) {
+  if (ix < 0 || iy < 0 || iz < 0 || iz >= g.nz) return -1;
+  const unsigned long long L =
+      (unsigned long long)iz + (unsigned long long)g.row * ((unsigned long long)iy + (unsigned long long)g.ny * (unsigned long long)ix);
+  return L < (unsigned long long)g.main_sz ? (long long)L : -1;
+}
+
+template <typename R>
+__device__ __forceinline__ double sv_deposit(const Geom &g, R *grid, double wv, const AxisTaps &ax,
+                                             const AxisTaps &ay, const AxisTaps &az) {
+  double s = 0.0;
+  for (int c = 0; c < az.n; c++) {
+    if (!az.on[c]) continue;
+    for (int b = 0; b < ay.n; b++) {
+      if (!ay.on[b]) continue;
+      for (int a = 0; a < ax.n; a++) {
+        if (!ax.on[a]) continue;
+        const long long L = sv_index(g, ax.idx[a], ay.idx[b], az.idx[c]);
+        if (L < 0) continue;
+        const double d = DMUL(DMUL(DMUL(wv, ax.w[a]), ay.w[b]), az.w[c]);
+        atomicAdd(grid + L, (R)d);
+        s += d;
+      }
+    }
+  }
+  return s;
+}
+
+__device__ __forceinline__ double sv_warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum NV per-thread doubles over the block and add them to global dst (one atomic per value and block).
+template <int NV>
+__device__ void sv_block_add(const double (&v)[NV], double *const (&dst)[NV]) {
+  __shared__ double red[32][NV];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  double t[NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++) t[k] = sv_warp_sum(v[k]);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; k++) red[wid][k] = t[k];
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+      double a = lane < nw ? red[lane][k] : 0.0;
+      a = sv_warp_sum(a);
+      if (lane == 0 && a != 0.0) atomicAdd(dst[k], a);
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ float sv_rsqrt(float a) { return rsqrtf(a); }
+__device__ __forceinline__ double sv_rsqrt(double a) { return rsqrt(a); }
+__device__ __forceinline__ float sv_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double sv_mul(double a, double b) { return __dmul_rn(a, b); }
+
+// compute_fkp (src/read_data.c:453-454) and the weight sums (src/main.c:151-163) of one catalogue:
+// the FKP factor in double, the weight stored back in the catalogue's type (float for the reference's
+// struct); w*w and w*w*nbar in that type, summed in double. which: 0 data, 1 randoms.
+template <typename T>
+__global__ void __launch_bounds__(256) k_sv_prepare(SvIn<T> in, long long n, int fkp, double fkp_pk, T *wout,
+                                                    SvStats *st, int which) {
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  int bad = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    T w = in.w[i];
+    const T nb = in.nbar[i];
+    if (fkp) {
+      const double f = __ddiv_rn(1.0, __dadd_rn(1.0, __dmul_rn((double)nb, fkp_pk)));
+      w = (T)__dmul_rn((double)w, f);
+      wout[i] = w;
+    }
+    if (!isfinite((double)w) || !isfinite((double)nb)) bad = 1;
+    const T ww = sv_mul(w, w);
+    s0 += (double)w;
+    s1 += (double)ww;
+    s2 += (double)sv_mul(ww, nb);
+  }
+  const double v[3] = {s0, s1, s2};
+  double *const dst[3] = {&st->wsum[which], &st->w2sum[which], &st->w2nsum[which]};
+  sv_block_add<3>(v, dst);
+  if (bad) atomicOr(&st->nonfinite, 1);
+}
+
+// assign_survey_data (src/read_data.c:471-494) for the density: every object with weight
+// prefactor * w into grid 0 and, shifted by half a cell, into grid 1. The randoms' prefactor is
+// -alpha = -(sum w_data / sum w_rand) (src/main.c:169, 229), read from the sums on the device.
+template <typename T, typename R>
+__global__ void __launch_bounds__(256) k_sv_paint(Geom g, SvIn<T> in, const T *wk, long long n, int which, R *g0,
+                                                  R *g1, SvStats *st) {
+  const double pref = which ? -__ddiv_rn(st->wsum[0], st->wsum[1]) : 1.0;
+  double l_ngrid = 0.0, l_dc0 = 0.0, l_dc1 = 0.0;
+  int bad = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double x = (double)in.x[i], y = (double)in.y[i], z = (double)in.z[i], w = (double)wk[i];
+    if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
+      bad = 1;
+      continue;
+    }
+    const double wp = __dmul_rn(pref, w);
+    AxisTaps ax, ay, az;
+    double got = 0.0;
+    if (sv_axes(g, x, y, z, ax, ay, az)) {
+      l_dc0 += sv_deposit(g, g0, wp, ax, ay, az);
+      got = wp;
+    }
+    l_ngrid += __ddiv_rn(got, w);
+    if (g.interlace && sv_axes(g, DADD(x, g.hx), DADD(y, g.hy), DADD(z, g.hz), ax, ay, az))
+      l_dc1 += sv_deposit(g, g1, wp, ax, ay, az);
+  }
+  const double v[3] = {l_ngrid, l_dc0, l_dc1};
+  double *const dst[3] = {&st->ngrid[which], &st->dc[0], &st->dc[1]};
+  sv_block_add<3>(v, dst);
+  if (bad) atomicOr(&st->nonfinite, 1);
+}
+
+// ------------------------------------------------------------------------ weighted term grids
+// w[c] = a[c] h_lm(r^) for every cell c = (ix, iy, iz < NZ) of the painted grid(s), r^ the unit vector
+// from the observer to the cell corner (ix dx + XMIN - X_Origin, ...) (src/main.c:551-559 and the
+// other product loops). A corner at the observer (r2 == 0) gets r2 = 1, as in the reference, so its
+// harmonics vanish. l = 0 copies the grid (src/main.c:503-511). Threads run along z (coalesced);
+// `rows` rows of one block share it.
+template <typename R>
+__global__ void __launch_bounds__(256) k_sv_weight(const R *a0, const R *a1, R *w0, R *w1, const R *vx, const R *vy,
+                                                   const R *vz, int nx, int ny, int nz, long long row, int l, int m,
+                                                   int tpr) {
+  const int rows_per_block = blockDim.x / tpr;
+  const long long r = (long long)blockIdx.x * rows_per_block + threadIdx.x / tpr;
+  if (r >= (long long)nx * ny) return;
+  const int ix = (int)(r / ny), iy = (int)(r - (long long)ix * ny);
+  const R px = vx[ix], py = vy[iy];
+  const R pxy = px * px + py * py;
+  const long long base = r * row;
+  for (int iz = threadIdx.x % tpr; iz < nz; iz += tpr) {
+    R h = (R)1;
+    if (l > 0) {
+      const R pz = vz[iz];
+      R r2 = pxy + pz * pz;
+      if (r2 == (R)0) r2 = (R)1;
+      const R inv = sv_rsqrt(r2);
+      h = harm<R>(l, m, px * inv, py * inv, pz * inv);
+    }
+    w0[base + iz] = a0[base + iz] * h;
+    if (a1) w1[base + iz] = a1[base + iz] * h;
+  }
+}
+
+// -------------------------------------------------------------------------------------- binning
+template <typename R>
+struct SvC;
+template <>
+struct SvC<float> {
+  typedef float2 C;
+};
+template <>
+struct SvC<double> {
+  typedef double2 C;
+};
+
+// What one assign pass needs beyond the periodic tables.
+template <typename R>
+struct SvAssign {
+  typedef typename SvC<R>::C C;
+  const C *g0, *g1;     // transformed term grid(s) [NX][NY][NZ/2+1]
+  C *F0;                // monopole field (the l = 0 pass writes it)
+  const double *dc;     // exact DC of the painted grid(s): the l = 0 pass's k = 0 mode
+  R coef;               // c_lm
+  int m;
+  // the observer's cell (l = 0 pass only): painted values there and e^{-2 pi i q o/N} per axis
+  int origin;
+  const R *a0, *a1;
+  long long oind;
+  const C *ox, *oy, *oz;
+};
+
+constexpr int SV_ICHUNK = 128;
+
+// assign_survey_power (src/main.c:781-967) for one FFT set. L = 0: F0 = the interlacing-combined
+// field, P0 += w |F0|^2; at k = 0 also P2 += L_2(0) w |F0|^2 and P4 += L_4(0) w |F0|^2; elsewhere the
+// observer cell's closed-form term for P2 and P4. L > 0: P_L += w c_lm h_lm(k^) X.F0 for k != 0, with
+// X.F0 = Re(X conj F0) for even L and dkr F0i - dki F0r for odd L (src/main.c:908-917). w = NM times
+// the deconvolution (times 0.25 when interlacing, :890-899). One thread per (ky, kz) column walks x
+// over a chunk of SV_ICHUNK; bin sums run per thread over equal-bin stretches, then per CTA in shared
+// memory, then FP64 global atomics. Modes beyond the top bin edge are skipped as in k_bin.
+template <typename R, int L>
+__global__ void __launch_bounds__(256) k_sv_assign(BinParams bp, BinTables t, SvAssign<R> sa, double *bins) {
+  typedef typename SvC<R>::C C;
+  constexpr bool F32 = sizeof(R) == 4;
+  const int nk = bp.nk;
+  __shared__ R sb[3 * 512];  // [3][nk] (L = 0: P0, P2, P4; else one row)
+  __shared__ double sE[515];
+  __shared__ float sElo[515], sEhi[515];
+  __shared__ R sfx2[SV_ICHUNK], scx[SV_ICHUNK], sfx[SV_ICHUNK];
+  __shared__ C sex[SV_ICHUNK], sox[SV_ICHUNK];
+  const int i0 = blockIdx.y * SV_ICHUNK, i1 = min(bp.nx, i0 + SV_ICHUNK);
+  for (int c = threadIdx.x; c < 3 * nk; c += blockDim.x) sb[c] = (R)0;
+  for (int c = threadIdx.x; c < nk + 3; c += blockDim.x) {
+    sE[c] = t.E[c];
+    sElo[c] = t.Elo[c];
+    sEhi[c] = t.Ehi[c];
+  }
+  for (int c = threadIdx.x; c < i1 - i0; c += blockDim.x) {
+    const int i = i0 + c;
+    if (F32) {
+      sfx2[c] = (R)t.fx2f[i];
+      scx[c] = (R)t.cxf[i];
+      sfx[c] = (R)t.fxf[i];
+      sex[c].x = (R)t.exf[i].x;
+      sex[c].y = (R)t.exf[i].y;
+    } else {
+      sfx2[c] = (R)t.fx2d[i];
+      scx[c] = (R)t.cxd[i];
+      sfx[c] = (R)t.fxd[i];
+      sex[c].x = (R)t.exd[i].x;
+      sex[c].y = (R)t.exd[i].y;
+    }
+    if (L == 0 && sa.origin) sox[c] = sa.ox[i];
+  }
+  __syncthreads();
+  const long long cols = (long long)bp.ny * bp.nzc;
+  const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (col < cols) {
+    const int j = (int)(col / bp.nzc), k = (int)(col - (long long)j * bp.nzc);
+    const R syz = F32 ? (R)(t.fy2f[j] + t.fz2f[k]) : (R)0;
+    const double fy2 = t.fy2d[j], fz2 = t.fz2d[k];
+    R cyz = F32 ? (R)(t.cyf[j] * t.czf[k]) : (R)(t.cyd[j] * t.czd[k]);
+    if (bp.interlace) cyz *= (R)0.25;
+    C eyz;
+    if (F32) {
+      const float2 a = t.eyf[j], b = t.ezf[k];
+      eyz.x = a.x * b.x - a.y * b.y;
+      eyz.y = a.x * b.y + a.y * b.x;
+    } else {
+      const double2 a = t.eyd[j], b = t.ezd[k];
+      eyz.x = a.x * b.x - a.y * b.y;
+      eyz.y = a.x * b.y + a.y * b.x;
+    }
+    const R fy = F32 ? (R)t.fyf[j] : (R)t.fyd[j], fz = F32 ? (R)t.fzf[k] : (R)t.fzd[k];
+    C oyz, o0, o1;
+    oyz.x = oyz.y = o0.x = o0.y = o1.x = o1.y = (R)0;
+    if (L == 0 && sa.origin) {
+      const C a = sa.oy[j], b = sa.oz[k];
+      oyz.x = a.x * b.x - a.y * b.y;
+      oyz.y = a.x * b.y + a.y * b.x;
+      o0.x = sa.a0[sa.oind];
+      if (bp.interlace) o1.x = sa.a1[sa.oind];
+    }
+    const long long base = (long long)j * bp.nzc + k;
+    R acc0 = (R)0, acc2 = (R)0, acc4 = (R)0;
+    int cur = -1;
+    R lo = (R)1, hi = (R)0;
+    const float top = sElo[nk + 1] - (float)(F32 ? (float)syz : (float)(fy2 + fz2));
+    const int rr = top > 0.0f ? min(bp.xhalf, (int)(sqrtf(top) / bp.fx_step) + 1) : -1;
+    for (int i = i0; i < i1; i++) {
+      if (i > rr && i < bp.nx - rr) {
+        i = bp.nx - rr - 1;
+        continue;
+      }
+      const int li = i - i0;
+      R s;
+      if (F32) s = sfx2[li] + syz;
+      else s = (R)__dadd_rn(__dadd_rn((double)sfx2[li], fy2), fz2);
+      if (!(s >= lo && s < hi)) {
+        int b = cur < -1 ? -1 : cur;
+        if (F32) {
+          const float sf = (float)s;
+          while (b < nk && sf >= sElo[b + 2]) b++;
+          while (b > -1 && sf < sEhi[b + 1]) b--;
+          if (sf >= sElo[b + 1] && sf < sEhi[b + 2]) {
+            lo = (R)sElo[b + 1];
+            hi = (R)sEhi[b + 2];
+          } else {  // within a few ulps of an edge: the exact FP64 s decides
+            b = exact_bin(sE, nk, __dadd_rn(__dadd_rn(t.fx2d[i], fy2), fz2), b);
+            lo = (R)1;
+            hi = (R)0;
+          }
+        } else {
+          b = exact_bin(sE, nk, (double)s, b);
+          lo = (R)sE[b + 1];
+          hi = (R)sE[b + 2];
+        }
+        if (b != cur) {
+          if (cur >= 0 && cur < nk) {
+            if (L == 0) {
+              if (acc0 != (R)0) atomicAdd(&sb[cur], acc0);
+              if (acc2 != (R)0) atomicAdd(&sb[nk + cur], acc2);
+              if (acc4 != (R)0) atomicAdd(&sb[2 * nk + cur], acc4);
+            } else if (acc0 != (R)0) {
+              atomicAdd(&sb[cur], acc0);
+            }
+            acc0 = acc2 = acc4 = (R)0;
+          }
+          cur = b;
+        }
+      }
+      if (cur < 0 || cur >= nk) continue;
+      const bool kzero = (i == 0 && col == 0);
+      if (L > 0 && kzero) continue;
+      const long long off = (long long)i * cols + base;
+      const C ex = sex[li];
+      C e;
+      e.x = ex.x * eyz.x - ex.y * eyz.y;
+      e.y = ex.x * eyz.y + ex.y * eyz.x;
+      C X = sa.g0[off];
+      if (L == 0 && kzero) {
+        X.x = (R)sa.dc[0];
+        X.y = (R)0;
+      }
+      if (bp.interlace) {
+        C a = sa.g1[off];
+        if (L == 0 && kzero) {
+          a.x = (R)sa.dc[1];
+          a.y = (R)0;
+        }
+        X.x += a.x * e.x - a.y * e.y;
+        X.y += a.x * e.y + a.y * e.x;
+      }
+      const R gc = cyz * scx[li] * (R)herm_nm(i, j, k, bp.xhalf);
+      if (L == 0) {
+        sa.F0[off] = X;
+        const R p = (X.x * X.x + X.y * X.y) * gc;
+        acc0 += p;
+        if (kzero) {
+          acc2 += (R)-0.5 * p;
+          acc4 += (R)0.375 * p;
+        } else if (sa.origin) {
+          // O = (delta_o + e delta_o,interlaced) e^{-i k.r_o}
+          C O = o0;
+          O.x += o1.x * e.x;
+          O.y += o1.x * e.y;
+          const C ph = sox[li];
+          C q;
+          q.x = ph.x * oyz.x - ph.y * oyz.y;
+          q.y = ph.x * oyz.y + ph.y * oyz.x;
+          const R orr = O.x * q.x - O.y * q.y, oii = O.x * q.y + O.y * q.x;
+          const R pc = (orr * X.x + oii * X.y) * gc;
+          acc2 += (R)-0.5 * pc;
+          acc4 += (R)0.375 * pc;
+        }
+      } else {
+        const C F = sa.F0[off];
+        const R v = (L & 1) ? X.x * F.y - X.y * F.x : X.x * F.x + X.y * F.y;
+        const R inv = sv_rsqrt(s);
+        const R hv = harm<R>(L, sa.m, sfx[li] * inv, fy * inv, fz * inv);
+        acc0 += gc * sa.coef * hv * v;
+      }
+    }
+    if (cur >= 0 && cur < nk) {
+      if (acc0 != (R)0) atomicAdd(&sb[cur], acc0);
+      if (L == 0) {
+        if (acc2 != (R)0) atomicAdd(&sb[nk + cur], acc2);
+        if (acc4 != (R)0) atomicAdd(&sb[2 * nk + cur], acc4);
+      }
+    }
+  }
+  __syncthreads();
+  // bins laid out [5][nk]
+  for (int c = threadIdx.x; c < (L == 0 ? 3 : 1) * nk; c += blockDim.x) {
+    const R v = sb[c];
+    if (v == (R)0) continue;
+    const int row = L == 0 ? 2 * (c / nk) : L;
+    atomicAdd(&bins[row * nk + c % nk], (double)v);
+  }
+}
+
+// ------------------------------------------------------------------------------------ the context
+struct capow_survey_ctx {
+  capow_params p;
+  capow_survey_params sv;
+  capow_options o;
+  int prec;  // CAPOW_FP64 or CAPOW_FP32_MIXED
+  Geom g;
+  BinParams bp;
+  BinTables bt;
+  int nslot;  // 1 + DoInterlacing
+  cudaStream_t stream;
+  bool own_stream;
+  void *paint;  // nslot painted grids, main_sz reals each
+  void *work;   // nslot term grids
+  void *F0;     // main_sz reals (complex [NX][NY][NZ/2+1])
+  void *vx, *vy, *vz;  // cell-corner offsets from the observer per axis (R)
+  SvStats *st;
+  double *bins;  // [5][nk]
+  unsigned long long *nmodes_d, *nmodes2d_d;
+  std::vector<unsigned long long> nmodes;
+  cufftHandle plan;
+  bool plan_ok, plan_per_grid;
+  // the observer's cell (r2 == 0), if any
+  int origin;
+  long long oind;
+  void *ox, *oy, *oz;
+  // staging of host catalogues and the FKP-weighted copies: [catalogue][x, y, z, w, nbar, wfkp]
+  void *stage[2][6];
+  size_t stage_bytes[2][6];
+  double *h_bins;
+  SvStats *h_st;
+  std::vector<void *> allocs;
+  cudaEvent_t ev[3];
+  int sets;
+  long long launches;
+  bool done;
+  char err[512];
+};
+
+static void *sv_dalloc(capow_survey_ctx *c, size_t bytes) {
+  void *p = nullptr;
+  if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+  c->allocs.push_back(p);
+  return p;
+}
+
+static int sv_validate(const capow_params *p, const capow_survey_params *sv, const capow_options *o, char *err,
+                       size_t n) {
+#define BAD(code, ...)             \
+  do {                             \
+    snprintf(err, n, __VA_ARGS__); \
+    return code;                   \
+  } while (0)
+  if (p->InterpOrder < 1 || p->InterpOrder > 3) BAD(CAPOW_EINVAL, "InterpOrder is neither 1, 2 nor 3");
+  if (p->DoInterlacing != 0 && p->DoInterlacing != 1) BAD(CAPOW_EINVAL, "DoInterlacing is neither 0 nor 1");
+  if (p->Output2D != 0 && p->Output2D != 1) BAD(CAPOW_EINVAL, "Output2D is neither 0 nor 1");
+  if (p->OutputLog != 0 && p->OutputLog != 1) BAD(CAPOW_EINVAL, "OutputLog is neither 0 nor 1");
+  if (p->NX <= 0 || p->NY <= 0 || p->NZ <= 0) BAD(CAPOW_EINVAL, "NX, NY and NZ must be > 0");
+  if (p->NK <= 0) BAD(CAPOW_EINVAL, "NK is less than 1");
+  if (p->NK > 512) BAD(CAPOW_ENOTSUP, "the survey binning holds at most 512 k bins");
+  if (!(p->XMAX > p->XMIN) || !(p->YMAX > p->YMIN) || !(p->ZMAX > p->ZMIN)) BAD(CAPOW_EINVAL, "box MAX must exceed MIN");
+  if (p->Maxk < p->Mink) BAD(CAPOW_EINVAL, "Maxk is less than Mink");
+  if (p->Momentum != 0) BAD(CAPOW_ENOTSUP, "the survey estimator is provided for the density (Momentum 0) only");
+  if (o->precision != CAPOW_FP64 && o->precision != CAPOW_FP32_MIXED)
+    BAD(CAPOW_ENOTSUP, "survey precision must be CAPOW_FP64 or CAPOW_FP32_MIXED");
+  if ((long long)p->NX * p->NY * 2 * (p->NZ / 2 + 1) >= (1LL << 40)) BAD(CAPOW_EINVAL, "grid too large");
+  if (!sv) BAD(CAPOW_EINVAL, "no survey parameters");
+  return CAPOW_OK;
+#undef BAD
+}
+
+template <typename T>
+static T *sv_upload(capow_survey_ctx *c, const std::vector<T> &h) {
+  T *d = (T *)sv_dalloc(c, sizeof(T) * h.size());
+  if (d && cudaMemcpy(d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+  return d;
+}
+
+// cell-corner offset from the observer along one axis, as the reference forms it (src/main.c:554)
+static double corner(int i, double d, double mn, double o) { return (double)i * d + mn - o; }
+
+extern "C" int capow_survey_create(const capow_params *p, const capow_survey_params *sv, const capow_options *opt,
+                                   capow_survey_ctx **out) {
+  if (!p || !out) return CAPOW_EINVAL;
+  *out = nullptr;
+  capow_options o;
+  memset(&o, 0, sizeof o);
+  if (opt) o = *opt;
+  else o.precision = CAPOW_FP32_MIXED;
+  capow_survey_ctx *c = new (std::nothrow) capow_survey_ctx();
+  if (!c) return CAPOW_ENOMEM;
+  int rc = sv_validate(p, sv, &o, c->err, sizeof c->err);
+  if (rc) {
+    fprintf(stderr, "capow_survey_create: %s\n", c->err);
+    delete c;
+    return rc;
+  }
+  c->p = *p;
+  c->sv = *sv;
+  c->o = o;
+  c->prec = o.precision;
+  *out = c;  // from here on capow_survey_destroy releases partial state
+  CK(c, cudaSetDevice(o.device));
+  if (o.stream) {
+    c->stream = (cudaStream_t)o.stream;
+    c->own_stream = false;
+  } else {
+    CK(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    c->own_stream = true;
+  }
+  for (int k = 0; k < 3; k++) CK(c, cudaEventCreate(&c->ev[k]));
+  c->g = make_geom(*p);
+  c->nslot = 1 + p->DoInterlacing;
+  const bool f64 = c->prec == CAPOW_FP64;
+  const size_t eb = f64 ? 8 : 4;
+  const size_t ge = (size_t)c->g.main_sz;
+  c->paint = sv_dalloc(c, eb * ge * c->nslot);
+  c->work = sv_dalloc(c, eb * ge * c->nslot);
+  c->F0 = sv_dalloc(c, eb * ge);
+  c->st = (SvStats *)sv_dalloc(c, sizeof(SvStats));
+  const int nk = p->NK;
+  c->bins = (double *)sv_dalloc(c, sizeof(double) * 5 * nk);
+  c->nmodes_d = (unsigned long long *)sv_dalloc(c, sizeof(unsigned long long) * nk);
+  c->nmodes2d_d = (unsigned long long *)sv_dalloc(c, sizeof(unsigned long long));
+  if (!c->paint || !c->work || !c->F0 || !c->st || !c->bins || !c->nmodes_d || !c->nmodes2d_d)
+    FAIL(c, CAPOW_ENOMEM, "device allocation failed (grids need %.2f GB)", eb * ge * (2.0 * c->nslot + 1) / 1e9);
+  CK(c, cudaMallocHost((void **)&c->h_bins, sizeof(double) * 5 * nk));
+  CK(c, cudaMallocHost((void **)&c->h_st, sizeof(SvStats)));
+  // corner offsets per axis, and the observer's cell: the corner whose three offsets square to 0
+  const Geom &g = c->g;
+  std::vector<double> v[3];
+  const int nn[3] = {p->NX, p->NY, p->NZ};
+  const double dd[3] = {g.dx, g.dy, g.dz}, mn[3] = {p->XMIN, p->YMIN, p->ZMIN},
+               org[3] = {sv->X_Origin, sv->Y_Origin, sv->Z_Origin};
+  int oc[3], ncand[3] = {0, 0, 0};
+  for (int a = 0; a < 3; a++) {
+    v[a].resize(nn[a]);
+    for (int i = 0; i < nn[a]; i++) {
+      v[a][i] = corner(i, dd[a], mn[a], org[a]);
+      if (v[a][i] * v[a][i] == 0.0) {
+        oc[a] = i;
+        ncand[a]++;
+      }
+    }
+  }
+  c->origin = ncand[0] && ncand[1] && ncand[2];
+  if (ncand[0] > 1 || ncand[1] > 1 || ncand[2] > 1)
+    FAIL(c, CAPOW_ENOTSUP, "several cell corners within 1e-154 of the observer along one axis");
+  if (f64) {
+    c->vx = sv_upload(c, v[0]);
+    c->vy = sv_upload(c, v[1]);
+    c->vz = sv_upload(c, v[2]);
+  } else {
+    std::vector<float> f[3];
+    for (int a = 0; a < 3; a++) {
+      f[a].resize(nn[a]);
+      for (int i = 0; i < nn[a]; i++) f[a][i] = (float)v[a][i];
+    }
+    c->vx = sv_upload(c, f[0]);
+    c->vy = sv_upload(c, f[1]);
+    c->vz = sv_upload(c, f[2]);
+  }
+  if (!c->vx || !c->vy || !c->vz) FAIL(c, CAPOW_ENOMEM, "observer offset tables");
+  if (c->origin) {
+    c->oind = (long long)oc[2] + g.row * ((long long)oc[1] + (long long)p->NY * oc[0]);
+    const int len[3] = {p->NX, p->NY, p->NZ / 2 + 1};
+    void **dst[3] = {&c->ox, &c->oy, &c->oz};
+    for (int a = 0; a < 3; a++) {
+      std::vector<double2> e2(len[a]);
+      std::vector<float2> e1(len[a]);
+      for (int q = 0; q < len[a]; q++) {  // e^{-2 pi i q o / N}, the exponent reduced exactly
+        const long long r = ((long long)q * oc[a]) % nn[a];
+        const double ang = -2.0 * M_PI * (double)r / (double)nn[a];
+        e2[q] = make_double2(cos(ang), sin(ang));
+        e1[q] = make_float2((float)cos(ang), (float)sin(ang));
+      }
+      *dst[a] = f64 ? (void *)sv_upload(c, e2) : (void *)sv_upload(c, e1);
+      if (!*dst[a]) FAIL(c, CAPOW_ENOMEM, "observer phase tables");
+    }
+  }
+  // bins: the periodic tables, exact edges and mode counts (the survey's modes, NM and Nyquist rule
+  // are the periodic ones, src/main.c:840-905)
+  BinParams &bp = c->bp;
+  memset(&bp, 0, sizeof bp);
+  bp.nx = p->NX; bp.ny = p->NY; bp.nz = p->NZ; bp.nzc = p->NZ / 2 + 1; bp.xhalf = p->NX / 2;
+  bp.nk = nk; bp.nmu = p->NMU; bp.los = 3; bp.interlace = p->DoInterlacing;
+  bp.odd = p->Odd_Multipoles; bp.out2d = 0; bp.nfields = 1;
+  bp.two_pi = 2.0 * M_PI;
+  bp.fx_step = (float)(1.0 / ((float)p->NX * g.dx));
+  bin_params_kguess(bp, *p);
+  if (build_bin_tables(*p, g, c->prec, c->bt, c->allocs, c->stream)) FAIL(c, CAPOW_ENOMEM, "bin tables");
+  CK(c, cudaMemsetAsync(c->nmodes_d, 0, sizeof(unsigned long long) * nk, c->stream));
+  launch_mode_counts(c->stream, bp, c->bt, c->nmodes_d, c->nmodes2d_d, &c->launches);
+  CK(c, cudaGetLastError());
+  c->nmodes.resize(nk);
+  CK(c, cudaMemcpyAsync(c->nmodes.data(), c->nmodes_d, sizeof(unsigned long long) * nk, cudaMemcpyDeviceToHost,
+                        c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  // one batched in-place real-to-complex plan over the nslot term grids (fftw_execute of plan and
+  // plan_interlace, src/main.c:513-514 and the product loops)
+  int n[3] = {p->NX, p->NY, p->NZ};
+  int inembed[3] = {p->NX, p->NY, 2 * bp.nzc}, onembed[3] = {p->NX, p->NY, bp.nzc};
+  const long long idist = (long long)ge, odist = (long long)ge / 2;
+  if (idist > 0x7fffffffLL || c->nslot == 1) {
+    CKFFT(c, cufftPlan3d(&c->plan, p->NX, p->NY, p->NZ, f64 ? CUFFT_D2Z : CUFFT_R2C));
+    c->plan_per_grid = true;
+  } else {
+    CKFFT(c, cufftPlanMany(&c->plan, 3, n, inembed, 1, (int)idist, onembed, 1, (int)odist, f64 ? CUFFT_D2Z : CUFFT_R2C,
+                           c->nslot));
+  }
+  c->plan_ok = true;
+  CKFFT(c, cufftSetStream(c->plan, c->stream));
+  return CAPOW_OK;
+}
+
+extern "C" void capow_survey_destroy(capow_survey_ctx *c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->plan_ok) cufftDestroy(c->plan);
+  for (void *q : c->allocs) cudaFree(q);
+  for (int a = 0; a < 2; a++)
+    for (int k = 0; k < 6; k++)
+      if (c->stage[a][k]) cudaFree(c->stage[a][k]);
+  if (c->h_bins) cudaFreeHost(c->h_bins);
+  if (c->h_st) cudaFreeHost(c->h_st);
+  for (int k = 0; k < 3; k++)
+    if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+extern "C" const char *capow_survey_last_error(const capow_survey_ctx *c) { return c ? c->err : "no context"; }
+extern "C" int64_t capow_survey_kernel_launches(const capow_survey_ctx *c) { return c ? c->launches : 0; }
+
+// device copy of one catalogue array (host input) in staging slot [cat][k]
+static int sv_stage(capow_survey_ctx *c, int cat, int k, const void *src, size_t bytes, bool on_device,
+                    const void **dst) {
+  if (on_device) {
+    *dst = src;
+    return CAPOW_OK;
+  }
+  if (c->stage_bytes[cat][k] < bytes) {
+    if (c->stage[cat][k]) cudaFree(c->stage[cat][k]);
+    c->stage[cat][k] = nullptr;
+    c->stage_bytes[cat][k] = 0;
+    CK(c, cudaMalloc(&c->stage[cat][k], bytes ? bytes : 16));
+    c->stage_bytes[cat][k] = bytes;
+  }
+  if (bytes) CK(c, cudaMemcpyAsync(c->stage[cat][k], src, bytes, cudaMemcpyHostToDevice, c->stream));
+  *dst = c->stage[cat][k];
+  return CAPOW_OK;
+}
+
+static int sv_blocks(long long n) {
+  long long b = (n + 255) / 256;
+  if (b > 152LL * 16) b = 152LL * 16;
+  return b < 1 ? 1 : (int)b;
+}
+
+template <typename T, typename R>
+static int sv_enqueue_catalogue(capow_survey_ctx *c, int cat, const capow_survey_catalogue *in) {
+  const size_t n = in->n, bytes = sizeof(T) * n;
+  const void *src[5] = {in->x, in->y, in->z, in->w, in->nbar};
+  const void *d[5];
+  for (int k = 0; k < 5; k++) {
+    int rc = sv_stage(c, cat, k, src[k], bytes, in->on_device != 0, &d[k]);
+    if (rc) return rc;
+  }
+  SvIn<T> sin{(const T *)d[0], (const T *)d[1], (const T *)d[2], (const T *)d[3], (const T *)d[4]};
+  const int fkp = c->sv.FKP_Column < 0;
+  const T *wk = sin.w;
+  if (fkp) {
+    if (c->stage_bytes[cat][5] < bytes) {
+      if (c->stage[cat][5]) cudaFree(c->stage[cat][5]);
+      c->stage[cat][5] = nullptr;
+      c->stage_bytes[cat][5] = 0;
+      CK(c, cudaMalloc(&c->stage[cat][5], bytes ? bytes : 16));
+      c->stage_bytes[cat][5] = bytes;
+    }
+    wk = (const T *)c->stage[cat][5];
+  }
+  if (n) {
+    k_sv_prepare<T><<<sv_blocks(n), 256, 0, c->stream>>>(sin, (long long)n, fkp, c->sv.FKP_Pk, (T *)wk, c->st, cat);
+    c->launches++;
+  }
+  return CAPOW_OK;
+}
+
+template <typename T, typename R>
+static void sv_launch_paint(capow_survey_ctx *c, int cat, const capow_survey_catalogue *in) {
+  const size_t n = in->n;
+  if (!n) return;
+  const void *d[5];
+  for (int k = 0; k < 5; k++) {
+    const void *src[5] = {in->x, in->y, in->z, in->w, in->nbar};
+    d[k] = in->on_device ? src[k] : c->stage[cat][k];
+  }
+  SvIn<T> sin{(const T *)d[0], (const T *)d[1], (const T *)d[2], (const T *)d[3], (const T *)d[4]};
+  const T *wk = c->sv.FKP_Column < 0 ? (const T *)c->stage[cat][5] : sin.w;
+  R *g0 = (R *)c->paint, *g1 = c->nslot > 1 ? (R *)c->paint + c->g.main_sz : nullptr;
+  k_sv_paint<T, R><<<sv_blocks(n), 256, 0, c->stream>>>(c->g, sin, wk, (long long)n, cat, g0, g1, c->st);
+  c->launches++;
+}
+
+template <typename R>
+static int sv_multipoles(capow_survey_ctx *c) {
+  typedef typename SvC<R>::C C;
+  const capow_params &p = c->p;
+  const Geom &g = c->g;
+  const long long ge = g.main_sz;
+  R *a0 = (R *)c->paint, *a1 = c->nslot > 1 ? a0 + ge : nullptr;
+  R *w0 = (R *)c->work, *w1 = c->nslot > 1 ? w0 + ge : nullptr;
+  int tpr = 1;
+  while (tpr < p.NZ && tpr < 256) tpr <<= 1;
+  const long long rows = (long long)p.NX * p.NY, rpb = 256 / tpr;
+  const unsigned wblocks = (unsigned)((rows + rpb - 1) / rpb);
+  const long long cols = (long long)p.NY * c->bp.nzc;
+  const dim3 agrid((unsigned)((cols + 255) / 256), (unsigned)((p.NX + SV_ICHUNK - 1) / SV_ICHUNK));
+  SvAssign<R> sa;
+  memset(&sa, 0, sizeof sa);
+  sa.g0 = (const C *)w0;
+  sa.g1 = (const C *)w1;
+  sa.F0 = (C *)c->F0;
+  sa.dc = (const double *)((const char *)c->st + offsetof(SvStats, dc));
+  sa.origin = c->origin;
+  sa.a0 = a0;
+  sa.a1 = a1;
+  sa.oind = c->oind;
+  sa.ox = (const C *)c->ox;
+  sa.oy = (const C *)c->oy;
+  sa.oz = (const C *)c->oz;
+  const int step = p.Odd_Multipoles ? 1 : 2;  // src/main.c:490-492
+  c->sets = 0;
+  for (int l = 0; l <= 4; l += step) {
+    for (int m = 0; m < 2 * l + 1; m++) {
+      k_sv_weight<R><<<wblocks, 256, 0, c->stream>>>(a0, a1, w0, w1, (const R *)c->vx, (const R *)c->vy,
+                                                     (const R *)c->vz, p.NX, p.NY, p.NZ, g.row, l, m, tpr);
+      c->launches++;
+      if (c->plan_per_grid) {
+        for (int s = 0; s < c->nslot; s++) {
+          R *wg = w0 + s * ge;
+          if (sizeof(R) == 8) CKFFT(c, cufftExecD2Z(c->plan, (cufftDoubleReal *)wg, (cufftDoubleComplex *)wg));
+          else CKFFT(c, cufftExecR2C(c->plan, (cufftReal *)wg, (cufftComplex *)wg));
+        }
+      } else if (sizeof(R) == 8) {
+        CKFFT(c, cufftExecD2Z(c->plan, (cufftDoubleReal *)w0, (cufftDoubleComplex *)w0));
+      } else {
+        CKFFT(c, cufftExecR2C(c->plan, (cufftReal *)w0, (cufftComplex *)w0));
+      }
+      sa.m = m;
+      sa.coef = (R)harm_coef(l, m);
+      switch (l) {
+        case 0: k_sv_assign<R, 0><<<agrid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins); break;
+        case 1: k_sv_assign<R, 1><<<agrid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins); break;
+        case 2: k_sv_assign<R, 2><<<agrid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins); break;
+        case 3: k_sv_assign<R, 3><<<agrid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins); break;
+        default: k_sv_assign<R, 4><<<agrid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins); break;
+      }
+      c->launches++;
+      c->sets++;
+    }
+  }
+  CK(c, cudaGetLastError());
+  return CAPOW_OK;
+}
+
+template <typename T, typename R>
+static int sv_run(capow_survey_ctx *c, const capow_survey_catalogue *data, const capow_survey_catalogue *rand) {
+  CK(c, cudaMemsetAsync(c->st, 0, sizeof(SvStats), c->stream));
+  CK(c, cudaMemsetAsync(c->bins, 0, sizeof(double) * 5 * c->p.NK, c->stream));
+  CK(c, cudaEventRecord(c->ev[0], c->stream));
+  CK(c, cudaMemsetAsync(c->paint, 0, sizeof(R) * (size_t)c->g.main_sz * c->nslot, c->stream));
+  int rc = sv_enqueue_catalogue<T, R>(c, 0, data);
+  if (!rc) rc = sv_enqueue_catalogue<T, R>(c, 1, rand);
+  if (rc) return rc;
+  sv_launch_paint<T, R>(c, 0, data);
+  sv_launch_paint<T, R>(c, 1, rand);
+  CK(c, cudaGetLastError());
+  CK(c, cudaEventRecord(c->ev[1], c->stream));
+  rc = sv_multipoles<R>(c);
+  if (rc) return rc;
+  CK(c, cudaEventRecord(c->ev[2], c->stream));
+  return CAPOW_OK;
+}
+
+static bool sv_cat_ok(const capow_survey_catalogue *c) {
+  if (!c || (c->dtype != CAPOW_F32 && c->dtype != CAPOW_F64)) return false;
+  if (c->n && (!c->x || !c->y || !c->z || !c->w || !c->nbar)) return false;
+  return true;
+}
+
+extern "C" int capow_survey_power(capow_survey_ctx *c, const capow_survey_catalogue *data,
+                                  const capow_survey_catalogue *rand, capow_spectrum *out, capow_survey_stats *st) {
+  if (!c) return CAPOW_EINVAL;
+  if (!sv_cat_ok(data) || !sv_cat_ok(rand))
+    FAIL(c, CAPOW_EINVAL, "survey catalogue: dtype must be CAPOW_F32 or CAPOW_F64 with x, y, z, w and nbar given");
+  if (data->dtype != rand->dtype) FAIL(c, CAPOW_EINVAL, "data and randoms must have the same dtype");
+  CK(c, cudaSetDevice(c->o.device));
+  c->done = false;
+  int rc;
+  const bool f64 = c->prec == CAPOW_FP64;
+  if (data->dtype == CAPOW_F32) rc = f64 ? sv_run<float, double>(c, data, rand) : sv_run<float, float>(c, data, rand);
+  else rc = f64 ? sv_run<double, double>(c, data, rand) : sv_run<double, float>(c, data, rand);
+  if (rc) return rc;
+  const int nk = c->p.NK;
+  CK(c, cudaMemcpyAsync(c->h_bins, c->bins, sizeof(double) * 5 * nk, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(c->h_st, c->st, sizeof(SvStats), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->done = true;
+  const SvStats &s = *c->h_st;
+  if (s.nonfinite) FAIL(c, CAPOW_EINVAL, "non-finite coordinate, weight or number density in a survey catalogue");
+  // src/main.c:166-176 (Momentum 0)
+  const double alpha = s.wsum[0] / s.wsum[1];
+  const double rand_nbwsq = s.w2sum[1] * (alpha * alpha);
+  const double rand_nbsqwsq = s.w2nsum[1] * alpha;
+  if (st) {
+    st->ngrid_data = s.ngrid[0];
+    st->ngrid_rand = s.ngrid[1] / -alpha;
+    st->data_nbw = s.wsum[0];
+    st->data_nbwsq = s.w2sum[0];
+    st->data_nbsqwsq = s.w2nsum[0];
+    st->rand_nbw = s.wsum[1];
+    st->rand_nbwsq = rand_nbwsq;
+    st->rand_nbsqwsq = rand_nbsqwsq;
+  }
+  if (out) {
+    for (int l = 0; l < 5; l++) {
+      if (!out->pk[l]) continue;
+      const bool have = (l % 2 == 0) || c->p.Odd_Multipoles;
+      for (int b = 0; b < nk; b++) out->pk[l][b] = have ? c->h_bins[l * nk + b] : 0.0;
+    }
+    if (out->nmodes)
+      for (int b = 0; b < nk; b++) out->nmodes[b] = (int64_t)c->nmodes[b];
+    if (c->p.Output2D) {  // the survey estimator fills no 2-D bins (src/main.c:476-479 only allocates them)
+      const int n2 = nk * c->p.NMU;
+      if (out->pk2d)
+        for (int b = 0; b < n2; b++) out->pk2d[b] = 0.0;
+      if (out->nmodes2d)
+        for (int b = 0; b < n2; b++) out->nmodes2d[b] = 0;
+    }
+    out->alpha = alpha;
+    out->shot = s.w2sum[0] + rand_nbwsq;
+    out->norm = rand_nbsqwsq;
+    out->last_bin = -1;
+    out->kind = 0;
+  }
+  return CAPOW_OK;
+}
+
+extern "C" int capow_survey_copy_grid(capow_survey_ctx *c, int which, double *host_out) {
+  if (!c || !host_out || which < 0 || which >= c->nslot) return CAPOW_EINVAL;
+  if (!c->done) FAIL(c, CAPOW_ESTATE, "no survey evaluation yet");
+  const size_t ge = (size_t)c->g.main_sz;
+  if (c->prec == CAPOW_FP64) {
+    CK(c, cudaMemcpy(host_out, (double *)c->paint + which * ge, sizeof(double) * ge, cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<float> tmp(ge);
+    CK(c, cudaMemcpy(tmp.data(), (float *)c->paint + which * ge, sizeof(float) * ge, cudaMemcpyDeviceToHost));
+    for (size_t q = 0; q < ge; q++) host_out[q] = tmp[q];
+  }
+  return CAPOW_OK;
+}
+
+extern "C" int capow_survey_stage_ms(capow_survey_ctx *c, float *paint_ms, float *multipole_ms, int *fft_sets) {
+  if (!c) return CAPOW_EINVAL;
+  if (!c->done) FAIL(c, CAPOW_ESTATE, "no survey evaluation yet");
+  if (paint_ms) CK(c, cudaEventElapsedTime(paint_ms, c->ev[0], c->ev[1]));
+  if (multipole_ms) CK(c, cudaEventElapsedTime(multipole_ms, c->ev[1], c->ev[2]));
+  if (fft_sets) *fft_sets = c->sets;
+  return CAPOW_OK;
+}

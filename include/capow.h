@@ -260,6 +260,93 @@ int64_t capow_kernel_launches(const capow_ctx *ctx);
 
 void capow_destroy(capow_ctx *ctx);
 
+/* ---------------------------------------------------------------- survey estimator */
+/* The reference's other estimator (Periodic 0, Survey 1; src/main.c:77-95, 149-204, 226-258, 279-288,
+ * 472-967): data and random catalogues in a non-periodic box seen from an observer, FKP weights,
+ * the random counts subtracted in the painted grid, and the Yamamoto multipoles, each an FFT of the
+ * density weighted by functions of the line of sight r^ to every cell, crossed with the monopole
+ * field F0. Density only (the reference's survey Momentum 0).
+ *
+ *   reference                                             this library
+ *   ----------------------------------------------------   -----------------------------------
+ *   read_survey_serial_ascii (read_data.c:184-361)         capow_read_survey (host)
+ *   compute_fkp              (read_data.c:450-466)         capow_survey_power (on the GPU)
+ *   sums, alpha, shot, norm  (main.c:149-204)              capow_survey_power (on the GPU)
+ *   assign_survey_data       (read_data.c:471-494, 514-745) capow_survey_power (on the GPU)
+ *   compute_survey_power + assign_survey_power
+ *                            (main.c:472-967)              capow_survey_power (on the GPU)
+ *   output_power arithmetic  (main.c:1019-1056)            capow_normalise
+ *
+ * The reference forms P_l from the Cartesian products of r^ (1, 3, 6, 10 and 15 FFTs for l = 0..4);
+ * this library uses the equivalent real solid harmonics of r^ (1, 3, 5, 7 and 9 FFTs), and adds the
+ * one cell the two forms treat differently (a cell whose corner is exactly the observer, where the
+ * reference's r^ products are 0) as a closed-form term. Same multipoles within FP64 rounding. */
+
+/* the survey tags of run_parameters.dat (read_params.c:145-222, vars.h) */
+typedef struct capow_survey_params {
+  int Periodic, Survey;                 /* estimator switches: Periodic 0, Survey 1 selects this one */
+  int Coord_Type;                       /* 0: Cartesian x y z; 1: RA, Dec (degrees), z; 2: RA, Dec (radians), z */
+  double X_Origin, Y_Origin, Z_Origin;  /* observer position, box units */
+  double REDMININ, REDMAXIN;            /* redshift cut of the reader */
+  long long NOBJ_Max;                   /* capacity of the reference's object arrays */
+  int NBAR_Column;                      /* > 0: number density from the catalogue (its 5th number);
+                                           < 0: the reference's compute_nbar (not provided: ENOTSUP) */
+  double SkyArea;
+  int FKP_Column;                       /* < 0: FKP weights w *= 1/(1 + nbar FKP_Pk) (main.c:89-94) */
+  double FKP_Pk, FKP_Pk_mom, FKP_Pk_cross;
+} capow_survey_params;
+
+/* One catalogue as the reference holds it after reading (struct survey_data, vars.h:136-142: float
+ * fields). dtype CAPOW_F32 reproduces the reference's float storage of the FKP weights bit for bit;
+ * CAPOW_F64 keeps every per-object value in double. */
+typedef struct capow_survey_catalogue {
+  size_t n;
+  int dtype;            /* CAPOW_F32 or CAPOW_F64, every array */
+  int on_device;        /* 1: device pointers; 0: host pointers (copied in) */
+  const void *x, *y, *z; /* Cartesian positions, box units */
+  const void *w;        /* weights as read (before FKP) */
+  const void *nbar;     /* number density */
+} capow_survey_catalogue;
+
+/* counters of one survey evaluation */
+typedef struct capow_survey_stats {
+  double ngrid_data, ngrid_rand; /* assign_survey_data's "gridded" sums: accepted objects counted w/w
+                                    (read_data.c:474-491; the randoms' sum divided by -alpha) */
+  double data_nbw, data_nbwsq, data_nbsqwsq; /* sum w, w^2, w^2 nbar over the data (main.c:151-156) */
+  double rand_nbw, rand_nbwsq, rand_nbsqwsq; /* the same over the randoms, the last two after the alpha
+                                                scaling of main.c:170-171 */
+} capow_survey_stats;
+
+typedef struct capow_survey_ctx capow_survey_ctx;
+
+/* create_grids for a survey run (main.c:1123-1251): params as for capow_create (LOS is not used;
+ * Momentum must be 0; Output2D gives the reference's all-zero 2-D bins), the observer and FKP
+ * settings from sv. Precision CAPOW_FP64 or CAPOW_FP32_MIXED (FP32 grids and FFTs, FP64 sums and
+ * bins); fft_path is ignored. Allocates 2 * (1 + DoInterlacing) + 1 padded grids: the painted grid
+ * (and its interlaced copy), as many work grids for the FFTs, and the complex F0 grid. */
+int capow_survey_create(const capow_params *p, const capow_survey_params *sv, const capow_options *opt,
+                        capow_survey_ctx **out);
+
+/* One survey evaluation: FKP weights (when FKP_Column < 0), the weight sums, alpha = sum w_d / sum w_r,
+ * the data painted with weight w and the randoms with -alpha w into the same grid(s), then every
+ * multipole (P1, P3 only with Odd_Multipoles). Fills out's raw sums, Nmodes, shot, norm and alpha as
+ * capow_power does (normalise with capow_normalise); st may be NULL. Ends with a stream
+ * synchronisation. CAPOW_EINVAL for a non-finite coordinate, weight or number density. */
+int capow_survey_power(capow_survey_ctx *ctx, const capow_survey_catalogue *data, const capow_survey_catalogue *rand,
+                       capow_spectrum *out, capow_survey_stats *st);
+
+/* the painted grid (which 0) or its interlaced copy (1) of the last evaluation, as float64 in the
+ * reference's padded layout [NX][NY][2*(NZ/2+1)] (data minus alpha randoms). For parity tests. */
+int capow_survey_copy_grid(capow_survey_ctx *ctx, int which, double *host_out);
+
+/* device milliseconds of the last evaluation: weights, sums and painting; the multipole FFTs and
+ * binning. And the number of FFT sets it ran (1 + 5 + 9, or 25 with odd multipoles). */
+int capow_survey_stage_ms(capow_survey_ctx *ctx, float *paint_ms, float *multipole_ms, int *fft_sets);
+
+int64_t capow_survey_kernel_launches(const capow_survey_ctx *ctx);
+const char *capow_survey_last_error(const capow_survey_ctx *ctx);
+void capow_survey_destroy(capow_survey_ctx *ctx);
+
 /* ---------------------------------------------------------------- host-side file formats */
 
 /* read_parameterfile + check_inputs (read_params.c:30-428): parse a run_parameters.dat with
@@ -274,6 +361,34 @@ int capow_read_params(const char *path, capow_params *out, char *msg, size_t msg
 int capow_read_catalogue(const char *path, int los, size_t *n, double **x, double **y, double **z, double **vlos,
                          char *msg, size_t msglen);
 void capow_free(void *p);
+
+/* read_parameterfile + check_inputs for either estimator: as capow_read_params, but a survey run
+ * (Periodic 0) is accepted and the survey tags are returned in sv (Periodic and Survey included). */
+int capow_read_survey_params(const char *path, capow_params *out, capow_survey_params *sv, char *msg, size_t msglen);
+
+/* One survey catalogue as read_survey_serial_ascii (read_data.c:184-361) keeps it: the reference's float
+ * fields of every object that passed the redshift cut, in file order. */
+typedef struct capow_survey_objects {
+  size_t n;                 /* objects kept (NKEEP) */
+  unsigned long long nread; /* catalogue lines read (NREAD) */
+  float *x, *y, *z;         /* Cartesian positions (converted from RA, Dec, z for Coord_Type 1, 2) */
+  float *w, *nbar, *redshift;
+  double lo[3], hi[3];      /* the "X, Y, Z" ranges the reference prints: min and max of the kept objects'
+                               coordinates, starting from 1e-30 and -1e30 (read_data.c:192-194, 344-349) */
+  double redmin, redmax;    /* min and max redshift of the kept objects (read_data.c:327-328) */
+  char *log;                /* what the reference prints while reading: the "Read N objects, kept K" progress
+                               lines and the objects skipped for zero weight (Coord_Type 1, 2) */
+} capow_survey_objects;
+
+/* read_survey_serial_ascii: `#` lines at the top skipped; per line 12 numbers for data (x y z w nbar
+ * ..., the reader keeps the 5th as nbar, read_data.c:244-250) or 8 for randoms; Coord_Type 0 takes the
+ * redshift from the distance |x| through the reference's 10000-point redshift-distance table
+ * (main.c:1233-1248: a natural cubic spline of z(r)); objects outside [REDMININ, REDMAXIN] are
+ * dropped; an object outside the grid less the interpolation margin is fatal (read_data.c:293-299).
+ * Errors (CAPOW_EINVAL) carry the reference's message in msg. Free with capow_survey_objects_free. */
+int capow_read_survey(const char *path, const capow_params *p, const capow_survey_params *sv, int randoms,
+                      capow_survey_objects *out, char *msg, size_t msglen);
+void capow_survey_objects_free(capow_survey_objects *o);
 
 /* output_power's file format (main.c:1058-1101), plus `<path>_2D` when Output2D. */
 int capow_write_output(const char *path, const capow_params *p, const capow_spectrum *s);

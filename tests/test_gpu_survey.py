@@ -1,0 +1,196 @@
+"""GPU parity of the survey estimator (capow_survey_*) against the oracle's restatement of the reference's
+survey path (pinned bit for bit to the unmodified reference on the golden survey cases): the unmodified
+reference's raw bin sums for the golden catalogues, the oracle on seeded catalogues (every order, with and
+without interlacing, odd multipoles, an observer inside the grid on a cell corner), painted grids, the
+weight sums, and the edge cases of the reader's float storage."""
+import os
+
+import numpy as np
+import pytest
+
+import capow_gb300 as cg
+import oracle as orc
+from parity_util import TOL, assert_spectrum
+from test_oracle_golden import SURVEY, write_survey_inputs
+
+pytestmark = pytest.mark.gpu
+
+
+def _catalogues(tmp_path, p, nd, nr, seed, origin_inside=False):
+    """Seeded data (12 columns) and random (8 columns) catalogues inside the reader's bounds."""
+    rng = np.random.default_rng(seed)
+    dx, dy, dz = (p.XMAX - p.XMIN) / p.NX, (p.YMAX - p.YMIN) / p.NY, (p.ZMAX - p.ZMIN) / p.NZ
+    m = p.InterpOrder - 1
+    lo = np.array([p.XMIN + m * dx, p.YMIN + m * dy, p.ZMIN + m * dz])
+    hi = np.array([p.XMAX - m * dx, p.YMAX - m * dy, p.ZMAX - m * dz]) - (0.5 * np.array([dx, dy, dz])
+                                                                          if p.DoInterlacing else 0.0)
+    span = hi - lo
+
+    def cat(n, cols, clustered):
+        a = np.zeros((n, cols))
+        if clustered:  # a few clumps on top of a uniform part, so the multipoles are not pure noise
+            c = lo + span * rng.uniform(0.2, 0.8, size=(8, 3))
+            k = rng.integers(0, 8, n)
+            pos = c[k] + rng.normal(scale=0.08, size=(n, 3)) * span
+            u = rng.uniform(size=n) < 0.4
+            pos[u] = lo + span * rng.uniform(size=(int(u.sum()), 3))
+            pos = np.clip(pos, lo, hi - 1e-9 * span)
+        else:
+            pos = lo + span * rng.uniform(size=(n, 3)) * (1 - 1e-12)
+        a[:, :3] = pos
+        a[:, 3] = rng.uniform(0.5, 1.5, n)
+        a[:, 4] = rng.uniform(1e-4, 3e-4, n)
+        return a
+
+    d, r = cat(nd, 12, True), cat(nr, 8, False)
+    df, rf = str(tmp_path / "data.txt"), str(tmp_path / "rand.txt")
+    np.savetxt(df, d, fmt="%.17g")
+    np.savetxt(rf, r, fmt="%.17g")
+    return df, rf
+
+
+def _write_params(tmp_path, **kw):
+    p = orc.Params(**kw)
+    pf = str(tmp_path / "p.dat")
+    p.write_file(pf)
+    prm, sv = cg.read_survey_params(pf)
+    return p, prm, sv
+
+
+def _gpu(prm, sv, df, rf, precision, grids=False, device_inputs=False):
+    data = cg.read_survey(df, prm, sv, False)
+    rand = cg.read_survey(rf, prm, sv, True)
+    keys = ("x", "y", "z", "w", "nbar")
+    if device_inputs:
+        import torch
+        dd = {k: torch.from_numpy(data[k]).cuda() for k in keys}
+        rr = {k: torch.from_numpy(rand[k]).cuda() for k in keys}
+    else:
+        dd, rr = {k: data[k] for k in keys}, {k: rand[k] for k in keys}
+    with cg.SurveySpectrum(prm, sv, precision=precision) as ss:
+        res = ss.power(dd, rr)
+        g = [ss.grid(w) for w in range(1 + prm.DoInterlacing)] if grids else None
+        res["launches"] = ss.kernel_launches()
+        res["stage"] = ss.stage_ms()
+    return res, g
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("name", sorted(SURVEY))
+def test_survey_golden_reference_sums(gpu, tmp_path, name, precision):
+    """The unmodified reference's raw sums for the golden survey catalogues, read by the product's reader."""
+    p, pf, df, rf, d = write_survey_inputs(tmp_path, name)
+    prm, sv = cg.read_survey_params(pf)
+    res, _ = _gpu(prm, sv, df, rf, precision)
+    ref = {k: d[k] for k in ("Pk0", "Pk1", "Pk2", "Pk3", "Pk4", "Nmodes")}
+    assert_spectrum(res, ref, np.abs(ref["Pk0"]), precision, odd=bool(p.Odd_Multipoles), label=f"{name} {precision}")
+    r = orc.survey_run(p, df, rf)
+    for k, v in (("alpha", r["alpha"]), ("shot", r["shot"]), ("norm", r["normf"])):
+        assert abs(res[k] - v) <= 1e-13 * abs(v), (k, res[k], v)
+    assert res["stage"][2] == (25 if p.Odd_Multipoles else 15)
+    assert res["launches"] > 0
+
+
+CASES = [(1, 0, 0), (2, 0, 1), (2, 1, 0), (3, 1, 1), (3, 0, 0), (1, 1, 1)]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("order,il,odd", CASES)
+def test_survey_matches_oracle(gpu, tmp_path, precision, order, il, odd):
+    """Seeded clustered data and uniform randoms on a 40x36x32 grid off the observer: raw sums, Nmodes,
+    alpha, shot, norm and the gridded counters against the oracle."""
+    p, prm, sv = _write_params(tmp_path, NX=40, NY=36, NZ=32, XMIN=300.0, XMAX=1100.0, YMIN=-400.0, YMAX=320.0,
+                               ZMIN=-300.0, ZMAX=340.0, InterpOrder=order, DoInterlacing=il, NK=20, Maxk=0.15,
+                               Odd_Multipoles=odd, Periodic=0, X_Origin=-50.0, Y_Origin=20.0, Z_Origin=5.0,
+                               REDMININ=0.0, REDMAXIN=5.0, NOBJ_Max=100000, NBAR_Column=5, FKP_Column=-1,
+                               FKP_Pk=4000.0)
+    df, rf = _catalogues(tmp_path, p, 4000, 30000, seed=order * 10 + il + 2 * odd)
+    r = orc.survey_run(p, df, rf, grids=True)
+    res, g = _gpu(prm, sv, df, rf, precision, grids=True)
+    label = f"{precision} order={order} il={il} odd={odd}"
+    assert_spectrum(res, r["raw"], np.abs(r["raw"]["Pk0"]), precision, odd=bool(odd), label=label)
+    for k, v in (("alpha", r["alpha"]), ("shot", r["shot"]), ("norm", r["normf"])):
+        assert abs(res[k] - v) <= 1e-13 * abs(v), (label, k)
+    assert abs(res["stats"]["ngrid_data"] - r["ngrid_data"]) <= 1e-9 * r["ngrid_data"]
+    assert abs(res["stats"]["ngrid_rand"] - r["ngrid_rand"]) <= 1e-9 * r["ngrid_rand"]
+    row = 2 * (p.NZ // 2 + 1)
+    for which, key in enumerate(("ddg", "ddg_interlace")[: 1 + il]):
+        a = g[which].reshape(p.NX, p.NY, row)[:, :, :p.NZ]
+        b = r["painted"][key][: p.NX * p.NY * row].reshape(p.NX, p.NY, row)[:, :, :p.NZ]
+        scale = np.abs(b).max()
+        err = np.abs(a - b).max() / scale
+        assert err <= (1e-12 if precision == "fp64" else 1e-5), (label, key, err)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("order", [2, 3])
+def test_survey_observer_on_a_cell_corner(gpu, tmp_path, precision, order):
+    """The observer inside the grid exactly on a cell corner (r2 == 0 there: the reference zeroes every
+    r^ product of that cell). The solid-harmonic multipoles add that cell's L_l(0) term in closed form."""
+    p, prm, sv = _write_params(tmp_path, NX=32, NY=32, NZ=32, XMIN=-400.0, XMAX=400.0, YMIN=-400.0, YMAX=400.0,
+                               ZMIN=-400.0, ZMAX=400.0, InterpOrder=order, DoInterlacing=1, NK=16, Maxk=0.12,
+                               Odd_Multipoles=1, Periodic=0, X_Origin=0.0, Y_Origin=0.0, Z_Origin=0.0,
+                               REDMININ=0.0, REDMAXIN=5.0, NOBJ_Max=100000, NBAR_Column=5, FKP_Column=-1,
+                               FKP_Pk=4000.0)
+    df, rf = _catalogues(tmp_path, p, 5000, 25000, seed=70 + order)
+    # a heavy object next to the observer, so the corner cell carries weight
+    with open(df, "a") as f:
+        f.write("1.0 2.0 -1.5 40 0.0002 0 0 0 0 0 0 0\n")
+    r = orc.survey_run(p, df, rf, grids=True)
+    oc = r["painted"]["ddg"].reshape(-1)[(16 * 32 + 16) * 34 + 16]
+    assert oc != 0.0
+    res, _ = _gpu(prm, sv, df, rf, precision)
+    assert_spectrum(res, r["raw"], np.abs(r["raw"]["Pk0"]), precision, odd=True, label=f"origin {precision}")
+
+
+def test_survey_float_storage_edges_and_device_inputs(gpu, tmp_path):
+    """Objects the reader accepts in double whose float copy lands on the grid edge (the Survey clamps
+    pull the stencil back), an object on the TSC x limit, and host vs device inputs giving the same sums."""
+    p, prm, sv = _write_params(tmp_path, NX=20, NY=24, NZ=16, XMIN=-500.0, XMAX=500.0, YMIN=-600.0, YMAX=600.0,
+                               ZMIN=-400.0, ZMAX=400.0, InterpOrder=2, DoInterlacing=0, NK=12, Maxk=0.09,
+                               Odd_Multipoles=1, Periodic=0, X_Origin=900.0, Y_Origin=900.0, Z_Origin=900.0,
+                               REDMININ=0.0, REDMAXIN=5.0, NOBJ_Max=100000, NBAR_Column=5, FKP_Column=-1,
+                               FKP_Pk=3000.0)
+    df, rf = _catalogues(tmp_path, p, 2000, 9000, seed=5)
+    dy = 1200.0 / 24
+    edge = 600.0 - dy  # YMAX_Interp for CIC; just below it in double, on it in float
+    below = np.nextafter(edge, -np.inf)
+    assert below < edge and np.float32(below) == np.float32(edge)
+    with open(df, "a") as f:
+        for x in (-100.0, 0.0, 250.0):
+            f.write(f"{x!r} {below!r} 10.0 1.2 0.0002 0 0 0 0 0 0 0\n")
+    r = orc.survey_run(p, df, rf)
+    for precision in ("fp64", "fp32"):
+        host, _ = _gpu(prm, sv, df, rf, precision)
+        dev, _ = _gpu(prm, sv, df, rf, precision, device_inputs=True)
+        assert_spectrum(host, r["raw"], np.abs(r["raw"]["Pk0"]), precision, odd=True, label=f"edges {precision}")
+        for k in ("Pk0", "Pk2", "Pk4"):
+            assert np.allclose(host[k], dev[k], rtol=1e-12 if precision == "fp64" else 1e-5, atol=0), k
+
+
+def test_survey_rejects_non_finite_and_bad_arguments(gpu, tmp_path):
+    p, prm, sv = _write_params(tmp_path, NX=16, NY=16, NZ=16, XMIN=0.0, XMAX=800.0, YMIN=0.0, YMAX=800.0,
+                               ZMIN=0.0, ZMAX=800.0, InterpOrder=2, DoInterlacing=0, NK=8, Maxk=0.1, Periodic=0,
+                               X_Origin=-10.0, REDMININ=0.0, REDMAXIN=5.0, NOBJ_Max=1000, NBAR_Column=5,
+                               FKP_Column=-1, FKP_Pk=1000.0)
+    rng = np.random.default_rng(1)
+    cat = {k: rng.uniform(100, 700, 100).astype(np.float32) for k in ("x", "y", "z")}
+    cat["w"] = np.ones(100, np.float32)
+    cat["nbar"] = np.full(100, 1e-4, np.float32)
+    bad = dict(cat)
+    bad["x"] = cat["x"].copy()
+    bad["x"][7] = np.nan
+    with cg.SurveySpectrum(prm, sv, precision="fp64") as ss:
+        with pytest.raises(cg.CapowError) as e:
+            ss.power(bad, cat)
+        assert e.value.status == cg.EINVAL
+        ok = ss.power(cat, cat)  # the context stays usable
+        assert np.isfinite(ok["Pk0"]).all()
+        mixed = dict(cat)
+        mixed["w"] = np.ones(100)
+        with pytest.raises(ValueError):
+            ss.power(mixed, cat)
+    p2 = cg.Params(**{**prm.__dict__, "Momentum": 1})
+    with pytest.raises(cg.CapowError) as e:
+        cg.SurveySpectrum(p2, sv)
+    assert e.value.status == cg.ENOTSUP

@@ -16,8 +16,8 @@ import oracle as orc
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = os.path.join(HERE, "golden")
-CASES = sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLD, "*.npz")))
 MANIFEST = json.load(open(os.path.join(GOLD, "manifest.json")))
+CASES = sorted(n for n in (os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLD, "*.npz"))) if n in MANIFEST)
 
 
 @pytest.fixture(scope="module", autouse=True)
