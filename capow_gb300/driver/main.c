@@ -1,10 +1,11 @@
-/* capow -- drop-in command-line driver for the periodic-box path, with the reference's
+/* capow -- drop-in command-line driver for the periodic-box and survey paths, with the reference's
  * argument contract, parameter file, catalogue format, stdout summary and output files
  * (src/main.c:28-298). The work runs on one GB300 through libcapow_gpu (include/capow.h).
  *
  *   capow <ParameterFile> <DataFile> <RandomFile> <OutputFile>
  *
- * RandomFile is accepted and unused, as in the reference's periodic branch.
+ * Periodic 1 reads DataFile only (RandomFile is accepted and unused, as in the reference's periodic
+ * branch); Periodic 0 with Survey 1 runs the survey estimator on DataFile and RandomFile.
  * Optional environment (the reference's parser rejects unknown tags, so these are not tags):
  *   CAPOW_PRECISION = fp32 (default) | fp64 | det
  *   CAPOW_SPECTRA   = e.g. "dd,dp,pp": one paint and one set of FFTs for several spectra;
@@ -43,6 +44,149 @@ static void die_status(capow_ctx *ctx, int rc, const char *where) {
   exit(1);
 }
 
+/* output_power's part of main (src/main.c:1004-1101) for one spectrum */
+static void write_spectrum(const capow_params *p, capow_spectrum *s, const char *name) {
+  printf("Writing multipoles to file: %s\n", name);
+  if (p->Output2D) printf("Writing 2D power spectrum to file:%s_2D\n", name);
+  fflush(stdout);
+  capow_normalise(p, s);
+  if (s->last_bin >= 0) {
+    printf("Last full bin: %d (k=%g)\n", s->last_bin, capow_bin_centre(p, s->last_bin));
+    fflush(stdout);
+  }
+  if (capow_write_output(name, p, s) != CAPOW_OK) {
+    printf("cannot open output file: %s\n", name);
+    printf("Fatal Error at line 142 in routine read_data\n");
+    exit(1);
+  }
+}
+
+/* read_survey_serial_ascii's stdout (src/read_data.c:207-210, 229-233, 343-349) around one read */
+static void read_one(const capow_params *p, const capow_survey_params *sv, const char *path, int randoms,
+                     capow_survey_objects *o) {
+  char msg[8192];
+  printf("Reading: %s\n", path);
+  fflush(stdout);
+  int rc = capow_read_survey(path, p, sv, randoms, o, msg, sizeof msg);
+  if (o->log) printf("%s", o->log);
+  if (rc != CAPOW_OK) die(msg);
+  printf("Have %llu objects\n", (unsigned long long)o->n);
+  printf("%12.6lf <   X  < %12.6lf\n", o->lo[0], o->hi[0]);
+  printf("%12.6lf <   Y  < %12.6lf\n", o->lo[1], o->hi[1]);
+  printf("%12.6lf <   Z  < %12.6lf\n", o->lo[2], o->hi[2]);
+  fflush(stdout);
+}
+
+/* The survey branch of main (src/main.c:77-95, 149-204, 226-258, 279-298): the stdout lines of
+ * compute_survey_power's Cartesian products (src/main.c:497-760) are printed as the reference prints
+ * them; the library computes the same multipoles through solid harmonics. */
+static int run_survey(const capow_params *p, const capow_survey_params *sv, const char *datafile,
+                      const char *randfile, const char *outfile) {
+  capow_options opt;
+  memset(&opt, 0, sizeof opt);
+  opt.precision = CAPOW_FP32_MIXED;
+  const char *pe = getenv("CAPOW_PRECISION");
+  if (pe && !strcmp(pe, "fp64")) opt.precision = CAPOW_FP64;
+  else if (pe && !strcmp(pe, "det")) die("CAPOW_PRECISION=det is not provided for the survey estimator\n");
+  const char *de = getenv("CAPOW_DEVICE");
+  if (de) opt.device = atoi(de);
+
+  banner("Allocating grid");
+  printf("Setting neighbours...\n");
+  printf("Reserving memory...\n");
+  fflush(stdout);
+  capow_survey_ctx *ctx = NULL;
+  int rc = capow_survey_create(p, sv, &opt, &ctx);
+  if (rc != CAPOW_OK) {
+    printf("capow_survey_create: %s (%s)\n", capow_strerror(rc), ctx ? capow_survey_last_error(ctx) : "");
+    fflush(stdout);
+    exit(1);
+  }
+  printf("Creating redshift-distance lookup table...\n");
+
+  banner("Reading input data and assigning to grid");
+  capow_survey_objects data, rand;
+  read_one(p, sv, datafile, 0, &data);
+  read_one(p, sv, randfile, 1, &rand);
+  if (sv->FKP_Column < 0) printf("Computing FKP Weights...\n");
+  fflush(stdout);
+
+  const int nk = p->NK, n2 = p->Output2D ? p->NK * p->NMU : 0;
+  double *store = (double *)calloc((size_t)(5 * nk + n2), sizeof(double));
+  int64_t *mstore = (int64_t *)calloc((size_t)(nk + n2), sizeof(int64_t));
+  capow_spectrum spec;
+  memset(&spec, 0, sizeof spec);
+  for (int l = 0; l < 5; l++) spec.pk[l] = store + l * nk;
+  spec.nmodes = mstore;
+  if (n2) {
+    spec.pk2d = store + 5 * nk;
+    spec.nmodes2d = mstore + nk;
+  }
+  capow_survey_catalogue dc = {data.n, CAPOW_F32, 0, data.x, data.y, data.z, data.w, data.nbar};
+  capow_survey_catalogue rc_ = {rand.n, CAPOW_F32, 0, rand.x, rand.y, rand.z, rand.w, rand.nbar};
+  capow_survey_stats st;
+  rc = capow_survey_power(ctx, &dc, &rc_, &spec, &st);
+  if (rc != CAPOW_OK) {
+    printf("capow_survey_power: %s (%s)\n", capow_strerror(rc), capow_survey_last_error(ctx));
+    fflush(stdout);
+    exit(1);
+  }
+  printf("Task 0 has %llu objects, gridded %lf\n", (unsigned long long)data.n, st.ngrid_data);
+
+  banner("Computing shot-noise and normalisation"); /* src/main.c:189-193 */
+  printf("alpha = %g\n", spec.alpha);
+  printf("shot-noise [data, randoms]    = %g, %g\n", st.data_nbwsq, st.rand_nbwsq);
+  printf("normalisation [data, randoms] = %g, %g\n", st.data_nbsqwsq, st.rand_nbsqwsq);
+  fflush(stdout);
+  banner("Subtracting off expected density");
+  printf("Task 0 has %llu objects, gridded %lf\n", (unsigned long long)rand.n, st.ngrid_rand);
+
+  const int step = p->Odd_Multipoles ? 1 : 2;
+  for (int l = 0; l <= 4; l += step) {
+    static const char *const title[5] = {"monopole", "dipole", "quadrupole", "octopole", "hexadecapole"};
+    static const char *const rule[5] = {"===============================================",
+                                        "=================================================",
+                                        "=================================================",
+                                        "=================================================",
+                                        "==================================================="};
+    printf("\nFourier transforming %s overdensity field\n%s\n", title[l], rule[l]);
+    if (l == 1)
+      for (int i = 0; i < 3; i++) printf("Indices: %d\n", i);
+    if (l == 2)
+      for (int i = 0; i < 3; i++)
+        for (int j = i; j < 3; j++) printf("Indices: %d %d\n", i, j);
+    if (l == 3) /* src/main.c:648-657 */
+      for (int i = 0; i < 3; i++)
+        for (int j = i; j < (i == 0 ? i + 2 : i + 1); j++)
+          for (int k = (j != i ? 2 : 0); k < 3; k++) printf("Indices: %d %d %d\n", i, j, k);
+    if (l == 4) /* src/main.c:709-730 */
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+          int klo = 0, khi = 3;
+          if (j != i) {
+            if (i == 1) klo = 2;
+            else if (i == 2) {
+              if (j == 1) continue;
+              klo = 1;
+              khi = 2;
+            } else klo = j;
+          }
+          for (int k = klo; k < khi; k++) printf("Indices: %d %d %d\n", i, j, k);
+        }
+  }
+  fflush(stdout);
+
+  banner("Outputting power spectra");
+  write_spectrum(p, &spec, outfile);
+  banner("Cleaning up");
+  capow_survey_destroy(ctx);
+  capow_survey_objects_free(&data);
+  capow_survey_objects_free(&rand);
+  free(store);
+  free(mstore);
+  return 0;
+}
+
 int main(int argc, char **argv) {
   if (argc < 5) { /* src/main.c:39-47 */
     printf("Input parameters not found\n");
@@ -52,11 +196,16 @@ int main(int argc, char **argv) {
   }
   banner("Reading Input Parameters and setting up CAPOW");
   capow_params p;
+  capow_survey_params sv;
   char msg[8192];
-  int rc = capow_read_params(argv[1], &p, msg, sizeof msg);
+  int rc = capow_read_survey_params(argv[1], &p, &sv, msg, sizeof msg);
   if (rc != CAPOW_OK) die(msg);
   if (msg[0]) printf("%s", msg); /* warnings */
   const char *datafile = argv[2], *outfile = argv[4];
+  if (!sv.Periodic) {
+    if (!sv.Survey) die("\nERROR: neither Periodic nor Survey is set.\n\n");
+    return run_survey(&p, &sv, datafile, argv[3], outfile);
+  }
 
   capow_options opt;
   memset(&opt, 0, sizeof opt);
@@ -158,19 +307,7 @@ int main(int argc, char **argv) {
     else
       snprintf(name, sizeof name, "%s.%s", outfile,
                spec[q].kind == CAPOW_SPEC_DD ? "dd" : (spec[q].kind == CAPOW_SPEC_DP ? "dp" : "pp"));
-    printf("Writing multipoles to file: %s\n", name);
-    if (p.Output2D) printf("Writing 2D power spectrum to file:%s_2D\n", name);
-    fflush(stdout);
-    capow_normalise(&p, &spec[q]);
-    if (spec[q].last_bin >= 0) {
-      printf("Last full bin: %d (k=%g)\n", spec[q].last_bin, capow_bin_centre(&p, spec[q].last_bin));
-      fflush(stdout);
-    }
-    if (capow_write_output(name, &p, &spec[q]) != CAPOW_OK) {
-      printf("cannot open output file: %s\n", name);
-      printf("Fatal Error at line 142 in routine read_data\n");
-      exit(1);
-    }
+    write_spectrum(&p, &spec[q], name);
   }
   banner("Cleaning up");
   capow_destroy(ctx);

@@ -99,3 +99,38 @@ def test_driver_fp32_matches_reference_within_tolerance(gpu, tmp_path, name, pre
     out, gold_out_text, outfile, gold_file = _run_driver(tmp_path, name, precision)
     _same_text_close_numbers(out, gold_out_text, 1e-5, f"{name} {precision} stdout")
     _output_close(outfile, gold_file, bool(MANIFEST[name]["params"]["Odd_Multipoles"]), f"{name} {precision} file")
+
+
+SURVEY = json.load(open(os.path.join(GOLD, "survey_manifest.json")))
+
+
+def _run_survey_driver(tmp_path, name, precision):
+    m = SURVEY[name]
+    d = np.load(os.path.join(GOLD, f"{name}.npz"))
+    po = orc.Params(**m["params"])
+    pf, df, rf, of = (str(tmp_path / f) for f in ("params.dat", "data.txt", "rand.txt", "out.txt"))
+    po.write_file(pf)
+    np.savetxt(df, d["data"], fmt="%.17g")
+    np.savetxt(rf, d["rand"], fmt="%.17g")
+    env = dict(os.environ, CAPOW_PRECISION=precision)
+    r = subprocess.run([cg.DRIVER_PATH, pf, df, rf, of], capture_output=True, text=True, env=env, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    gold = open(os.path.join(GOLD, f"{name}.stdout")).read()
+    gold = gold.replace("{DATAFILE}", df).replace("{RANDFILE}", rf).replace("{OUTFILE}", of)
+    return r.stdout, gold, open(of).read(), open(os.path.join(GOLD, f"{name}.out")).read(), po
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("name", sorted(SURVEY))
+def test_driver_survey_reproduces_reference_stdout_and_file(gpu, tmp_path, name, precision):
+    """The survey branch of main (Periodic 0, Survey 1) on the golden survey catalogues: the reader's
+    counts and ranges, the FKP line, the gridded counters, alpha, shot noise and normalisation, the
+    multipole banners with the reference's index lines, and the output file. stdout is byte for byte in
+    both precisions (the weight sums are FP64 in both); the file token for token (FP64) or within the FP32
+    path's tolerance."""
+    out, gold, outfile, gold_file, po = _run_survey_driver(tmp_path, name, precision)
+    assert out == gold, name
+    if precision == "fp64":
+        _output_equal_but_roundoff(outfile, gold_file, name)
+    else:
+        _output_close(outfile, gold_file, bool(po.Odd_Multipoles), name)
