@@ -373,6 +373,125 @@ def scale_bench(args):
     print(json.dumps(line), flush=True)
 
 
+SURVEY_PARAMS = dict(NX=512, NY=512, NZ=512, XMIN=-1000.0, XMAX=1000.0, YMIN=-1000.0, YMAX=1000.0, ZMIN=-1000.0,
+                     ZMAX=1000.0, InterpOrder=3, DoInterlacing=1, NK=100, NMU=1, Output2D=0, OutputLog=0, Mink=0.0,
+                     Maxk=0.5, Omega_m=0.3089, Redshift=0.1, LOS=0, Momentum=0, Odd_Multipoles=0)
+
+
+def survey_catalogues(n_side: int, L: float, radius: float, ratio: int, seed: int):
+    """A full-sky survey around an observer at the box centre: data = a Zel'dovich lattice of n_side^3 in
+    [-L/2, L/2)^3 kept within `radius`; randoms = `ratio` times as many uniform points in the same ball;
+    w = 1, nbar = N_data / V_ball. float32 host arrays (the reference's object fields)."""
+    from capow_gb300 import synth
+
+    x, y, z, vx, vy, vz = synth.zeldovich(n_side, L=L, mesh=512, rms_cells=1.5, seed=seed)
+    pos = np.stack([x, y, z], 1).astype(np.float64) - L / 2
+    d = pos[(pos ** 2).sum(1) < radius ** 2]
+    rng = np.random.default_rng(seed + 1)
+    nr = ratio * len(d)
+    u = rng.normal(size=(nr, 3))
+    r = u / np.linalg.norm(u, axis=1)[:, None] * (radius * rng.uniform(size=(nr, 1)) ** (1.0 / 3.0))
+    nbar = len(d) / (4.0 / 3.0 * np.pi * radius ** 3)
+
+    def cat(a):
+        n = len(a)
+        return {"x": a[:, 0].astype(np.float32), "y": a[:, 1].astype(np.float32), "z": a[:, 2].astype(np.float32),
+                "w": np.ones(n, np.float32), "nbar": np.full(n, nbar, np.float32)}
+    return cat(d), cat(r)
+
+
+def survey_bench(args):
+    """The survey estimator (Periodic 0, Survey 1): a full-sky survey around an observer at the centre of a
+    2000 Mpc/h box, 192^3-lattice Zel'dovich data inside radius 950 (3.1M objects) and 10x as many uniform
+    randoms, TSC on a 512^3 grid with interlacing, FKP weights (P_FKP = 10^4), P0/P2/P4 to k = 0.5
+    (15 FFT sets of two grids). Times FP32 and FP64 evaluations with the catalogues resident in HBM (CUDA
+    events on the context stream) and through the C ABI with host arrays (e2e), and the oracle (the
+    reference's survey algorithm in C, one core) beside the GPU on a bounded sample: a 128^3 grid with
+    1/16 of the objects, timed on both. Prints one JSON line."""
+    import torch
+
+    import capow_gb300 as cg
+    import oracle as orc
+
+    dev = torch.device("cuda", 0)
+    data, rand = survey_catalogues(192, 2000.0, 950.0, 10, SEED)
+    p = cg.Params(**SURVEY_PARAMS)
+    sv = cg.SurveyParams(X_Origin=0.0, Y_Origin=0.0, Z_Origin=0.0, FKP_Column=-1, FKP_Pk=1e4, NBAR_Column=5)
+    dd = {k: torch.from_numpy(v).to(dev) for k, v in data.items()}
+    rr = {k: torch.from_numpy(v).to(dev) for k, v in rand.items()}
+    ts = torch.cuda.Stream(device=dev)
+    out = {}
+    for prec, reps in (("fp32", max(args.steps, 3)), ("fp64", 3)):
+        with cg.SurveySpectrum(p, sv, precision=prec, stream=ts.cuda_stream) as ss:
+            for _ in range(2):
+                ss.power(dd, rr)
+            times, walls = [], []
+            for _ in range(reps):
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(ts)
+                res = ss.power(dd, rr)
+                e1.record(ts)
+                torch.cuda.synchronize()
+                times.append(e0.elapsed_time(e1))
+                stage = ss.stage_ms()
+            for _ in range(reps):  # end to end: host float32 arrays copied in by the call
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                ss.power(data, rand)
+                walls.append((time.perf_counter() - t0) * 1e3)
+            out[prec] = {"ms": statistics.median(times), "e2e_ms": statistics.median(walls), "res": res,
+                         "stage": stage, "launches": ss.kernel_launches()}
+    r32, r64 = out["fp32"]["res"], out["fp64"]["res"]
+    m = np.asarray(r64["Nmodes"]) > 0
+    acc = {f"l{l}": float(np.max((2 * l + 1) * np.abs(r32[f"Pk{l}"][m] - r64[f"Pk{l}"][m]) / np.abs(r64["Pk0"][m])))
+           for l in (0, 2, 4)}
+    # bounded sample for the CPU: 128^3 grid, 1/16 of the objects, through the oracle and the GPU
+    ps = cg.Params(**dict(SURVEY_PARAMS, NX=128, NY=128, NZ=128, NK=25))
+    sub = {k: v[::16] for k, v in data.items()}, {k: v[::16] for k, v in rand.items()}
+    import tempfile
+    with tempfile.TemporaryDirectory() as tmp:
+        po = orc.Params(**{**SURVEY_PARAMS, "NX": 128, "NY": 128, "NZ": 128, "NK": 25, "Periodic": 0,
+                           "X_Origin": 0.0, "Y_Origin": 0.0, "Z_Origin": 0.0, "REDMININ": 0.0, "REDMAXIN": 10.0,
+                           "NOBJ_Max": 1 << 30, "NBAR_Column": 5, "FKP_Column": -1, "FKP_Pk": 1e4})
+        files = []
+        for nm, c, cols in (("d", sub[0], 12), ("r", sub[1], 8)):
+            a = np.zeros((len(c["x"]), cols))
+            for j, k in enumerate(("x", "y", "z", "w", "nbar")):
+                a[:, j] = c[k]
+            f = os.path.join(tmp, nm + ".txt")
+            np.savetxt(f, a, fmt="%.9g")
+            files.append(f)
+        t0 = time.perf_counter()
+        orc.survey_run(po, files[0], files[1])
+        cpu_s = time.perf_counter() - t0
+    with cg.SurveySpectrum(ps, sv, precision="fp64", stream=ts.cuda_stream) as ss:
+        ss.power(sub[0], sub[1])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ss.power(sub[0], sub[1])
+        gpu_sample_ms = (time.perf_counter() - t0) * 1e3
+    nd, nr = len(data["x"]), len(rand["x"])
+    line = {"metric": "ms per survey P0/2/4(k), 512^3 TSC interlaced, 3.1M data + 31M randoms", "unit": "ms",
+            "higher_is_better": False, "value": round(out["fp32"]["ms"], 3), "n_gpus": 1, "dtype": "f32",
+            "fp64_ms": round(out["fp64"]["ms"], 2),
+            "e2e": {"value": round(out["fp32"]["e2e_ms"], 3), "unit": "ms",
+                    "h2d_bytes_per_step": 4 * 5 * (nd + nr), "d2h_bytes_per_step": 8 * 5 * p.NK},
+            "fp64_e2e_ms": round(out["fp64"]["e2e_ms"], 2),
+            "stages_ms": {prec: {"paint": round(out[prec]["stage"][0], 3),
+                                 "multipoles": round(out[prec]["stage"][1], 3), "fft_sets": out[prec]["stage"][2]}
+                          for prec in ("fp32", "fp64")},
+            "gpu_launches": int(out["fp32"]["launches"]), "accuracy_fp32_vs_fp64": acc,
+            "cpu_baseline": {"value": round(cpu_s * 1e3, 1), "unit": "ms", "cores": 1, "kind": "port",
+                             "sample": f"128^3 grid, {len(sub[0]['x'])} data + {len(sub[1]['x'])} randoms (1/16), "
+                                       "the oracle's survey path (Cartesian products: 22 FFT sets)",
+                             "gpu_fp64_ms_same_sample": round(gpu_sample_ms, 2), "cpu_model": cpu_model()},
+            "data": "synthetic (seeded Zel'dovich lattice within a ball; uniform randoms)",
+            "config": {"workload": f"survey: {nd} data, {nr} randoms, observer at the centre of a 2000 Mpc/h box, "
+                                   "TSC 512^3 interlaced, FKP P=1e4, NK=100 to k=0.5, even multipoles"}}
+    print(json.dumps(line), flush=True)
+
+
 def gpu_bench(args, world, rank, local):
     import torch
 
@@ -528,6 +647,7 @@ def main():
     ap.add_argument("--batch", action="store_true", help="run the batched-mocks workload instead (mocks/s)")
     ap.add_argument("--mocks", type=int, default=256)
     ap.add_argument("--scale", action="store_true", help="run the 1024^3 / 134M-particle workload instead")
+    ap.add_argument("--survey", action="store_true", help="run the survey-estimator workload instead")
     ap.add_argument("--profile-case", action="store_true",
                     help="run the 8x smaller workload for profiler captures (prints stage times only)")
     args = ap.parse_args()
@@ -540,6 +660,9 @@ def main():
         return
     if args.scale:
         scale_bench(args)
+        return
+    if args.survey:
+        survey_bench(args)
         return
     world, rank, local = dist_init()
     log = (lambda *a: print(*a, file=sys.stderr, flush=True))
