@@ -309,6 +309,71 @@ extern "C" int capow_create(const capow_params *p, const capow_options *opt, cap
   return CAPOW_OK;
 }
 
+// A context that paints only: the grids, counters and FP32 tile buffers of capow_create, without bin
+// tables, plans or FFT buffers (capow_paint and capow_power refuse it: plan_ok stays false). survey != 0
+// selects the Survey rules: one density field, no RSD shift and no wrap, the halo slices discarded, the
+// Survey clamps at the upper grid edge (Geom.los = 4, Geom.survey = 1). The survey estimator paints its
+// FP32 grids through it, on the stream given in o->stream.
+int create_paint_ctx(const capow_params *p, const capow_options *o, int survey, capow_ctx **out) {
+  *out = nullptr;
+  capow_ctx *c = new (std::nothrow) capow_ctx();
+  if (!c) return CAPOW_ENOMEM;
+  c->p = *p;
+  c->o = *o;
+  c->o.spectra = CAPOW_SPEC_REFERENCE;
+  if (survey) {
+    c->p.LOS = 3;
+    c->p.Momentum = 0;
+  }
+  int rc = validate(&c->p, &c->o, c->err, sizeof c->err);
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  c->prec = o->precision;
+  *out = c;
+  CK(c, cudaSetDevice(o->device));
+  if (o->stream) {
+    c->stream = (cudaStream_t)o->stream;
+  } else {
+    CK(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    c->own_stream = true;
+  }
+  for (int k = 0; k < 4; k++) CK(c, cudaEventCreate(&c->ev[k]));
+  CK(c, cudaEventCreate(&c->ev_tile[0]));
+  CK(c, cudaEventCreate(&c->ev_tile[1]));
+  c->g = make_geom(c->p);
+  if (c->prec != CAPOW_FP64 && !(c->g.margin < 0.25f))
+    FAIL(c, CAPOW_ENOTSUP, "box coordinates too large for FP32 cell positions (error margin %.3g cells); use FP64",
+         (double)c->g.margin);
+  plan_fields(c);
+  if (survey) {
+    c->g.los = 4;
+    c->g.survey = 1;
+    c->fs.need_v = 0;
+    c->fs.moments = 0;
+    c->moments = 0;
+  }
+  const size_t eb = c->prec == CAPOW_FP64 ? 8 : 4;
+  c->grid_elems = (size_t)c->g.main_sz;
+  c->grid_base = dalloc(c, eb * c->grid_elems * c->nslot);
+  c->st = (DevStats *)dalloc(c, sizeof(DevStats));
+  c->dcv = (double *)dalloc(c, sizeof(double) * 4);
+  c->fixed_scale = (double *)dalloc(c, sizeof(double) * 2);
+  if (!c->grid_base || !c->st || !c->dcv || !c->fixed_scale)
+    FAIL(c, CAPOW_ENOMEM, "device allocation failed (grids need %.2f GB)", eb * c->grid_elems * c->nslot / 1e9);
+  CK(c, cudaMallocHost((void **)&c->h_st, sizeof(DevStats)));
+  if (c->prec != CAPOW_FP64) {
+    c->tg = choose_tiles(c->g, c->nslot, c->prec == CAPOW_FP32_DETERMINISTIC);
+    c->pb.counts = (unsigned *)dalloc(c, sizeof(unsigned) * c->tg.ntiles);
+    c->pb.offsets = (unsigned *)dalloc(c, sizeof(unsigned) * (c->tg.ntiles + 1));
+    c->pb.cursor = (unsigned *)dalloc(c, sizeof(unsigned) * c->tg.ntiles);
+    c->pb.fixed_scale = c->fixed_scale;
+    if (!c->pb.counts || !c->pb.offsets || !c->pb.cursor) FAIL(c, CAPOW_ENOMEM, "tile table allocation failed");
+  }
+  return CAPOW_OK;
+}
+
 extern "C" int capow_num_spectra(const capow_ctx *c) { return c ? c->bp.nspec : 0; }
 
 extern "C" int64_t capow_kernel_launches(const capow_ctx *c) { return c ? c->launches : 0; }
@@ -498,7 +563,7 @@ extern "C" int capow_paint(capow_ctx *c, const capow_particles *parts) {
 
 // Sync, read the counters, repaint once with a larger record buffer when the tile lists
 // overflowed. Returns a status for fatal conditions found by the paint.
-static int settle_paint(capow_ctx *c) {
+int settle_paint(capow_ctx *c) {
   CK(c, cudaMemcpyAsync(c->h_st, c->st, sizeof(DevStats), cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   if (c->h_st->overflow && c->pb.bucket_cap) {  // the overflow list filled: two passes from now on

@@ -19,7 +19,8 @@
 struct Geom {
   int nx, ny, nz;     // NX NY NZ
   int order;          // InterpOrder
-  int los;            // LOS
+  int los;            // LOS (4: survey grid, no RSD shift and no wrap)
+  int survey;         // add_to_grid's Survey branches (src/read_data.c:577-590, 672-688) instead of Periodic
   int interlace;      // DoInterlacing
   int nxtra;          // Local_nxtra = NX + InterpOrder (src/main.c:1134)
   int nzc;            // NZ/2 + 1
@@ -132,10 +133,75 @@ CAPOW_HD void tsc_axis64(double scale, bool is_x, int n, int nxtra, int los, Axi
   t.idx[2] = hi; t.w[2] = wh; t.on[2] = (hi < lim);
 }
 
+// One axis of add_to_grid's Survey branch (single rank). CIC (src/read_data.c:554-590): ix = (int)scale,
+// neighbour ix + 1; TSC (:629-688): ix = (int)(scale + 0.5), neighbours ix -/+ 1. When the upper
+// neighbour equals lim (Local_nxtra along x, NY or NZ) the stencil moves down one cell, its weights
+// unchanged. Write guards (:592-605, :690-742): CIC y/z neighbour < N; TSC centre y/z < N, low > 0,
+// high < lim.
+CAPOW_HD void survey_cic64(double scale, bool is_x, int n, int lim, AxisTaps &t) {
+  int i = (int)scale;
+  const double d = DSUB(scale, (double)i);
+  int nb = i + 1;
+  if (nb == lim) {
+    nb = lim - 1;
+    i = lim - 2;
+  }
+  t.n = 2;
+  t.idx[0] = i;  t.w[0] = DSUB(1.0, d); t.on[0] = 1;
+  t.idx[1] = nb; t.w[1] = d;            t.on[1] = is_x ? 1 : (nb < n);
+  t.on[2] = 0;
+}
+
+CAPOW_HD void survey_tsc64(double scale, bool is_x, int n, int lim, AxisTaps &t) {
+  int i = (int)DADD(scale, 0.5);
+  const double d = DSUB(scale, (double)i);
+  const double wc = DSUB(0.75, DMUL(d, d));
+  const double a = DSUB(0.5, d), b = DADD(0.5, d);
+  const double wl = DMUL(DMUL(0.5, a), a);
+  const double wh = DMUL(DMUL(0.5, b), b);
+  int lo = i - 1, hi = i + 1;
+  if (hi == lim) {
+    hi = lim - 1;
+    i = lim - 2;
+    lo = lim - 3;
+  }
+  t.n = 3;
+  t.idx[0] = i;  t.w[0] = wc; t.on[0] = is_x ? 1 : (i < n);
+  t.idx[1] = lo; t.w[1] = wl; t.on[1] = (lo > 0);
+  t.idx[2] = hi; t.w[2] = wh; t.on[2] = (hi < lim);
+}
+
+// Acceptance of one Survey add_to_grid call along one axis a (0 x, 1 y, 2 z; rank 0 of one): x in
+// [XMIN, XMAX) for NN and CIC, [XMIN, XMAX + dx) for TSC (:519-527, :546-552, :617-619); y, z in [MIN, MAX).
+CAPOW_HD bool survey_accept_axis(const Geom &g, int a, double c) {
+  const double mn = a == 0 ? g.xmin : (a == 1 ? g.ymin : g.zmin);
+  double mx = a == 0 ? g.xmax_l : (a == 1 ? g.ymax : g.zmax);
+  if (a == 0 && g.order == 3) mx = DADD(mx, g.dx);
+  return !((c < mn) || (c >= mx));
+}
+
+// Taps of one axis for a Survey run (CIC and TSC; NN has no Survey branch: the periodic rule).
+CAPOW_HD void survey_axis_taps(const Geom &g, int a, double c, AxisTaps &t) {
+  const double mn = a == 0 ? g.xmin : (a == 1 ? g.ymin : g.zmin);
+  const double d = a == 0 ? g.dx : (a == 1 ? g.dy : g.dz);
+  const int n = a == 0 ? g.nx : (a == 1 ? g.ny : g.nz);
+  const int lim = a == 0 ? g.nxtra : n;
+  const double s = DDIV(DSUB(c, mn), d);
+  if (g.order == 2) survey_cic64(s, a == 0, n, lim, t);
+  else survey_tsc64(s, a == 0, n, lim, t);
+}
+
 // Acceptance and per-axis taps of one add_to_grid call. (x, y, z) are the coordinates the
 // reader passes (already RSD-shifted, +d/2 for the interlaced copy). Returns false when the
 // particle is rejected (add_to_grid returns 0.0).
 CAPOW_HD bool exact_axes(const Geom &g, double x, double y, double z, AxisTaps &ax, AxisTaps &ay, AxisTaps &az) {
+  if (g.survey && g.order > 1) {
+    if (!survey_accept_axis(g, 0, x) || !survey_accept_axis(g, 1, y) || !survey_accept_axis(g, 2, z)) return false;
+    survey_axis_taps(g, 0, x, ax);
+    survey_axis_taps(g, 1, y, ay);
+    survey_axis_taps(g, 2, z, az);
+    return true;
+  }
   const double xmin = g.xmin, xmax = g.xmax_l;
   if (g.order == 1) {  // src/read_data.c:519-541
     if ((x < xmin) || (x >= xmax)) return false;
@@ -180,6 +246,11 @@ CAPOW_HD bool exact_axes(const Geom &g, double x, double y, double z, AxisTaps &
 // One axis of exact_axes (0 x, 1 y, 2 z): that axis's acceptance test and taps. A particle is
 // accepted when all three axes accept it, so the three can be evaluated independently.
 CAPOW_HD bool exact_axis(const Geom &g, int a, double c, AxisTaps &t) {
+  if (g.survey && g.order > 1) {
+    if (!survey_accept_axis(g, a, c)) return false;
+    survey_axis_taps(g, a, c, t);
+    return true;
+  }
   const double mn = a == 0 ? g.xmin : (a == 1 ? g.ymin : g.zmin);
   const double mx = a == 0 ? g.xmax_l : (a == 1 ? g.ymax : g.zmax);
   const double d = a == 0 ? g.dx : (a == 1 ? g.dy : g.dz);

@@ -104,8 +104,11 @@ struct capow_ctx {
 // capow_api.cu: paint the last catalogue again and prepare the DC values (capow_backward).
 int enqueue_backward_paint(capow_ctx *c);
 
-// capow_api.cu pieces shared with batch.cu
+// capow_api.cu pieces shared with batch.cu and survey.cu
 Geom make_geom(const capow_params &p);
+int create_paint_ctx(const capow_params *p, const capow_options *o, int survey, capow_ctx **out);
+// sync, read the paint counters into c->h_st, repaint c->last when the tile lists overflowed
+int settle_paint(capow_ctx *c);
 int enqueue_paint(capow_ctx *c, const capow_particles &d);
 int enqueue_power_kernels(capow_ctx *c);
 int prepare_paint_buffers(capow_ctx *c, unsigned long long nmax, bool weights);

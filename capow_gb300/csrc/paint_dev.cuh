@@ -51,6 +51,14 @@ __device__ __forceinline__ bool is_edge(const Geom &g, float sx, float sy, float
     e |= edge1(__fadd_rn(sx, 0.5f), g.nx, limx, g.order, g.margin, wrap) |
          edge1(__fadd_rn(sy, 0.5f), g.ny, (float)g.ny, g.order, g.margin, wrap) |
          edge1(__fadd_rn(sz, 0.5f), g.nz, (float)g.nz, g.order, g.margin, wrap);
+  if (g.survey && g.order > 1) {
+    // the Survey clamp moves a y or z stencil down one cell when its upper neighbour reaches N:
+    // scale in [N - 1, N) for CIC, [N - 1.5, N - 0.5) for TSC (x never gets there inside the
+    // acceptance); everything from there up takes the exact rules
+    const float up = (g.order == 3 ? 1.5f : 1.0f) + g.margin;
+    const float sh = g.interlace ? 0.5f : 0.0f;
+    e |= !(__fadd_rn(sy, sh) < (float)g.ny - up) | !(__fadd_rn(sz, sh) < (float)g.nz - up);
+  }
   return e;
 }
 

@@ -102,68 +102,9 @@ static double harm_coef(int l, int m) {
 }
 
 // -------------------------------------------------------------------------- paint (exact FP64 rules)
-// One axis of add_to_grid's Survey branch. CIC (src/read_data.c:554-590): ix = (int)scale, neighbour
-// ix + 1; TSC (:629-688): ix = (int)(scale + 0.5), neighbours ix -/+ 1. When the upper neighbour
-// equals lim (Local_nxtra along x, NY or NZ) the stencil moves down one cell, weights unchanged.
-// Write guards (:592-605, :690-742): CIC y/z neighbour < N; TSC centre y/z < N, low > 0, high < lim.
-__device__ __forceinline__ void sv_cic(double scale, bool is_x, int n, int lim, AxisTaps &t) {
-  int i = (int)scale;
-  const double d = DSUB(scale, (double)i);
-  int nb = i + 1;
-  if (nb == lim) {
-    nb = lim - 1;
-    i = lim - 2;
-  }
-  t.n = 2;
-  t.idx[0] = i;  t.w[0] = DSUB(1.0, d); t.on[0] = 1;
-  t.idx[1] = nb; t.w[1] = d;            t.on[1] = is_x ? 1 : (nb < n);
-  t.on[2] = 0;
-}
-
-__device__ __forceinline__ void sv_tsc(double scale, bool is_x, int n, int lim, AxisTaps &t) {
-  int i = (int)DADD(scale, 0.5);
-  const double d = DSUB(scale, (double)i);
-  const double wc = DSUB(0.75, DMUL(d, d));
-  const double a = DSUB(0.5, d), b = DADD(0.5, d);
-  const double wl = DMUL(DMUL(0.5, a), a);
-  const double wh = DMUL(DMUL(0.5, b), b);
-  int lo = i - 1, hi = i + 1;
-  if (hi == lim) {
-    hi = lim - 1;
-    i = lim - 2;
-    lo = lim - 3;
-  }
-  t.n = 3;
-  t.idx[0] = i;  t.w[0] = wc; t.on[0] = is_x ? 1 : (i < n);
-  t.idx[1] = lo; t.w[1] = wl; t.on[1] = (lo > 0);
-  t.idx[2] = hi; t.w[2] = wh; t.on[2] = (hi < lim);
-}
-
-// Acceptance and taps of one Survey add_to_grid call (rank 0 of one: x in [XMIN, XMAX) for NN and
-// CIC, [XMIN, XMAX + dx) for TSC, :519-527, :546-552, :617-619). NN has no Survey branch.
-__device__ __forceinline__ bool sv_axes(const Geom &g, double x, double y, double z, AxisTaps &ax, AxisTaps &ay,
-                                        AxisTaps &az) {
-  if (g.order == 1) return exact_axes(g, x, y, z, ax, ay, az);
-  const double xmin = g.xmin, xmax = g.xmax_l;
-  if (g.order == 2) {
-    if ((x < xmin) || (x >= xmax)) return false;
-  } else if ((x < xmin) || (x >= DADD(xmax, g.dx))) {
-    return false;
-  }
-  if ((y < g.ymin) || (y >= g.ymax)) return false;
-  if ((z < g.zmin) || (z >= g.zmax)) return false;
-  const double sx = DDIV(DSUB(x, xmin), g.dx), sy = DDIV(DSUB(y, g.ymin), g.dy), sz = DDIV(DSUB(z, g.zmin), g.dz);
-  if (g.order == 2) {
-    sv_cic(sx, true, g.nx, g.nxtra, ax);
-    sv_cic(sy, false, g.ny, g.ny, ay);
-    sv_cic(sz, false, g.nz, g.nz, az);
-  } else {
-    sv_tsc(sx, true, g.nx, g.nxtra, ax);
-    sv_tsc(sy, false, g.ny, g.ny, ay);
-    sv_tsc(sz, false, g.nz, g.nz, az);
-  }
-  return true;
-}
+// exact_axes (common.cuh) applies add_to_grid's Survey branches when Geom.survey is set: acceptance as for a
+// periodic run with LOS != 0, and the stencil pulled back one cell where its upper neighbour reaches the
+// axis limit (src/read_data.c:577-590, 672-688). NN has no Survey branch.
 
 // Linear index of a write (src/read_data.c:536 form) that reaches the FFT input, else -1: the halo
 // slices are discarded, the padding columns are not read by the transform, and an index the
@@ -275,17 +216,48 @@ __global__ void __launch_bounds__(256) k_sv_paint(Geom g, SvIn<T> in, const T *w
     const double wp = __dmul_rn(pref, w);
     AxisTaps ax, ay, az;
     double got = 0.0;
-    if (sv_axes(g, x, y, z, ax, ay, az)) {
+    if (exact_axes(g, x, y, z, ax, ay, az)) {
       l_dc0 += sv_deposit(g, g0, wp, ax, ay, az);
       got = wp;
     }
     l_ngrid += __ddiv_rn(got, w);
-    if (g.interlace && sv_axes(g, DADD(x, g.hx), DADD(y, g.hy), DADD(z, g.hz), ax, ay, az))
+    if (g.interlace && exact_axes(g, DADD(x, g.hx), DADD(y, g.hy), DADD(z, g.hz), ax, ay, az))
       l_dc1 += sv_deposit(g, g1, wp, ax, ay, az);
   }
   const double v[3] = {l_ngrid, l_dc0, l_dc1};
   double *const dst[3] = {&st->ngrid[which], &st->dc[0], &st->dc[1]};
   sv_block_add<3>(v, dst);
+  if (bad) atomicOr(&st->nonfinite, 1);
+}
+
+// The FP32 paint takes data and randoms as one catalogue for the tile kernels: this writes object i of
+// one catalogue at off + i of the combined float arrays, with the weight prefactor * w already applied
+// (1 for data, -alpha for randoms, as k_sv_paint), and adds its assign_survey_data counter: the object
+// counts w/w when add_to_grid accepts it (src/read_data.c:488; acceptance only, no taps).
+template <typename T>
+__global__ void __launch_bounds__(256) k_sv_combine(Geom g, SvIn<T> in, const T *wk, long long n, int which,
+                                                    long long off, float *cx, float *cy, float *cz, float *cw,
+                                                    SvStats *st) {
+  const double pref = which ? -__ddiv_rn(st->wsum[0], st->wsum[1]) : 1.0;
+  double l_ngrid = 0.0;
+  int bad = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double x = (double)in.x[i], y = (double)in.y[i], z = (double)in.z[i], w = (double)wk[i];
+    if (!(isfinite(x) && isfinite(y) && isfinite(z))) bad = 1;
+    const double wp = __dmul_rn(pref, w);
+    const bool acc = g.order == 1 ? !((x < g.xmin) || (x >= g.xmax_l) || (y < g.ymin) || (y >= g.ymax) ||
+                                      (z < g.zmin) || (z >= g.zmax))
+                                  : (survey_accept_axis(g, 0, x) && survey_accept_axis(g, 1, y) &&
+                                     survey_accept_axis(g, 2, z));
+    l_ngrid += __ddiv_rn(acc ? wp : 0.0, w);
+    cx[off + i] = (float)x;
+    cy[off + i] = (float)y;
+    cz[off + i] = (float)z;
+    cw[off + i] = (float)wp;
+  }
+  const double v[1] = {l_ngrid};
+  double *const dst[1] = {&st->ngrid[which]};
+  sv_block_add<1>(v, dst);
   if (bad) atomicOr(&st->nonfinite, 1);
 }
 
@@ -550,7 +522,10 @@ struct capow_survey_ctx {
   int nslot;  // 1 + DoInterlacing
   cudaStream_t stream;
   bool own_stream;
-  void *paint;  // nslot painted grids, main_sz reals each
+  void *paint;  // nslot painted grids, main_sz reals each (FP32: the paint context's grids)
+  capow_ctx *pc;  // FP32: the paint-only context whose tile kernels paint data and randoms
+  float *comb;    // FP32: the combined catalogue for it, [x | y | z | w] of comb_cap objects each
+  size_t comb_cap;
   void *work;   // nslot term grids
   void *F0;     // main_sz reals (complex [NX][NY][NZ/2+1])
   void *vx, *vy, *vz;  // cell-corner offsets from the observer per axis (R)
@@ -650,11 +625,21 @@ extern "C" int capow_survey_create(const capow_params *p, const capow_survey_par
   }
   for (int k = 0; k < 3; k++) CK(c, cudaEventCreate(&c->ev[k]));
   c->g = make_geom(*p);
+  c->g.los = 4;  // no RSD shift, no wrap, the halo discarded
+  c->g.survey = 1;
   c->nslot = 1 + p->DoInterlacing;
   const bool f64 = c->prec == CAPOW_FP64;
   const size_t eb = f64 ? 8 : 4;
   const size_t ge = (size_t)c->g.main_sz;
-  c->paint = sv_dalloc(c, eb * ge * c->nslot);
+  if (f64) {
+    c->paint = sv_dalloc(c, eb * ge * c->nslot);
+  } else {  // the FP32 grids are painted by the tile kernels of a paint-only context on this stream
+    capow_options po = o;
+    po.stream = (void *)c->stream;
+    rc = create_paint_ctx(p, &po, 1, &c->pc);
+    if (rc) FAIL(c, rc, "paint context: %s", c->pc ? capow_last_error(c->pc) : "invalid parameters");
+    c->paint = c->pc->grid_base;
+  }
   c->work = sv_dalloc(c, eb * ge * c->nslot);
   c->F0 = sv_dalloc(c, eb * ge);
   c->st = (SvStats *)sv_dalloc(c, sizeof(SvStats));
@@ -757,6 +742,8 @@ extern "C" void capow_survey_destroy(capow_survey_ctx *c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->plan_ok) cufftDestroy(c->plan);
+  if (c->pc) capow_destroy(c->pc);
+  if (c->comb) cudaFree(c->comb);
   for (void *q : c->allocs) cudaFree(q);
   for (int a = 0; a < 2; a++)
     for (int k = 0; k < 6; k++)
@@ -826,20 +813,76 @@ static int sv_enqueue_catalogue(capow_survey_ctx *c, int cat, const capow_survey
   return CAPOW_OK;
 }
 
+// the device view of one catalogue after sv_enqueue_catalogue (staged copies for host input) and the
+// weights to paint (the FKP-weighted copy when FKP_Column < 0)
+template <typename T>
+static SvIn<T> sv_device_view(capow_survey_ctx *c, int cat, const capow_survey_catalogue *in, const T **wk) {
+  const void *src[5] = {in->x, in->y, in->z, in->w, in->nbar};
+  const void *d[5];
+  for (int k = 0; k < 5; k++) d[k] = in->on_device ? src[k] : c->stage[cat][k];
+  SvIn<T> sin{(const T *)d[0], (const T *)d[1], (const T *)d[2], (const T *)d[3], (const T *)d[4]};
+  *wk = c->sv.FKP_Column < 0 ? (const T *)c->stage[cat][5] : sin.w;
+  return sin;
+}
+
+// FP64: every object with global FP64 atomics (k_sv_paint), the reference's per-object double products.
 template <typename T, typename R>
 static void sv_launch_paint(capow_survey_ctx *c, int cat, const capow_survey_catalogue *in) {
   const size_t n = in->n;
   if (!n) return;
-  const void *d[5];
-  for (int k = 0; k < 5; k++) {
-    const void *src[5] = {in->x, in->y, in->z, in->w, in->nbar};
-    d[k] = in->on_device ? src[k] : c->stage[cat][k];
-  }
-  SvIn<T> sin{(const T *)d[0], (const T *)d[1], (const T *)d[2], (const T *)d[3], (const T *)d[4]};
-  const T *wk = c->sv.FKP_Column < 0 ? (const T *)c->stage[cat][5] : sin.w;
+  const T *wk;
+  SvIn<T> sin = sv_device_view<T>(c, cat, in, &wk);
   R *g0 = (R *)c->paint, *g1 = c->nslot > 1 ? (R *)c->paint + c->g.main_sz : nullptr;
   k_sv_paint<T, R><<<sv_blocks(n), 256, 0, c->stream>>>(c->g, sin, wk, (long long)n, cat, g0, g1, c->st);
   c->launches++;
+}
+
+// FP32: data and randoms combined into one float catalogue with the prefactors applied, painted by the
+// paint context's tile kernels (shared-memory tiles written once; objects near the grid's discontinuities,
+// the Survey clamp region included, take the exact FP64 rules). The paint settles on the host (one
+// synchronisation) so that a tile-list overflow repaints before the multipoles read the grids.
+template <typename T>
+static int sv_paint_tiles(capow_survey_ctx *c, const capow_survey_catalogue *data, const capow_survey_catalogue *rand) {
+  const size_t n = data->n + rand->n;
+  if (c->comb_cap < n) {
+    if (c->comb) cudaFree(c->comb);
+    c->comb = nullptr;
+    c->comb_cap = 0;
+    CK(c, cudaMalloc(&c->comb, sizeof(float) * 4 * (n ? n : 1)));
+    c->comb_cap = n;
+  }
+  float *cx = c->comb, *cy = cx + c->comb_cap, *cz = cy + c->comb_cap, *cw = cz + c->comb_cap;
+  const capow_survey_catalogue *cats[2] = {data, rand};
+  long long off = 0;
+  for (int cat = 0; cat < 2; cat++) {
+    const long long m = (long long)cats[cat]->n;
+    if (m) {
+      const T *wk;
+      SvIn<T> sin = sv_device_view<T>(c, cat, cats[cat], &wk);
+      k_sv_combine<T><<<sv_blocks(m), 256, 0, c->stream>>>(c->g, sin, wk, m, cat, off, cx, cy, cz, cw, c->st);
+      c->launches++;
+    }
+    off += m;
+  }
+  CK(c, cudaGetLastError());
+  capow_particles d;
+  memset(&d, 0, sizeof d);
+  d.n = n;
+  d.dtype = CAPOW_F32;
+  d.on_device = 1;
+  d.x = cx;
+  d.y = cy;
+  d.z = cz;
+  d.w = cw;
+  capow_ctx *pc = c->pc;
+  pc->last = d;
+  pc->painted = true;
+  const long long before = pc->launches;
+  int rc = enqueue_paint(pc, d);
+  if (!rc) rc = settle_paint(pc);
+  c->launches += pc->launches - before;
+  if (rc) FAIL(c, rc, "survey paint: %s", capow_last_error(pc));
+  return CAPOW_OK;
 }
 
 template <typename R>
@@ -861,7 +904,8 @@ static int sv_multipoles(capow_survey_ctx *c) {
   sa.g0 = (const C *)w0;
   sa.g1 = (const C *)w1;
   sa.F0 = (C *)c->F0;
-  sa.dc = (const double *)((const char *)c->st + offsetof(SvStats, dc));
+  sa.dc = c->pc ? (const double *)((const char *)c->pc->st + offsetof(DevStats, dc))
+               : (const double *)((const char *)c->st + offsetof(SvStats, dc));
   sa.origin = c->origin;
   sa.a0 = a0;
   sa.a1 = a1;
@@ -909,12 +953,17 @@ static int sv_run(capow_survey_ctx *c, const capow_survey_catalogue *data, const
   CK(c, cudaMemsetAsync(c->st, 0, sizeof(SvStats), c->stream));
   CK(c, cudaMemsetAsync(c->bins, 0, sizeof(double) * 5 * c->p.NK, c->stream));
   CK(c, cudaEventRecord(c->ev[0], c->stream));
-  CK(c, cudaMemsetAsync(c->paint, 0, sizeof(R) * (size_t)c->g.main_sz * c->nslot, c->stream));
   int rc = sv_enqueue_catalogue<T, R>(c, 0, data);
   if (!rc) rc = sv_enqueue_catalogue<T, R>(c, 1, rand);
   if (rc) return rc;
-  sv_launch_paint<T, R>(c, 0, data);
-  sv_launch_paint<T, R>(c, 1, rand);
+  if constexpr (sizeof(R) == 8) {
+    CK(c, cudaMemsetAsync(c->paint, 0, sizeof(R) * (size_t)c->g.main_sz * c->nslot, c->stream));
+    sv_launch_paint<T, R>(c, 0, data);
+    sv_launch_paint<T, R>(c, 1, rand);
+  } else {
+    rc = sv_paint_tiles<T>(c, data, rand);
+    if (rc) return rc;
+  }
   CK(c, cudaGetLastError());
   CK(c, cudaEventRecord(c->ev[1], c->stream));
   rc = sv_multipoles<R>(c);
