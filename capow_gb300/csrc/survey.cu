@@ -32,6 +32,7 @@
 
 #include <new>
 #include <vector>
+#include <type_traits>
 
 #include "ctx.cuh"
 
@@ -265,30 +266,49 @@ __global__ void __launch_bounds__(256) k_sv_combine(Geom g, SvIn<T> in, const T 
 // w[c] = a[c] h_lm(r^) for every cell c = (ix, iy, iz < NZ) of the painted grid(s), r^ the unit vector
 // from the observer to the cell corner (ix dx + XMIN - X_Origin, ...) (src/main.c:551-559 and the
 // other product loops). A corner at the observer (r2 == 0) gets r2 = 1, as in the reference, so its
-// harmonics vanish. l = 0 copies the grid (src/main.c:503-511). Threads run along z (coalesced);
-// `rows` rows of one block share it.
+// harmonics vanish. l = 0 copies the grid (src/main.c:503-511). One warp per (x, y) row, grid-stride
+// over rows; each lane moves z pairs (rows have an even length, so pairs are aligned vector loads).
+template <typename R>
+__device__ __forceinline__ R sv_cell_weight(int l, int m, R px, R py, R pxy, R pz) {
+  R r2 = pxy + pz * pz;
+  if (r2 == (R)0) r2 = (R)1;
+  const R inv = sv_rsqrt(r2);
+  return harm<R>(l, m, px * inv, py * inv, pz * inv);
+}
+
 template <typename R>
 __global__ void __launch_bounds__(256) k_sv_weight(const R *a0, const R *a1, R *w0, R *w1, const R *vx, const R *vy,
-                                                   const R *vz, int nx, int ny, int nz, long long row, int l, int m,
-                                                   int tpr) {
-  const int rows_per_block = blockDim.x / tpr;
-  const long long r = (long long)blockIdx.x * rows_per_block + threadIdx.x / tpr;
-  if (r >= (long long)nx * ny) return;
-  const int ix = (int)(r / ny), iy = (int)(r - (long long)ix * ny);
-  const R px = vx[ix], py = vy[iy];
-  const R pxy = px * px + py * py;
-  const long long base = r * row;
-  for (int iz = threadIdx.x % tpr; iz < nz; iz += tpr) {
-    R h = (R)1;
-    if (l > 0) {
-      const R pz = vz[iz];
-      R r2 = pxy + pz * pz;
-      if (r2 == (R)0) r2 = (R)1;
-      const R inv = sv_rsqrt(r2);
-      h = harm<R>(l, m, px * inv, py * inv, pz * inv);
+                                                   const R *vz, int nx, int ny, int nz, long long row, int l, int m) {
+  typedef typename std::conditional<sizeof(R) == 4, float2, double2>::type R2;
+  const int lane = threadIdx.x & 31;
+  const long long nrows = (long long)nx * ny;
+  const int npairs = (nz + 1) >> 1;
+  const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; r < nrows; r += wstride) {
+    const int ix = (int)(r / ny), iy = (int)(r - (long long)ix * ny);
+    const R px = vx[ix], py = vy[iy];
+    const R pxy = px * px + py * py;
+    const R2 *s0 = reinterpret_cast<const R2 *>(a0 + r * row);
+    const R2 *s1 = a1 ? reinterpret_cast<const R2 *>(a1 + r * row) : nullptr;
+    R2 *d0 = reinterpret_cast<R2 *>(w0 + r * row);
+    R2 *d1 = a1 ? reinterpret_cast<R2 *>(w1 + r * row) : nullptr;
+    for (int p = lane; p < npairs; p += 32) {
+      R h0 = (R)1, h1 = (R)1;
+      if (l > 0) {
+        h0 = sv_cell_weight<R>(l, m, px, py, pxy, vz[2 * p]);
+        h1 = 2 * p + 1 < nz ? sv_cell_weight<R>(l, m, px, py, pxy, vz[2 * p + 1]) : (R)0;
+      }
+      R2 v = s0[p];
+      v.x *= h0;
+      v.y *= h1;
+      d0[p] = v;
+      if (s1) {
+        R2 u = s1[p];
+        u.x *= h0;
+        u.y *= h1;
+        d1[p] = u;
+      }
     }
-    w0[base + iz] = a0[base + iz] * h;
-    if (a1) w1[base + iz] = a1[base + iz] * h;
   }
 }
 
@@ -893,10 +913,9 @@ static int sv_multipoles(capow_survey_ctx *c) {
   const long long ge = g.main_sz;
   R *a0 = (R *)c->paint, *a1 = c->nslot > 1 ? a0 + ge : nullptr;
   R *w0 = (R *)c->work, *w1 = c->nslot > 1 ? w0 + ge : nullptr;
-  int tpr = 1;
-  while (tpr < p.NZ && tpr < 256) tpr <<= 1;
-  const long long rows = (long long)p.NX * p.NY, rpb = 256 / tpr;
-  const unsigned wblocks = (unsigned)((rows + rpb - 1) / rpb);
+  const long long rows = (long long)p.NX * p.NY;
+  // one warp per row, 8 per CTA, grid-stride beyond 16 CTAs per SM
+  const unsigned wblocks = (unsigned)std::min<long long>((rows + 7) / 8, 152LL * 16);
   const long long cols = (long long)p.NY * c->bp.nzc;
   const dim3 agrid((unsigned)((cols + 255) / 256), (unsigned)((p.NX + SV_ICHUNK - 1) / SV_ICHUNK));
   SvAssign<R> sa;
@@ -918,7 +937,7 @@ static int sv_multipoles(capow_survey_ctx *c) {
   for (int l = 0; l <= 4; l += step) {
     for (int m = 0; m < 2 * l + 1; m++) {
       k_sv_weight<R><<<wblocks, 256, 0, c->stream>>>(a0, a1, w0, w1, (const R *)c->vx, (const R *)c->vy,
-                                                     (const R *)c->vz, p.NX, p.NY, p.NZ, g.row, l, m, tpr);
+                                                     (const R *)c->vz, p.NX, p.NY, p.NZ, g.row, l, m);
       c->launches++;
       if (c->plan_per_grid) {
         for (int s = 0; s < c->nslot; s++) {
