@@ -373,6 +373,81 @@ def scale_bench(args):
     print(json.dumps(line), flush=True)
 
 
+PARAM_TAGS = ("NumFilesInParallel NX NY NZ XMIN XMAX YMIN YMAX ZMIN ZMAX DoInterlacing InterpOrder NK NMU Output2D "
+              "OutputLog Mink Maxk Omega_m Redshift Periodic LOS Survey Momentum X_Origin Y_Origin Z_Origin REDMININ "
+              "REDMAXIN NOBJ_Max Coord_Type x_Column y_Column z_Column NBAR_Column SkyArea FKP_Column FKP_Pk "
+              "FKP_Pk_mom FKP_Pk_cross Odd_Multipoles").split()
+
+
+def write_params_file(path: str, params: dict) -> None:
+    """A run_parameters.dat with the 41 tags the reference's reader requires (src/read_params.c:65-227):
+    the given values, the periodic estimator, and neutral survey tags."""
+    v = {t: 0 for t in PARAM_TAGS}
+    v.update(NumFilesInParallel=1, Periodic=1, Survey=0, NOBJ_Max=1, x_Column=1, y_Column=2, z_Column=3,
+             NBAR_Column=4, SkyArea=1.0, FKP_Column=5, FKP_Pk=1.0, FKP_Pk_mom=1.0, FKP_Pk_cross=1.0, REDMAXIN=1.0)
+    v.update(params)
+    with open(path, "w") as f:
+        for t in PARAM_TAGS:
+            f.write(f"{t} {v[t]!r}\n" if isinstance(v[t], float) else f"{t} {v[t]}\n")
+
+
+def cli_bench(args):
+    """The drop-in driver end to end: `capow <params> <data> none <out>` as a user runs it, timed as whole
+    processes (CUDA context creation included) with the driver's own phase times (CAPOW_TIMING=1).
+    Two runs: the headline workload (16,777,216 Zel'dovich particles, TSC 512^3, dd+dp+pp through
+    CAPOW_SPECTRA) from a binary column catalogue (float32), and the plain run's workload (2,097,152
+    uniform particles, CIC 128^3, LOS = z) from a text catalogue written with %.9g. Median of
+    `--steps` runs each (at least 3). Prints one JSON line."""
+    import tempfile
+
+    import capow_gb300 as cg
+    from capow_gb300 import synth
+
+    reps = max(args.steps, 3)
+
+    def run(pf, df, env_extra):
+        env = dict(os.environ, CAPOW_TIMING="1", **env_extra)
+        walls, phases = [], []
+        with tempfile.TemporaryDirectory() as tmp:
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                r = subprocess.run([cg.DRIVER_PATH, pf, df, "none", os.path.join(tmp, "out.txt")],
+                                   capture_output=True, text=True, env=env, timeout=600)
+                walls.append(time.perf_counter() - t0)
+                if r.returncode != 0:
+                    raise RuntimeError(r.stdout[-2000:] + r.stderr[-2000:])
+                line = [s for s in r.stderr.splitlines() if s.startswith("capow timing")][-1]
+                toks = line.split(":", 1)[1].split()
+                phases.append({toks[i]: float(toks[i + 1]) for i in range(0, len(toks), 2)})
+        med = {k: round(statistics.median(p[k] for p in phases), 4) for k in phases[0]}
+        return {"wall_s": round(statistics.median(walls), 4), "phases_s": med}
+
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        x, y, z, vx, vy, vz = make_particles()
+        pf, df = os.path.join(tmp, "c1.dat"), os.path.join(tmp, "c1.bin")
+        write_params_file(pf, PARAMS)
+        cg.write_soa_catalogue(df, x, y, z, vx, vy, vz, dtype=np.float32)
+        out["c1_binary"] = run(pf, df, {"CAPOW_SPECTRA": "dd,dp,pp", "CAPOW_PRECISION": "fp32"})
+        out["c1_binary"]["catalogue_bytes"] = os.path.getsize(df)
+        rng = np.random.default_rng(1)
+        n0 = 2_097_152
+        pos = rng.uniform(0.0, 1000.0, size=(n0, 3))
+        vel = rng.normal(0.0, 300.0, size=(n0, 3))
+        p0 = dict(PARAMS, NX=128, NY=128, NZ=128, InterpOrder=2, NK=41, Maxk=0.41)
+        pf0, df0 = os.path.join(tmp, "c0.dat"), os.path.join(tmp, "c0.txt")
+        write_params_file(pf0, p0)
+        np.savetxt(df0, np.hstack([pos, vel]), fmt="%.9g")
+        out["c0_text"] = run(pf0, df0, {"CAPOW_PRECISION": "fp32"})
+        out["c0_text"]["catalogue_bytes"] = os.path.getsize(df0)
+    line = {"metric": "capow CLI wall time per run (process start to exit)", "unit": "s", "higher_is_better": False,
+            "value": out["c1_binary"]["wall_s"], "n_gpus": 1, "runs": reps, **out,
+            "data": "synthetic (seeded Zel'dovich lattice; uniform particles for the text run)",
+            "config": {"workload": f"{WORKLOAD}, binary float32 columns, CAPOW_SPECTRA=dd,dp,pp; and 2,097,152 "
+                                   "uniform particles, CIC 128^3, LOS=z, text catalogue (%.9g)"}}
+    print(json.dumps(line), flush=True)
+
+
 SURVEY_PARAMS = dict(NX=512, NY=512, NZ=512, XMIN=-1000.0, XMAX=1000.0, YMIN=-1000.0, YMAX=1000.0, ZMIN=-1000.0,
                      ZMAX=1000.0, InterpOrder=3, DoInterlacing=1, NK=100, NMU=1, Output2D=0, OutputLog=0, Mink=0.0,
                      Maxk=0.5, Omega_m=0.3089, Redshift=0.1, LOS=0, Momentum=0, Odd_Multipoles=0)
@@ -648,6 +723,7 @@ def main():
     ap.add_argument("--mocks", type=int, default=256)
     ap.add_argument("--scale", action="store_true", help="run the 1024^3 / 134M-particle workload instead")
     ap.add_argument("--survey", action="store_true", help="run the survey-estimator workload instead")
+    ap.add_argument("--cli", action="store_true", help="time the capow driver end to end instead")
     ap.add_argument("--profile-case", action="store_true",
                     help="run the 8x smaller workload for profiler captures (prints stage times only)")
     args = ap.parse_args()
@@ -663,6 +739,9 @@ def main():
         return
     if args.survey:
         survey_bench(args)
+        return
+    if args.cli:
+        cli_bench(args)
         return
     world, rank, local = dist_init()
     log = (lambda *a: print(*a, file=sys.stderr, flush=True))

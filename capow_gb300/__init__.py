@@ -126,7 +126,8 @@ EXPORTS = [
     "capow_last_error", "capow_paint_noalloc", "capow_backward", "capow_batch", "capow_tile_kernel_ms",
     "capow_batch_release", "capow_survey_create", "capow_survey_power", "capow_survey_copy_grid",
     "capow_survey_stage_ms", "capow_survey_kernel_launches", "capow_survey_last_error", "capow_survey_destroy",
-    "capow_read_survey_params", "capow_read_survey", "capow_survey_objects_free",
+    "capow_read_survey_params", "capow_read_survey", "capow_survey_objects_free", "capow_is_soa_catalogue",
+    "capow_read_catalogue_soa", "capow_free_host",
 ]
 
 _lib = None
@@ -193,6 +194,12 @@ def lib() -> ctypes.CDLL:
                                     ctypes.c_size_t]
     L.capow_survey_objects_free.argtypes = [ctypes.POINTER(_SurveyObjects)]
     L.capow_survey_objects_free.restype = None
+    L.capow_is_soa_catalogue.argtypes = [ctypes.c_char_p]
+    L.capow_read_catalogue_soa.argtypes = [ctypes.c_char_p, ip, ctypes.POINTER(ctypes.c_size_t),
+                                           ctypes.POINTER(ip)] + [ctypes.POINTER(vp)] * 4 + [ctypes.c_char_p,
+                                                                                             ctypes.c_size_t]
+    L.capow_free_host.argtypes = [vp]
+    L.capow_free_host.restype = None
     _lib = L
     return L
 
@@ -256,6 +263,44 @@ def read_catalogue(path: str, los: int):
         L.capow_free(ctypes.cast(p, ctypes.c_void_p))
         out.append(a)
     return tuple(out)
+
+
+SOA_MAGIC = b"CAPOWSOA"
+
+
+def write_soa_catalogue(path: str, x, y, z, vx, vy, vz, dtype=np.float32) -> None:
+    """Write a binary catalogue (include/capow.h: "CAPOWSOA", version 1, dtype, n, 6 columns, then the
+    columns x, y, z, vx, vy, vz), which the `capow` driver reads in place of a text catalogue."""
+    dt = np.dtype(dtype)
+    if dt not in (np.float32, np.float64):
+        raise ValueError("dtype must be float32 or float64")
+    cols = [np.ascontiguousarray(c, dtype=dt) for c in (x, y, z, vx, vy, vz)]
+    n = len(cols[0])
+    if any(len(c) != n for c in cols):
+        raise ValueError("columns differ in length")
+    header = SOA_MAGIC + np.array([1, 1 if dt == np.float64 else 0], "<u4").tobytes() + \
+        np.array([n], "<u8").tobytes() + np.array([6, 0], "<u4").tobytes()
+    with open(path, "wb") as f:
+        f.write(header)
+        for c in cols:
+            f.write(c.astype(dt.newbyteorder("<"), copy=False).tobytes())
+
+
+def read_catalogue_soa(path: str, los: int):
+    """capow_read_catalogue_soa: returns (x, y, z, vlos) arrays of the file's dtype."""
+    L = lib()
+    n, dt = ctypes.c_size_t(), ctypes.c_int()
+    ptrs = [ctypes.c_void_p() for _ in range(4)]
+    msg = ctypes.create_string_buffer(4096)
+    rc = L.capow_read_catalogue_soa(path.encode(), los, ctypes.byref(n), ctypes.byref(dt),
+                                    *[ctypes.byref(p) for p in ptrs], msg, len(msg))
+    if rc != OK:
+        raise CapowError(rc, msg.value.decode())
+    ct = ctypes.c_double if dt.value == F64 else ctypes.c_float
+    out = tuple(np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ct)), shape=(n.value,)).copy()
+                if n.value else np.zeros(0, dtype=np.float64 if dt.value == F64 else np.float32) for p in ptrs)
+    L.capow_free_host(ptrs[0])
+    return out
 
 
 def _ptr_of(a):

@@ -38,6 +38,11 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libcapow_gpu")
 
 
+def _cuda_include(nvcc: str) -> str:
+    """The toolkit's include directory (the host C sources call the CUDA runtime for pinned memory)."""
+    return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "include")
+
+
 def _newer(target: str, deps) -> bool:
     if not os.path.exists(target):
         return True
@@ -68,7 +73,7 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
         objs.append(o)
         if force or _newer(o, [s] + hdrs):
             jobs.append(["gcc", "-O2", "-std=gnu99", "-fPIC", "-ffp-contract=off", "-Wall", "-pthread", "-I",
-                         os.path.join(ROOT, "include"), "-c", s, "-o", o])
+                         os.path.join(ROOT, "include"), "-I", _cuda_include(nvcc), "-c", s, "-o", o])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -276,3 +276,88 @@ int capow_read_catalogue(const char *path, int los, size_t *n_out, double **x, d
 }
 
 void capow_free(void *p) { free(p); }
+
+/* ------------------------------------------------------------------ binary SoA catalogues */
+/* A catalogue the reference has no reader for: the six columns x y z vx vy vz as little-endian
+ * arrays after a 32-byte header (magic "CAPOWSOA", version 1, dtype 0 float32 / 1 float64, n, 6
+ * columns). The columns the paint needs (x, y, z and the one LOS selects) are read into one host
+ * allocation, page-locked with cudaHostRegister where a device is present, so the paint's
+ * host-to-device copies run at the link's full rate. */
+#include <cuda_runtime_api.h>
+
+typedef struct {
+  char magic[8];
+  uint32_t version, dtype;
+  uint64_t n;
+  uint32_t ncols, reserved;
+} soa_header;
+
+void capow_free_host(void *p);
+
+int capow_is_soa_catalogue(const char *path) {
+  FILE *f = fopen(path, "rb");
+  if (!f) return 0;
+  char m[8];
+  const int ok = fread(m, 1, 8, f) == 8 && memcmp(m, "CAPOWSOA", 8) == 0;
+  fclose(f);
+  return ok;
+}
+
+int capow_read_catalogue_soa(const char *path, int los, size_t *n_out, int *dtype, void **x, void **y, void **z,
+                             void **vlos, char *msg, size_t msglen) {
+  if (msg && msglen) msg[0] = 0;
+  *n_out = 0;
+  *x = *y = *z = *vlos = NULL;
+  FILE *f = fopen(path, "rb");
+  if (!f) {
+    if (msg) snprintf(msg, msglen, "Task 0 cannot open input file\nFatal Error at line 96 in routine read_data\n");
+    return CAPOW_EINVAL;
+  }
+  soa_header h;
+  if (fread(&h, sizeof h, 1, f) != 1 || memcmp(h.magic, "CAPOWSOA", 8) != 0 || h.version != 1 || h.dtype > 1 ||
+      h.ncols != 6) {
+    fclose(f);
+    if (msg) snprintf(msg, msglen, "%s: not a version-1 CAPOWSOA catalogue with 6 columns\n", path);
+    return CAPOW_EINVAL;
+  }
+  const size_t eb = h.dtype ? 8 : 4, col = (size_t)h.n * eb;
+  fseek(f, 0, SEEK_END);
+  const long sz = ftell(f);
+  if (sz < 0 || (unsigned long long)sz < sizeof h + 6ULL * col) {
+    fclose(f);
+    if (msg) snprintf(msg, msglen, "%s: truncated (%llu particles declared)\n", path, (unsigned long long)h.n);
+    return CAPOW_EINVAL;
+  }
+  char *base = NULL;
+  const size_t bytes = 4 * (col ? col : 1);
+  if (posix_memalign((void **)&base, 4096, bytes) != 0) {
+    fclose(f);
+    return CAPOW_ENOMEM;
+  }
+  if (cudaHostRegister(base, bytes, cudaHostRegisterDefault) != cudaSuccess) (void)cudaGetLastError(); /* pageable */
+  const int vcol = los == 1 ? 3 : (los == 2 ? 4 : 5); /* src/read_data.c:65-76 */
+  const int cols[4] = {0, 1, 2, vcol};
+  for (int k = 0; k < 4; k++) {
+    if (fseek(f, (long)(sizeof h + (size_t)cols[k] * col), SEEK_SET) != 0 ||
+        (col && fread(base + (size_t)k * col, 1, col, f) != col)) {
+      fclose(f);
+      capow_free_host(base);
+      if (msg) snprintf(msg, msglen, "%s: read error\n", path);
+      return CAPOW_EINVAL;
+    }
+  }
+  fclose(f);
+  *n_out = (size_t)h.n;
+  *dtype = h.dtype ? CAPOW_F64 : CAPOW_F32;
+  *x = base;
+  *y = base + col;
+  *z = base + 2 * col;
+  *vlos = base + 3 * col;
+  return CAPOW_OK;
+}
+
+void capow_free_host(void *p) {
+  if (!p) return;
+  if (cudaHostUnregister(p) != cudaSuccess) (void)cudaGetLastError();
+  free(p);
+}

@@ -11,11 +11,14 @@
  *   CAPOW_SPECTRA   = e.g. "dd,dp,pp": one paint and one set of FFTs for several spectra;
  *                     each is written to <OutputFile>.<name>
  *   CAPOW_DEVICE    = CUDA device ordinal
- * Any failure prints the reference's message and exits with status 1 (FatalError,
+ *   CAPOW_TIMING    = 1: wall-clock phases of a periodic run on stderr
+ * A periodic DataFile that starts with "CAPOWSOA" is read as binary columns (capow_read_catalogue_soa)
+ * instead of text. Any failure prints the reference's message and exits with status 1 (FatalError,
  * src/main.c:1298-1303). */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include "capow.h"
 
@@ -25,6 +28,29 @@ static void banner(const char *t) {
   for (size_t i = 0; i < n; i++) putchar('=');
   printf("\n");
   fflush(stdout);
+}
+
+/* CAPOW_TIMING=1: wall-clock phases of a periodic run on stderr (stdout stays the reference's) */
+enum { T_START, T_CREATE, T_READ, T_POWER, T_END, T_N };
+static double g_t[T_N];
+
+static void stamp(int k) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  g_t[k] = ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+static void report_times(void) {
+  const char *e = getenv("CAPOW_TIMING");
+  if (!e || e[0] != '1') return;
+  fprintf(stderr,
+          "capow timing (s): params+create %.4f read %.4f paint+power %.4f output+cleanup %.4f total %.4f\n",
+          g_t[T_CREATE] - g_t[T_START], g_t[T_READ] - g_t[T_CREATE], g_t[T_POWER] - g_t[T_READ],
+          g_t[T_END] - g_t[T_POWER], g_t[T_END] - g_t[T_START]);
+}
+
+static double value_at(const void *a, int dtype, int64_t i) {
+  return dtype == CAPOW_F64 ? ((const double *)a)[i] : (double)((const float *)a)[i];
 }
 
 static void die(const char *msg) {
@@ -188,6 +214,7 @@ static int run_survey(const capow_params *p, const capow_survey_params *sv, cons
 }
 
 int main(int argc, char **argv) {
+  stamp(T_START);
   if (argc < 5) { /* src/main.c:39-47 */
     printf("Input parameters not found\n");
     printf("Call with <ParameterFile, DataFile, RandomFile, OutputFile>\n");
@@ -231,18 +258,28 @@ int main(int argc, char **argv) {
   rc = capow_create(&p, &opt, &ctx);
   if (rc != CAPOW_OK) die_status(ctx, rc, "capow_create");
   printf("Creating redshift-distance lookup table...\n");
+  stamp(T_CREATE);
 
   banner("Reading input data and assigning to grid");
   printf("\nReading: %s\n", datafile);
   fflush(stdout);
   size_t n = 0;
-  double *x, *y, *z, *v;
-  rc = capow_read_catalogue(datafile, p.LOS, &n, &x, &y, &z, &v, msg, sizeof msg);
+  void *x = NULL, *y = NULL, *z = NULL, *v = NULL;
+  int dtype = CAPOW_F64;
+  const int soa = capow_is_soa_catalogue(datafile); /* binary columns instead of text */
+  if (soa) {
+    rc = capow_read_catalogue_soa(datafile, p.LOS, &n, &dtype, &x, &y, &z, &v, msg, sizeof msg);
+  } else {
+    double *ax = NULL, *ay = NULL, *az = NULL, *av = NULL;
+    rc = capow_read_catalogue(datafile, p.LOS, &n, &ax, &ay, &az, &av, msg, sizeof msg);
+    x = ax; y = ay; z = az; v = av;
+  }
   if (rc != CAPOW_OK) die(msg);
+  stamp(T_READ);
   capow_particles parts;
   memset(&parts, 0, sizeof parts);
   parts.n = n;
-  parts.dtype = CAPOW_F64;
+  parts.dtype = dtype;
   parts.on_device = 0;
   parts.x = x; parts.y = y; parts.z = z; parts.vlos = v; parts.w = NULL;
   rc = capow_paint(ctx, &parts);
@@ -251,7 +288,8 @@ int main(int argc, char **argv) {
   rc = capow_get_stats(ctx, &st);
   if (rc == CAPOW_EBOUNDS && st.first_out_of_box >= 0) { /* src/read_data.c:81-84 */
     const int64_t i = st.first_out_of_box;
-    printf("Task 0 has particle out of grid bounds: x=%lf, y=%lf, z=%lf\n", x[i], y[i], z[i]);
+    printf("Task 0 has particle out of grid bounds: x=%lf, y=%lf, z=%lf\n", value_at(x, dtype, i),
+           value_at(y, dtype, i), value_at(z, dtype, i));
     printf("Fatal Error at line 110 in routine read_data\n");
     fflush(stdout);
     exit(1);
@@ -299,6 +337,7 @@ int main(int argc, char **argv) {
   banner("Iterating over grid cells");
   rc = capow_power(ctx, spec, ns);
   if (rc != CAPOW_OK) die_status(ctx, rc, "capow_power");
+  stamp(T_POWER);
 
   banner("Outputting power spectra"); /* src/main.c:1004-1101 */
   for (int q = 0; q < ns; q++) {
@@ -311,8 +350,14 @@ int main(int argc, char **argv) {
   }
   banner("Cleaning up");
   capow_destroy(ctx);
-  capow_free(x); capow_free(y); capow_free(z); capow_free(v);
+  if (soa) {
+    capow_free_host(x);
+  } else {
+    capow_free(x); capow_free(y); capow_free(z); capow_free(v);
+  }
   free(store);
   free(mstore);
+  stamp(T_END);
+  report_times();
   return 0;
 }

@@ -1,5 +1,5 @@
 /* capow.h -- C ABI of libcapow_gpu, the GB300 (sm_103a) implementation of CAPOW's
- * periodic-box power-spectrum path.
+ * periodic-box power-spectrum path, and of its survey estimator (capow_survey_*, below).
  *
  * The reference has no plugin interface: its periodic path is a chain of C functions
  * sharing globals (src/proto.h:25-46, src/vars.h). Each entry point below replaces one
@@ -50,8 +50,7 @@ extern "C" {
 
 /* ---------------------------------------------------------------- parameters */
 /* The run_parameters.dat tags that drive the periodic path (read_params.c:65-227), with the
- * reference's names and meanings. Survey-only tags are accepted by the driver's parser for
- * file compatibility and ignored here. */
+ * reference's names and meanings. The survey tags are in capow_survey_params (below). */
 typedef struct capow_params {
   int NX, NY, NZ;                           /* grid cells per axis (vars.h:79-81) */
   double XMIN, XMAX, YMIN, YMAX, ZMIN, ZMAX; /* box (vars.h:83-85) */
@@ -361,6 +360,18 @@ int capow_read_params(const char *path, capow_params *out, char *msg, size_t msg
 int capow_read_catalogue(const char *path, int los, size_t *n, double **x, double **y, double **z, double **vlos,
                          char *msg, size_t msglen);
 void capow_free(void *p);
+
+/* Binary catalogues (no reference counterpart; the reference reads ASCII only). A file that starts
+ * with the 8 bytes "CAPOWSOA" holds a 32-byte little-endian header -- magic, uint32 version (1),
+ * uint32 dtype (0 float32, 1 float64), uint64 n, uint32 ncols (6), uint32 reserved -- then the six
+ * columns x, y, z, vx, vy, vz, each n values. capow_read_catalogue_soa reads x, y, z and the column
+ * LOS selects into one host allocation, page-locked where a device is present (x is its base: free
+ * with capow_free_host), and reports
+ * their dtype (CAPOW_F32 / CAPOW_F64). The driver reads such a DataFile instead of parsing text. */
+int capow_is_soa_catalogue(const char *path);
+int capow_read_catalogue_soa(const char *path, int los, size_t *n, int *dtype, void **x, void **y, void **z,
+                             void **vlos, char *msg, size_t msglen);
+void capow_free_host(void *p);
 
 /* read_parameterfile + check_inputs for either estimator: as capow_read_params, but a survey run
  * (Periodic 0) is accepted and the survey tags are returned in sv (Periodic and Survey included). */

@@ -254,3 +254,27 @@ def test_driver_param_errors_print_reference_stdout(tmp_path, case):
                        text=True)
     assert r.returncode == 1
     assert r.stdout == e["stdout"].replace("{PARAMFILE}", str(pf))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("los", [0, 1, 2, 3])
+def test_soa_catalogue_round_trip(tmp_path, dtype, los):
+    """The binary column catalogue the driver reads instead of text: x, y, z and the LOS column, bit for
+    bit, in the file's dtype; a text file is not taken for one; a truncated file is an error."""
+    rng = np.random.default_rng(los)
+    cols = [rng.uniform(0, 1000, 1001).astype(dtype) for _ in range(6)]
+    f = str(tmp_path / "c.bin")
+    cg.write_soa_catalogue(f, *cols, dtype=dtype)
+    assert cg.lib().capow_is_soa_catalogue(f.encode()) == 1
+    x, y, z, v = cg.read_catalogue_soa(f, los)
+    assert x.dtype == dtype
+    for a, b in zip((x, y, z, v), cols[:3] + [cols[3 if los == 1 else (4 if los == 2 else 5)]]):
+        assert np.array_equal(a, b)
+    t = tmp_path / "c.txt"
+    t.write_text("1 2 3 4 5 6\n")
+    assert cg.lib().capow_is_soa_catalogue(str(t).encode()) == 0
+    raw = open(f, "rb").read()
+    open(f, "wb").write(raw[:-8])
+    with pytest.raises(cg.CapowError) as e:
+        cg.read_catalogue_soa(f, los)
+    assert "truncated" in str(e.value)
