@@ -127,7 +127,7 @@ EXPORTS = [
     "capow_batch_release", "capow_survey_create", "capow_survey_power", "capow_survey_copy_grid",
     "capow_survey_stage_ms", "capow_survey_kernel_launches", "capow_survey_last_error", "capow_survey_destroy",
     "capow_read_survey_params", "capow_read_survey", "capow_survey_objects_free", "capow_is_soa_catalogue",
-    "capow_read_catalogue_soa", "capow_free_host",
+    "capow_read_catalogue_soa", "capow_free_host", "capow_survey_nbar",
 ]
 
 _lib = None
@@ -200,6 +200,8 @@ def lib() -> ctypes.CDLL:
                                                                                              ctypes.c_size_t]
     L.capow_free_host.argtypes = [vp]
     L.capow_free_host.restype = None
+    L.capow_survey_nbar.argtypes = [P, SP, ctypes.POINTER(_SurveyObjects), ctypes.POINTER(_SurveyObjects),
+                                    ctypes.POINTER(ctypes.c_void_p), ctypes.c_char_p, ctypes.c_size_t]
     _lib = L
     return L
 
@@ -617,25 +619,65 @@ def read_survey_params(path: str):
     return Params.from_c(c), SurveyParams.from_c(s)
 
 
-def read_survey(path: str, params: Params, survey: SurveyParams, randoms: bool) -> dict:
-    """capow_read_survey: the objects read_survey_serial_ascii keeps (float32 arrays) and its counters."""
+def _read_survey_objects(path: str, params: Params, survey: SurveyParams, randoms: bool) -> _SurveyObjects:
     L = lib()
     o = _SurveyObjects()
     msg = ctypes.create_string_buffer(8192)
     pc, sc = params.to_c(), survey.to_c()
     rc = L.capow_read_survey(path.encode(), ctypes.byref(pc), ctypes.byref(sc), int(randoms), ctypes.byref(o), msg,
                              len(msg))
-    log = ctypes.string_at(o.log).decode() if o.log else ""
     if rc != OK:
+        log = ctypes.string_at(o.log).decode() if o.log else ""
         L.capow_survey_objects_free(ctypes.byref(o))
         err = CapowError(rc, msg.value.decode())
         err.log = log
         raise err
+    return o
+
+
+def _survey_objects_dict(o: _SurveyObjects) -> dict:
     out = {k: (np.ctypeslib.as_array(getattr(o, k), shape=(o.n,)).copy() if o.n else np.zeros(0, np.float32))
            for k in ("x", "y", "z", "w", "nbar", "redshift")}
-    out.update(n=o.n, nread=o.nread, lo=list(o.lo), hi=list(o.hi), redmin=o.redmin, redmax=o.redmax, log=log)
-    L.capow_survey_objects_free(ctypes.byref(o))
+    out.update(n=o.n, nread=o.nread, lo=list(o.lo), hi=list(o.hi), redmin=o.redmin, redmax=o.redmax,
+               log=ctypes.string_at(o.log).decode() if o.log else "")
     return out
+
+
+def read_survey(path: str, params: Params, survey: SurveyParams, randoms: bool) -> dict:
+    """capow_read_survey: the objects read_survey_serial_ascii keeps (float32 arrays) and its counters."""
+    o = _read_survey_objects(path, params, survey, randoms)
+    out = _survey_objects_dict(o)
+    lib().capow_survey_objects_free(ctypes.byref(o))
+    return out
+
+
+def read_survey_pair(data_path: str, rand_path: str, params: Params, survey: SurveyParams):
+    """Both catalogues of a survey run as the reference's main reads them: capow_read_survey twice and,
+    for NBAR_Column < 0, capow_survey_nbar (compute_nbar). Returns (data, randoms, printed nbar lines)."""
+    L = lib()
+    d = _read_survey_objects(data_path, params, survey, False)
+    try:
+        r = _read_survey_objects(rand_path, params, survey, True)
+    except CapowError:
+        L.capow_survey_objects_free(ctypes.byref(d))
+        raise
+    nlog = ""
+    try:
+        if survey.NBAR_Column < 0:
+            pc, sc = params.to_c(), survey.to_c()
+            logp = ctypes.c_void_p()
+            msg = ctypes.create_string_buffer(4096)
+            rc = L.capow_survey_nbar(ctypes.byref(pc), ctypes.byref(sc), ctypes.byref(d), ctypes.byref(r),
+                                     ctypes.byref(logp), msg, len(msg))
+            if logp.value:
+                nlog = ctypes.string_at(logp.value).decode()
+                L.capow_free(logp)
+            if rc != OK:
+                raise CapowError(rc, msg.value.decode())
+        return _survey_objects_dict(d), _survey_objects_dict(r), nlog
+    finally:
+        L.capow_survey_objects_free(ctypes.byref(d))
+        L.capow_survey_objects_free(ctypes.byref(r))
 
 
 def _survey_cat(cat):

@@ -220,10 +220,6 @@ int capow_read_survey(const char *path, const capow_params *p, const capow_surve
   if (msg && msglen) msg[0] = 0;
   if (!path || !p || !sv || !out) return CAPOW_EINVAL;
   memset(out, 0, sizeof *out);
-  if (sv->NBAR_Column < 0) {
-    if (msg) snprintf(msg, msglen, "NBAR_Column < 0 (number density from the randoms) is not provided\n");
-    return CAPOW_ENOTSUP;
-  }
   FILE *f = fopen(path, "rb");
   if (!f) { /* src/read_data.c:213 */
     if (msg) snprintf(msg, msglen, "Task 0 cannot open input file\nFatal Error at line 113 in routine read_data\n");
@@ -407,4 +403,94 @@ int capow_read_survey(const char *path, const capow_params *p, const capow_surve
     return CAPOW_ENOMEM;
   }
   return CAPOW_OK;
+}
+
+/* compute_nbar (src/read_data.c:385-446), one rank. The number density per redshift bin of width
+ * (REDMAX - REDMIN) / nbins, nbins = ceil((REDMAXIN - REDMININ) / 0.002), REDMIN and REDMAX the range of
+ * the kept objects of both catalogues; counts over the volume of the bin's shell of sky area SkyArea
+ * (square degrees); a natural cubic spline through the bin centres, with the raw end values at half a
+ * bin beyond each end; every object's nbar from that spline, stored in its float field. As in the
+ * reference, the counts loop runs over the data's indices but reads the randoms' redshifts (:401-405);
+ * with more data than randoms the reference reads objects it never filled, which is an error here. */
+int capow_survey_nbar(const capow_params *p, const capow_survey_params *sv, capow_survey_objects *data,
+                      capow_survey_objects *rand, char **log_out, char *msg, size_t msglen) {
+  if (msg && msglen) msg[0] = 0;
+  if (log_out) *log_out = NULL;
+  if (!p || !sv || !data || !rand) return CAPOW_EINVAL;
+  const int nbins = (int)(ceil((sv->REDMAXIN - sv->REDMININ) / 0.002));
+  if (nbins < 1) {
+    if (msg) snprintf(msg, msglen, "compute_nbar needs REDMAXIN > REDMININ\n");
+    return CAPOW_EINVAL;
+  }
+  if (data->n > rand->n) {
+    if (msg)
+      snprintf(msg, msglen, "compute_nbar reads the redshifts of the first %zu randoms, but only %zu were kept\n",
+               data->n, rand->n);
+    return CAPOW_EINVAL;
+  }
+  const double redmin = data->redmin < rand->redmin ? data->redmin : rand->redmin;
+  const double redmax = data->redmax > rand->redmax ? data->redmax : rand->redmax;
+  const double rbw = (redmax - redmin) / (float)nbins;
+  double *znbar = (double *)calloc((size_t)nbins + 2, sizeof(double));
+  double *nbar = (double *)calloc((size_t)nbins + 2, sizeof(double));
+  redshift_table tab;
+  memset(&tab, 0, sizeof tab);
+  nspline sp;
+  memset(&sp, 0, sizeof sp);
+  textbuf log = {0};
+  int rc = CAPOW_OK;
+  if (!znbar || !nbar || table_build(&tab, p->Omega_m)) {
+    rc = CAPOW_ENOMEM;
+    goto done;
+  }
+  tb_add(&log, "Calculating Number Density...\n");
+  for (size_t i = 0; i < data->n; i++) {
+    int nb = (int)(floor(((double)rand->redshift[i] - redmin) / rbw)) + 1;
+    if (nb == nbins + 1) nb--;
+    if (nb < 0 || nb > nbins + 1) {
+      if (msg) snprintf(msg, msglen, "compute_nbar: redshift %g outside [%g, %g]\n", (double)rand->redshift[i], redmin,
+                        redmax);
+      rc = CAPOW_EINVAL;
+      goto done;
+    }
+    nbar[nb]++;
+  }
+  for (int i = 0; i < nbins; i++) {
+    double outer, inner;
+    if (nspline_eval(&tab.r_of_z, (i + 1) * rbw + redmin, &outer) || nspline_eval(&tab.r_of_z, i * rbw + redmin, &inner)) {
+      if (msg) snprintf(msg, msglen, "interpolation error: redshift outside the redshift-distance table\n");
+      rc = CAPOW_EINVAL;
+      goto done;
+    }
+    const double volume =
+        sv->SkyArea / (180.0 * 180.0) * M_PI * M_PI * (outer * outer * outer - inner * inner * inner) / 3.0;
+    znbar[i + 1] = (i + 0.5) * rbw + redmin;
+    nbar[i + 1] /= volume;
+    tb_add(&log, "%12.6lf, %12.6lf\n", znbar[i + 1], nbar[i + 1]);
+  }
+  znbar[0] = redmin - 0.5 * rbw;
+  znbar[nbins + 1] = redmax + 0.5 * rbw;
+  if (nspline_init(&sp, znbar, nbar, nbins + 2)) {
+    rc = CAPOW_ENOMEM;
+    goto done;
+  }
+  capow_survey_objects *cats[2] = {data, rand};
+  for (int c = 0; c < 2; c++)
+    for (size_t i = 0; i < cats[c]->n; i++) {
+      double v;
+      if (nspline_eval(&sp, (double)cats[c]->redshift[i], &v)) {
+        if (msg) snprintf(msg, msglen, "interpolation error: redshift outside the number-density table\n");
+        rc = CAPOW_EINVAL;
+        goto done;
+      }
+      cats[c]->nbar[i] = (float)v;
+    }
+done:
+  free(znbar);
+  free(nbar);
+  table_free(&tab);
+  nspline_free(&sp);
+  if (log_out) *log_out = log.s;
+  else free(log.s);
+  return rc;
 }

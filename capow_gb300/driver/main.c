@@ -134,6 +134,14 @@ static int run_survey(const capow_params *p, const capow_survey_params *sv, cons
   capow_survey_objects data, rand;
   read_one(p, sv, datafile, 0, &data);
   read_one(p, sv, randfile, 1, &rand);
+  if (sv->NBAR_Column < 0) { /* compute_nbar, src/main.c:88 */
+    char *nlog = NULL;
+    char msg[1024];
+    rc = capow_survey_nbar(p, sv, &data, &rand, &nlog, msg, sizeof msg);
+    if (nlog) printf("%s", nlog);
+    capow_free(nlog);
+    if (rc != CAPOW_OK) die(msg);
+  }
   if (sv->FKP_Column < 0) printf("Computing FKP Weights...\n");
   fflush(stdout);
 

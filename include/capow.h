@@ -289,7 +289,7 @@ typedef struct capow_survey_params {
   double REDMININ, REDMAXIN;            /* redshift cut of the reader */
   long long NOBJ_Max;                   /* capacity of the reference's object arrays */
   int NBAR_Column;                      /* > 0: number density from the catalogue (its 5th number);
-                                           < 0: the reference's compute_nbar (not provided: ENOTSUP) */
+                                           < 0: the reference's compute_nbar (capow_survey_nbar) */
   double SkyArea;
   int FKP_Column;                       /* < 0: FKP weights w *= 1/(1 + nbar FKP_Pk) (main.c:89-94) */
   double FKP_Pk, FKP_Pk_mom, FKP_Pk_cross;
@@ -400,6 +400,16 @@ typedef struct capow_survey_objects {
 int capow_read_survey(const char *path, const capow_params *p, const capow_survey_params *sv, int randoms,
                       capow_survey_objects *out, char *msg, size_t msglen);
 void capow_survey_objects_free(capow_survey_objects *o);
+
+/* compute_nbar (read_data.c:385-446) for NBAR_Column < 0, after both catalogues are read (their nbar
+ * fields are overwritten): counts per redshift bin (ceil((REDMAXIN - REDMININ) / 0.002) bins over the
+ * kept objects' redshift range) over the volume of the bin's shell of SkyArea square degrees, a natural
+ * cubic spline through the bin centres, and every object's nbar from it. As in the reference the counts
+ * come from the redshifts of the first NDATA randoms (:401-405); more data than randoms is CAPOW_EINVAL
+ * (the reference reads objects it never filled). *log receives the reference's printed lines (malloc'd,
+ * free with capow_free). */
+int capow_survey_nbar(const capow_params *p, const capow_survey_params *sv, capow_survey_objects *data,
+                      capow_survey_objects *rand, char **log, char *msg, size_t msglen);
 
 /* output_power's file format (main.c:1058-1101), plus `<path>_2D` when Output2D. */
 int capow_write_output(const char *path, const capow_params *p, const capow_spectrum *s);

@@ -442,6 +442,10 @@ def _survey_lib():
         L.orc_survey_power.argtypes = [P, ctypes.POINTER(OrcSurvey), dp, dp, dp, dp, dp, dp, dp, ip]
         L.orc_survey_redshift.restype = ctypes.c_double
         L.orc_survey_redshift.argtypes = [ctypes.c_double, ctypes.c_double]
+        L.orc_survey_distance.restype = ctypes.c_double
+        L.orc_survey_distance.argtypes = [ctypes.c_double, ctypes.c_double]
+        L.orc_cspline_eval.restype = ctypes.c_double
+        L.orc_cspline_eval.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double]
         L._survey_bound = True
     return L
 
@@ -486,9 +490,44 @@ def survey_read(p: Params, path: str, randoms: bool) -> dict:
     k = np.array(keep, dtype=np.int64)
     f32 = np.float32
     out = {"x": a[k, 0].astype(f32), "y": a[k, 1].astype(f32), "z": a[k, 2].astype(f32),
-           "weight": a[k, 3].astype(f32), "redshift": np.array(red).astype(f32), "nread": a.shape[0]}
+           "weight": a[k, 3].astype(f32), "redshift": np.array(red).astype(f32), "nread": a.shape[0],
+           "redmin": min(red, default=1.0e30), "redmax": max(red, default=-1.0e30)}  # REDMIN/REDMAX, :327-328
     out["nbar"] = a[k, 4].astype(f32) if p.NBAR_Column > 0 else np.zeros(len(k), f32)
     return out
+
+
+def survey_nbar(p: Params, data: dict, rand: dict) -> list:
+    """compute_nbar (src/read_data.c:385-446, one rank) in place on both catalogues' float nbar: counts of
+    the first NDATA randoms' redshifts (the reference indexes the randoms with the data's count, :401-405)
+    in ceil((REDMAXIN - REDMININ) / 0.002) bins over [REDMIN, REDMAX] of both catalogues, over each bin's
+    shell volume (SkyArea square degrees, distances from the table's r(z) spline), then a natural cubic
+    spline through the bin centres with the raw end values half a bin outside. Returns the printed lines."""
+    L = _survey_lib()
+    nbins = int(np.ceil((p.REDMAXIN - p.REDMININ) / 0.002))
+    redmin = min(data["redmin"], rand["redmin"])
+    redmax = max(data["redmax"], rand["redmax"])
+    rbw = (redmax - redmin) / float(np.float32(nbins))
+    znbar = np.zeros(nbins + 2)
+    nbar = np.zeros(nbins + 2)
+    lines = ["Calculating Number Density..."]
+    for i in range(len(data["x"])):
+        nb = int(np.floor((float(rand["redshift"][i]) - redmin) / rbw)) + 1
+        if nb == nbins + 1:
+            nb -= 1
+        nbar[nb] += 1.0
+    for i in range(nbins):
+        outer = L.orc_survey_distance(p.Omega_m, (i + 1) * rbw + redmin)
+        inner = L.orc_survey_distance(p.Omega_m, i * rbw + redmin)
+        volume = p.SkyArea / (180.0 * 180.0) * np.pi * np.pi * (outer * outer * outer - inner * inner * inner) / 3.0
+        znbar[i + 1] = (i + 0.5) * rbw + redmin
+        nbar[i + 1] /= volume
+        lines.append("%12.6f, %12.6f" % (znbar[i + 1], nbar[i + 1]))
+    znbar[0] = redmin - 0.5 * rbw
+    znbar[nbins + 1] = redmax + 0.5 * rbw
+    for c in (data, rand):
+        c["nbar"] = np.array([L.orc_cspline_eval(nbins + 2, _dp(znbar), _dp(nbar), float(z)) for z in c["redshift"]],
+                             dtype=np.float64).astype(np.float32)
+    return lines
 
 
 def survey_fkp(p: Params, cat: dict) -> None:
@@ -505,6 +544,7 @@ def survey_run(p: Params, data_path: str, rand_path: str, grids: bool = False) -
     L = _survey_lib()
     data = survey_read(p, data_path, False)
     rand = survey_read(p, rand_path, True)
+    nbar_lines = survey_nbar(p, data, rand) if p.NBAR_Column < 0 else []
     if p.FKP_Column < 0:
         survey_fkp(p, data)
         survey_fkp(p, rand)
@@ -540,4 +580,4 @@ def survey_run(p: Params, data_path: str, rand_path: str, grids: bool = False) -
             "ndata": len(wd), "nrand": len(wr), "ngrid_data": ngrid_d, "ngrid_rand": ngrid_r / -alpha,
             "sums": {"data_nbw": data_nbw, "data_nbwsq": data_nbwsq, "data_nbsqwsq": data_nbsqwsq,
                      "rand_nbwsq": rand_nbwsq, "rand_nbsqwsq": rand_nbsqwsq},
-            "data": data, "rand": rand, "painted": painted}
+            "data": data, "rand": rand, "painted": painted, "nbar_lines": nbar_lines}

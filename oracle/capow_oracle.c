@@ -748,31 +748,51 @@ static double orc_hubble_inv(double z, void *par) {
   return 1.0 / sqrt(om * (1.0 + z) * (1.0 + z) * (1.0 + z) + (1.0 - om)); /* src/read_data.c:376-379 */
 }
 
-double orc_survey_redshift(double omega_m, double r) {
-  static double cached_om = -1.0;
-  static gsl_spline *red_spline = NULL;
-  if (!red_spline || cached_om != omega_m) {
-    const int nbins = 10000;
-    const double redmin = 0.0, redmax = 10.0, redbinwidth = (redmax - redmin) / (double)(nbins - 1);
-    double *zt = (double *)malloc(nbins * sizeof(double)), *rt = (double *)malloc(nbins * sizeof(double));
-    double om = omega_m;
-    gsl_function F;
-    F.function = &orc_hubble_inv;
-    F.params = &om;
-    zt[0] = 0.0;
-    rt[0] = 0.0;
-    for (int i = 1; i < nbins; i++) { /* comoving_distance, src/read_data.c:365-373 */
-      double result, error;
-      zt[i] = i * redbinwidth + redmin;
-      gsl_integration_qags(&F, 0.0, zt[i], 0, 1e-7, 1000, NULL, &result, &error);
-      rt[i] = 299792.458 * result / 100.0;
-    }
-    if (red_spline) gsl_spline_free(red_spline);
-    red_spline = gsl_spline_alloc(gsl_interp_cspline, nbins);
-    gsl_spline_init(red_spline, rt, zt, nbins);
-    free(zt);
-    free(rt);
-    cached_om = omega_m;
+static double g_table_om = -1.0;
+static gsl_spline *g_red_spline = NULL, *g_dist_spline = NULL;
+
+static void survey_table(double omega_m) {
+  if (g_red_spline && g_table_om == omega_m) return;
+  const int nbins = 10000;
+  const double redmin = 0.0, redmax = 10.0, redbinwidth = (redmax - redmin) / (double)(nbins - 1);
+  double *zt = (double *)malloc(nbins * sizeof(double)), *rt = (double *)malloc(nbins * sizeof(double));
+  double om = omega_m;
+  gsl_function F;
+  F.function = &orc_hubble_inv;
+  F.params = &om;
+  zt[0] = 0.0;
+  rt[0] = 0.0;
+  for (int i = 1; i < nbins; i++) { /* comoving_distance, src/read_data.c:365-373 */
+    double result, error;
+    zt[i] = i * redbinwidth + redmin;
+    gsl_integration_qags(&F, 0.0, zt[i], 0, 1e-7, 1000, NULL, &result, &error);
+    rt[i] = 299792.458 * result / 100.0;
   }
-  return gsl_spline_eval(red_spline, r, NULL);
+  if (g_red_spline) gsl_spline_free(g_red_spline);
+  if (g_dist_spline) gsl_spline_free(g_dist_spline);
+  g_red_spline = gsl_spline_alloc(gsl_interp_cspline, nbins);
+  g_dist_spline = gsl_spline_alloc(gsl_interp_cspline, nbins);
+  gsl_spline_init(g_red_spline, rt, zt, nbins); /* src/main.c:1247 */
+  gsl_spline_init(g_dist_spline, zt, rt, nbins);
+  free(zt);
+  free(rt);
+  g_table_om = omega_m;
+}
+
+double orc_survey_redshift(double omega_m, double r) {
+  survey_table(omega_m);
+  return gsl_spline_eval(g_red_spline, r, NULL);
+}
+
+double orc_survey_distance(double omega_m, double z) {
+  survey_table(omega_m);
+  return gsl_spline_eval(g_dist_spline, z, NULL);
+}
+
+double orc_cspline_eval(int n, const double *x, const double *y, double t) {
+  gsl_spline *s = gsl_spline_alloc(gsl_interp_cspline, (size_t)n);
+  gsl_spline_init(s, x, y, (size_t)n);
+  const double v = gsl_spline_eval(s, t, NULL);
+  gsl_spline_free(s);
+  return v;
 }

@@ -98,6 +98,11 @@ void orc_survey_power(const orc_params *p, const orc_survey *sp, const double *d
 /* the redshift of comoving distance r from the table create_grids builds (src/main.c:1233-1248,
  * comoving_distance src/read_data.c:365-380), through the GSL stand-ins (orc_gsl.c) */
 double orc_survey_redshift(double omega_m, double r);
+/* the comoving distance of redshift z from the same table (dist_spline, src/main.c:1246-1247) */
+double orc_survey_distance(double omega_m, double z);
+/* a natural cubic spline through (x[i], y[i]), i < n, at t (gsl_interp_cspline through the stand-ins;
+ * compute_nbar's nbar_spline, src/read_data.c:428-438) */
+double orc_cspline_eval(int n, const double *x, const double *y, double t);
 
 #ifdef __cplusplus
 }

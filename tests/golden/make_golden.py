@@ -164,6 +164,11 @@ SURVEY_CASES = [
     ("sv_nn_il", dict(NX=16, NY=16, NZ=16, XMIN=0.0, XMAX=600.0, YMIN=0.0, YMAX=600.0, ZMIN=-100.0, ZMAX=500.0,
                       InterpOrder=1, DoInterlacing=1, NK=8, Maxk=0.08, Odd_Multipoles=1, REDMININ=0.0, REDMAXIN=5.0,
                       FKP_Pk=3000.0, X_Origin=300.0, Y_Origin=300.0, Z_Origin=-200.0), 1000, 10000, 13),
+    # the number density from the randoms' redshifts (compute_nbar, NBAR_Column < 0), observer at the centre
+    ("sv_cic_nbar", dict(NX=24, NY=24, NZ=24, XMIN=-600.0, XMAX=600.0, YMIN=-600.0, YMAX=600.0, ZMIN=-600.0,
+                         ZMAX=600.0, InterpOrder=2, DoInterlacing=1, NK=10, Maxk=0.1, Odd_Multipoles=0,
+                         REDMININ=0.0, REDMAXIN=0.3, FKP_Pk=4000.0, NBAR_Column=-1, SkyArea=41253.0), 1500, 12000,
+     14),
 ]
 
 
@@ -188,8 +193,8 @@ def main_survey():
     manifest = {}
     with tempfile.TemporaryDirectory() as td:
         for name, kw, nd, nr, seed in SURVEY_CASES:
-            p = orc.Params(**kw, Periodic=0, Coord_Type=0, NBAR_Column=5, FKP_Column=-1,
-                           NOBJ_Max=max(nd, nr) + 10)
+            p = orc.Params(**{"Periodic": 0, "Coord_Type": 0, "NBAR_Column": 5, "FKP_Column": -1, **kw,
+                              "NOBJ_Max": max(nd, nr) + 10})
             rng = np.random.default_rng(seed)
             data, rand = survey_catalogue(p, nd, 12, rng), survey_catalogue(p, nr, 8, rng)
             pf, df, rf, of, dump = (os.path.join(td, f"{name}.{e}") for e in ("dat", "data", "rand", "out", "dump"))

@@ -83,8 +83,7 @@ def _write_params(tmp_path, **kw):
 
 
 def _gpu(prm, sv, df, rf, precision, grids=False, device_inputs=False):
-    data = cg.read_survey(df, prm, sv, False)
-    rand = cg.read_survey(rf, prm, sv, True)
+    data, rand, _ = cg.read_survey_pair(df, rf, prm, sv)
     keys = ("x", "y", "z", "w", "nbar")
     if device_inputs:
         import torch

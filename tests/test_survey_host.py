@@ -127,3 +127,36 @@ def test_survey_reader_redshift_cut_and_progress_lines(tmp_path):
                        z_orc[inside].astype(np.float32), rtol=1e-6)
     lines = got["log"].splitlines()
     assert len(lines) == 1 and lines[0].startswith("Read 1000000 objects, kept ")
+
+
+def test_survey_nbar_matches_the_oracle_and_the_reference_table(tmp_path):
+    """compute_nbar (NBAR_Column < 0) on the golden catalogue that uses it: the lines the reference printed
+    (the per-bin number density table), and every object's nbar against the oracle's restatement (the
+    distance tables differ in the last digits, so float nbar may differ in the last bit)."""
+    name = "sv_cic_nbar"
+    p, pf, df, rf, d = write_survey_inputs(tmp_path, name)
+    prm, sv = _read_params(pf)
+    assert sv.NBAR_Column < 0
+    data, rand, log = cg.read_survey_pair(df, rf, prm, sv)
+    txt = open(os.path.join(os.path.dirname(__file__), "golden", f"{name}.stdout")).read().splitlines()
+    at = txt.index("Calculating Number Density...")
+    lines = log.splitlines()
+    assert lines == txt[at: at + len(lines)]
+    assert txt[at + len(lines)] == "Computing FKP Weights..."
+    od, orr = orc.survey_read(p, df, False), orc.survey_read(p, rf, True)
+    assert orc.survey_nbar(p, od, orr) == lines
+    for mine, ref in ((data, od), (rand, orr)):
+        assert np.allclose(mine["nbar"], ref["nbar"], rtol=1e-6, atol=0)
+        assert np.mean(mine["nbar"] == ref["nbar"]) > 0.99
+
+
+def test_survey_nbar_rejects_more_data_than_randoms(tmp_path):
+    p, pf = _params_file(tmp_path, NBAR_Column=-1, REDMAXIN=0.3)
+    prm, sv = _read_params(pf)
+    row = "10 20 30 1.5 0.001 0 0 0 0 0 0 0\n"
+    f, g = tmp_path / "d.txt", tmp_path / "r.txt"
+    f.write_text(row * 3)
+    g.write_text("10 20 30 1 0 0 0 0\n" * 2)
+    with pytest.raises(cg.CapowError) as e:
+        cg.read_survey_pair(str(f), str(g), prm, sv)
+    assert e.value.status == cg.EINVAL and "randoms" in str(e.value)
