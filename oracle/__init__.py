@@ -113,6 +113,8 @@ class Params:
     SkyArea: float = 1.0
     FKP_Column: int = -1
     FKP_Pk: float = 0.0
+    FKP_Pk_mom: float = 0.0
+    FKP_Pk_cross: float = 0.0
 
     def to_c(self) -> OrcParams:
         return OrcParams(self.NX, self.NY, self.NZ, self.XMIN, self.XMAX, self.YMIN, self.YMAX, self.ZMIN,
@@ -133,7 +135,8 @@ class Params:
             Z_Origin=repr(float(self.Z_Origin)), REDMININ=repr(float(self.REDMININ)),
             REDMAXIN=repr(float(self.REDMAXIN)), NOBJ_Max=self.NOBJ_Max, Coord_Type=self.Coord_Type, x_Column=1,
             y_Column=2, z_Column=3, NBAR_Column=self.NBAR_Column, SkyArea=repr(float(self.SkyArea)),
-            FKP_Column=self.FKP_Column, FKP_Pk=repr(float(self.FKP_Pk)), FKP_Pk_mom=0, FKP_Pk_cross=0,
+            FKP_Column=self.FKP_Column, FKP_Pk=repr(float(self.FKP_Pk)),
+            FKP_Pk_mom=repr(float(self.FKP_Pk_mom)), FKP_Pk_cross=repr(float(self.FKP_Pk_cross)),
             Odd_Multipoles=self.Odd_Multipoles,
         )
         with open(path, "w") as f:
@@ -437,9 +440,11 @@ def _survey_lib():
         dp = ctypes.POINTER(ctypes.c_double)
         ip = ctypes.POINTER(ctypes.c_int)
         P = ctypes.POINTER(OrcParams)
-        L.orc_survey_paint.restype = ctypes.c_double
-        L.orc_survey_paint.argtypes = [P, ctypes.c_int64, dp, dp, dp, dp, ctypes.c_double, dp, dp]
-        L.orc_survey_power.argtypes = [P, ctypes.POINTER(OrcSurvey), dp, dp, dp, dp, dp, dp, dp, ip]
+        L.orc_survey_assign.restype = ctypes.c_double
+        L.orc_survey_assign.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int64, dp, dp, dp, dp, dp, dp,
+                                        ctypes.c_double, dp, dp, dp, dp]
+        L.orc_survey_power.argtypes = [P, ctypes.POINTER(OrcSurvey), ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp,
+                                       dp, ip]
         L.orc_survey_redshift.restype = ctypes.c_double
         L.orc_survey_redshift.argtypes = [ctypes.c_double, ctypes.c_double]
         L.orc_survey_distance.restype = ctypes.c_double
@@ -493,6 +498,17 @@ def survey_read(p: Params, path: str, randoms: bool) -> dict:
            "weight": a[k, 3].astype(f32), "redshift": np.array(red).astype(f32), "nread": a.shape[0],
            "redmin": min(red, default=1.0e30), "redmax": max(red, default=-1.0e30)}  # REDMIN/REDMAX, :327-328
     out["nbar"] = a[k, 4].astype(f32) if p.NBAR_Column > 0 else np.zeros(len(k), f32)
+    if p.Momentum:  # :308-316; a random line carries no log-distance (its pv is never used), only the error
+        q = 3.0 / 2.0 * p.Omega_m - 1.0
+        tr = np.array(red, dtype=np.float64)
+        zmod = tr * (1.0 + 0.5 * (1.0 - q) * tr - 1.0 / 6.0 * (2.0 - q - 3.0 * q * q) * tr * tr)
+        logdist = np.zeros(len(k)) if randoms else a[k, 6]
+        logdist_err = a[k, 6] if randoms else a[k, 7]
+        out["pv"] = (299792.458 * zmod * np.log(10.0) * logdist / (1.0 + zmod)).astype(f32)
+        out["pverr"] = (299792.458 * zmod * np.log(10.0) * logdist_err / (1.0 + zmod)).astype(f32)
+    else:
+        out["pv"] = out["pverr"] = np.zeros(len(k), f32)
+    out["weight_pv"] = np.zeros(len(k), f32)
     return out
 
 
@@ -531,53 +547,95 @@ def survey_nbar(p: Params, data: dict, rand: dict) -> list:
 
 
 def survey_fkp(p: Params, cat: dict) -> None:
-    """compute_fkp for the density (src/read_data.c:450-466): weight *= 1 / (1 + nbar FKP_Pk) in double, stored
-    back into the float weight, in place."""
-    w = cat["weight"].astype(np.float64) * (1.0 / (1.0 + cat["nbar"].astype(np.float64) * p.FKP_Pk))
-    cat["weight"] = w.astype(np.float32)
+    """compute_fkp (src/read_data.c:450-466) in place, products in double and results stored back in the float
+    fields. Momentum 0: w *= 1/(1 + nbar FKP_Pk). Momentum 1: w *= 1/((pverr^2 + 300^2) + nbar FKP_Pk_mom), with
+    pverr^2 a float product. Momentum 2, 3: the density and velocity weights, both times the cross factor
+    1/sqrt(1 + w_d w_v nbar^2 FKP_Pk_cross^2), into weight and weight_pv."""
+    f32 = np.float32
+    w = cat["weight"].astype(np.float64)
+    nb = cat["nbar"].astype(np.float64)
+    pe2 = (cat["pverr"] * cat["pverr"]).astype(np.float64)  # float * float
+    if p.Momentum == 0:
+        cat["weight"] = (w * (1.0 / (1.0 + nb * p.FKP_Pk))).astype(f32)
+    elif p.Momentum == 1:
+        cat["weight"] = (w * (1.0 / ((pe2 + 300.0 * 300.0) + nb * p.FKP_Pk_mom))).astype(f32)
+    else:
+        tw = 1.0 / (1.0 + nb * p.FKP_Pk)
+        twpv = 1.0 / ((pe2 + 300.0 * 300.0) + nb * p.FKP_Pk_mom)
+        twc = 1.0 / np.sqrt(1.0 + tw * twpv * nb * nb * p.FKP_Pk_cross * p.FKP_Pk_cross)
+        cat["weight_pv"] = (w * twpv * twc).astype(f32)
+        cat["weight"] = (w * (tw * twc)).astype(f32)
 
 
 def survey_run(p: Params, data_path: str, rand_path: str, grids: bool = False) -> dict:
-    """The survey branch of main for the density (src/main.c:77-95, 149-204, 226-258, 279-288): read data and
-    randoms, FKP weights, alpha / shot / norm, data minus alpha randoms painted, the Yamamoto multipoles,
-    output_power's normalisation."""
+    """The survey branch of main (src/main.c:77-95, 149-204, 226-258, 279-288) for Momentum 0-3: read data and
+    randoms, n(z) when NBAR_Column < 0, FKP weights, the sums, alpha, shot and norm of the Momentum, the
+    painted grids (data minus alpha randoms; Momentum 1 paints the data's w pv only; Momentum 2, 3 add the
+    data's w_pv pv momentum grid), the Yamamoto multipoles, output_power's normalisation."""
     L = _survey_lib()
+    m = p.Momentum
     data = survey_read(p, data_path, False)
     rand = survey_read(p, rand_path, True)
     nbar_lines = survey_nbar(p, data, rand) if p.NBAR_Column < 0 else []
     if p.FKP_Column < 0:
         survey_fkp(p, data)
         survey_fkp(p, rand)
-    wd, wr = data["weight"], rand["weight"]  # float32: the products below are float products, as in C
-    data_nbw, data_nbwsq, data_nbsqwsq = _seqsum(wd), _seqsum(wd * wd), _seqsum(wd * wd * data["nbar"])
-    rand_nbw, rand_nbwsq, rand_nbsqwsq = _seqsum(wr), _seqsum(wr * wr), _seqsum(wr * wr * rand["nbar"])
-    wd, wr = wd.astype(np.float64), wr.astype(np.float64)
-    for c in (data, rand):
-        for a in ("x", "y", "z"):
-            c[a] = c[a].astype(np.float64)
+    elif m >= 2:
+        raise ValueError("Momentum 2, 3 need the FKP weights: the reference leaves weight_pv unset otherwise")
+    # float32 fields: the products below are float products, summed in double, as in C (:151-163)
+    wd, wr, nd_, nr_ = data["weight"], rand["weight"], data["nbar"], rand["nbar"]
+    data_nbw, data_nbwsq, data_nbsqwsq = _seqsum(wd), _seqsum(wd * wd), _seqsum(wd * wd * nd_)
+    data_vr = data_vrsq = data_nbsqwsq_pv = 0.0
+    if m:
+        wpv, pv = data["weight_pv"], data["pv"]
+        data_vr, data_vrsq = _seqsum(wd * wpv * pv), _seqsum(wd * wd * pv * pv)
+        data_nbsqwsq_pv = _seqsum(wpv * wpv * nd_)
+    rand_nbw, rand_nbwsq, rand_nbsqwsq = _seqsum(wr), _seqsum(wr * wr), _seqsum(wr * wr * nr_)
+    rand_nbsqwsq_pv = _seqsum(rand["weight_pv"] * rand["weight_pv"] * nr_) if m == 2 else 0.0
     alpha = data_nbw / rand_nbw
     rand_nbwsq *= alpha * alpha
     rand_nbsqwsq *= alpha
-    shot = data_nbwsq + rand_nbwsq
-    norm = rand_nbsqwsq
+    if m == 0:
+        shot, norm = data_nbwsq + rand_nbwsq, rand_nbsqwsq
+    elif m == 1:
+        shot, norm = data_vrsq, rand_nbsqwsq
+    elif m == 2:
+        shot, norm = data_vr, float(np.sqrt(rand_nbsqwsq * rand_nbsqwsq_pv))
+    else:
+        shot, norm = data_vrsq, float(np.sqrt(rand_nbsqwsq * rand_nbsqwsq_pv))
+    d64 = {c: {a: v.astype(np.float64) for a, v in cat.items() if isinstance(v, np.ndarray)}
+           for c, cat in (("d", data), ("r", rand))}
     pc = p.to_c()
     nd = lib().orc_grid_doubles(ctypes.byref(pc))
     ddg = np.zeros(nd)
     ddgi = np.zeros(nd) if p.DoInterlacing else None
-    ngrid_d = L.orc_survey_paint(ctypes.byref(pc), len(wd), _dp(data["x"]), _dp(data["y"]), _dp(data["z"]), _dp(wd),
-                                 1.0, _dp(ddg), _dp(ddgi))
-    ngrid_r = L.orc_survey_paint(ctypes.byref(pc), len(wr), _dp(rand["x"]), _dp(rand["y"]), _dp(rand["z"]), _dp(wr),
-                                 -alpha, _dp(ddg), _dp(ddgi))
-    painted = {"ddg": ddg.copy(), "ddg_interlace": None if ddgi is None else ddgi.copy()} if grids else None
+    ddgm = np.zeros(nd) if m >= 2 else None
+    ddgmi = np.zeros(nd) if m >= 2 and p.DoInterlacing else None
+
+    def assign(c, is_data, pref):
+        a = d64[c]
+        return L.orc_survey_assign(ctypes.byref(pc), m, is_data, len(a["x"]), _dp(a["x"]), _dp(a["y"]), _dp(a["z"]),
+                                   _dp(a["weight"]), _dp(a["weight_pv"]), _dp(a["pv"]), pref, _dp(ddg), _dp(ddgi),
+                                   _dp(ddgm) if is_data else None, _dp(ddgmi) if is_data else None)
+
+    ngrid_d = assign("d", 1, 1.0)
+    ngrid_r = assign("r", 0, -alpha) if m != 1 else None  # src/main.c:229
+    painted = ({"ddg": ddg.copy(), "ddg_interlace": None if ddgi is None else ddgi.copy(),
+                "ddg_mom": None if ddgm is None else ddgm.copy(),
+                "ddg_mom_interlace": None if ddgmi is None else ddgmi.copy()} if grids else None)
     NK = p.NK
     pk = [np.zeros(NK) for _ in range(5)]
     nm = np.zeros(NK, np.int32)
     sp = OrcSurvey(p.X_Origin, p.Y_Origin, p.Z_Origin)
-    L.orc_survey_power(ctypes.byref(pc), ctypes.byref(sp), _dp(ddg), _dp(ddgi), *[_dp(a) for a in pk], _ip(nm))
+    L.orc_survey_power(ctypes.byref(pc), ctypes.byref(sp), m, _dp(ddg), _dp(ddgi), _dp(ddgm), _dp(ddgmi),
+                       *[_dp(a) for a in pk], _ip(nm))
     raw = {"Pk0": pk[0], "Pk1": pk[1], "Pk2": pk[2], "Pk3": pk[3], "Pk4": pk[4], "Nmodes": nm}
-    normed, last = normalise(p, raw, shot, norm)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        normed, last = normalise(p, raw, shot, norm)
     return {"raw": raw, "norm": normed, "last": last, "alpha": alpha, "shot": shot, "normf": norm,
-            "ndata": len(wd), "nrand": len(wr), "ngrid_data": ngrid_d, "ngrid_rand": ngrid_r / -alpha,
+            "ndata": len(wd), "nrand": len(wr), "ngrid_data": ngrid_d,
+            "ngrid_rand": None if ngrid_r is None else ngrid_r / -alpha,
             "sums": {"data_nbw": data_nbw, "data_nbwsq": data_nbwsq, "data_nbsqwsq": data_nbsqwsq,
-                     "rand_nbwsq": rand_nbwsq, "rand_nbsqwsq": rand_nbsqwsq},
+                     "rand_nbwsq": rand_nbwsq, "rand_nbsqwsq": rand_nbsqwsq, "data_vr": data_vr,
+                     "data_vrsq": data_vrsq, "data_nbsqwsq_pv": data_nbsqwsq_pv, "rand_nbsqwsq_pv": rand_nbsqwsq_pv},
             "data": data, "rand": rand, "painted": painted, "nbar_lines": nbar_lines}

@@ -540,15 +540,25 @@ double orc_survey_add(const orc_params *p, double x, double y, double z, double 
 /* assign_survey_data for the density (src/read_data.c:471-494, Momentum 0): each object, and its
  * copy shifted by half a cell into the interlaced grid, with weight prefactor * w. Returns
  * sum(add_to_grid / w) (the reference's NGRID of the call). */
-double orc_survey_paint(const orc_params *p, int64_t n, const double *x, const double *y, const double *z,
-                        const double *w, double prefactor, double *ddg, double *ddg_interlace) {
+double orc_survey_assign(const orc_params *p, int momentum, int is_data, int64_t n, const double *x, const double *y,
+                         const double *z, const double *w, const double *wpv, const double *pv, double prefactor,
+                         double *ddg, double *ddg_i, double *ddg_m, double *ddg_mi) {
   const geom g = mk_geom(p);
   double ngrid = 0.0;
   for (int64_t i = 0; i < n; i++) {
-    ngrid += orc_survey_add(p, x[i], y[i], z[i], prefactor * w[i], 1.0, ddg) / w[i];
-    if (p->do_interlacing)
-      orc_survey_add(p, x[i] + g.dx / 2.0, y[i] + g.dy / 2.0, z[i] + g.dz / 2.0, prefactor * w[i], 1.0,
-                     ddg_interlace);
+    const double xi = x[i] + g.dx / 2.0, yi = y[i] + g.dy / 2.0, zi = z[i] + g.dz / 2.0;
+    if (momentum == 1) { /* :476-478: the divisor pv * weight is a float product */
+      const float pw = (float)pv[i] * (float)w[i];
+      ngrid += orc_survey_add(p, x[i], y[i], z[i], w[i], prefactor * pv[i], ddg) / (double)pw;
+      if (p->do_interlacing) orc_survey_add(p, xi, yi, zi, w[i], prefactor * pv[i], ddg_i);
+    } else { /* :479-486 */
+      ngrid += orc_survey_add(p, x[i], y[i], z[i], prefactor * w[i], 1.0, ddg) / w[i];
+      if (p->do_interlacing) orc_survey_add(p, xi, yi, zi, prefactor * w[i], 1.0, ddg_i);
+      if (momentum && is_data) {
+        orc_survey_add(p, x[i], y[i], z[i], wpv[i], prefactor * pv[i], ddg_m);
+        if (p->do_interlacing) orc_survey_add(p, xi, yi, zi, wpv[i], prefactor * pv[i], ddg_mi);
+      }
+    }
   }
   return ngrid;
 }
@@ -613,10 +623,13 @@ static void survey_weight(const orc_params *p, const orc_survey *sp, int l, cons
       }
 }
 
-/* assign_survey_power for the density (src/main.c:781-967, Momentum 0) over the transformed term grid
- * dk (and its interlaced copy); multipole 0 stores the combined field in F0. */
-static void survey_assign(const orc_params *p, int l, const int *ijk, const double *d2, const double *d2i, double *F0,
+/* assign_survey_power (src/main.c:781-967) over the transformed term grid d2 (and its interlaced copy);
+ * multipole 0 stores the combined field in F0. With Momentum 2, 3 the momentum term grid m2 (m2i) is
+ * combined too, multipole 0 stores it in F0m, and the power is the cross form of :876-887. */
+static void survey_assign(const orc_params *p, int momentum, int l, const int *ijk, const double *d2,
+                          const double *d2i, const double *m2, const double *m2i, double *F0, double *F0m,
                           double *pk[5], int *nmodes) {
+  const int cross = (momentum != 0) && (momentum != 1);
   const geom g = mk_geom(p);
   const int NK = p->nk;
   const double ny_x = M_PI / g.dx, ny_y = M_PI / g.dy, ny_z = M_PI / g.dz;
@@ -651,15 +664,38 @@ static void survey_assign(const orc_params *p, int l, const int *ijk, const doub
           dkr += a * cosk - b * sink;
           dki += a * sink + b * cosk;
         }
+        double mkr = 0.0, mki = 0.0;
+        if (cross) { /* :859-869 */
+          mkr = m2[ind];
+          mki = m2[ind + 1];
+          if (p->do_interlacing) {
+            double kh = ax + ay + az, sink = sin(kh), cosk = cos(kh);
+            double a = m2i[ind], b = m2i[ind + 1];
+            mkr += a * cosk - b * sink;
+            mki += a * sink + b * cosk;
+          }
+        }
         double power;
-        if (l == 0) {
+        if (!cross) {
+          if (l == 0) {
+            F0[ind] = dkr;
+            F0[ind + 1] = dki;
+            power = (dkr * dkr + dki * dki) * grid_cor;
+          } else if (l % 2) {
+            power = (dkr * F0[ind + 1] - dki * F0[ind]) * grid_cor;
+          } else {
+            power = (dkr * F0[ind] + dki * F0[ind + 1]) * grid_cor;
+          }
+        } else if (l == 0) {
           F0[ind] = dkr;
           F0[ind + 1] = dki;
-          power = (dkr * dkr + dki * dki) * grid_cor;
+          F0m[ind] = mkr;
+          F0m[ind + 1] = mki;
+          power = (dkr * mki - dki * mkr) * grid_cor;
         } else if (l % 2) {
-          power = (dkr * F0[ind + 1] - dki * F0[ind]) * grid_cor;
+          power = 0.5 * (dkr * F0m[ind] + dki * F0m[ind + 1] + mkr * F0[ind] + mki * F0[ind + 1]) * grid_cor;
         } else {
-          power = (dkr * F0[ind] + dki * F0[ind + 1]) * grid_cor;
+          power = 0.5 * (dkr * F0m[ind + 1] - dki * F0m[ind] + mkr * F0[ind + 1] - mki * F0[ind]) * grid_cor;
         }
         int NM = 2;
         if (k == 0) {
@@ -709,9 +745,11 @@ static void survey_assign(const orc_params *p, int l, const int *ijk, const doub
       }
 }
 
-void orc_survey_power(const orc_params *p, const orc_survey *sp, const double *ddg, const double *ddg_interlace,
-                      double *pk0, double *pk1, double *pk2, double *pk3, double *pk4, int *nmodes) {
+void orc_survey_power(const orc_params *p, const orc_survey *sp, int momentum, const double *ddg,
+                      const double *ddg_interlace, const double *ddg_m, const double *ddg_mi, double *pk0,
+                      double *pk1, double *pk2, double *pk3, double *pk4, int *nmodes) {
   const int NK = p->nk;
+  const int cross = (momentum != 0) && (momentum != 1);
   double *pk[5] = {pk0, pk1, pk2, pk3, pk4};
   double dummy[NK > 0 ? NK : 1];
   for (int l = 0; l < 5; l++) {
@@ -723,6 +761,9 @@ void orc_survey_power(const orc_params *p, const orc_survey *sp, const double *d
   double *d2 = (double *)calloc((size_t)nd, sizeof(double));
   double *d2i = p->do_interlacing ? (double *)calloc((size_t)nd, sizeof(double)) : NULL;
   double *F0 = (double *)calloc((size_t)nd, sizeof(double));
+  double *m2 = cross ? (double *)calloc((size_t)nd, sizeof(double)) : NULL;
+  double *m2i = cross && p->do_interlacing ? (double *)calloc((size_t)nd, sizeof(double)) : NULL;
+  double *F0m = cross ? (double *)calloc((size_t)nd, sizeof(double)) : NULL;
   const int step = p->odd_multipoles ? 1 : 2; /* src/main.c:490-492 */
   for (int l = 0; l <= 4; l += step) {
     int t[15][3];
@@ -734,12 +775,23 @@ void orc_survey_power(const orc_params *p, const orc_survey *sp, const double *d
         survey_weight(p, sp, l, t[q], ddg_interlace, d2i);
         orc_fft_r2c_3d_inplace(p->nx, p->ny, p->nz, d2i);
       }
-      survey_assign(p, l, t[q], d2, d2i, F0, pk, nmodes);
+      if (cross) { /* the momentum grids get the same products (src/main.c:515-526, 560-573, ...) */
+        survey_weight(p, sp, l, t[q], ddg_m, m2);
+        orc_fft_r2c_3d_inplace(p->nx, p->ny, p->nz, m2);
+        if (m2i) {
+          survey_weight(p, sp, l, t[q], ddg_mi, m2i);
+          orc_fft_r2c_3d_inplace(p->nx, p->ny, p->nz, m2i);
+        }
+      }
+      survey_assign(p, momentum, l, t[q], d2, d2i, m2, m2i, F0, F0m, pk, nmodes);
     }
   }
   free(d2);
   free(d2i);
   free(F0);
+  free(m2);
+  free(m2i);
+  free(F0m);
 }
 
 /* ---- the redshift-distance table of create_grids (src/main.c:1233-1248) */

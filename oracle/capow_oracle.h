@@ -85,15 +85,21 @@ typedef struct {
 /* add_to_grid with the Survey branches (src/read_data.c:514-745) */
 double orc_survey_add(const orc_params *p, double x, double y, double z, double w, double vr, double *density);
 
-/* assign_survey_data (src/read_data.c:471-494): every object with weight prefactor * w, and into the
- * interlaced grid half a cell up; returns sum(add_to_grid / w) */
-double orc_survey_paint(const orc_params *p, int64_t n, const double *x, const double *y, const double *z,
-                        const double *w, double prefactor, double *ddg, double *ddg_interlace);
+/* assign_survey_data (src/read_data.c:471-494) for every Momentum. The object fields are the reference's
+ * floats, passed as doubles (exact). Momentum 1: w * prefactor pv into ddg (and, half a cell up, ddg_i),
+ * NGRID += add_to_grid / (float)(pv w); otherwise: prefactor w into ddg, NGRID += add_to_grid / w, and for
+ * data with Momentum 2, 3: w_pv * prefactor pv into ddg_m (ddg_mi). wpv and pv may be NULL for Momentum 0.
+ * Returns NGRID. */
+double orc_survey_assign(const orc_params *p, int momentum, int is_data, int64_t n, const double *x, const double *y,
+                         const double *z, const double *w, const double *wpv, const double *pv, double prefactor,
+                         double *ddg, double *ddg_i, double *ddg_m, double *ddg_mi);
 
-/* compute_survey_power + assign_survey_power (src/main.c:472-967, Momentum 0): raw bin sums of the
- * Yamamoto multipoles from the painted grids (data minus alpha randoms); the oracle FFT in place of FFTW */
-void orc_survey_power(const orc_params *p, const orc_survey *sp, const double *ddg, const double *ddg_interlace,
-                      double *pk0, double *pk1, double *pk2, double *pk3, double *pk4, int *nmodes);
+/* compute_survey_power + assign_survey_power (src/main.c:472-967): raw bin sums of the Yamamoto multipoles
+ * from the painted grids; Momentum 2, 3 also transform the momentum grids and bin the cross terms with F0 and
+ * F0_mom (ddg_m, ddg_mi NULL otherwise); the oracle FFT in place of FFTW */
+void orc_survey_power(const orc_params *p, const orc_survey *sp, int momentum, const double *ddg,
+                      const double *ddg_interlace, const double *ddg_m, const double *ddg_mi, double *pk0,
+                      double *pk1, double *pk2, double *pk3, double *pk4, int *nmodes);
 
 /* the redshift of comoving distance r from the table create_grids builds (src/main.c:1233-1248,
  * comoving_distance src/read_data.c:365-380), through the GSL stand-ins (orc_gsl.c) */

@@ -169,6 +169,21 @@ SURVEY_CASES = [
                          ZMAX=600.0, InterpOrder=2, DoInterlacing=1, NK=10, Maxk=0.1, Odd_Multipoles=0,
                          REDMININ=0.0, REDMAXIN=0.3, FKP_Pk=4000.0, NBAR_Column=-1, SkyArea=41253.0), 1500, 12000,
      14),
+    # velocity surveys: the peculiar velocities from log-distance ratios, P_vv (Momentum 1) and the
+    # density-velocity cross spectra. The reference's survey Momentum 2 writes its momentum grid before
+    # allocating it (create_grids allocates ddg_mom only for Momentum not in {0, 2, 5}, src/main.c:1198) and
+    # crashes; Momentum 3 runs the same cross-spectrum code (its norm, src/main.c:164-165, 184-186, is zero)
+    ("sv_vv_tsc_il", dict(NX=24, NY=24, NZ=24, XMIN=50.0, XMAX=650.0, YMIN=-300.0, YMAX=300.0, ZMIN=-300.0,
+                          ZMAX=300.0, InterpOrder=3, DoInterlacing=1, NK=10, Maxk=0.12, Odd_Multipoles=1,
+                          REDMININ=0.0, REDMAXIN=5.0, FKP_Pk=4000.0, FKP_Pk_mom=5.0e9, Momentum=1), 1500, 6000, 15),
+    ("sv_dv_cic_il", dict(NX=24, NY=20, NZ=16, XMIN=-700.0, XMAX=-100.0, YMIN=100.0, YMAX=600.0, ZMIN=-200.0,
+                          ZMAX=200.0, InterpOrder=2, DoInterlacing=1, NK=10, Maxk=0.12, Odd_Multipoles=1,
+                          REDMININ=0.0, REDMAXIN=5.0, FKP_Pk=4000.0, FKP_Pk_mom=5.0e9, FKP_Pk_cross=1.0e5,
+                          Momentum=3, X_Origin=30.0, Y_Origin=-10.0, Z_Origin=0.0), 1500, 9000, 16),
+    ("sv_dv3_tsc", dict(NX=16, NY=16, NZ=16, XMIN=100.0, XMAX=500.0, YMIN=-200.0, YMAX=200.0, ZMIN=-200.0,
+                        ZMAX=200.0, InterpOrder=3, DoInterlacing=0, NK=8, Maxk=0.12, Odd_Multipoles=0,
+                        REDMININ=0.0, REDMAXIN=5.0, FKP_Pk=4000.0, FKP_Pk_mom=5.0e9, FKP_Pk_cross=1.0e5,
+                        Momentum=3), 1000, 6000, 17),
 ]
 
 
@@ -181,7 +196,14 @@ def survey_catalogue(p, n, ncol, rng):
     pos = rng.uniform(lo + 1e-3 * d, hi - 1e-3 * d, size=(n, 3))
     w = rng.uniform(0.5, 1.5, n)
     nb = 1e-4 * (1.0 + 0.5 * np.sin(np.linalg.norm(pos, axis=1) / 200.0))
-    return np.concatenate([pos, w[:, None], nb[:, None], np.zeros((n, ncol - 5))], axis=1)
+    out = np.concatenate([pos, w[:, None], nb[:, None], np.zeros((n, ncol - 5))], axis=1)
+    if p.Momentum:  # log-distance ratios and their errors (data: 7th and 8th numbers; randoms: the 7th error)
+        if ncol == 12:
+            out[:, 6] = rng.normal(0.0, 0.05, n)
+            out[:, 7] = rng.uniform(0.05, 0.1, n)
+        else:
+            out[:, 6] = rng.uniform(0.05, 0.1, n)
+    return out
 
 
 def main_survey():

@@ -172,4 +172,16 @@ def test_oracle_survey_matches_reference_bit_for_bit(tmp_path, name):
         assert np.array_equal(r["raw"][k], d[k]), (name, k)
     # the normalised first data row of the reference's output file
     row = [float(t) for t in open(os.path.join(GOLD, f"{name}.out")).read().splitlines()[3].split()]
-    assert abs(row[1] - r["norm"]["Pk0"][0]) <= 1e-5 * abs(row[1]) + 1e-9
+    got = r["norm"]["Pk0"][0]
+    if np.isfinite(row[1]):
+        assert abs(row[1] - got) <= 1e-5 * abs(row[1]) + 1e-9
+    else:  # Momentum 3: the reference's norm is zero
+        assert got == row[1]
+    # the scalars the reference printed (src/main.c:189-203)
+    txt = open(os.path.join(GOLD, f"{name}.stdout")).read()
+    if p.Momentum == 0:
+        assert f"alpha = {r['alpha']:g}" in txt
+    elif p.Momentum == 1:
+        assert f"shot-noise [data]    = {r['sums']['data_vrsq']:g} " in txt
+    else:
+        assert f"shot-noise    = {r['sums']['data_vr']:g}" in txt and f"normalisation = {r['normf']:g}" in txt
