@@ -103,17 +103,18 @@ class _SurveyParams(ctypes.Structure):
 class _SurveyCatalogue(ctypes.Structure):
     _fields_ = [("n", ctypes.c_size_t), ("dtype", ctypes.c_int), ("on_device", ctypes.c_int),
                 ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("z", ctypes.c_void_p),
-                ("w", ctypes.c_void_p), ("nbar", ctypes.c_void_p)]
+                ("w", ctypes.c_void_p), ("nbar", ctypes.c_void_p), ("pv", ctypes.c_void_p), ("pverr", ctypes.c_void_p)]
 
 
 class _SurveyStats(ctypes.Structure):
     _fields_ = [(k, ctypes.c_double) for k in ("ngrid_data", "ngrid_rand", "data_nbw", "data_nbwsq", "data_nbsqwsq",
-                                               "rand_nbw", "rand_nbwsq", "rand_nbsqwsq")]
+                                               "rand_nbw", "rand_nbwsq", "rand_nbsqwsq", "data_vr", "data_vrsq",
+                                               "data_nbsqwsq_pv", "rand_nbsqwsq_pv")]
 
 
 class _SurveyObjects(ctypes.Structure):
     _fields_ = [("n", ctypes.c_size_t), ("nread", ctypes.c_ulonglong)] + [
-        (k, ctypes.POINTER(ctypes.c_float)) for k in ("x", "y", "z", "w", "nbar", "redshift")] + [
+        (k, ctypes.POINTER(ctypes.c_float)) for k in ("x", "y", "z", "w", "nbar", "redshift", "pv", "pverr")] + [
         ("lo", ctypes.c_double * 3), ("hi", ctypes.c_double * 3), ("redmin", ctypes.c_double),
         ("redmax", ctypes.c_double), ("log", ctypes.c_void_p)]
 
@@ -637,7 +638,7 @@ def _read_survey_objects(path: str, params: Params, survey: SurveyParams, random
 
 def _survey_objects_dict(o: _SurveyObjects) -> dict:
     out = {k: (np.ctypeslib.as_array(getattr(o, k), shape=(o.n,)).copy() if o.n else np.zeros(0, np.float32))
-           for k in ("x", "y", "z", "w", "nbar", "redshift")}
+           for k in ("x", "y", "z", "w", "nbar", "redshift", "pv", "pverr")}
     out.update(n=o.n, nread=o.nread, lo=list(o.lo), hi=list(o.hi), redmin=o.redmin, redmax=o.redmax,
                log=ctypes.string_at(o.log).decode() if o.log else "")
     return out
@@ -680,10 +681,19 @@ def read_survey_pair(data_path: str, rand_path: str, params: Params, survey: Sur
         L.capow_survey_objects_free(ctypes.byref(r))
 
 
-def _survey_cat(cat):
-    """A capow_survey_catalogue for a dict (or tuple) of x, y, z, w, nbar arrays (numpy: host; CUDA tensors:
-    device), plus the arrays to keep alive."""
-    arrs = [cat[k] for k in ("x", "y", "z", "w", "nbar")] if isinstance(cat, dict) else list(cat)
+def _survey_cat(cat, velocities: bool):
+    """A capow_survey_catalogue for a dict (or tuple) of x, y, z, w, nbar arrays and, with velocities, pv and
+    pverr (numpy: host; CUDA tensors: device), plus the arrays to keep alive. A randoms catalogue may leave
+    pv out (it is not read)."""
+    keys = ("x", "y", "z", "w", "nbar") + (("pv", "pverr") if velocities else ())
+    if isinstance(cat, dict):
+        if velocities and "pv" not in cat and "pverr" in cat:
+            cat = dict(cat, pv=cat["pverr"])
+        arrs = [cat[k] for k in keys]
+    else:
+        arrs = list(cat)[:len(keys)]
+        if len(arrs) != len(keys):
+            raise ValueError(f"survey catalogue needs {', '.join(keys)}")
     ptrs = [_ptr_of(a) for a in arrs]
     codes = {p[1] for p in ptrs}
     devs = {p[2] for p in ptrs}
@@ -692,7 +702,8 @@ def _survey_cat(cat):
     n = len(ptrs[0][3])
     if any(len(p[3]) != n for p in ptrs):
         raise ValueError("survey catalogue arrays differ in length")
-    return _SurveyCatalogue(n, codes.pop(), devs.pop(), *[p[0] for p in ptrs]), [p[3] for p in ptrs]
+    addr = [p[0] for p in ptrs] + [None] * (7 - len(ptrs))
+    return _SurveyCatalogue(n, codes.pop(), devs.pop(), *addr), [p[3] for p in ptrs]
 
 
 class SurveySpectrum:
@@ -722,8 +733,8 @@ class SurveySpectrum:
     def power(self, data, rand) -> dict:
         """Raw bin sums, Nmodes, shot, norm, alpha and the survey counters (capow_survey_power)."""
         p = self.params
-        dc, keep_d = _survey_cat(data)
-        rc_, keep_r = _survey_cat(rand)
+        dc, keep_d = _survey_cat(data, p.Momentum != 0)
+        rc_, keep_r = _survey_cat(rand, p.Momentum != 0)
         pk = [np.zeros(p.NK) for _ in range(5)]
         nm = np.zeros(p.NK, np.int64)
         n2d = p.NK * p.NMU if p.Output2D else 0
@@ -765,7 +776,9 @@ class SurveySpectrum:
         return d
 
     def grid(self, which: int) -> np.ndarray:
-        """The painted grid (0) or its interlaced copy (1) of the last evaluation, padded reference layout."""
+        """A painted grid of the last evaluation, padded reference layout. which = stencil * fields + field:
+        the density (field 0) and, for Momentum 2 and 3, the momentum grid (field 1); stencil 1 is the
+        interlaced copy."""
         p = self.params
         out = np.zeros(p.NX * p.NY * 2 * (p.NZ // 2 + 1))
         self._check(lib().capow_survey_copy_grid(self._ctx, which,

@@ -311,9 +311,10 @@ extern "C" int capow_create(const capow_params *p, const capow_options *opt, cap
 
 // A context that paints only: the grids, counters and FP32 tile buffers of capow_create, without bin
 // tables, plans or FFT buffers (capow_paint and capow_power refuse it: plan_ok stays false). survey != 0
-// selects the Survey rules: one density field, no RSD shift and no wrap, the halo slices discarded, the
-// Survey clamps at the upper grid edge (Geom.los = 4, Geom.survey = 1). The survey estimator paints its
-// FP32 grids through it, on the stream given in o->stream.
+// selects the Survey rules with that many fields: 1 (the particles' w) or 2 (w, and w vlos in the
+// second field); no RSD shift and no wrap, the halo slices discarded, the Survey clamps at the upper grid
+// edge (Geom.los = 4, Geom.survey = 1). The survey estimator paints its FP32 grids through it, on the
+// stream given in o->stream.
 int create_paint_ctx(const capow_params *p, const capow_options *o, int survey, capow_ctx **out) {
   *out = nullptr;
   capow_ctx *c = new (std::nothrow) capow_ctx();
@@ -323,7 +324,7 @@ int create_paint_ctx(const capow_params *p, const capow_options *o, int survey, 
   c->o.spectra = CAPOW_SPEC_REFERENCE;
   if (survey) {
     c->p.LOS = 3;
-    c->p.Momentum = 0;
+    c->p.Momentum = survey == 2 ? 1 : 0;  // fields w and w v^1
   }
   int rc = validate(&c->p, &c->o, c->err, sizeof c->err);
   if (rc) {
@@ -350,7 +351,7 @@ int create_paint_ctx(const capow_params *p, const capow_options *o, int survey, 
   if (survey) {
     c->g.los = 4;
     c->g.survey = 1;
-    c->fs.need_v = 0;
+    c->fs.need_v = survey == 2;
     c->fs.moments = 0;
     c->moments = 0;
   }

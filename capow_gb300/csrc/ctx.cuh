@@ -106,6 +106,7 @@ int enqueue_backward_paint(capow_ctx *c);
 
 // capow_api.cu pieces shared with batch.cu and survey.cu
 Geom make_geom(const capow_params &p);
+// survey: 0, or the number of survey fields (1: w; 2: w and w vlos)
 int create_paint_ctx(const capow_params *p, const capow_options *o, int survey, capow_ctx **out);
 // sync, read the paint counters into c->h_st, repaint c->last when the tile lists overflowed
 int settle_paint(capow_ctx *c);

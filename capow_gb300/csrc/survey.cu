@@ -1,27 +1,35 @@
-// Survey-mode estimator (Periodic 0, Survey 1, density) on one GB300: the C ABI's capow_survey_*.
+// Survey-mode estimator (Periodic 0, Survey 1; Momentum 0 to 3) on one GB300: the C ABI's capow_survey_*.
 //
 // Reference semantics (single rank; paths relative to the CAPOW source tree):
-//   src/read_data.c:450-466  compute_fkp: weight *= 1/(1 + nbar FKP_Pk), stored back in the float field
+//   src/read_data.c:450-466  compute_fkp: the FKP weights of the density (Momentum 0), of the velocities
+//                            (Momentum 1: 1/((pverr^2 + 300^2) + nbar FKP_Pk_mom)) or both with their
+//                            cross factor (Momentum 2, 3: weight and weight_pv), stored in float fields
 //   src/main.c:149-204       sums over data and randoms, alpha, shot, norm
-//   src/read_data.c:471-494  assign_survey_data: data with prefactor 1, randoms with -alpha, each object
-//                            and its copy shifted by half a cell (interlacing)
+//   src/read_data.c:471-494  assign_survey_data: the density of data (prefactor 1) and randoms (-alpha);
+//                            Momentum 1: the data's w pv only; Momentum 2, 3: also the data's w_pv pv into
+//                            the momentum grid; each object and its copy shifted by half a cell
 //   src/read_data.c:514-745  add_to_grid's Survey branches: no wrap; a neighbour that reaches the axis
 //                            limit pulls the stencil back by one cell (:577-590, :672-688); the halo
 //                            slices past NX are discarded (no neighbour rank, src/main.c:1162-1188)
-//   src/main.c:472-775       compute_survey_power: the density times products of the unit vector r^
-//                            from the observer to every cell corner, one FFT per product
+//   src/main.c:472-775       compute_survey_power: the grids times products of the unit vector r^ from
+//                            the observer to every cell corner, one FFT per product (and per grid)
 //   src/main.c:781-967       assign_survey_power: interlacing combine, deconvolution, the products'
-//                            k^ factors, crossed with F0 (the monopole field) and binned
+//                            k^ factors, crossed with F0 (and F0_mom) and binned
 //
 // Multipoles through solid harmonics. For a unit k^, the reference builds
-//   F_l(k) = sum_r L_l(k^.r^) delta(r) e^{-ik.r}
+//   F_l(k) = sum_r L_l(k^.r^) f(r) e^{-ik.r}
 // from the Cartesian products r^_i r^_j ... (1, 3, 6, 10, 15 FFTs for l = 0..4). By the addition
 // theorem L_l(k^.u) = sum_m c_lm h_lm(k^) h_lm(u) with h_lm the 2l+1 real harmonic polynomials of
-// degree l (below), so F_l = sum_m c_lm h_lm(k^) FFT[h_lm(r^) delta] takes 1, 3, 5, 7, 9 FFTs. The two
+// degree l (below), so F_l = sum_m c_lm h_lm(k^) FFT[h_lm(r^) f] takes 1, 3, 5, 7, 9 FFTs. The two
 // forms agree on every cell with |r^| = 1. The cell whose corner is the observer (r2 == 0, where the
 // reference sets r2 = 1 and all its products vanish) enters the reference's P2 and P4 through the
-// constant terms of L_2 and L_4 only: L_l(0) delta_o e^{-ik.r_o}, added here in closed form. At k = 0
-// the reference skips every l > 0 product and keeps L_l(0) |F0|^2.
+// constant terms of L_2 and L_4 only: L_l(0) f_o e^{-ik.r_o}, added here in closed form. At k = 0 the
+// reference skips every l > 0 product. For the density (and Momentum 1) P_l = sum Re or Im(F_l conj F0),
+// and the constant terms of L_2 and L_4 at the other cells cancel against its l = 0 bins except at
+// k = 0. For the cross spectra (Momentum 2, 3) each product enters as half the sum of its density
+// against F0_mom and its momentum against F0, and that symmetric form of F0 against F0_mom vanishes, so
+// the reference's l = 0 terms -0.5 X0 and +0.375 X0 (X0 = its monopole power) stay in P2 and P4 at every
+// mode; the l = 0 pass adds them.
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <math.h>
@@ -31,24 +39,31 @@
 #include <string.h>
 
 #include <new>
-#include <vector>
 #include <type_traits>
+#include <vector>
 
 #include "ctx.cuh"
 
 // ------------------------------------------------------------------------------------ device state
 struct SvStats {
   double wsum[2], w2sum[2], w2nsum[2];  // [0] data, [1] randoms: sum w, w^2, w^2 nbar (src/main.c:151-163)
-  double ngrid[2];                      // sum of add_to_grid(...)/weight (src/read_data.c:488)
-  double dc[2];                         // FP64 sum of the deposits reaching the FFT input: main, interlaced
-  int nonfinite;                        // a non-finite coordinate, weight or number density
+  double vr, vrsq;                      // data: sum w w_pv pv, w^2 pv^2 (Momentum 1-3)
+  double w2npv[2];                      // sum w_pv^2 nbar: data (Momentum 1-3), randoms (Momentum 2)
+  double ngrid[2];                      // assign_survey_data's NGRID (src/read_data.c:474-491)
+  double dc[4];                         // FP64 sum of the deposits reaching the FFT input, per grid slot
+  int nonfinite;                        // a non-finite coordinate, weight, number density or velocity
   int pad;
 };
 
+// Catalogue arrays on the device. pv, pverr are null for Momentum 0.
 template <typename T>
 struct SvIn {
-  const T *x, *y, *z, *w, *nbar;
+  const T *x, *y, *z, *w, *nbar, *pv, *pverr;
 };
+
+// Grid slot of (stencil, field): stencil 0 normal, 1 interlaced; field 0 density, 1 momentum (Momentum 2, 3).
+// The periodic path's order, so that the FP32 paint context's grids are the survey's slots.
+__host__ __device__ __forceinline__ int sv_slot(int stencil, int field, int nf) { return stencil * nf + field; }
 
 // Real harmonic polynomials of degree l (m = 0 .. 2l) and the factors c_lm of
 // L_l(n.u) = sum_m c_lm h_lm(n) h_lm(u) for unit n and u.
@@ -171,90 +186,155 @@ __device__ __forceinline__ double sv_rsqrt(double a) { return rsqrt(a); }
 __device__ __forceinline__ float sv_mul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double sv_mul(double a, double b) { return __dmul_rn(a, b); }
 
-// compute_fkp (src/read_data.c:453-454) and the weight sums (src/main.c:151-163) of one catalogue:
-// the FKP factor in double, the weight stored back in the catalogue's type (float for the reference's
-// struct); w*w and w*w*nbar in that type, summed in double. which: 0 data, 1 randoms.
+// compute_fkp (src/read_data.c:450-466) and the weight sums (src/main.c:151-163) of one catalogue. The FKP
+// factors in double, the weights stored back in the catalogue's type (float for the reference's struct):
+//   Momentum 0: w *= 1/(1 + nbar FKP_Pk);
+//   Momentum 1: w *= 1/((pverr^2 + 300^2) + nbar FKP_Pk_mom), pverr^2 in the catalogue's type;
+//   Momentum 2, 3: with t = 1/(1 + nbar FKP_Pk), t_pv the Momentum 1 factor and the cross factor
+//     t_c = 1/sqrt(1 + t t_pv nbar nbar FKP_Pk_cross FKP_Pk_cross): w_pv = w t_pv t_c, w = w (t t_c).
+// The sums' products are in the catalogue's type, summed in double. which: 0 data, 1 randoms.
 template <typename T>
-__global__ void __launch_bounds__(256) k_sv_prepare(SvIn<T> in, long long n, int fkp, double fkp_pk, T *wout,
-                                                    SvStats *st, int which) {
-  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+__global__ void __launch_bounds__(256) k_sv_prepare(SvIn<T> in, long long n, int fkp, int mom, double pk, double pk_mom,
+                                                    double pk_cross, T *wout, T *wpvout, SvStats *st, int which) {
+  double s[6] = {0, 0, 0, 0, 0, 0};  // w, w^2, w^2 nbar, w w_pv pv, w^2 pv^2, w_pv^2 nbar
   int bad = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    T w = in.w[i];
+    T w = in.w[i], wpv = (T)0;
     const T nb = in.nbar[i];
+    const T pe = mom ? in.pverr[i] : (T)0;
     if (fkp) {
-      const double f = __ddiv_rn(1.0, __dadd_rn(1.0, __dmul_rn((double)nb, fkp_pk)));
-      w = (T)__dmul_rn((double)w, f);
+      const double nbd = (double)nb;
+      if (mom == 0) {
+        w = (T)__dmul_rn((double)w, __ddiv_rn(1.0, __dadd_rn(1.0, __dmul_rn(nbd, pk))));
+      } else {
+        const double tpv = __ddiv_rn(1.0, __dadd_rn(__dadd_rn((double)sv_mul(pe, pe), 90000.0), __dmul_rn(nbd, pk_mom)));
+        if (mom == 1) {
+          w = (T)__dmul_rn((double)w, tpv);
+        } else {
+          const double tw = __ddiv_rn(1.0, __dadd_rn(1.0, __dmul_rn(nbd, pk)));
+          const double q = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(tw, tpv), nbd), nbd), pk_cross), pk_cross);
+          const double tc = __ddiv_rn(1.0, __dsqrt_rn(__dadd_rn(1.0, q)));
+          wpv = (T)__dmul_rn(__dmul_rn((double)w, tpv), tc);
+          w = (T)__dmul_rn((double)w, __dmul_rn(tw, tc));
+          wpvout[i] = wpv;
+        }
+      }
       wout[i] = w;
     }
-    if (!isfinite((double)w) || !isfinite((double)nb)) bad = 1;
+    if (!isfinite((double)w) || !isfinite((double)nb) || !isfinite((double)pe)) bad = 1;
     const T ww = sv_mul(w, w);
-    s0 += (double)w;
-    s1 += (double)ww;
-    s2 += (double)sv_mul(ww, nb);
+    s[0] += (double)w;
+    s[1] += (double)ww;
+    s[2] += (double)sv_mul(ww, nb);
+    if (mom && which == 0) {
+      const T pv = in.pv[i];
+      if (!isfinite((double)pv)) bad = 1;
+      s[3] += (double)sv_mul(sv_mul(w, wpv), pv);
+      s[4] += (double)sv_mul(sv_mul(ww, pv), pv);
+      s[5] += (double)sv_mul(sv_mul(wpv, wpv), nb);
+    } else if (mom == 2 && which == 1) {
+      s[5] += (double)sv_mul(sv_mul(wpv, wpv), nb);
+    }
   }
-  const double v[3] = {s0, s1, s2};
-  double *const dst[3] = {&st->wsum[which], &st->w2sum[which], &st->w2nsum[which]};
-  sv_block_add<3>(v, dst);
+  double *const dst[6] = {&st->wsum[which], &st->w2sum[which], &st->w2nsum[which], &st->vr, &st->vrsq,
+                          &st->w2npv[which]};
+  if (which == 0) {
+    sv_block_add<6>(s, dst);
+  } else {
+    const double v[4] = {s[0], s[1], s[2], s[5]};
+    double *const d4[4] = {dst[0], dst[1], dst[2], dst[5]};
+    sv_block_add<4>(v, d4);
+  }
   if (bad) atomicOr(&st->nonfinite, 1);
 }
 
-// assign_survey_data (src/read_data.c:471-494) for the density: every object with weight
-// prefactor * w into grid 0 and, shifted by half a cell, into grid 1. The randoms' prefactor is
-// -alpha = -(sum w_data / sum w_rand) (src/main.c:169, 229), read from the sums on the device.
+// Grid pointers of a survey paint: the slots of sv_slot.
+template <typename R>
+struct SvGrids {
+  R *g[4];
+};
+
+// assign_survey_data (src/read_data.c:471-494), FP64: each object and, half a cell up, its interlaced copy.
+// Momentum 1 (data only): w pv into the density slots, NGRID += add_to_grid / (pv w) (a product in the
+// catalogue's type). Otherwise prefactor w into the density slots, NGRID += add_to_grid / w, and for the
+// data of Momentum 2, 3 also w_pv pv into the momentum slots. The randoms' prefactor is -alpha =
+// -(sum w_data / sum w_rand) (src/main.c:169, 229), read from the sums on the device.
 template <typename T, typename R>
-__global__ void __launch_bounds__(256) k_sv_paint(Geom g, SvIn<T> in, const T *wk, long long n, int which, R *g0,
-                                                  R *g1, SvStats *st) {
+__global__ void __launch_bounds__(256) k_sv_paint(Geom g, SvIn<T> in, const T *wk, const T *wpv, long long n, int which,
+                                                  int mom, int nf, SvGrids<R> gr, SvStats *st) {
   const double pref = which ? -__ddiv_rn(st->wsum[0], st->wsum[1]) : 1.0;
-  double l_ngrid = 0.0, l_dc0 = 0.0, l_dc1 = 0.0;
+  double l_ngrid = 0.0, l_dc[4] = {0, 0, 0, 0};
   int bad = 0;
+  const int sd0 = sv_slot(0, 0, nf), sd1 = sv_slot(1, 0, nf), sm0 = sv_slot(0, 1, nf), sm1 = sv_slot(1, 1, nf);
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const double x = (double)in.x[i], y = (double)in.y[i], z = (double)in.z[i], w = (double)wk[i];
     if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
       bad = 1;
       continue;
     }
-    const double wp = __dmul_rn(pref, w);
-    AxisTaps ax, ay, az;
-    double got = 0.0;
-    if (exact_axes(g, x, y, z, ax, ay, az)) {
-      l_dc0 += sv_deposit(g, g0, wp, ax, ay, az);
-      got = wp;
+    double dval, got = 0.0;  // the density slots' deposit value (add_to_grid's w * vr)
+    double div;
+    if (mom == 1) {
+      dval = __dmul_rn(w, __dmul_rn(pref, (double)in.pv[i]));
+      div = (double)sv_mul(in.pv[i], wk[i]);
+    } else {
+      dval = __dmul_rn(pref, w);
+      div = w;
     }
-    l_ngrid += __ddiv_rn(got, w);
-    if (g.interlace && exact_axes(g, DADD(x, g.hx), DADD(y, g.hy), DADD(z, g.hz), ax, ay, az))
-      l_dc1 += sv_deposit(g, g1, wp, ax, ay, az);
+    const bool mfield = mom >= 2 && which == 0;
+    const double mval = mfield ? __dmul_rn((double)wpv[i], __dmul_rn(pref, (double)in.pv[i])) : 0.0;
+    AxisTaps ax, ay, az;
+    if (exact_axes(g, x, y, z, ax, ay, az)) {
+      l_dc[sd0] += sv_deposit(g, gr.g[sd0], dval, ax, ay, az);
+      if (mfield) l_dc[sm0] += sv_deposit(g, gr.g[sm0], mval, ax, ay, az);
+      got = mom == 1 ? w : dval;
+    }
+    l_ngrid += __ddiv_rn(got, div);
+    if (g.interlace && exact_axes(g, DADD(x, g.hx), DADD(y, g.hy), DADD(z, g.hz), ax, ay, az)) {
+      l_dc[sd1] += sv_deposit(g, gr.g[sd1], dval, ax, ay, az);
+      if (mfield) l_dc[sm1] += sv_deposit(g, gr.g[sm1], mval, ax, ay, az);
+    }
   }
-  const double v[3] = {l_ngrid, l_dc0, l_dc1};
-  double *const dst[3] = {&st->ngrid[which], &st->dc[0], &st->dc[1]};
-  sv_block_add<3>(v, dst);
+  const double v[5] = {l_ngrid, l_dc[0], l_dc[1], l_dc[2], l_dc[3]};
+  double *const dst[5] = {&st->ngrid[which], &st->dc[0], &st->dc[1], &st->dc[2], &st->dc[3]};
+  sv_block_add<5>(v, dst);
   if (bad) atomicOr(&st->nonfinite, 1);
 }
 
-// The FP32 paint takes data and randoms as one catalogue for the tile kernels: this writes object i of
-// one catalogue at off + i of the combined float arrays, with the weight prefactor * w already applied
-// (1 for data, -alpha for randoms, as k_sv_paint), and adds its assign_survey_data counter: the object
-// counts w/w when add_to_grid accepts it (src/read_data.c:488; acceptance only, no taps).
+// The FP32 paint takes data and randoms as one catalogue for the tile kernels: this writes object i of one
+// catalogue at off + i of the combined float arrays with the weight of its density deposit (prefactor w;
+// Momentum 1: w pv) and, for Momentum 2, 3, the v with w v = w_pv pv (the tile kernels' second field is
+// w v; 0 for randoms), and adds its assign_survey_data counter (acceptance only, no taps).
 template <typename T>
-__global__ void __launch_bounds__(256) k_sv_combine(Geom g, SvIn<T> in, const T *wk, long long n, int which,
-                                                    long long off, float *cx, float *cy, float *cz, float *cw,
-                                                    SvStats *st) {
+__global__ void __launch_bounds__(256) k_sv_combine(Geom g, SvIn<T> in, const T *wk, const T *wpv, long long n,
+                                                    int which, int mom, long long off, float *cx, float *cy, float *cz,
+                                                    float *cw, float *cv, SvStats *st) {
   const double pref = which ? -__ddiv_rn(st->wsum[0], st->wsum[1]) : 1.0;
   double l_ngrid = 0.0;
   int bad = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const double x = (double)in.x[i], y = (double)in.y[i], z = (double)in.z[i], w = (double)wk[i];
     if (!(isfinite(x) && isfinite(y) && isfinite(z))) bad = 1;
-    const double wp = __dmul_rn(pref, w);
     const bool acc = g.order == 1 ? !((x < g.xmin) || (x >= g.xmax_l) || (y < g.ymin) || (y >= g.ymax) ||
                                       (z < g.zmin) || (z >= g.zmax))
                                   : (survey_accept_axis(g, 0, x) && survey_accept_axis(g, 1, y) &&
                                      survey_accept_axis(g, 2, z));
-    l_ngrid += __ddiv_rn(acc ? wp : 0.0, w);
+    double wp;
+    if (mom == 1) {
+      wp = __dmul_rn(w, (double)in.pv[i]);
+      l_ngrid += __ddiv_rn(acc ? w : 0.0, (double)sv_mul(in.pv[i], wk[i]));
+    } else {
+      wp = __dmul_rn(pref, w);
+      l_ngrid += __ddiv_rn(acc ? wp : 0.0, w);
+    }
     cx[off + i] = (float)x;
     cy[off + i] = (float)y;
     cz[off + i] = (float)z;
     cw[off + i] = (float)wp;
+    if (mom >= 2) {
+      const double mv = which == 0 ? __dmul_rn((double)wpv[i], (double)in.pv[i]) : 0.0;
+      cv[off + i] = (wp != 0.0) ? (float)__ddiv_rn(mv, wp) : 0.0f;
+    }
   }
   const double v[1] = {l_ngrid};
   double *const dst[1] = {&st->ngrid[which]};
@@ -263,11 +343,11 @@ __global__ void __launch_bounds__(256) k_sv_combine(Geom g, SvIn<T> in, const T 
 }
 
 // ------------------------------------------------------------------------ weighted term grids
-// w[c] = a[c] h_lm(r^) for every cell c = (ix, iy, iz < NZ) of the painted grid(s), r^ the unit vector
-// from the observer to the cell corner (ix dx + XMIN - X_Origin, ...) (src/main.c:551-559 and the
-// other product loops). A corner at the observer (r2 == 0) gets r2 = 1, as in the reference, so its
-// harmonics vanish. l = 0 copies the grid (src/main.c:503-511). One warp per (x, y) row, grid-stride
-// over rows; each lane moves z pairs (rows have an even length, so pairs are aligned vector loads).
+// w[c] = a[c] h_lm(r^) for every cell c = (ix, iy, iz < NZ) of a painted grid (and its interlaced copy),
+// r^ the unit vector from the observer to the cell corner (ix dx + XMIN - X_Origin, ...) (src/main.c:551-559
+// and the other product loops). A corner at the observer (r2 == 0) gets r2 = 1, as in the reference, so its
+// harmonics vanish. l = 0 copies the grid (src/main.c:503-511). One warp per (x, y) row, grid-stride over
+// rows; each lane moves z pairs (rows have an even length, so pairs are aligned vector loads).
 template <typename R>
 __device__ __forceinline__ R sv_cell_weight(int l, int m, R px, R py, R pxy, R pz) {
   R r2 = pxy + pz * pz;
@@ -328,28 +408,41 @@ struct SvC<double> {
 template <typename R>
 struct SvAssign {
   typedef typename SvC<R>::C C;
-  const C *g0, *g1;     // transformed term grid(s) [NX][NY][NZ/2+1]
-  C *F0;                // monopole field (the l = 0 pass writes it)
-  const double *dc;     // exact DC of the painted grid(s): the l = 0 pass's k = 0 mode
+  const C *gd0, *gd1;   // transformed density term grid(s) [NX][NY][NZ/2+1]: normal, interlaced
+  const C *gm0, *gm1;   // the momentum term grids (Momentum 2, 3)
+  C *F0, *F0m;          // monopole fields (the l = 0 pass writes them)
+  const double *dc;     // exact DC of each painted slot: the l = 0 pass's k = 0 mode
+  int sd0, sd1, sm0, sm1;  // slots of dc and of the painted grids
   R coef;               // c_lm
   int m;
   // the observer's cell (l = 0 pass only): painted values there and e^{-2 pi i q o/N} per axis
   int origin;
-  const R *a0, *a1;
+  const R *a[4];        // painted grids by slot
   long long oind;
   const C *ox, *oy, *oz;
 };
 
 constexpr int SV_ICHUNK = 128;
 
-// assign_survey_power (src/main.c:781-967) for one FFT set. L = 0: F0 = the interlacing-combined
-// field, P0 += w |F0|^2; at k = 0 also P2 += L_2(0) w |F0|^2 and P4 += L_4(0) w |F0|^2; elsewhere the
-// observer cell's closed-form term for P2 and P4. L > 0: P_L += w c_lm h_lm(k^) X.F0 for k != 0, with
-// X.F0 = Re(X conj F0) for even L and dkr F0i - dki F0r for odd L (src/main.c:908-917). w = NM times
-// the deconvolution (times 0.25 when interlacing, :890-899). One thread per (ky, kz) column walks x
-// over a chunk of SV_ICHUNK; bin sums run per thread over equal-bin stretches, then per CTA in shared
-// memory, then FP64 global atomics. Modes beyond the top bin edge are skipped as in k_bin.
-template <typename R, int L>
+template <typename C, typename R>
+__device__ __forceinline__ R sv_imf(const C &a, const C &b) { return a.x * b.y - a.y * b.x; }
+template <typename C, typename R>
+__device__ __forceinline__ R sv_ref(const C &a, const C &b) { return a.x * b.x + a.y * b.y; }
+
+// assign_survey_power (src/main.c:781-967) for one FFT set; the power forms of :870-887. w = NM times the
+// deconvolution (times 0.25 when interlacing, :890-899).
+//  Density (CROSS false). L = 0: F0 = the interlacing-combined field, P0 += w |F0|^2; at k = 0 also
+//   P2 += L_2(0) w |F0|^2, P4 += L_4(0) w |F0|^2; elsewhere the observer cell's closed-form term.
+//   L > 0: P_L += w c_lm h_lm(k^) X.F0 for k != 0, X.F0 = Re(X conj F0) for even L, dkr F0i - dki F0r
+//   for odd L.
+//  Cross (Momentum 2, 3). L = 0: F0, F0m = the combined density and momentum fields, X0 = Im(conj F0 F0m),
+//   P0 += w X0, P2 -= 0.5 w X0, P4 += 0.375 w X0 at every mode, and the observer cell's term.
+//   L > 0: P_L += w c_lm h_lm(k^) (G_d.F0m + G_m.F0) / 2, with the Re form for odd L and the Im form
+//   (a.r b.i - a.i b.r) for even L.
+// One thread per (ky, kz) column walks x over a chunk of SV_ICHUNK; bin sums run per thread over equal-bin
+// stretches, then per CTA in shared memory, then FP64 global atomics. Modes beyond the top bin edge are
+// skipped as in k_bin.
+template <typename R, int L, bool CROSS>
 __global__ void __launch_bounds__(256) k_sv_assign(BinParams bp, BinTables t, SvAssign<R> sa, double *bins) {
   typedef typename SvC<R>::C C;
   constexpr bool F32 = sizeof(R) == 4;
@@ -403,14 +496,19 @@ __global__ void __launch_bounds__(256) k_sv_assign(BinParams bp, BinTables t, Sv
       eyz.y = a.x * b.y + a.y * b.x;
     }
     const R fy = F32 ? (R)t.fyf[j] : (R)t.fyd[j], fz = F32 ? (R)t.fzf[k] : (R)t.fzd[k];
-    C oyz, o0, o1;
-    oyz.x = oyz.y = o0.x = o0.y = o1.x = o1.y = (R)0;
+    C oyz;
+    R od0 = (R)0, od1 = (R)0, om0 = (R)0, om1 = (R)0;  // painted values at the observer's cell
+    oyz.x = oyz.y = (R)0;
     if (L == 0 && sa.origin) {
       const C a = sa.oy[j], b = sa.oz[k];
       oyz.x = a.x * b.x - a.y * b.y;
       oyz.y = a.x * b.y + a.y * b.x;
-      o0.x = sa.a0[sa.oind];
-      if (bp.interlace) o1.x = sa.a1[sa.oind];
+      od0 = sa.a[sa.sd0][sa.oind];
+      if (bp.interlace) od1 = sa.a[sa.sd1][sa.oind];
+      if (CROSS) {
+        om0 = sa.a[sa.sm0][sa.oind];
+        if (bp.interlace) om1 = sa.a[sa.sm1][sa.oind];
+      }
     }
     const long long base = (long long)j * bp.nzc + k;
     R acc0 = (R)0, acc2 = (R)0, acc4 = (R)0;
@@ -468,45 +566,89 @@ __global__ void __launch_bounds__(256) k_sv_assign(BinParams bp, BinTables t, Sv
       C e;
       e.x = ex.x * eyz.x - ex.y * eyz.y;
       e.y = ex.x * eyz.y + ex.y * eyz.x;
-      C X = sa.g0[off];
+      C X = sa.gd0[off], M;
+      M.x = M.y = (R)0;
       if (L == 0 && kzero) {
-        X.x = (R)sa.dc[0];
+        X.x = (R)sa.dc[sa.sd0];
         X.y = (R)0;
       }
-      if (bp.interlace) {
-        C a = sa.g1[off];
+      if (CROSS) {
+        M = sa.gm0[off];
         if (L == 0 && kzero) {
-          a.x = (R)sa.dc[1];
+          M.x = (R)sa.dc[sa.sm0];
+          M.y = (R)0;
+        }
+      }
+      if (bp.interlace) {
+        C a = sa.gd1[off];
+        if (L == 0 && kzero) {
+          a.x = (R)sa.dc[sa.sd1];
           a.y = (R)0;
         }
         X.x += a.x * e.x - a.y * e.y;
         X.y += a.x * e.y + a.y * e.x;
+        if (CROSS) {
+          C b = sa.gm1[off];
+          if (L == 0 && kzero) {
+            b.x = (R)sa.dc[sa.sm1];
+            b.y = (R)0;
+          }
+          M.x += b.x * e.x - b.y * e.y;
+          M.y += b.x * e.y + b.y * e.x;
+        }
       }
       const R gc = cyz * scx[li] * (R)herm_nm(i, j, k, bp.xhalf);
       if (L == 0) {
         sa.F0[off] = X;
-        const R p = (X.x * X.x + X.y * X.y) * gc;
-        acc0 += p;
-        if (kzero) {
-          acc2 += (R)-0.5 * p;
-          acc4 += (R)0.375 * p;
-        } else if (sa.origin) {
-          // O = (delta_o + e delta_o,interlaced) e^{-i k.r_o}
-          C O = o0;
-          O.x += o1.x * e.x;
-          O.y += o1.x * e.y;
+        if (CROSS) sa.F0m[off] = M;
+        // the observer cell's closed-form field, O = (f_o + e f_o,interlaced) e^{-i k.r_o}
+        C q;
+        q.x = q.y = (R)0;
+        if (sa.origin && !kzero) {
           const C ph = sox[li];
-          C q;
           q.x = ph.x * oyz.x - ph.y * oyz.y;
           q.y = ph.x * oyz.y + ph.y * oyz.x;
-          const R orr = O.x * q.x - O.y * q.y, oii = O.x * q.y + O.y * q.x;
-          const R pc = (orr * X.x + oii * X.y) * gc;
-          acc2 += (R)-0.5 * pc;
-          acc4 += (R)0.375 * pc;
+        }
+        if (!CROSS) {
+          const R p = (X.x * X.x + X.y * X.y) * gc;
+          acc0 += p;
+          if (kzero) {
+            acc2 += (R)-0.5 * p;
+            acc4 += (R)0.375 * p;
+          } else if (sa.origin) {
+            C O;
+            O.x = (od0 + od1 * e.x) * q.x - (od1 * e.y) * q.y;
+            O.y = (od0 + od1 * e.x) * q.y + (od1 * e.y) * q.x;
+            const R pc = sv_ref<C, R>(O, X) * gc;
+            acc2 += (R)-0.5 * pc;
+            acc4 += (R)0.375 * pc;
+          }
+        } else {
+          const R x0 = sv_imf<C, R>(X, M) * gc;
+          acc0 += x0;
+          acc2 += (R)-0.5 * x0;
+          acc4 += (R)0.375 * x0;
+          if (sa.origin && !kzero) {
+            C Od, Om;
+            Od.x = (od0 + od1 * e.x) * q.x - (od1 * e.y) * q.y;
+            Od.y = (od0 + od1 * e.x) * q.y + (od1 * e.y) * q.x;
+            Om.x = (om0 + om1 * e.x) * q.x - (om1 * e.y) * q.y;
+            Om.y = (om0 + om1 * e.x) * q.y + (om1 * e.y) * q.x;
+            const R pc = (R)0.5 * (sv_imf<C, R>(Od, M) + sv_imf<C, R>(Om, X)) * gc;
+            acc2 += (R)-0.5 * pc;
+            acc4 += (R)0.375 * pc;
+          }
         }
       } else {
-        const C F = sa.F0[off];
-        const R v = (L & 1) ? X.x * F.y - X.y * F.x : X.x * F.x + X.y * F.y;
+        R v;
+        if (!CROSS) {
+          const C F = sa.F0[off];
+          v = (L & 1) ? sv_imf<C, R>(X, F) : sv_ref<C, R>(X, F);
+        } else {
+          const C F = sa.F0[off], Fm = sa.F0m[off];
+          v = (L & 1) ? (R)0.5 * (sv_ref<C, R>(X, Fm) + sv_ref<C, R>(M, F))
+                      : (R)0.5 * (sv_imf<C, R>(X, Fm) + sv_imf<C, R>(M, F));
+        }
         const R inv = sv_rsqrt(s);
         const R hv = harm<R>(L, sa.m, sfx[li] * inv, fy * inv, fz * inv);
         acc0 += gc * sa.coef * hv * v;
@@ -531,23 +673,27 @@ __global__ void __launch_bounds__(256) k_sv_assign(BinParams bp, BinTables t, Sv
 }
 
 // ------------------------------------------------------------------------------------ the context
+#define SV_STAGE 9  // staged arrays per catalogue: x, y, z, w, nbar, pv, pverr, FKP w, FKP w_pv
+
 struct capow_survey_ctx {
   capow_params p;
   capow_survey_params sv;
   capow_options o;
   int prec;  // CAPOW_FP64 or CAPOW_FP32_MIXED
+  int mom;   // Momentum 0..3
+  int nf;    // painted fields: 1, or 2 (density and momentum) for Momentum 2, 3
   Geom g;
   BinParams bp;
   BinTables bt;
-  int nslot;  // 1 + DoInterlacing
+  int nslot;  // nf * (1 + DoInterlacing)
   cudaStream_t stream;
   bool own_stream;
   void *paint;  // nslot painted grids, main_sz reals each (FP32: the paint context's grids)
   capow_ctx *pc;  // FP32: the paint-only context whose tile kernels paint data and randoms
-  float *comb;    // FP32: the combined catalogue for it, [x | y | z | w] of comb_cap objects each
+  float *comb;    // FP32: the combined catalogue for it, [x | y | z | w | v] of comb_cap objects each
   size_t comb_cap;
   void *work;   // nslot term grids
-  void *F0;     // main_sz reals (complex [NX][NY][NZ/2+1])
+  void *F0, *F0m;  // main_sz reals each (complex [NX][NY][NZ/2+1]); F0m for Momentum 2, 3
   void *vx, *vy, *vz;  // cell-corner offsets from the observer per axis (R)
   SvStats *st;
   double *bins;  // [5][nk]
@@ -559,9 +705,8 @@ struct capow_survey_ctx {
   int origin;
   long long oind;
   void *ox, *oy, *oz;
-  // staging of host catalogues and the FKP-weighted copies: [catalogue][x, y, z, w, nbar, wfkp]
-  void *stage[2][6];
-  size_t stage_bytes[2][6];
+  void *stage[2][SV_STAGE];
+  size_t stage_bytes[2][SV_STAGE];
   double *h_bins;
   SvStats *h_st;
   std::vector<void *> allocs;
@@ -586,6 +731,7 @@ static int sv_validate(const capow_params *p, const capow_survey_params *sv, con
     snprintf(err, n, __VA_ARGS__); \
     return code;                   \
   } while (0)
+  if (!sv) BAD(CAPOW_EINVAL, "no survey parameters");
   if (p->InterpOrder < 1 || p->InterpOrder > 3) BAD(CAPOW_EINVAL, "InterpOrder is neither 1, 2 nor 3");
   if (p->DoInterlacing != 0 && p->DoInterlacing != 1) BAD(CAPOW_EINVAL, "DoInterlacing is neither 0 nor 1");
   if (p->Output2D != 0 && p->Output2D != 1) BAD(CAPOW_EINVAL, "Output2D is neither 0 nor 1");
@@ -595,11 +741,12 @@ static int sv_validate(const capow_params *p, const capow_survey_params *sv, con
   if (p->NK > 512) BAD(CAPOW_ENOTSUP, "the survey binning holds at most 512 k bins");
   if (!(p->XMAX > p->XMIN) || !(p->YMAX > p->YMIN) || !(p->ZMAX > p->ZMIN)) BAD(CAPOW_EINVAL, "box MAX must exceed MIN");
   if (p->Maxk < p->Mink) BAD(CAPOW_EINVAL, "Maxk is less than Mink");
-  if (p->Momentum != 0) BAD(CAPOW_ENOTSUP, "the survey estimator is provided for the density (Momentum 0) only");
+  if (p->Momentum < 0 || p->Momentum > 3) BAD(CAPOW_ENOTSUP, "the survey estimator has Momentum 0 to 3");
+  if (p->Momentum >= 2 && sv->FKP_Column >= 0)
+    BAD(CAPOW_EINVAL, "survey Momentum 2 and 3 need the FKP weights (FKP_Column < 0): w_pv is set by them only");
   if (o->precision != CAPOW_FP64 && o->precision != CAPOW_FP32_MIXED)
     BAD(CAPOW_ENOTSUP, "survey precision must be CAPOW_FP64 or CAPOW_FP32_MIXED");
   if ((long long)p->NX * p->NY * 2 * (p->NZ / 2 + 1) >= (1LL << 40)) BAD(CAPOW_EINVAL, "grid too large");
-  if (!sv) BAD(CAPOW_EINVAL, "no survey parameters");
   return CAPOW_OK;
 #undef BAD
 }
@@ -634,6 +781,8 @@ extern "C" int capow_survey_create(const capow_params *p, const capow_survey_par
   c->sv = *sv;
   c->o = o;
   c->prec = o.precision;
+  c->mom = p->Momentum;
+  c->nf = c->mom >= 2 ? 2 : 1;
   *out = c;  // from here on capow_survey_destroy releases partial state
   CK(c, cudaSetDevice(o.device));
   if (o.stream) {
@@ -647,7 +796,7 @@ extern "C" int capow_survey_create(const capow_params *p, const capow_survey_par
   c->g = make_geom(*p);
   c->g.los = 4;  // no RSD shift, no wrap, the halo discarded
   c->g.survey = 1;
-  c->nslot = 1 + p->DoInterlacing;
+  c->nslot = c->nf * (1 + p->DoInterlacing);
   const bool f64 = c->prec == CAPOW_FP64;
   const size_t eb = f64 ? 8 : 4;
   const size_t ge = (size_t)c->g.main_sz;
@@ -656,19 +805,21 @@ extern "C" int capow_survey_create(const capow_params *p, const capow_survey_par
   } else {  // the FP32 grids are painted by the tile kernels of a paint-only context on this stream
     capow_options po = o;
     po.stream = (void *)c->stream;
-    rc = create_paint_ctx(p, &po, 1, &c->pc);
+    rc = create_paint_ctx(p, &po, c->nf, &c->pc);
     if (rc) FAIL(c, rc, "paint context: %s", c->pc ? capow_last_error(c->pc) : "invalid parameters");
     c->paint = c->pc->grid_base;
   }
   c->work = sv_dalloc(c, eb * ge * c->nslot);
   c->F0 = sv_dalloc(c, eb * ge);
+  if (c->nf == 2) c->F0m = sv_dalloc(c, eb * ge);
   c->st = (SvStats *)sv_dalloc(c, sizeof(SvStats));
   const int nk = p->NK;
   c->bins = (double *)sv_dalloc(c, sizeof(double) * 5 * nk);
   c->nmodes_d = (unsigned long long *)sv_dalloc(c, sizeof(unsigned long long) * nk);
   c->nmodes2d_d = (unsigned long long *)sv_dalloc(c, sizeof(unsigned long long));
-  if (!c->paint || !c->work || !c->F0 || !c->st || !c->bins || !c->nmodes_d || !c->nmodes2d_d)
-    FAIL(c, CAPOW_ENOMEM, "device allocation failed (grids need %.2f GB)", eb * ge * (2.0 * c->nslot + 1) / 1e9);
+  if (!c->paint || !c->work || !c->F0 || (c->nf == 2 && !c->F0m) || !c->st || !c->bins || !c->nmodes_d ||
+      !c->nmodes2d_d)
+    FAIL(c, CAPOW_ENOMEM, "device allocation failed (grids need %.2f GB)", eb * ge * (2.0 * c->nslot + c->nf) / 1e9);
   CK(c, cudaMallocHost((void **)&c->h_bins, sizeof(double) * 5 * nk));
   CK(c, cudaMallocHost((void **)&c->h_st, sizeof(SvStats)));
   // corner offsets per axis, and the observer's cell: the corner whose three offsets square to 0
@@ -741,8 +892,8 @@ extern "C" int capow_survey_create(const capow_params *p, const capow_survey_par
   CK(c, cudaMemcpyAsync(c->nmodes.data(), c->nmodes_d, sizeof(unsigned long long) * nk, cudaMemcpyDeviceToHost,
                         c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
-  // one batched in-place real-to-complex plan over the nslot term grids (fftw_execute of plan and
-  // plan_interlace, src/main.c:513-514 and the product loops)
+  // one batched in-place real-to-complex plan over the nslot term grids (fftw_execute of plan, plan_interlace,
+  // plan_mom and plan_mom_interlace, src/main.c:513-526 and the product loops)
   int n[3] = {p->NX, p->NY, p->NZ};
   int inembed[3] = {p->NX, p->NY, 2 * bp.nzc}, onembed[3] = {p->NX, p->NY, bp.nzc};
   const long long idist = (long long)ge, odist = (long long)ge / 2;
@@ -766,7 +917,7 @@ extern "C" void capow_survey_destroy(capow_survey_ctx *c) {
   if (c->comb) cudaFree(c->comb);
   for (void *q : c->allocs) cudaFree(q);
   for (int a = 0; a < 2; a++)
-    for (int k = 0; k < 6; k++)
+    for (int k = 0; k < SV_STAGE; k++)
       if (c->stage[a][k]) cudaFree(c->stage[a][k]);
   if (c->h_bins) cudaFreeHost(c->h_bins);
   if (c->h_st) cudaFreeHost(c->h_st);
@@ -779,22 +930,14 @@ extern "C" void capow_survey_destroy(capow_survey_ctx *c) {
 extern "C" const char *capow_survey_last_error(const capow_survey_ctx *c) { return c ? c->err : "no context"; }
 extern "C" int64_t capow_survey_kernel_launches(const capow_survey_ctx *c) { return c ? c->launches : 0; }
 
-// device copy of one catalogue array (host input) in staging slot [cat][k]
-static int sv_stage(capow_survey_ctx *c, int cat, int k, const void *src, size_t bytes, bool on_device,
-                    const void **dst) {
-  if (on_device) {
-    *dst = src;
-    return CAPOW_OK;
-  }
-  if (c->stage_bytes[cat][k] < bytes) {
-    if (c->stage[cat][k]) cudaFree(c->stage[cat][k]);
-    c->stage[cat][k] = nullptr;
-    c->stage_bytes[cat][k] = 0;
-    CK(c, cudaMalloc(&c->stage[cat][k], bytes ? bytes : 16));
-    c->stage_bytes[cat][k] = bytes;
-  }
-  if (bytes) CK(c, cudaMemcpyAsync(c->stage[cat][k], src, bytes, cudaMemcpyHostToDevice, c->stream));
-  *dst = c->stage[cat][k];
+// a device buffer of at least `bytes` in staging slot [cat][k]
+static int sv_stage_buffer(capow_survey_ctx *c, int cat, int k, size_t bytes) {
+  if (c->stage_bytes[cat][k] >= bytes && c->stage[cat][k]) return CAPOW_OK;
+  if (c->stage[cat][k]) cudaFree(c->stage[cat][k]);
+  c->stage[cat][k] = nullptr;
+  c->stage_bytes[cat][k] = 0;
+  CK(c, cudaMalloc(&c->stage[cat][k], bytes ? bytes : 16));
+  c->stage_bytes[cat][k] = bytes;
   return CAPOW_OK;
 }
 
@@ -804,82 +947,101 @@ static int sv_blocks(long long n) {
   return b < 1 ? 1 : (int)b;
 }
 
-template <typename T, typename R>
-static int sv_enqueue_catalogue(capow_survey_ctx *c, int cat, const capow_survey_catalogue *in) {
-  const size_t n = in->n, bytes = sizeof(T) * n;
-  const void *src[5] = {in->x, in->y, in->z, in->w, in->nbar};
-  const void *d[5];
-  for (int k = 0; k < 5; k++) {
-    int rc = sv_stage(c, cat, k, src[k], bytes, in->on_device != 0, &d[k]);
+// The device view of one catalogue: device arrays as given, host arrays copied into the staging slots.
+// *wk and *wpv are the weights to paint: the FKP-weighted copies when FKP_Column < 0.
+template <typename T>
+static int sv_device_view(capow_survey_ctx *c, int cat, const capow_survey_catalogue *in, bool copy, SvIn<T> *sin,
+                          const T **wk, const T **wpv) {
+  const size_t bytes = sizeof(T) * in->n;
+  const void *src[7] = {in->x, in->y, in->z, in->w, in->nbar, in->pv, in->pverr};
+  const void *d[7];
+  for (int k = 0; k < 7; k++) {
+    if (k >= 5 && !c->mom) {  // pv, pverr: Momentum 1-3 only
+      d[k] = nullptr;
+      continue;
+    }
+    if (!src[k] || in->on_device) {
+      d[k] = src[k];
+      continue;
+    }
+    if (copy) {
+      int rc = sv_stage_buffer(c, cat, k, bytes);
+      if (rc) return rc;
+      if (bytes) CK(c, cudaMemcpyAsync(c->stage[cat][k], src[k], bytes, cudaMemcpyHostToDevice, c->stream));
+    }
+    d[k] = c->stage[cat][k];
+  }
+  *sin = SvIn<T>{(const T *)d[0], (const T *)d[1], (const T *)d[2], (const T *)d[3], (const T *)d[4], (const T *)d[5],
+                 (const T *)d[6]};
+  const bool fkp = c->sv.FKP_Column < 0;
+  if (fkp && copy) {
+    int rc = sv_stage_buffer(c, cat, 7, bytes);
+    if (!rc && c->mom >= 2) rc = sv_stage_buffer(c, cat, 8, bytes);
     if (rc) return rc;
   }
-  SvIn<T> sin{(const T *)d[0], (const T *)d[1], (const T *)d[2], (const T *)d[3], (const T *)d[4]};
-  const int fkp = c->sv.FKP_Column < 0;
-  const T *wk = sin.w;
-  if (fkp) {
-    if (c->stage_bytes[cat][5] < bytes) {
-      if (c->stage[cat][5]) cudaFree(c->stage[cat][5]);
-      c->stage[cat][5] = nullptr;
-      c->stage_bytes[cat][5] = 0;
-      CK(c, cudaMalloc(&c->stage[cat][5], bytes ? bytes : 16));
-      c->stage_bytes[cat][5] = bytes;
-    }
-    wk = (const T *)c->stage[cat][5];
-  }
-  if (n) {
-    k_sv_prepare<T><<<sv_blocks(n), 256, 0, c->stream>>>(sin, (long long)n, fkp, c->sv.FKP_Pk, (T *)wk, c->st, cat);
+  *wk = fkp ? (const T *)c->stage[cat][7] : sin->w;
+  *wpv = c->mom >= 2 ? (const T *)c->stage[cat][8] : nullptr;
+  return CAPOW_OK;
+}
+
+template <typename T>
+static int sv_enqueue_catalogue(capow_survey_ctx *c, int cat, const capow_survey_catalogue *in) {
+  SvIn<T> sin;
+  const T *wk, *wpv;
+  int rc = sv_device_view<T>(c, cat, in, true, &sin, &wk, &wpv);
+  if (rc) return rc;
+  if (in->n) {
+    k_sv_prepare<T><<<sv_blocks(in->n), 256, 0, c->stream>>>(sin, (long long)in->n, c->sv.FKP_Column < 0, c->mom,
+                                                             c->sv.FKP_Pk, c->sv.FKP_Pk_mom, c->sv.FKP_Pk_cross,
+                                                             (T *)wk, (T *)wpv, c->st, cat);
     c->launches++;
   }
   return CAPOW_OK;
 }
 
-// the device view of one catalogue after sv_enqueue_catalogue (staged copies for host input) and the
-// weights to paint (the FKP-weighted copy when FKP_Column < 0)
-template <typename T>
-static SvIn<T> sv_device_view(capow_survey_ctx *c, int cat, const capow_survey_catalogue *in, const T **wk) {
-  const void *src[5] = {in->x, in->y, in->z, in->w, in->nbar};
-  const void *d[5];
-  for (int k = 0; k < 5; k++) d[k] = in->on_device ? src[k] : c->stage[cat][k];
-  SvIn<T> sin{(const T *)d[0], (const T *)d[1], (const T *)d[2], (const T *)d[3], (const T *)d[4]};
-  *wk = c->sv.FKP_Column < 0 ? (const T *)c->stage[cat][5] : sin.w;
-  return sin;
-}
-
 // FP64: every object with global FP64 atomics (k_sv_paint), the reference's per-object double products.
 template <typename T, typename R>
-static void sv_launch_paint(capow_survey_ctx *c, int cat, const capow_survey_catalogue *in) {
-  const size_t n = in->n;
-  if (!n) return;
-  const T *wk;
-  SvIn<T> sin = sv_device_view<T>(c, cat, in, &wk);
-  R *g0 = (R *)c->paint, *g1 = c->nslot > 1 ? (R *)c->paint + c->g.main_sz : nullptr;
-  k_sv_paint<T, R><<<sv_blocks(n), 256, 0, c->stream>>>(c->g, sin, wk, (long long)n, cat, g0, g1, c->st);
+static int sv_launch_paint(capow_survey_ctx *c, int cat, const capow_survey_catalogue *in) {
+  if (!in->n) return CAPOW_OK;
+  SvIn<T> sin;
+  const T *wk, *wpv;
+  int rc = sv_device_view<T>(c, cat, in, false, &sin, &wk, &wpv);
+  if (rc) return rc;
+  SvGrids<R> gr;
+  for (int s = 0; s < 4; s++) gr.g[s] = s < c->nslot ? (R *)c->paint + s * c->g.main_sz : nullptr;
+  k_sv_paint<T, R><<<sv_blocks(in->n), 256, 0, c->stream>>>(c->g, sin, wk, wpv, (long long)in->n, cat, c->mom, c->nf,
+                                                            gr, c->st);
   c->launches++;
+  return CAPOW_OK;
 }
 
-// FP32: data and randoms combined into one float catalogue with the prefactors applied, painted by the
-// paint context's tile kernels (shared-memory tiles written once; objects near the grid's discontinuities,
-// the Survey clamp region included, take the exact FP64 rules). The paint settles on the host (one
-// synchronisation) so that a tile-list overflow repaints before the multipoles read the grids.
+// FP32: data and randoms (Momentum 1: data only) combined into one float catalogue with the prefactors
+// applied, painted by the paint context's tile kernels (shared-memory tiles written once; objects near the
+// grid's discontinuities, the Survey clamp region included, take the exact FP64 rules). The paint settles on
+// the host (one synchronisation) so that a tile-list overflow repaints before the multipoles read the grids.
 template <typename T>
 static int sv_paint_tiles(capow_survey_ctx *c, const capow_survey_catalogue *data, const capow_survey_catalogue *rand) {
-  const size_t n = data->n + rand->n;
-  if (c->comb_cap < n) {
+  const int ncat = c->mom == 1 ? 1 : 2;  // src/main.c:229: Momentum 1 paints no randoms
+  const size_t n = data->n + (ncat == 2 ? rand->n : 0);
+  if (c->comb_cap < n || !c->comb) {
     if (c->comb) cudaFree(c->comb);
     c->comb = nullptr;
     c->comb_cap = 0;
-    CK(c, cudaMalloc(&c->comb, sizeof(float) * 4 * (n ? n : 1)));
-    c->comb_cap = n;
+    CK(c, cudaMalloc(&c->comb, sizeof(float) * 5 * (n ? n : 1)));
+    c->comb_cap = n ? n : 1;
   }
-  float *cx = c->comb, *cy = cx + c->comb_cap, *cz = cy + c->comb_cap, *cw = cz + c->comb_cap;
+  float *cx = c->comb, *cy = cx + c->comb_cap, *cz = cy + c->comb_cap, *cw = cz + c->comb_cap, *cv = cw + c->comb_cap;
   const capow_survey_catalogue *cats[2] = {data, rand};
   long long off = 0;
-  for (int cat = 0; cat < 2; cat++) {
+  for (int cat = 0; cat < ncat; cat++) {
     const long long m = (long long)cats[cat]->n;
     if (m) {
-      const T *wk;
-      SvIn<T> sin = sv_device_view<T>(c, cat, cats[cat], &wk);
-      k_sv_combine<T><<<sv_blocks(m), 256, 0, c->stream>>>(c->g, sin, wk, m, cat, off, cx, cy, cz, cw, c->st);
+      SvIn<T> sin;
+      const T *wk, *wpv;
+      int rc = sv_device_view<T>(c, cat, cats[cat], false, &sin, &wk, &wpv);
+      if (rc) return rc;
+      k_sv_combine<T><<<sv_blocks(m), 256, 0, c->stream>>>(c->g, sin, wk, wpv, m, cat, c->mom, off, cx, cy, cz, cw, cv,
+                                                           c->st);
       c->launches++;
     }
     off += m;
@@ -894,6 +1056,7 @@ static int sv_paint_tiles(capow_survey_ctx *c, const capow_survey_catalogue *dat
   d.y = cy;
   d.z = cz;
   d.w = cw;
+  d.vlos = c->nf == 2 ? cv : nullptr;
   capow_ctx *pc = c->pc;
   pc->last = d;
   pc->painted = true;
@@ -905,14 +1068,25 @@ static int sv_paint_tiles(capow_survey_ctx *c, const capow_survey_catalogue *dat
   return CAPOW_OK;
 }
 
+template <typename R, int L>
+static void sv_launch_assign(capow_survey_ctx *c, const dim3 &grid, const SvAssign<R> &sa) {
+  if (c->nf == 2) k_sv_assign<R, L, true><<<grid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins);
+  else k_sv_assign<R, L, false><<<grid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins);
+}
+
 template <typename R>
 static int sv_multipoles(capow_survey_ctx *c) {
   typedef typename SvC<R>::C C;
   const capow_params &p = c->p;
   const Geom &g = c->g;
   const long long ge = g.main_sz;
-  R *a0 = (R *)c->paint, *a1 = c->nslot > 1 ? a0 + ge : nullptr;
-  R *w0 = (R *)c->work, *w1 = c->nslot > 1 ? w0 + ge : nullptr;
+  const int nf = c->nf, il = p.DoInterlacing;
+  R *a[4], *w[4];
+  for (int s = 0; s < 4; s++) {
+    a[s] = s < c->nslot ? (R *)c->paint + s * ge : nullptr;
+    w[s] = s < c->nslot ? (R *)c->work + s * ge : nullptr;
+  }
+  const int sd0 = sv_slot(0, 0, nf), sd1 = sv_slot(1, 0, nf), sm0 = sv_slot(0, 1, nf), sm1 = sv_slot(1, 1, nf);
   const long long rows = (long long)p.NX * p.NY;
   // one warp per row, 8 per CTA, grid-stride beyond 16 CTAs per SM
   const unsigned wblocks = (unsigned)std::min<long long>((rows + 7) / 8, 152LL * 16);
@@ -920,14 +1094,20 @@ static int sv_multipoles(capow_survey_ctx *c) {
   const dim3 agrid((unsigned)((cols + 255) / 256), (unsigned)((p.NX + SV_ICHUNK - 1) / SV_ICHUNK));
   SvAssign<R> sa;
   memset(&sa, 0, sizeof sa);
-  sa.g0 = (const C *)w0;
-  sa.g1 = (const C *)w1;
+  sa.gd0 = (const C *)w[sd0];
+  sa.gd1 = il ? (const C *)w[sd1] : nullptr;
+  sa.gm0 = nf == 2 ? (const C *)w[sm0] : nullptr;
+  sa.gm1 = nf == 2 && il ? (const C *)w[sm1] : nullptr;
   sa.F0 = (C *)c->F0;
+  sa.F0m = (C *)c->F0m;
   sa.dc = c->pc ? (const double *)((const char *)c->pc->st + offsetof(DevStats, dc))
                : (const double *)((const char *)c->st + offsetof(SvStats, dc));
+  sa.sd0 = sd0;
+  sa.sd1 = sd1;
+  sa.sm0 = sm0;
+  sa.sm1 = sm1;
   sa.origin = c->origin;
-  sa.a0 = a0;
-  sa.a1 = a1;
+  for (int s = 0; s < 4; s++) sa.a[s] = a[s];
   sa.oind = c->oind;
   sa.ox = (const C *)c->ox;
   sa.oy = (const C *)c->oy;
@@ -936,28 +1116,31 @@ static int sv_multipoles(capow_survey_ctx *c) {
   c->sets = 0;
   for (int l = 0; l <= 4; l += step) {
     for (int m = 0; m < 2 * l + 1; m++) {
-      k_sv_weight<R><<<wblocks, 256, 0, c->stream>>>(a0, a1, w0, w1, (const R *)c->vx, (const R *)c->vy,
-                                                     (const R *)c->vz, p.NX, p.NY, p.NZ, g.row, l, m);
-      c->launches++;
+      for (int f = 0; f < nf; f++) {  // the density grid (and its interlaced copy), then the momentum grid
+        const int s0 = sv_slot(0, f, nf), s1 = sv_slot(1, f, nf);
+        k_sv_weight<R><<<wblocks, 256, 0, c->stream>>>(a[s0], il ? a[s1] : nullptr, w[s0], il ? w[s1] : nullptr,
+                                                       (const R *)c->vx, (const R *)c->vy, (const R *)c->vz, p.NX,
+                                                       p.NY, p.NZ, g.row, l, m);
+        c->launches++;
+      }
       if (c->plan_per_grid) {
         for (int s = 0; s < c->nslot; s++) {
-          R *wg = w0 + s * ge;
-          if (sizeof(R) == 8) CKFFT(c, cufftExecD2Z(c->plan, (cufftDoubleReal *)wg, (cufftDoubleComplex *)wg));
-          else CKFFT(c, cufftExecR2C(c->plan, (cufftReal *)wg, (cufftComplex *)wg));
+          if (sizeof(R) == 8) CKFFT(c, cufftExecD2Z(c->plan, (cufftDoubleReal *)w[s], (cufftDoubleComplex *)w[s]));
+          else CKFFT(c, cufftExecR2C(c->plan, (cufftReal *)w[s], (cufftComplex *)w[s]));
         }
       } else if (sizeof(R) == 8) {
-        CKFFT(c, cufftExecD2Z(c->plan, (cufftDoubleReal *)w0, (cufftDoubleComplex *)w0));
+        CKFFT(c, cufftExecD2Z(c->plan, (cufftDoubleReal *)w[0], (cufftDoubleComplex *)w[0]));
       } else {
-        CKFFT(c, cufftExecR2C(c->plan, (cufftReal *)w0, (cufftComplex *)w0));
+        CKFFT(c, cufftExecR2C(c->plan, (cufftReal *)w[0], (cufftComplex *)w[0]));
       }
       sa.m = m;
       sa.coef = (R)harm_coef(l, m);
       switch (l) {
-        case 0: k_sv_assign<R, 0><<<agrid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins); break;
-        case 1: k_sv_assign<R, 1><<<agrid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins); break;
-        case 2: k_sv_assign<R, 2><<<agrid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins); break;
-        case 3: k_sv_assign<R, 3><<<agrid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins); break;
-        default: k_sv_assign<R, 4><<<agrid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins); break;
+        case 0: sv_launch_assign<R, 0>(c, agrid, sa); break;
+        case 1: sv_launch_assign<R, 1>(c, agrid, sa); break;
+        case 2: sv_launch_assign<R, 2>(c, agrid, sa); break;
+        case 3: sv_launch_assign<R, 3>(c, agrid, sa); break;
+        default: sv_launch_assign<R, 4>(c, agrid, sa); break;
       }
       c->launches++;
       c->sets++;
@@ -972,13 +1155,14 @@ static int sv_run(capow_survey_ctx *c, const capow_survey_catalogue *data, const
   CK(c, cudaMemsetAsync(c->st, 0, sizeof(SvStats), c->stream));
   CK(c, cudaMemsetAsync(c->bins, 0, sizeof(double) * 5 * c->p.NK, c->stream));
   CK(c, cudaEventRecord(c->ev[0], c->stream));
-  int rc = sv_enqueue_catalogue<T, R>(c, 0, data);
-  if (!rc) rc = sv_enqueue_catalogue<T, R>(c, 1, rand);
+  int rc = sv_enqueue_catalogue<T>(c, 0, data);
+  if (!rc) rc = sv_enqueue_catalogue<T>(c, 1, rand);
   if (rc) return rc;
   if constexpr (sizeof(R) == 8) {
     CK(c, cudaMemsetAsync(c->paint, 0, sizeof(R) * (size_t)c->g.main_sz * c->nslot, c->stream));
-    sv_launch_paint<T, R>(c, 0, data);
-    sv_launch_paint<T, R>(c, 1, rand);
+    rc = sv_launch_paint<T, R>(c, 0, data);
+    if (!rc && c->mom != 1) rc = sv_launch_paint<T, R>(c, 1, rand);  // src/main.c:229
+    if (rc) return rc;
   } else {
     rc = sv_paint_tiles<T>(c, data, rand);
     if (rc) return rc;
@@ -991,17 +1175,21 @@ static int sv_run(capow_survey_ctx *c, const capow_survey_catalogue *data, const
   return CAPOW_OK;
 }
 
-static bool sv_cat_ok(const capow_survey_catalogue *c) {
+static bool sv_cat_ok(const capow_survey_catalogue *c, int mom, bool data) {
   if (!c || (c->dtype != CAPOW_F32 && c->dtype != CAPOW_F64)) return false;
   if (c->n && (!c->x || !c->y || !c->z || !c->w || !c->nbar)) return false;
+  if (c->n && mom && !c->pverr) return false;
+  if (c->n && mom && data && !c->pv) return false;
   return true;
 }
 
 extern "C" int capow_survey_power(capow_survey_ctx *c, const capow_survey_catalogue *data,
                                   const capow_survey_catalogue *rand, capow_spectrum *out, capow_survey_stats *st) {
   if (!c) return CAPOW_EINVAL;
-  if (!sv_cat_ok(data) || !sv_cat_ok(rand))
-    FAIL(c, CAPOW_EINVAL, "survey catalogue: dtype must be CAPOW_F32 or CAPOW_F64 with x, y, z, w and nbar given");
+  if (!sv_cat_ok(data, c->mom, true) || !sv_cat_ok(rand, c->mom, false))
+    FAIL(c, CAPOW_EINVAL,
+         "survey catalogue: dtype must be CAPOW_F32 or CAPOW_F64 with x, y, z, w and nbar given (and pv, pverr for "
+         "Momentum 1-3)");
   if (data->dtype != rand->dtype) FAIL(c, CAPOW_EINVAL, "data and randoms must have the same dtype");
   CK(c, cudaSetDevice(c->o.device));
   c->done = false;
@@ -1016,20 +1204,32 @@ extern "C" int capow_survey_power(capow_survey_ctx *c, const capow_survey_catalo
   CK(c, cudaStreamSynchronize(c->stream));
   c->done = true;
   const SvStats &s = *c->h_st;
-  if (s.nonfinite) FAIL(c, CAPOW_EINVAL, "non-finite coordinate, weight or number density in a survey catalogue");
-  // src/main.c:166-176 (Momentum 0)
+  if (s.nonfinite)
+    FAIL(c, CAPOW_EINVAL, "non-finite coordinate, weight, number density or velocity in a survey catalogue");
+  // src/main.c:166-186
   const double alpha = s.wsum[0] / s.wsum[1];
   const double rand_nbwsq = s.w2sum[1] * (alpha * alpha);
   const double rand_nbsqwsq = s.w2nsum[1] * alpha;
+  double shot, norm;
+  switch (c->mom) {
+    case 0: shot = s.w2sum[0] + rand_nbwsq; norm = rand_nbsqwsq; break;
+    case 1: shot = s.vrsq; norm = rand_nbsqwsq; break;
+    case 2: shot = s.vr; norm = sqrt(rand_nbsqwsq * s.w2npv[1]); break;
+    default: shot = s.vrsq; norm = sqrt(rand_nbsqwsq * s.w2npv[1]); break;
+  }
   if (st) {
     st->ngrid_data = s.ngrid[0];
-    st->ngrid_rand = s.ngrid[1] / -alpha;
+    st->ngrid_rand = c->mom == 1 ? 0.0 : s.ngrid[1] / -alpha;
     st->data_nbw = s.wsum[0];
     st->data_nbwsq = s.w2sum[0];
     st->data_nbsqwsq = s.w2nsum[0];
     st->rand_nbw = s.wsum[1];
     st->rand_nbwsq = rand_nbwsq;
     st->rand_nbsqwsq = rand_nbsqwsq;
+    st->data_vr = s.vr;
+    st->data_vrsq = s.vrsq;
+    st->data_nbsqwsq_pv = s.w2npv[0];
+    st->rand_nbsqwsq_pv = s.w2npv[1];
   }
   if (out) {
     for (int l = 0; l < 5; l++) {
@@ -1047,8 +1247,8 @@ extern "C" int capow_survey_power(capow_survey_ctx *c, const capow_survey_catalo
         for (int b = 0; b < n2; b++) out->nmodes2d[b] = 0;
     }
     out->alpha = alpha;
-    out->shot = s.w2sum[0] + rand_nbwsq;
-    out->norm = rand_nbsqwsq;
+    out->shot = shot;
+    out->norm = norm;
     out->last_bin = -1;
     out->kind = 0;
   }

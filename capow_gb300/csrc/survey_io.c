@@ -199,14 +199,16 @@ void capow_survey_objects_free(capow_survey_objects *o) {
   free(o->w);
   free(o->nbar);
   free(o->redshift);
+  free(o->pv);
+  free(o->pverr);
   free(o->log);
   memset(o, 0, sizeof *o);
 }
 
 static int grow(capow_survey_objects *o, size_t *cap) {
   size_t nc = *cap ? 2 * *cap : 65536;
-  float **arr[6] = {&o->x, &o->y, &o->z, &o->w, &o->nbar, &o->redshift};
-  for (int k = 0; k < 6; k++) {
+  float **arr[8] = {&o->x, &o->y, &o->z, &o->w, &o->nbar, &o->redshift, &o->pv, &o->pverr};
+  for (int k = 0; k < 8; k++) {
     float *q = (float *)realloc(*arr[k], sizeof(float) * nc);
     if (!q) return -1;
     *arr[k] = q;
@@ -214,6 +216,9 @@ static int grow(capow_survey_objects *o, size_t *cap) {
   *cap = nc;
   return 0;
 }
+
+/* natural log; capow_read_survey's text buffer is named log */
+static double log_of(double a) { return log(a); }
 
 int capow_read_survey(const char *path, const capow_params *p, const capow_survey_params *sv, int randoms,
                       capow_survey_objects *out, char *msg, size_t msglen) {
@@ -369,6 +374,15 @@ int capow_read_survey(const char *path, const capow_params *p, const capow_surve
     out->redshift[nkeep] = (float)tred;
     out->w[nkeep] = (float)tw;
     out->nbar[nkeep] = sv->NBAR_Column > 0 ? (float)tnbar : 0.0f;
+    out->pv[nkeep] = out->pverr[nkeep] = 0.0f;
+    if (p->Momentum) { /* src/read_data.c:308-316 */
+      const double ln10 = log_of(10.0);
+      const double q = 3.0 / 2.0 * p->Omega_m - 1.0;
+      const double zmod = tred * (1.0 + 0.5 * (1.0 - q) * tred - 1.0 / 6.0 * (2.0 - q - 3.0 * q * q) * tred * tred);
+      const double tlogdist = randoms ? 0.0 : v[6], tlogdist_err = randoms ? v[6] : v[7];
+      out->pv[nkeep] = (float)(LIGHT_SPEED * zmod * ln10 * tlogdist / (1.0 + zmod));
+      out->pverr[nkeep] = (float)(LIGHT_SPEED * zmod * ln10 * tlogdist_err / (1.0 + zmod));
+    }
     nkeep++;
     if (tred < redmin) redmin = tred;
     if (tred > redmax) redmax = tred;

@@ -156,8 +156,8 @@ static int run_survey(const capow_params *p, const capow_survey_params *sv, cons
     spec.pk2d = store + 5 * nk;
     spec.nmodes2d = mstore + nk;
   }
-  capow_survey_catalogue dc = {data.n, CAPOW_F32, 0, data.x, data.y, data.z, data.w, data.nbar};
-  capow_survey_catalogue rc_ = {rand.n, CAPOW_F32, 0, rand.x, rand.y, rand.z, rand.w, rand.nbar};
+  capow_survey_catalogue dc = {data.n, CAPOW_F32, 0, data.x, data.y, data.z, data.w, data.nbar, data.pv, data.pverr};
+  capow_survey_catalogue rc_ = {rand.n, CAPOW_F32, 0, rand.x, rand.y, rand.z, rand.w, rand.nbar, rand.pv, rand.pverr};
   capow_survey_stats st;
   rc = capow_survey_power(ctx, &dc, &rc_, &spec, &st);
   if (rc != CAPOW_OK) {
@@ -167,13 +167,23 @@ static int run_survey(const capow_params *p, const capow_survey_params *sv, cons
   }
   printf("Task 0 has %llu objects, gridded %lf\n", (unsigned long long)data.n, st.ngrid_data);
 
-  banner("Computing shot-noise and normalisation"); /* src/main.c:189-193 */
-  printf("alpha = %g\n", spec.alpha);
-  printf("shot-noise [data, randoms]    = %g, %g\n", st.data_nbwsq, st.rand_nbwsq);
-  printf("normalisation [data, randoms] = %g, %g\n", st.data_nbsqwsq, st.rand_nbsqwsq);
+  banner("Computing shot-noise and normalisation"); /* src/main.c:189-203 */
+  if (p->Momentum == 0) {
+    printf("alpha = %g\n", spec.alpha);
+    printf("shot-noise [data, randoms]    = %g, %g\n", st.data_nbwsq, st.rand_nbwsq);
+    printf("normalisation [data, randoms] = %g, %g\n", st.data_nbsqwsq, st.rand_nbsqwsq);
+  } else if (p->Momentum == 1) {
+    printf("shot-noise [data]    = %g \n", st.data_vrsq);
+    printf("normalisation [data, randoms] = %g, %g\n", st.data_nbsqwsq, st.rand_nbsqwsq);
+  } else {
+    printf("alpha = %g\n", spec.alpha);
+    printf("shot-noise    = %g\n", st.data_vr);
+    printf("normalisation = %g\n", spec.norm);
+  }
   fflush(stdout);
   banner("Subtracting off expected density");
-  printf("Task 0 has %llu objects, gridded %lf\n", (unsigned long long)rand.n, st.ngrid_rand);
+  if (p->Momentum != 1) /* src/main.c:229: Momentum 1 assigns no randoms */
+    printf("Task 0 has %llu objects, gridded %lf\n", (unsigned long long)rand.n, st.ngrid_rand);
 
   const int step = p->Odd_Multipoles ? 1 : 2;
   for (int l = 0; l <= 4; l += step) {

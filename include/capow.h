@@ -264,7 +264,18 @@ void capow_destroy(capow_ctx *ctx);
  * 472-967): data and random catalogues in a non-periodic box seen from an observer, FKP weights,
  * the random counts subtracted in the painted grid, and the Yamamoto multipoles, each an FFT of the
  * density weighted by functions of the line of sight r^ to every cell, crossed with the monopole
- * field F0. Density only (the reference's survey Momentum 0).
+ * field F0. params.Momentum selects, as in the reference:
+ *   0  the density multipoles;
+ *   1  the velocity multipoles: the data's w pv painted (no randoms), FKP weights from pverr,
+ *      shot = sum w^2 pv^2, norm = alpha sum w_r^2 nbar_r;
+ *   2  the density-velocity cross multipoles: the density (data minus alpha randoms) and the data's
+ *      w_pv pv, crossed with F0 and F0_mom (main.c:876-887), shot = sum w w_pv pv,
+ *      norm = sqrt(alpha sum w_r^2 nbar_r * sum w_pv,r^2 nbar_r). The reference itself crashes here
+ *      (its survey paint writes the momentum grid create_grids leaves unallocated for Momentum 2,
+ *      main.c:1198); this library computes what that code describes;
+ *   3  the cross multipoles with shot = sum w^2 pv^2 and the reference's norm, which is zero (the
+ *      randoms' w_pv sum is taken for Momentum 2 only, main.c:164-165), so the normalised spectra
+ *      are infinite as the reference's are.
  *
  *   reference                                             this library
  *   ----------------------------------------------------   -----------------------------------
@@ -305,37 +316,48 @@ typedef struct capow_survey_catalogue {
   const void *x, *y, *z; /* Cartesian positions, box units */
   const void *w;        /* weights as read (before FKP) */
   const void *nbar;     /* number density */
+  const void *pv, *pverr; /* peculiar velocity and its error (Momentum 1-3; NULL for Momentum 0). The
+                             randoms' pv is not used. */
 } capow_survey_catalogue;
 
 /* counters of one survey evaluation */
 typedef struct capow_survey_stats {
   double ngrid_data, ngrid_rand; /* assign_survey_data's "gridded" sums: accepted objects counted w/w
-                                    (read_data.c:474-491; the randoms' sum divided by -alpha) */
+                                    (read_data.c:474-491; the randoms' sum divided by -alpha; Momentum 1
+                                    counts w/(pv w) and paints no randoms) */
   double data_nbw, data_nbwsq, data_nbsqwsq; /* sum w, w^2, w^2 nbar over the data (main.c:151-156) */
   double rand_nbw, rand_nbwsq, rand_nbsqwsq; /* the same over the randoms, the last two after the alpha
                                                 scaling of main.c:170-171 */
+  double data_vr, data_vrsq, data_nbsqwsq_pv; /* sum w w_pv pv, w^2 pv^2, w_pv^2 nbar (Momentum 1-3) */
+  double rand_nbsqwsq_pv;                     /* sum w_pv^2 nbar over the randoms (Momentum 2) */
 } capow_survey_stats;
 
 typedef struct capow_survey_ctx capow_survey_ctx;
 
 /* create_grids for a survey run (main.c:1123-1251): params as for capow_create (LOS is not used;
- * Momentum must be 0; Output2D gives the reference's all-zero 2-D bins), the observer and FKP
- * settings from sv. Precision CAPOW_FP64 or CAPOW_FP32_MIXED (FP32 grids and FFTs, FP64 sums and
- * bins); fft_path is ignored. Allocates 2 * (1 + DoInterlacing) + 1 padded grids: the painted grid
- * (and its interlaced copy), as many work grids for the FFTs, and the complex F0 grid. */
+ * Momentum 0 to 3; Output2D gives the reference's all-zero 2-D bins), the observer and FKP settings
+ * from sv. Precision CAPOW_FP64 or CAPOW_FP32_MIXED (FP32 grids and FFTs, FP64 sums and bins);
+ * fft_path is ignored. Allocates, per painted field (two for Momentum 2, 3), the painted grid and its
+ * interlaced copy, as many work grids for the FFTs, and a complex F0 grid. Momentum 2 and 3 need the
+ * FKP weights (FKP_Column < 0): the reference leaves w_pv unset otherwise (CAPOW_EINVAL). */
 int capow_survey_create(const capow_params *p, const capow_survey_params *sv, const capow_options *opt,
                         capow_survey_ctx **out);
 
 /* One survey evaluation: FKP weights (when FKP_Column < 0), the weight sums, alpha = sum w_d / sum w_r,
  * the data painted with weight w and the randoms with -alpha w into the same grid(s), then every
- * multipole (P1, P3 only with Odd_Multipoles). Fills out's raw sums, Nmodes, shot, norm and alpha as
+ * multipole (P1, P3 only with Odd_Multipoles). Momentum 1 paints only the data's w pv (its auto spectrum;
+ * shot sum w^2 pv^2); Momentum 2 and 3 also paint the data's w_pv pv and cross it with the density (shot
+ * sum w w_pv pv or sum w^2 pv^2, norm sqrt(rand_nbsqwsq rand_nbsqwsq_pv): 0 for Momentum 3, as in the
+ * reference, whose Momentum 3 output is therefore infinite). Fills out's raw sums, Nmodes, shot, norm and alpha as
  * capow_power does (normalise with capow_normalise); st may be NULL. Ends with a stream
- * synchronisation. CAPOW_EINVAL for a non-finite coordinate, weight or number density. */
+ * synchronisation. CAPOW_EINVAL for a non-finite coordinate, weight, number density or velocity. */
 int capow_survey_power(capow_survey_ctx *ctx, const capow_survey_catalogue *data, const capow_survey_catalogue *rand,
                        capow_spectrum *out, capow_survey_stats *st);
 
-/* the painted grid (which 0) or its interlaced copy (1) of the last evaluation, as float64 in the
- * reference's padded layout [NX][NY][2*(NZ/2+1)] (data minus alpha randoms). For parity tests. */
+/* a painted grid of the last evaluation, as float64 in the reference's padded layout [NX][NY][2*(NZ/2+1)]:
+ * which = stencil * fields + field, field 0 the density (data minus alpha randoms; Momentum 1: the data's
+ * w pv) and, for Momentum 2 and 3, field 1 the data's w_pv pv; stencil 1 the interlaced copy. For parity
+ * tests. */
 int capow_survey_copy_grid(capow_survey_ctx *ctx, int which, double *host_out);
 
 /* device milliseconds of the last evaluation: weights, sums and painting; the multipole FFTs and
@@ -384,6 +406,9 @@ typedef struct capow_survey_objects {
   unsigned long long nread; /* catalogue lines read (NREAD) */
   float *x, *y, *z;         /* Cartesian positions (converted from RA, Dec, z for Coord_Type 1, 2) */
   float *w, *nbar, *redshift;
+  float *pv, *pverr;        /* Momentum != 0: c zmod ln10 logdist / (1 + zmod) and the same of the error
+                               (read_data.c:308-316, zmod the redshift's second-order distance factor);
+                               the data's 7th and 8th numbers, the randoms' 7th (their pv is 0: unused) */
   double lo[3], hi[3];      /* the "X, Y, Z" ranges the reference prints: min and max of the kept objects'
                                coordinates, starting from 1e-30 and -1e30 (read_data.c:192-194, 344-349) */
   double redmin, redmax;    /* min and max redshift of the kept objects (read_data.c:327-328) */

@@ -40,10 +40,12 @@ def test_survey_reader_matches_the_oracle(tmp_path, name, randoms):
     got = cg.read_survey(path, prm, sv, randoms)
     ref = orc.survey_read(p, path, randoms)
     assert got["n"] == len(ref["x"]) and got["nread"] == ref["nread"]
-    for k in ("x", "y", "z", "weight", "nbar", "redshift"):
+    for k in ("x", "y", "z", "weight", "nbar", "redshift", "pv", "pverr"):
         mine = got["w" if k == "weight" else k]
         assert mine.dtype == np.float32
         assert np.array_equal(mine, ref[k]), k
+    if p.Momentum:  # the velocity cases carry log-distance ratios: pv and its error are not all zero
+        assert np.any(got["pverr"] != 0) and (randoms or np.any(got["pv"] != 0))
     # "Have N objects" and the ranges, as the unmodified reference printed them for this catalogue
     txt = open(os.path.join(os.path.dirname(__file__), "golden", f"{name}.stdout")).read().splitlines()
     at = [i for i, t in enumerate(txt) if t.startswith("Have ")][1 if randoms else 0]
