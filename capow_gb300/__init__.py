@@ -687,14 +687,13 @@ def _survey_cat(cat, velocities: bool):
     pv out (it is not read)."""
     keys = ("x", "y", "z", "w", "nbar") + (("pv", "pverr") if velocities else ())
     if isinstance(cat, dict):
-        if velocities and "pv" not in cat and "pverr" in cat:
-            cat = dict(cat, pv=cat["pverr"])
-        arrs = [cat[k] for k in keys]
+        arrs = [cat.get(k) if k == "pv" else cat[k] for k in keys]
     else:
         arrs = list(cat)[:len(keys)]
         if len(arrs) != len(keys):
             raise ValueError(f"survey catalogue needs {', '.join(keys)}")
-    ptrs = [_ptr_of(a) for a in arrs]
+    given = [k for k, a in zip(keys, arrs) if a is not None]
+    ptrs = [_ptr_of(a) for a in arrs if a is not None]
     codes = {p[1] for p in ptrs}
     devs = {p[2] for p in ptrs}
     if len(codes) != 1 or len(devs) != 1:
@@ -702,7 +701,8 @@ def _survey_cat(cat, velocities: bool):
     n = len(ptrs[0][3])
     if any(len(p[3]) != n for p in ptrs):
         raise ValueError("survey catalogue arrays differ in length")
-    addr = [p[0] for p in ptrs] + [None] * (7 - len(ptrs))
+    where = dict(zip(given, (p[0] for p in ptrs)))
+    addr = [where.get(k) for k in ("x", "y", "z", "w", "nbar", "pv", "pverr")]
     return _SurveyCatalogue(n, codes.pop(), devs.pop(), *addr), [p[3] for p in ptrs]
 
 

@@ -121,20 +121,23 @@ def _run_survey_driver(tmp_path, name, precision):
 
 
 def _output_nonfinite(got: str, want: str, raw, odd: bool, rel: float, label: str):
-    """An output file with norm = 0 (survey Momentum 3, as the reference computes it): every multipole
-    prints as inf, -inf or nan. Header lines equal; per row the k centre and Nmodes equal; each entry
-    prints the same where the reference's raw sum for it is clearly signed (above rel of the row's
-    largest raw |P|); a nan matches a nan of either sign (0/0 gives -nan on x86-64 and nan on AArch64);
-    an entry whose raw sum is a rounding-level zero only has to be non-finite."""
+    """An output file with norm = 0 (survey Momentum 3, as the reference computes it): every multipole of
+    a bin with modes prints as inf, -inf or nan. Header lines equal; per row the k centre and Nmodes equal;
+    each entry prints the same where the reference's raw sum for it is clearly signed (above rel of the
+    largest raw |P| within two bins); a nan matches a nan of either sign (0/0 gives -nan on x86-64 and nan
+    on AArch64); an entry whose raw sum is a rounding-level zero only has to be non-finite."""
     gl, wl = got.splitlines(), want.splitlines()
     assert gl[:3] == wl[:3] and len(gl) == len(wl), label
     cols = [0, 1, 2, 3, 4] if odd else [0, 2, 4]
+    allp = np.abs(np.array([raw[f"Pk{l}"] for l in cols]))
     for b, (a, c) in enumerate(zip(gl[3:], wl[3:])):
         ta, tc = a.split(), c.split()
         assert len(ta) == len(tc) == len(cols) + 2 and ta[0] == tc[0] and ta[-1] == tc[-1], (label, a, c)
         r = np.array([raw[f"Pk{l}"][b] for l in cols])
-        scale = np.abs(r).max()
+        scale = allp[:, max(0, b - 2):b + 3].max()
         for j in range(len(cols)):
+            if ta[1 + j] == tc[1 + j]:
+                continue
             x, y = float(ta[1 + j]), float(tc[1 + j])
             assert not np.isfinite(x) and not np.isfinite(y), (label, a, c)
             if np.isnan(x) and np.isnan(y):

@@ -248,7 +248,7 @@ def test_survey_rejects_non_finite_and_bad_arguments(gpu, tmp_path):
     p1 = cg.Params(**{**prm.__dict__, "Momentum": 1})
     with cg.SurveySpectrum(p1, sv, precision="fp64") as ss:
         with pytest.raises(cg.CapowError) as e:
-            ss.power(dict(cat, pverr=cat["w"]), dict(cat, pverr=cat["w"]))
+            ss.power(dict(cat, pverr=cat["w"]), dict(cat, pverr=cat["w"]))  # the data without pv
         assert e.value.status == cg.EINVAL
         v = dict(cat, pv=np.full(100, 250.0, np.float32), pverr=np.full(100, 40.0, np.float32))
         ok = ss.power(v, dict(cat, pverr=v["pverr"]))
