@@ -1137,6 +1137,16 @@ __global__ void __launch_bounds__(ZR_THREADS) k_zr2c(ZrGeo zg, BinTables t, cons
     const int sl = blk / per_slot, rem = blk - sl * per_slot;
     const int x = rem / zg.nyb, y0 = (rem - x * zg.nyb) * ZB;
     __syncthreads();  // tables written; the previous block's output has read sd
+    // the CTA's next block is ZB contiguous padded rows: one bulk prefetch into L2 while this one runs
+    const int nb = blk + (int)gridDim.x;
+    if (threadIdx.x == 0 && nb < nblk) {
+      const int sl2 = nb / per_slot, rem2 = nb - sl2 * per_slot;
+      const int x2 = rem2 / zg.nyb, y2 = (rem2 - x2 * zg.nyb) * ZB;
+      const float *nxt = in + sl2 * zg.in_slot + (long long)x2 * zg.slice + (long long)y2 * zg.row;
+      const unsigned bytes = ((unsigned)(min(ZB, zg.ny - y2) * zg.row) * 4u) & ~15u;
+      if (bytes && (((unsigned long long)nxt & 15ull) == 0))
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(nxt), "r"(bytes) : "memory");
+    }
     zr2c_block<ZB>(zg, z, in, out, sd, sl, x, y0);
   }
 }

@@ -71,7 +71,7 @@ def test_batch_mocks_match_the_oracle(gpu):
     out = cg.run_batch(mocks, precision="fp32", graph=True, autotune=True)
     for (p, parts), (status, res) in zip(mocks, out):
         assert status == cg.OK
-        kw = {f.name: getattr(p, f.name) for f in orc.Params.__dataclass_fields__.values()}
+        kw = {f.name: getattr(p, f.name) for f in orc.Params.__dataclass_fields__.values() if hasattr(p, f.name)}
         po = orc.Params(**kw)
         x, y, z, vz = (t.cpu().numpy() for t in parts[:4])
         zero = np.zeros_like(x)
