@@ -4,15 +4,15 @@
 // FP64 path (k_paint64): one thread per particle, the reference's double arithmetic,
 // global FP64 atomics into zeroed grids. It is the plain FP64 GPU path.
 //
-// FP32 path (k_count -> k_scan -> k_scatter -> k_tile_paint): particles are bucketed into
-// the output tiles their stencils touch (a counting sort; a particle near a tile face is
+// FP32 path (k_bucket -> k_tile_rec -> k_edge_fixup; deterministic: k_count -> k_scan -> k_scatter ->
+// k_tile_rec_det): particles are bucketed into the output tiles their stencils touch (a counting sort; a particle near a tile face is
 // listed in each neighbouring tile), then one CTA per tile accumulates every stencil tap of
 // its particles in shared memory and writes the tile once with coalesced stores. Every grid
 // cell is written exactly once: no memset of the grids, no global atomics on them. Particles
 // within a few ulps of a discontinuity of the reference's rules (acceptance bounds, the TSC
 // low-tap drop, the LOS==0 x shift, NN cell edges, non-finite input) take the exact FP64 rules
-// inside the same tile kernel, so indices and acceptance match the reference bit for bit.
-// The deterministic variant accumulates int64 fixed point in shared memory.
+// (k_edge_fixup; in the deterministic variant, inside the tile kernel), so indices and acceptance match
+// the reference bit for bit. The deterministic variant accumulates int64 fixed point in shared memory.
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -614,22 +614,12 @@ __global__ void __launch_bounds__(256, 4) k_bucket(Geom g, FieldSpec fs, TileGeo
   if (ovf_full) atomicOr(&st->overflow, 1);
 }
 
-// Pass 4: one CTA per tile. Shared memory holds the tile of every grid slot; taps outside the
-// tile are skipped (another tile owns them). The particle's home tile also adds it to the
-// statistics that need exact decisions: NGRID, the out-of-box count and the LOS == 0 error.
-// FP32 accumulation adds the float; the deterministic variant adds round(value * 2^S) as an integer.
-__device__ __forceinline__ void acc_add(float *p, float v, double) { atomicAdd(p, v); }
-__device__ __forceinline__ void acc_add(unsigned long long *p, float v, double scale) {
-  atomicAdd(p, (unsigned long long)__double2ll_rn((double)v * scale));
-}
-__device__ __forceinline__ void acc_add64(float *p, double v, double) { atomicAdd(p, (float)v); }
+// Deterministic accumulation: round(value * 2^S) added as an integer (S from k_scan, per field).
 __device__ __forceinline__ void acc_add64(unsigned long long *p, double v, double scale) {
   atomicAdd(p, (unsigned long long)__double2ll_rn(v * scale));
 }
 
-#define TAP_RB 32  // records a warp stages at a time
-
-// One axis of a record's stencil for the lane-per-tap deposit: the taps' offsets in the shared tile
+// One axis of a record's stencil: the taps' offsets in the shared tile
 // (index within the tile times the axis pitch) and weights; a tap that the reference drops or that
 // lies outside this tile gets weight 0.
 __device__ __forceinline__ void stage_axis32(const AxisTapsF &t, int origin, int extent, int pitch, float *W,
@@ -662,209 +652,6 @@ __device__ __forceinline__ void stage_axis64(const Geom &g, const AxisTaps &t, i
     ok = ok && l >= 0 && l < extent;
     W[k] = ok ? (float)t.w[k] : 0.0f;
     O[k] = ok ? l * pitch : 0;
-  }
-}
-
-// Pass 4: one CTA per tile; shared memory holds the tile of every grid slot with bank-spreading
-// pitches. Each warp stages 32 records at a time (lane = record: tap offsets and weights per axis),
-// then deposits them one record after another with lane = tap, so the 27 shared-memory atomics of
-// a record hit 27 different banks. The particle's home tile also adds it to the statistics that need
-// exact decisions: NGRID, the out-of-box count and the LOS == 0 error.
-template <typename T, typename Acc>
-__global__ void __launch_bounds__(256, 2) k_tile_paint(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in,
-                                                    long long n, const unsigned *offsets, const float4 *recs,
-                                                    const float *recw, unsigned long long capacity, GridPtrs grids,
-                                                    const double *fixed_scale, DevStats *st) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  const int nf = fs.nfields, nst = g.interlace ? 2 : 1, nslot = nf * nst;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  Acc *sm = (Acc *)smraw;
-  const size_t tile_bytes = ((size_t)nslot * tg.slot * sizeof(Acc) + 15) & ~(size_t)15;
-  float *Wst = (float *)(smraw + tile_bytes) + warp * (TAP_RB * 9);
-  int *Ost = (int *)(smraw + tile_bytes) + nwarps * (TAP_RB * 9) + warp * (TAP_RB * 9);
-  float2 *Vst = (float2 *)((int *)(smraw + tile_bytes) + 2 * nwarps * (TAP_RB * 9)) + warp * TAP_RB;
-  const int tile = blockIdx.x;
-  const int bz = tile % tg.nbz, by = (tile / tg.nbz) % tg.nby, bx = tile / (tg.nbz * tg.nby);
-  const int x0 = bx * tg.tx, y0 = by * tg.ty, z0 = bz * tg.tz;
-  const int ex = min(tg.tx, g.nx - x0), ey = min(tg.ty, g.ny - y0), ez = min(tg.tz, g.nz - z0);
-  for (int c = threadIdx.x; c < nslot * tg.slot; c += blockDim.x) sm[c] = (Acc)0;
-  __syncthreads();
-  const double sc0 = fixed_scale ? fixed_scale[0] : 1.0, sc1 = fixed_scale ? fixed_scale[1] : 1.0;
-  // this lane's tap in the deposit phase
-  const int K = g.order;
-  const bool tap_on = lane < K * K * K;
-  const int tdx = tap_on ? lane / (K * K) : 0, tdy = tap_on ? (lane / K) % K : 0, tdz = tap_on ? lane % K : 0;
-  float f_grid = 0.0f, f_out = 0.0f;
-  double d_grid = 0.0, d_out = 0.0;
-  int fatal = 0;
-  unsigned rb = offsets[tile], re = offsets[tile + 1];
-  if (re > capacity) re = (unsigned)capacity;
-  if (rb > re) rb = re;
-  for (unsigned base = rb + warp * TAP_RB; base < re; base += nwarps * TAP_RB) {
-    const unsigned r = base + lane;
-    const bool have = r < re;
-    const int cnt = min((unsigned)TAP_RB, re - base);
-    // ---- this lane's record
-    float4 rec = make_float4(0.f, 0.f, 0.f, 0.f);
-    float w = 1.0f;
-    bool special = false;
-    unsigned idx = 0;
-    double x = 0, y = 0, z = 0, v = 0, wd = 1;
-    if (have) {
-      rec = recs[r];
-      special = rec.x == SPECIAL_MARK;
-      if (special) {
-        idx = __float_as_uint(rec.y);
-        if ((long long)idx >= n) {
-          special = false;
-          rec.x = rec.y = rec.z = -1.0e30f;  // taps nowhere
-        } else {
-          exact_pos(g, fs, in, idx, x, y, z, v, wd);
-          const Prep p = prep32(g, fs, in, idx);
-          if (home_of(g, tg, p.sx, p.sy, p.sz) == tile) {  // statistics with exact decisions
-            if (outside_box(g, x, y, z)) {                   // src/read_data.c:81-88
-              d_out += 1.0;
-              if (g.los == 0) {
-                fatal = 1;
-                atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)idx);
-              }
-            }
-            AxisTaps ax, ay, az;
-            if (exact_axes(g, x, y, z, ax, ay, az)) d_grid += wd;
-          }
-        }
-      } else {
-        w = recw ? recw[r] : 1.0f;
-        if (home_of(g, tg, rec.x, rec.y, rec.z) == tile) {
-          if (accept32(g, rec.x, rec.y, rec.z)) f_grid += w;
-          if (outside32(g, rec.x, rec.y, rec.z)) f_out += 1.0f;  // src/read_data.c:81-88
-        }
-      }
-    }
-    float va, vb;
-    if (special) {
-      va = (float)wpow64(wd, v, fs.ea);
-      vb = (float)wpow64(wd, v, fs.eb);
-    } else {
-      va = w;
-      vb = w;
-      for (int e = 0; e < fs.ea; e++) va *= rec.w;
-      for (int e = 0; e < fs.eb; e++) vb *= rec.w;
-    }
-    Vst[lane] = make_float2(va, vb);
-    for (int stn = 0; stn < nst; stn++) {
-      float *W = Wst + lane * 9;
-      int *O = Ost + lane * 9;
-      if (!have) {
-#pragma unroll
-        for (int k = 0; k < 9; k++) { W[k] = 0.0f; O[k] = 0; }
-      } else if (special) {
-        AxisTaps ax, ay, az;
-        const double px = stn ? DADD(x, g.hx) : x, py = stn ? DADD(y, g.hy) : y, pz = stn ? DADD(z, g.hz) : z;
-        const bool acc = exact_axes(g, px, py, pz, ax, ay, az);
-        if (!acc) {
-#pragma unroll
-          for (int k = 0; k < 9; k++) { W[k] = 0.0f; O[k] = 0; }
-        } else {
-          stage_axis64(g, ax, 0, x0, ex, tg.px, W, O);
-          stage_axis64(g, ay, 1, y0, ey, tg.py, W + 3, O + 3);
-          stage_axis64(g, az, 2, z0, ez, 1, W + 6, O + 6);
-          // CIC rounding edge: y index NY lands in row 0 of the next x slice (src/read_data.c:592-593);
-          // deposited here directly (a handful of taps at most)
-          if (g.order == 2 && ay.n > 0 && ay.idx[0] == g.ny && ay.on[0]) {
-            for (int a = 0; a < ax.n; a++)
-              for (int c = 0; c < az.n; c++) {
-                if (!(ax.on[a] && az.on[c])) continue;
-                long long L = canon_index(g, ax.idx[a], ay.idx[0], az.idx[c]);
-                if (L < 0) continue;
-                int ix, iy, iz;
-                decode(g, L, ix, iy, iz);
-                ix -= x0; iy -= y0; iz -= z0;
-                if (ix < 0 || ix >= ex || iy < 0 || iy >= ey || iz < 0 || iz >= ez) continue;
-                const int cell = ix * tg.px + iy * tg.py + iz;
-                const double tw = DMUL(DMUL(ax.w[a], ay.w[0]), az.w[c]);
-                acc_add64(sm + (stn * nf) * tg.slot + cell, DMUL(wpow64(wd, v, fs.ea), tw), sc0);
-                if (nf == 2) acc_add64(sm + (stn * nf + 1) * tg.slot + cell, DMUL(wpow64(wd, v, fs.eb), tw), sc1);
-              }
-          }
-        }
-      } else {
-        const float sx = stn ? __fadd_rn(rec.x, 0.5f) : rec.x, sy = stn ? __fadd_rn(rec.y, 0.5f) : rec.y,
-                    sz = stn ? __fadd_rn(rec.z, 0.5f) : rec.z;
-        if (!accept32(g, sx, sy, sz)) {
-#pragma unroll
-          for (int k = 0; k < 9; k++) { W[k] = 0.0f; O[k] = 0; }
-        } else {
-          AxisTapsF tx, ty, tz;
-          axis32(g.order, sx, 0, g.nx, g.los, tx);
-          axis32(g.order, sy, 1, g.ny, g.los, ty);
-          axis32(g.order, sz, 1, g.nz, g.los, tz);
-          stage_axis32(tx, x0, ex, tg.px, W, O);
-          stage_axis32(ty, y0, ey, tg.py, W + 3, O + 3);
-          stage_axis32(tz, z0, ez, 1, W + 6, O + 6);
-        }
-      }
-      __syncwarp();
-      // ---- deposit: lane = tap, one record after another
-      Acc *sA = sm + (stn * nf) * tg.slot, *sB = sA + tg.slot;
-      for (int j = 0; j < cnt; j++) {
-        const float *Wj = Wst + j * 9;
-        const int *Oj = Ost + j * 9;
-        const float wt = Wj[tdx] * Wj[3 + tdy] * Wj[6 + tdz];
-        if (tap_on && wt != 0.0f) {
-          const int off = Oj[tdx] + Oj[3 + tdy] + Oj[6 + tdz];
-          const float2 vv = Vst[j];
-          acc_add(sA + off, vv.x * wt, sc0);
-          if (nf == 2) acc_add(sB + off, vv.y * wt, sc1);
-        }
-      }
-      __syncwarp();
-    }
-  }
-  {
-    const double vals[2] = {d_grid + (double)f_grid, d_out + (double)f_out};
-    double *const dst[2] = {&st->ngrid, &st->nout};
-    block_add<2>(vals, dst);
-    if (fatal) atomicOr(&st->fatal, 1);
-  }
-  // ---- write the tile: pairs of cells along z as float2 (rows start 8-byte aligned in global
-  // memory: the padded row length 2*(NZ/2+1) is even)
-  const int tsz = tg.tx * tg.ty * tg.tz;
-  const int npair = tsz >> 1;
-  for (int slot = 0; slot < nslot; slot++) {
-    float *gp = (float *)grids.g[slot];
-    const Acc *s = sm + slot * tg.slot;
-    const double inv = (slot % nf) ? 1.0 / sc1 : 1.0 / sc0;
-    float dsum = 0.0f;  // FP32 over this thread's cells; FP64 across threads
-    unsigned long long fsum = 0;
-    for (int q = threadIdx.x; q < npair; q += blockDim.x) {
-      const int c = q << 1;
-      const int rz = c & (tg.tz - 1), ly = (c >> tg.lz) & (tg.ty - 1), lx = c >> (tg.lz + tg.ly);
-      if (lx >= ex || ly >= ey || rz >= ez) continue;
-      const int sidx = lx * tg.px + ly * tg.py + rz;
-      const Acc a0 = s[sidx], a1 = s[sidx + 1];
-      float v0, v1;
-      if (sizeof(Acc) == 8) {
-        v0 = (float)((double)(long long)a0 * inv);
-        v1 = (float)((double)(long long)a1 * inv);
-        fsum += (unsigned long long)a0 + (rz + 1 < ez ? (unsigned long long)a1 : 0ULL);
-      } else {
-        v0 = (float)a0;
-        v1 = (float)a1;
-        dsum += v0 + (rz + 1 < ez ? v1 : 0.0f);
-      }
-      float *dst = gp + (long long)(x0 + lx) * g.slice + (long long)(y0 + ly) * g.row + z0 + rz;
-      if (rz + 1 < ez) *reinterpret_cast<float2 *>(dst) = make_float2(v0, v1);
-      else dst[0] = v0;
-    }
-    if (sizeof(Acc) == 8) {
-      for (int o = 16; o > 0; o >>= 1) fsum += __shfl_xor_sync(FULL_MASK, fsum, o);
-      if ((threadIdx.x & 31) == 0 && fsum) atomicAdd(&st->dc_fixed[slot], fsum);
-    } else {
-      const double vals[1] = {(double)dsum};
-      double *const dst1[1] = {&st->dc[slot]};
-      block_add<1>(vals, dst1);
-    }
   }
 }
 
@@ -1158,6 +945,300 @@ __global__ void __launch_bounds__(256, 3) k_tile_rec(Geom g, FieldSpec fs, TileG
   block_add_f<NS * NF>(dsums, dsts);
 }
 
+// --------------------------------------------------------------------- deterministic tile paint
+// Tiles with at most this many records accumulate in two-limb cells at a tile scale; denser ones in
+// uint64 cells at the run's global scale (64-bit shared atomics: slower, and rare).
+#define DET_FAST_RECORDS 8192u
+
+// A deposit p (an FP32 value already in the tile's fixed point, |p| < 2^40) split as p = h 2^k + l with
+// h = floor(p 2^-k) and l = p - h 2^k in [0, 2^k] (k <= 22), both made integers by the FMA rounding of
+// rint_small and added with two native int32 shared atomics; the cell's value is hi 2^k + lo. The FMA
+// that forms l is exact except for a negative p of magnitude below 2^k, where the deposit may come out
+// one unit of the fixed point away from round(p): still a fixed function of p, whatever the order.
+__device__ __forceinline__ void limb_add(int *lo, int *hi, float p, float two_mk, float two_k) {
+  const float h = floorf(p * two_mk);
+  const float l = __fmaf_rn(-h, two_k, p);
+  atomicAdd(lo, rint_small(l, 1.0f));
+  atomicAdd(hi, rint_small(h, 1.0f));
+}
+
+// Scale exponent of a tile: (record count) * (largest |w v^e| of its records) * 2^S < 2^40, so that no
+// cell of one pass (each record adds at most |w v^e| 2^S to a cell) leaves the limbs' range. Both inputs
+// are independent of the order of the records.
+__device__ __forceinline__ int det_scale_exp(unsigned cnt, float max_abs) {
+  const float bound = (float)cnt * max_abs * 1.001f;
+  if (!(bound > 0.0f) || !isfinite(bound)) return 0;
+  const int S = 39 - ilogbf(bound);
+  return S > 100 ? 100 : (S < -100 ? -100 : S);
+}
+
+struct DetPass {
+  int *lo, *hi;                  // two-limb cells of field 0 (field 1: + 2 slot); null in the uint64 mode
+  unsigned long long *u;         // uint64 cells of field 0 (field 1: + slot)
+  int slotw;
+  float scA, scB, two_mk, two_k;  // fixed-point scales of the fields; 2^-k, 2^k
+  double sc0, sc1;                // the same scales in FP64 (the CIC rounding-edge products)
+};
+
+template <int NF>
+__device__ __forceinline__ void det_add(const DetPass &d, int off, float pa, float pb) {
+  if (d.lo) {
+    limb_add(d.lo + off, d.hi + off, pa, d.two_mk, d.two_k);
+    if (NF == 2) limb_add(d.lo + 2 * d.slotw + off, d.hi + 2 * d.slotw + off, pb, d.two_mk, d.two_k);
+  } else {
+    atomicAdd(d.u + off, (unsigned long long)__float2ll_rn(pa));
+    if (NF == 2) atomicAdd(d.u + d.slotw + off, (unsigned long long)__float2ll_rn(pb));
+  }
+}
+
+// |w v^e| of one record for the tile's scale: the FP32 value, or for a special record its exact one.
+template <typename T>
+__device__ __forceinline__ void det_record_value(const Geom &g, const FieldSpec &fs, const PIn<T> &in, long long n,
+                                                 const float4 &rec, float w, float &va, float &vb) {
+  if (rec.x == SPECIAL_MARK) {
+    const unsigned idx = __float_as_uint(rec.y);
+    va = vb = 0.0f;
+    if ((long long)idx >= n) return;
+    double x, y, z, v, wd;
+    exact_pos(g, fs, in, idx, x, y, z, v, wd);
+    va = (float)wpow64(wd, v, fs.ea);
+    vb = (float)wpow64(wd, v, fs.eb);
+    return;
+  }
+  va = w;
+  vb = w;
+  for (int e = 0; e < fs.ea; e++) va *= rec.w;
+  for (int e = 0; e < fs.eb; e++) vb *= rec.w;
+}
+
+// The exact FP64 rules of one special record (a particle within a few ulps of a discontinuity of the
+// reference's rules, listed by its index) for stencil stn: its taps inside this tile. With stats its
+// home tile also counts it in NGRID, in the out-of-box count and for the LOS == 0 error.
+template <typename T, int NF>
+__device__ void det_special(const Geom &g, const FieldSpec &fs, const TileGeo &tg, const PIn<T> &in, long long n,
+                            unsigned idx, int tile, int x0, int y0, int z0, int ex, int ey, int ez, int stn,
+                            bool stats, const DetPass &d, double &d_grid, double &d_out, int &fatal, DevStats *st) {
+  if ((long long)idx >= n) return;
+  double x, y, z, v, wd;
+  exact_pos(g, fs, in, idx, x, y, z, v, wd);
+  if (stats) {
+    const Prep p = prep32(g, fs, in, idx);
+    if (home_of(g, tg, p.sx, p.sy, p.sz) == tile) {
+      if (outside_box(g, x, y, z)) {  // src/read_data.c:81-88
+        d_out += 1.0;
+        if (g.los == 0) {
+          fatal = 1;
+          atomicMax(&st->fatal_inv, ~0ULL - (unsigned long long)idx);
+        }
+      }
+      AxisTaps ax, ay, az;
+      if (exact_axes(g, x, y, z, ax, ay, az)) d_grid += wd;
+    }
+  }
+  const double va64 = wpow64(wd, v, fs.ea), vb64 = wpow64(wd, v, fs.eb);
+  const float va = (float)va64 * d.scA, vb = (float)vb64 * d.scB;
+  AxisTaps ax, ay, az;
+  const double px = stn ? DADD(x, g.hx) : x, py = stn ? DADD(y, g.hy) : y, pz = stn ? DADD(z, g.hz) : z;
+  if (!exact_axes(g, px, py, pz, ax, ay, az)) return;
+  float W[9];
+  int O[9];
+  stage_axis64(g, ax, 0, x0, ex, tg.px, W, O);
+  stage_axis64(g, ay, 1, y0, ey, tg.py, W + 3, O + 3);
+  stage_axis64(g, az, 2, z0, ez, 1, W + 6, O + 6);
+  // CIC rounding edge: y index NY lands in row 0 of the next x slice (src/read_data.c:592-593)
+  if (g.order == 2 && ay.n > 0 && ay.idx[0] == g.ny && ay.on[0]) {
+    for (int a = 0; a < ax.n; a++)
+      for (int c = 0; c < az.n; c++) {
+        if (!(ax.on[a] && az.on[c])) continue;
+        const long long L = canon_index(g, ax.idx[a], ay.idx[0], az.idx[c]);
+        if (L < 0) continue;
+        int ix, iy, iz;
+        decode(g, L, ix, iy, iz);
+        ix -= x0;
+        iy -= y0;
+        iz -= z0;
+        if (ix < 0 || ix >= ex || iy < 0 || iy >= ey || iz < 0 || iz >= ez) continue;
+        const double tw = DMUL(DMUL(ax.w[a], ay.w[0]), az.w[c]);
+        det_add<NF>(d, ix * tg.px + iy * tg.py + iz, (float)(DMUL(va64, tw) * d.sc0), (float)(DMUL(vb64, tw) * d.sc1));
+      }
+  }
+  for (int a = 0; a < 3; a++)
+    for (int b2 = 0; b2 < 3; b2++)
+      for (int c = 0; c < 3; c++) {
+        const float wt = W[a] * W[3 + b2] * W[6 + c];
+        if (wt != 0.0f) det_add<NF>(d, O[a] + O[3 + b2] + O[6 + c], va * wt, vb * wt);
+      }
+}
+
+// Deterministic tile kernel (k_count -> k_scan -> k_scatter -> here): one CTA per tile and, as in k_tile_rec,
+// lane = record; the two stencils one after the other (one pass each over the tile's records), each pass
+// holding both fields of its stencil in shared memory as int64 fixed point. The cells of a tile with at most
+// DET_FAST_RECORDS records are two int32 limbs at the tile's own scale (det_scale_exp: from the record count
+// and the largest |w v^e|, both independent of the order of the records); denser tiles use uint64 cells at
+// the run's global scale (k_scan: the catalogue's sum of |w v^e| times 2^S below 2^62). A deposit is the FP32
+// product at that scale rounded once to an integer, and integer addition makes every cell, and so the grids,
+// independent of the order of the deposits: bit-reproducible. Special records take the exact FP64 rules
+// here (det_special). The home tile of each record counts it in NGRID and the out-of-box count (k_count only
+// counted the tiles); the slots' DC sums go to the exact global integer sums at the global scale.
+template <typename T, int K, int NF, bool IL>
+__global__ void __launch_bounds__(256, 3) k_tile_rec_det(Geom g, FieldSpec fs, TileGeo tg, PIn<T> in, long long n,
+                                                         const unsigned *offsets, const float4 *recs,
+                                                         const float *recw, unsigned long long capacity,
+                                                         GridPtrs grids, const double *fixed_scale, DevStats *st) {
+  extern __shared__ __align__(16) int smd[];
+  constexpr int NS = IL ? 2 : 1;
+  const int tile = blockIdx.x;
+  const int bz = tile % tg.nbz, by = (tile / tg.nbz) % tg.nby, bx = tile / (tg.nbz * tg.nby);
+  const int x0 = bx * tg.tx, y0 = by * tg.ty, z0 = bz * tg.tz;
+  const int ex = min(tg.tx, g.nx - x0), ey = min(tg.ty, g.ny - y0), ez = min(tg.tz, g.nz - z0);
+  const int slotw = tg.slot;
+  unsigned long long rb = offsets[tile], re = offsets[tile + 1];
+  if (re > capacity) re = capacity;
+  if (rb > re) rb = re;
+  const unsigned cnt = (unsigned)(re - rb);
+  const bool fast = cnt <= DET_FAST_RECORDS;
+  __shared__ float red_max[2][32];
+  float ma = 0.0f, mb = 0.0f;
+  if (fast) {  // the tile's largest |w v^e| per field
+    for (unsigned long long r = rb + threadIdx.x; r < re; r += blockDim.x) {
+      float va, vb;
+      det_record_value(g, fs, in, n, recs[r], recw ? recw[r] : 1.0f, va, vb);
+      ma = fmaxf(ma, fabsf(va));
+      mb = fmaxf(mb, fabsf(vb));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      ma = fmaxf(ma, __shfl_xor_sync(FULL_MASK, ma, o));
+      mb = fmaxf(mb, __shfl_xor_sync(FULL_MASK, mb, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      red_max[0][threadIdx.x >> 5] = ma;
+      red_max[1][threadIdx.x >> 5] = mb;
+    }
+    __syncthreads();
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+      ma = fmaxf(ma, red_max[0][k]);
+      mb = fmaxf(mb, red_max[1][k]);
+    }
+  }
+  const double G0 = fixed_scale[0], G1 = fixed_scale[1];
+  const int SA = det_scale_exp(cnt, ma), SB = det_scale_exp(cnt, mb);
+  const int kb = 31 - (32 - __clz(cnt));  // k with cnt 2^k < 2^31
+  const int k = kb > 22 ? 22 : kb;
+  DetPass d;
+  d.slotw = slotw;
+  if (fast) {
+    d.lo = smd;
+    d.hi = smd + slotw;
+    d.u = nullptr;
+    d.scA = ldexpf(1.0f, SA);
+    d.scB = ldexpf(1.0f, SB);
+    d.two_mk = ldexpf(1.0f, -k);
+    d.two_k = ldexpf(1.0f, k);
+  } else {
+    d.lo = d.hi = nullptr;
+    d.u = reinterpret_cast<unsigned long long *>(smd);
+    d.scA = (float)G0;
+    d.scB = (float)G1;
+    d.two_mk = d.two_k = 1.0f;
+  }
+  d.sc0 = (double)d.scA;
+  d.sc1 = (double)d.scB;
+  float f_grid = 0.0f, f_out = 0.0f;
+  double d_grid = 0.0, d_out = 0.0;
+  int fatal = 0;
+#pragma unroll 1
+  for (int stn = 0; stn < NS; stn++) {
+    for (int c = threadIdx.x; c < NF * 2 * slotw; c += blockDim.x) smd[c] = 0;
+    __syncthreads();
+    for (unsigned long long r = rb + threadIdx.x; r < re; r += blockDim.x) {
+      const float4 rec = recs[r];
+      if (rec.x == SPECIAL_MARK) {
+        det_special<T, NF>(g, fs, tg, in, n, __float_as_uint(rec.y), tile, x0, y0, z0, ex, ey, ez, stn, stn == 0, d,
+                           d_grid, d_out, fatal, st);
+        continue;
+      }
+      const float w = recw ? recw[r] : 1.0f;
+      if (stn == 0 && home_of(g, tg, rec.x, rec.y, rec.z) == tile) {
+        if (accept32(g, rec.x, rec.y, rec.z)) f_grid += w;
+        if (outside32(g, rec.x, rec.y, rec.z)) f_out += 1.0f;  // src/read_data.c:81-88
+      }
+      float va = w, vb = w;
+      for (int e = 0; e < fs.ea; e++) va *= rec.w;
+      for (int e = 0; e < fs.eb; e++) vb *= rec.w;
+      va *= d.scA;
+      vb *= d.scB;
+      const float sx = stn ? __fadd_rn(rec.x, 0.5f) : rec.x, sy = stn ? __fadd_rn(rec.y, 0.5f) : rec.y,
+                  sz = stn ? __fadd_rn(rec.z, 0.5f) : rec.z;
+      if (!accept32(g, sx, sy, sz)) continue;
+      AxisTapsF ax, ay, az;
+      axis32k<K>(sx, 0, g.nx, g.los, ax);
+      axis32k<K>(sy, 1, g.ny, g.los, ay);
+      axis32k<K>(sz, 1, g.nz, g.los, az);
+      float wx[3], wy[3], wz[3];
+      int ox[3], oy[3], oz[3];
+      stage_axis32(ax, x0, ex, tg.px, wx, ox);
+      stage_axis32(ay, y0, ey, tg.py, wy, oy);
+      stage_axis32(az, z0, ez, 1, wz, oz);
+#pragma unroll
+      for (int a = 0; a < K; a++)
+#pragma unroll
+        for (int b2 = 0; b2 < K; b2++) {
+          const float wxy = wx[a] * wy[b2];
+          if (wxy == 0.0f) continue;
+          const float pa = va * wxy, pb = vb * wxy;
+          const int oxy = ox[a] + oy[b2];
+#pragma unroll
+          for (int c = 0; c < K; c++)
+            if (wz[c] != 0.0f) det_add<NF>(d, oxy + oz[c], pa * wz[c], pb * wz[c]);
+        }
+    }
+    __syncthreads();
+    // write this stencil's slots: pairs of cells along z as float2 (rows start 8-byte aligned in global
+    // memory: the padded row length 2*(NZ/2+1) is even); the slots' integer DC sums at the global scale
+    const int npair = (tg.tx * tg.ty * tg.tz) >> 1;
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+      const int slot = stn * NF + f;
+      float *gp = (float *)grids.g[slot];
+      const double inv = fast ? ldexp(1.0, -(f ? SB : SA)) : 1.0 / (f ? G1 : G0);
+      long long isum = 0;
+      for (int q = threadIdx.x; q < npair; q += blockDim.x) {
+        const int c = q << 1;
+        const int rz = c & (tg.tz - 1), ly = (c >> tg.lz) & (tg.ty - 1), lx = c >> (tg.lz + tg.ly);
+        if (lx >= ex || ly >= ey || rz >= ez) continue;
+        const int sidx = lx * tg.px + ly * tg.py + rz;
+        long long a0, a1;
+        if (fast) {
+          const int *lo = smd + 2 * f * slotw, *hi = lo + slotw;
+          a0 = (long long)hi[sidx] * (1ll << k) + (long long)lo[sidx];
+          a1 = (long long)hi[sidx + 1] * (1ll << k) + (long long)lo[sidx + 1];
+        } else {
+          const unsigned long long *u = reinterpret_cast<const unsigned long long *>(smd) + f * slotw;
+          a0 = (long long)u[sidx];
+          a1 = (long long)u[sidx + 1];
+        }
+        const bool two = rz + 1 < ez;
+        isum += a0 + (two ? a1 : 0ll);
+        float *dst = gp + (long long)(x0 + lx) * g.slice + (long long)(y0 + ly) * g.row + z0 + rz;
+        if (two) *reinterpret_cast<float2 *>(dst) = make_float2((float)((double)a0 * inv), (float)((double)a1 * inv));
+        else dst[0] = (float)((double)a0 * inv);
+      }
+      for (int o = 16; o > 0; o >>= 1) isum += __shfl_xor_sync(FULL_MASK, isum, o);
+      if ((threadIdx.x & 31) == 0 && isum) {
+        // to the global scale: exact (a power of two) where it is the finer one, else rounded once
+        const long long gsum = fast ? __double2ll_rn((double)isum * ((f ? G1 : G0) * inv)) : isum;
+        atomicAdd(&st->dc_fixed[slot], (unsigned long long)gsum);
+      }
+    }
+    __syncthreads();
+  }
+  const double vals[2] = {d_grid + (double)f_grid, d_out + (double)f_out};
+  double *const dst[2] = {&st->ngrid, &st->nout};
+  block_add<2>(vals, dst);
+  if (fatal) atomicOr(&st->fatal, 1);
+}
+
 // Bucket mode: records that found their tile's bucket full, deposited after the tiles were written
 // (FP32 global atomics), each restricted to the taps inside its own tile, with their DC sums.
 template <int K, int NF, bool IL>
@@ -1301,8 +1382,10 @@ static int log2i(int p) {
 }
 
 TileGeo choose_tiles(const Geom &g, int nslots, int deterministic) {
-  // 4 grid slots x 8x16x32 floats = 64 KB (three CTAs per SM); the int64 variant halves the volume.
-  if (deterministic) return make_tiles(g, (nslots > 2) ? 4 : 8, 16, 32);
+  // 4 grid slots x 8x16x32 floats = 64 KB (three CTAs per SM). The deterministic kernel holds one stencil's
+  // fields at a time, as 8-byte cells: the same tiles for two fields (or one field interlaced), the
+  // 16x16x32 ones for a single field otherwise.
+  if (deterministic) return make_tiles(g, nslots == 1 ? 16 : 8, 16, 32);
   return make_tiles(g, nslots <= 2 ? 16 : 8, 16, 32);
 }
 
@@ -1332,9 +1415,7 @@ TileGeo make_tiles(const Geom &g, int tx, int ty, int tz) {
 }
 
 size_t tile_smem_bytes(const TileGeo &tg, int nslots, int deterministic) {
-  const size_t tile = ((size_t)nslots * tg.slot * (deterministic ? 8 : 4) + 15) & ~(size_t)15;
-  const size_t stage = (size_t)(256 / 32) * TAP_RB * (9 * 4 + 9 * 4 + 8);
-  return tile + stage;
+  return ((size_t)nslots * tg.slot * (deterministic ? 8 : 4) + 15) & ~(size_t)15;
 }
 
 size_t rec_smem_bytes(const TileGeo &tg, int nslots) { return (size_t)nslots * tg.slot * 4; }
@@ -1367,6 +1448,28 @@ static void launch_rec_k(cudaStream_t s, const Geom &g, const FieldSpec &fs, con
   } else {
     if (g.interlace) launch_rec<K, 1, true>(s, g, fs, tg, b, weights, grids, st);
     else launch_rec<K, 1, false>(s, g, fs, tg, b, weights, grids, st);
+  }
+}
+
+template <typename T, int K, int NF, bool IL>
+static void launch_det(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, const PIn<T> &in,
+                       long long n, const PaintBufs &b, const GridPtrs &grids, DevStats *st) {
+  const size_t smem = tile_smem_bytes(tg, NF, 1);
+  cudaFuncSetAttribute(k_tile_rec_det<T, K, NF, IL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_tile_rec_det<T, K, NF, IL><<<tg.ntiles, 256, smem, s>>>(g, fs, tg, in, n, b.offsets, b.recs,
+                                                            in.w ? b.recw : nullptr, b.capacity, grids, b.fixed_scale,
+                                                            st);
+}
+
+template <typename T, int K>
+static void launch_det_k(cudaStream_t s, const Geom &g, const FieldSpec &fs, const TileGeo &tg, const PIn<T> &in,
+                         long long n, const PaintBufs &b, const GridPtrs &grids, DevStats *st) {
+  if (fs.nfields == 2) {
+    if (g.interlace) launch_det<T, K, 2, true>(s, g, fs, tg, in, n, b, grids, st);
+    else launch_det<T, K, 2, false>(s, g, fs, tg, in, n, b, grids, st);
+  } else {
+    if (g.interlace) launch_det<T, K, 1, true>(s, g, fs, tg, in, n, b, grids, st);
+    else launch_det<T, K, 1, false>(s, g, fs, tg, in, n, b, grids, st);
   }
 }
 
@@ -1408,13 +1511,10 @@ static void run_paint32(cudaStream_t s, const Geom &g, const FieldSpec &fs, cons
   k_scatter<T><<<nb, th, 0, s>>>(g, fs, tg, in, n, b.cursor, b.recs, in.w ? b.recw : nullptr, b.capacity,
                                  split ? b.edge_list : nullptr, b.edge_count);
   if (det) {
-    const int nslot = fs.nfields * (g.interlace ? 2 : 1);
-    const size_t smem = tile_smem_bytes(tg, nslot, 1);
-    cudaFuncSetAttribute(k_tile_paint<T, unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (b.tile_ev0) cudaEventRecord(b.tile_ev0, s);
-    k_tile_paint<T, unsigned long long><<<tg.ntiles, 256, smem, s>>>(g, fs, tg, in, n, b.offsets, b.recs,
-                                                                      in.w ? b.recw : nullptr, b.capacity, grids,
-                                                                      b.fixed_scale, st);
+    if (g.order == 3) launch_det_k<T, 3>(s, g, fs, tg, in, n, b, grids, st);
+    else if (g.order == 2) launch_det_k<T, 2>(s, g, fs, tg, in, n, b, grids, st);
+    else launch_det_k<T, 1>(s, g, fs, tg, in, n, b, grids, st);
     if (b.tile_ev1) cudaEventRecord(b.tile_ev1, s);
     *launches += 4;
   } else {
