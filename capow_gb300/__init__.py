@@ -152,7 +152,7 @@ def lib() -> ctypes.CDLL:
     L.capow_batch.argtypes = [ctypes.POINTER(_Mock), ip, O, ip]
     L.capow_batch_release.restype = None
     L.capow_batch_release.argtypes = []
-    L.capow_backward.argtypes = [vp, ctypes.POINTER(ctypes.POINTER(ctypes.c_double) * 5), ctypes.POINTER(_Grads)]
+    L.capow_backward.argtypes = [vp, ctypes.POINTER(ctypes.POINTER(ctypes.c_double)), ctypes.POINTER(_Grads)]
     L.capow_power.argtypes = [vp, ctypes.POINTER(_Spectrum), ip]
     L.capow_normalise.argtypes = [P, ctypes.POINTER(_Spectrum)]
     L.capow_num_spectra.argtypes = [vp]
@@ -442,16 +442,21 @@ class PowerSpectrum:
             out.append(d)
         return out
 
-    def backward(self, dL_dP: dict, out=None) -> dict:
+    def backward(self, dL_dP, out=None) -> dict:
         """capow_backward: gradients of a loss with respect to the last painted catalogue.
 
-        dL_dP maps "Pk0".."Pk4" to arrays of NK (missing keys: zero). Returns a dict of float64
-        host arrays dx, dy, dz, dvlos, dw; or pass `out`, a dict of contiguous device arrays
+        dL_dP maps "Pk0".."Pk4" to arrays of NK (missing keys: zero) for a context with one spectrum,
+        or is a list of such dicts, one per spectrum in the order power() returns them. Returns a dict
+        of float64 host arrays dx, dy, dz, dvlos, dw; or pass `out`, a dict of contiguous device arrays
         (torch tensors) of the particles' dtype, to receive them on the device."""
         p = self.params
-        arrs = [np.ascontiguousarray(dL_dP.get(f"Pk{l}", np.zeros(p.NK)), dtype=np.float64) for l in range(5)]
-        ptrs = (ctypes.POINTER(ctypes.c_double) * 5)(*[a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-                                                        for a in arrs])
+        per = [dL_dP] if isinstance(dL_dP, dict) else list(dL_dP)
+        nspec = lib().capow_num_spectra(self._ctx)
+        if len(per) != nspec:
+            raise ValueError(f"backward needs dL/dP for each of the context's {nspec} spectra")
+        arrs = [np.ascontiguousarray(d.get(f"Pk{l}", np.zeros(p.NK)), dtype=np.float64) for d in per for l in range(5)]
+        ptrs = (ctypes.POINTER(ctypes.c_double) * len(arrs))(*[a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+                                                                for a in arrs])
         names = ("dx", "dy", "dz", "dvlos", "dw")
         if out is not None:
             t = next(iter(out.values()))

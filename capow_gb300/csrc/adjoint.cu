@@ -1,20 +1,25 @@
-// capow_backward: the adjoint of the periodic density-multipole pipeline (paint -> mean subtraction
-// -> 3-D FFT -> interlace combine -> deconvolved Legendre binning -> output_power normalisation),
-// giving dL/d(x, y, z, v_los, w) of every particle from dL/dP_l(k). The reference has no adjoint;
-// the forward it inverts is src/read_data.c:32-179, 514-745 and src/main.c:106-148, 211-225,
-// 266-271, 302-468, 1019-1056.
+// capow_backward: the adjoint of the periodic multipole pipeline (paint -> mean subtraction -> 3-D FFT ->
+// interlace combine -> deconvolved Legendre binning -> output_power normalisation), giving dL/d(x, y, z,
+// v_los, w) of every particle from dL/dP_l(k) of every spectrum of the context: the density and the
+// momentum fields (any Momentum, or the dd / dp / pp selection) and their products |A|^2, Re A*B, Im A*B,
+// |B|^2. The reference has no adjoint; the forward it inverts is src/read_data.c:32-179, 514-745 and
+// src/main.c:106-148, 211-225, 266-271, 302-468, 1019-1056.
 //
 // Steps, all on the context's stream:
 //  1. repaint the last catalogue and take the full 3-D R2C transform of every slot;
-//  2. per half-space mode k: Gamma = dL/dF'(k) = 2 NM gc sum_l c_l(bin) L_l(mu) F'(k), with
-//     F' = F + e Fi the interlace combine and c_l = dL/dP_l * (2l+1) / (Nmodes * norm); the slots
-//     get Gamma and conj(e) Gamma;
+//  2. per half-space mode k, the gradient with respect to each interlace-combined field (as the pair
+//     dL/dRe, dL/dIm, written as a complex number):
+//       dL/dA' = NM gc sum_l L_l(mu) (2 c_AA,l A' + c_ReAB,l B' - i c_ImAB,l B'),
+//       dL/dB' = NM gc sum_l L_l(mu) (c_ReAB,l A' + i c_ImAB,l A' + 2 c_BB,l B'),
+//     with c_q,l = sum over the spectra of product q of dL/dP_l * (2l+1) / (Nmodes * norm); the normal
+//     slot of a field gets it and the interlaced slot conj(e) times it (A' = A + e A_interlaced);
 //  3. Hermitian completion: Phi = Gamma / 2 off the kz = 0 and kz = NZ/2 planes, and
 //     Phi(k) = (Gamma(k) + conj Gamma(-k)) / 2 on them, so that the unnormalised C2R transform of Phi
 //     is exactly dL/dgrid(x) = Re sum_k Gamma(k) e^{+i k.x};
-//  4. per particle: the transpose of its deposit (the same taps, halo fold and dropped writes) read
-//     from dL/dgrid with the weight derivatives, plus the dependence of NGRID (shot, norm and the
-//     mean subtraction) for the weights.
+//  4. per particle: the transpose of its deposit into each field (the same taps, halo fold and dropped
+//     writes) read from dL/dgrid with the derivatives of the deposit values w v^e, plus the dependence
+//     of NGRID (shot, norm and the mean subtraction of the density) on the accepted weights and of the
+//     shot noise's velocity moment sum w v^m / sum w on every particle read.
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <math.h>
@@ -37,6 +42,12 @@ struct AdjC<double> {
   typedef double2 C;
 };
 
+// The grid slots, stencil * fields + field: A, (B,) A interlaced, (B interlaced).
+template <typename R>
+struct AdjSlots {
+  typename AdjC<R>::C *s[4];
+};
+
 // Hermitian multiplicity NM, src/main.c:422-429 (as in the bin kernels)
 __device__ __forceinline__ int adj_nm(int i, int j, int k, int xhalf) {
   if (k != 0) return 2;
@@ -54,73 +65,100 @@ __device__ __forceinline__ int adj_bin(const double *E, int nk, double s) {
   return lo - 1;
 }
 
-// dL/dF'(k) for one half-space mode, returned for the normal slot (gA) and the interlaced slot (gAi).
-template <typename R>
-__device__ __forceinline__ void adj_gamma(const BinParams &bp, const BinTables &t, const double *coef, int i, int j,
-                                          int k, const typename AdjC<R>::C *gA, const typename AdjC<R>::C *gAi,
-                                          const double *dcv, double2 &gF, double2 &gFi) {
-  gF = make_double2(0.0, 0.0);
-  gFi = make_double2(0.0, 0.0);
+__device__ __forceinline__ double2 adj_cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// dL/dF(k) of every slot for one half-space mode. coef: [product][5][nk] (products |A|^2, Re A*B, Im A*B,
+// |B|^2); pmask: the products with a nonzero coefficient.
+template <typename R, int NF>
+__device__ __forceinline__ void adj_gamma(const BinParams &bp, const BinTables &t, const double *coef, int pmask,
+                                          int i, int j, int k, const AdjSlots<R> &sl, const double *dcv,
+                                          double2 *g) {
+  constexpr int NSMAX = 2 * NF;
+#pragma unroll
+  for (int q = 0; q < NSMAX; q++) g[q] = make_double2(0.0, 0.0);
   const double s = __dadd_rn(__dadd_rn(t.fx2d[i], t.fy2d[j]), t.fz2d[k]);
   const int b = adj_bin(t.E, bp.nk, s);
   if (b < 0 || b >= bp.nk) return;
   const long long off = ((long long)i * bp.ny + j) * bp.nzc + k;
   const bool dc = (i == 0 && j == 0 && k == 0);
-  double2 F = make_double2((double)gA[off].x, (double)gA[off].y);
-  if (dc) F = make_double2(dcv[0], 0.0);
-  double2 e = make_double2(1.0, 0.0), Fp = F;
+  double2 F[NSMAX];
+  const int ns = bp.interlace ? NSMAX : NF;
+  for (int q = 0; q < ns; q++) {
+    F[q] = make_double2((double)sl.s[q][off].x, (double)sl.s[q][off].y);
+    if (dc) F[q] = make_double2(dcv[q], 0.0);
+  }
+  double2 e = make_double2(1.0, 0.0);
+  double2 A = F[0], B = NF == 2 ? F[1] : make_double2(0.0, 0.0);
   double gc = t.cxd[i] * t.cyd[j] * t.czd[k] * (double)adj_nm(i, j, k, bp.xhalf);
   if (bp.interlace) {
-    double2 Fi = make_double2((double)gAi[off].x, (double)gAi[off].y);
-    if (dc) Fi = make_double2(dcv[1], 0.0);
-    const double2 ex = t.exd[i], ey = t.eyd[j], ez = t.ezd[k];
-    const double2 exy = make_double2(ex.x * ey.x - ex.y * ey.y, ex.x * ey.y + ex.y * ey.x);
-    e = make_double2(exy.x * ez.x - exy.y * ez.y, exy.x * ez.y + exy.y * ez.x);
-    Fp = make_double2(F.x + Fi.x * e.x - Fi.y * e.y, F.y + Fi.x * e.y + Fi.y * e.x);
+    e = adj_cmul(adj_cmul(t.exd[i], t.eyd[j]), t.ezd[k]);
+    const double2 ai = adj_cmul(F[NF], e);
+    A = make_double2(A.x + ai.x, A.y + ai.y);
+    if (NF == 2) {
+      const double2 bi = adj_cmul(F[NF + 1], e);
+      B = make_double2(B.x + bi.x, B.y + bi.y);
+    }
     gc *= 0.25;
   }
   const double fl = bp.los == 1 ? t.fxd[i] : (bp.los == 2 ? t.fyd[j] : t.fzd[k]);
   const double mu = s > 0.0 ? fl / sqrt(s) : 0.0, mu2 = mu * mu;
+  const double Lv[5] = {1.0, mu, 1.5 * mu2 - 0.5, (2.5 * mu2 - 1.5) * mu, (4.375 * mu2 - 3.75) * mu2 + 0.375};
   const int nk = bp.nk;
-  double G = coef[0 * nk + b] + coef[2 * nk + b] * (1.5 * mu2 - 0.5) +
-             coef[4 * nk + b] * ((4.375 * mu2 - 3.75) * mu2 + 0.375);
-  if (bp.odd) G += coef[1 * nk + b] * mu + coef[3 * nk + b] * ((2.5 * mu2 - 1.5) * mu);
-  G *= 2.0 * gc;
-  gF = make_double2(G * Fp.x, G * Fp.y);
-  if (bp.interlace) gFi = make_double2(e.x * gF.x + e.y * gF.y, e.x * gF.y - e.y * gF.x);  // conj(e) * gF
+  double G[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    if (!((pmask >> q) & 1)) continue;
+    for (int l = 0; l < 5; l++) {
+      if ((l & 1) && !bp.odd) continue;
+      G[q] += coef[(q * 5 + l) * nk + b] * Lv[l];
+    }
+    G[q] *= gc;
+  }
+  // dL/dA' and dL/dB' as (dL/dRe, dL/dIm)
+  double2 gA = make_double2(2.0 * G[0] * A.x + G[1] * B.x + G[2] * B.y, 2.0 * G[0] * A.y + G[1] * B.y - G[2] * B.x);
+  g[0] = gA;
+  double2 gB = make_double2(0.0, 0.0);
+  if (NF == 2) {
+    gB = make_double2(G[1] * A.x - G[2] * A.y + 2.0 * G[3] * B.x, G[1] * A.y + G[2] * A.x + 2.0 * G[3] * B.y);
+    g[1] = gB;
+  }
+  if (bp.interlace) {  // conj(e) times the combined field's gradient
+    g[NF] = make_double2(e.x * gA.x + e.y * gA.y, e.x * gA.y - e.y * gA.x);
+    if (NF == 2) g[NF + 1] = make_double2(e.x * gB.x + e.y * gB.y, e.x * gB.y - e.y * gB.x);
+  }
 }
 
 // Step 2+3 off the self-conjugate planes: Phi = Gamma / 2, in place.
-template <typename R>
-__global__ void __launch_bounds__(256) k_adj_modes(BinParams bp, BinTables t, const double *coef,
-                                                   typename AdjC<R>::C *gA, typename AdjC<R>::C *gAi,
-                                                   const double *dcv, int kz_lo, int kz_hi) {
+template <typename R, int NF>
+__global__ void __launch_bounds__(256) k_adj_modes(BinParams bp, BinTables t, const double *coef, int pmask,
+                                                   AdjSlots<R> sl, const double *dcv, int kz_lo, int kz_hi) {
   const int nkz = kz_hi - kz_lo;
   if (nkz <= 0) return;
+  const int ns = bp.interlace ? 2 * NF : NF;
   const long long total = (long long)bp.nx * bp.ny * nkz;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
        q += (long long)gridDim.x * blockDim.x) {
     const int k = kz_lo + (int)(q % nkz);
     const long long r = q / nkz;
     const int j = (int)(r % bp.ny), i = (int)(r / bp.ny);
-    double2 gF, gFi;
-    adj_gamma<R>(bp, t, coef, i, j, k, gA, gAi, dcv, gF, gFi);
+    double2 g[2 * NF];
+    adj_gamma<R, NF>(bp, t, coef, pmask, i, j, k, sl, dcv, g);
     const long long off = ((long long)i * bp.ny + j) * bp.nzc + k;
-    gA[off].x = (R)(0.5 * gF.x);
-    gA[off].y = (R)(0.5 * gF.y);
-    if (bp.interlace) {
-      gAi[off].x = (R)(0.5 * gFi.x);
-      gAi[off].y = (R)(0.5 * gFi.y);
+    for (int s = 0; s < ns; s++) {
+      sl.s[s][off].x = (R)(0.5 * g[s].x);
+      sl.s[s][off].y = (R)(0.5 * g[s].y);
     }
   }
 }
 
 // Step 2+3 on one self-conjugate plane kz: each mode pair (k, -k) by the thread of its lower index.
-// Also records Re Gamma(0) of both slots (the mean subtraction makes F(0) = sum - NGRID).
-template <typename R>
-__global__ void __launch_bounds__(256) k_adj_plane(BinParams bp, BinTables t, const double *coef,
-                                                   typename AdjC<R>::C *gA, typename AdjC<R>::C *gAi,
-                                                   const double *dcv, int kz, double *gamma0) {
+// Also records Re Gamma(0) of the density's slots (its mean subtraction makes F(0) = sum - NGRID).
+template <typename R, int NF>
+__global__ void __launch_bounds__(256) k_adj_plane(BinParams bp, BinTables t, const double *coef, int pmask,
+                                                   AdjSlots<R> sl, const double *dcv, int kz, double *gamma0) {
+  const int ns = bp.interlace ? 2 * NF : NF;
   const long long total = (long long)bp.nx * bp.ny;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
        q += (long long)gridDim.x * blockDim.x) {
@@ -128,34 +166,27 @@ __global__ void __launch_bounds__(256) k_adj_plane(BinParams bp, BinTables t, co
     const int i2 = (bp.nx - i) % bp.nx, j2 = (bp.ny - j) % bp.ny;
     const long long q2 = (long long)i2 * bp.ny + j2;
     if (q2 < q) continue;  // the partner's thread handles the pair
-    double2 a, ai, b, bi;
-    adj_gamma<R>(bp, t, coef, i, j, kz, gA, gAi, dcv, a, ai);
+    double2 a[2 * NF], b[2 * NF];
+    adj_gamma<R, NF>(bp, t, coef, pmask, i, j, kz, sl, dcv, a);
     if (kz == 0 && i == 0 && j == 0) {
-      gamma0[0] = a.x;
-      gamma0[1] = ai.x;
+      gamma0[0] = a[0].x;
+      gamma0[1] = bp.interlace ? a[NF].x : 0.0;
     }
     const long long off = ((long long)i * bp.ny + j) * bp.nzc + kz, off2 = ((long long)i2 * bp.ny + j2) * bp.nzc + kz;
     if (q2 == q) {  // self-conjugate mode: Phi = Re Gamma
-      gA[off].x = (R)a.x;
-      gA[off].y = (R)0;
-      if (bp.interlace) {
-        gAi[off].x = (R)ai.x;
-        gAi[off].y = (R)0;
+      for (int s = 0; s < ns; s++) {
+        sl.s[s][off].x = (R)a[s].x;
+        sl.s[s][off].y = (R)0;
       }
       continue;
     }
-    adj_gamma<R>(bp, t, coef, i2, j2, kz, gA, gAi, dcv, b, bi);
-    const double2 p = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));  // (Gamma(k) + conj Gamma(-k)) / 2
-    gA[off].x = (R)p.x;
-    gA[off].y = (R)p.y;
-    gA[off2].x = (R)p.x;
-    gA[off2].y = (R)(-p.y);
-    if (bp.interlace) {
-      const double2 pi = make_double2(0.5 * (ai.x + bi.x), 0.5 * (ai.y - bi.y));
-      gAi[off].x = (R)pi.x;
-      gAi[off].y = (R)pi.y;
-      gAi[off2].x = (R)pi.x;
-      gAi[off2].y = (R)(-pi.y);
+    adj_gamma<R, NF>(bp, t, coef, pmask, i2, j2, kz, sl, dcv, b);
+    for (int s = 0; s < ns; s++) {
+      const double2 p = make_double2(0.5 * (a[s].x + b[s].x), 0.5 * (a[s].y - b[s].y));  // (Gamma(k) + conj Gamma(-k)) / 2
+      sl.s[s][off].x = (R)p.x;
+      sl.s[s][off].y = (R)p.y;
+      sl.s[s][off2].x = (R)p.x;
+      sl.s[s][off2].y = (R)(-p.y);
     }
   }
 }
@@ -177,22 +208,42 @@ __device__ __forceinline__ void adj_axis_deriv(int order, double scale, double *
   }
 }
 
-// dL/d(particle) from the deposit's gradient sums: g0 = sum G W, gs = sum G dW/dscale per axis.
+// What the readout needs beyond the gradient grids: dL/dNGRID (for the accepted weights) and the shot
+// noise's moments: dL/d(sum w v^m / sum w) for m = 1..4, with that ratio c[m] and sum w over the catalogue.
+struct AdjScalars {
+  double dLdN;
+  double dLdc[5], c[5];
+  double wsum;
+};
+
+// dL/d(particle) from the deposit's gradient sums per field: g0 = sum G W, gs = sum G dW/dscale per axis.
 template <typename T>
-__device__ __forceinline__ void adj_store(const Geom &g, const FieldSpec &fs, double v, double w, double g0,
-                                          const double *gs, bool accepted, double dLdN, long long p, T *ox, T *oy,
-                                          T *oz, T *ov, T *ow) {
-  const int e = fs.ea;
-  double ve = 1.0;
-  for (int k = 0; k < e; k++) ve *= v;
-  const double val = w * ve;  // deposit value w v^e (field A)
-  const double dxr = val * gs[0] / g.dx, dyr = val * gs[1] / g.dy, dzr = val * gs[2] / g.dz;
-  const double dw = ve * g0 + (accepted ? dLdN : 0.0);
-  double dv = 0.0;
-  if (e > 0) {
-    double vm = 1.0;
+__device__ __forceinline__ void adj_store(const Geom &g, const FieldSpec &fs, double v, double w, const double *g0,
+                                          const double (*gs)[3], bool accepted, bool read, const AdjScalars &as,
+                                          long long p, T *ox, T *oy, T *oz, T *ov, T *ow) {
+  double dxr = 0.0, dyr = 0.0, dzr = 0.0, dw = 0.0, dv = 0.0;
+  for (int f = 0; f < fs.nfields; f++) {
+    const int e = f ? fs.eb : fs.ea;
+    double ve = 1.0, vm = 1.0;
+    for (int k = 0; k < e; k++) ve *= v;
     for (int k = 0; k < e - 1; k++) vm *= v;
-    dv = w * (double)e * vm * g0;
+    const double val = w * ve;  // the field's deposit value w v^e
+    dxr += val * gs[f][0] / g.dx;
+    dyr += val * gs[f][1] / g.dy;
+    dzr += val * gs[f][2] / g.dz;
+    dw += ve * g0[f];
+    if (e > 0) dv += w * (double)e * vm * g0[f];
+  }
+  if (accepted) dw += as.dLdN;
+  if (read) {  // the shot noise's sum w v^m / sum w over every particle read (src/read_data.c:132-138)
+    double vm = 1.0;
+    for (int m = 1; m <= 4; m++) {
+      if (as.dLdc[m] != 0.0) {
+        dw += as.dLdc[m] * (vm * v - as.c[m]) / as.wsum;
+        dv += as.dLdc[m] * (double)m * w * vm / as.wsum;
+      }
+      vm *= v;
+    }
   }
   const double rsd = g.rsd_opz / g.rsd_den;  // d(shifted LOS coordinate)/dv
   if (g.los == 1) dv += rsd * dxr;
@@ -205,18 +256,20 @@ __device__ __forceinline__ void adj_store(const Geom &g, const FieldSpec &fs, do
   if (ow) ow[p] = (T)dw;
 }
 
-// Step 4 for one particle by the exact FP64 rules: the transpose of its deposit (same taps, halo
-// fold and dropped writes) read from dL/dgrid with the weight derivatives.
+// Step 4 for one particle by the exact FP64 rules: the transpose of its deposits (same taps, halo
+// fold and dropped writes) read from dL/dgrid with the weight derivatives. gr: the real slots.
 template <typename T, typename R>
 __device__ __forceinline__ void adj_particle_exact(const Geom &g, const FieldSpec &fs, const PIn<T> &in, long long p,
-                                                   const R *gA, const R *gAi, double dLdN, T *ox, T *oy, T *oz,
+                                                   const R *const *gr, const AdjScalars &as, T *ox, T *oy, T *oz,
                                                    T *ov, T *ow) {
   double x = (double)in.x[p], y = (double)in.y[p], z = (double)in.z[p];
   const double v = fs.need_v ? (double)in.v[p] : 0.0, w = in.w ? (double)in.w[p] : 1.0;
+  const bool read = isfinite(x) && isfinite(y) && isfinite(z) && isfinite(v) && isfinite(w);
   if (g.los == 1) x = rsd_shift64(g, x, v);
   else if (g.los == 2) y = rsd_shift64(g, y, v);
   else if (g.los == 3) z = rsd_shift64(g, z, v);
-  double g0 = 0.0, gs[3] = {0.0, 0.0, 0.0};
+  const int nf = fs.nfields;
+  double g0[2] = {0.0, 0.0}, gs[2][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
   bool accepted = false;
   {  // a particle outside the box (LOS != 0) is still painted where a stencil accepts it (src/read_data.c:81-97)
     const int nst = g.interlace ? 2 : 1;
@@ -232,31 +285,44 @@ __device__ __forceinline__ void adj_particle_exact(const Geom &g, const FieldSpe
       adj_axis_deriv(g.order, DDIV(DSUB(qx, g.xmin), g.dx), dx3);
       adj_axis_deriv(g.order, DDIV(DSUB(py, g.ymin), g.dy), dy3);
       adj_axis_deriv(g.order, DDIV(DSUB(pz, g.zmin), g.dz), dz3);
-      const R *gr = st ? gAi : gA;
       for (int c = 0; c < az.n; c++)
         for (int b = 0; b < ay.n; b++)
           for (int a = 0; a < ax.n; a++) {
             if (!(ax.on[a] && ay.on[b] && az.on[c])) continue;
             const long long L = canon_index(g, ax.idx[a], ay.idx[b], az.idx[c]);
             if (L < 0) continue;
-            const double G = (double)gr[L];
-            g0 += G * ax.w[a] * ay.w[b] * az.w[c];
-            gs[0] += G * dx3[a] * ay.w[b] * az.w[c];
-            gs[1] += G * ax.w[a] * dy3[b] * az.w[c];
-            gs[2] += G * ax.w[a] * ay.w[b] * dz3[c];
+            for (int f = 0; f < nf; f++) {
+              const double G = (double)gr[st * nf + f][L];
+              g0[f] += G * ax.w[a] * ay.w[b] * az.w[c];
+              gs[f][0] += G * dx3[a] * ay.w[b] * az.w[c];
+              gs[f][1] += G * ax.w[a] * dy3[b] * az.w[c];
+              gs[f][2] += G * ax.w[a] * ay.w[b] * dz3[c];
+            }
           }
     }
   }
-  adj_store(g, fs, v, w, g0, gs, accepted, dLdN, p, ox, oy, oz, ov, ow);
+  adj_store(g, fs, v, w, g0, gs, accepted, read, as, p, ox, oy, oz, ov, ow);
+}
+
+template <typename R>
+struct AdjGrids {
+  const R *s[4];
+};
+
+// dL/dNGRID on the device: the host's part minus Re Gamma(0) of the density's slots
+__device__ __forceinline__ AdjScalars adj_scalars(const Geom &g, const AdjScalars &h, const double *gamma0) {
+  AdjScalars a = h;
+  a.dLdN = h.dLdN - gamma0[0] - (g.interlace ? gamma0[1] : 0.0);
+  return a;
 }
 
 template <typename T, typename R>
-__global__ void __launch_bounds__(128) k_adj_readout(Geom g, FieldSpec fs, PIn<T> in, long long n, const R *gA,
-                                                     const R *gAi, double dLdN_host, const double *gamma0,
-                                                     T *ox, T *oy, T *oz, T *ov, T *ow) {
-  const double dLdN = dLdN_host - gamma0[0] - (g.interlace ? gamma0[1] : 0.0);
+__global__ void __launch_bounds__(128) k_adj_readout(Geom g, FieldSpec fs, PIn<T> in, long long n, AdjGrids<R> gr,
+                                                     AdjScalars hs, const double *gamma0, T *ox, T *oy, T *oz,
+                                                     T *ov, T *ow) {
+  const AdjScalars as = adj_scalars(g, hs, gamma0);
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x)
-    adj_particle_exact<T, R>(g, fs, in, p, gA, gAi, dLdN, ox, oy, oz, ov, ow);
+    adj_particle_exact<T, R>(g, fs, in, p, gr.s, as, ox, oy, oz, ov, ow);
 }
 
 // FP32 per-axis weight derivatives of the taps axis32k produced (same offset d).
@@ -281,18 +347,20 @@ __device__ __forceinline__ void adj_axis_deriv32(float s, int kind, int n, int l
 // Step 4 for FP32 contexts: particles away from every edge of the reference's rules gather their
 // taps with the FP32 rules of the paint (the same ones that deposited them); the others take the
 // exact FP64 path.
-template <int K, typename T>
+template <int K, int NF, typename T>
 __global__ void __launch_bounds__(128) k_adj_readout32(Geom g, FieldSpec fs, PIn<T> in, long long n,
-                                                       const float *gA, const float *gAi, double dLdN_host,
-                                                       const double *gamma0, T *ox, T *oy, T *oz, T *ov, T *ow) {
-  const double dLdN = dLdN_host - gamma0[0] - (g.interlace ? gamma0[1] : 0.0);
+                                                       AdjGrids<float> gr, AdjScalars hs, const double *gamma0,
+                                                       T *ox, T *oy, T *oz, T *ov, T *ow) {
+  const AdjScalars as = adj_scalars(g, hs, gamma0);
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
     const Prep pr = prep32(g, fs, in, p);
     if (!pr.fin || is_edge(g, pr.sx, pr.sy, pr.sz)) {
-      adj_particle_exact<T, float>(g, fs, in, p, gA, gAi, dLdN, ox, oy, oz, ov, ow);
+      adj_particle_exact<T, float>(g, fs, in, p, gr.s, as, ox, oy, oz, ov, ow);
       continue;
     }
-    float g0 = 0.0f, gs[3] = {0.0f, 0.0f, 0.0f};
+    float g0[NF], gs[NF][3];
+#pragma unroll
+    for (int f = 0; f < NF; f++) g0[f] = gs[f][0] = gs[f][1] = gs[f][2] = 0.0f;
     bool accepted = false;
     const int nst = g.interlace ? 2 : 1;
     for (int st = 0; st < nst; st++) {
@@ -308,7 +376,6 @@ __global__ void __launch_bounds__(128) k_adj_readout32(Geom g, FieldSpec fs, PIn
       adj_axis_deriv32<K>(sx, 0, g.nx, g.los, dx3);
       adj_axis_deriv32<K>(sy, 1, g.ny, g.los, dy3);
       adj_axis_deriv32<K>(sz, 1, g.nz, g.los, dz3);
-      const float *gr = st ? gAi : gA;
 #pragma unroll
       for (int a = 0; a < K; a++) {
         if (ax.idx[a] < 0) continue;
@@ -319,18 +386,26 @@ __global__ void __launch_bounds__(128) k_adj_readout32(Geom g, FieldSpec fs, PIn
 #pragma unroll
           for (int c = 0; c < K; c++) {
             if (az.idx[c] < 0) continue;
-            const float G = gr[rowb + az.idx[c]];
             const float wyz = ay.w[b] * az.w[c];
-            g0 += G * ax.w[a] * wyz;
-            gs[0] += G * dx3[a] * wyz;
-            gs[1] += G * ax.w[a] * dy3[b] * az.w[c];
-            gs[2] += G * ax.w[a] * ay.w[b] * dz3[c];
+#pragma unroll
+            for (int f = 0; f < NF; f++) {
+              const float G = gr.s[st * NF + f][rowb + az.idx[c]];
+              g0[f] += G * ax.w[a] * wyz;
+              gs[f][0] += G * dx3[a] * wyz;
+              gs[f][1] += G * ax.w[a] * dy3[b] * az.w[c];
+              gs[f][2] += G * ax.w[a] * ay.w[b] * dz3[c];
+            }
           }
         }
       }
     }
-    const double gsd[3] = {(double)gs[0], (double)gs[1], (double)gs[2]};
-    adj_store(g, fs, (double)pr.v, (double)pr.w, (double)g0, gsd, accepted, dLdN, p, ox, oy, oz, ov, ow);
+    double g0d[2] = {0.0, 0.0}, gsd[2][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+#pragma unroll
+    for (int f = 0; f < NF; f++) {
+      g0d[f] = (double)g0[f];
+      for (int a = 0; a < 3; a++) gsd[f][a] = (double)gs[f][a];
+    }
+    adj_store(g, fs, (double)pr.v, (double)pr.w, g0d, gsd, accepted, true, as, p, ox, oy, oz, ov, ow);
   }
 }
 
@@ -360,46 +435,102 @@ static int adj_blocks(long long work) {
   return (int)(b < 1 ? 1 : b);
 }
 
-extern "C" int capow_backward(capow_ctx *c, const double *const dL_dP[5], const capow_grads *out) {
+template <typename R, int NF>
+static void adj_mode_kernels(capow_ctx *c, const double *coef_d, int pmask, double *gamma0) {
+  const capow_params &p = c->p;
+  const size_t eb = sizeof(R);
+  AdjSlots<R> sl;
+  for (int s = 0; s < 4; s++)
+    sl.s[s] = s < c->nslot ? (typename AdjC<R>::C *)((char *)c->grid_base + eb * c->grid_elems * s) : nullptr;
+  const int nyq = (p.NZ % 2 == 0) ? p.NZ / 2 : -1;
+  const int kz_hi = nyq > 0 ? nyq : c->bp.nzc;
+  const long long interior = (long long)p.NX * p.NY * (kz_hi - 1 > 0 ? kz_hi - 1 : 0);
+  const int nbm = adj_blocks(interior), nbp = adj_blocks((long long)p.NX * p.NY);
+  k_adj_modes<R, NF><<<nbm, 256, 0, c->stream>>>(c->bp, c->bt, coef_d, pmask, sl, c->dcv, 1, kz_hi);
+  k_adj_plane<R, NF><<<nbp, 256, 0, c->stream>>>(c->bp, c->bt, coef_d, pmask, sl, c->dcv, 0, gamma0);
+  if (nyq > 0) k_adj_plane<R, NF><<<nbp, 256, 0, c->stream>>>(c->bp, c->bt, coef_d, pmask, sl, c->dcv, nyq, gamma0);
+  c->launches += nyq > 0 ? 3 : 2;
+}
+
+template <typename T>
+static void adj_readout(capow_ctx *c, long long n, const AdjScalars &hs, const double *gamma0, void *const *dev) {
+  const capow_particles &d = c->last;
+  const PIn<T> in{(const T *)d.x, (const T *)d.y, (const T *)d.z, (const T *)d.vlos, (const T *)d.w};
+  const int nb = (int)((n + 127) / 128 > 152 * 16 ? 152 * 16 : ((n + 127) / 128 < 1 ? 1 : (n + 127) / 128));
+  T *o[5];
+  for (int k = 0; k < 5; k++) o[k] = (T *)dev[k];
+  const size_t eb = c->prec == CAPOW_FP64 ? 8 : 4;
+  if (c->prec == CAPOW_FP64) {
+    AdjGrids<double> gr;
+    for (int s = 0; s < 4; s++) gr.s[s] = s < c->nslot ? (const double *)((char *)c->grid_base + eb * c->grid_elems * s) : nullptr;
+    k_adj_readout<T, double><<<nb, 128, 0, c->stream>>>(c->g, c->fs, in, n, gr, hs, gamma0, o[0], o[1], o[2], o[3], o[4]);
+    return;
+  }
+  AdjGrids<float> gr;
+  for (int s = 0; s < 4; s++) gr.s[s] = s < c->nslot ? (const float *)((char *)c->grid_base + eb * c->grid_elems * s) : nullptr;
+  const int K = c->p.InterpOrder;
+#define ADJ_RUN32(KK, NFF) \
+  k_adj_readout32<KK, NFF, T><<<nb, 128, 0, c->stream>>>(c->g, c->fs, in, n, gr, hs, gamma0, o[0], o[1], o[2], o[3], o[4])
+  if (c->fs.nfields == 2) {
+    if (K == 3) ADJ_RUN32(3, 2);
+    else if (K == 2) ADJ_RUN32(2, 2);
+    else ADJ_RUN32(1, 2);
+  } else {
+    if (K == 3) ADJ_RUN32(3, 1);
+    else if (K == 2) ADJ_RUN32(2, 1);
+    else ADJ_RUN32(1, 1);
+  }
+#undef ADJ_RUN32
+}
+
+extern "C" int capow_backward(capow_ctx *c, const double *const *dL_dP, const capow_grads *out) {
   if (!c || !dL_dP || !out) return CAPOW_EINVAL;
   if (!c->powered) FAIL(c, CAPOW_ESTATE, "capow_backward needs capow_paint and capow_power first");
-  if (c->fs.nfields != 1 || c->bp.nspec != 1 || !c->bp.mean_sub_a || c->fs.ea != 0)
-    FAIL(c, CAPOW_ENOTSUP, "capow_backward covers the density auto-spectrum (Momentum 0 or spectra = DD)");
   if (out->dtype != CAPOW_F32 && out->dtype != CAPOW_F64) FAIL(c, CAPOW_EINVAL, "grads dtype must be F32 or F64");
   CK(c, cudaSetDevice(c->o.device));
   const capow_params &p = c->p;
-  const int nk = p.NK;
+  const int nk = p.NK, nf = c->fs.nfields;
   const long long n = (long long)c->last.n;
-  // ---- host: per-bin coefficients c_l(b) = dL/dP_l(b) (2l+1) / (Nmodes(b) norm), and dL/dNGRID
-  // through norm = NGRID^2 / V and shot = NGRID (src/main.c:106-148, 1019-1056)
+  // ---- host: per-product, per-bin coefficients c_q,l(b) = sum over the spectra of product q of
+  // dL/dP_l(b) (2l+1) / (Nmodes(b) norm); dL/dNGRID through norm = NGRID^2 / V and shot = NGRID c_m;
+  // dL/dc_m through the shot (src/main.c:106-148, 1019-1056)
   const DevStats &st = *c->h_st;
   const double N = st.ngrid;
   const double V = (p.XMAX - p.XMIN) * (p.YMAX - p.YMIN) * (p.ZMAX - p.ZMIN);
   const double norm = N * N / V;
+  AdjScalars hs;
+  memset(&hs, 0, sizeof hs);
+  hs.wsum = st.nsq;
+  hs.c[0] = 1.0;
+  for (int m = 1; m <= 4; m++) hs.c[m] = c->moments && st.nsq != 0.0 ? st.vr[m - 1] / st.nsq : 0.0;
   int last = -1;  // output_power zeroes the highest filled bin (its output does not depend on anything)
   for (int b = 0; b < nk; b++)
     if (c->nmodes[b] > 0) last = b;
-  std::vector<double> coef(5 * nk, 0.0);
-  double dLdN = 0.0;
-  for (int b = 0; b < nk; b++) {
-    const double nm = (double)c->nmodes[b];
-    if (nm <= 0.0 || b == last || norm <= 0.0) continue;
-    for (int l = 0; l < 5; l++) {
-      if ((l == 1 || l == 3) && !p.Odd_Multipoles) continue;
-      const double g = dL_dP[l] ? dL_dP[l][b] : 0.0;
-      if (g == 0.0) continue;
-      coef[l * nk + b] = g * (double)(2 * l + 1) / (nm * norm);
-      const double S = c->h_bins[l * nk + b];  // raw sum of product 0 (|A|^2), multipole l
-      const double P = l == 0 ? (S - nm * N) / (nm * norm) : (double)(2 * l + 1) * S / (nm * norm);
-      const double dPdN = l == 0 ? -2.0 * P / N - V / (N * N) : -2.0 * P / N;
-      dLdN += g * dPdN;
+  std::vector<double> coef(NPROD * 5 * nk, 0.0);
+  int pmask = 0;
+  for (int q = 0; q < c->bp.nspec; q++) {
+    const int pq = spectrum_product(nf, c->bp.spec[q]);
+    const int m = c->shot_moment[q];
+    const double shot = N * hs.c[m];
+    for (int b = 0; b < nk; b++) {
+      const double nm = (double)c->nmodes[b];
+      if (nm <= 0.0 || b == last || norm <= 0.0) continue;
+      for (int l = 0; l < 5; l++) {
+        if ((l == 1 || l == 3) && !p.Odd_Multipoles) continue;
+        const double gl = dL_dP[q * 5 + l] ? dL_dP[q * 5 + l][b] : 0.0;
+        if (gl == 0.0) continue;
+        coef[(pq * 5 + l) * nk + b] += gl * (double)(2 * l + 1) / (nm * norm);
+        pmask |= 1 << pq;
+        const double S = c->h_bins[(pq * 5 + l) * nk + b];  // the raw sum of this product and multipole
+        const double P = l == 0 ? (S / nm - shot) / norm : (double)(2 * l + 1) * S / (nm * norm);
+        hs.dLdN += gl * (l == 0 ? -2.0 * P / N - hs.c[m] / norm : -2.0 * P / N);
+        if (l == 0 && m > 0) hs.dLdc[m] += gl * (-N / norm);
+      }
     }
   }
-  if (!c->adj_coef) {
-    CK(c, cudaMalloc(&c->adj_coef, sizeof(double) * 5 * nk + 2 * sizeof(double)));
-  }
-  double *coef_d = c->adj_coef, *gamma0 = c->adj_coef + 5 * nk;
-  CK(c, cudaMemcpyAsync(coef_d, coef.data(), sizeof(double) * 5 * nk, cudaMemcpyHostToDevice, c->stream));
+  if (!c->adj_coef) CK(c, cudaMalloc(&c->adj_coef, sizeof(double) * NPROD * 5 * nk + 2 * sizeof(double)));
+  double *coef_d = c->adj_coef, *gamma0 = c->adj_coef + NPROD * 5 * nk;
+  CK(c, cudaMemcpyAsync(coef_d, coef.data(), sizeof(double) * NPROD * 5 * nk, cudaMemcpyHostToDevice, c->stream));
   CK(c, cudaMemsetAsync(gamma0, 0, 2 * sizeof(double), c->stream));
   int rc = make_3d_plans(c);
   if (rc) return rc;
@@ -409,29 +540,18 @@ extern "C" int capow_backward(capow_ctx *c, const double *const dL_dP[5], const 
   const bool f64 = c->prec == CAPOW_FP64;
   if (f64) CKFFT(c, cufftExecD2Z(c->adj_fwd, (cufftDoubleReal *)c->grid_base, (cufftDoubleComplex *)c->grid_base));
   else CKFFT(c, cufftExecR2C(c->adj_fwd, (cufftReal *)c->grid_base, (cufftComplex *)c->grid_base));
-  // ---- mode gradients and Hermitian completion, then the inverse transform
-  const size_t eb = f64 ? 8 : 4;
-  void *gA = c->grid_base, *gAi = p.DoInterlacing ? (char *)c->grid_base + eb * c->grid_elems : nullptr;
-  const int nyq = (p.NZ % 2 == 0) ? p.NZ / 2 : -1;
-  const int kz_hi = nyq > 0 ? nyq : c->bp.nzc;
-  const long long interior = (long long)p.NX * p.NY * (kz_hi - 1 > 0 ? kz_hi - 1 : 0);
-  const int nbm = adj_blocks(interior), nbp = adj_blocks((long long)p.NX * p.NY);
+  // ---- mode gradients and Hermitian completion, then the inverse transform. Re Gamma(0) enters dL/dNGRID
+  // only where the density is mean-subtracted (F(0) = sum - NGRID); otherwise gamma0 is cleared after
   if (f64) {
-    k_adj_modes<double><<<nbm, 256, 0, c->stream>>>(c->bp, c->bt, coef_d, (double2 *)gA, (double2 *)gAi, c->dcv, 1, kz_hi);
-    k_adj_plane<double><<<nbp, 256, 0, c->stream>>>(c->bp, c->bt, coef_d, (double2 *)gA, (double2 *)gAi, c->dcv, 0, gamma0);
-    if (nyq > 0)
-      k_adj_plane<double><<<nbp, 256, 0, c->stream>>>(c->bp, c->bt, coef_d, (double2 *)gA, (double2 *)gAi, c->dcv, nyq,
-                                                      gamma0);
+    if (nf == 2) adj_mode_kernels<double, 2>(c, coef_d, pmask, gamma0);
+    else adj_mode_kernels<double, 1>(c, coef_d, pmask, gamma0);
     CKFFT(c, cufftExecZ2D(c->adj_inv, (cufftDoubleComplex *)c->grid_base, (cufftDoubleReal *)c->grid_base));
   } else {
-    k_adj_modes<float><<<nbm, 256, 0, c->stream>>>(c->bp, c->bt, coef_d, (float2 *)gA, (float2 *)gAi, c->dcv, 1, kz_hi);
-    k_adj_plane<float><<<nbp, 256, 0, c->stream>>>(c->bp, c->bt, coef_d, (float2 *)gA, (float2 *)gAi, c->dcv, 0, gamma0);
-    if (nyq > 0)
-      k_adj_plane<float><<<nbp, 256, 0, c->stream>>>(c->bp, c->bt, coef_d, (float2 *)gA, (float2 *)gAi, c->dcv, nyq,
-                                                     gamma0);
+    if (nf == 2) adj_mode_kernels<float, 2>(c, coef_d, pmask, gamma0);
+    else adj_mode_kernels<float, 1>(c, coef_d, pmask, gamma0);
     CKFFT(c, cufftExecC2R(c->adj_inv, (cufftComplex *)c->grid_base, (cufftReal *)c->grid_base));
   }
-  c->launches += nyq > 0 ? 3 : 2;
+  if (!c->bp.mean_sub_a) CK(c, cudaMemsetAsync(gamma0, 0, 2 * sizeof(double), c->stream));
   CK(c, cudaGetLastError());
   // ---- per-particle readout into device buffers (the caller's, or staging for host outputs)
   const size_t ob = out->dtype == CAPOW_F64 ? 8 : 4;
@@ -453,35 +573,10 @@ extern "C" int capow_backward(capow_ctx *c, const double *const dL_dP[5], const 
       dev[k] = c->adj_stage[k];
     }
   }
-  const capow_particles &d = c->last;
-  const int nb = (int)((n + 127) / 128 > 152 * 16 ? 152 * 16 : ((n + 127) / 128 < 1 ? 1 : (n + 127) / 128));
-#define ADJ_IN(TI) \
-  PIn<TI> { (const TI *)d.x, (const TI *)d.y, (const TI *)d.z, (const TI *)d.vlos, (const TI *)d.w }
-#define ADJ_OUT(TO) (TO *)dev[0], (TO *)dev[1], (TO *)dev[2], (TO *)dev[3], (TO *)dev[4]
-#define ADJ_RUN64(T) \
-  k_adj_readout<T, double><<<nb, 128, 0, c->stream>>>(c->g, c->fs, ADJ_IN(T), n, (const double *)gA, \
-                                                      (const double *)gAi, dLdN, gamma0, ADJ_OUT(T))
-#define ADJ_RUN32(K, T) \
-  k_adj_readout32<K, T><<<nb, 128, 0, c->stream>>>(c->g, c->fs, ADJ_IN(T), n, (const float *)gA, \
-                                                   (const float *)gAi, dLdN, gamma0, ADJ_OUT(T))
-  if (d.dtype != out->dtype)
+  if (c->last.dtype != out->dtype)
     FAIL(c, CAPOW_EINVAL, "capow_backward: gradient dtype must match the painted particles' dtype");
-  if (f64) {
-    if (d.dtype == CAPOW_F64) ADJ_RUN64(double);
-    else ADJ_RUN64(float);
-  } else if (d.dtype == CAPOW_F64) {
-    if (p.InterpOrder == 3) ADJ_RUN32(3, double);
-    else if (p.InterpOrder == 2) ADJ_RUN32(2, double);
-    else ADJ_RUN32(1, double);
-  } else {
-    if (p.InterpOrder == 3) ADJ_RUN32(3, float);
-    else if (p.InterpOrder == 2) ADJ_RUN32(2, float);
-    else ADJ_RUN32(1, float);
-  }
-#undef ADJ_IN
-#undef ADJ_OUT
-#undef ADJ_RUN64
-#undef ADJ_RUN32
+  if (c->last.dtype == CAPOW_F64) adj_readout<double>(c, n, hs, gamma0, dev);
+  else adj_readout<float>(c, n, hs, gamma0, dev);
   c->launches++;
   CK(c, cudaGetLastError());
   if (!out->on_device)

@@ -96,7 +96,7 @@ Geom make_geom(const capow_params &p) {
 }
 
 // Product of one spectrum in the bin kernels' [product][5][NK] sums: |A|^2, Re(A*B), Im(A*B), |B|^2.
-static int spectrum_product(int nfields, const SpecDef &sd) {
+int spectrum_product(int nfields, const SpecDef &sd) {
   return nfields == 1 ? 0 : (sd.x == sd.y ? (sd.x == 0 ? 0 : 3) : (sd.imag ? 2 : 1));
 }
 

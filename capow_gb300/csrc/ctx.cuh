@@ -103,6 +103,8 @@ struct capow_ctx {
 
 // capow_api.cu: paint the last catalogue again and prepare the DC values (capow_backward).
 int enqueue_backward_paint(capow_ctx *c);
+// product of one spectrum in the bin kernels' [product][5][NK] sums: |A|^2, Re(A*B), Im(A*B), |B|^2
+int spectrum_product(int nfields, const SpecDef &sd);
 
 // capow_api.cu pieces shared with batch.cu and survey.cu
 Geom make_geom(const capow_params &p);

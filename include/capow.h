@@ -193,16 +193,18 @@ typedef struct capow_grads {
   void *dw;          /* dL/d(weight), including its effect on NGRID (norm, shot, mean subtraction) */
 } capow_grads;
 
-/* Adjoint of capow_power + capow_normalise for the density auto-spectrum (Momentum 0, or
- * spectra = CAPOW_SPEC_DD): given dL/dP_l(k) of the normalised multipoles (dL_dP[l] = double[NK],
- * l = 0..4; NULL for a multipole the loss does not use), writes dL/dx, dL/dy, dL/dz, dL/dv_los
- * and dL/dw of every particle of the last capow_paint. The reference has no adjoint; this inverts
- * read_data.c:32-179, 514-745 and main.c:106-148, 211-225, 266-271, 302-468, 1019-1056: repaint,
- * full 3-D R2C, per-mode dL/dF, Hermitian completion, C2R, and the transposed deposit with the
- * weight derivatives. Call after capow_power; it leaves the grids holding dL/dgrid, so paint
- * again before the next capow_power. The output_power rule that zeroes the highest filled bin
- * makes that bin's gradient zero. */
-int capow_backward(capow_ctx *ctx, const double *const dL_dP[5], const capow_grads *out);
+/* Adjoint of capow_power + capow_normalise for every spectrum of the context (any Momentum, or the
+ * dd / dp / pp selection): given dL/dP_l(k) of the normalised multipoles, 5 entries per spectrum in the
+ * order capow_power returns them (dL_dP[5 q + l] = double[NK] for spectrum q and multipole l = 0..4;
+ * NULL for a multipole the loss does not use; one spectrum: 5 entries, as before), writes dL/dx, dL/dy,
+ * dL/dz, dL/dv_los and dL/dw of every particle of the last capow_paint. The velocity enters through the
+ * RSD shift (LOS != 0), the momentum fields' w v^e deposits and the shot noise's sum w v^m / sum w. The
+ * reference has no adjoint; this inverts read_data.c:32-179, 514-745 and main.c:106-148, 211-225,
+ * 266-271, 302-468, 1019-1056: repaint, full 3-D R2C, per-mode dL/dF of both fields, Hermitian
+ * completion, C2R, and the transposed deposits with the weight derivatives. Call after capow_power; it
+ * leaves the grids holding dL/dgrid, so paint again before the next capow_power. The output_power rule
+ * that zeroes the highest filled bin makes that bin's gradient zero. */
+int capow_backward(capow_ctx *ctx, const double *const *dL_dP, const capow_grads *out);
 
 /* ---------------------------------------------------------------- batched mocks */
 /* One mock of a batch: its own parameters (box, grid, order, ...) and device-resident catalogue.
