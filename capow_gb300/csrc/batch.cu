@@ -1,11 +1,15 @@
 // capow_batch: many independent periodic-box mocks (each its own box, grid, interpolation order and
 // catalogue) in one call. The reference runs one mock per process (src/main.c:28-298); here:
-//  * mocks that share a grid shape share one context: grids, cuFFT plans, tile tables and record
-//    buffers are allocated once per shape and sized for its largest catalogue;
+//  * mocks that share a grid shape share a small ring of contexts (BATCH_RING): grids, cuFFT plans, tile
+//    tables and record buffers are allocated per context and sized for its largest catalogue, and the
+//    shape's mocks alternate between the ring's contexts;
+//  * every context runs on a stream of its own, forked from the batch stream by one event and joined
+//    back by another, so that the mocks of different contexts (of one shape or of different shapes)
+//    overlap on the GPU: small grids do not fill it one kernel at a time;
 //  * each mock has its own bin tables, mode counts, counters and bins (its box sets the k grid);
-//  * every mock is enqueued on one stream with no host synchronisation and no allocation, so the
-//    whole batch can be captured as one CUDA graph and launched once; the bins, counts and counters
-//    of all mocks are read back at the end;
+//  * every mock is enqueued with no host synchronisation and no allocation, so the whole batch (the
+//    fork, every context's work and the join) can be captured as one CUDA graph and launched once; the
+//    bins, counts and counters of all mocks are read back at the end;
 //  * an autotuner times candidate tile shapes of the FP32 paint on the first mock of each shape.
 #include <cuda_runtime.h>
 #include <math.h>
@@ -84,11 +88,17 @@ std::map<ShapeKey, TileGeo> g_tuned;
 // the same sizes) only launches: the graph as it is when the arrays are the same, or updated in place
 // (cudaGraphExecUpdate) when they moved. A call with another signature, or capow_batch_release,
 // frees it.
+constexpr int BATCH_RING = 2;  // contexts per grid shape
+
 struct BatchState {
   std::vector<unsigned char> sig;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
-  std::map<ShapeKey, capow_ctx *> ctxs;
+  std::map<ShapeKey, std::vector<capow_ctx *>> rings;
+  std::vector<capow_ctx *> all;          // every context of every ring
+  std::vector<cudaStream_t> ctx_streams;  // their streams (owned here)
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> joins;         // one per context
   std::vector<capow_ctx *> ctx_of;
   std::vector<int> status0;  // per-mock status found while setting up (e.g. CAPOW_ENOTSUP)
   std::vector<MockDev> md;
@@ -108,8 +118,12 @@ BatchState *g_batch = nullptr;
 void free_batch_state(BatchState *b) {
   if (!b) return;
   if (b->stream) cudaStreamSynchronize(b->stream);
+  for (cudaStream_t s : b->ctx_streams) cudaStreamSynchronize(s);
   if (b->exec) cudaGraphExecDestroy(b->exec);
-  for (auto &kv : b->ctxs) capow_destroy(kv.second);
+  for (capow_ctx *c : b->all) capow_destroy(c);
+  for (cudaStream_t s : b->ctx_streams) cudaStreamDestroy(s);
+  if (b->fork) cudaEventDestroy(b->fork);
+  for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
   if (b->tab_dev) cudaFree(b->tab_dev);
   if (b->arena) cudaFree(b->arena);
   if (b->own_stream) cudaStreamDestroy(b->stream);
@@ -170,23 +184,33 @@ int setup_batch(BatchState *b, const capow_mock *mocks, int nmocks, const capow_
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return CAPOW_ECUDA;
     b->own_stream = true;
   }
-  capow_options so = o;
-  so.stream = b->stream;
-  std::map<ShapeKey, unsigned long long> nmax;
-  std::map<ShapeKey, bool> wts;
+  if (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) return CAPOW_ECUDA;
+  std::map<capow_ctx *, unsigned long long> nmax;
+  std::map<capow_ctx *, bool> wts;
   b->ctx_of.assign(nmocks, nullptr);
-  // the shared context of a shape is created for its largest interpolation order (the record buffers
-  // are sized for the widest footprint)
-  std::map<ShapeKey, int> max_order;
+  // the contexts of a shape are created for its largest interpolation order (the record buffers are
+  // sized for the widest footprint); the ring has BATCH_RING contexts, or one per mock when fewer
+  std::map<ShapeKey, int> max_order, count;
   for (int i = 0; i < nmocks; i++)
     if (!b->status0[i]) {
       int &mo = max_order[shape_of(mocks[i].params)];
       mo = std::max(mo, mocks[i].params.InterpOrder);
+      count[shape_of(mocks[i].params)]++;
     }
+  std::map<ShapeKey, int> seen;
   for (int i = 0; i < nmocks; i++) {
     if (b->status0[i]) continue;
     const ShapeKey k = shape_of(mocks[i].params);
-    if (!b->ctxs.count(k)) {
+    std::vector<capow_ctx *> &ring = b->rings[k];
+    const int want = std::min(BATCH_RING, count[k]);
+    const int slot = seen[k]++ % want;
+    if ((int)ring.size() <= slot) {
+      cudaStream_t cs = nullptr;
+      cudaEvent_t je = nullptr;
+      if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return CAPOW_ECUDA;
+      b->ctx_streams.push_back(cs);  // freed with the state whatever follows
+      capow_options so = o;
+      so.stream = cs;
       capow_ctx *c = nullptr;
       capow_params cp = mocks[i].params;
       cp.InterpOrder = max_order[k];
@@ -196,13 +220,24 @@ int setup_batch(BatchState *b, const capow_mock *mocks, int nmocks, const capow_
         b->status0[i] = r;
         continue;
       }
+      if (cudaEventCreateWithFlags(&je, cudaEventDisableTiming) != cudaSuccess) {
+        capow_destroy(c);
+        return CAPOW_ECUDA;
+      }
       c->quiet = true;
-      c->two_pass = true;  // record buffers sized once per shape (prepare_paint_buffers)
-      b->ctxs[k] = c;
+      c->two_pass = true;  // record buffers sized once per context (prepare_paint_buffers)
+      ring.push_back(c);
+      b->all.push_back(c);
+      b->joins.push_back(je);
     }
-    b->ctx_of[i] = b->ctxs[k];
-    nmax[k] = std::max(nmax[k], (unsigned long long)mocks[i].parts.n);
-    wts[k] = wts[k] || mocks[i].parts.w != nullptr;
+    if (ring.empty()) {
+      b->status0[i] = CAPOW_ECUDA;
+      continue;
+    }
+    capow_ctx *c = ring[slot < (int)ring.size() ? slot : 0];
+    b->ctx_of[i] = c;
+    nmax[c] = std::max(nmax[c], (unsigned long long)mocks[i].parts.n);
+    wts[c] = wts[c] || mocks[i].parts.w != nullptr;
   }
   // ---- per-mock tables and output buffers (one device arena for the small per-mock arrays)
   b->per = ((sizeof(DevStats) + 255) & ~(size_t)255) + 256;  // counters + 4 DC values
@@ -263,19 +298,24 @@ int setup_batch(BatchState *b, const capow_mock *mocks, int nmocks, const capow_
       return CAPOW_ENOMEM;
     for (int i = 0; i < nmocks; i++)
       if (b->ctx_of[i]) relocate_bin_tables(b->md[i].bt, (const char *)b->tab_dev + tab_off[i]);
+    // the contexts' streams read the tables: the upload completes first
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess) return CAPOW_ECUDA;
   }
-  // ---- record buffers for the largest catalogue of each shape; the tile autotuner (its choice is
-  // kept per grid shape for later calls)
-  for (auto &kv : b->ctxs) {
-    capow_ctx *c = kv.second;
-    int rc = prepare_paint_buffers(c, nmax[kv.first], wts[kv.first]);
+  // ---- record buffers for the largest catalogue of each context; the tile autotuner, on the first
+  // context of each shape (its choice is kept per grid shape for later calls and given to the ring)
+  for (capow_ctx *c : b->all) {
+    int rc = prepare_paint_buffers(c, nmax[c], wts[c]);
     if (rc) return rc;
+  }
+  for (auto &kv : b->rings) {
+    if (kv.second.empty()) continue;
+    capow_ctx *c = kv.second[0];
     if (!(flags & CAPOW_BATCH_AUTOTUNE) || c->prec != CAPOW_FP32_MIXED) continue;
     {
       std::lock_guard<std::mutex> lock(g_tuned_mu);
       auto it = g_tuned.find(kv.first);
       if (it != g_tuned.end()) {
-        c->tg = it->second;
+        for (capow_ctx *r : kv.second) r->tg = it->second;
         continue;
       }
     }
@@ -302,22 +342,21 @@ int setup_batch(BatchState *b, const capow_mock *mocks, int nmocks, const capow_
         best = tg;
       }
     }
-    c->tg = best;
     c->pb = keep_pb;
+    for (capow_ctx *r : kv.second) r->tg = best;
     std::lock_guard<std::mutex> lock(g_tuned_mu);
     g_tuned[kv.first] = best;
   }
-  // ---- one uncaptured pass over the first mock of each shape: every kernel and plan a graph holds
+  // ---- one uncaptured pass over the first mock of each context: every kernel and plan a graph holds
   // has run once before a capture starts
   if (flags & CAPOW_BATCH_GRAPH) {
-    for (auto &kv : b->ctxs) {
-      capow_ctx *c = kv.second;
+    for (capow_ctx *c : b->all) {
       for (int i = 0; i < nmocks; i++) {
         if (b->ctx_of[i] != c) continue;
         bind_mock(c, mocks[i].params, b->md[i]);
         capow_particles d = mocks[i].parts;
         if (!c->fs.need_v) d.vlos = nullptr;
-        launch_mode_counts(b->stream, c->bp, c->bt, b->md[i].nmodes, nullptr, &c->launches);
+        launch_mode_counts(c->stream, c->bp, c->bt, b->md[i].nmodes, nullptr, &c->launches);
         int rc = enqueue_paint(c, d);
         if (!rc) rc = enqueue_power_kernels(c);
         if (rc) return rc;
@@ -325,23 +364,32 @@ int setup_batch(BatchState *b, const capow_mock *mocks, int nmocks, const capow_
       }
     }
   }
+  for (cudaStream_t s : b->ctx_streams)
+    if (cudaStreamSynchronize(s) != cudaSuccess) return CAPOW_ECUDA;
   return cudaStreamSynchronize(b->stream) == cudaSuccess ? CAPOW_OK : CAPOW_ECUDA;
 }
 
-// Every mock's kernels on the batch stream (no host synchronisation, no allocation).
+// Every mock's kernels on its context's stream, forked from the batch stream and joined back to it (no
+// host synchronisation, no allocation).
 int enqueue_batch(BatchState *b, capow_mock *mocks, int nmocks) {
+  cudaEventRecord(b->fork, b->stream);
+  for (capow_ctx *c : b->all) cudaStreamWaitEvent(c->stream, b->fork, 0);
   for (int i = 0; i < nmocks; i++) {
     capow_ctx *c = b->ctx_of[i];
     if (!c) continue;
     bind_mock(c, mocks[i].params, b->md[i]);
     const int nk = mocks[i].params.NK;
-    cudaMemsetAsync(b->md[i].nmodes, 0, sizeof(unsigned long long) * nk, b->stream);
-    launch_mode_counts(b->stream, c->bp, c->bt, b->md[i].nmodes, nullptr, &c->launches);
+    cudaMemsetAsync(b->md[i].nmodes, 0, sizeof(unsigned long long) * nk, c->stream);
+    launch_mode_counts(c->stream, c->bp, c->bt, b->md[i].nmodes, nullptr, &c->launches);
     capow_particles d = mocks[i].parts;
     if (!c->fs.need_v) d.vlos = nullptr;
     int r = enqueue_paint(c, d);
     if (!r) r = enqueue_power_kernels(c);
     if (r) mocks[i].status = r;
+  }
+  for (size_t k = 0; k < b->all.size(); k++) {
+    cudaEventRecord(b->joins[k], b->all[k]->stream);
+    cudaStreamWaitEvent(b->stream, b->joins[k], 0);
   }
   return CAPOW_OK;
 }
