@@ -10,7 +10,9 @@
 //  * every mock is enqueued with no host synchronisation and no allocation, so the whole batch (the
 //    fork, every context's work and the join) can be captured as one CUDA graph and launched once; the
 //    bins, counts and counters of all mocks are read back at the end;
-//  * an autotuner times candidate tile shapes of the FP32 paint on the first mock of each shape.
+//  * the FP32 paint is the one-pass bucket paint, its buffers sized per context before anything is
+//    enqueued; an autotuner times candidate tile shapes and then bucket capacity factors on the first
+//    mock of each shape.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
@@ -78,9 +80,17 @@ int time_paint(capow_ctx *c, const capow_particles &d, float *ms) {
   return rc;
 }
 
-// tile shapes chosen by the autotuner, per grid shape, for the life of the process
+// tile shapes and bucket factors chosen by the autotuner, per grid shape, for the life of the process
+struct Tuned {
+  TileGeo tg;
+  float bucket_factor;
+};
 std::mutex g_tuned_mu;
-std::map<ShapeKey, TileGeo> g_tuned;
+std::map<ShapeKey, Tuned> g_tuned;
+
+// Bucket capacity factors the autotuner times (records per tile = factor * mean share + 64): smaller
+// buckets write fewer record slots, larger ones send fewer records to the slower overflow path.
+const float kBucketFactors[] = {1.5f, 2.0f, 3.0f};
 
 // The device state of one batch signature (the mocks' parameters, sizes and array kinds, the options
 // and flags): shared contexts, per-mock tables and outputs, and the instantiated graph. It is kept
@@ -224,8 +234,7 @@ int setup_batch(BatchState *b, const capow_mock *mocks, int nmocks, const capow_
         capow_destroy(c);
         return CAPOW_ECUDA;
       }
-      c->quiet = true;
-      c->two_pass = true;  // record buffers sized once per context (prepare_paint_buffers)
+      c->quiet = true;  // record buffers sized once per context (prepare_paint_buffers)
       ring.push_back(c);
       b->all.push_back(c);
       b->joins.push_back(je);
@@ -301,8 +310,9 @@ int setup_batch(BatchState *b, const capow_mock *mocks, int nmocks, const capow_
     // the contexts' streams read the tables: the upload completes first
     if (cudaStreamSynchronize(b->stream) != cudaSuccess) return CAPOW_ECUDA;
   }
-  // ---- record buffers for the largest catalogue of each context; the tile autotuner, on the first
-  // context of each shape (its choice is kept per grid shape for later calls and given to the ring)
+  // ---- record buffers for the largest catalogue of each context; the autotuner, on the first context of
+  // each shape: the tile shape, then the one-pass buckets' capacity factor (its choice is kept per grid
+  // shape for later calls and given to the ring); then the buffers again for the chosen settings
   for (capow_ctx *c : b->all) {
     int rc = prepare_paint_buffers(c, nmax[c], wts[c]);
     if (rc) return rc;
@@ -315,7 +325,10 @@ int setup_batch(BatchState *b, const capow_mock *mocks, int nmocks, const capow_
       std::lock_guard<std::mutex> lock(g_tuned_mu);
       auto it = g_tuned.find(kv.first);
       if (it != g_tuned.end()) {
-        for (capow_ctx *r : kv.second) r->tg = it->second;
+        for (capow_ctx *r : kv.second) {
+          r->tg = it->second.tg;
+          r->bucket_factor = it->second.bucket_factor;
+        }
         continue;
       }
     }
@@ -327,7 +340,6 @@ int setup_batch(BatchState *b, const capow_mock *mocks, int nmocks, const capow_
       }
     if (first < 0) continue;
     const TileGeo keep = c->tg;
-    const PaintBufs keep_pb = c->pb;
     bind_mock(c, mocks[first].params, b->md[first]);
     TileGeo best = keep;
     float best_ms = 1e30f;
@@ -342,10 +354,27 @@ int setup_batch(BatchState *b, const capow_mock *mocks, int nmocks, const capow_
         best = tg;
       }
     }
-    c->pb = keep_pb;
-    for (capow_ctx *r : kv.second) r->tg = best;
+    c->tg = best;
+    float best_f = c->bucket_factor;
+    best_ms = 1e30f;
+    for (float f : kBucketFactors) {
+      c->bucket_factor = f;
+      float ms = 0.0f;
+      if (time_paint(c, mocks[first].parts, &ms) == CAPOW_OK && ms < best_ms) {
+        best_ms = ms;
+        best_f = f;
+      }
+    }
+    for (capow_ctx *r : kv.second) {
+      r->tg = best;
+      r->bucket_factor = best_f;
+    }
     std::lock_guard<std::mutex> lock(g_tuned_mu);
-    g_tuned[kv.first] = best;
+    g_tuned[kv.first] = Tuned{best, best_f};
+  }
+  for (capow_ctx *c : b->all) {  // the buffers for the chosen tiles and buckets: enqueues allocate nothing
+    int rc = prepare_paint_buffers(c, nmax[c], wts[c]);
+    if (rc) return rc;
   }
   // ---- one uncaptured pass over the first mock of each context: every kernel and plan a graph holds
   // has run once before a capture starts

@@ -455,6 +455,36 @@ static int ensure_records(capow_ctx *c, unsigned long long need, bool weights) {
   return CAPOW_OK;
 }
 
+// Records per tile of a one-pass bucket paint of n particles.
+static unsigned bucket_capacity(const capow_ctx *c, unsigned long long n) {
+  const double mean = tile_dup_estimate(c->g, c->tg) * (double)n / (double)c->tg.ntiles;
+  const double f = c->bucket_factor > 0.0f ? (double)c->bucket_factor : 2.0;
+  return ((unsigned)(f * mean) + 64 + 31) & ~31u;
+}
+
+// The bucket records and the overflow list of a one-pass paint of up to n particles.
+static int ensure_buckets(capow_ctx *c, unsigned long long n, bool weights) {
+  int rc = ensure_records(c, (unsigned long long)bucket_capacity(c, n) * c->tg.ntiles, weights);
+  if (rc) return rc;
+  const unsigned long long ocap = n / 4 + 65536;
+  if (!c->pb.ovf_count) CK(c, cudaMalloc(&c->pb.ovf_count, sizeof(unsigned)));
+  if (c->pb.ovf_cap < ocap || (weights && !c->pb.ovf_w)) {
+    if (c->pb.ovf_recs) cudaFree(c->pb.ovf_recs);
+    if (c->pb.ovf_w) cudaFree(c->pb.ovf_w);
+    if (c->pb.ovf_tile) cudaFree(c->pb.ovf_tile);
+    c->pb.ovf_recs = nullptr;
+    c->pb.ovf_w = nullptr;
+    c->pb.ovf_tile = nullptr;
+    c->pb.ovf_cap = 0;
+    CK(c, cudaMalloc(&c->pb.ovf_recs, sizeof(float4) * ocap));
+    CK(c, cudaMalloc(&c->pb.ovf_tile, sizeof(unsigned) * ocap));
+    if (weights) CK(c, cudaMalloc(&c->pb.ovf_w, sizeof(float) * ocap));
+    c->pb.ovf_cap = ocap;
+  }
+  return CAPOW_OK;
+}
+
+
 int enqueue_paint(capow_ctx *c, const capow_particles &d) {
   const long long n = (long long)d.n;
   GridPtrs gp = grid_ptrs(c);
@@ -474,28 +504,11 @@ int enqueue_paint(capow_ctx *c, const capow_particles &d) {
     }
     c->pb.bucket_cap = 0;
     if (c->prec == CAPOW_FP32_MIXED && !c->two_pass) {
-      // bucket mode: each tile gets twice its mean share of the records (plus slack); the overflow
-      // list takes up to a quarter of the catalogue; beyond that the paint falls back to two passes
-      const double mean = tile_dup_estimate(c->g, c->tg) * (double)n / (double)c->tg.ntiles;
-      const unsigned cap = ((unsigned)(2.0 * mean) + 64 + 31) & ~31u;
-      int rc = ensure_records(c, (unsigned long long)cap * c->tg.ntiles, d.w != nullptr);
+      // bucket mode: each tile gets bucket_factor times its mean share of the records (plus slack); the
+      // overflow list takes up to a quarter of the catalogue; beyond that the paint falls back to two passes
+      int rc = ensure_buckets(c, (unsigned long long)n, d.w != nullptr);
       if (rc) return rc;
-      const unsigned long long ocap = (unsigned long long)n / 4 + 65536;
-      if (!c->pb.ovf_count) CK(c, cudaMalloc(&c->pb.ovf_count, sizeof(unsigned)));
-      if (c->pb.ovf_cap < ocap || (d.w && !c->pb.ovf_w)) {
-        if (c->pb.ovf_recs) cudaFree(c->pb.ovf_recs);
-        if (c->pb.ovf_w) cudaFree(c->pb.ovf_w);
-        if (c->pb.ovf_tile) cudaFree(c->pb.ovf_tile);
-        c->pb.ovf_recs = nullptr;
-        c->pb.ovf_w = nullptr;
-        c->pb.ovf_tile = nullptr;
-        c->pb.ovf_cap = 0;
-        CK(c, cudaMalloc(&c->pb.ovf_recs, sizeof(float4) * ocap));
-        CK(c, cudaMalloc(&c->pb.ovf_tile, sizeof(unsigned) * ocap));
-        if (d.w) CK(c, cudaMalloc(&c->pb.ovf_w, sizeof(float) * ocap));
-        c->pb.ovf_cap = ocap;
-      }
-      c->pb.bucket_cap = cap;
+      c->pb.bucket_cap = bucket_capacity(c, (unsigned long long)n);
     } else {
       unsigned long long want = (unsigned long long)(tile_dup_estimate(c->g, c->tg) * 1.25 * n) + 65536;
       if (c->pb.capacity < want / 2 || (d.w && !c->pb.recw)) {
@@ -519,8 +532,9 @@ int enqueue_paint(capow_ctx *c, const capow_particles &d) {
   return CAPOW_OK;
 }
 
-// Size the FP32 record and edge buffers for catalogues of up to nmax particles (so that a later
-// enqueue_paint allocates nothing).
+// Size the FP32 record and edge buffers for catalogues of up to nmax particles (the one-pass buckets at
+// the context's bucket_factor and their overflow list, unless two_pass), so that a later enqueue_paint
+// allocates nothing.
 int prepare_paint_buffers(capow_ctx *c, unsigned long long nmax, bool weights) {
   if (c->prec == CAPOW_FP64) return CAPOW_OK;
   if (!c->pb.edge_count) CK(c, cudaMalloc(&c->pb.edge_count, sizeof(unsigned)));
@@ -531,6 +545,7 @@ int prepare_paint_buffers(capow_ctx *c, unsigned long long nmax, bool weights) {
     CK(c, cudaMalloc(&c->pb.edge_list, sizeof(unsigned) * (nmax + 1)));
     c->pb.edge_cap = nmax + 1;
   }
+  if (c->prec == CAPOW_FP32_MIXED && !c->two_pass) return ensure_buckets(c, nmax, weights);
   const unsigned long long want = (unsigned long long)(tile_dup_estimate(c->g, c->tg) * 1.25 * nmax) + 65536;
   return ensure_records(c, want, weights);
 }

@@ -56,6 +56,7 @@ struct capow_ctx {
   // capow_backward (created on first use): full 3-D plans, bin coefficients, host-output staging
   bool quiet;           // skip the stage-timing event records (batched enqueue, graph capture)
   bool two_pass;        // FP32 paint: count/scan/scatter instead of the one-pass buckets
+  float bucket_factor;  // one-pass buckets: records per tile = factor * the tile's mean share + 64 (0: 2)
   bool adj_plans;
   cufftHandle adj_fwd, adj_inv;
   double *adj_coef;
@@ -114,6 +115,8 @@ int create_paint_ctx(const capow_params *p, const capow_options *o, int survey, 
 int settle_paint(capow_ctx *c);
 int enqueue_paint(capow_ctx *c, const capow_particles &d);
 int enqueue_power_kernels(capow_ctx *c);
+// Size the FP32 record and edge buffers (and, unless two_pass, the one-pass buckets at bucket_factor and
+// their overflow list) for catalogues of up to nmax particles, so that a later enqueue_paint allocates nothing.
 int prepare_paint_buffers(capow_ctx *c, unsigned long long nmax, bool weights);
 void fill_spectra(const capow_ctx *c, const capow_params &p, const DevStats &st, const double *h_bins,
                   const unsigned long long *nmodes, const unsigned long long *nmodes2d, capow_spectrum *out);
