@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "bin.cuh"
+#include "harm.cuh"
 #include "paint.cuh"
 
 // ------------------------------------------------------------------------------------ host side
@@ -1017,6 +1018,25 @@ struct ZrGeo {
   long long slice, in_slot, out_slot;
 };
 
+// Geometry of a z pass over nslot grids ([NX][NY][row] floats, slot stride in_slot) into the transposed
+// slots (slot stride out_slot complex); nyb is set by the launcher from its rows per CTA.
+static ZrGeo zr2c_geo(const BinParams &bp, int nslot, long long in_slot, int row, long long out_slot) {
+  ZrGeo zg;
+  int lm = 0;
+  while ((2 << lm) < bp.nz) lm++;  // M = NZ / 2 = 2^lm
+  zg.log2m = lm;
+  zg.nx = bp.nx;
+  zg.ny = bp.ny;
+  zg.nzc = bp.nzc;
+  zg.row = row;
+  zg.nyb = 0;
+  zg.slice = (long long)bp.ny * row;
+  zg.in_slot = in_slot;
+  zg.out_slot = out_slot;
+  zg.ns = nslot;
+  return zg;
+}
+
 // Shared tables of the z pass: radix-8 twiddles (stw), the row of Z[k] after the DIF stages (spos)
 // and the real-input split twiddles (stp), carved after a data area of `data_bytes`.
 struct ZrTables {
@@ -1046,12 +1066,17 @@ __device__ ZrTables zr2c_load_tables(const BinTables &t, int log2m, unsigned cha
   return z;
 }
 
+// The z pass's loads: a pair of consecutive reals of row y of plane x (z = 2n, 2n + 1), read once.
+struct ZrPlainLoad {
+  __device__ __forceinline__ float2 operator()(const float2 *p, int, int, int) const { return __ldcs(p); }
+};
+
 // One block of the z pass: ZB rows y0.. of plane x of slot sl, through the shared data area sd
 // ([M][ZB + 1]). The caller has synchronised after the tables were written and after any earlier use
-// of sd.
-template <int ZB>
+// of sd. ld reads the input pairs (ZrPlainLoad, or a weighting load).
+template <int ZB, class LD = ZrPlainLoad>
 __device__ __forceinline__ void zr2c_block(const ZrGeo &zg, const ZrTables &z, const float *in, float2 *out,
-                                           float2 *sd, int sl, int x, int y0) {
+                                           float2 *sd, int sl, int x, int y0, const LD &ld = LD()) {
   constexpr int LZB = ZB == 16 ? 4 : 3;
   const int log2m = zg.log2m, M = 1 << log2m, P = ZB + 1, Q1 = M >> 3;
   const float *src = in + sl * zg.in_slot + (long long)x * zg.slice;
@@ -1062,7 +1087,7 @@ __device__ __forceinline__ void zr2c_block(const ZrGeo &zg, const ZrTables &z, c
     const float2 *rp = reinterpret_cast<const float2 *>(src + (long long)(y < zg.ny ? y : 0) * zg.row) + jj;
     float2 a[8];
 #pragma unroll
-    for (int q = 0; q < 8; q++) a[q] = y < zg.ny ? __ldcs(rp + q * Q1) : make_float2(0.0f, 0.0f);
+    for (int q = 0; q < 8; q++) a[q] = y < zg.ny ? ld(rp + q * Q1, x, y, jj + q * Q1) : make_float2(0.0f, 0.0f);
     dft8(a);
     if (jj > 0) twiddle8(a, z.stw + 8 * jj);
     float2 *p = sd + jj * P + r;
@@ -1149,6 +1174,85 @@ __global__ void __launch_bounds__(ZR_THREADS) k_zr2c(ZrGeo zg, BinTables t, cons
     }
     zr2c_block<ZB>(zg, z, in, out, sd, sl, x, y0);
   }
+}
+
+// The survey estimator's weighted z pass: the input of a set (l, m) is the painted grid times h_lm(r^) of
+// each cell (harm.cuh), applied as the rows are read, so that no weighted grid is written.
+struct ZrWeight {
+  const float *vx, *vy, *vz;  // cell-corner offsets from the observer per axis
+  int l, m;
+};
+
+// The degree L is a compile-time constant, so the polynomial of each m is specialised.
+template <int L>
+struct ZrWeightLoad {
+  ZrWeight w;
+  __device__ __forceinline__ float2 operator()(const float2 *p, int x, int y, int n) const {
+    float2 v = __ldcs(p);
+    const float px = __ldg(w.vx + x), py = __ldg(w.vy + y), pxy = px * px + py * py;
+    const float2 pz = __ldg(reinterpret_cast<const float2 *>(w.vz) + n);  // z = 2n, 2n + 1
+    v.x *= sv_cell_weight<float>(L, w.m, px, py, pxy, pz.x);
+    v.y *= sv_cell_weight<float>(L, w.m, px, py, pxy, pz.y);
+    return v;
+  }
+};
+
+template <int ZB, int L>
+__global__ void __launch_bounds__(ZR_THREADS) k_zr2c_w(ZrGeo zg, BinTables t, const float *in, float2 *out,
+                                                       ZrWeightLoad<L> ld) {
+  extern __shared__ __align__(16) unsigned char smz[];
+  const int M = 1 << zg.log2m;
+  float2 *sd = (float2 *)smz;  // [M][ZB + 1]
+  const ZrTables z = zr2c_load_tables(t, zg.log2m, smz + align16(8u * (unsigned)M * (ZB + 1)));
+  const int per_slot = zg.nx * zg.nyb, nblk = per_slot * zg.ns;
+  for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+    const int sl = blk / per_slot, rem = blk - sl * per_slot;
+    const int x = rem / zg.nyb, y0 = (rem - x * zg.nyb) * ZB;
+    __syncthreads();
+    zr2c_block<ZB, ZrWeightLoad<L>>(zg, z, in, out, sd, sl, x, y0, ld);
+  }
+}
+
+template <int ZB, int L>
+static void launch_zr2c_w_l(cudaStream_t s, const ZrGeo &zg, const BinTables &t, int nslot, const float *in,
+                            float2 *out, const ZrWeight &w) {
+  const int M = 1 << zg.log2m;
+  const size_t smem = align16(8u * (unsigned)M * (ZB + 1)) + zr2c_tables_bytes(zg.log2m);
+  cudaFuncSetAttribute(k_zr2c_w<ZB, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 1, dev = 0, nsm = 152;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zr2c_w<ZB, L>, ZR_THREADS, smem);
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const long long nblk = (long long)zg.nx * zg.nyb * nslot;
+  long long grid = (long long)(per_sm > 0 ? per_sm : 1) * nsm;
+  if (grid > nblk) grid = nblk;
+  k_zr2c_w<ZB, L><<<(unsigned)grid, ZR_THREADS, smem, s>>>(zg, t, in, out, ZrWeightLoad<L>{w});
+}
+
+template <int ZB>
+static void launch_zr2c_w_t(cudaStream_t s, const ZrGeo &zg, const BinTables &t, int nslot, const float *in,
+                            float2 *out, const ZrWeight &w) {
+  switch (w.l) {
+    case 1: launch_zr2c_w_l<ZB, 1>(s, zg, t, nslot, in, out, w); break;
+    case 2: launch_zr2c_w_l<ZB, 2>(s, zg, t, nslot, in, out, w); break;
+    case 3: launch_zr2c_w_l<ZB, 3>(s, zg, t, nslot, in, out, w); break;
+    default: launch_zr2c_w_l<ZB, 4>(s, zg, t, nslot, in, out, w); break;
+  }
+}
+
+void launch_zr2c_weighted(cudaStream_t s, const BinParams &bp, const BinTables &t, int nslot, const float *in,
+                          long long in_slot, int row, float2 *out, long long out_slot, const float *vx,
+                          const float *vy, const float *vz, int l, int m, long long *launches) {
+  ZrGeo zg = zr2c_geo(bp, nslot, in_slot, row, out_slot);
+  const ZrWeight ld{vx, vy, vz, l, m};
+  if (bp.nz <= 512) {
+    zg.nyb = (bp.ny + 15) / 16;
+    launch_zr2c_w_t<16>(s, zg, t, nslot, in, out, ld);
+  } else {
+    zg.nyb = (bp.ny + 7) / 8;
+    launch_zr2c_w_t<8>(s, zg, t, nslot, in, out, ld);
+  }
+  (*launches)++;
 }
 
 // ------------------------------------------------------------ z and y axes in one launch (FP32)
@@ -1513,18 +1617,7 @@ static void launch_zr2c_t(cudaStream_t s, const ZrGeo &zg, const BinTables &t, i
 
 void launch_zr2c(cudaStream_t s, const BinParams &bp, const BinTables &t, int nslot, const float *in,
                  long long in_slot, int row, float2 *out, long long out_slot, long long *launches) {
-  ZrGeo zg;
-  int lm = 0;
-  while ((2 << lm) < bp.nz) lm++;  // M = NZ / 2 = 2^lm
-  zg.log2m = lm;
-  zg.nx = bp.nx;
-  zg.ny = bp.ny;
-  zg.nzc = bp.nzc;
-  zg.row = row;
-  zg.slice = (long long)bp.ny * row;
-  zg.in_slot = in_slot;
-  zg.out_slot = out_slot;
-  zg.ns = nslot;
+  ZrGeo zg = zr2c_geo(bp, nslot, in_slot, row, out_slot);
   if (bp.nz <= 512) {  // 16 rows per CTA: 128-byte segments per kz
     zg.nyb = (bp.ny + 15) / 16;
     launch_zr2c_t<16>(s, zg, t, nslot, in, out);

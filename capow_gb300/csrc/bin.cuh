@@ -122,6 +122,11 @@ void launch_zy(cudaStream_t s, const BinParams &bp, const BinTables &t, int nslo
                long long *launches);
 // Real-to-complex DFT along z of every row of every painted grid (in: [NX][NY][row] floats, slot
 // stride in_slot floats), out of place into out (slot stride out_slot complex) as [NX][NZ/2+1][NY].
+// The same z pass with the survey estimator's cell weights h_lm(r^) applied to the input as it is read (vx,
+// vy, vz: the cell-corner offsets from the observer per axis).
+void launch_zr2c_weighted(cudaStream_t s, const BinParams &bp, const BinTables &t, int nslot, const float *in,
+                          long long in_slot, int row, float2 *out, long long out_slot, const float *vx,
+                          const float *vy, const float *vz, int l, int m, long long *launches);
 void launch_zr2c(cudaStream_t s, const BinParams &bp, const BinTables &t, int nslot, const float *in,
                  long long in_slot, int row, float2 *out, long long out_slot, long long *launches);
 void launch_xbin(cudaStream_t s, const BinParams &bp, const BinTables &t, const XbinGeo &xg, void *const slots[4],

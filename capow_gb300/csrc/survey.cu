@@ -43,6 +43,7 @@
 #include <vector>
 
 #include "ctx.cuh"
+#include "harm.cuh"
 
 // ------------------------------------------------------------------------------------ device state
 struct SvStats {
@@ -64,49 +65,6 @@ struct SvIn {
 // Grid slot of (stencil, field): stencil 0 normal, 1 interlaced; field 0 density, 1 momentum (Momentum 2, 3).
 // The periodic path's order, so that the FP32 paint context's grids are the survey's slots.
 __host__ __device__ __forceinline__ int sv_slot(int stencil, int field, int nf) { return stencil * nf + field; }
-
-// Real harmonic polynomials of degree l (m = 0 .. 2l) and the factors c_lm of
-// L_l(n.u) = sum_m c_lm h_lm(n) h_lm(u) for unit n and u.
-template <typename R>
-__device__ __forceinline__ R harm(int l, int m, R x, R y, R z) {
-  const R x2 = x * x, y2 = y * y, z2 = z * z;
-  switch (l) {
-    case 1:
-      return m == 0 ? x : (m == 1 ? y : z);
-    case 2:
-      switch (m) {
-        case 0: return x * y;
-        case 1: return y * z;
-        case 2: return x * z;
-        case 3: return x2 - y2;
-        default: return (R)2 * z2 - x2 - y2;
-      }
-    case 3:
-      switch (m) {
-        case 0: return x * (x2 - (R)3 * y2);
-        case 1: return y * ((R)3 * x2 - y2);
-        case 2: return z * (x2 - y2);
-        case 3: return x * y * z;
-        case 4: return x * ((R)4 * z2 - x2 - y2);
-        case 5: return y * ((R)4 * z2 - x2 - y2);
-        default: return z * ((R)2 * z2 - (R)3 * x2 - (R)3 * y2);
-      }
-    default: {
-      const R p = x2 + y2;
-      switch (m) {
-        case 0: return x * y * (x2 - y2);
-        case 1: return x2 * x2 - (R)6 * x2 * y2 + y2 * y2;
-        case 2: return y * z * ((R)3 * x2 - y2);
-        case 3: return x * z * (x2 - (R)3 * y2);
-        case 4: return x * y * ((R)6 * z2 - p);
-        case 5: return (x2 - y2) * ((R)6 * z2 - p);
-        case 6: return y * z * ((R)4 * z2 - (R)3 * p);
-        case 7: return x * z * ((R)4 * z2 - (R)3 * p);
-        default: return (R)8 * z2 * z2 - (R)24 * z2 * p + (R)3 * p * p;
-      }
-    }
-  }
-}
 
 static double harm_coef(int l, int m) {
   static const double c1[3] = {1, 1, 1};
@@ -181,8 +139,6 @@ __device__ void sv_block_add(const double (&v)[NV], double *const (&dst)[NV]) {
   __syncthreads();
 }
 
-__device__ __forceinline__ float sv_rsqrt(float a) { return rsqrtf(a); }
-__device__ __forceinline__ double sv_rsqrt(double a) { return rsqrt(a); }
 __device__ __forceinline__ float sv_mul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double sv_mul(double a, double b) { return __dmul_rn(a, b); }
 
@@ -349,14 +305,6 @@ __global__ void __launch_bounds__(256) k_sv_combine(Geom g, SvIn<T> in, const T 
 // harmonics vanish. l = 0 copies the grid (src/main.c:503-511). One warp per (x, y) row, grid-stride over
 // rows; each lane moves z pairs (rows have an even length, so pairs are aligned vector loads).
 template <typename R>
-__device__ __forceinline__ R sv_cell_weight(int l, int m, R px, R py, R pxy, R pz) {
-  R r2 = pxy + pz * pz;
-  if (r2 == (R)0) r2 = (R)1;
-  const R inv = sv_rsqrt(r2);
-  return harm<R>(l, m, px * inv, py * inv, pz * inv);
-}
-
-template <typename R>
 __global__ void __launch_bounds__(256) k_sv_weight(const R *a0, const R *a1, R *w0, R *w1, const R *vx, const R *vy,
                                                    const R *vz, int nx, int ny, int nz, long long row, int l, int m) {
   typedef typename std::conditional<sizeof(R) == 4, float2, double2>::type R2;
@@ -442,7 +390,7 @@ __device__ __forceinline__ R sv_ref(const C &a, const C &b) { return a.x * b.x +
 // One thread per (ky, kz) column walks x over a chunk of SV_ICHUNK; bin sums run per thread over equal-bin
 // stretches, then per CTA in shared memory, then FP64 global atomics. Modes beyond the top bin edge are
 // skipped as in k_bin.
-template <typename R, int L, bool CROSS>
+template <typename R, int L, bool CROSS, bool TR>
 __global__ void __launch_bounds__(256) k_sv_assign(BinParams bp, BinTables t, SvAssign<R> sa, double *bins) {
   typedef typename SvC<R>::C C;
   constexpr bool F32 = sizeof(R) == 4;
@@ -480,7 +428,9 @@ __global__ void __launch_bounds__(256) k_sv_assign(BinParams bp, BinTables t, Sv
   const long long cols = (long long)bp.ny * bp.nzc;
   const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (col < cols) {
-    const int j = (int)(col / bp.nzc), k = (int)(col - (long long)j * bp.nzc);
+    // the column (ky, kz): [NX][NY][NZ/2+1] grids, or TR: the transposed [NX][NZ/2+1][NY] of the z-pass path
+    const int j = TR ? (int)(col % bp.ny) : (int)(col / bp.nzc);
+    const int k = TR ? (int)(col / bp.ny) : (int)(col - (long long)j * bp.nzc);
     const R syz = F32 ? (R)(t.fy2f[j] + t.fz2f[k]) : (R)0;
     const double fy2 = t.fy2d[j], fz2 = t.fz2d[k];
     R cyz = F32 ? (R)(t.cyf[j] * t.czf[k]) : (R)(t.cyd[j] * t.czd[k]);
@@ -510,7 +460,7 @@ __global__ void __launch_bounds__(256) k_sv_assign(BinParams bp, BinTables t, Sv
         if (bp.interlace) om1 = sa.a[sa.sm1][sa.oind];
       }
     }
-    const long long base = (long long)j * bp.nzc + k;
+    const long long base = TR ? (long long)k * bp.ny + j : (long long)j * bp.nzc + k;
     R acc0 = (R)0, acc2 = (R)0, acc4 = (R)0;
     int cur = -1;
     R lo = (R)1, hi = (R)0;
@@ -701,6 +651,11 @@ struct capow_survey_ctx {
   std::vector<unsigned long long> nmodes;
   cufftHandle plan;
   bool plan_ok, plan_per_grid;
+  // FP32 with a power-of-two NZ: the z axis by the weighted z pass into the transposed [NX][NZ/2+1][NY]
+  // work slots, then cuFFT along y (contiguous rows) and along x (strided), in place
+  bool tr;
+  cufftHandle yplan, xplan;
+  bool yplan_ok, xplan_ok;
   // the observer's cell (r2 == 0), if any
   int origin;
   long long oind;
@@ -892,6 +847,25 @@ extern "C" int capow_survey_create(const capow_params *p, const capow_survey_par
   CK(c, cudaMemcpyAsync(c->nmodes.data(), c->nmodes_d, sizeof(unsigned long long) * nk, cudaMemcpyDeviceToHost,
                         c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
+  // FP32 with a power-of-two NZ: the transposed path (its z pass weights the painted grids as it reads
+  // them, so no weighted grid is written; the y axis is then a contiguous batched transform)
+  if (!f64 && c->bt.twz && zr2c_supported(bp)) {
+    const long long yrows = (long long)c->nslot * p->NX * bp.nzc, xcols = (long long)bp.nzc * p->NY;
+    int ny = p->NY, nx = p->NX, emb = p->NX;
+    if (yrows <= 0x7fffffffLL && xcols <= 0x7fffffffLL &&
+        cufftPlanMany(&c->yplan, 1, &ny, nullptr, 1, ny, nullptr, 1, ny, CUFFT_C2C, (int)yrows) == CUFFT_SUCCESS) {
+      c->yplan_ok = true;
+      if (cufftPlanMany(&c->xplan, 1, &nx, &emb, (int)xcols, 1, &emb, (int)xcols, 1, CUFFT_C2C, (int)xcols) ==
+          CUFFT_SUCCESS) {
+        c->xplan_ok = true;
+        c->tr = true;
+        CKFFT(c, cufftSetStream(c->yplan, c->stream));
+        CKFFT(c, cufftSetStream(c->xplan, c->stream));
+        return CAPOW_OK;
+      }
+    }
+    (void)cudaGetLastError();  // no room for the plans: the 3-D transform below
+  }
   // one batched in-place real-to-complex plan over the nslot term grids (fftw_execute of plan, plan_interlace,
   // plan_mom and plan_mom_interlace, src/main.c:513-526 and the product loops)
   int n[3] = {p->NX, p->NY, p->NZ};
@@ -913,6 +887,8 @@ extern "C" void capow_survey_destroy(capow_survey_ctx *c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->plan_ok) cufftDestroy(c->plan);
+  if (c->yplan_ok) cufftDestroy(c->yplan);
+  if (c->xplan_ok) cufftDestroy(c->xplan);
   if (c->pc) capow_destroy(c->pc);
   if (c->comb) cudaFree(c->comb);
   for (void *q : c->allocs) cudaFree(q);
@@ -1070,8 +1046,14 @@ static int sv_paint_tiles(capow_survey_ctx *c, const capow_survey_catalogue *dat
 
 template <typename R, int L>
 static void sv_launch_assign(capow_survey_ctx *c, const dim3 &grid, const SvAssign<R> &sa) {
-  if (c->nf == 2) k_sv_assign<R, L, true><<<grid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins);
-  else k_sv_assign<R, L, false><<<grid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins);
+  if (c->tr) {
+    if (c->nf == 2) k_sv_assign<R, L, true, true><<<grid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins);
+    else k_sv_assign<R, L, false, true><<<grid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins);
+  } else if (c->nf == 2) {
+    k_sv_assign<R, L, true, false><<<grid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins);
+  } else {
+    k_sv_assign<R, L, false, false><<<grid, 256, 0, c->stream>>>(c->bp, c->bt, sa, c->bins);
+  }
 }
 
 template <typename R>
@@ -1116,14 +1098,32 @@ static int sv_multipoles(capow_survey_ctx *c) {
   c->sets = 0;
   for (int l = 0; l <= 4; l += step) {
     for (int m = 0; m < 2 * l + 1; m++) {
-      for (int f = 0; f < nf; f++) {  // the density grid (and its interlaced copy), then the momentum grid
+      bool transformed = false;
+      if constexpr (sizeof(R) == 4) {
+        if (c->tr) {  // weighted z pass into the transposed work slots, then y and x in place
+          const long long tslot = ge / 2;
+          if (l == 0)
+            launch_zr2c(c->stream, c->bp, c->bt, c->nslot, (const float *)a[0], ge, (int)g.row, (float2 *)w[0],
+                        tslot, &c->launches);
+          else
+            launch_zr2c_weighted(c->stream, c->bp, c->bt, c->nslot, (const float *)a[0], ge, (int)g.row,
+                                 (float2 *)w[0], tslot, (const float *)c->vx, (const float *)c->vy,
+                                 (const float *)c->vz, l, m, &c->launches);
+          CKFFT(c, cufftExecC2C(c->yplan, (cufftComplex *)w[0], (cufftComplex *)w[0], CUFFT_FORWARD));
+          for (int s = 0; s < c->nslot; s++)
+            CKFFT(c, cufftExecC2C(c->xplan, (cufftComplex *)w[s], (cufftComplex *)w[s], CUFFT_FORWARD));
+          transformed = true;
+        }
+      }
+      for (int f = 0; f < nf && !transformed; f++) {  // the density grid (and its interlaced copy), then momentum
         const int s0 = sv_slot(0, f, nf), s1 = sv_slot(1, f, nf);
         k_sv_weight<R><<<wblocks, 256, 0, c->stream>>>(a[s0], il ? a[s1] : nullptr, w[s0], il ? w[s1] : nullptr,
                                                        (const R *)c->vx, (const R *)c->vy, (const R *)c->vz, p.NX,
                                                        p.NY, p.NZ, g.row, l, m);
         c->launches++;
       }
-      if (c->plan_per_grid) {
+      if (transformed) {
+      } else if (c->plan_per_grid) {
         for (int s = 0; s < c->nslot; s++) {
           if (sizeof(R) == 8) CKFFT(c, cufftExecD2Z(c->plan, (cufftDoubleReal *)w[s], (cufftDoubleComplex *)w[s]));
           else CKFFT(c, cufftExecR2C(c->plan, (cufftReal *)w[s], (cufftComplex *)w[s]));
