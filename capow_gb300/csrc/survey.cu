@@ -763,6 +763,9 @@ extern "C" int capow_survey_create(const capow_params *p, const capow_survey_par
     rc = create_paint_ctx(p, &po, c->nf, &c->pc);
     if (rc) FAIL(c, rc, "paint context: %s", c->pc ? capow_last_error(c->pc) : "invalid parameters");
     c->paint = c->pc->grid_base;
+    // a survey fills part of the box (a ball or a sky cut), so an occupied tile holds several times the
+    // box's mean share of the records: buckets of four mean shares keep them out of the overflow path
+    c->pc->bucket_factor = 4.0f;
   }
   c->work = sv_dalloc(c, eb * ge * c->nslot);
   c->F0 = sv_dalloc(c, eb * ge);
