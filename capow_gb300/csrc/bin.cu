@@ -1073,21 +1073,43 @@ struct ZrPlainLoad {
 
 // One block of the z pass: ZB rows y0.. of plane x of slot sl, through the shared data area sd
 // ([M][ZB + 1]). The caller has synchronised after the tables were written and after any earlier use
-// of sd. ld reads the input pairs (ZrPlainLoad, or a weighting load).
-template <int ZB, class LD = ZrPlainLoad>
+// of sd. ld reads the input pairs (ZrPlainLoad, or a weighting load). SP = 2: the block holds ZB / 2
+// rows of each of the slots sl and sl + 1 (columns r and r + ZB / 2 are row y0 + r of each), and one
+// thread reads the same cells of both, so that a weighting load's weights are evaluated once for both.
+template <int ZB, class LD = ZrPlainLoad, int SP = 1>
 __device__ __forceinline__ void zr2c_block(const ZrGeo &zg, const ZrTables &z, const float *in, float2 *out,
                                            float2 *sd, int sl, int x, int y0, const LD &ld = LD()) {
   constexpr int LZB = ZB == 16 ? 4 : 3;
+  constexpr int RS = ZB / SP;  // rows of each slot
   const int log2m = zg.log2m, M = 1 << log2m, P = ZB + 1, Q1 = M >> 3;
   const float *src = in + sl * zg.in_slot + (long long)x * zg.slice;
   // first DIF stage (span M) straight from the rows: butterfly (row r, jj) reads z[jj + q M/8];
   // lanes run along a row, so each of a warp's 8 loads is one contiguous 256-byte piece
-  for (int u = threadIdx.x; u < (ZB << (log2m - 3)); u += blockDim.x) {
+  for (int u = threadIdx.x; u < (RS << (log2m - 3)); u += blockDim.x) {
     const int jj = u & (Q1 - 1), r = u >> (log2m - 3), y = y0 + r;
     const float2 *rp = reinterpret_cast<const float2 *>(src + (long long)(y < zg.ny ? y : 0) * zg.row) + jj;
     float2 a[8];
+    if constexpr (SP == 1) {
 #pragma unroll
-    for (int q = 0; q < 8; q++) a[q] = y < zg.ny ? ld(rp + q * Q1, x, y, jj + q * Q1) : make_float2(0.0f, 0.0f);
+      for (int q = 0; q < 8; q++) a[q] = y < zg.ny ? ld(rp + q * Q1, x, y, jj + q * Q1) : make_float2(0.0f, 0.0f);
+    } else {
+      const float2 *rpb = rp + (zg.in_slot >> 1);  // the same row of slot sl + 1 (in_slot floats is even)
+      float2 b[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        a[q] = b[q] = make_float2(0.0f, 0.0f);
+        if (y < zg.ny) {
+          const float2 w = ld.weights(x, y, jj + q * Q1), va = __ldcs(rp + q * Q1), vb = __ldcs(rpb + q * Q1);
+          a[q] = make_float2(va.x * w.x, va.y * w.y);
+          b[q] = make_float2(vb.x * w.x, vb.y * w.y);
+        }
+      }
+      dft8(b);
+      if (jj > 0) twiddle8(b, z.stw + 8 * jj);
+      float2 *pb = sd + jj * P + r + RS;
+#pragma unroll
+      for (int q = 0; q < 8; q++) pb[q * Q1 * P] = b[q];
+    }
     dft8(a);
     if (jj > 0) twiddle8(a, z.stw + 8 * jj);
     float2 *p = sd + jj * P + r;
@@ -1135,10 +1157,10 @@ __device__ __forceinline__ void zr2c_block(const ZrGeo &zg, const ZrTables &z, c
   }
   // real-input split and transposed store, X[k] and X[M-k] from the same pair: with
   // A = Z[k] + conj Z[M-k], B = Z[k] - conj Z[M-k] and w^M = -1, X[k] = (A + (-i) w^k B) / 2 and
-  // X[M-k] = (conj A + (-i) conj(w^k B)) / 2. The thread's row r is the same on every step.
-  const int r = threadIdx.x & (ZB - 1), y = y0 + r;
+  // X[M-k] = (conj A + (-i) conj(w^k B)) / 2. The thread's column r is the same on every step.
+  const int r = threadIdx.x & (ZB - 1), y = y0 + r % RS, so = r / RS;
   if (y < zg.ny) {
-    float2 *dst = out + sl * zg.out_slot + (long long)x * zg.nzc * zg.ny + y;
+    float2 *dst = out + (sl + so) * zg.out_slot + (long long)x * zg.nzc * zg.ny + y;
     for (int k = threadIdx.x >> LZB; k <= (M >> 1); k += blockDim.x >> LZB) {
       const float2 zk = sd[z.spos[k & (M - 1)] * P + r];
       const float2 zm = sd[z.spos[(M - k) & (M - 1)] * P + r];
@@ -1187,46 +1209,60 @@ struct ZrWeight {
 template <int L>
 struct ZrWeightLoad {
   ZrWeight w;
-  __device__ __forceinline__ float2 operator()(const float2 *p, int x, int y, int n) const {
-    float2 v = __ldcs(p);
+  // the weights of cells z = 2n and 2n + 1 of row y of plane x
+  __device__ __forceinline__ float2 weights(int x, int y, int n) const {
     const float px = __ldg(w.vx + x), py = __ldg(w.vy + y), pxy = px * px + py * py;
-    const float2 pz = __ldg(reinterpret_cast<const float2 *>(w.vz) + n);  // z = 2n, 2n + 1
-    v.x *= sv_cell_weight<float>(L, w.m, px, py, pxy, pz.x);
-    v.y *= sv_cell_weight<float>(L, w.m, px, py, pxy, pz.y);
-    return v;
+    const float2 pz = __ldg(reinterpret_cast<const float2 *>(w.vz) + n);
+    return make_float2(sv_cell_weight<float>(L, w.m, px, py, pxy, pz.x),
+                       sv_cell_weight<float>(L, w.m, px, py, pxy, pz.y));
+  }
+  __device__ __forceinline__ float2 operator()(const float2 *p, int x, int y, int n) const {
+    const float2 v = __ldcs(p), c = weights(x, y, n);
+    return make_float2(v.x * c.x, v.y * c.y);
   }
 };
 
-template <int ZB, int L>
+// SP = 2 (an even number of slots): each block takes ZB / 2 rows of a pair of slots, whose cells share
+// their weights (the weights depend on the cell only).
+template <int ZB, int L, int SP>
 __global__ void __launch_bounds__(ZR_THREADS) k_zr2c_w(ZrGeo zg, BinTables t, const float *in, float2 *out,
                                                        ZrWeightLoad<L> ld) {
   extern __shared__ __align__(16) unsigned char smz[];
+  constexpr int RS = ZB / SP;
   const int M = 1 << zg.log2m;
   float2 *sd = (float2 *)smz;  // [M][ZB + 1]
   const ZrTables z = zr2c_load_tables(t, zg.log2m, smz + align16(8u * (unsigned)M * (ZB + 1)));
-  const int per_slot = zg.nx * zg.nyb, nblk = per_slot * zg.ns;
+  const int per_group = zg.nx * zg.nyb, nblk = per_group * (zg.ns / SP);
   for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
-    const int sl = blk / per_slot, rem = blk - sl * per_slot;
-    const int x = rem / zg.nyb, y0 = (rem - x * zg.nyb) * ZB;
+    const int grp = blk / per_group, rem = blk - grp * per_group;
+    const int x = rem / zg.nyb, y0 = (rem - x * zg.nyb) * RS;
     __syncthreads();
-    zr2c_block<ZB, ZrWeightLoad<L>>(zg, z, in, out, sd, sl, x, y0, ld);
+    zr2c_block<ZB, ZrWeightLoad<L>, SP>(zg, z, in, out, sd, grp * SP, x, y0, ld);
   }
+}
+
+template <int ZB, int L, int SP>
+static void launch_zr2c_w_sp(cudaStream_t s, ZrGeo zg, const BinTables &t, int nslot, const float *in,
+                             float2 *out, const ZrWeight &w) {
+  const int M = 1 << zg.log2m;
+  zg.nyb = (zg.ny + ZB / SP - 1) / (ZB / SP);
+  const size_t smem = align16(8u * (unsigned)M * (ZB + 1)) + zr2c_tables_bytes(zg.log2m);
+  cudaFuncSetAttribute(k_zr2c_w<ZB, L, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 1, dev = 0, nsm = 152;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zr2c_w<ZB, L, SP>, ZR_THREADS, smem);
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const long long nblk = (long long)zg.nx * zg.nyb * (nslot / SP);
+  long long grid = (long long)(per_sm > 0 ? per_sm : 1) * nsm;
+  if (grid > nblk) grid = nblk;
+  k_zr2c_w<ZB, L, SP><<<(unsigned)grid, ZR_THREADS, smem, s>>>(zg, t, in, out, ZrWeightLoad<L>{w});
 }
 
 template <int ZB, int L>
 static void launch_zr2c_w_l(cudaStream_t s, const ZrGeo &zg, const BinTables &t, int nslot, const float *in,
                             float2 *out, const ZrWeight &w) {
-  const int M = 1 << zg.log2m;
-  const size_t smem = align16(8u * (unsigned)M * (ZB + 1)) + zr2c_tables_bytes(zg.log2m);
-  cudaFuncSetAttribute(k_zr2c_w<ZB, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  int per_sm = 1, dev = 0, nsm = 152;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zr2c_w<ZB, L>, ZR_THREADS, smem);
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const long long nblk = (long long)zg.nx * zg.nyb * nslot;
-  long long grid = (long long)(per_sm > 0 ? per_sm : 1) * nsm;
-  if (grid > nblk) grid = nblk;
-  k_zr2c_w<ZB, L><<<(unsigned)grid, ZR_THREADS, smem, s>>>(zg, t, in, out, ZrWeightLoad<L>{w});
+  if (nslot % 2 == 0 && (zg.in_slot % 2) == 0) launch_zr2c_w_sp<ZB, L, 2>(s, zg, t, nslot, in, out, w);
+  else launch_zr2c_w_sp<ZB, L, 1>(s, zg, t, nslot, in, out, w);
 }
 
 template <int ZB>

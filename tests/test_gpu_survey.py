@@ -160,6 +160,21 @@ def test_survey_matches_oracle(gpu, tmp_path, precision, order, il, odd):
         assert err <= (1e-12 if precision == "fp64" else 5e-5), (label, key, err)
 
 
+def test_survey_long_z_axis(gpu, tmp_path):
+    """A 16 x 16 x 1024 grid: the FP32 path's z pass takes its eight-row blocks there (its weighted variant
+    included), with odd multipoles; against the oracle."""
+    p, prm, sv = _write_params(tmp_path, NX=16, NY=16, NZ=1024, XMIN=300.0, XMAX=700.0, YMIN=-200.0, YMAX=200.0,
+                               ZMIN=-2000.0, ZMAX=2000.0, InterpOrder=3, DoInterlacing=1, NK=12, Maxk=0.06,
+                               Odd_Multipoles=1, Periodic=0, X_Origin=-40.0, Y_Origin=10.0, Z_Origin=5.0,
+                               REDMININ=0.0, REDMAXIN=5.0, NOBJ_Max=100000, NBAR_Column=5, FKP_Column=-1,
+                               FKP_Pk=4000.0)
+    df, rf = _catalogues(tmp_path, p, 3000, 20000, seed=57)
+    r = orc.survey_run(p, df, rf)
+    for precision in ("fp32", "fp64"):
+        res, _ = _gpu(prm, sv, df, rf, precision)
+        assert_survey(res, r["raw"], p, precision, label=f"long z {precision}")
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 @pytest.mark.parametrize("order,momentum", [(2, 0), (3, 0), (3, 1), (2, 2)])
 def test_survey_observer_on_a_cell_corner(gpu, tmp_path, precision, order, momentum):
