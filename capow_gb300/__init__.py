@@ -128,8 +128,10 @@ EXPORTS = [
     "capow_batch_release", "capow_survey_create", "capow_survey_power", "capow_survey_copy_grid",
     "capow_survey_stage_ms", "capow_survey_kernel_launches", "capow_survey_last_error", "capow_survey_destroy",
     "capow_read_survey_params", "capow_read_survey", "capow_survey_objects_free", "capow_is_soa_catalogue",
-    "capow_read_catalogue_soa", "capow_free_host", "capow_survey_nbar",
+    "capow_read_catalogue_soa", "capow_free_host", "capow_survey_nbar", "capow_abi_version",
 ]
+
+ABI_VERSION = 2  # the CAPOW_ABI_VERSION of include/capow.h that this mirror follows
 
 _lib = None
 
@@ -143,6 +145,11 @@ def lib() -> ctypes.CDLL:
         raise ImportError(f"{LIB_PATH} is missing; build it with `python -m capow_gb300.build` "
                           "(the CUDA library is required: there is no CPU path)")
     L = ctypes.CDLL(LIB_PATH)
+    L.capow_abi_version.restype = ctypes.c_int
+    L.capow_abi_version.argtypes = []
+    if L.capow_abi_version() != ABI_VERSION:
+        raise ImportError(f"{LIB_PATH} has ABI version {L.capow_abi_version()}, this module follows {ABI_VERSION}: "
+                          "rebuild it with `python -m capow_gb300.build`")
     vp, ip = ctypes.c_void_p, ctypes.c_int
     P, O = ctypes.POINTER(_Params), ctypes.POINTER(_Options)
     L.capow_create.argtypes = [P, O, ctypes.POINTER(vp)]

@@ -375,6 +375,8 @@ int create_paint_ctx(const capow_params *p, const capow_options *o, int survey, 
   return CAPOW_OK;
 }
 
+extern "C" int capow_abi_version(void) { return CAPOW_ABI_VERSION; }
+
 extern "C" int capow_num_spectra(const capow_ctx *c) { return c ? c->bp.nspec : 0; }
 
 extern "C" int64_t capow_kernel_launches(const capow_ctx *c) { return c ? c->launches : 0; }

@@ -233,6 +233,11 @@ static int run_survey(const capow_params *p, const capow_survey_params *sv, cons
 
 int main(int argc, char **argv) {
   stamp(T_START);
+  if (capow_abi_version() != CAPOW_ABI_VERSION) {
+    printf("libcapow_gpu has ABI version %d, this driver was built for %d\n", capow_abi_version(), CAPOW_ABI_VERSION);
+    fflush(stdout);
+    exit(1);
+  }
   if (argc < 5) { /* src/main.c:39-47 */
     printf("Input parameters not found\n");
     printf("Call with <ParameterFile, DataFile, RandomFile, OutputFile>\n");

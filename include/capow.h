@@ -35,7 +35,11 @@
 extern "C" {
 #endif
 
-#define CAPOW_ABI_VERSION 1
+/* Version of the structs and entry points below. 2: capow_survey_catalogue, capow_survey_stats and
+ * capow_survey_objects carry the velocity fields of Momentum 1-3, and capow_backward takes 5 gradient
+ * arrays per spectrum. A caller compiled against one version checks capow_abi_version() at run time. */
+#define CAPOW_ABI_VERSION 2
+int capow_abi_version(void); /* CAPOW_ABI_VERSION of the loaded library */
 
 /* ---------------------------------------------------------------- status codes */
 #define CAPOW_OK 0
