@@ -162,6 +162,26 @@ def test_deterministic_mode_is_bit_reproducible(gpu):
         assert np.array_equal(a[2][k], b[2][k]), k
 
 
+def test_deterministic_dense_tiles(gpu):
+    """A clump of 60,000 particles inside two cells: its tiles hold far more than the 8192 records of the
+    deterministic kernel's two-limb cells, so they take its uint64 cells at the run's global scale, beside
+    ordinary tiles. The grids against the oracle and bit-reproducible."""
+    po, pc = params_pair(NX=32, NY=32, NZ=32, InterpOrder=3, LOS=3, DoInterlacing=1, Momentum=1, **BASE)
+    x, y, z, vx, vy, vz = particles(po, 20000, seed=9)
+    rng = np.random.default_rng(10)
+    d = np.array([(po.XMAX - po.XMIN) / po.NX, (po.YMAX - po.YMIN) / po.NY, (po.ZMAX - po.ZMIN) / po.NZ])
+    c = np.array([po.XMIN, po.YMIN, po.ZMIN]) + d * np.array([10.3, 17.6, 20.2])
+    clump = c[:, None] + rng.uniform(-1.0, 1.0, size=(3, 60000)) * d[:, None]
+    parts = (np.r_[x, clump[0]], np.r_[y, clump[1]], np.r_[z, clump[2]], np.r_[vx, rng.normal(0, 300, 60000)],
+             np.r_[vy, rng.normal(0, 300, 60000)], np.r_[vz, rng.normal(0, 300, 60000)])
+    ref = oracle_run(po, parts, 1)
+    a = gpu_run(pc, parts, "det", grids=True)
+    b = gpu_run(pc, parts, "det", grids=True)
+    for k in a[2]:
+        assert np.array_equal(a[2][k], b[2][k]), k
+        grid_close(a[2][k], ref["painted"][k], po, "det", f"dense det {k}")
+
+
 def test_out_of_box_los0_is_an_error(gpu):
     po, pc = params_pair(NX=16, NY=16, NZ=16, InterpOrder=2, LOS=0, DoInterlacing=0, Momentum=0, **BASE)
     x, y, z, vx, vy, vz = particles(po, 100, seed=1, edges=False)
