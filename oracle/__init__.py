@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import ctypes
 import dataclasses
+import math
 import os
 import subprocess
 import sys
@@ -462,11 +463,14 @@ def _seqsum(a) -> float:
 
 
 def survey_read(p: Params, path: str, randoms: bool) -> dict:
-    """read_survey_serial_ascii (src/read_data.c:184-361) for Cartesian input (Coord_Type 0) with the number
-    density from its column (NBAR_Column > 0): data lines hold 12 numbers, randoms 8; the weight is the
-    4th, the number density the 5th (the reader copies that column into nbar, :244-250). Objects whose
-    redshift (the distance table's inverse at |x|, :259-266) lies outside [REDMININ, REDMAXIN] are dropped;
-    an object outside the grid less the interpolation margin is the reference's fatal error (:293-299)."""
+    """read_survey_serial_ascii (src/read_data.c:184-361) with the number density from its column
+    (NBAR_Column > 0): data lines hold 12 numbers, randoms 8; the weight is the 4th, the number density the
+    5th (the reader copies that column into nbar, :244-250). Cartesian input (Coord_Type 0) takes the
+    redshift from the distance table's inverse at |x| (:259-266); angular input (Coord_Type 1: RA and Dec in
+    degrees, 2: in radians) reads the redshift as the third number, skips objects of zero weight and places
+    the rest at the table's distance r(z) along the direction (:267-291). Objects whose redshift lies outside
+    [REDMININ, REDMAXIN] are dropped; an object outside the grid less the interpolation margin is the
+    reference's fatal error (:293-299)."""
     L = _survey_lib()
     a = np.loadtxt(path, comments="#", ndmin=2)
     need = 8 if randoms else 12
@@ -482,19 +486,32 @@ def survey_read(p: Params, path: str, randoms: bool) -> dict:
         zhi -= 0.5 * dz
     keep = []
     red = []
+    pos = []
     for i in range(a.shape[0]):
-        tx, ty, tz = a[i, 0], a[i, 1], a[i, 2]
-        tred = L.orc_survey_redshift(p.Omega_m, float(np.sqrt(tx * tx + ty * ty + tz * tz)))
-        if tred < p.REDMININ or tred > p.REDMAXIN:
-            continue
+        tx, ty, tz = float(a[i, 0]), float(a[i, 1]), float(a[i, 2])
+        if p.Coord_Type == 0:
+            tred = L.orc_survey_redshift(p.Omega_m, math.sqrt(tx * tx + ty * ty + tz * tz))
+            if tred < p.REDMININ or tred > p.REDMAXIN:
+                continue
+        else:
+            tred = tz
+            if tred < p.REDMININ or tred > p.REDMAXIN or a[i, 3] == 0.0:
+                continue
+            tdist = L.orc_survey_distance(p.Omega_m, tred)
+            ra, dec = (tx * (math.pi / 180.0), ty * (math.pi / 180.0)) if p.Coord_Type == 1 else (tx, ty)
+            tx = tdist * math.cos(dec) * math.cos(ra)
+            ty = tdist * math.cos(dec) * math.sin(ra)
+            tz = tdist * math.sin(dec)
         if tx < xlo or tx >= xhi or ty < ylo or ty >= yhi or tz < zlo or tz >= zhi:
             raise ValueError(f"object out of grid bounds for chosen InterpOrder: x={tx}, y={ty}, z={tz}")
         keep.append(i)
         red.append(tred)
+        pos.append((tx, ty, tz))
     # the reference keeps each object in float fields (struct survey_data, src/vars.h:136-142)
     k = np.array(keep, dtype=np.int64)
     f32 = np.float32
-    out = {"x": a[k, 0].astype(f32), "y": a[k, 1].astype(f32), "z": a[k, 2].astype(f32),
+    xyz = np.array(pos, dtype=np.float64).reshape(-1, 3)
+    out = {"x": xyz[:, 0].astype(f32), "y": xyz[:, 1].astype(f32), "z": xyz[:, 2].astype(f32),
            "weight": a[k, 3].astype(f32), "redshift": np.array(red).astype(f32), "nread": a.shape[0],
            "redmin": min(red, default=1.0e30), "redmax": max(red, default=-1.0e30)}  # REDMIN/REDMAX, :327-328
     out["nbar"] = a[k, 4].astype(f32) if p.NBAR_Column > 0 else np.zeros(len(k), f32)

@@ -151,8 +151,8 @@ def main():
     print("wrote", len(CASES), "cases")
 
 
-# survey-mode cases (Periodic 0, Survey 1, Momentum 0, Cartesian input, number density from its column,
-# FKP weights): name, params, data objects, random objects, seed
+# survey-mode cases (Periodic 0, Survey 1; Cartesian input unless a case sets Coord_Type; number density from its
+# column unless NBAR_Column < 0; FKP weights): name, params, data objects, random objects, seed
 SURVEY_CASES = [
     ("sv_tsc_il_odd", dict(NX=32, NY=32, NZ=32, XMIN=100.0, XMAX=1100.0, YMIN=-500.0, YMAX=500.0, ZMIN=-500.0,
                            ZMAX=500.0, InterpOrder=3, DoInterlacing=1, NK=12, Maxk=0.09, Odd_Multipoles=1,
@@ -184,7 +184,25 @@ SURVEY_CASES = [
                         ZMAX=200.0, InterpOrder=3, DoInterlacing=0, NK=8, Maxk=0.12, Odd_Multipoles=0,
                         REDMININ=0.0, REDMAXIN=5.0, FKP_Pk=4000.0, FKP_Pk_mom=5.0e9, FKP_Pk_cross=1.0e5,
                         Momentum=3), 1000, 6000, 17),
+    # RA, Dec (degrees) and redshift input (Coord_Type 1): the reader's redshift-to-distance table and angle
+    # conversion (src/read_data.c:267-291), the observer at the origin of the converted coordinates
+    ("sv_radec_tsc_il", dict(NX=24, NY=24, NZ=24, XMIN=300.0, XMAX=900.0, YMIN=-300.0, YMAX=300.0, ZMIN=-300.0,
+                             ZMAX=300.0, InterpOrder=3, DoInterlacing=1, NK=10, Maxk=0.12, Odd_Multipoles=1,
+                             REDMININ=0.0, REDMAXIN=5.0, FKP_Pk=5000.0, Coord_Type=1), 1500, 12000, 18),
 ]
+
+
+def to_radec(p, cat):
+    """Cartesian positions (observer at the origin) as RA and Dec in degrees and redshift, in place of the first
+    three columns: the redshift of each distance from the oracle's redshift-distance table."""
+    L = orc._survey_lib()
+    r = np.linalg.norm(cat[:, :3], axis=1)
+    ra = np.degrees(np.arctan2(cat[:, 1], cat[:, 0])) % 360.0
+    dec = np.degrees(np.arcsin(cat[:, 2] / r))
+    z = np.array([L.orc_survey_redshift(p.Omega_m, float(v)) for v in r])
+    out = cat.copy()
+    out[:, 0], out[:, 1], out[:, 2] = ra, dec, z
+    return out
 
 
 def survey_catalogue(p, n, ncol, rng):
@@ -219,6 +237,8 @@ def main_survey():
                               "NOBJ_Max": max(nd, nr) + 10})
             rng = np.random.default_rng(seed)
             data, rand = survey_catalogue(p, nd, 12, rng), survey_catalogue(p, nr, 8, rng)
+            if p.Coord_Type == 1:
+                data, rand = to_radec(p, data), to_radec(p, rand)
             pf, df, rf, of, dump = (os.path.join(td, f"{name}.{e}") for e in ("dat", "data", "rand", "out", "dump"))
             p.write_file(pf)
             np.savetxt(df, data, fmt="%.17g")

@@ -104,6 +104,39 @@ def test_survey_reader_errors_and_quirks(tmp_path):
         cg.read_survey(str(f), prm2, sv2, False)
 
 
+@pytest.mark.parametrize("coord", [1, 2])
+def test_survey_reader_angular_input(tmp_path, coord):
+    """Coord_Type 1 (RA, Dec in degrees) and 2 (radians), redshift third: positions at the table's distance
+    r(z) along each direction against the oracle's reader, bit for bit in float; objects of zero weight
+    skipped with the reference's printed line; the redshift cut applied to the third number."""
+    p, pf = _params_file(tmp_path, Coord_Type=coord, REDMININ=0.02, REDMAXIN=0.15, NOBJ_Max=10000, XMIN=-1000.0,
+                         XMAX=1000.0, YMIN=-1000.0, YMAX=1000.0, ZMIN=-1000.0, ZMAX=1000.0)
+    prm, sv = _read_params(pf)
+    rng = np.random.default_rng(11 + coord)
+    n = 3000
+    scale = 180.0 / np.pi if coord == 1 else 1.0
+    a = np.zeros((n, 12))
+    a[:, 0] = rng.uniform(0.0, 2.0 * np.pi, n) * scale
+    a[:, 1] = np.arcsin(rng.uniform(-1.0, 1.0, n)) * scale
+    a[:, 2] = rng.uniform(0.0, 0.16, n)  # ~6% above REDMAXIN or below REDMININ
+    a[:, 3] = rng.uniform(0.5, 1.5, n)
+    a[:, 4] = 1e-4
+    a[7, 2], a[7, 3] = 0.05, 0.0  # zero weight inside the redshift range: skipped and printed
+    a[9, 2], a[9, 3] = 0.5, 0.0  # zero weight outside it: dropped by the cut first, silently
+    f = str(tmp_path / "ang.txt")
+    np.savetxt(f, a, fmt="%.17g")
+    got = cg.read_survey(f, prm, sv, False)
+    ref = orc.survey_read(p, f, False)
+    assert got["nread"] == n and got["n"] == len(ref["x"])
+    assert 0 < got["n"] < n - 100
+    for k in ("x", "y", "z", "weight", "redshift"):
+        assert np.array_equal(got["w" if k == "weight" else k], ref[k]), k
+    r = np.sqrt(got["x"].astype(np.float64) ** 2 + got["y"] ** 2 + got["z"] ** 2)
+    d = np.array([orc._survey_lib().orc_survey_distance(p.Omega_m, float(z)) for z in ref["redshift"]])
+    assert np.allclose(r, d, rtol=1e-5)
+    assert got["log"].splitlines() == ["%lf, %lf, %lf, %lf, %lf".replace("%lf", "%f") % tuple(a[7, :5])]
+
+
 def test_survey_reader_redshift_cut_and_progress_lines(tmp_path):
     """The redshift of each object from its distance (the redshift-distance table) against the oracle's
     table, and the 'Read N objects, kept K' line every million lines."""
