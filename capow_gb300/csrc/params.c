@@ -2,7 +2,7 @@
  * and checks (src/read_params.c:30-290 read_parameterfile, :294-428 check_inputs).
  *
  * The tag set and the message texts are kept identical on purpose: the same parameter file
- * must drive both the reference and this build, and scripts that parse the reference's
+ * must drive both the reference and this library, and scripts that parse the reference's
  * stdout keep working. capow_read_params serves the periodic path and refuses a survey run;
  * capow_read_survey_params accepts both and also returns the survey tags. */
 #include <stddef.h>

@@ -1,15 +1,15 @@
 """CPU oracle for the CAPOW periodic power-spectrum path (TEST INFRASTRUCTURE ONLY).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` / ``--impl
-reference`` legs of ``bench.py`` import this package, always as the checker or the
-timed CPU baseline, never as part of the product. The product (``capow_gb300``)
-never imports it.
+reference`` legs of ``bench.py`` import this package, always as the oracle the results are
+compared with or the timed CPU baseline, never as part of the product. The product
+(``capow_gb300``) never imports it.
 
 Two oracles live here:
 
 * ``liborc`` -- ``capow_oracle.c``, a plain-C restatement of the reference's periodic
   path (src/read_data.c:32-179, 514-745; src/main.c:106-148, 211-225, 266-271,
-  302-468, 1019-1056). It builds on any host, including the GPU machine.
+  302-468, 1019-1056). It builds on any host, the GPU machine included.
 * ``oracle/_ref/capow_ref`` -- the UNMODIFIED reference sources compiled against the
   single-rank MPI / FFTW / GSL stand-ins in ``shims/`` (``Makefile.ref``). It can only
   be built where the reference sources are mounted; it pins the restatement and
