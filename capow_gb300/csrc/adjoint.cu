@@ -6,7 +6,8 @@
 // src/main.c:106-148, 211-225, 266-271, 302-468, 1019-1056.
 //
 // Steps, all on the context's stream:
-//  1. repaint the last catalogue and take the full 3-D R2C transform of every slot;
+//  1. the painted grids of the last catalogue (still in the slots when capow_power took the transposed
+//     path, which reads them out of place; repainted otherwise) and their full 3-D R2C transform;
 //  2. per half-space mode k, the gradient with respect to each interlace-combined field (as the pair
 //     dL/dRe, dL/dIm, written as a complex number):
 //       dL/dA' = NM gc sum_l L_l(mu) (2 c_AA,l A' + c_ReAB,l B' - i c_ImAB,l B'),
@@ -130,10 +131,90 @@ __device__ __forceinline__ void adj_gamma(const BinParams &bp, const BinTables &
   }
 }
 
-// Step 2+3 off the self-conjugate planes: Phi = Gamma / 2, in place.
+__device__ __forceinline__ float2 adj_cmulf(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// adj_gamma for FP32 contexts, in FP32 (the FP32 gradients' tolerance) with the forward's exact bin: the
+// FP32 s = fx^2 + (fy^2 + fz^2) of the bin kernels tested against the safe FP32 edges, the exact FP64 s
+// for a mode within a few ulps of an edge. coef_f: the per-bin coefficients in FP32.
+template <int NF>
+__device__ __forceinline__ void adj_gamma32(const BinParams &bp, const BinTables &t, const float *coef_f, int pmask,
+                                            int i, int j, int k, const AdjSlots<float> &sl, const double *dcv,
+                                            float2 *g) {
+  constexpr int NSMAX = 2 * NF;
+#pragma unroll
+  for (int q = 0; q < NSMAX; q++) g[q] = make_float2(0.0f, 0.0f);
+  const int nk = bp.nk;
+  const float s = t.fx2f[i] + (t.fy2f[j] + t.fz2f[k]);
+  int b;
+  if (!bp.lg) {
+    const float v = sqrtf(s) * bp.kscale + bp.koff;
+    b = v < 0.0f ? -1 : (v >= (float)nk ? nk : (int)v);
+  } else {
+    int a = 0, z = nk + 2;  // Elo[a] <= s < Elo[z]
+    while (z - a > 1) {
+      const int mid = (a + z) >> 1;
+      if (t.Elo[mid] <= s) a = mid;
+      else z = mid;
+    }
+    b = a - 1;
+  }
+  while (b < nk && s >= t.Elo[b + 2]) b++;
+  while (b > -1 && s < t.Ehi[b + 1]) b--;
+  if (!(s >= t.Elo[b + 1] && s < t.Ehi[b + 2])) b = exact_bin(t.E, nk, exact_s(t, i, j, k), b);
+  if (b < 0 || b >= nk) return;
+  const long long off = ((long long)i * bp.ny + j) * bp.nzc + k;
+  const bool dc = (i == 0 && j == 0 && k == 0);
+  float2 F[NSMAX];
+  const int ns = bp.interlace ? NSMAX : NF;
+  for (int q = 0; q < ns; q++) F[q] = dc ? make_float2((float)dcv[q], 0.0f) : sl.s[q][off];
+  float2 e = make_float2(1.0f, 0.0f);
+  float2 A = F[0], B = NF == 2 ? F[1] : make_float2(0.0f, 0.0f);
+  float gc = t.cxf[i] * t.cyf[j] * t.czf[k] * (float)adj_nm(i, j, k, bp.xhalf);
+  if (bp.interlace) {
+    e = adj_cmulf(t.exf[i], adj_cmulf(t.eyf[j], t.ezf[k]));
+    const float2 ai = adj_cmulf(F[NF], e);
+    A = make_float2(A.x + ai.x, A.y + ai.y);
+    if (NF == 2) {
+      const float2 bi = adj_cmulf(F[NF + 1], e);
+      B = make_float2(B.x + bi.x, B.y + bi.y);
+    }
+    gc *= 0.25f;
+  }
+  const float fl = bp.los == 1 ? t.fxf[i] : (bp.los == 2 ? t.fyf[j] : t.fzf[k]);
+  const float mu = s > 0.0f ? fl * rsqrtf(s) : 0.0f, mu2 = mu * mu;
+  const float Lv[5] = {1.0f, mu, 1.5f * mu2 - 0.5f, (2.5f * mu2 - 1.5f) * mu, (4.375f * mu2 - 3.75f) * mu2 + 0.375f};
+  float G[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    if (!((pmask >> q) & 1)) continue;
+#pragma unroll
+    for (int l = 0; l < 5; l++) {
+      if ((l & 1) && !bp.odd) continue;
+      G[q] += coef_f[(q * 5 + l) * nk + b] * Lv[l];
+    }
+    G[q] *= gc;
+  }
+  const float2 gA = make_float2(2.0f * G[0] * A.x + G[1] * B.x + G[2] * B.y, 2.0f * G[0] * A.y + G[1] * B.y - G[2] * B.x);
+  g[0] = gA;
+  float2 gB = make_float2(0.0f, 0.0f);
+  if (NF == 2) {
+    gB = make_float2(G[1] * A.x - G[2] * A.y + 2.0f * G[3] * B.x, G[1] * A.y + G[2] * A.x + 2.0f * G[3] * B.y);
+    g[1] = gB;
+  }
+  if (bp.interlace) {  // conj(e) times the combined field's gradient
+    g[NF] = make_float2(e.x * gA.x + e.y * gA.y, e.x * gA.y - e.y * gA.x);
+    if (NF == 2) g[NF + 1] = make_float2(e.x * gB.x + e.y * gB.y, e.x * gB.y - e.y * gB.x);
+  }
+}
+
+// Step 2+3 off the self-conjugate planes: Phi = Gamma / 2, in place (FP32 contexts: adj_gamma32 with the
+// FP32 coefficients coef_f).
 template <typename R, int NF>
-__global__ void __launch_bounds__(256) k_adj_modes(BinParams bp, BinTables t, const double *coef, int pmask,
-                                                   AdjSlots<R> sl, const double *dcv, int kz_lo, int kz_hi) {
+__global__ void __launch_bounds__(256) k_adj_modes(BinParams bp, BinTables t, const double *coef, const float *coef_f,
+                                                   int pmask, AdjSlots<R> sl, const double *dcv, int kz_lo,
+                                                   int kz_hi) {
   const int nkz = kz_hi - kz_lo;
   if (nkz <= 0) return;
   const int ns = bp.interlace ? 2 * NF : NF;
@@ -143,12 +224,18 @@ __global__ void __launch_bounds__(256) k_adj_modes(BinParams bp, BinTables t, co
     const int k = kz_lo + (int)(q % nkz);
     const long long r = q / nkz;
     const int j = (int)(r % bp.ny), i = (int)(r / bp.ny);
-    double2 g[2 * NF];
-    adj_gamma<R, NF>(bp, t, coef, pmask, i, j, k, sl, dcv, g);
     const long long off = ((long long)i * bp.ny + j) * bp.nzc + k;
-    for (int s = 0; s < ns; s++) {
-      sl.s[s][off].x = (R)(0.5 * g[s].x);
-      sl.s[s][off].y = (R)(0.5 * g[s].y);
+    if constexpr (sizeof(R) == 4) {
+      float2 g[2 * NF];
+      adj_gamma32<NF>(bp, t, coef_f, pmask, i, j, k, sl, dcv, g);
+      for (int s = 0; s < ns; s++) sl.s[s][off] = make_float2(0.5f * g[s].x, 0.5f * g[s].y);
+    } else {
+      double2 g[2 * NF];
+      adj_gamma<R, NF>(bp, t, coef, pmask, i, j, k, sl, dcv, g);
+      for (int s = 0; s < ns; s++) {
+        sl.s[s][off].x = (R)(0.5 * g[s].x);
+        sl.s[s][off].y = (R)(0.5 * g[s].y);
+      }
     }
   }
 }
@@ -344,14 +431,81 @@ __device__ __forceinline__ void adj_axis_deriv32(float s, int kind, int n, int l
   }
 }
 
+// The constants of adj_store in FP32, formed once per thread: 1/d per axis and d(shifted LOS coordinate)/dv
+// as the paint's FP32 scales use them, dL/dNGRID, and dL/dc_m / sum w with c_m.
+struct AdjK32 {
+  float idx, idy, idz, rsd, dLdN;
+  float dLdc_w[5], c[5];
+  bool shot_moments;
+};
+
+__device__ __forceinline__ AdjK32 adj_k32(const Geom &g, const AdjScalars &as) {
+  AdjK32 k;
+  k.idx = g.idx_f;
+  k.idy = g.idy_f;
+  k.idz = g.idz_f;
+  k.rsd = g.rsd_f;
+  k.dLdN = (float)as.dLdN;
+  k.shot_moments = false;
+  for (int m = 0; m < 5; m++) {
+    k.dLdc_w[m] = m > 0 && as.dLdc[m] != 0.0 ? (float)(as.dLdc[m] / as.wsum) : 0.0f;
+    k.c[m] = (float)as.c[m];
+    k.shot_moments |= k.dLdc_w[m] != 0.0f;
+  }
+  return k;
+}
+
+// adj_store in FP32 for a particle of the FP32 readout (finite, so read; the gradient sums g0, gs from
+// its FP32 gather).
+template <int NF, typename T>
+__device__ __forceinline__ void adj_store32(const FieldSpec &fs, float v, float w, const float *g0,
+                                            const float (*gs)[3], bool accepted, const AdjK32 &k, int los,
+                                            long long p, T *ox, T *oy, T *oz, T *ov, T *ow) {
+  float dxr = 0.0f, dyr = 0.0f, dzr = 0.0f, dw = 0.0f, dv = 0.0f;
+#pragma unroll
+  for (int f = 0; f < NF; f++) {
+    const int e = f ? fs.eb : fs.ea;
+    float ve = 1.0f, vm = 1.0f;
+    for (int q = 0; q < e; q++) ve *= v;
+    for (int q = 0; q < e - 1; q++) vm *= v;
+    const float val = w * ve;  // the field's deposit value w v^e
+    dxr += val * gs[f][0];
+    dyr += val * gs[f][1];
+    dzr += val * gs[f][2];
+    dw += ve * g0[f];
+    if (e > 0) dv += w * (float)e * vm * g0[f];
+  }
+  dxr *= k.idx;
+  dyr *= k.idy;
+  dzr *= k.idz;
+  if (accepted) dw += k.dLdN;
+  if (k.shot_moments) {  // the shot noise's sum w v^m / sum w over every particle read (src/read_data.c:132-138)
+    float vm = 1.0f;
+    for (int m = 1; m <= 4; m++) {
+      dw += k.dLdc_w[m] * (vm * v - k.c[m]);
+      dv += k.dLdc_w[m] * (float)m * w * vm;
+      vm *= v;
+    }
+  }
+  if (los == 1) dv += k.rsd * dxr;
+  else if (los == 2) dv += k.rsd * dyr;
+  else if (los == 3) dv += k.rsd * dzr;
+  if (ox) ox[p] = (T)dxr;
+  if (oy) oy[p] = (T)dyr;
+  if (oz) oz[p] = (T)dzr;
+  if (ov) ov[p] = (T)dv;
+  if (ow) ow[p] = (T)dw;
+}
+
 // Step 4 for FP32 contexts: particles away from every edge of the reference's rules gather their
-// taps with the FP32 rules of the paint (the same ones that deposited them); the others take the
-// exact FP64 path.
+// taps with the FP32 rules of the paint (the same ones that deposited them) and form their gradient in
+// FP32; the others take the exact FP64 path.
 template <int K, int NF, typename T>
 __global__ void __launch_bounds__(128) k_adj_readout32(Geom g, FieldSpec fs, PIn<T> in, long long n,
                                                        AdjGrids<float> gr, AdjScalars hs, const double *gamma0,
                                                        T *ox, T *oy, T *oz, T *ov, T *ow) {
   const AdjScalars as = adj_scalars(g, hs, gamma0);
+  const AdjK32 k32 = adj_k32(g, as);
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
     const Prep pr = prep32(g, fs, in, p);
     if (!pr.fin || is_edge(g, pr.sx, pr.sy, pr.sz)) {
@@ -399,13 +553,7 @@ __global__ void __launch_bounds__(128) k_adj_readout32(Geom g, FieldSpec fs, PIn
         }
       }
     }
-    double g0d[2] = {0.0, 0.0}, gsd[2][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
-#pragma unroll
-    for (int f = 0; f < NF; f++) {
-      g0d[f] = (double)g0[f];
-      for (int a = 0; a < 3; a++) gsd[f][a] = (double)gs[f][a];
-    }
-    adj_store(g, fs, (double)pr.v, (double)pr.w, g0d, gsd, accepted, true, as, p, ox, oy, oz, ov, ow);
+    adj_store32<NF, T>(fs, pr.v, pr.w, g0, gs, accepted, k32, g.los, p, ox, oy, oz, ov, ow);
   }
 }
 
@@ -436,7 +584,7 @@ static int adj_blocks(long long work) {
 }
 
 template <typename R, int NF>
-static void adj_mode_kernels(capow_ctx *c, const double *coef_d, int pmask, double *gamma0) {
+static void adj_mode_kernels(capow_ctx *c, const double *coef_d, const float *coef_f, int pmask, double *gamma0) {
   const capow_params &p = c->p;
   const size_t eb = sizeof(R);
   AdjSlots<R> sl;
@@ -446,7 +594,7 @@ static void adj_mode_kernels(capow_ctx *c, const double *coef_d, int pmask, doub
   const int kz_hi = nyq > 0 ? nyq : c->bp.nzc;
   const long long interior = (long long)p.NX * p.NY * (kz_hi - 1 > 0 ? kz_hi - 1 : 0);
   const int nbm = adj_blocks(interior), nbp = adj_blocks((long long)p.NX * p.NY);
-  k_adj_modes<R, NF><<<nbm, 256, 0, c->stream>>>(c->bp, c->bt, coef_d, pmask, sl, c->dcv, 1, kz_hi);
+  k_adj_modes<R, NF><<<nbm, 256, 0, c->stream>>>(c->bp, c->bt, coef_d, coef_f, pmask, sl, c->dcv, 1, kz_hi);
   k_adj_plane<R, NF><<<nbp, 256, 0, c->stream>>>(c->bp, c->bt, coef_d, pmask, sl, c->dcv, 0, gamma0);
   if (nyq > 0) k_adj_plane<R, NF><<<nbp, 256, 0, c->stream>>>(c->bp, c->bt, coef_d, pmask, sl, c->dcv, nyq, gamma0);
   c->launches += nyq > 0 ? 3 : 2;
@@ -528,27 +676,34 @@ extern "C" int capow_backward(capow_ctx *c, const double *const *dL_dP, const ca
       }
     }
   }
-  if (!c->adj_coef) CK(c, cudaMalloc(&c->adj_coef, sizeof(double) * NPROD * 5 * nk + 2 * sizeof(double)));
-  double *coef_d = c->adj_coef, *gamma0 = c->adj_coef + NPROD * 5 * nk;
-  CK(c, cudaMemcpyAsync(coef_d, coef.data(), sizeof(double) * NPROD * 5 * nk, cudaMemcpyHostToDevice, c->stream));
+  // device: the coefficients in FP64, Re Gamma(0) of the density's two slots, the coefficients in FP32
+  const size_t ncoef = (size_t)NPROD * 5 * nk;
+  if (!c->adj_coef)
+    CK(c, cudaMalloc(&c->adj_coef, sizeof(double) * (ncoef + 2) + sizeof(float) * ncoef));
+  double *coef_d = c->adj_coef, *gamma0 = c->adj_coef + ncoef;
+  float *coef_f = (float *)(c->adj_coef + ncoef + 2);
+  CK(c, cudaMemcpyAsync(coef_d, coef.data(), sizeof(double) * ncoef, cudaMemcpyHostToDevice, c->stream));
+  const std::vector<float> coef32(coef.begin(), coef.end());
+  CK(c, cudaMemcpyAsync(coef_f, coef32.data(), sizeof(float) * ncoef, cudaMemcpyHostToDevice, c->stream));
   CK(c, cudaMemsetAsync(gamma0, 0, 2 * sizeof(double), c->stream));
   int rc = make_3d_plans(c);
   if (rc) return rc;
-  // ---- forward again: paint, DC values, full 3-D transform
+  // ---- the forward's grids (repainted unless the power stage left them in place), full 3-D transform
   rc = enqueue_backward_paint(c);
   if (rc) return rc;
+  c->grids_intact = false;  // the transform below runs in place
   const bool f64 = c->prec == CAPOW_FP64;
   if (f64) CKFFT(c, cufftExecD2Z(c->adj_fwd, (cufftDoubleReal *)c->grid_base, (cufftDoubleComplex *)c->grid_base));
   else CKFFT(c, cufftExecR2C(c->adj_fwd, (cufftReal *)c->grid_base, (cufftComplex *)c->grid_base));
   // ---- mode gradients and Hermitian completion, then the inverse transform. Re Gamma(0) enters dL/dNGRID
   // only where the density is mean-subtracted (F(0) = sum - NGRID); otherwise gamma0 is cleared after
   if (f64) {
-    if (nf == 2) adj_mode_kernels<double, 2>(c, coef_d, pmask, gamma0);
-    else adj_mode_kernels<double, 1>(c, coef_d, pmask, gamma0);
+    if (nf == 2) adj_mode_kernels<double, 2>(c, coef_d, coef_f, pmask, gamma0);
+    else adj_mode_kernels<double, 1>(c, coef_d, coef_f, pmask, gamma0);
     CKFFT(c, cufftExecZ2D(c->adj_inv, (cufftDoubleComplex *)c->grid_base, (cufftDoubleReal *)c->grid_base));
   } else {
-    if (nf == 2) adj_mode_kernels<float, 2>(c, coef_d, pmask, gamma0);
-    else adj_mode_kernels<float, 1>(c, coef_d, pmask, gamma0);
+    if (nf == 2) adj_mode_kernels<float, 2>(c, coef_d, coef_f, pmask, gamma0);
+    else adj_mode_kernels<float, 1>(c, coef_d, coef_f, pmask, gamma0);
     CKFFT(c, cufftExecC2R(c->adj_inv, (cufftComplex *)c->grid_base, (cufftReal *)c->grid_base));
   }
   if (!c->bp.mean_sub_a) CK(c, cudaMemsetAsync(gamma0, 0, 2 * sizeof(double), c->stream));
@@ -584,5 +739,6 @@ extern "C" int capow_backward(capow_ctx *c, const double *const *dL_dP, const ca
       if (dst[k]) CK(c, cudaMemcpyAsync(dst[k], dev[k], ob * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   c->powered = true;  // the grids hold dL/dgrid now: a new paint is needed before capow_power
+  c->grids_intact = false;
   return CAPOW_OK;
 }

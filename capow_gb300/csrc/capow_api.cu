@@ -531,6 +531,7 @@ int enqueue_paint(capow_ctx *c, const capow_particles &d) {
   }
   CK(c, cudaGetLastError());
   if (!c->quiet) CK(c, cudaEventRecord(c->ev[1], c->stream));
+  c->grids_intact = true;
   return CAPOW_OK;
 }
 
@@ -553,6 +554,8 @@ int prepare_paint_buffers(capow_ctx *c, unsigned long long nmax, bool weights) {
 }
 
 int enqueue_backward_paint(capow_ctx *c) {
+  // the transposed fused power stage reads the slots out of place: the forward's grids and DC values stand
+  if (c->grids_intact) return CAPOW_OK;
   int rc = enqueue_paint(c, c->last);
   if (rc) return rc;
   launch_dc_prepare(c->stream, c->st, c->prec == CAPOW_FP32_DETERMINISTIC, c->nslot, c->fs.nfields,
@@ -665,6 +668,7 @@ int enqueue_power_kernels(capow_ctx *c) {
       CKFFT(c, cufftExecC2C(c->yplan, (cufftComplex *)c->tbuf, (cufftComplex *)c->tbuf, CUFFT_FORWARD));
       for (int k = 0; k < 4; k++) slots[k] = k < c->nslot ? (void *)(c->tbuf + c->tslot * k) : nullptr;
     } else {
+      c->grids_intact = false;
       CKFFT(c, cufftExecR2C(c->plan, (cufftReal *)c->grid_base, (cufftComplex *)c->grid_base));
       GridPtrs gp = grid_ptrs(c);
       for (int k = 0; k < 4; k++) slots[k] = gp.g[k];
@@ -677,6 +681,7 @@ int enqueue_power_kernels(capow_ctx *c) {
     if (!c->quiet) CK(c, cudaEventRecord(c->ev[3], c->stream));
     return CAPOW_OK;
   }
+  c->grids_intact = false;  // the 3-D transform below runs in place
   if (c->grid_elems > 0x7fffffffULL) {
     const size_t eb = f64 ? 8 : 4;
     for (int s = 0; s < c->nslot; s++) {

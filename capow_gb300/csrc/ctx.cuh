@@ -67,6 +67,7 @@ struct capow_ctx {
   size_t stage_bytes[5];
   capow_particles last;   // device view of the last painted catalogue
   bool painted, powered;
+  bool grids_intact;  // the slots still hold the last paint: the power stage read them out of place
   // host pinned readback
   double *h_bins;
   DevStats *h_st;

@@ -181,5 +181,6 @@ extern "C" int capow_paint_noalloc(capow_ctx *c, const capow_particles *parts) {
                  b, c->st, &c->launches);
   CK(c, cudaGetLastError());
   CK(c, cudaEventRecord(c->ev[1], c->stream));
+  c->grids_intact = true;
   return CAPOW_OK;
 }

@@ -172,9 +172,10 @@ int capow_paint(capow_ctx *ctx, const capow_particles *parts);
  * - every input array must be device memory of the context's device (CAPOW_EINVAL otherwise).
  * capow_get_stats, capow_copy_grid and capow_power then work as after capow_paint and allocate
  * nothing (the worst-case bound keeps the record lists from overflowing, so the repaint that
- * capow_power does after an overflow cannot happen). capow_backward is not covered: it repaints the
- * catalogue through capow_paint's buffers, which it allocates on first use, so a caller that cannot
- * allocate must not call it on a context painted this way. capow_tile_kernel_ms returns
+ * capow_power does after an overflow cannot happen). capow_backward is not covered: it creates its 3-D
+ * plans and coefficient buffers on first use and, when capow_power transformed the grids in place,
+ * repaints the catalogue through capow_paint's buffers, so a caller that cannot allocate must not
+ * call it on a context painted this way. capow_tile_kernel_ms returns
  * CAPOW_ESTATE after this paint (its tile launch is not timed). */
 int capow_paint_noalloc(capow_ctx *ctx, const capow_particles *parts);
 
@@ -204,7 +205,8 @@ typedef struct capow_grads {
  * dL/dz, dL/dv_los and dL/dw of every particle of the last capow_paint. The velocity enters through the
  * RSD shift (LOS != 0), the momentum fields' w v^e deposits and the shot noise's sum w v^m / sum w. The
  * reference has no adjoint; this inverts read_data.c:32-179, 514-745 and main.c:106-148, 211-225,
- * 266-271, 302-468, 1019-1056: repaint, full 3-D R2C, per-mode dL/dF of both fields, Hermitian
+ * 266-271, 302-468, 1019-1056: the painted grids (still in place after the transposed power stage,
+ * repainted after one that transformed them in place), full 3-D R2C, per-mode dL/dF of both fields, Hermitian
  * completion, C2R, and the transposed deposits with the weight derivatives. Call after capow_power; it
  * leaves the grids holding dL/dgrid, so paint again before the next capow_power. The output_power rule
  * that zeroes the highest filled bin makes that bin's gradient zero. */

@@ -364,6 +364,34 @@ def test_backward_fp32_matches_fp64_at_c3_size(gpu):
         assert rel <= 2e-3, f"{k}: relative L2 difference {rel:.2e}"
 
 
+@pytest.mark.parametrize("fft_path", ["auto", "one_launch", "3d"])
+def test_backward_after_power_equals_backward_after_repaint(gpu, fft_path):
+    """The transposed power stages (auto, one_launch on a power-of-two grid) read the painted grids out of
+    place, so capow_backward starts from them; the 3-D path transforms them in place and capow_backward
+    repaints. A second capow_backward (its first left dL/dgrid in the slots) always repaints: both calls
+    give the same gradients on every path."""
+    import torch
+
+    from capow_gb300 import synth
+
+    p = cg.Params(NX=64, NY=64, NZ=64, NK=30, Maxk=0.3, **BASE)
+    x, y, z, vx, vy, vz = synth.zeldovich(48, L=1000.0, mesh=64, rms_cells=1.5, seed=5, torch_device=gpu)
+    d = [torch.from_numpy(a).to(gpu) for a in (x, y, z, vz)]
+    with cg.PowerSpectrum(p, precision="fp32", spectra=["dd", "dp", "pp"], fft_path=fft_path) as ps:
+        ps.paint(*d)
+        r = [ps.normalise(s) for s in ps.power()]
+        dl = [{"Pk0": 2 * s["Pk0"], "Pk2": 2 * s["Pk2"]} for s in r]
+        outs = []
+        for _ in range(2):
+            g = {k: torch.empty_like(d[0]) for k in ("dx", "dy", "dz", "dvlos", "dw")}
+            ps.backward(dl, out=g)
+            outs.append({k: v.double().cpu().numpy() for k, v in g.items()})
+    for k in outs[0]:
+        a, b = outs[0][k], outs[1][k]
+        assert np.linalg.norm(b) > 0.0, k
+        assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(b), (fft_path, k)
+
+
 DDPP = (["dd", "dp", "pp"], (0, 1), True, [(0, 0), (2, 1), (3, 2)])
 
 
