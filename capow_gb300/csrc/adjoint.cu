@@ -530,6 +530,7 @@ __global__ void __launch_bounds__(128) k_adj_readout32(Geom g, FieldSpec fs, PIn
       adj_axis_deriv32<K>(sx, 0, g.nx, g.los, dx3);
       adj_axis_deriv32<K>(sy, 1, g.ny, g.los, dy3);
       adj_axis_deriv32<K>(sz, 1, g.nz, g.los, dz3);
+      // per (x, y) tap pair, the z taps' sums S = sum_c G W_z and D = sum_c G dW_z, then the pair's weights
 #pragma unroll
       for (int a = 0; a < K; a++) {
         if (ax.idx[a] < 0) continue;
@@ -537,18 +538,26 @@ __global__ void __launch_bounds__(128) k_adj_readout32(Geom g, FieldSpec fs, PIn
         for (int b = 0; b < K; b++) {
           if (ay.idx[b] < 0) continue;
           const long long rowb = ((long long)ax.idx[a] * g.ny + ay.idx[b]) * g.row;
+          float S[NF], D[NF];
+#pragma unroll
+          for (int f = 0; f < NF; f++) S[f] = D[f] = 0.0f;
 #pragma unroll
           for (int c = 0; c < K; c++) {
             if (az.idx[c] < 0) continue;
-            const float wyz = ay.w[b] * az.w[c];
 #pragma unroll
             for (int f = 0; f < NF; f++) {
               const float G = gr.s[st * NF + f][rowb + az.idx[c]];
-              g0[f] += G * ax.w[a] * wyz;
-              gs[f][0] += G * dx3[a] * wyz;
-              gs[f][1] += G * ax.w[a] * dy3[b] * az.w[c];
-              gs[f][2] += G * ax.w[a] * ay.w[b] * dz3[c];
+              S[f] += G * az.w[c];
+              D[f] += G * dz3[c];
             }
+          }
+          const float wxy = ax.w[a] * ay.w[b], dxy = dx3[a] * ay.w[b], xdy = ax.w[a] * dy3[b];
+#pragma unroll
+          for (int f = 0; f < NF; f++) {
+            g0[f] += wxy * S[f];
+            gs[f][0] += dxy * S[f];
+            gs[f][1] += xdy * S[f];
+            gs[f][2] += wxy * D[f];
           }
         }
       }
