@@ -640,29 +640,9 @@ def gpu_bench(args, world, rank, local):
     e2e_ms = max_over_ranks(world, e2e_ms, dev) / (args.steps * world)
     h2d = sum(int(h.numel() * h.element_size()) for h in host)
     d2h = 3 * 5 * PARAMS["NK"] * 8
-    # ---- adjoint (C3 workload): the same particles, density multipoles on a 256^3 TSC grid; forward
-    # (paint + power) and capow_backward timed separately with CUDA events
-    adj = None
+    # ---- adjoint (C3 workload): the same particles, density multipoles on a 256^3 TSC grid
     try:
-        p3 = cg.Params(**dict(PARAMS, NX=256, NY=256, NZ=256, NK=80, Maxk=0.8))
-        with cg.PowerSpectrum(p3, precision="fp32", device=local, stream=sh) as pa:
-            gbuf = {k: torch.empty_like(d[0]) for k in ("dx", "dy", "dz", "dvlos", "dw")}
-            torch.cuda.synchronize()
-            fw, bw = [], []
-            for it in range(4):
-                e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-                e0.record(ts)
-                pa.paint(*d)
-                r3 = pa.normalise(pa.power()[0])
-                e1.record(ts)
-                pa.backward({"Pk0": 2 * r3["Pk0"], "Pk2": 2 * r3["Pk2"]}, out=gbuf)
-                e2.record(ts)
-                torch.cuda.synchronize()
-                if it:
-                    fw.append(e0.elapsed_time(e1))
-                    bw.append(e1.elapsed_time(e2))
-        adj = {"workload": "same 16,777,216 particles, TSC 256^3, interlaced, LOS=z, loss sum_l (P_l)^2, l=0,2",
-               "forward_ms": round(statistics.median(fw), 3), "backward_ms": round(statistics.median(bw), 3)}
+        adj = adjoint_timing(d, ts, local, steps=3, warmup=1)
     except cg.CapowError as e:  # pragma: no cover
         adj = {"error": str(e)}
     # ---- FP64 GPU path on the same workload (fewer steps: it is the slow baseline)
@@ -709,6 +689,54 @@ def gpu_bench(args, world, rank, local):
     }
 
 
+ADJOINT_WORKLOAD = "same 16,777,216 particles, TSC 256^3, interlaced, LOS=z, loss sum_l (P_l)^2, l=0,2"
+
+
+def adjoint_timing(d, ts, local, steps, warmup):
+    """The adjoint workload (C3): the headline particles d (device tensors x, y, z, v_los) painted on a 256^3
+    TSC grid, density multipoles, loss sum over l = 0, 2 of (P_l)^2. Forward (paint + power) and
+    capow_backward are timed separately with CUDA events on the context's stream ts; medians in ms."""
+    import torch
+
+    import capow_gb300 as cg
+
+    p3 = cg.Params(**dict(PARAMS, NX=256, NY=256, NZ=256, NK=80, Maxk=0.8))
+    with cg.PowerSpectrum(p3, precision="fp32", device=local, stream=ts.cuda_stream) as pa:
+        gbuf = {k: torch.empty_like(d[0]) for k in ("dx", "dy", "dz", "dvlos", "dw")}
+        torch.cuda.synchronize()
+        fw, bw = [], []
+        for it in range(warmup + steps):
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(ts)
+            pa.paint(*d)
+            r3 = pa.normalise(pa.power()[0])
+            e1.record(ts)
+            pa.backward({"Pk0": 2 * r3["Pk0"], "Pk2": 2 * r3["Pk2"]}, out=gbuf)
+            e2.record(ts)
+            torch.cuda.synchronize()
+            if it >= warmup:
+                fw.append(e0.elapsed_time(e1))
+                bw.append(e1.elapsed_time(e2))
+    return {"workload": ADJOINT_WORKLOAD, "forward_ms": round(statistics.median(fw), 3),
+            "backward_ms": round(statistics.median(bw), 3)}
+
+
+def adjoint_bench(args):
+    """The adjoint workload alone, for timing and profiler captures of capow_backward: one JSON line."""
+    import torch
+
+    dev = torch.device("cuda", 0)
+    x, y, z, vx, vy, vz = make_particles()
+    d = [torch.from_numpy(a).to(dev) for a in (x, y, z, vz)]
+    ts = torch.cuda.Stream(device=dev)
+    adj = adjoint_timing(d, ts, 0, args.steps, args.warmup)
+    line = {"metric": "ms per capow_backward (adjoint of paint + power + normalise)", "value": adj["backward_ms"],
+            "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": False,
+            "dtype": "f32", "data": "synthetic (seeded Zel'dovich lattice, float32 positions/velocities)",
+            "config": {"workload": ADJOINT_WORKLOAD}, "forward_ms": adj["forward_ms"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -724,6 +752,7 @@ def main():
     ap.add_argument("--scale", action="store_true", help="run the 1024^3 / 134M-particle workload instead")
     ap.add_argument("--survey", action="store_true", help="run the survey-estimator workload instead")
     ap.add_argument("--cli", action="store_true", help="time the capow driver end to end instead")
+    ap.add_argument("--adjoint", action="store_true", help="time capow_backward on the adjoint workload instead")
     ap.add_argument("--profile-case", action="store_true",
                     help="run the 8x smaller workload for profiler captures (prints stage times only)")
     args = ap.parse_args()
@@ -742,6 +771,9 @@ def main():
         return
     if args.cli:
         cli_bench(args)
+        return
+    if args.adjoint:
+        adjoint_bench(args)
         return
     world, rank, local = dist_init()
     log = (lambda *a: print(*a, file=sys.stderr, flush=True))
