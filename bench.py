@@ -5,12 +5,14 @@ Workload (the headline configuration): 256^3 = 16,777,216 Zel'dovich-displaced l
 density-density, density-momentum and momentum-momentum spectra from one paint, LOS = z (RSD shift),
 NK = 161 linear bins to k = 1.61 h/Mpc.
 
-One step = one full evaluation: paint (4 grids) -> 4 in-place cuFFT R2C -> fused bin kernel ->
-device-to-host copy of the bins. ``value`` times steps with the particles already resident in HBM
-(CUDA events on the context stream, barrier + synchronize on both sides, max over ranks);
-``e2e`` times the same evaluation through the public C-ABI call with pinned HOST particle buffers,
-host-to-device copies inside the timed region. Grids (2.15 GB) and particles (268 MB) exceed L2,
-so no separate flush is needed.
+One step = one full evaluation: paint (4 grids) -> z pass (k_zr2c) and cuFFT y pass -> fused x-axis
+FFT + bin kernel -> device-to-host copy of the bins. ``value`` times steps with the particles already
+resident in HBM (CUDA events on the context stream, barrier + synchronize on both sides, max over
+ranks); ``e2e`` times the same evaluations through the public C-ABI calls with pinned HOST particle
+buffers, each step's host-to-device copy and read-back inside the timed region, as a stream of
+catalogues (capow_power_enqueue / capow_power_result, each copy overlapping the previous evaluation);
+``e2e_sequential`` the same one call after the other. Grids (2.15 GB) and particles (268 MB) exceed
+L2, so no separate flush is needed.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -627,17 +629,35 @@ def gpu_bench(args, world, rank, local):
     ms_per = total_ms / (args.steps * world)
     stage_ms = stage_acc / nsamp
     tile_ms = tile_acc / nsamp
-    # ---- e2e: host buffers through the public API
+    # ---- e2e: host buffers through the public API, every step copying its catalogue from pinned host
+    # memory and reading its sums back. A stream of K evaluations: power_enqueue, the next catalogue's
+    # paint (its copy runs while this power stage does), power_result. e2e_sequential: paint + power
+    # one after the other (each copy waits for the previous evaluation's result).
+    def stream_host(k):
+        hs = [h.numpy() for h in host]
+        ps.paint(*hs)
+        out = None
+        for i in range(k):
+            ps.power_enqueue()
+            if i + 1 < k:
+                ps.paint(*hs)
+            out = ps.power_result()
+        return out
+
+    def timed_host(run):
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        run()
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3
+        return max_over_ranks(world, ms, dev) / (args.steps * world)
+
     for _ in range(2):
         step_host()
-    barrier(world)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        res_h = step_host()
-    torch.cuda.synchronize()
-    e2e_ms = (time.perf_counter() - t0) * 1e3
-    e2e_ms = max_over_ranks(world, e2e_ms, dev) / (args.steps * world)
+    stream_host(2)
+    e2e_seq_ms = timed_host(lambda: [step_host() for _ in range(args.steps)])
+    e2e_ms = timed_host(lambda: stream_host(args.steps))
     h2d = sum(int(h.numel() * h.element_size()) for h in host)
     d2h = 3 * 5 * PARAMS["NK"] * 8
     # ---- adjoint (C3 workload): the same particles, density multipoles on a 256^3 TSC grid
@@ -682,7 +702,8 @@ def gpu_bench(args, world, rank, local):
     B64 = algorithmic_bytes(n, ng, nc, 4, 32, 8, 16)
     pk = peaks()
     return {
-        "ms_per": ms_per, "wall_ms": wall, "stage_ms": stage_ms, "launches": launches, "e2e_ms": e2e_ms, "h2d": h2d,
+        "ms_per": ms_per, "wall_ms": wall, "stage_ms": stage_ms, "launches": launches, "e2e_ms": e2e_ms,
+        "e2e_seq_ms": e2e_seq_ms, "h2d": h2d,
         "d2h": d2h, "fp64_ms": fp64_ms, "acc": acc, "B32": B32, "B64": B64, "peaks": pk, "clocks": clk.summary(),
         "n": n, "parts": parts, "adjoint": adj, "tile_ms": tile_ms, "tile_records": tile_records,
         "res": res, "r64": r64,
@@ -812,7 +833,10 @@ def main():
         "config": config_dict(r["n"]),
         "precision": PRECISION,
         "e2e": {"value": round(r["e2e_ms"], 4), "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
-                "d2h_bytes_per_step": r["d2h"]},
+                "d2h_bytes_per_step": r["d2h"],
+                "mode": "stream of host catalogues: capow_power_enqueue, next capow_paint, capow_power_result"},
+        "e2e_sequential": {"value": round(r["e2e_seq_ms"], 4), "unit": UNIT,
+                           "mode": "capow_paint then capow_power per catalogue"},
         "gpu_launches": int(r["launches"]),
         "stages_ms": {"paint": round(paint_ms, 4), "fft": round(fft_ms, 4), "bin": round(bin_ms, 4)},
         "roofline": None,

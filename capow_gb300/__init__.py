@@ -129,9 +129,10 @@ EXPORTS = [
     "capow_survey_stage_ms", "capow_survey_kernel_launches", "capow_survey_last_error", "capow_survey_destroy",
     "capow_read_survey_params", "capow_read_survey", "capow_survey_objects_free", "capow_is_soa_catalogue",
     "capow_read_catalogue_soa", "capow_free_host", "capow_survey_nbar", "capow_abi_version",
+    "capow_power_enqueue", "capow_power_result",
 ]
 
-ABI_VERSION = 2  # the CAPOW_ABI_VERSION of include/capow.h that this mirror follows
+ABI_VERSION = 3  # the CAPOW_ABI_VERSION of include/capow.h that this mirror follows
 
 _lib = None
 
@@ -161,6 +162,8 @@ def lib() -> ctypes.CDLL:
     L.capow_batch_release.argtypes = []
     L.capow_backward.argtypes = [vp, ctypes.POINTER(ctypes.POINTER(ctypes.c_double)), ctypes.POINTER(_Grads)]
     L.capow_power.argtypes = [vp, ctypes.POINTER(_Spectrum), ip]
+    L.capow_power_enqueue.argtypes = [vp]
+    L.capow_power_result.argtypes = [vp, ctypes.POINTER(_Spectrum), ip]
     L.capow_normalise.argtypes = [P, ctypes.POINTER(_Spectrum)]
     L.capow_num_spectra.argtypes = [vp]
     L.capow_copy_grid.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_double)]
@@ -362,6 +365,7 @@ class PowerSpectrum:
             raise CapowError(rc, f"capow_create: {lib().capow_strerror(rc).decode()}: {err}")
         self.nspec = lib().capow_num_spectra(self._ctx)
         self._keep = []
+        self._keep_prev = []
 
     def _err(self) -> str:
         if not self._ctx:
@@ -384,6 +388,9 @@ class PowerSpectrum:
         for p in parts:
             if p[0] is not None and len(p[3]) != n:
                 raise ValueError("particle arrays differ in length")
+        # a host catalogue's copy may still be running when the next catalogue is painted behind a
+        # pending power stage (power_enqueue): the previous paint's arrays stay referenced until then
+        self._keep_prev = self._keep
         self._keep = [p[3] for p in parts]
         pc = _Particles(n, codes.pop(), devs.pop(), *[p[0] for p in parts])
         self._check(lib().capow_paint(self._ctx, ctypes.byref(pc)), "capow_paint")
@@ -420,6 +427,23 @@ class PowerSpectrum:
 
     def power(self) -> List[dict]:
         """Raw bin sums + shot/norm/alpha for each spectrum (capow_power)."""
+        specs, bufs = self._spectrum_buffers()
+        self._check(lib().capow_power(self._ctx, specs, self.nspec), "capow_power")
+        return self._spectrum_dicts(specs, bufs)
+
+    def power_enqueue(self) -> None:
+        """capow_power_enqueue: queue the power stage of the painted catalogue and return at once. One
+        paint() of the next catalogue may follow (its host copy overlaps this power stage) before
+        power_result()."""
+        self._check(lib().capow_power_enqueue(self._ctx), "capow_power_enqueue")
+
+    def power_result(self) -> List[dict]:
+        """capow_power_result: wait for the queued power stage; the same dicts as power()."""
+        specs, bufs = self._spectrum_buffers()
+        self._check(lib().capow_power_result(self._ctx, specs, self.nspec), "capow_power_result")
+        return self._spectrum_dicts(specs, bufs)
+
+    def _spectrum_buffers(self):
         p = self.params
         n2d = p.NK * p.NMU if p.Output2D else 0
         specs = (_Spectrum * self.nspec)()
@@ -436,7 +460,11 @@ class PowerSpectrum:
             if n2d:
                 specs[q].pk2d = p2.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
                 specs[q].nmodes2d = n2.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
-        self._check(lib().capow_power(self._ctx, specs, self.nspec), "capow_power")
+        return specs, bufs
+
+    def _spectrum_dicts(self, specs, bufs) -> List[dict]:
+        p = self.params
+        n2d = p.NK * p.NMU if p.Output2D else 0
         out = []
         for q in range(self.nspec):
             pk, nm, p2, n2 = bufs[q]

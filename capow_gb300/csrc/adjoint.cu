@@ -642,6 +642,7 @@ static void adj_readout(capow_ctx *c, long long n, const AdjScalars &hs, const d
 
 extern "C" int capow_backward(capow_ctx *c, const double *const *dL_dP, const capow_grads *out) {
   if (!c || !dL_dP || !out) return CAPOW_EINVAL;
+  if (c->pending) FAIL(c, CAPOW_ESTATE, "capow_power_result of the power stage in flight first");
   if (!c->powered) FAIL(c, CAPOW_ESTATE, "capow_backward needs capow_paint and capow_power first");
   if (out->dtype != CAPOW_F32 && out->dtype != CAPOW_F64) FAIL(c, CAPOW_EINVAL, "grads dtype must be F32 or F64");
   CK(c, cudaSetDevice(c->o.device));

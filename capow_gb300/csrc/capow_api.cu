@@ -396,28 +396,29 @@ static int stage_input(capow_ctx *c, const capow_particles *in, capow_particles 
   const bool chunked = c->prec == CAPOW_FP32_MIXED && !c->two_pass && (long long)in->n >= CAPOW_CHUNK_MIN_PARTICLES;
   if (chunked && !c->copy_stream) {
     CK(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-    CK(c, cudaEventCreateWithFlags(&c->copy_start, cudaEventDisableTiming));
     for (int k = 0; k < CAPOW_CHUNKS; k++) CK(c, cudaEventCreateWithFlags(&c->chunk_ev[k], cudaEventDisableTiming));
   }
-  if (chunked) {  // the staging buffers are free once the context stream's earlier work is done
-    CK(c, cudaEventRecord(c->copy_start, c->stream));
-    CK(c, cudaStreamWaitEvent(c->copy_stream, c->copy_start, 0));
-  }
+  // the set this catalogue fills is free once the paint that last read it is done (stage_free; the
+  // context stream's later work, such as a queued power stage, does not hold the copy back)
+  const int set = c->stage_set;
+  if (!c->stage_free[set]) CK(c, cudaEventCreateWithFlags(&c->stage_free[set], cudaEventDisableTiming));
+  if (chunked && c->stage_used[set]) CK(c, cudaStreamWaitEvent(c->copy_stream, c->stage_free[set], 0));
   for (int k = 0; k < 5; k++) {
     if (!src[k]) {
       *dst[k] = nullptr;
       continue;
     }
     size_t bytes = eb * in->n;
-    if (c->stage_bytes[k] < bytes) {
-      if (c->stage[k]) cudaFree(c->stage[k]);
-      c->stage[k] = nullptr;
-      c->stage_bytes[k] = 0;
-      CK(c, cudaMalloc(&c->stage[k], bytes));
-      c->stage_bytes[k] = bytes;
+    if (c->stage_bytes[set][k] < bytes) {
+      if (c->stage_used[set]) CK(c, cudaEventSynchronize(c->stage_free[set]));
+      if (c->stage[set][k]) cudaFree(c->stage[set][k]);
+      c->stage[set][k] = nullptr;
+      c->stage_bytes[set][k] = 0;
+      CK(c, cudaMalloc(&c->stage[set][k], bytes));
+      c->stage_bytes[set][k] = bytes;
     }
-    if (!chunked) CK(c, cudaMemcpyAsync(c->stage[k], src[k], bytes, cudaMemcpyHostToDevice, c->stream));
-    *dst[k] = c->stage[k];
+    if (!chunked) CK(c, cudaMemcpyAsync(c->stage[set][k], src[k], bytes, cudaMemcpyHostToDevice, c->stream));
+    *dst[k] = c->stage[set][k];
   }
   if (chunked) {
     const long long n = (long long)in->n;
@@ -425,14 +426,26 @@ static int stage_input(capow_ctx *c, const capow_particles *in, capow_particles 
       const long long c0 = n * q / CAPOW_CHUNKS, c1 = n * (q + 1) / CAPOW_CHUNKS;
       for (int k = 0; k < 5; k++)
         if (src[k])
-          CK(c, cudaMemcpyAsync((char *)c->stage[k] + eb * c0, (const char *)src[k] + eb * c0, eb * (c1 - c0),
+          CK(c, cudaMemcpyAsync((char *)c->stage[set][k] + eb * c0, (const char *)src[k] + eb * c0, eb * (c1 - c0),
                                 cudaMemcpyHostToDevice, c->copy_stream));
       CK(c, cudaEventRecord(c->chunk_ev[q], c->copy_stream));
     }
     // everything after the bucket pass (and any repaint) also waits for the last chunk
     c->nchunk = CAPOW_CHUNKS;
   }
+  c->stage_set ^= 1;
   dev->on_device = 1;
+  return CAPOW_OK;
+}
+
+// After a paint of catalogue d has been queued: if d lies in a staging set, that set is free again once
+// the context stream passes this point.
+static int mark_stage_read(capow_ctx *c, const capow_particles &d) {
+  for (int s = 0; s < 2; s++)
+    if (d.x && d.x == c->stage[s][0] && c->stage_free[s]) {
+      CK(c, cudaEventRecord(c->stage_free[s], c->stream));
+      c->stage_used[s] = true;
+    }
   return CAPOW_OK;
 }
 
@@ -532,7 +545,7 @@ int enqueue_paint(capow_ctx *c, const capow_particles &d) {
   CK(c, cudaGetLastError());
   if (!c->quiet) CK(c, cudaEventRecord(c->ev[1], c->stream));
   c->grids_intact = true;
-  return CAPOW_OK;
+  return mark_stage_read(c, d);
 }
 
 // Size the FP32 record and edge buffers for catalogues of up to nmax particles (the one-pass buckets at
@@ -571,6 +584,8 @@ extern "C" int capow_paint(capow_ctx *c, const capow_particles *parts) {
   if (!parts->x || !parts->y || !parts->z) FAIL(c, CAPOW_EINVAL, "x, y and z are required");
   if (c->fs.need_v && !parts->vlos) FAIL(c, CAPOW_EINVAL, "vlos is required for LOS != 0 or momentum fields");
   if (parts->n >= 0xFFFFFFF0ULL) FAIL(c, CAPOW_EINVAL, "too many particles for one paint");
+  if (c->pending && c->pend_paint)
+    FAIL(c, CAPOW_ESTATE, "one capow_paint at most between capow_power_enqueue and capow_power_result");
   CK(c, cudaSetDevice(c->o.device));
   capow_particles d;
   int rc = stage_input(c, parts, &d);
@@ -579,6 +594,7 @@ extern "C" int capow_paint(capow_ctx *c, const capow_particles *parts) {
   c->last = d;
   c->painted = true;
   c->powered = false;
+  if (c->pending) c->pend_paint = true;
   return enqueue_paint(c, d);
 }
 
@@ -610,6 +626,7 @@ int settle_paint(capow_ctx *c) {
 
 extern "C" int capow_get_stats(capow_ctx *c, capow_stats *out) {
   if (!c || !out) return CAPOW_EINVAL;
+  if (c->pending) FAIL(c, CAPOW_ESTATE, "capow_power_result of the power stage in flight first");
   if (!c->painted) FAIL(c, CAPOW_ESTATE, "capow_get_stats before capow_paint");
   int rc = CAPOW_OK;
   if (!c->powered) rc = settle_paint(c);
@@ -625,6 +642,7 @@ extern "C" int capow_get_stats(capow_ctx *c, capow_stats *out) {
 
 extern "C" int capow_copy_grid(capow_ctx *c, int which, double *host_out) {
   if (!c || !host_out) return CAPOW_EINVAL;
+  if (c->pending) FAIL(c, CAPOW_ESTATE, "capow_power_result of the power stage in flight first");
   if (!c->painted || c->powered) FAIL(c, CAPOW_ESTATE, "capow_copy_grid is valid between paint and power");
   int slot = which;
   if (c->fs.nfields == 1) {
@@ -719,34 +737,64 @@ static int enqueue_power(capow_ctx *c) {
   return CAPOW_OK;
 }
 
-extern "C" int capow_power(capow_ctx *c, capow_spectrum *out, int nout) {
+extern "C" int capow_power_enqueue(capow_ctx *c) {
   if (!c) return CAPOW_EINVAL;
+  if (c->pending) FAIL(c, CAPOW_ESTATE, "capow_power_result of the power stage in flight first");
   if (!c->painted) FAIL(c, CAPOW_ESTATE, "capow_power before capow_paint");
   if (c->powered) FAIL(c, CAPOW_ESTATE, "grids already transformed; paint again");
-  if (nout < c->bp.nspec || !out) FAIL(c, CAPOW_EINVAL, "need room for %d spectra", c->bp.nspec);
   CK(c, cudaSetDevice(c->o.device));
   int rc = enqueue_power(c);
   if (rc) return rc;
+  if (!c->power_ev) CK(c, cudaEventCreateWithFlags(&c->power_ev, cudaEventDisableTiming));
+  CK(c, cudaEventRecord(c->power_ev, c->stream));
   c->powered = true;
-  CK(c, cudaStreamSynchronize(c->stream));
-  if (c->h_st->overflow) {  // rare: tile lists outgrew the estimate; repaint and redo
-    c->powered = false;
+  c->pending = true;
+  c->pend_paint = false;
+  c->pend_last = c->last;
+  return CAPOW_OK;
+}
+
+extern "C" int capow_power_result(capow_ctx *c, capow_spectrum *out, int nout) {
+  if (!c) return CAPOW_EINVAL;
+  if (!c->pending) FAIL(c, CAPOW_ESTATE, "capow_power_result without capow_power_enqueue");
+  if (nout < c->bp.nspec || !out) FAIL(c, CAPOW_EINVAL, "need room for %d spectra", c->bp.nspec);
+  CK(c, cudaSetDevice(c->o.device));
+  c->pending = false;
+  const bool queued = c->pend_paint;  // a paint of the next catalogue runs behind this power stage
+  c->pend_paint = false;
+  CK(c, cudaEventSynchronize(c->power_ev));
+  if (c->h_st->overflow) {  // rare: tile lists outgrew the estimate; repaint this catalogue and redo
+    int rc = CAPOW_OK;
     if (c->pb.bucket_cap) c->two_pass = true;  // the bucket overflow list filled
-    else rc = ensure_records(c, (unsigned long long)c->h_st->nrecords + 65536, c->last.w != nullptr);
+    else rc = ensure_records(c, (unsigned long long)c->h_st->nrecords + 65536, c->pend_last.w != nullptr);
     if (rc) return rc;
-    rc = enqueue_paint(c, c->last);
+    rc = enqueue_paint(c, c->pend_last);
     if (rc) return rc;
     rc = enqueue_power(c);
     if (rc) return rc;
-    c->powered = true;
     CK(c, cudaStreamSynchronize(c->stream));
     if (c->h_st->overflow) FAIL(c, CAPOW_ENOMEM, "tile record buffer overflow after resize");
+    if (queued) {  // the queued paint ran before this repaint: paint the next catalogue again
+      rc = enqueue_paint(c, c->last);
+      if (rc) return rc;
+    }
   }
   if (c->h_st->nonfinite) FAIL(c, CAPOW_EINVAL, "non-finite particle coordinate, velocity or weight");
   if (c->h_st->fatal) FAIL(c, CAPOW_EBOUNDS, "particle out of grid bounds with LOS == 0");
   if (c->h_st->timeout) FAIL(c, CAPOW_ETIMEOUT, "a bounded wait of the z + y transform gave up");
   fill_spectra(c, c->p, *c->h_st, c->h_bins, c->nmodes.data(), c->nmodes2d.data(), out);
   return CAPOW_OK;
+}
+
+extern "C" int capow_power(capow_ctx *c, capow_spectrum *out, int nout) {
+  if (!c) return CAPOW_EINVAL;
+  if (c->pending) FAIL(c, CAPOW_ESTATE, "capow_power_result of the power stage in flight first");
+  if (!c->painted) FAIL(c, CAPOW_ESTATE, "capow_power before capow_paint");
+  if (c->powered) FAIL(c, CAPOW_ESTATE, "grids already transformed; paint again");
+  if (nout < c->bp.nspec || !out) FAIL(c, CAPOW_EINVAL, "need room for %d spectra", c->bp.nspec);
+  int rc = capow_power_enqueue(c);
+  if (rc) return rc;
+  return capow_power_result(c, out, nout);
 }
 
 // Host side of capow_power for one catalogue: shot noise and normalisation (src/main.c:117-148,
@@ -831,6 +879,7 @@ extern "C" int capow_normalise(const capow_params *p, capow_spectrum *s) {
 
 extern "C" int capow_stage_ms(capow_ctx *c, float *paint_ms, float *fft_ms, float *bin_ms) {
   if (!c) return CAPOW_EINVAL;
+  if (c->pending) FAIL(c, CAPOW_ESTATE, "capow_power_result of the power stage in flight first");
   CK(c, cudaEventSynchronize(c->ev[3]));
   float a = 0, b = 0, d = 0;
   CK(c, cudaEventElapsedTime(&a, c->ev[0], c->ev[1]));
@@ -844,6 +893,7 @@ extern "C" int capow_stage_ms(capow_ctx *c, float *paint_ms, float *fft_ms, floa
 
 extern "C" int capow_tile_kernel_ms(capow_ctx *c, float *ms, int64_t *records) {
   if (!c) return CAPOW_EINVAL;
+  if (c->pending) FAIL(c, CAPOW_ESTATE, "capow_power_result of the power stage in flight first");
   if (c->prec == CAPOW_FP64 || !c->tile_timed)
     FAIL(c, CAPOW_ESTATE, "no timed FP32 tile deposit: paint an FP32 context first");
   CK(c, cudaEventSynchronize(c->ev_tile[1]));
@@ -874,8 +924,12 @@ extern "C" void capow_destroy(capow_ctx *c) {
   for (int k = 0; k < 5; k++)
     if (c->adj_stage[k]) cudaFree(c->adj_stage[k]);
   for (void *p : c->allocs) cudaFree(p);
-  for (int k = 0; k < 5; k++)
-    if (c->stage[k]) cudaFree(c->stage[k]);
+  for (int s = 0; s < 2; s++) {
+    for (int k = 0; k < 5; k++)
+      if (c->stage[s][k]) cudaFree(c->stage[s][k]);
+    if (c->stage_free[s]) cudaEventDestroy(c->stage_free[s]);
+  }
+  if (c->power_ev) cudaEventDestroy(c->power_ev);
   if (c->pb.recs) cudaFree(c->pb.recs);
   if (c->pb.recw) cudaFree(c->pb.recw);
   if (c->pb.edge_list) cudaFree(c->pb.edge_list);
@@ -893,7 +947,6 @@ extern "C" void capow_destroy(capow_ctx *c) {
   if (c->copy_stream) {
     cudaStreamSynchronize(c->copy_stream);
     cudaStreamDestroy(c->copy_stream);
-    cudaEventDestroy(c->copy_start);
     for (int k = 0; k < CAPOW_CHUNKS; k++) cudaEventDestroy(c->chunk_ev[k]);
   }
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);

@@ -62,12 +62,21 @@ struct capow_ctx {
   double *adj_coef;
   void *adj_stage[5];
   size_t adj_stage_bytes[5];
-  // staging for host particle input
-  void *stage[5];
-  size_t stage_bytes[5];
+  // staging for host particle input: two sets, alternating between host-input paints, so that a
+  // catalogue's copy can run while the previous one's power stage still reads its own set
+  void *stage[2][5];
+  size_t stage_bytes[2][5];
+  int stage_set;                 // the set the next host-input paint fills
+  cudaEvent_t stage_free[2];     // recorded on the context stream after the last paint that read each set
+  bool stage_used[2];
   capow_particles last;   // device view of the last painted catalogue
   bool painted, powered;
   bool grids_intact;  // the slots still hold the last paint: the power stage read them out of place
+  // capow_power_enqueue .. capow_power_result: the power stage in flight (its catalogue, for a repaint
+  // after an overflow) and whether one capow_paint has been queued behind it
+  bool pending, pend_paint;
+  capow_particles pend_last;
+  cudaEvent_t power_ev;
   // host pinned readback
   double *h_bins;
   DevStats *h_st;
@@ -77,7 +86,7 @@ struct capow_ctx {
   // host catalogues of FP32 bucket-mode paints are copied in CAPOW_CHUNKS chunks on copy_stream, and
   // the bucket pass of each chunk starts when its copy lands (chunk_ev); nchunk > 1 for that paint
   cudaStream_t copy_stream;
-  cudaEvent_t chunk_ev[4], copy_start;
+  cudaEvent_t chunk_ev[4];
   int nchunk;
   bool tile_timed;         // the last FP32 paint recorded ev_tile
   long long launches;

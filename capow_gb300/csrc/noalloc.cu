@@ -112,6 +112,7 @@ static NoallocLayout noalloc_layout(const TileGeo &tg, unsigned long long n, uns
 extern "C" int capow_paint_noalloc(capow_ctx *c, const capow_particles *parts) {
   if (!c || !parts) return CAPOW_EINVAL;
   if (!c->plan_ok) FAIL(c, CAPOW_ESTATE, "context not fully created");
+  if (c->pending) FAIL(c, CAPOW_ESTATE, "capow_power_result of the power stage in flight first");
   if (c->prec == CAPOW_FP64) FAIL(c, CAPOW_ENOTSUP, "capow_paint_noalloc covers the FP32 precisions only");
   if (parts->dtype != CAPOW_F32 && parts->dtype != CAPOW_F64) FAIL(c, CAPOW_EINVAL, "dtype must be F32 or F64");
   if (!parts->on_device) FAIL(c, CAPOW_EINVAL, "capow_paint_noalloc takes device-resident particles only");

@@ -37,8 +37,9 @@ extern "C" {
 
 /* Version of the structs and entry points below. 2: capow_survey_catalogue, capow_survey_stats and
  * capow_survey_objects carry the velocity fields of Momentum 1-3, and capow_backward takes 5 gradient
- * arrays per spectrum. A caller compiled against one version checks capow_abi_version() at run time. */
-#define CAPOW_ABI_VERSION 2
+ * arrays per spectrum. 3: capow_power_enqueue and capow_power_result. A caller compiled against one
+ * version checks capow_abi_version() at run time. */
+#define CAPOW_ABI_VERSION 3
 int capow_abi_version(void); /* CAPOW_ABI_VERSION of the loaded library */
 
 /* ---------------------------------------------------------------- status codes */
@@ -188,6 +189,17 @@ int capow_get_stats(capow_ctx *ctx, capow_stats *out);
  * (or the single Momentum spectrum). `out` has room for `nout` spectra. Ends with a
  * stream synchronisation and the device-to-host copy of the bins. */
 int capow_power(capow_ctx *ctx, capow_spectrum *out, int nout);
+
+/* capow_power in two halves, for a stream of catalogues through one context: capow_power_enqueue queues
+ * the power stage and the read-back of its sums and returns at once; capow_power_result waits for them
+ * and fills `out` as capow_power does (CAPOW_ESTATE without a pending power stage). Between the two the
+ * context takes one capow_paint of the next catalogue: its kernels run after this power stage, and a
+ * host catalogue's copy into the other of two staging buffers starts at once, so that it overlaps this
+ * power stage. Every other call on the context returns CAPOW_ESTATE until capow_power_result. If this
+ * catalogue's tile lists overflowed, capow_power_result repaints it, redoes the power stage and paints
+ * the queued catalogue again. capow_power is capow_power_enqueue followed by capow_power_result. */
+int capow_power_enqueue(capow_ctx *ctx);
+int capow_power_result(capow_ctx *ctx, capow_spectrum *out, int nout);
 
 /* gradients of a loss with respect to every particle of the last paint (capow_backward) */
 typedef struct capow_grads {
