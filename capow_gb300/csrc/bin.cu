@@ -1066,9 +1066,13 @@ __device__ ZrTables zr2c_load_tables(const BinTables &t, int log2m, unsigned cha
   return z;
 }
 
-// The z pass's loads: a pair of consecutive reals of row y of plane x (z = 2n, 2n + 1), read once.
+// The z pass's loads: a pair of consecutive reals of row y of plane x (z = 2n, 2n + 1), read once. A load
+// functor's row(x, y) gives what is fixed along one row, and its load(p, n) reads pair n at p.
+struct ZrPlainRow {
+  __device__ __forceinline__ float2 load(const float2 *p, int) const { return __ldcs(p); }
+};
 struct ZrPlainLoad {
-  __device__ __forceinline__ float2 operator()(const float2 *p, int, int, int) const { return __ldcs(p); }
+  __device__ __forceinline__ ZrPlainRow row(int, int) const { return ZrPlainRow(); }
 };
 
 // One block of the z pass: ZB rows y0.. of plane x of slot sl, through the shared data area sd
@@ -1088,10 +1092,11 @@ __device__ __forceinline__ void zr2c_block(const ZrGeo &zg, const ZrTables &z, c
   for (int u = threadIdx.x; u < (RS << (log2m - 3)); u += blockDim.x) {
     const int jj = u & (Q1 - 1), r = u >> (log2m - 3), y = y0 + r;
     const float2 *rp = reinterpret_cast<const float2 *>(src + (long long)(y < zg.ny ? y : 0) * zg.row) + jj;
+    const auto rw = ld.row(x, y < zg.ny ? y : 0);  // what the row's loads share (a weighting load's row terms)
     float2 a[8];
     if constexpr (SP == 1) {
 #pragma unroll
-      for (int q = 0; q < 8; q++) a[q] = y < zg.ny ? ld(rp + q * Q1, x, y, jj + q * Q1) : make_float2(0.0f, 0.0f);
+      for (int q = 0; q < 8; q++) a[q] = y < zg.ny ? rw.load(rp + q * Q1, jj + q * Q1) : make_float2(0.0f, 0.0f);
     } else {
       const float2 *rpb = rp + (zg.in_slot >> 1);  // the same row of slot sl + 1 (in_slot floats is even)
       float2 b[8];
@@ -1099,7 +1104,7 @@ __device__ __forceinline__ void zr2c_block(const ZrGeo &zg, const ZrTables &z, c
       for (int q = 0; q < 8; q++) {
         a[q] = b[q] = make_float2(0.0f, 0.0f);
         if (y < zg.ny) {
-          const float2 w = ld.weights(x, y, jj + q * Q1), va = __ldcs(rp + q * Q1), vb = __ldcs(rpb + q * Q1);
+          const float2 w = rw.weights(jj + q * Q1), va = __ldcs(rp + q * Q1), vb = __ldcs(rpb + q * Q1);
           a[q] = make_float2(va.x * w.x, va.y * w.y);
           b[q] = make_float2(vb.x * w.x, vb.y * w.y);
         }
@@ -1205,20 +1210,29 @@ struct ZrWeight {
   int l, m;
 };
 
+// One row (plane x, row y) of a set: its harmonic's polynomial in pz (HarmRow, formed once per row), so
+// that a cell's weight is a Horner step per degree, one rsqrt and L - 1 products.
+template <int L>
+struct ZrWeightRow {
+  HarmRow<L> h;
+  const float *vz;
+  // the weights of cells z = 2n and 2n + 1
+  __device__ __forceinline__ float2 weights(int n) const {
+    const float2 pz = __ldg(reinterpret_cast<const float2 *>(vz) + n);
+    return make_float2(h.at(pz.x), h.at(pz.y));
+  }
+  __device__ __forceinline__ float2 load(const float2 *p, int n) const {
+    const float2 v = __ldcs(p), c = weights(n);
+    return make_float2(v.x * c.x, v.y * c.y);
+  }
+};
+
 // The degree L is a compile-time constant, so the polynomial of each m is specialised.
 template <int L>
 struct ZrWeightLoad {
   ZrWeight w;
-  // the weights of cells z = 2n and 2n + 1 of row y of plane x
-  __device__ __forceinline__ float2 weights(int x, int y, int n) const {
-    const float px = __ldg(w.vx + x), py = __ldg(w.vy + y), pxy = px * px + py * py;
-    const float2 pz = __ldg(reinterpret_cast<const float2 *>(w.vz) + n);
-    return make_float2(sv_cell_weight<float>(L, w.m, px, py, pxy, pz.x),
-                       sv_cell_weight<float>(L, w.m, px, py, pxy, pz.y));
-  }
-  __device__ __forceinline__ float2 operator()(const float2 *p, int x, int y, int n) const {
-    const float2 v = __ldcs(p), c = weights(x, y, n);
-    return make_float2(v.x * c.x, v.y * c.y);
+  __device__ __forceinline__ ZrWeightRow<L> row(int x, int y) const {
+    return ZrWeightRow<L>{HarmRow<L>(w.m, __ldg(w.vx + x), __ldg(w.vy + y)), w.vz};
   }
 };
 
