@@ -281,7 +281,10 @@ __global__ void __launch_bounds__(256) k_sv_combine(Geom g, SvIn<T> in, const T 
       l_ngrid += __ddiv_rn(acc ? w : 0.0, (double)sv_mul(in.pv[i], wk[i]));
     } else {
       wp = __dmul_rn(pref, w);
-      l_ngrid += __ddiv_rn(acc ? wp : 0.0, w);
+      // the counter's term (pref w) / w is pref to the last ulp (the sum agrees to ~1e-16); only w == 0
+      // takes the quotient, whose 0 / 0 is the reference's NaN (and a rejected object's 0 / 0 too)
+      if (w != 0.0) l_ngrid += acc ? pref : 0.0;
+      else l_ngrid += __ddiv_rn(acc ? wp : 0.0, w);
     }
     cx[off + i] = (float)x;
     cy[off + i] = (float)y;
