@@ -27,18 +27,18 @@ def catalogue(seed, n=4_500_000, clump=0.0):
     return [x, y, z, v]
 
 
-def one_by_one(p, cats):
+def one_by_one(p, cats, precision="fp32"):
     out = []
     for c in cats:
-        with cg.PowerSpectrum(p, precision="fp32", spectra=SPECTRA) as ps:
+        with cg.PowerSpectrum(p, precision=precision, spectra=SPECTRA) as ps:
             ps.paint(*c)
             out.append(ps.power())
     return out
 
 
-def pipelined(p, cats):
+def pipelined(p, cats, precision="fp32"):
     out = []
-    with cg.PowerSpectrum(p, precision="fp32", spectra=SPECTRA) as ps:
+    with cg.PowerSpectrum(p, precision=precision, spectra=SPECTRA) as ps:
         ps.paint(*cats[0])
         for i in range(len(cats)):
             ps.power_enqueue()
@@ -66,6 +66,14 @@ def assert_same(got, ref, label, scalar_tol=1e-12):
 def test_pipelined_catalogues_match_one_context_each(gpu):
     cats = [catalogue(s) for s in (11, 12, 13)]
     assert_same(pipelined(cg.Params(**P), cats), one_by_one(cg.Params(**P), cats), "pipelined")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "det"])
+def test_pipelined_other_precisions(gpu, precision):
+    """FP64 and the deterministic mode, with catalogues small enough to be copied on the context's stream
+    (no chunks): the staging sets alternate all the same."""
+    cats = [catalogue(s, n=300_000) for s in (41, 42, 43)]
+    assert_same(pipelined(cg.Params(**P), cats, precision), one_by_one(cg.Params(**P), cats, precision), precision)
 
 
 def test_pipelined_state_rules(gpu):
