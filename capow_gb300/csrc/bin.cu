@@ -1753,7 +1753,9 @@ bool xbin_plan(const BinParams &bp, int nslot, XbinGeo &xg, bool transposed) {
   xg.nkb = (xg.n_inner + xg.kc - 1) / xg.kc;
   xg.nblocks = xg.n_outer * xg.nkb;
   const int np = bp.nfields == 1 ? 1 : 4, nl = bp.odd ? 5 : 3;
-  for (xg.nbc = 4; xg.nbc > 1; xg.nbc >>= 1)  // up to 4 bin copies as fit (8 measured slower: less L1)
+  // up to 2 bin copies as fit: at 512^3 the bin stage took 1.50 ms with 2, 1.58 with 1 and 1.61 with 4
+  // (more copies leave less L1; 8 were slower still)
+  for (xg.nbc = 2; xg.nbc > 1; xg.nbc >>= 1)
     if (xbin_smem_layout(xg.log2n, xg.ncol, np, nl, bp.nk, xg.nbc).total <= 220 * 1024) break;
   return xbin_smem_layout(xg.log2n, xg.ncol, np, nl, bp.nk, xg.nbc).total <= 220 * 1024;
 }
