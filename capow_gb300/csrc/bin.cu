@@ -967,9 +967,10 @@ __global__ void __launch_bounds__(XBIN_THREADS) k_xfft_bin(BinParams bp, BinTabl
             for (int l2 = 0; l2 < NL; l2++) atomicAdd(&sbw[(qq * NL + l2) * nk + cur], acc[qq][l2]);
       }
     }
-    // every 4 blocks, the FP32 block bins (a few hundred modes per bin at most) are added into the
+    // every 8 blocks, the FP32 block bins (a few hundred modes per bin at most) are added into the
     // CTA's FP64 bins and cleared; the next block's first barrier orders the clearing before its flushes
-    if ((++nproc & 3) == 0) {
+    // (at 512^3: every 8 blocks 1.494 ms, every 4 1.508, every 2 1.535)
+    if ((++nproc & 7) == 0) {
       __syncthreads();
       for (int c = threadIdx.x; c < nbins; c += blockDim.x) {
         float v = 0.0f;
